@@ -1,0 +1,308 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 RAM kinetic step.
+
+Workload (default): the four-species step on the standard RAM grid
+(e-, H+, He+, O+; NR=20 x NT=25 x NE=35 x NPA=72 = 1,260,000 cells per
+species; dipole field, Volland-Stern potential with Kp rising 1->6 over
+4320 DTs steps, DTs = 5 s).  One bench step is one ram_run call: the Strang
+pair R,P,E,MU,CEX,ATMOL | ATMOL,CEX,MU,E,P,R for every species, the periodic
+copy, the magnetopause mask, DtsNext and the ANISCH moments -- two DTs
+steps, i.e. 2 x 4 x 1.26e6 = 10.08e6 cell-updates.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line (rank 0).  Under torchrun every rank advances its own
+replica of the workload on its own GPU (the path has no exchange step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "ram-scb_gb300"))
+
+METRIC = "FP64 cell-updates/s"
+UNIT = "cell-updates/s"
+# FP64 add/mul/fma per face of each sweep kernel (csrc/sweeps.cu), counted from
+# the source: coefficient, a-term, X, beta|X|, face fma, flux, two update ops;
+# DRIFTE's coefficient is two ops; the CFL-tracking forward E/MU add one.
+FP64_OPS_PER_FACE = {"driftr": 8, "driftp": 8, "drifte": 9.5, "driftmu": 8.5}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="four_sp", choices=["four_sp", "single_h", "refined"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_desc(wl):
+    g = wl.grid
+    return (f"{wl.name}: {len(g.species)} species ({','.join(wl.meta['species'])}) "
+            f"{g.nr}x{g.nt}x{g.ne}x{g.npa}, Kp ramp 1->6 (VOLS), DTs={wl.dts}s")
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ CPU legs
+def cpu_time_oracle(wl, seconds, nthreads):
+    """Time the CPU oracle (the reference's routines restated in C, species
+    loop under OpenMP like the reference) on this workload; returns
+    (cell-updates/s, steps, elapsed)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import numpy as np
+    import pyoracle
+
+    o = pyoracle.Oracle(wl.grid, wl.fields)
+    f2 = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    cells = 2 * wl.grid.ncell * len(wl.grid.species)
+    o.ram_run(f2, wl.fgeos, wl.dts, kp=wl.kp(0), nthreads=nthreads)  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.ram_run(f2, wl.fgeos, wl.dts, kp=wl.kp(2 * n), nthreads=nthreads)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 1000:
+            break
+    return cells * n / el, n, el
+
+
+def run_reference(args, rank, world):
+    from ramgpu import workload as W
+
+    if rank != 0:
+        return
+    wl = W.make_workload(args.workload)
+    ns = len(wl.grid.species)
+    threads = min(ns, os.cpu_count() or 1)
+    budget = max(5.0, min(60.0, 0.4 * max(args.steps, 1)))
+    v, n, el = cpu_time_oracle(wl, budget, threads)
+    sample = (f"{n} ram_run calls of the workload ({workload_desc(wl)}), {el:.1f} s; "
+              f"C restatement of the reference routines (no Fortran compiler), OpenMP over species")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": n, "warmup": 1, "ms_per_step": 1e3 * el / n, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload_desc(wl), "step": "one ram_run call (2 DTs steps)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------ GPU leg
+def run_gb300(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    from ramgpu import abi, workload as W
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    wl = W.make_workload(args.workload)
+    g = wl.grid
+    ns = len(g.species)
+    gpu = abi.RamGpu(g, wl.fields)
+    stream = torch.cuda.Stream(device=dev)
+    gpu.set_stream(stream.cuda_stream)
+    for s in range(ns):
+        gpu.upload_f2(0, s, wl.f2[s])
+        gpu.set_boundary(0, s, wl.fgeos[s])
+    cells_per_step = 2 * g.ncell * ns
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    def kp_at(step):
+        return wl.kp(2 * step)
+
+    # warm-up (also builds the DTs tables)
+    for w in range(args.warmup):
+        gpu.set_kp(-1, kp_at(w))
+        gpu.ram_run(wl.dts)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(0.3)
+    gpu.set_timing(True)
+    gpu.kernel_times()
+    launches0 = gpu.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize(dev)
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+        gpu.set_kp(-1, kp_at(args.warmup + k))
+        ev[k][0].record(stream)
+        gpu.ram_run_async(wl.dts)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - wall0
+    launches = gpu.launch_count() - launches0
+    ktimes = gpu.kernel_times()
+    gpu.set_timing(False)
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * cells_per_step * args.steps / (total_ms / 1e3)
+
+    # dominant kernel and its roofline (per launch, from the events above)
+    hbm_peak, peak_kind = measured_peaks()
+    sweep = {k: v for k, v in ktimes.items() if k.startswith("drift")}
+    dom = max(sweep, key=lambda k: sweep[k][0])
+    dom_ms = sweep[dom][0] / sweep[dom][1]
+    nitems = ns
+    bytes_per_launch = 16.0 * g.ncell * nitems  # F2 read + write once per sweep
+    achieved = bytes_per_launch / (dom_ms / 1e3) / 1e9
+    nfaces = g.ncell * nitems
+    fp64 = FP64_OPS_PER_FACE[dom] * nfaces / (dom_ms / 1e3) / 1e9
+
+    # end-to-end through the C ABI with host buffers (pinned), full F2 in and out
+    e2e_steps = max(3, min(10, args.steps))
+    pin = [torch.empty(g.ncell, dtype=torch.float64, pin_memory=True) for _ in range(ns)]
+    host = [np.reshape(p.numpy(), (g.nr, g.nt, g.ne, g.npa), order="F") for p in pin]
+    for s in range(ns):
+        host[s][...] = gpu.download_f2(0, s)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        for s in range(ns):
+            gpu.upload_f2(0, s, host[s])
+        gpu.set_kp(-1, kp_at(k))
+        gpu.ram_run(wl.dts)
+        for s in range(ns):
+            gpu.lib.ramgpu_download_f2(gpu.h, 0, s, host[s].ctypes.data_as(abi._P))
+        pe, pa = gpu.moments(0, 0)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": world * cells_per_step * e2e_steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": 8 * g.ncell * ns + 8,
+           "d2h_bytes_per_step": 8 * g.ncell * ns + 16 * g.nr * g.nt,
+           "path": "ramgpu_upload_f2 (pinned host) + ramgpu_set_kp + ramgpu_ram_run + "
+                   "ramgpu_download_f2 + ramgpu_moments, every step"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, n, el = cpu_time_oracle(wl, args.cpu_seconds, min(ns, os.cpu_count() or 1))
+        cpu = {"value": v, "unit": UNIT, "cores": min(ns, os.cpu_count() or 1), "kind": "port",
+               "sample": f"{n} ram_run calls of the same workload in {el:.1f} s (C restatement of the "
+                         f"reference routines, OpenMP over species as the reference)"}
+    gpu.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_desc(wl), "step": "one ram_run call = 2 DTs steps",
+                   "cells_per_step": cells_per_step, "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None, "kernel": dom,
+                     "kernel_ms": dom_ms, "peak_kind": peak_kind,
+                     "fp64_gflops": fp64, "fp64_ops_per_face": FP64_OPS_PER_FACE[dom]},
+        "kernels_ms": {k: round(v[0] / v[1], 5) for k, v in ktimes.items()},
+        "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+        "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_gb300(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,197 @@
+/*
+ * ramgpu.h -- C ABI of the GB300 (sm_103a) implementation of RAM's
+ * bounce-averaged kinetic step.
+ *
+ * The entry points replace the body of the species loop of the reference's
+ * `ram_run` and its tail (src/ModRamRun.f90:64-222), which `run_ramscb`
+ * calls once per iteration (src/ModRamScbRun.f90:85).  The reference has no
+ * plugin interface: its path is a set of species-indexed Fortran
+ * subroutines sharing module globals.  This header turns that state into a
+ * context object that owns every device buffer; the distribution function
+ * F2 stays resident on the GPU across calls.
+ *
+ * Conventions
+ *  - Every function returns int: RAMGPU_OK (0) or a negative RAMGPU_ERR_*.
+ *    ramgpu_last_error() gives the message.  The library never exits or
+ *    aborts the caller.
+ *  - Host arrays are borrowed for the duration of a call only and use the
+ *    reference's Fortran column-major layout and dimensions, so a Fortran
+ *    caller passes its module arrays as they are (iso_c_binding).
+ *  - Species index s is 0-based here (Fortran S-1); member m is 0-based.
+ *  - All arithmetic is IEEE binary64.  Calls are synchronous on the
+ *    context's stream unless stated otherwise.
+ *  - One context per host thread.
+ */
+#ifndef RAMGPU_H
+#define RAMGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RAMGPU_OK 0
+#define RAMGPU_ERR_ARG (-1)      /* bad argument, size or ordering */
+#define RAMGPU_ERR_CUDA (-2)     /* CUDA runtime error */
+#define RAMGPU_ERR_STATE (-3)    /* call made before its inputs were set */
+#define RAMGPU_ERR_NUMERIC (-4)  /* non-finite value detected */
+#define RAMGPU_ERR_NOMEM (-5)    /* device allocation failed */
+
+/* Charge-exchange cross-section branch of CEPARA (src/ModRamLoss.f90:38-87). */
+#define RAMGPU_CEX_NONE 0      /* "Electron" (CEX_file 'na'): no loss */
+#define RAMGPU_CEX_HYDROGEN 1  /* "Hydrogen"  src/ModRamLoss.f90:39-53 */
+#define RAMGPU_CEX_HELIUM1 2   /* "HeliumP1"  src/ModRamLoss.f90:54-68 */
+#define RAMGPU_CEX_OXYGEN1 3   /* "OxygenP1"  src/ModRamLoss.f90:69-83 */
+
+/* Flags of ramgpu_config.flags */
+#define RAMGPU_FLAG_CLOSED 1u    /* closed outer faces in R, E, MU: conserves sum F2*WE*WMU
+                                    (new mode; the reference has no such switch) */
+#define RAMGPU_FLAG_NO_ATMOL 2u  /* skip ATMOL (the reference calls it every step,
+                                    src/ModRamRun.f90:122,127) */
+#define RAMGPU_FLAG_LOSSES 4u    /* SUMRC bookkeeping LSDR/LSCHA/LSATM each ram_run
+                                    (src/ModRamRun.f90:77-175,231-259) */
+
+typedef struct ramgpu_ctx ramgpu_ctx;
+
+/* Grid sizes and scheme parameters.  Mirrors #RAMGRID / #RAMLIMITER
+ * (src/IM_set_parameters.f90:152-161) and ModRamGrids (src/ModRamGrids.f90:15-19). */
+typedef struct {
+    int nr, nt, ne, npa;   /* NR, NT, NE, NPA */
+    int ns;                /* species kinds (the reference's NS) */
+    int n_members;         /* ensemble members; 1 reproduces the reference */
+    double betalim;        /* BetaLim, clamped to [1,2] as IM_set_parameters does */
+    double fraccfl;        /* FracCFL (0.8 in the reference) */
+    double dtsmin;         /* DTsMin (0.1 s in the reference) */
+    unsigned flags;        /* RAMGPU_FLAG_* */
+} ramgpu_config;
+
+/* Grid and factor tables produced by ARRAYS (src/ModRamInit.f90:364-587).
+ * Shapes are the reference's, Fortran order; per-species arrays carry the
+ * leading NS index like the reference: GREL(NS,NE), FFACTOR(NS,NR,NE,NPA). */
+typedef struct {
+    const double *lz, *rlz;          /* (NR+1) */
+    const double *phi;               /* (NT) */
+    double dl1, mdr, dphi, conf1, conf2;
+    const double *ekev, *ebnd, *we, *de;   /* (NE) */
+    const double *mu, *dmu, *wmu;          /* (NPA) */
+    const double *upa;               /* (NR), real as in the reference */
+    const double *rmas;              /* (NS) */
+    const double *grel, *grbnd, *v;  /* (NS,NE) */
+    const double *epp, *ernh;        /* (NS,NE) */
+    const double *ffactor;           /* (NS,NR,NE,NPA) */
+} ramgpu_grid;
+
+/* ---- lifetime ------------------------------------------------------------ */
+
+/* Replaces ram_allocate's RAM arrays (src/ModRamInit.f90:68-120). */
+int ramgpu_create(const ramgpu_config *cfg, ramgpu_ctx **out);
+int ramgpu_destroy(ramgpu_ctx *ctx);
+/* Copies the last error message of ctx (or of the last failed create when
+ * ctx is NULL) into buf. */
+int ramgpu_last_error(const ramgpu_ctx *ctx, char *buf, size_t len);
+/* Use this CUDA stream (cudaStream_t) for all work; NULL = the context's own. */
+int ramgpu_set_stream(ramgpu_ctx *ctx, void *stream);
+
+/* ---- inputs -------------------------------------------------------------- */
+
+/* species(S)%s_charge and the CEPARA branch (src/ModRamSpecies.f90:37-138). */
+int ramgpu_set_species(ramgpu_ctx *ctx, int s, int charge, int cex_kind);
+/* ARRAYS output (src/ModRamInit.f90:364-587). */
+int ramgpu_set_grid(ramgpu_ctx *ctx, const ramgpu_grid *grid);
+/* computehI / dipole field tables (src/ModRamScb.f90:567-619):
+ * FNHS, FNIS, BOUNHS, BOUNIS, HDNS, dIdt, dIbndt : (NR+1,NT,NPA)
+ * BNES, dBdt, EIR, EIP : (NR+1,NT);  outsideMGNP : int (NR,NT) */
+int ramgpu_set_fields(ramgpu_ctx *ctx, const double *fnhs, const double *fnis,
+                      const double *bounhs, const double *bounis, const double *hdns,
+                      const double *didt, const double *dibndt, const double *bnes,
+                      const double *dbdt, const double *eir, const double *eip,
+                      const int *outside_mgnp);
+/* GEOSB output FGEOS(S,:,:,:) of one species (src/ModRamBoundary.f90:241-319):
+ * (NT,NE,NPA).  member < 0 sets it for every member. */
+int ramgpu_set_boundary(ramgpu_ctx *ctx, int member, int s, const double *fgeos_s);
+/* Potential VT(NR+1,NT) for a member (the non-VOLS branch, src/ModRamRun.f90:49). */
+int ramgpu_set_potential(ramgpu_ctx *ctx, int member, const double *vt);
+/* Kp for the Volland-Stern potential computed on the device
+ * (src/ModRamRun.f90:45-54).  member < 0 sets every member. */
+int ramgpu_set_kp(ramgpu_ctx *ctx, int member, double kp);
+/* Species a member advances (default: all ns).  list holds 0-based species. */
+int ramgpu_set_member_species(ramgpu_ctx *ctx, int member, int n, const int *list);
+/* Retire (0) or re-activate (1) a member; retired members are not advanced. */
+int ramgpu_set_member_active(ramgpu_ctx *ctx, int member, int active);
+
+/* ---- state --------------------------------------------------------------- */
+
+/* F2(S,:,:,:,:) of one species as a contiguous (NR,NT,NE,NPA) array. */
+int ramgpu_upload_f2(ramgpu_ctx *ctx, int member, int s, const double *f2_s);
+int ramgpu_download_f2(ramgpu_ctx *ctx, int member, int s, double *f2_s);
+/* The whole reference array F2(NS,NR,NT,NE,NPA) of one member. */
+int ramgpu_upload_f2_all(ramgpu_ctx *ctx, int member, const double *f2);
+int ramgpu_download_f2_all(ramgpu_ctx *ctx, int member, double *f2);
+/* Device pointer to F2 of (member, s), (NR,NT,NE,NPA) contiguous; for
+ * zero-copy interop.  Valid until ramgpu_destroy. */
+int ramgpu_f2_device_ptr(ramgpu_ctx *ctx, int member, int s, double **dptr);
+
+/* ---- the step ------------------------------------------------------------ */
+
+/* One ram_run call (src/ModRamRun.f90:16-225, without the optional
+ * Coulomb/WPI/EMIC/FLC processes): for every active member and species the
+ * Strang pair R,P,E,MU,[CEX],ATMOL | ATMOL,[CEX],MU,E,P,R of length dts each,
+ * then F2(:,:,NT,:,:)=F2(:,:,1,:,:), the magnetopause mask, DtsNext, and
+ * the ANISCH moments (with their F2(:,:,:,:,1) side effect). */
+int ramgpu_ram_run(ramgpu_ctx *ctx, double dts);
+/* One DTs half of ram_run without the tail: order 0 = R,P,E,MU,[CEX],ATMOL;
+ * order 1 = ATMOL,[CEX],MU,E,P,R. */
+int ramgpu_half_step(ramgpu_ctx *ctx, double dts, int order);
+/* Same as ramgpu_ram_run but enqueued only (no synchronisation, no host
+ * reads), for CUDA-graph capture and overlap.  Inputs set by the calls
+ * above are read at execution time. */
+int ramgpu_ram_run_async(ramgpu_ctx *ctx, double dts);
+
+/* Diagnostic: one operator of the step on every active item, as the
+ * reference routine of the same name (the coefficient tables for dts are
+ * rebuilt first).  op: 0 DRIFTR, 1 DRIFTP, 2 DRIFTE, 3 DRIFTMU,
+ * 4 CHAREXCHANGE (src/ModRamLoss.f90:457), 5 ATMOL (src/ModRamLoss.f90:485),
+ * 6 ANISCH moments.  cfl != 0 also records the DtDrift* of that sweep. */
+#define RAMGPU_OP_DRIFTR 0
+#define RAMGPU_OP_DRIFTP 1
+#define RAMGPU_OP_DRIFTE 2
+#define RAMGPU_OP_DRIFTMU 3
+#define RAMGPU_OP_CHAREXCHANGE 4
+#define RAMGPU_OP_ATMOL 5
+#define RAMGPU_OP_ANISCH 6
+int ramgpu_apply_op(ramgpu_ctx *ctx, double dts, int op, int cfl);
+
+/* ---- outputs ------------------------------------------------------------- */
+
+/* PPERT(S,:,:), PPART(S,:,:) of the last ram_run: (NR,NT) each. */
+int ramgpu_moments(ramgpu_ctx *ctx, int member, int s, double *ppert, double *ppart);
+/* FLUX(S,:,:,:,:) = F2/FFACTOR/FNHS of the current state (src/ModRamRun.f90:208-222):
+ * (NR,NT,NE,NPA); entries the reference leaves unset are 0. */
+int ramgpu_flux(ramgpu_ctx *ctx, int member, int s, double *flux_s);
+/* DtDriftR/P/E/Mu of the last ram_run for (member,s), and DtsNext over all
+ * species of the member (src/ModRamRun.f90:204-205).  out: 5 doubles. */
+int ramgpu_cfl(ramgpu_ctx *ctx, int member, int s, double *out5);
+/* SUMRC bookkeeping (needs RAMGPU_FLAG_LOSSES): SETRC, LSDR, LSCHA, LSATM
+ * accumulated since the last ramgpu_reset_losses.  out: 4 doubles. */
+int ramgpu_losses(ramgpu_ctx *ctx, int member, int s, double *out4);
+int ramgpu_reset_losses(ramgpu_ctx *ctx);
+
+/* Number of kernel launches this context has issued (diagnostics). */
+long long ramgpu_launch_count(const ramgpu_ctx *ctx);
+
+/* Per-kernel timing with CUDA events recorded on the context's stream
+ * around every launch group (diagnostics; no reference counterpart).
+ * Kernel classes: 0 member tables, 1 DRIFTR ghost planes, 2 DRIFTR, 3 DRIFTP,
+ * 4 DRIFTE, 5 DRIFTMU (+fused loss), 6 periodic copy/mask, 7 ANISCH,
+ * 8 DTs tables, 9 SUMRC/loss bookkeeping.  ramgpu_kernel_times synchronises,
+ * adds the elapsed times of completed launches into ms[16] and counts[16]
+ * (caller-zeroed) and forgets them. */
+#define RAMGPU_NKCLASS 16
+int ramgpu_set_timing(ramgpu_ctx *ctx, int enable);
+int ramgpu_kernel_times(ramgpu_ctx *ctx, double *ms, long long *counts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

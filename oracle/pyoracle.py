@@ -1,0 +1,238 @@
+"""ctypes binding of the CPU oracle (oracle/ram_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline / reference leg, never by the product.  Parity of
+the oracle against the Fortran reference is unpinned (no Fortran compiler,
+no per-routine golden vectors in the reference); see ram_oracle.h.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ORACLE_DIR = Path(__file__).resolve().parent
+LIB_PATH = ORACLE_DIR / "liboracle.so"
+
+_P = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int)
+
+
+class RoGrid(C.Structure):
+    _fields_ = [("nr", C.c_int), ("nt", C.c_int), ("ne", C.c_int), ("npa", C.c_int),
+                ("lz", _P), ("rlz", _P), ("phi", _P),
+                ("dl1", C.c_double), ("mdr", C.c_double), ("dphi", C.c_double),
+                ("conf1", C.c_double), ("conf2", C.c_double),
+                ("ekev", _P), ("ebnd", _P), ("we", _P), ("de", _P),
+                ("mu", _P), ("dmu", _P), ("wmu", _P), ("upa", _P),
+                ("fnhs", _P), ("fnis", _P), ("bounhs", _P), ("bounis", _P), ("hdns", _P),
+                ("didt", _P), ("dibndt", _P), ("bnes", _P), ("dbdt", _P), ("eir", _P), ("eip", _P),
+                ("outside_mgnp", _IP)]
+
+
+class RoSpecies(C.Structure):
+    _fields_ = [("qs", C.c_int), ("cex_kind", C.c_int), ("rmas", C.c_double),
+                ("grel", _P), ("grbnd", _P), ("v", _P), ("ffactor", _P), ("epp", _P), ("ernh", _P)]
+
+
+class RoParams(C.Structure):
+    _fields_ = [("betalim", C.c_double), ("fraccfl", C.c_double), ("dts", C.c_double),
+                ("dtsmin", C.c_double), ("closed", C.c_int), ("do_atmol", C.c_int)]
+
+
+class RoDriftPara(C.Structure):
+    _fields_ = [("vr", _P), ("p1", _P), ("p2", _P), ("edot", _P), ("mudot", _P)]
+
+
+class RoLosses(C.Structure):
+    _fields_ = [("setrc", C.c_double), ("lsdr", C.c_double), ("lscha", C.c_double),
+                ("lsatm", C.c_double)]
+
+
+def build(force: bool = False) -> Path:
+    src = ORACLE_DIR / "ram_oracle.c"
+    if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < src.stat().st_mtime:
+        cc = os.environ.get("CC", "gcc")
+        subprocess.run([cc, "-O2", "-ffp-contract=off", "-fPIC", "-fopenmp", "-std=c11", "-shared",
+                        "-o", str(LIB_PATH), str(src), "-lm"], check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB_PATH))
+        gp, sp, pp = C.POINTER(RoGrid), C.POINTER(RoSpecies), C.POINTER(RoParams)
+        dpp = C.POINTER(RoDriftPara)
+        lib.ro_vt_vols.argtypes = [gp, C.c_double, _P]
+        lib.ro_driftpara.argtypes = [gp, sp, pp, dpp]
+        lib.ro_driftr.argtypes = [gp, sp, pp, dpp, _P, _P, _P, _P]
+        lib.ro_driftr.restype = C.c_double
+        for n in ("ro_driftp", "ro_drifte", "ro_driftmu"):
+            f = getattr(lib, n)
+            f.argtypes = [gp, sp, pp, dpp, _P, _P, _P]
+            f.restype = C.c_double
+        lib.ro_cepara.argtypes = [gp, sp, pp, _P, _P]
+        lib.ro_charexchange.argtypes = [gp, _P, _P]
+        lib.ro_atmol.argtypes = [gp, _P, _P]
+        lib.ro_sumrc.argtypes = [gp, _P]
+        lib.ro_sumrc.restype = C.c_double
+        lib.ro_anisch.argtypes = [gp, sp, _P, _P, _P]
+        lib.ro_flux.argtypes = [gp, sp, _P, _P]
+        PP = C.POINTER(_P)
+        lib.ro_ram_run.argtypes = [gp, C.c_int, sp, pp, C.c_double, _P, _P, PP, PP, PP, PP, PP,
+                                   C.POINTER(RoLosses), _P, C.c_int]
+        lib.ro_half_step.argtypes = [gp, sp, pp, dpp, _P, _P, _P, _P, _P, C.c_int]
+        _lib = lib
+    return _lib
+
+
+def _f(a, dtype=np.float64):
+    return np.asfortranarray(np.asarray(a, dtype=dtype))
+
+
+def _p(a):
+    return a.ctypes.data_as(_P) if a is not None else None
+
+
+class Oracle:
+    """CPU restatement of the reference routines for one grid and field set.
+
+    F2 arrays are Fortran-ordered (NR,NT,NE,NPA) float64 and are updated in
+    place."""
+
+    def __init__(self, grid, fields, betalim=1.5, fraccfl=0.8, dtsmin=0.1):
+        self.lib = load()
+        self.grid = grid
+        self.ns = len(grid.species)
+        self.betalim, self.fraccfl, self.dtsmin = betalim, fraccfl, dtsmin
+        g = grid
+        self._keep = {}
+
+        def keep(name, a, dtype=np.float64):
+            arr = _f(a, dtype)
+            self._keep[name] = arr
+            return arr
+
+        rg = RoGrid()
+        rg.nr, rg.nt, rg.ne, rg.npa = g.nr, g.nt, g.ne, g.npa
+        for k in ("lz", "rlz", "phi", "ekev", "ebnd", "we", "de", "mu", "dmu", "wmu", "upa"):
+            setattr(rg, k, _p(keep(k, getattr(g, k))))
+        rg.dl1, rg.mdr, rg.dphi, rg.conf1, rg.conf2 = g.dl1, g.mdr, g.dphi, g.conf1, g.conf2
+        for k in ("fnhs", "fnis", "bounhs", "bounis", "hdns", "didt", "dibndt", "bnes", "dbdt", "eir", "eip"):
+            setattr(rg, k, _p(keep("f_" + k, getattr(fields, k))))
+        rg.outside_mgnp = keep("outside", fields.outside, np.int32).ctypes.data_as(_IP)
+        self.rg = rg
+        self.sp = (RoSpecies * self.ns)()
+        for s, spc in enumerate(g.species):
+            o = self.sp[s]
+            o.qs, o.cex_kind, o.rmas = spc.charge, spc.cex_kind, g.rmas[s]
+            o.grel = _p(keep(f"grel{s}", g.grel[s]))
+            o.grbnd = _p(keep(f"grbnd{s}", g.grbnd[s]))
+            o.v = _p(keep(f"v{s}", g.v[s]))
+            o.ffactor = _p(keep(f"ff{s}", g.ffactor[s]))
+            o.epp = _p(keep(f"epp{s}", g.epp[s]))
+            o.ernh = _p(keep(f"ernh{s}", g.ernh[s]))
+
+    def params(self, dts, closed=False, do_atmol=True):
+        return RoParams(self.betalim, self.fraccfl, float(dts), self.dtsmin, int(closed), int(do_atmol))
+
+    def vt_vols(self, kp):
+        vt = np.zeros((self.grid.nr + 1, self.grid.nt), order="F")
+        self.lib.ro_vt_vols(C.byref(self.rg), float(kp), _p(vt))
+        return vt
+
+    def driftpara(self, s, dts):
+        g = self.grid
+        dp = {"vr": np.zeros(g.nr), "p1": np.zeros(g.nr), "p2": np.zeros((g.nr, g.ne), order="F"),
+              "edot": np.zeros((g.nr, g.ne), order="F"), "mudot": np.zeros((g.nr, g.npa), order="F")}
+        st = RoDriftPara(*[_p(dp[k]) for k in ("vr", "p1", "p2", "edot", "mudot")])
+        p = self.params(dts)
+        self.lib.ro_driftpara(C.byref(self.rg), C.byref(self.sp[s]), C.byref(p), C.byref(st))
+        dp["_struct"] = st
+        return dp
+
+    def sweep(self, which, s, f2, vt, dts, fgeos=None, closed=False, cdrift=None):
+        """Run one DRIFT* routine on f2 (Fortran array, in place); returns DtDrift*."""
+        dp = self.driftpara(s, dts)
+        p = self.params(dts, closed)
+        args = [C.byref(self.rg), C.byref(self.sp[s]), C.byref(p), C.byref(dp["_struct"]), _p(vt)]
+        cd = _p(cdrift) if cdrift is not None else None
+        if which == "R":
+            fg = _f(fgeos if fgeos is not None else np.zeros((self.grid.nt, self.grid.ne, self.grid.npa)))
+            return self.lib.ro_driftr(*args, _p(fg), _p(f2), cd)
+        fn = {"P": self.lib.ro_driftp, "E": self.lib.ro_drifte, "MU": self.lib.ro_driftmu}[which]
+        return fn(*args, _p(f2), cd)
+
+    def cepara(self, s, dts, do_atmol=True):
+        g = self.grid
+        charge = np.zeros((g.nr, g.nt, g.ne, g.npa), order="F")
+        atlos = np.zeros((g.nr, g.ne), order="F")
+        p = self.params(dts, do_atmol=do_atmol)
+        self.lib.ro_cepara(C.byref(self.rg), C.byref(self.sp[s]), C.byref(p), _p(charge), _p(atlos))
+        return charge, atlos
+
+    def sumrc(self, f2):
+        return self.lib.ro_sumrc(C.byref(self.rg), _p(f2))
+
+    def anisch(self, s, f2):
+        g = self.grid
+        pe = np.zeros((g.nr, g.nt), order="F")
+        pa = np.zeros((g.nr, g.nt), order="F")
+        self.lib.ro_anisch(C.byref(self.rg), C.byref(self.sp[s]), _p(f2), _p(pe), _p(pa))
+        return pe, pa
+
+    def flux(self, s, f2):
+        g = self.grid
+        out = np.zeros((g.nr, g.nt, g.ne, g.npa), order="F")
+        self.lib.ro_flux(C.byref(self.rg), C.byref(self.sp[s]), _p(f2), _p(out))
+        return out
+
+    def half_step(self, s, f2, vt, fgeos, dts, order, closed=False, do_atmol=True):
+        dp = self.driftpara(s, dts)
+        p = self.params(dts, closed, do_atmol)
+        charge, atlos = self.cepara(s, dts, do_atmol)
+        self.lib.ro_half_step(C.byref(self.rg), C.byref(self.sp[s]), C.byref(p), C.byref(dp["_struct"]),
+                              _p(vt), _p(_f(fgeos)), _p(charge), _p(atlos), _p(f2), int(order))
+
+    def ram_run(self, f2s, fgeos, dts, kp=None, vt=None, closed=False, do_atmol=True,
+                losses=None, want_flux=False, nthreads=1, species=None):
+        """One ram_run call over the species in ``species`` (default all);
+        f2s/fgeos are lists indexed by species."""
+        g = self.grid
+        idx = list(range(self.ns)) if species is None else list(species)
+        n = len(idx)
+        sp_arr = (RoSpecies * n)(*[self.sp[s] for s in idx])
+        p = self.params(dts, closed, do_atmol)
+        fg = [_f(fgeos[s]) for s in idx]
+        for s in idx:
+            assert f2s[s].flags["F_CONTIGUOUS"] and f2s[s].dtype == np.float64
+        PArr = _P * n
+        pe = [np.zeros((g.nr, g.nt), order="F") for _ in idx]
+        pa = [np.zeros((g.nr, g.nt), order="F") for _ in idx]
+        fl = [np.zeros((g.nr, g.nt, g.ne, g.npa), order="F") for _ in idx] if want_flux else None
+        vt_out = np.zeros((g.nr + 1, g.nt), order="F")
+        vt_in = _f(vt) if vt is not None else None
+        ls = (RoLosses * n)()
+        if losses is not None:
+            for t, s in enumerate(idx):
+                ls[t].setrc, ls[t].lsdr, ls[t].lscha, ls[t].lsatm = losses[s]
+        dn = C.c_double()
+        self.lib.ro_ram_run(C.byref(self.rg), n, sp_arr, C.byref(p), float(kp if kp is not None else 0.0),
+                            _p(vt_in), _p(vt_out), PArr(*[_p(a) for a in fg]),
+                            PArr(*[_p(f2s[s]) for s in idx]), PArr(*[_p(a) for a in pe]),
+                            PArr(*[_p(a) for a in pa]), PArr(*[_p(a) for a in fl]) if fl else None,
+                            ls, C.byref(dn), int(nthreads))
+        out = {"vt": vt_out, "ppert": dict(zip(idx, pe)), "ppart": dict(zip(idx, pa)),
+               "dts_next": dn.value,
+               "losses": {s: (ls[t].setrc, ls[t].lsdr, ls[t].lscha, ls[t].lsatm) for t, s in enumerate(idx)}}
+        if fl:
+            out["flux"] = dict(zip(idx, fl))
+        return out

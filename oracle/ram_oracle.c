@@ -1,0 +1,730 @@
+/*
+ * ram_oracle.c -- CPU oracle (TEST INFRASTRUCTURE ONLY; see ram_oracle.h).
+ *
+ * Restates, loop for loop and with the same double literals and operation
+ * order, these reference routines (paths relative to the reference project):
+ *   DRIFTPARA  src/ModRamDrift.f90:36-88
+ *   DRIFTR     src/ModRamDrift.f90:95-198
+ *   DRIFTP     src/ModRamDrift.f90:204-279
+ *   DRIFTE     src/ModRamDrift.f90:285-376
+ *   DRIFTMU    src/ModRamDrift.f90:382-473
+ *   CEPARA     src/ModRamLoss.f90:19-170 (analytic H/He/O branches)
+ *   CHAREXCHANGE src/ModRamLoss.f90:457-478
+ *   ATMOL      src/ModRamLoss.f90:485-507
+ *   SUMRC      src/ModRamRun.f90:231-259
+ *   ANISCH     src/ModRamRun.f90:343-415 (moment block only)
+ *   ram_run    src/ModRamRun.f90:16-225 (without Coulomb/WPI/EMIC/FLC)
+ * Constants are those of src/ModRamConst.f90:13-23.
+ *
+ * Addition not in the reference: p->closed selects closed outer faces in
+ * R, E and MU (FBND at both ends forced to zero) so that the weighted
+ * content  sum F2*WE*WMU  is conserved; it is applied identically here and
+ * in the CUDA kernels.
+ */
+#include "ram_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* src/ModRamConst.f90:13-23 (all double under -fdefault-real-8) */
+static const double RE = 6.371E6;
+static const double HMIN_UNUSED = 2E5;
+static const double Q = 1.602E-19;
+static const double CS = 2.998E8;
+static const double PI = 3.1415926535897932384626433832795;
+
+/* 1-based Fortran index helpers for one species. */
+#define NR (g->nr)
+#define NT (g->nt)
+#define NE (g->ne)
+#define NPA (g->npa)
+#define IX4(I, J, K, L) ((size_t)((((L)-1) * NE + (K)-1) * NT + (J)-1) * NR + (I)-1)
+#define IXF(I, J, L) ((size_t)(((L)-1) * NT + (J)-1) * (NR + 1) + (I)-1)
+#define IX2(I, J) ((size_t)((J)-1) * (NR + 1) + (I)-1)
+#define IXM(I, J) ((size_t)((J)-1) * NR + (I)-1)
+#define IXG(J, K, L) ((size_t)(((L)-1) * NE + (K)-1) * NT + (J)-1)
+#define IXFF(I, K, L) ((size_t)(((L)-1) * NE + (K)-1) * NR + (I)-1)
+#define IXRK(I, K) ((size_t)((K)-1) * NR + (I)-1)
+#define IXRL(I, L) ((size_t)((L)-1) * NR + (I)-1)
+
+#define F2(I, J, K, L) f2[IX4(I, J, K, L)]
+#define FNHS(I, J, L) g->fnhs[IXF(I, J, L)]
+#define FNIS(I, J, L) g->fnis[IXF(I, J, L)]
+#define BOUNHS(I, J, L) g->bounhs[IXF(I, J, L)]
+#define BOUNIS(I, J, L) g->bounis[IXF(I, J, L)]
+#define HDNS(I, J, L) g->hdns[IXF(I, J, L)]
+#define DIDT(I, J, L) g->didt[IXF(I, J, L)]
+#define DIBNDT(I, J, L) g->dibndt[IXF(I, J, L)]
+#define BNES(I, J) g->bnes[IX2(I, J)]
+#define DBDT(I, J) g->dbdt[IX2(I, J)]
+#define EIR(I, J) g->eir[IX2(I, J)]
+#define EIP(I, J) g->eip[IX2(I, J)]
+#define VT(I, J) vt[IX2(I, J)]
+#define OUTSIDE(I, J) g->outside_mgnp[IXM(I, J)]
+#define RLZ(I) g->rlz[(I)-1]
+#define LZ(I) g->lz[(I)-1]
+#define PHI(J) g->phi[(J)-1]
+#define EKEV(K) g->ekev[(K)-1]
+#define EBND(K) g->ebnd[(K)-1]
+#define WE(K) g->we[(K)-1]
+#define DE(K) g->de[(K)-1]
+#define MU(L) g->mu[(L)-1]
+#define DMU(L) g->dmu[(L)-1]
+#define WMU(L) g->wmu[(L)-1]
+#define UPA(I) g->upa[(I)-1]
+#define GREL(K) sp->grel[(K)-1]
+#define GRBND(K) sp->grbnd[(K)-1]
+#define VV(K) sp->v[(K)-1]
+#define FFACTOR(I, K, L) sp->ffactor[IXFF(I, K, L)]
+#define EPP(K) sp->epp[(K)-1]
+#define ERNH(K) sp->ernh[(K)-1]
+#define VR(I) dp->vr[(I)-1]
+#define P1(I) dp->p1[(I)-1]
+#define P2(I, K) dp->p2[IXRK(I, K)]
+#define EDOT(I, K) dp->edot[IXRK(I, K)]
+#define MUDOT(I, L) dp->mudot[IXRL(I, L)]
+
+static inline double dmax(double a, double b) { return a > b ? a : b; }
+static inline double dmin(double a, double b) { return a < b ? a : b; }
+/* Fortran MAX/MIN for the limiter: MAX(MIN(B*R,1.),MIN(R,B)) */
+static inline double limiter(double betalim, double r)
+{
+    return dmax(dmin(betalim * r, 1.), dmin(r, betalim));
+}
+
+void ro_vt_vols(const ro_grid *g, double kp, double *vt)
+{
+    /* AVS=7.05E-6/(1.-0.159*KP+0.0093*KP**2)**3/RE ; PHIOFS = 0 */
+    double t = 1. - 0.159 * kp + 0.0093 * (kp * kp);
+    double avs = 7.05E-6 / (t * t * t) / RE;
+    const double phiofs = 0 * PI / 12.;
+    for (int I = 1; I <= NR + 1; ++I)
+        for (int J = 1; J <= NT; ++J) {
+            double lr = LZ(I) * RE;
+            VT(I, J) = avs * (lr * lr) * sin(PHI(J) - phiofs);
+        }
+}
+
+void ro_driftpara(const ro_grid *g, const ro_species *sp, const ro_params *p, ro_driftpara_t *dp)
+{
+    const double DTs = p->dts, MDR = g->mdr, DPHI = g->dphi;
+    const int QS = sp->qs;
+    for (int I = 1; I <= NR; ++I) {
+        VR(I) = DTs / MDR / (RLZ(I) + 0.5 * MDR) / 2 / DPHI;
+        P1(I) = DTs / DPHI / 2 / MDR / RLZ(I);
+        for (int K = 1; K <= NE; ++K)
+            P2(I, K) = DTs * EKEV(K) * 1000 * (GREL(K) + 1) / GREL(K) / (RLZ(I) * RLZ(I)) / DPHI / QS;
+    }
+    for (int I = 1; I <= NR; ++I) {
+        for (int L = 1; L <= NPA - 1; ++L) {
+            double MUBOUN = MU(L) + 0.5 * WMU(L);
+            MUDOT(I, L) = (1. - MUBOUN * MUBOUN) * DTs / 2 / MUBOUN / RLZ(I);
+        }
+        MUDOT(I, NPA) = 0.;
+        for (int K = 1; K <= NE; ++K)
+            EDOT(I, K) = EBND(K) * DTs / RLZ(I) * (GRBND(K) + 1) / GRBND(K) / 2.;
+    }
+}
+
+/* ------------------------------------------------------------------ DRIFTR */
+double ro_driftr(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                 const ro_driftpara_t *dp, const double *vt, const double *fgeos,
+                 double *f2, double *cdrift)
+{
+    const double DTs = p->dts, MDR = g->mdr, DPHI = g->dphi, BetaLim = p->betalim;
+    const int QS = sp->qs;
+    double DtDriftR = 100000.0;
+    int *sgn = (int *)malloc(sizeof(int) * NR * NT);
+    double *CR = (double *)calloc((size_t)NR * NT, sizeof(double));
+    double *F = (double *)calloc((size_t)NR + 2, sizeof(double)); /* F(1:NR+2) -> F[0..NR+1] */
+    double *FBND = (double *)calloc((size_t)NR, sizeof(double));
+    double *CD = (double *)malloc(sizeof(double) * NR); /* CDriftR(:,J,K,L) of the current line */
+#define FF(n) F[(n)-1]
+#define FB(n) FBND[(n)-1]
+#define SG(i, j) sgn[IXM(i, j)]
+    for (int i = 0; i < NR * NT; ++i) sgn[i] = 1;
+
+    for (int I = 1; I <= NR; ++I)
+        for (int J = 1; J <= NT; ++J) {
+            int J0 = J - 1;
+            if (J == 1) J0 = NT - 1;
+            int J1 = J + 1;
+            if (J == NT) J1 = 2;
+            double den = BNES(I, J) + BNES(I + 1, J);
+            CR[IXM(I, J)] = VR(I) * (VT(I, J0) + VT(I + 1, J0) - VT(I, J1) - VT(I + 1, J1)) / den
+                          + (EIP(I, J) + EIP(I + 1, J)) / den * DTs / MDR;
+        }
+
+    for (int K = 1; K <= NE; ++K) {
+        double P4 = DTs * EKEV(K) * 1000.0 * (GREL(K) + 1) / GREL(K) / DPHI / MDR / QS;
+        for (int L = 1; L <= NPA; ++L)
+            for (int J = 1; J <= NT; ++J) {
+                for (int I = 1; I <= NR; ++I) FF(I) = F2(I, J, K, L);
+                int J0 = J - 1;
+                if (J == 1) J0 = NT - 1;
+                int J1 = J + 1;
+                if (J == NT) J1 = 2;
+                for (int I = 1; I <= NR; ++I) {
+                    double CGR1 = FNIS(I + 1, J1, L) + FNIS(I, J1, L) - FNIS(I + 1, J0, L) - FNIS(I, J0, L);
+                    double CGR2 = BNES(I + 1, J1) + BNES(I, J1) - BNES(I + 1, J0) - BNES(I, J0);
+                    double CGR3 = CGR1 + (FNIS(I + 1, J, L) + FNIS(I, J, L) - 2 * FNHS(I + 1, J, L)
+                                          - 2 * FNHS(I, J, L)) * CGR2 / 2. / (BNES(I + 1, J) + BNES(I, J));
+                    double CGR = CGR3 / (FNHS(I, J, L) + FNHS(I + 1, J, L)) * P4 / 2.
+                                 / (BNES(I, J) + BNES(I + 1, J)) / (RLZ(I) + 0.5 * MDR);
+                    CD[I - 1] = CR[IXM(I, J)] + CGR;
+                    if (OUTSIDE(I, J) == 0) {
+                        double ctemp = dmax(fabs(CD[I - 1]), 1E-10);
+                        DtDriftR = dmin(DtDriftR, p->fraccfl * DTs / ctemp);
+                    }
+                    SG(I, J) = 1;
+                    if (CD[I - 1] < 0) SG(I, J) = -1;
+                }
+                int UR;
+                if (SG(NR, J) == 1) {
+                    FB(1) = 0.;
+                    FB(NR) = FF(NR);
+                    UR = NR - 1;
+                } else {
+                    FB(1) = FF(2);
+                    UR = NR;
+                    if (OUTSIDE(NR, J) == 1) {
+                        FF(NR + 1) = 0.;
+                        FF(NR + 2) = 0.;
+                    } else {
+                        FF(NR + 1) = fgeos[IXG(J, K, L)] * g->conf1 * FNHS(NR, J, L);
+                        FF(NR + 2) = fgeos[IXG(J, K, L)] * g->conf2 * FNHS(NR, J, L);
+                    }
+                }
+                for (int I = 2; I <= UR; ++I) {
+                    int s = SG(I, J);
+                    double X = FF(I + 1) - FF(I);
+                    double FUP = 0.5 * (FF(I) + FF(I + 1) - s * X);
+                    if (fabs(X) <= 1.E-27) FB(I) = FUP;
+                    if (fabs(X) > 1.E-27) {
+                        int N = I + 1 - s;
+                        double R = (FF(N) - FF(N - 1)) / X;
+                        if (R <= 0) FB(I) = FUP;
+                        if (R > 0) {
+                            double LIM = limiter(BetaLim, R);
+                            double CORR = -0.5 * (CD[I - 1] - s) * X;
+                            FB(I) = FUP + LIM * CORR;
+                        }
+                    }
+                }
+                if (p->closed) {
+                    FB(1) = 0.;
+                    FB(NR) = 0.;
+                }
+                for (int I = 2; I <= NR; ++I) {
+                    F2(I, J, K, L) = F2(I, J, K, L) - CD[I - 1] * FB(I) + CD[I - 2] * FB(I - 1);
+                    if (F2(I, J, K, L) < 0) F2(I, J, K, L) = 1E-15;
+                }
+                if (cdrift)
+                    for (int I = 1; I <= NR; ++I) cdrift[IX4(I, J, K, L)] = CD[I - 1];
+            }
+    }
+#undef FF
+#undef FB
+#undef SG
+    free(sgn);
+    free(CR);
+    free(F);
+    free(FBND);
+    free(CD);
+    return DtDriftR;
+}
+
+/* ------------------------------------------------------------------ DRIFTP */
+double ro_driftp(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                 const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift)
+{
+    const double DTs = p->dts, MDR = g->mdr, DPHI = g->dphi, BetaLim = p->betalim;
+    double DtDriftP = 100000.0;
+    const double OME = 7.3E-5;
+    double *F = (double *)calloc((size_t)NT, sizeof(double));
+    double *FBND = (double *)calloc((size_t)NT, sizeof(double));
+    double *CD = (double *)calloc((size_t)NT, sizeof(double));
+#define FF(n) F[(n)-1]
+#define FB(n) FBND[(n)-1]
+#define C(n) CD[(n)-1]
+    for (int L = 1; L <= NPA; ++L)
+        for (int K = 1; K <= NE; ++K)
+            for (int I = 2; I <= NR; ++I) {
+                for (int J = 1; J <= NT; ++J) FF(J) = F2(I, J, K, L);
+                for (int J = 2; J <= NT; ++J) {
+                    int J1 = J + 1;
+                    if (J == NT) J1 = 2;
+                    double GPA1 = FNIS(I, J, L) + FNIS(I, J1, L)
+                                  + (FNIS(I + 1, J1, L) + FNIS(I + 1, J, L) - FNIS(I - 1, J, L) - FNIS(I - 1, J1, L))
+                                  * RLZ(I) / 2. / MDR;
+                    double GPA2 = RLZ(I) / 4. / MDR * (FNIS(I, J, L) + FNIS(I, J1, L) - 2 * FNHS(I, J, L) - 2 * FNHS(I, J1, L))
+                                  * (BNES(I + 1, J1) + BNES(I + 1, J) - BNES(I - 1, J) - BNES(I - 1, J1))
+                                  / (BNES(I, J) + BNES(I, J1));
+                    C(J) = ((VT(I + 1, J) + VT(I + 1, J1) - VT(I - 1, J) - VT(I - 1, J1)) * P1(I)
+                            - P2(I, K) * (GPA1 + GPA2) / (FNHS(I, J, L) + FNHS(I, J1, L))
+                            - (EIR(I, J1) + EIR(I, J)) / RLZ(I) * DTs / DPHI)
+                               / (BNES(I, J) + BNES(I, J1))
+                           + OME * DTs / DPHI;
+                    if (OUTSIDE(I, J) == 0) {
+                        double ctemp = dmax(fabs(C(J)), 1E-10);
+                        DtDriftP = dmin(DtDriftP, p->fraccfl * DTs / ctemp);
+                    }
+                    int s = 1;
+                    if (C(J) < 0) s = -1;
+                    double X = FF(J1) - FF(J);
+                    double FUP = 0.5 * (FF(J) + FF(J1) - s * X);
+                    if (fabs(X) <= 1.E-27) FB(J) = FUP;
+                    if (fabs(X) > 1.E-27) {
+                        int N = J + 1 - s;
+                        if (N > NT) N = N - NT + 1;
+                        double R = (FF(N) - FF(N - 1)) / X;
+                        if (R <= 0) FB(J) = FUP;
+                        if (R > 0) {
+                            double LIM = limiter(BetaLim, R);
+                            double CORR = -0.5 * (C(J) - s) * X;
+                            FB(J) = FUP + LIM * CORR;
+                        }
+                    }
+                }
+                C(1) = C(NT);
+                FB(1) = FB(NT);
+                for (int J = 2; J <= NT; ++J) {
+                    F2(I, J, K, L) = F2(I, J, K, L) - C(J) * FB(J) + C(J - 1) * FB(J - 1);
+                    if (F2(I, J, K, L) < 0) F2(I, J, K, L) = 1E-15;
+                }
+                F2(I, 1, K, L) = F2(I, NT, K, L);
+                if (cdrift)
+                    for (int J = 1; J <= NT; ++J) cdrift[IX4(I, J, K, L)] = C(J);
+            }
+#undef FF
+#undef FB
+#undef C
+    free(F);
+    free(FBND);
+    free(CD);
+    return DtDriftP;
+}
+
+/* ------------------------------------------------------------------ DRIFTE */
+double ro_drifte(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                 const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift)
+{
+    const double DTs = p->dts, MDR = g->mdr, DPHI = g->dphi, BetaLim = p->betalim;
+    const int QS = sp->qs;
+    double DtDriftE = 10000.0;
+    const double OME = 7.3E-5;
+    /* F(0:NE+2) -> F[0..NE+2] */
+    double *F = (double *)calloc((size_t)NE + 3, sizeof(double));
+    double *FBND = (double *)calloc((size_t)NE, sizeof(double));
+    double *CD = (double *)calloc((size_t)NE, sizeof(double));
+#define FF(n) F[(n)]
+#define FB(n) FBND[(n)-1]
+#define C(n) CD[(n)-1]
+    double EZERO = EKEV(1) - WE(1);
+    double GRZERO = 1. + EZERO * 1000. * Q / sp->rmas / CS / CS;
+    FF(NE + 1) = 0.;
+    FF(NE + 2) = 0.;
+    for (int J = 1; J <= NT; ++J) {
+        int J0 = J - 1;
+        if (J == 1) J0 = NT - 1;
+        int J2 = J + 1;
+        if (J == NT) J2 = 2;
+        for (int I = 2; I <= NR; ++I) {
+            double DRD1 = (EIP(I, J) * RLZ(I) - (VT(I, J2) - VT(I, J0)) / 2. / DPHI) / BNES(I, J);
+            double DPD1 = OME * RLZ(I) + ((VT(I + 1, J) - VT(I - 1, J)) / 2 / MDR - EIR(I, J)) / BNES(I, J);
+            for (int L = 1; L <= NPA; ++L) {
+                double GPA = (1. - FNIS(I, J, L) / 2. / FNHS(I, J, L)) / BNES(I, J);
+                double GPR1 = GPA * (BNES(I + 1, J) - BNES(I - 1, J)) / 2. / MDR;
+                double GPR2 = -FNIS(I, J, L) / FNHS(I, J, L) / RLZ(I);
+                double GPR3 = -(FNIS(I + 1, J, L) - FNIS(I - 1, J, L)) / 2. / MDR / FNHS(I, J, L);
+                double GPP1 = GPA * (BNES(I, J2) - BNES(I, J0)) / 2. / DPHI;
+                double GPP2 = -(FNIS(I, J2, L) - FNIS(I, J0, L)) / 2. / DPHI / FNHS(I, J, L);
+                double DRD2 = (FNIS(I, J2, L) - FNIS(I, J0, L)) / 2. / DPHI
+                              + (FNIS(I, J, L) - 2 * FNHS(I, J, L)) * (BNES(I, J2) - BNES(I, J0)) / 4 / BNES(I, J) / DPHI;
+                double DPD2 = FNIS(I, J, L) + (FNIS(I + 1, J, L) - FNIS(I - 1, J, L)) * RLZ(I) / 2 / MDR
+                              + RLZ(I) * (FNIS(I, J, L) - 2 * FNHS(I, J, L)) / 4 / MDR * (BNES(I + 1, J) - BNES(I - 1, J)) / BNES(I, J);
+                for (int K = 1; K <= NE; ++K) FF(K) = F2(I, J, K, L);
+                FF(1) = FF(2) * GREL(1) / GREL(2) * sqrt((GREL(2) * GREL(2) - 1) / (GREL(1) * GREL(1) - 1));
+                FF(0) = FF(1) * GRZERO / GREL(1) * sqrt((GREL(1) * GREL(1) - 1) / (GRZERO * GRZERO - 1));
+                for (int K = 1; K <= NE; ++K) {
+                    double EDT1 = EBND(K) * 1e3 * (GRBND(K) + 1) / 2 / GRBND(K) / FNHS(I, J, L) / RLZ(I) / BNES(I, J) / QS;
+                    double DRDT = DRD1 + EDT1 * DRD2 * RLZ(I);
+                    double DPDT = DPD1 - EDT1 * DPD2;
+                    double dBdt1 = DBDT(I, J) * (1. - FNIS(I, J, L) / 2. / FNHS(I, J, L)) * RLZ(I) / BNES(I, J);
+                    double dIdt1 = -DIDT(I, J, L) * RLZ(I) / FNHS(I, J, L);
+                    C(K) = EDOT(I, K) * ((GPR1 + GPR2 + GPR3) * DRDT + (GPP1 + GPP2) * DPDT + dBdt1 + dIdt1);
+                    if (OUTSIDE(I, J) == 0) {
+                        double ctemp = dmax(fabs(C(K)), 1E-10);
+                        DtDriftE = dmin(DtDriftE, p->fraccfl * DTs * DE(K) / ctemp);
+                    }
+                    int s = 1;
+                    if (C(K) < 0) s = -1;
+                    double X = FF(K + 1) - FF(K);
+                    double FUP = 0.5 * (FF(K) + FF(K + 1) - s * X);
+                    if (fabs(X) <= 1.E-27) FB(K) = FUP;
+                    if (fabs(X) > 1.E-27) {
+                        int N = K + 1 - s;
+                        double R = (FF(N) - FF(N - 1)) / X;
+                        if (R <= 0) FB(K) = FUP;
+                        if (R > 0) {
+                            double LIM = limiter(BetaLim, R);
+                            double CORR = -0.5 * (C(K) / DE(K) - s) * X;
+                            FB(K) = FUP + LIM * CORR;
+                        }
+                    }
+                }
+                if (p->closed) {
+                    FB(1) = 0.;
+                    FB(NE) = 0.;
+                }
+                for (int K = 2; K <= NE; ++K) {
+                    F2(I, J, K, L) = F2(I, J, K, L) - C(K) / WE(K) * FB(K) + C(K - 1) / WE(K) * FB(K - 1);
+                    if (F2(I, J, K, L) < 0) F2(I, J, K, L) = 1E-15;
+                }
+                if (cdrift)
+                    for (int K = 1; K <= NE; ++K) cdrift[IX4(I, J, K, L)] = C(K);
+            }
+        }
+    }
+#undef FF
+#undef FB
+#undef C
+    free(F);
+    free(FBND);
+    free(CD);
+    return DtDriftE;
+}
+
+/* ----------------------------------------------------------------- DRIFTMU */
+double ro_driftmu(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                  const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift)
+{
+    const double DTs = p->dts, MDR = g->mdr, DPHI = g->dphi, BetaLim = p->betalim;
+    const int QS = sp->qs;
+    double DtDriftMu = 10000.0;
+    const double OME = 7.3E-5;
+    double *F = (double *)calloc((size_t)NPA, sizeof(double));
+    double *FBND = (double *)calloc((size_t)NPA, sizeof(double));
+    double *CD = (double *)calloc((size_t)NPA, sizeof(double));
+#define FF(n) F[(n)-1]
+#define FB(n) FBND[(n)-1]
+#define C(n) CD[(n)-1]
+    for (int K = 1; K <= NE; ++K)
+        for (int J = 1; J <= NT; ++J) {
+            int J0 = J - 1;
+            if (J == 1) J0 = NT - 1;
+            int J1 = J + 1;
+            if (J == NT) J1 = 2;
+            for (int I = 2; I <= NR; ++I) {
+                for (int L = 1; L <= NPA; ++L) FF(L) = F2(I, J, K, L);
+                FF(1) = FF(2);
+                double DRM1 = (EIP(I, J) * RLZ(I) - (VT(I, J1) - VT(I, J0)) / 2 / DPHI) / BNES(I, J);
+                double DPM1 = OME * RLZ(I) + ((VT(I + 1, J) - VT(I - 1, J)) / 2 / MDR - EIR(I, J)) / BNES(I, J);
+                for (int L = 2; L <= NPA; ++L) {
+                    double CMUDOT = MUDOT(I, L) * BOUNIS(I, J, L) / BOUNHS(I, J, L);
+                    double GMR1 = (BNES(I + 1, J) - BNES(I - 1, J)) / 4 / MDR / BNES(I, J);
+                    double GMR2 = 1 / RLZ(I);
+                    double GMR3 = (BOUNIS(I + 1, J, L) - BOUNIS(I - 1, J, L)) / 2 / MDR / BOUNIS(I, J, L);
+                    double GMP1 = (BNES(I, J1) - BNES(I, J0)) / 4 / DPHI / BNES(I, J);
+                    double GMP2 = (BOUNIS(I, J1, L) - BOUNIS(I, J0, L)) / 2 / DPHI / BOUNIS(I, J, L);
+                    double EDT = EKEV(K) * 1e3 * (GREL(K) + 1) / 2 / GREL(K) / BOUNHS(I, J, L) / RLZ(I) / BNES(I, J) / QS;
+                    double DRM2 = (BOUNIS(I, J1, L) - BOUNIS(I, J0, L)) / 2 / DPHI
+                                  + (BOUNIS(I, J, L) - 2 * BOUNHS(I, J, L)) * (BNES(I, J1) - BNES(I, J0)) / 4 / BNES(I, J) / DPHI;
+                    double DPM2 = BOUNIS(I, J, L) + (BOUNIS(I + 1, J, L) - BOUNIS(I - 1, J, L)) * RLZ(I) / 2 / MDR
+                                  + (BOUNIS(I, J, L) - 2 * BOUNHS(I, J, L)) * RLZ(I) / 4 / MDR * (BNES(I + 1, J) - BNES(I - 1, J)) / BNES(I, J);
+                    double DRDM = DRM1 + EDT * DRM2 * RLZ(I);
+                    double DPDM = DPM1 - EDT * DPM2;
+                    double dBdt2 = DBDT(I, J) / 2. / BNES(I, J) * RLZ(I);
+                    double dIbndt2 = DIBNDT(I, J, L) * RLZ(I) / BOUNIS(I, J, L);
+                    C(L) = -CMUDOT * ((GMR1 + GMR2 + GMR3) * DRDM + (GMP1 + GMP2) * DPDM + dBdt2 + dIbndt2);
+                    if (OUTSIDE(I, J) == 0) {
+                        double ctemp = dmax(fabs(C(L)), 1E-32);
+                        DtDriftMu = dmin(DtDriftMu, p->fraccfl * DTs * DMU(L) / ctemp);
+                    }
+                    int s = 1;
+                    if (C(L) < 0.0) s = -1;
+                    if (L <= NPA - 2) {
+                        double X = FF(L + 1) - FF(L);
+                        double FUP = 0.5 * (FF(L) + FF(L + 1) - s * X);
+                        if (fabs(X) <= 1.E-27) FB(L) = FUP;
+                        if (fabs(X) > 1.E-27) {
+                            int N = L + 1 - s;
+                            double R = (FF(N) - FF(N - 1)) / X;
+                            if (R <= 0) FB(L) = FUP;
+                            if (R > 0) {
+                                double LIM = limiter(BetaLim, R);
+                                double CORR = -0.5 * (C(L) / DMU(L) - s) * X;
+                                FB(L) = FUP + LIM * CORR;
+                            }
+                        }
+                    }
+                }
+                C(1) = 0.;
+                FB(1) = 0.;
+                FB(NPA - 1) = FF(NPA);
+                if (p->closed) FB(NPA - 1) = 0.;
+                for (int L = 2; L <= NPA - 1; ++L) {
+                    F2(I, J, K, L) = F2(I, J, K, L) - C(L) / WMU(L) * FB(L) + C(L - 1) / WMU(L) * FB(L - 1);
+                    if (F2(I, J, K, L) < 0) F2(I, J, K, L) = 1E-15;
+                }
+                F2(I, J, K, NPA) = F2(I, J, K, NPA - 1) * FNHS(I, J, NPA) * MU(NPA) / FNHS(I, J, NPA - 1) / MU(NPA - 1);
+                if (cdrift)
+                    for (int L = 1; L <= NPA; ++L) cdrift[IX4(I, J, K, L)] = C(L);
+            }
+        }
+#undef FF
+#undef FB
+#undef C
+    free(F);
+    free(FBND);
+    free(CD);
+    return DtDriftMu;
+}
+
+/* ------------------------------------------------------------------ CEPARA */
+void ro_cepara(const ro_grid *g, const ro_species *sp, const ro_params *p, double *charge, double *atlos)
+{
+    const double DTs = p->dts;
+    size_t n = (size_t)NR * NT * NE * NPA;
+    for (size_t i = 0; i < n; ++i) charge[i] = 1.;
+    if (sp->cex_kind >= 1 && sp->cex_kind <= 3) {
+        for (int L = 2; L <= NPA; ++L)
+            for (int K = 2; K <= NE; ++K)
+                for (int I = 2; I <= NR; ++I)
+                    for (int J = 1; J <= NT; ++J) {
+                        double X = log10(EKEV(K));
+                        if (X < -2.) X = -2.;
+                        double X2 = X * X, X3 = X2 * X, X4 = X2 * X2, Y;
+                        if (sp->cex_kind == 1)
+                            Y = -18.767 - 0.11017 * X - 3.8173e-2 * X2 - 0.1232 * X3 - 5.0488e-2 * X4;
+                        else if (sp->cex_kind == 2)
+                            Y = -20.789 + 0.92316 * X - 0.68017 * X2 + 0.66153 * X3 - 0.20998 * X4;
+                        else
+                            Y = -18.987 - 0.10613 * X - 5.4841E-3 * X2 - 1.6262E-2 * X3 - 7.0554E-3 * X4;
+                        double ALPHA = pow(10., Y) * VV(K) * HDNS(I, J, L) * DTs;
+                        charge[IX4(I, J, K, L)] = exp(-ALPHA);
+                    }
+    }
+    for (int K = 2; K <= NE; ++K)
+        for (int I = 2; I <= NR; ++I) {
+            double TAUB = 2 * RLZ(I) / VV(K);
+            atlos[IXRK(I, K)] = exp(-DTs / TAUB);
+        }
+}
+
+void ro_charexchange(const ro_grid *g, double *f2, const double *charge)
+{
+    for (int K = 2; K <= NE; ++K)
+        for (int J = 1; J <= NT; ++J)
+            for (int I = 2; I <= NR; ++I)
+                for (int L = 2; L <= NPA; ++L) F2(I, J, K, L) = F2(I, J, K, L) * charge[IX4(I, J, K, L)];
+}
+
+void ro_atmol(const ro_grid *g, double *f2, const double *atlos)
+{
+    for (int K = 2; K <= NE; ++K)
+        for (int J = 1; J <= NT; ++J)
+            for (int I = 2; I <= NR; ++I) {
+                int u = (int)UPA(I);
+                for (int L = u; L <= NPA; ++L)
+                    F2(I, J, K, L) = F2(I, J, K, L) * pow(atlos[IXRK(I, K)], 1 / FNHS(I, J, L));
+            }
+}
+
+double ro_sumrc(const ro_grid *g, const double *f2)
+{
+    double setrc = 0.;
+    for (int I = 2; I <= NR; ++I)
+        for (int K = 2; K <= NE; ++K)
+            for (int L = 2; L <= NPA; ++L)
+                for (int J = 1; J <= NT - 1; ++J) {
+                    double WEIGHT = F2(I, J, K, L) * WE(K) * WMU(L);
+                    setrc = setrc + EKEV(K) * WEIGHT;
+                }
+    return setrc;
+}
+
+void ro_anisch(const ro_grid *g, const ro_species *sp, double *f2, double *ppert, double *ppart)
+{
+    const double cv = CS * 100;
+    const double RFAC = 4 * PI / cv;
+    int khi[5] = {6, 10, 25, 30, 35};
+    khi[4] = NE;
+    for (int I = 2; I <= NR; ++I)
+        for (int J = 1; J <= NT; ++J) {
+            int klo = 2;
+            double PPERT = 0., PPART = 0.;
+            for (int iwa = 0; iwa < 5; ++iwa) {
+                double PPER = 0., PPAR = 0., RNHT = 0., EDEN = 0.;
+                for (int K = klo; K <= khi[iwa]; ++K) {
+                    F2(I, J, K, 1) = F2(I, J, K, 2);
+                    double SUME = 0., SUMA = 0., SUMN = 0.;
+                    int u = (int)(UPA(I) - 1);
+                    for (int L = 1; L <= u; ++L) {
+                        double ERNM = WMU(L) / FFACTOR(I, K, L) / FNHS(I, J, L);
+                        double EPMA = ERNM * MU(L) * MU(L);
+                        double EPME = ERNM - EPMA;
+                        SUME = SUME + F2(I, J, K, L) * EPME;
+                        SUMA = SUMA + F2(I, J, K, L) * EPMA;
+                        SUMN = SUMN + F2(I, J, K, L) * ERNM;
+                    }
+                    PPER = PPER + EPP(K) * SUME;
+                    PPAR = PPAR + EPP(K) * SUMA;
+                    RNHT = RNHT + ERNH(K) * SUMN;
+                    EDEN = EDEN + ERNH(K) * EKEV(K) * SUMN;
+                }
+                PPAR = 2 * RFAC * PPAR;
+                PPER = RFAC * PPER;
+                klo = khi[iwa] + 1;
+                PPERT = PPERT + PPER;
+                PPART = PPART + PPAR;
+            }
+            if (ppert) ppert[IXM(I, J)] = PPERT;
+            if (ppart) ppart[IXM(I, J)] = PPART;
+        }
+}
+
+void ro_flux(const ro_grid *g, const ro_species *sp, const double *f2, double *flux)
+{
+    for (int I = 2; I <= NR; ++I)
+        for (int K = 2; K <= NE; ++K)
+            for (int L = 2; L <= NPA; ++L)
+                for (int J = 1; J <= NT - 1; ++J)
+                    flux[IX4(I, J, K, L)] = F2(I, J, K, L) / FFACTOR(I, K, L) / FNHS(I, J, L);
+}
+
+static void alloc_dp(const ro_grid *g, ro_driftpara_t *dp)
+{
+    dp->vr = (double *)calloc((size_t)NR, sizeof(double));
+    dp->p1 = (double *)calloc((size_t)NR, sizeof(double));
+    dp->p2 = (double *)calloc((size_t)NR * NE, sizeof(double));
+    dp->edot = (double *)calloc((size_t)NR * NE, sizeof(double));
+    dp->mudot = (double *)calloc((size_t)NR * NPA, sizeof(double));
+}
+static void free_dp(ro_driftpara_t *dp)
+{
+    free(dp->vr);
+    free(dp->p1);
+    free(dp->p2);
+    free(dp->edot);
+    free(dp->mudot);
+}
+
+void ro_half_step(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                  const ro_driftpara_t *dp, const double *vt, const double *fgeos,
+                  const double *charge, const double *atlos, double *f2, int order)
+{
+    if (order == 0) {
+        ro_driftr(g, sp, p, dp, vt, fgeos, f2, NULL);
+        ro_driftp(g, sp, p, dp, vt, f2, NULL);
+        ro_drifte(g, sp, p, dp, vt, f2, NULL);
+        ro_driftmu(g, sp, p, dp, vt, f2, NULL);
+        if (sp->cex_kind) ro_charexchange(g, f2, charge);
+        if (p->do_atmol) ro_atmol(g, f2, atlos);
+    } else {
+        if (p->do_atmol) ro_atmol(g, f2, atlos);
+        if (sp->cex_kind) ro_charexchange(g, f2, charge);
+        ro_driftmu(g, sp, p, dp, vt, f2, NULL);
+        ro_drifte(g, sp, p, dp, vt, f2, NULL);
+        ro_driftp(g, sp, p, dp, vt, f2, NULL);
+        ro_driftr(g, sp, p, dp, vt, fgeos, f2, NULL);
+    }
+}
+
+int ro_ram_run(const ro_grid *g, int ns, const ro_species *sp_all, const ro_params *p,
+               double kp, const double *vt_in, double *vt_out,
+               const double *const *fgeos, double *const *f2s,
+               double *const *ppert, double *const *ppart, double *const *flux,
+               ro_losses *losses, double *dts_next, int nthreads)
+{
+    size_t nvt = (size_t)(NR + 1) * NT;
+    double *vt = (double *)malloc(sizeof(double) * nvt);
+    if (vt_in)
+        memcpy(vt, vt_in, sizeof(double) * nvt);
+    else
+        ro_vt_vols(g, kp, vt);
+    if (vt_out) memcpy(vt_out, vt, sizeof(double) * nvt);
+
+    double *dtr = (double *)malloc(sizeof(double) * ns * 4);
+    size_t ncell = (size_t)NR * NT * NE * NPA;
+#ifdef _OPENMP
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 1)
+#endif
+    for (int iS = 0; iS < ns; ++iS) {
+        const ro_species *sp = &sp_all[iS];
+        double *f2 = f2s[iS];
+        double *charge = (double *)malloc(sizeof(double) * ncell);
+        double *atlos = (double *)calloc((size_t)NR * NE, sizeof(double));
+        ro_driftpara_t dpv;
+        ro_driftpara_t *dp = &dpv;
+        alloc_dp(g, dp);
+        ro_cepara(g, sp, p, charge, atlos);
+        ro_driftpara(g, sp, p, dp);
+        double setrc = losses ? losses[iS].setrc : 0., s1;
+        double lsdr = 0., lscha = 0., lsatm = 0.;
+        /* forward half */
+        dtr[iS * 4 + 0] = ro_driftr(g, sp, p, dp, vt, fgeos[iS], f2, NULL);
+        dtr[iS * 4 + 1] = ro_driftp(g, sp, p, dp, vt, f2, NULL);
+        dtr[iS * 4 + 2] = ro_drifte(g, sp, p, dp, vt, f2, NULL);
+        dtr[iS * 4 + 3] = ro_driftmu(g, sp, p, dp, vt, f2, NULL);
+        s1 = ro_sumrc(g, f2); lsdr += setrc - s1; setrc = s1;
+        if (sp->cex_kind) {
+            ro_charexchange(g, f2, charge);
+            s1 = ro_sumrc(g, f2); lscha += setrc - s1; setrc = s1;
+        }
+        if (p->do_atmol) {
+            ro_atmol(g, f2, atlos);
+            s1 = ro_sumrc(g, f2); lsatm += setrc - s1; setrc = s1;
+            /* reverse half */
+            ro_atmol(g, f2, atlos);
+            s1 = ro_sumrc(g, f2); lsatm += setrc - s1; setrc = s1;
+        }
+        if (sp->cex_kind) {
+            ro_charexchange(g, f2, charge);
+            s1 = ro_sumrc(g, f2); lscha += setrc - s1; setrc = s1;
+        }
+        ro_driftmu(g, sp, p, dp, vt, f2, NULL);
+        ro_drifte(g, sp, p, dp, vt, f2, NULL);
+        ro_driftp(g, sp, p, dp, vt, f2, NULL);
+        ro_driftr(g, sp, p, dp, vt, fgeos[iS], f2, NULL);
+        s1 = ro_sumrc(g, f2); lsdr += setrc - s1; setrc = s1;
+        if (losses) {
+            losses[iS].setrc = setrc;
+            losses[iS].lsdr += lsdr;
+            losses[iS].lscha += lscha;
+            losses[iS].lsatm += lsatm;
+        }
+        free_dp(dp);
+        free(charge);
+        free(atlos);
+    }
+    /* periodic copy F2(:,:,NT,:,:) = F2(:,:,1,:,:) and magnetopause mask */
+    for (int iS = 0; iS < ns; ++iS) {
+        double *f2 = f2s[iS];
+        for (int L = 1; L <= NPA; ++L)
+            for (int K = 1; K <= NE; ++K)
+                for (int I = 1; I <= NR; ++I) F2(I, NT, K, L) = F2(I, 1, K, L);
+        for (int I = 1; I <= NR; ++I)
+            for (int J = 1; J <= NT; ++J)
+                if (OUTSIDE(I, J) == 1)
+                    for (int L = 1; L <= NPA; ++L)
+                        for (int K = 1; K <= NE; ++K) F2(I, J, K, L) = 1.e-31;
+    }
+    double dn = 1e300;
+    for (int i = 0; i < ns * 4; ++i) dn = dmin(dn, dtr[i]);
+    if (ns == 0) dn = p->dtsmin;
+    if (dts_next) *dts_next = dmax(dn, p->dtsmin);
+    for (int iS = 0; iS < ns; ++iS) {
+        ro_anisch(g, &sp_all[iS], f2s[iS], ppert ? ppert[iS] : NULL, ppart ? ppart[iS] : NULL);
+        if (flux && flux[iS]) ro_flux(g, &sp_all[iS], f2s[iS], flux[iS]);
+    }
+    free(dtr);
+    free(vt);
+    (void)HMIN_UNUSED;
+    return 0;
+}

@@ -1,0 +1,142 @@
+/*
+ * ram_oracle.h -- CPU oracle for the RAM bounce-averaged kinetic step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the
+ * reference routines on the advection hot path, used as the checker for
+ * the CUDA path and as the timed CPU baseline.  Nothing in the product
+ * (the ramgpu library and its host package) links or calls it.
+ *
+ * Parity status: the reference is Fortran 90 and no Fortran compiler
+ * exists on either build machine, and the reference ships no per-routine
+ * golden vectors for these routines.  Parity of this restatement is
+ * therefore UNPINNED by the reference itself; it is pinned by
+ * known-answer tests (hand-computed limiter branches, exact conservation,
+ * identity at zero drift, periodicity, the DRIFTR stale-ghost case, the
+ * ANISCH L=1 side effect) and by an independent NumPy restatement of the
+ * charge-exchange and moment formulas.
+ *
+ * Layout: every array is Fortran column-major with the reference's
+ * dimensions, for ONE species (the reference's leading S index removed):
+ *   F2, CDrift*, CHARGE, FLUX : (NR, NT, NE, NPA)
+ *   FNHS, FNIS, BOUNHS, BOUNIS, HDNS, dIdt, dIbndt : (NR+1, NT, NPA)
+ *   BNES, dBdt, VT, EIR, EIP : (NR+1, NT)
+ *   outsideMGNP : int (NR, NT)
+ *   FGEOS : (NT, NE, NPA)      FFACTOR : (NR, NE, NPA)
+ *   ATLOS : (NR, NE)           PPERT, PPART : (NR, NT)
+ * Build: gcc -O2 -ffp-contract=off (the reference is compiled without FMA
+ * contraction, and every unsuffixed literal is double because RAM is built
+ * with -fdefault-real-8).
+ */
+#ifndef RAM_ORACLE_H
+#define RAM_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int nr, nt, ne, npa;
+    /* radial / azimuthal grid (src/ModRamInit.f90:392-421) */
+    const double *lz, *rlz;       /* NR+1 */
+    const double *phi;            /* NT */
+    double dl1, mdr, dphi, conf1, conf2;
+    /* energy grid (src/ModRamInit.f90:429-459) */
+    const double *ekev, *ebnd, *we, *de;    /* NE */
+    /* pitch-angle cosine grid (src/ModRamInit.f90:477-544) */
+    const double *mu, *dmu, *wmu;           /* NPA */
+    const double *upa;                      /* NR, real-valued as in the reference */
+    /* field tables (src/ModRamVariables.f90:31-37) */
+    const double *fnhs, *fnis, *bounhs, *bounis, *hdns, *didt, *dibndt;
+    const double *bnes, *dbdt, *eir, *eip;
+    const int *outside_mgnp;
+} ro_grid;
+
+typedef struct {
+    int qs;            /* species(S)%s_charge */
+    int cex_kind;      /* 0 none, 1 Hydrogen, 2 HeliumP1, 3 OxygenP1 */
+    double rmas;       /* rest mass [kg] */
+    const double *grel, *grbnd, *v;          /* NE */
+    const double *ffactor;                   /* (NR, NE, NPA) */
+    const double *epp, *ernh;                /* NE */
+} ro_species;
+
+typedef struct {
+    double betalim;    /* BetaLim (src/ModRamParams.f90:86) */
+    double fraccfl;    /* FracCFL (src/ModRamVariables.f90:100) */
+    double dts;        /* DTs */
+    double dtsmin;     /* DTsMin (src/ModRamTiming.f90:28) */
+    int closed;        /* 1: closed faces, conservation mode (new; not in the reference) */
+    int do_atmol;      /* 1: call ATMOL as ram_run does */
+} ro_params;
+
+/* Per-species drift parameters from DRIFTPARA (src/ModRamDrift.f90:36-88). */
+typedef struct {
+    double *vr, *p1;          /* NR */
+    double *p2, *edot;        /* (NR, NE) */
+    double *mudot;            /* (NR, NPA) */
+} ro_driftpara_t;
+
+/* Loss bookkeeping of one ram_run call (src/ModRamRun.f90:77-175). */
+typedef struct {
+    double setrc;               /* SETRC after the call */
+    double lsdr, lscha, lsatm;  /* ELORC accumulated into LSDR/LSCHA/LSATM */
+} ro_losses;
+
+/* VOLS potential, src/ModRamRun.f90:45-54.  vt: (NR+1, NT). */
+void ro_vt_vols(const ro_grid *g, double kp, double *vt);
+
+/* DRIFTPARA.  Arrays in dp are caller-allocated. */
+void ro_driftpara(const ro_grid *g, const ro_species *sp, const ro_params *p, ro_driftpara_t *dp);
+
+/* The four sweeps; each updates f2 in place, optionally stores the face
+ * coefficients in cdrift (NR,NT,NE,NPA; may be NULL) and returns DtDrift*. */
+double ro_driftr(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                 const ro_driftpara_t *dp, const double *vt, const double *fgeos,
+                 double *f2, double *cdrift);
+double ro_driftp(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                 const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift);
+double ro_drifte(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                 const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift);
+double ro_driftmu(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                  const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift);
+
+/* CEPARA analytic branches: charge (NR,NT,NE,NPA), atlos (NR,NE). */
+void ro_cepara(const ro_grid *g, const ro_species *sp, const ro_params *p,
+               double *charge, double *atlos);
+void ro_charexchange(const ro_grid *g, double *f2, const double *charge);
+void ro_atmol(const ro_grid *g, double *f2, const double *atlos);
+double ro_sumrc(const ro_grid *g, const double *f2);
+/* ANISCH moment block; modifies f2(:,:,K,1) for K=2..NE, I=2..NR. */
+void ro_anisch(const ro_grid *g, const ro_species *sp, double *f2, double *ppert, double *ppart);
+/* FLUX = F2/FFACTOR/FNHS (src/ModRamRun.f90:208-222); flux must be zeroed by the caller. */
+void ro_flux(const ro_grid *g, const ro_species *sp, const double *f2, double *flux);
+
+/* One ram_run call (src/ModRamRun.f90:16-225) for ns species.
+ *   kp        : Kp for the VOLS potential (ignored when vt_in != NULL)
+ *   vt_in     : optional precomputed potential (NR+1,NT)
+ *   vt_out    : optional, receives the potential used
+ *   fgeos[s]  : boundary (NT,NE,NPA) per species
+ *   f2[s]     : state (NR,NT,NE,NPA) per species, updated in place
+ *   ppert/ppart[s] : (NR,NT) per species, may be NULL
+ *   flux[s]   : (NR,NT,NE,NPA) per species, may be NULL
+ *   losses[s] : per species, may be NULL; setrc must hold the previous SETRC
+ *   dts_next  : DtsNext
+ *   nthreads  : OpenMP threads over species (the reference's parallel loop)
+ * Returns 0. */
+int ro_ram_run(const ro_grid *g, int ns, const ro_species *sp, const ro_params *p,
+               double kp, const double *vt_in, double *vt_out,
+               const double *const *fgeos, double *const *f2,
+               double *const *ppert, double *const *ppart, double *const *flux,
+               ro_losses *losses, double *dts_next, int nthreads);
+
+/* One DTs half of ram_run for one species (the measurement "step"):
+ * order 0 = R,P,E,MU,[CEX],[ATMOL]; order 1 = [ATMOL],[CEX],MU,E,P,R.
+ * charge/atlos from ro_cepara. */
+void ro_half_step(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                  const ro_driftpara_t *dp, const double *vt, const double *fgeos,
+                  const double *charge, const double *atlos, double *f2, int order);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,757 @@
+// abi.cu -- the extern "C" entry points declared in include/ramgpu.h.
+//
+// The context owns every device buffer.  ramgpu_ram_run enqueues, per call,
+//   member tables (VT, E x B, U terms)   2 kernels
+//   DRIFTR ghost planes + scan           2
+//   R, P, E, MU (+ fused CEX/ATMOL)      4   (forward half, CFL tracked)
+//   MU, E, P, R                          4   (reverse half)
+//   periodic copy + magnetopause mask    1
+//   ANISCH moments                       2
+// for all active (member, species) items in one launch each, mirroring the
+// species loop of src/ModRamRun.f90:64-222.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/ramgpu.h"
+#include "kernels.cuh"
+
+using namespace ramgpu;
+
+namespace {
+thread_local std::string g_create_error;
+constexpr int kSumrcBlocks = 64;
+constexpr int kSumrcStages = 7;
+}  // namespace
+
+struct ramgpu_ctx {
+  ramgpu_config cfg;
+  Dev d;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  std::vector<void*> allocs;
+  // host mirrors
+  std::vector<int> qs, cex;
+  std::vector<int> member_active;
+  std::vector<std::vector<int>> member_species;
+  std::vector<int2> items_h;
+  int2* items_d = nullptr;
+  bool items_dirty = true;
+  bool have_grid = false, have_fields = false;
+  bool field_dirty = true, static_dirty = true;
+  double tables_dts = -1.0;
+  int any_outside = 0;
+  double last_dts = 0.0;
+  // loss bookkeeping on the device: per slot {SETRC, LSDR, LSCHA, LSATM, valid}
+  double* losses = nullptr;
+  double* sumrc_part = nullptr;
+  double* upa_h_dummy = nullptr;
+  long long launches = 0;
+  // optional per-kernel-class timing
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_free;
+  struct Span { int kind; cudaEvent_t a, b; };
+  std::vector<Span> spans;
+};
+
+// ------------------------------------------------------------------ helpers
+static cudaEvent_t take_event(ramgpu_ctx* c) {
+  cudaEvent_t e = nullptr;
+  if (!c->ev_free.empty()) {
+    e = c->ev_free.back();
+    c->ev_free.pop_back();
+  } else {
+    cudaEventCreate(&e);
+  }
+  return e;
+}
+// Brackets a launch group with events when timing is enabled.
+struct Timed {
+  ramgpu_ctx* c;
+  int kind;
+  cudaEvent_t a = nullptr;
+  Timed(ramgpu_ctx* c_, int k) : c(c_), kind(k) {
+    if (c->timing) {
+      a = take_event(c);
+      cudaEventRecord(a, c->stream);
+    }
+  }
+  ~Timed() {
+    if (c->timing && a) {
+      cudaEvent_t b = take_event(c);
+      cudaEventRecord(b, c->stream);
+      c->spans.push_back({kind, a, b});
+    }
+  }
+};
+static int fail(ramgpu_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  else g_create_error = msg;
+  return code;
+}
+static int cuda_fail(ramgpu_ctx* c, cudaError_t e, const char* where) {
+  return fail(c, RAMGPU_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(call)                                                  \
+  do {                                                            \
+    cudaError_t e_ = (call);                                      \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);      \
+  } while (0)
+#define CKL(where)                                                \
+  do {                                                            \
+    cudaError_t e_ = cudaGetLastError();                          \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, where);      \
+  } while (0)
+
+template <class T>
+static T* dalloc(ramgpu_ctx* c, size_t n, bool* ok) {
+  void* p = nullptr;
+  if (n == 0) n = 1;
+  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
+    *ok = false;
+    return nullptr;
+  }
+  cudaMemset(p, 0, n * sizeof(T));
+  c->allocs.push_back(p);
+  return (T*)p;
+}
+
+static int check_ctx(ramgpu_ctx* ctx) { return ctx ? RAMGPU_OK : RAMGPU_ERR_ARG; }
+
+static int check_ms(ramgpu_ctx* ctx, int member, int s) {
+  if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, RAMGPU_ERR_ARG, "member out of range");
+  if (s < 0 || s >= ctx->cfg.ns) return fail(ctx, RAMGPU_ERR_ARG, "species out of range");
+  return RAMGPU_OK;
+}
+
+static int rebuild_items(ramgpu_ctx* ctx) {
+  ctx->items_h.clear();
+  for (int m = 0; m < ctx->cfg.n_members; ++m) {
+    if (!ctx->member_active[m]) continue;
+    for (int s : ctx->member_species[m]) ctx->items_h.push_back(make_int2(m, s));
+  }
+  if (!ctx->items_h.empty())
+    CK(cudaMemcpyAsync(ctx->items_d, ctx->items_h.data(), sizeof(int2) * ctx->items_h.size(),
+                       cudaMemcpyHostToDevice, ctx->stream));
+  ctx->d.items = ctx->items_d;
+  ctx->d.nitems = (int)ctx->items_h.size();
+  ctx->items_dirty = false;
+  return RAMGPU_OK;
+}
+
+static unsigned dev_flags(const ramgpu_ctx* ctx) {
+  return (ctx->cfg.flags & 7u) | (ctx->any_outside ? 0x80000000u : 0u);
+}
+
+// Bring every derived table up to date for step length dts.
+static int prepare(ramgpu_ctx* ctx, double dts) {
+  if (!ctx->have_grid || !ctx->have_fields)
+    return fail(ctx, RAMGPU_ERR_STATE, "ramgpu_set_grid and ramgpu_set_fields must be called first");
+  if (!(dts > 0.0) || !isfinite(dts)) return fail(ctx, RAMGPU_ERR_ARG, "dts must be positive and finite");
+  ctx->d.flags = dev_flags(ctx);
+  Timed tm_(ctx, 8);
+  if (ctx->field_dirty) {
+    launch_field_tables(ctx->d, ctx->stream);
+    ctx->launches += 1;
+    CKL("field tables");
+    ctx->field_dirty = false;
+    ctx->static_dirty = true;
+    ctx->tables_dts = -1.0;
+  }
+  if (ctx->static_dirty) {
+    launch_species_static(ctx->d, ctx->stream);
+    ctx->launches += 2;
+    CKL("species tables");
+    ctx->static_dirty = false;
+    ctx->tables_dts = -1.0;
+  }
+  if (ctx->tables_dts != dts) {
+    launch_dts_tables(ctx->d, dts, ctx->stream);
+    ctx->launches += 3;
+    CKL("dts tables");
+    ctx->tables_dts = dts;
+  }
+  if (ctx->items_dirty) {
+    int rc = rebuild_items(ctx);
+    if (rc) return rc;
+  }
+  return RAMGPU_OK;
+}
+
+// SUMRC of every item into stage buffer `stage`, then fold into the device
+// accumulators: which = -1 (set SETRC only), 1 LSDR, 2 LSCHA, 3 LSATM.
+__global__ void k_losses_fold(Dev d, const double* part, int nblk, double* losses, int which) {
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= d.nitems) return;
+  const int2 item = d.items[it];
+  const int slot = item.x * d.ns + item.y;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += part[(long long)it * nblk + b];
+  double* L = losses + (long long)slot * 5;
+  if (which >= 1 && L[4] != 0.0) L[which] += L[0] - s;  // ELORC = ENOLD - SETRC
+  L[0] = s;
+  L[4] = 1.0;
+}
+
+static int sumrc_stage(ramgpu_ctx* ctx, int stage, int which) {
+  double* part = ctx->sumrc_part + (size_t)stage * ctx->d.nm * ctx->d.ns * kSumrcBlocks;
+  Timed tm_(ctx, 9);
+  launch_sumrc(ctx->d, part, kSumrcBlocks, ctx->stream);
+  k_losses_fold<<<(ctx->d.nitems + 127) / 128, 128, 0, ctx->stream>>>(ctx->d, part, kSumrcBlocks,
+                                                                     ctx->losses, which);
+  ctx->launches += 2;
+  CKL("sumrc");
+  return RAMGPU_OK;
+}
+
+static int enqueue_forward(ramgpu_ctx* ctx, double dts, bool loss_fused, const double* loss_table) {
+  CK(cudaMemsetAsync(ctx->d.cflq, 0, sizeof(unsigned long long) * 4 * ctx->d.nm * ctx->d.ns, ctx->stream));
+  { Timed t(ctx, 2); launch_sweep_r(ctx->d, dts, true, ctx->stream); }
+  { Timed t(ctx, 3); launch_sweep_p(ctx->d, dts, true, ctx->stream); }
+  { Timed t(ctx, 4); launch_sweep_e(ctx->d, dts, true, ctx->stream); }
+  { Timed t(ctx, 5); launch_sweep_mu(ctx->d, dts, true, loss_fused ? 1 : 0, loss_table, ctx->stream); }
+  ctx->launches += 4;
+  CKL("forward sweeps");
+  return RAMGPU_OK;
+}
+
+static int enqueue_reverse(ramgpu_ctx* ctx, double dts, bool loss_fused, const double* loss_table) {
+  { Timed t(ctx, 5); launch_sweep_mu(ctx->d, dts, false, loss_fused ? 2 : 0, loss_table, ctx->stream); }
+  { Timed t(ctx, 4); launch_sweep_e(ctx->d, dts, false, ctx->stream); }
+  { Timed t(ctx, 3); launch_sweep_p(ctx->d, dts, false, ctx->stream); }
+  { Timed t(ctx, 2); launch_sweep_r(ctx->d, dts, false, ctx->stream); }
+  ctx->launches += 4;
+  CKL("reverse sweeps");
+  return RAMGPU_OK;
+}
+
+static int enqueue_ram_run(ramgpu_ctx* ctx, double dts) {
+  int rc = prepare(ctx, dts);
+  if (rc) return rc;
+  ctx->last_dts = dts;
+  if (ctx->d.nitems == 0) return RAMGPU_OK;
+  { Timed t(ctx, 0); launch_member_coef(ctx->d, dts, ctx->stream); }
+  { Timed t(ctx, 1); launch_ghost(ctx->d, ctx->stream); }
+  ctx->launches += 4;
+  CKL("member tables");
+  const bool losses = ctx->cfg.flags & RAMGPU_FLAG_LOSSES;
+  if (!losses) {
+    // R,P,E,MU then CEX,ATMOL,ATMOL,CEX folded into the MU store
+    if ((rc = enqueue_forward(ctx, dts, true, ctx->d.loss2))) return rc;
+    if ((rc = enqueue_reverse(ctx, dts, false, nullptr))) return rc;
+  } else {
+    if ((rc = enqueue_forward(ctx, dts, false, nullptr))) return rc;
+    if ((rc = sumrc_stage(ctx, 0, 1))) return rc;
+    { Timed t(ctx, 9); launch_loss_apply(ctx->d, ctx->d.charge, ctx->stream); }
+    if ((rc = sumrc_stage(ctx, 1, 2))) return rc;
+    { Timed t(ctx, 9); launch_loss_apply(ctx->d, ctx->d.atm, ctx->stream); }
+    if ((rc = sumrc_stage(ctx, 2, 3))) return rc;
+    { Timed t(ctx, 9); launch_loss_apply(ctx->d, ctx->d.atm, ctx->stream); }
+    if ((rc = sumrc_stage(ctx, 3, 3))) return rc;
+    { Timed t(ctx, 9); launch_loss_apply(ctx->d, ctx->d.charge, ctx->stream); }
+    if ((rc = sumrc_stage(ctx, 4, 2))) return rc;
+    ctx->launches += 4;
+    if ((rc = enqueue_reverse(ctx, dts, false, nullptr))) return rc;
+    if ((rc = sumrc_stage(ctx, 5, 1))) return rc;
+  }
+  { Timed t(ctx, 6); launch_finish(ctx->d, ctx->stream); }
+  { Timed t(ctx, 7); launch_moments(ctx->d, ctx->stream); }
+  ctx->launches += 3;
+  CKL("finish/moments");
+  return RAMGPU_OK;
+}
+
+// =================================================================== ABI
+extern "C" {
+
+int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
+  if (!cfg || !out) return fail(nullptr, RAMGPU_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (cfg->nr < 4 || cfg->nt < 5 || cfg->ne < 31 || cfg->npa < 5 || cfg->ns < 1 || cfg->n_members < 1)
+    return fail(nullptr, RAMGPU_ERR_ARG,
+                "grid too small: need NR>=4, NT>=5, NE>=31 (ANISCH bands), NPA>=5, NS>=1, members>=1");
+  const long long ncell = (long long)cfg->nr * cfg->nt * cfg->ne * cfg->npa;
+  if (ncell > (1LL << 40)) return fail(nullptr, RAMGPU_ERR_ARG, "grid too large");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+    return fail(nullptr, RAMGPU_ERR_CUDA, "no CUDA device");
+  ramgpu_ctx* ctx = new ramgpu_ctx();
+  ctx->cfg = *cfg;
+  ctx->cfg.betalim = cfg->betalim > 2.0 ? 2.0 : (cfg->betalim < 1.0 ? 1.0 : cfg->betalim);
+  Dev& d = ctx->d;
+  memset(&d, 0, sizeof(d));
+  d.nr = cfg->nr; d.nt = cfg->nt; d.ne = cfg->ne; d.npa = cfg->npa;
+  d.ns = cfg->ns; d.nm = cfg->n_members; d.ncell = ncell; d.nf = cfg->nr + 1;
+  d.betalim = ctx->cfg.betalim;
+  const size_t nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa, ns = d.ns, nm = d.nm, nf = d.nf;
+  const size_t nijl = nr * nt * npa, nfield = nf * nt * npa, nslot = nm * ns;
+  bool ok = true;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) ok = false;
+  ctx->own_stream = ok;
+  d.lz = dalloc<double>(ctx, nf, &ok); d.rlz = dalloc<double>(ctx, nf, &ok);
+  d.phi = dalloc<double>(ctx, nt, &ok);
+  d.ekev = dalloc<double>(ctx, ne, &ok); d.ebnd = dalloc<double>(ctx, ne, &ok);
+  d.we = dalloc<double>(ctx, ne, &ok); d.de = dalloc<double>(ctx, ne, &ok);
+  d.mu = dalloc<double>(ctx, npa, &ok); d.dmu = dalloc<double>(ctx, npa, &ok);
+  d.wmu = dalloc<double>(ctx, npa, &ok);
+  d.upa_atm = dalloc<int>(ctx, nr, &ok); d.upa_mom = dalloc<int>(ctx, nr, &ok);
+  d.mhde = dalloc<double>(ctx, ne, &ok); d.iwe = dalloc<double>(ctx, ne, &ok);
+  d.ide = dalloc<double>(ctx, ne, &ok);
+  d.mhdmu = dalloc<double>(ctx, npa, &ok); d.iwmu = dalloc<double>(ctx, npa, &ok);
+  d.idmu = dalloc<double>(ctx, npa, &ok);
+  d.grel = dalloc<double>(ctx, ns * ne, &ok); d.grbnd = dalloc<double>(ctx, ns * ne, &ok);
+  d.vel = dalloc<double>(ctx, ns * ne, &ok); d.epp = dalloc<double>(ctx, ns * ne, &ok);
+  d.rmas = dalloc<double>(ctx, ns, &ok);
+  d.qs = dalloc<int>(ctx, ns, &ok); d.cex_kind = dalloc<int>(ctx, ns, &ok);
+  d.ffactor = dalloc<double>(ctx, ns * nr * ne * npa, &ok);
+  d.fnhs = dalloc<double>(ctx, nfield, &ok); d.fnis = dalloc<double>(ctx, nfield, &ok);
+  d.bounhs = dalloc<double>(ctx, nfield, &ok); d.bounis = dalloc<double>(ctx, nfield, &ok);
+  d.hdns = dalloc<double>(ctx, nfield, &ok); d.didt = dalloc<double>(ctx, nfield, &ok);
+  d.dibndt = dalloc<double>(ctx, nfield, &ok);
+  d.bnes = dalloc<double>(ctx, nf * nt, &ok); d.dbdt = dalloc<double>(ctx, nf * nt, &ok);
+  d.eir = dalloc<double>(ctx, nf * nt, &ok); d.eip = dalloc<double>(ctx, nf * nt, &ok);
+  d.outside = dalloc<int>(ctx, nr * nt, &ok);
+  d.grt = dalloc<double>(ctx, nijl, &ok); d.gpt = dalloc<double>(ctx, nijl, &ok);
+  d.gre = dalloc<double>(ctx, nijl, &ok); d.gpe = dalloc<double>(ctx, nijl, &ok);
+  d.ze = dalloc<double>(ctx, nijl, &ok); d.wet = dalloc<double>(ctx, nijl, &ok);
+  d.gmr = dalloc<double>(ctx, nijl, &ok); d.gmp = dalloc<double>(ctx, nijl, &ok);
+  d.zm = dalloc<double>(ctx, nijl, &ok); d.hm = dalloc<double>(ctx, nijl, &ok);
+  d.cmu0 = dalloc<double>(ctx, nijl, &ok); d.wm = dalloc<double>(ctx, nijl, &ok);
+  d.cmudot = dalloc<double>(ctx, nijl, &ok);
+  d.rho = dalloc<double>(ctx, nr * nt, &ok);
+  d.epme = dalloc<double>(ctx, ns * ncell, &ok); d.epma = dalloc<double>(ctx, ns * ncell, &ok);
+  d.p4 = dalloc<double>(ctx, ns * ne, &ok);
+  d.p2 = dalloc<double>(ctx, ns * ne * nr, &ok); d.edot = dalloc<double>(ctx, ns * ne * nr, &ok);
+  d.eb = dalloc<double>(ctx, ns * ne, &ok); d.ek = dalloc<double>(ctx, ns * ne, &ok);
+  d.kap = dalloc<double>(ctx, ns * 2, &ok);
+  d.loss1 = dalloc<double>(ctx, ns * ncell, &ok); d.loss2 = dalloc<double>(ctx, ns * ncell, &ok);
+  d.charge = dalloc<double>(ctx, ns * ncell, &ok); d.atm = dalloc<double>(ctx, ns * ncell, &ok);
+  d.kp = dalloc<double>(ctx, nm, &ok); d.vt_mode = dalloc<int>(ctx, nm, &ok);
+  d.vt = dalloc<double>(ctx, nm * nf * nt, &ok);
+  d.cr = dalloc<double>(ctx, nm * nr * nt, &ok); d.ca = dalloc<double>(ctx, nm * nr * nt, &ok);
+  d.ue = dalloc<double>(ctx, nm * nijl, &ok); d.um = dalloc<double>(ctx, nm * nijl, &ok);
+  d.f2 = dalloc<double>(ctx, nslot * ncell, &ok);
+  d.fgeos = dalloc<double>(ctx, nslot * nt * ne * npa, &ok);
+  d.plane_last = dalloc<double>(ctx, nslot * ne * npa, &ok);
+  d.plane_has = dalloc<int>(ctx, nslot * ne * npa, &ok);
+  d.plane_carry = dalloc<double>(ctx, nslot * ne * npa, &ok);
+  d.cflq = dalloc<unsigned long long>(ctx, nslot * 4, &ok);
+  d.mom_part = dalloc<double>(ctx, nslot * nr * nt * ne * 2, &ok);
+  d.ppert = dalloc<double>(ctx, nslot * nr * nt, &ok);
+  d.ppart = dalloc<double>(ctx, nslot * nr * nt, &ok);
+  ctx->items_d = dalloc<int2>(ctx, nslot, &ok);
+  ctx->losses = dalloc<double>(ctx, nslot * 5, &ok);
+  ctx->sumrc_part = dalloc<double>(ctx, (size_t)kSumrcStages * nslot * kSumrcBlocks, &ok);
+  if (!ok) {
+    ramgpu_destroy(ctx);
+    return fail(nullptr, RAMGPU_ERR_NOMEM, "device allocation failed");
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    ramgpu_destroy(ctx);
+    return fail(nullptr, RAMGPU_ERR_CUDA, "device initialisation failed");
+  }
+  ctx->qs.assign(ns, 1);
+  ctx->cex.assign(ns, 0);
+  ctx->member_active.assign(nm, 1);
+  ctx->member_species.assign(nm, std::vector<int>());
+  for (size_t m = 0; m < nm; ++m)
+    for (size_t s = 0; s < ns; ++s) ctx->member_species[m].push_back((int)s);
+  std::vector<int> one(ns, 1);
+  cudaMemcpy((void*)d.qs, one.data(), sizeof(int) * ns, cudaMemcpyHostToDevice);
+  *out = ctx;
+  return RAMGPU_OK;
+}
+
+int ramgpu_destroy(ramgpu_ctx* ctx) {
+  if (!ctx) return RAMGPU_ERR_ARG;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (void* p : ctx->allocs) cudaFree(p);
+  for (auto& sp : ctx->spans) { cudaEventDestroy(sp.a); cudaEventDestroy(sp.b); }
+  for (cudaEvent_t e : ctx->ev_free) cudaEventDestroy(e);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return RAMGPU_OK;
+}
+
+int ramgpu_last_error(const ramgpu_ctx* ctx, char* buf, size_t len) {
+  if (!buf || len == 0) return RAMGPU_ERR_ARG;
+  const std::string& e = ctx ? ctx->err : g_create_error;
+  snprintf(buf, len, "%s", e.c_str());
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_stream(ramgpu_ctx* ctx, void* stream) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (stream) {
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    ctx->own_stream = false;
+    ctx->stream = (cudaStream_t)stream;
+  }
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_species(ramgpu_ctx* ctx, int s, int charge, int cex_kind) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (s < 0 || s >= ctx->cfg.ns) return fail(ctx, RAMGPU_ERR_ARG, "species out of range");
+  if (charge == 0) return fail(ctx, RAMGPU_ERR_ARG, "species charge must be nonzero");
+  if (cex_kind < 0 || cex_kind > 3) return fail(ctx, RAMGPU_ERR_ARG, "unknown cex_kind");
+  ctx->qs[s] = charge;
+  ctx->cex[s] = cex_kind;
+  CK(cudaMemcpy((void*)ctx->d.qs, ctx->qs.data(), sizeof(int) * ctx->cfg.ns, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy((void*)ctx->d.cex_kind, ctx->cex.data(), sizeof(int) * ctx->cfg.ns, cudaMemcpyHostToDevice));
+  ctx->static_dirty = true;
+  ctx->tables_dts = -1.0;
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_grid(ramgpu_ctx* ctx, const ramgpu_grid* g) {
+  if (check_ctx(ctx) || !g) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  const ramgpu_grid& G = *g;
+  if (!G.lz || !G.rlz || !G.phi || !G.ekev || !G.ebnd || !G.we || !G.de || !G.mu || !G.dmu ||
+      !G.wmu || !G.upa || !G.rmas || !G.grel || !G.grbnd || !G.v || !G.epp || !G.ffactor)
+    return fail(ctx, RAMGPU_ERR_ARG, "ramgpu_grid has a null array");
+  Dev& d = ctx->d;
+  const int nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa, ns = d.ns;
+  d.dl1 = G.dl1; d.mdr = G.mdr; d.dphi = G.dphi; d.conf1 = G.conf1; d.conf2 = G.conf2;
+  auto up = [&](const double* dst, const double* src, size_t n) {
+    return cudaMemcpy((void*)dst, src, n * sizeof(double), cudaMemcpyHostToDevice);
+  };
+  CK(up(d.lz, G.lz, nr + 1)); CK(up(d.rlz, G.rlz, nr + 1)); CK(up(d.phi, G.phi, nt));
+  CK(up(d.ekev, G.ekev, ne)); CK(up(d.ebnd, G.ebnd, ne)); CK(up(d.we, G.we, ne)); CK(up(d.de, G.de, ne));
+  CK(up(d.mu, G.mu, npa)); CK(up(d.dmu, G.dmu, npa)); CK(up(d.wmu, G.wmu, npa));
+  CK(up(d.rmas, G.rmas, ns));
+  std::vector<int> ua(nr), um(nr);
+  for (int i = 0; i < nr; ++i) {
+    ua[i] = (int)G.upa[i];          // int(UPA(I)) in ATMOL
+    um[i] = (int)(G.upa[i] - 1);    // int(UPA(I)-1) in ANISCH
+    if (ua[i] < 2 || ua[i] > npa + 1) return fail(ctx, RAMGPU_ERR_ARG, "UPA out of range");
+  }
+  CK(cudaMemcpy((void*)d.upa_atm, ua.data(), sizeof(int) * nr, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy((void*)d.upa_mom, um.data(), sizeof(int) * nr, cudaMemcpyHostToDevice));
+  std::vector<double> r1(ne), r2(ne), r3(ne), q1(npa), q2(npa), q3(npa);
+  for (int k = 0; k < ne; ++k) { r1[k] = -0.5 / G.de[k]; r2[k] = 1.0 / G.we[k]; r3[k] = 1.0 / G.de[k]; }
+  for (int l = 0; l < npa; ++l) { q1[l] = -0.5 / G.dmu[l]; q2[l] = 1.0 / G.wmu[l]; q3[l] = 1.0 / G.dmu[l]; }
+  CK(up(d.mhde, r1.data(), ne)); CK(up(d.iwe, r2.data(), ne)); CK(up(d.ide, r3.data(), ne));
+  CK(up(d.mhdmu, q1.data(), npa)); CK(up(d.iwmu, q2.data(), npa)); CK(up(d.idmu, q3.data(), npa));
+  // (NS,NE) Fortran -> [s][k]
+  std::vector<double> t(ns * ne);
+  auto tr2 = [&](const double* dst, const double* src) {
+    for (int s = 0; s < ns; ++s)
+      for (int k = 0; k < ne; ++k) t[s * ne + k] = src[(size_t)k * ns + s];
+    return up(dst, t.data(), (size_t)ns * ne);
+  };
+  CK(tr2(d.grel, G.grel)); CK(tr2(d.grbnd, G.grbnd)); CK(tr2(d.vel, G.v)); CK(tr2(d.epp, G.epp));
+  // FFACTOR(NS,NR,NE,NPA) -> [s][(L*NE+K)*NR+I]
+  const size_t per = (size_t)nr * ne * npa;
+  std::vector<double> ff(ns * per);
+  for (size_t c = 0; c < per; ++c)
+    for (int s = 0; s < ns; ++s) ff[(size_t)s * per + c] = G.ffactor[c * ns + s];
+  CK(up(d.ffactor, ff.data(), ns * per));
+  ctx->have_grid = true;
+  ctx->field_dirty = true;
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_fields(ramgpu_ctx* ctx, const double* fnhs, const double* fnis, const double* bounhs,
+                      const double* bounis, const double* hdns, const double* didt,
+                      const double* dibndt, const double* bnes, const double* dbdt,
+                      const double* eir, const double* eip, const int* outside_mgnp) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (!fnhs || !fnis || !bounhs || !bounis || !hdns || !didt || !dibndt || !bnes || !dbdt || !eir ||
+      !eip || !outside_mgnp)
+    return fail(ctx, RAMGPU_ERR_ARG, "null field array");
+  Dev& d = ctx->d;
+  const size_t nfield = (size_t)d.nf * d.nt * d.npa, n2 = (size_t)d.nf * d.nt;
+  auto up = [&](const double* dst, const double* src, size_t n) {
+    return cudaMemcpy((void*)dst, src, n * sizeof(double), cudaMemcpyHostToDevice);
+  };
+  CK(up(d.fnhs, fnhs, nfield)); CK(up(d.fnis, fnis, nfield)); CK(up(d.bounhs, bounhs, nfield));
+  CK(up(d.bounis, bounis, nfield)); CK(up(d.hdns, hdns, nfield)); CK(up(d.didt, didt, nfield));
+  CK(up(d.dibndt, dibndt, nfield));
+  CK(up(d.bnes, bnes, n2)); CK(up(d.dbdt, dbdt, n2)); CK(up(d.eir, eir, n2)); CK(up(d.eip, eip, n2));
+  CK(cudaMemcpy((void*)d.outside, outside_mgnp, sizeof(int) * d.nr * d.nt, cudaMemcpyHostToDevice));
+  ctx->any_outside = 0;
+  for (int i = 0; i < d.nr * d.nt; ++i)
+    if (outside_mgnp[i] == 1) ctx->any_outside = 1;
+  ctx->have_fields = true;
+  ctx->field_dirty = true;
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_boundary(ramgpu_ctx* ctx, int member, int s, const double* fgeos_s) {
+  if (check_ctx(ctx) || !fgeos_s) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  const size_t n = (size_t)ctx->d.nt * ctx->d.ne * ctx->d.npa;
+  int m0 = member, m1 = member + 1;
+  if (member < 0) { m0 = 0; m1 = ctx->cfg.n_members; }
+  for (int m = m0; m < m1; ++m) {
+    if (int rc = check_ms(ctx, m, s)) return rc;
+    CK(cudaMemcpy(ctx->d.fgeos + (size_t)(m * ctx->d.ns + s) * n, fgeos_s, n * sizeof(double),
+                  cudaMemcpyHostToDevice));
+  }
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_potential(ramgpu_ctx* ctx, int member, const double* vt) {
+  if (check_ctx(ctx) || !vt) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (int rc = check_ms(ctx, member, 0)) return rc;
+  const size_t n = (size_t)ctx->d.nf * ctx->d.nt;
+  CK(cudaMemcpy(ctx->d.vt + (size_t)member * n, vt, n * sizeof(double), cudaMemcpyHostToDevice));
+  int zero = 0;
+  CK(cudaMemcpy(ctx->d.vt_mode + member, &zero, sizeof(int), cudaMemcpyHostToDevice));
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_kp(ramgpu_ctx* ctx, int member, double kp) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (!isfinite(kp)) return fail(ctx, RAMGPU_ERR_ARG, "kp must be finite");
+  int m0 = member, m1 = member + 1;
+  if (member < 0) { m0 = 0; m1 = ctx->cfg.n_members; }
+  for (int m = m0; m < m1; ++m) {
+    if (int rc = check_ms(ctx, m, 0)) return rc;
+    int one = 1;
+    CK(cudaMemcpyAsync(ctx->d.kp + m, &kp, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d.vt_mode + m, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_member_species(ramgpu_ctx* ctx, int member, int n, const int* list) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (int rc = check_ms(ctx, member, 0)) return rc;
+  if (n < 0 || n > ctx->cfg.ns || (n > 0 && !list)) return fail(ctx, RAMGPU_ERR_ARG, "bad species list");
+  std::vector<int> v;
+  for (int i = 0; i < n; ++i) {
+    if (list[i] < 0 || list[i] >= ctx->cfg.ns) return fail(ctx, RAMGPU_ERR_ARG, "species out of range");
+    for (int x : v)
+      if (x == list[i]) return fail(ctx, RAMGPU_ERR_ARG, "duplicate species in list");
+    v.push_back(list[i]);
+  }
+  ctx->member_species[member] = v;
+  ctx->items_dirty = true;
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_member_active(ramgpu_ctx* ctx, int member, int active) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (int rc = check_ms(ctx, member, 0)) return rc;
+  ctx->member_active[member] = active ? 1 : 0;
+  ctx->items_dirty = true;
+  return RAMGPU_OK;
+}
+
+int ramgpu_upload_f2(ramgpu_ctx* ctx, int member, int s, const double* f2_s) {
+  if (check_ctx(ctx) || !f2_s) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (int rc = check_ms(ctx, member, s)) return rc;
+  const size_t n = ctx->d.ncell;
+  CK(cudaMemcpyAsync(ctx->d.f2 + (size_t)(member * ctx->d.ns + s) * n, f2_s, n * sizeof(double),
+                     cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return RAMGPU_OK;
+}
+
+int ramgpu_download_f2(ramgpu_ctx* ctx, int member, int s, double* f2_s) {
+  if (check_ctx(ctx) || !f2_s) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (int rc = check_ms(ctx, member, s)) return rc;
+  const size_t n = ctx->d.ncell;
+  CK(cudaMemcpyAsync(f2_s, ctx->d.f2 + (size_t)(member * ctx->d.ns + s) * n, n * sizeof(double),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return RAMGPU_OK;
+}
+
+int ramgpu_upload_f2_all(ramgpu_ctx* ctx, int member, const double* f2) {
+  if (check_ctx(ctx) || !f2) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  const int ns = ctx->d.ns;
+  const size_t n = ctx->d.ncell;
+  std::vector<double> t(n);
+  for (int s = 0; s < ns; ++s) {
+    for (size_t c = 0; c < n; ++c) t[c] = f2[c * ns + s];
+    if (int rc = ramgpu_upload_f2(ctx, member, s, t.data())) return rc;
+  }
+  return RAMGPU_OK;
+}
+
+int ramgpu_download_f2_all(ramgpu_ctx* ctx, int member, double* f2) {
+  if (check_ctx(ctx) || !f2) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  const int ns = ctx->d.ns;
+  const size_t n = ctx->d.ncell;
+  std::vector<double> t(n);
+  for (int s = 0; s < ns; ++s) {
+    if (int rc = ramgpu_download_f2(ctx, member, s, t.data())) return rc;
+    for (size_t c = 0; c < n; ++c) f2[c * ns + s] = t[c];
+  }
+  return RAMGPU_OK;
+}
+
+int ramgpu_f2_device_ptr(ramgpu_ctx* ctx, int member, int s, double** dptr) {
+  if (check_ctx(ctx) || !dptr) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (int rc = check_ms(ctx, member, s)) return rc;
+  *dptr = ctx->d.f2 + (size_t)(member * ctx->d.ns + s) * ctx->d.ncell;
+  return RAMGPU_OK;
+}
+
+int ramgpu_ram_run_async(ramgpu_ctx* ctx, double dts) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  return enqueue_ram_run(ctx, dts);
+}
+
+int ramgpu_ram_run(ramgpu_ctx* ctx, double dts) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  int rc = enqueue_ram_run(ctx, dts);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return RAMGPU_OK;
+}
+
+int ramgpu_half_step(ramgpu_ctx* ctx, double dts, int order) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (order != 0 && order != 1) return fail(ctx, RAMGPU_ERR_ARG, "order must be 0 or 1");
+  int rc = prepare(ctx, dts);
+  if (rc) return rc;
+  ctx->last_dts = dts;
+  if (ctx->d.nitems == 0) return RAMGPU_OK;
+  launch_member_coef(ctx->d, dts, ctx->stream);
+  launch_ghost(ctx->d, ctx->stream);
+  ctx->launches += 4;
+  CKL("member tables");
+  if (order == 0) rc = enqueue_forward(ctx, dts, true, ctx->d.loss1);
+  else rc = enqueue_reverse(ctx, dts, true, ctx->d.loss1);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return RAMGPU_OK;
+}
+
+int ramgpu_apply_op(ramgpu_ctx* ctx, double dts, int op, int cfl) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (op < 0 || op > 6) return fail(ctx, RAMGPU_ERR_ARG, "unknown op");
+  int rc = prepare(ctx, dts);
+  if (rc) return rc;
+  ctx->last_dts = dts;
+  if (ctx->d.nitems == 0) return RAMGPU_OK;
+  launch_member_coef(ctx->d, dts, ctx->stream);
+  launch_ghost(ctx->d, ctx->stream);
+  ctx->launches += 4;
+  if (cfl) CK(cudaMemsetAsync(ctx->d.cflq, 0, sizeof(unsigned long long) * 4 * ctx->d.nm * ctx->d.ns, ctx->stream));
+  switch (op) {
+    case 0: launch_sweep_r(ctx->d, dts, cfl != 0, ctx->stream); break;
+    case 1: launch_sweep_p(ctx->d, dts, cfl != 0, ctx->stream); break;
+    case 2: launch_sweep_e(ctx->d, dts, cfl != 0, ctx->stream); break;
+    case 3: launch_sweep_mu(ctx->d, dts, cfl != 0, 0, nullptr, ctx->stream); break;
+    case 4: launch_loss_apply(ctx->d, ctx->d.charge, ctx->stream); break;
+    case 5: launch_loss_apply(ctx->d, ctx->d.atm, ctx->stream); break;
+    case 6: launch_moments(ctx->d, ctx->stream); ctx->launches += 1; break;
+  }
+  ctx->launches += 1;
+  CKL("apply_op");
+  CK(cudaStreamSynchronize(ctx->stream));
+  return RAMGPU_OK;
+}
+
+int ramgpu_moments(ramgpu_ctx* ctx, int member, int s, double* ppert, double* ppart) {
+  if (check_ctx(ctx) || !ppert || !ppart) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (int rc = check_ms(ctx, member, s)) return rc;
+  const size_t n = (size_t)ctx->d.nr * ctx->d.nt, o = (size_t)(member * ctx->d.ns + s) * n;
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(ppert, ctx->d.ppert + o, n * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(ppart, ctx->d.ppart + o, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return RAMGPU_OK;
+}
+
+int ramgpu_flux(ramgpu_ctx* ctx, int member, int s, double* flux_s) {
+  if (check_ctx(ctx) || !flux_s) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (int rc = check_ms(ctx, member, s)) return rc;
+  if (!ctx->have_grid || !ctx->have_fields) return fail(ctx, RAMGPU_ERR_STATE, "grid/fields not set");
+  const size_t n = ctx->d.ncell;
+  // The moment-partial buffer of this slot is reused as staging only when
+  // large enough; otherwise a temporary device buffer is used.
+  double* tmp = nullptr;
+  CK(cudaMalloc(&tmp, n * sizeof(double)));
+  launch_flux(ctx->d, member * ctx->d.ns + s, s, tmp, ctx->stream);
+  ctx->launches += 1;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(flux_s, tmp, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "flux");
+  return RAMGPU_OK;
+}
+
+int ramgpu_cfl(ramgpu_ctx* ctx, int member, int s, double* out5) {
+  if (check_ctx(ctx) || !out5) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (int rc = check_ms(ctx, member, s)) return rc;
+  const int ns = ctx->d.ns;
+  std::vector<unsigned long long> q(4 * ns);
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(q.data(), ctx->d.cflq + (size_t)member * ns * 4, sizeof(unsigned long long) * 4 * ns,
+                cudaMemcpyDeviceToHost));
+  const double fr = ctx->cfg.fraccfl * ctx->last_dts;
+  const double init[4] = {100000.0, 100000.0, 10000.0, 10000.0};
+  // smallest 1/DMU(NPA) floor term of DRIFTMU's L = NPA face (CDriftMu = 0 there)
+  double dmu_n = 0.0;
+  CK(cudaMemcpy(&dmu_n, ctx->d.dmu + ctx->d.npa - 1, sizeof(double), cudaMemcpyDeviceToHost));
+  double dtsnext = 1e300;
+  for (int sp : ctx->member_species[member]) {
+    for (int w = 0; w < 4; ++w) {
+      double qq;
+      unsigned long long b = q[sp * 4 + w];
+      memcpy(&qq, &b, sizeof(double));
+      if (w == 3 && b != 0ULL) qq = fmax(qq, 1E-32 / dmu_n);
+      double dt = b ? fmin(init[w], fr / qq) : init[w];
+      if (sp == s) out5[w] = dt;
+      dtsnext = fmin(dtsnext, dt);
+    }
+  }
+  if (ctx->member_species[member].empty()) dtsnext = ctx->cfg.dtsmin;
+  out5[4] = fmax(dtsnext, ctx->cfg.dtsmin);
+  return RAMGPU_OK;
+}
+
+int ramgpu_losses(ramgpu_ctx* ctx, int member, int s, double* out4) {
+  if (check_ctx(ctx) || !out4) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (int rc = check_ms(ctx, member, s)) return rc;
+  double v[5];
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(v, ctx->losses + (size_t)(member * ctx->d.ns + s) * 5, sizeof(v), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 4; ++i) out4[i] = v[i];
+  return RAMGPU_OK;
+}
+
+int ramgpu_reset_losses(ramgpu_ctx* ctx) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  CK(cudaMemsetAsync(ctx->losses, 0, sizeof(double) * 5 * ctx->d.nm * ctx->d.ns, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return RAMGPU_OK;
+}
+
+long long ramgpu_launch_count(const ramgpu_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int ramgpu_set_timing(ramgpu_ctx* ctx, int enable) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  ctx->timing = enable != 0;
+  return RAMGPU_OK;
+}
+
+int ramgpu_kernel_times(ramgpu_ctx* ctx, double* ms, long long* counts) {
+  if (check_ctx(ctx) || !ms || !counts) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (auto& sp : ctx->spans) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, sp.a, sp.b) == cudaSuccess && sp.kind >= 0 && sp.kind < RAMGPU_NKCLASS) {
+      ms[sp.kind] += t;
+      counts[sp.kind] += 1;
+    }
+    ctx->ev_free.push_back(sp.a);
+    ctx->ev_free.push_back(sp.b);
+  }
+  ctx->spans.clear();
+  return RAMGPU_OK;
+}
+
+}  // extern "C"

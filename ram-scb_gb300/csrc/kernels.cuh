@@ -1,0 +1,51 @@
+// kernels.cuh -- launchers shared between the kernel files and the C ABI.
+#pragma once
+#include "ramgpu_internal.cuh"
+
+namespace ramgpu {
+
+// DRIFTR boundary ghost F(NR+n) = FGEOS(S,J,K,L)*CONFn*FNHS(NR,J,L), or 0 outside
+// the magnetopause (src/ModRamDrift.f90:161-167).  0-based j,k,l.
+__device__ __forceinline__ double ghost_value(const Dev& d, int slot, int j, int k, int l,
+                                              double conf) {
+  const int nr = d.nr;
+  if (d.outside[(long long)j * nr + nr - 1] == 1) return 0.0;
+  const double fg = d.fgeos[(long long)slot * d.nt * d.ne * d.npa + ((long long)l * d.ne + k) * d.nt + j];
+  return fg * conf * d.fnhs[((long long)l * d.nt + j) * d.nf + nr - 1];
+}
+
+// Sign test of CDriftR(NR,J,K,L) exactly as the sweep computes it.
+__device__ __forceinline__ bool inflow_line(const Dev& d, int m, int j, int l, double p4) {
+  const int nr = d.nr;
+  const double c = fma(d.grt[((long long)l * d.nt + j) * nr + nr - 1], p4,
+                       d.cr[((long long)m * d.nt + j) * nr + nr - 1]);
+  return is_neg(c);
+}
+
+// Stale F(NR+1) seen by outflow line (J,K,L): the value written by the most
+// recent inflow line before it in the K->L->J order of DRIFTR, 0 if none.
+__device__ __forceinline__ double stale_ghost(const Dev& d, int m, int slot, int j, int k, int l,
+                                              double p4) {
+  for (int jj = j - 1; jj >= 0; --jj)
+    if (inflow_line(d, m, jj, l, p4)) return ghost_value(d, slot, jj, k, l, d.conf1);
+  return d.plane_carry[(long long)slot * d.ne * d.npa + (long long)k * d.npa + l];
+}
+
+void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st);
+void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st);
+void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st);
+void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
+                     cudaStream_t st);
+
+void launch_field_tables(const Dev& d, cudaStream_t st);
+void launch_species_static(const Dev& d, cudaStream_t st);
+void launch_dts_tables(const Dev& d, double dts, cudaStream_t st);
+void launch_member_coef(const Dev& d, double dts, cudaStream_t st);
+void launch_ghost(const Dev& d, cudaStream_t st);
+void launch_loss_apply(const Dev& d, const double* table, cudaStream_t st);
+void launch_finish(const Dev& d, cudaStream_t st);
+void launch_moments(const Dev& d, cudaStream_t st);
+void launch_sumrc(const Dev& d, double* part, int nblk, cudaStream_t st);
+void launch_flux(const Dev& d, int slot, int s, double* out, cudaStream_t st);
+
+}  // namespace ramgpu

@@ -1,0 +1,148 @@
+// ramgpu_internal.cuh -- device-side state and shared helpers of the GB300
+// RAM kinetic step.
+//
+// Data layout in HBM (all FP64, Fortran order inside one species):
+//   f2      [member][species][L][K][J][I]   (= F2(S,I,J,K,L) of the reference
+//                                            with S hoisted out; I fastest)
+//   fields  [L][J][I'] with I' = 1..NR+1     (FNHS etc., src/ModRamVariables.f90:31-37)
+//   per-member tables (VT-dependent) [member][L][J][I]
+//   per-species tables (DTs-dependent) [species][...]
+// One thread advances one line of a sweep; the line is streamed through a
+// rolling register window, so no line buffer is kept.
+//
+// Cost model: on GB300 the FP64 add/mul/fma pipe issues ~0.5 T lane-ops/s
+// while FP64 min/max, integer and FP32 pipes are 16-70x faster, so every
+// sign test, threshold test and select is done on the integer bit pattern
+// and the limiter uses fmin/fmax, leaving 8-9 FP64 add/mul/fma per face.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ramgpu {
+
+constexpr double kOME = 7.3E-5;        // Earth's angular velocity, src/ModRamDrift.f90:224
+constexpr double kRE = 6.371E6;        // src/ModRamConst.f90:14
+constexpr double kQ = 1.602E-19;       // src/ModRamConst.f90:19
+constexpr double kCS = 2.998E8;        // src/ModRamConst.f90:20
+constexpr double kPI = 3.1415926535897932384626433832795;
+
+struct Dev {
+  // sizes
+  int nr, nt, ne, npa, ns, nm;
+  long long ncell;  // NR*NT*NE*NPA
+  int nf;           // NR+1
+  // scalars
+  double mdr, dphi, dl1, conf1, conf2, betalim;
+  unsigned flags;
+  // grid vectors
+  const double *lz, *rlz, *phi, *ekev, *ebnd, *we, *de, *mu, *dmu, *wmu;
+  const int *upa_atm;   // int(UPA(I)): first loss-cone L (1-based), NR
+  const int *upa_mom;   // int(UPA(I)-1): last L of the ANISCH sum, NR
+  // reciprocal grid tables: -0.5/DE, 1/WE, 1/DE (NE); -0.5/DMU, 1/WMU, 1/DMU (NPA)
+  const double *mhde, *iwe, *ide, *mhdmu, *iwmu, *idmu;
+  // per-species grid (ns x NE)
+  const double *grel, *grbnd, *vel;
+  const double *epp;
+  const double *rmas;     // (ns)
+  const double *ffactor;  // (ns, NR, NE, NPA)
+  const int *qs;        // species charge
+  const int *cex_kind;
+  // fields, (NR+1,NT,NPA) / (NR+1,NT) / int (NR,NT)
+  const double *fnhs, *fnis, *bounhs, *bounis, *hdns, *didt, *dibndt;
+  const double *bnes, *dbdt, *eir, *eip;
+  const int *outside;
+  // field-only derived tables, (NR,NT,NPA) unless noted
+  double *grt;            // R: gradient-curvature factor, CGR = grt*P4(K)
+  double *gpt;            // P: CDriftP = A(I,J) + P2(I,K)*gpt
+  double *gre, *gpe, *ze, *wet;   // E: GPR1+2+3, GPP1+2, dBdt1+dIdt1, EDT1 factor
+  double *gmr, *gmp, *zm, *hm, *cmu0;  // MU
+  double *rho;            // (NR,NT): FNHS(NPA)*MU(NPA)/FNHS(NPA-1)/MU(NPA-1)
+  double *epme, *epma;    // (ns, ncell): ANISCH weights, exact reference formula
+  // DTs-dependent per-species small tables
+  double *p4;             // (ns, NE)
+  double *p2;             // (ns, NR, NE)
+  double *edot;           // (ns, NR, NE)
+  double *eb, *ek;        // (ns, NE)
+  double *kap;            // (ns, 2): extrapolation factors of F(1), F(0) in DRIFTE
+  double *wm;             // (NR,NT,NPA): -CMUDOT*HM, DTs-dependent, species-free
+  double *cmudot;         // (NR,NT,NPA): MUDOT(I,L)*BOUNIS/BOUNHS, DTs-dependent
+  double *loss1;          // (ns, ncell): CHARGE*ATLOS^(1/FNHS) (one half step)
+  double *loss2;          // (ns, ncell): ((CHARGE*ATM)*ATM)*CHARGE (both halves)
+  double *charge, *atm;   // (ns, ncell): separate factors for the bookkeeping path
+  // per-member VT-dependent tables
+  double *kp;             // (nm)
+  int *vt_mode;           // (nm): 1 = VOLS from kp, 0 = explicit VT
+  double *vt;             // (nm, NR+1, NT)
+  double *cr;             // (nm, NR, NT)
+  double *ca;             // (nm, NR, NT)
+  double *ue, *um;        // (nm, NR, NT, NPA)
+  // per (member, species) slot
+  double *f2;             // (nm*ns, ncell)
+  double *fgeos;          // (nm*ns, NT*NE*NPA)
+  double *plane_last;     // (nm*ns, NE*NPA): DRIFTR F(NR+1) of the last inflow line of plane (K,L)
+  int *plane_has;         // (nm*ns, NE*NPA): plane (K,L) has an inflow line
+  double *plane_carry;    // (nm*ns, NE*NPA): F(NR+1) left by planes before (K,L) in K->L order
+  unsigned long long *cflq;  // (nm*ns, 4): max over cells of the CFL quotient, as bits
+  double *mom_part;       // (nm*ns, NR, NT, NE, 2) per-K moment partials
+  double *ppert, *ppart;  // (nm*ns, NR, NT)
+  double *sumrc_part;     // (nm*ns, nblk) SUMRC partial sums
+  // work list
+  const int2 *items;      // (member, species)
+  int nitems;
+};
+
+// ---------------------------------------------------------------- bit tests
+__device__ __forceinline__ unsigned long long dbits(double x) {
+  return (unsigned long long)__double_as_longlong(x);
+}
+// x < 0.0 exactly as the Fortran test `C.lt.0` (false for -0.0 and NaN with
+// the sign bit clear).
+__device__ __forceinline__ bool is_neg(double x) { return dbits(x) > 0x8000000000000000ULL; }
+__device__ __forceinline__ bool is_neg_or_nan(double x) { return (long long)dbits(x) < 0 && (dbits(x) << 1) != 0; }
+// |x| > 1e-27
+__device__ __forceinline__ bool abs_gt_1em27(double x) {
+  const unsigned long long t = 0x3A53CE9A36F23C10ULL;  // bits of 1.0E-27
+  return (dbits(x) & 0x7FFFFFFFFFFFFFFFULL) > t;
+}
+// d*x > 0 (both nonzero, same sign)
+__device__ __forceinline__ bool same_sign_nonzero(double d, double x) {
+  unsigned long long bd = dbits(d), bx = dbits(x);
+  return ((long long)(bd ^ bx) >= 0) && ((bd << 1) != 0) && ((bx << 1) != 0);
+}
+
+// Flux-limited face value of the reference sweeps (src/ModRamDrift.f90:169-183):
+//   FUP = upwind value; if |X|<=1e-27 or R<=0: FBND=FUP
+//   else FBND = FUP + LIMITER(R)*CORR, LIMITER = max(min(beta R,1),min(R,beta)),
+//        CORR = -0.5*(Cd - s)*X = a*X,  R = D/X.
+// Division-free: for D*X>0, LIMITER*X = sign(X)*max(min(beta|D|,|X|),min(|D|,beta|X|)).
+// bx = beta*|x|, bd = beta*|d| (the neighbour face's bx).  One FP64 fma.
+__device__ __forceinline__ double face_value(double x, double bx, double d, double bd,
+                                             double fup, double a) {
+  double ax = fabs(x), ad = fabs(d);
+  double lx = fmax(fmin(bd, ax), fmin(ad, bx));
+  lx = copysign(lx, x);
+  double fb = fma(a, lx, fup);
+  bool act = abs_gt_1em27(x) && same_sign_nonzero(d, x);
+  return act ? fb : fup;
+}
+
+// F2 < 0 -> 1e-15 (src/ModRamDrift.f90:187-190)
+__device__ __forceinline__ double clip(double v) { return is_neg(v) ? 1E-15 : v; }
+
+// 64-bit max-reduction of a non-negative double across a warp, then one
+// atomicMax on the bit pattern (order-independent, hence deterministic).
+__device__ __forceinline__ void warp_atomic_max(unsigned long long *slot, double q) {
+  unsigned long long v = dbits(q);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  if ((threadIdx.x & 31) == 0 && v != 0ULL) atomicMax(slot, v);
+}
+
+__host__ __device__ inline long long idx4(int i, int j, int k, int l, int nr, int nt, int ne) {
+  return (((long long)l * ne + k) * nt + j) * nr + i;
+}
+
+}  // namespace ramgpu

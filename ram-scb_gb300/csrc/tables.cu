@@ -1,0 +1,560 @@
+// tables.cu -- coefficient tables, losses, moments and bookkeeping kernels.
+//
+// The drift coefficients of the reference are recomputed per cell and per
+// call; here they are split into factors that change at different rates:
+//   fields only (set_fields)      : grt, gpt, gre, gpe, ze, wet, gmr, gmp, zm, hm, cmu0, rho
+//   species only (set_grid)       : eb, ek, kap, ANISCH weights epme/epma
+//   DTs (when DTs changes)        : p4, p2, edot, cmudot, wm, CHARGE/ATMOL factors
+//   potential VT (every ram_run)  : cr, ca, ue, um
+// so that a sweep face needs one or two FP64 operations for its coefficient.
+// Formulas restate src/ModRamDrift.f90:36-88 (DRIFTPARA), :118-146 (DRIFTR),
+// :232-239 (DRIFTP), :310-342 (DRIFTE), :415-433 (DRIFTMU),
+// src/ModRamLoss.f90:19-170 (CEPARA), :485-507 (ATMOL),
+// src/ModRamRun.f90:45-54 (VOLS), :186-201 (periodic copy, mask),
+// :231-259 (SUMRC), :343-404 (ANISCH moments), :208-222 (FLUX).
+#include <math.h>
+#include "kernels.cuh"
+
+namespace ramgpu {
+
+// 1-based accessors in the reference's index order (I, J, L) / (I, J).
+#define NRr (d.nr)
+#define NTt (d.nt)
+#define FIX(I, J, L) ((((long long)(L)-1) * d.nt + ((J)-1)) * d.nf + ((I)-1))
+#define BIX(I, J) (((long long)(J)-1) * d.nf + ((I)-1))
+#define TIX(I, J, L) ((((long long)(L)-1) * d.nt + ((J)-1)) * d.nr + ((I)-1))
+#define FNHS(I, J, L) d.fnhs[FIX(I, J, L)]
+#define FNIS(I, J, L) d.fnis[FIX(I, J, L)]
+#define BOUNHS(I, J, L) d.bounhs[FIX(I, J, L)]
+#define BOUNIS(I, J, L) d.bounis[FIX(I, J, L)]
+#define HDNS(I, J, L) d.hdns[FIX(I, J, L)]
+#define DIDT(I, J, L) d.didt[FIX(I, J, L)]
+#define DIBNDT(I, J, L) d.dibndt[FIX(I, J, L)]
+#define BNES(I, J) d.bnes[BIX(I, J)]
+#define DBDT(I, J) d.dbdt[BIX(I, J)]
+#define EIR(I, J) d.eir[BIX(I, J)]
+#define EIP(I, J) d.eip[BIX(I, J)]
+#define RLZ(I) d.rlz[(I)-1]
+#define LZ(I) d.lz[(I)-1]
+#define EKEV(K) d.ekev[(K)-1]
+#define EBND(K) d.ebnd[(K)-1]
+#define WE(K) d.we[(K)-1]
+#define MU(L) d.mu[(L)-1]
+#define WMU(L) d.wmu[(L)-1]
+
+__device__ __forceinline__ void wrapj(int J, int nt, int& J0, int& J1) {
+  J0 = J - 1;
+  if (J == 1) J0 = nt - 1;
+  J1 = J + 1;
+  if (J == nt) J1 = 2;
+}
+
+// ------------------------------------------------------------ field tables
+__global__ void k_field_tables(Dev d) {
+  const long long n = (long long)d.nr * d.nt * d.npa;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int I = 1 + (int)(t % d.nr);
+  const int J = 1 + (int)((t / d.nr) % d.nt);
+  const int L = 1 + (int)(t / ((long long)d.nr * d.nt));
+  const double MDR = d.mdr, DPHI = d.dphi;
+  int J0, J1;
+  wrapj(J, d.nt, J0, J1);
+  // DRIFTR gradient-curvature factor (src/ModRamDrift.f90:140-144)
+  {
+    double CGR1 = FNIS(I + 1, J1, L) + FNIS(I, J1, L) - FNIS(I + 1, J0, L) - FNIS(I, J0, L);
+    double CGR2 = BNES(I + 1, J1) + BNES(I, J1) - BNES(I + 1, J0) - BNES(I, J0);
+    double CGR3 = CGR1 + (FNIS(I + 1, J, L) + FNIS(I, J, L) - 2 * FNHS(I + 1, J, L) - 2 * FNHS(I, J, L))
+                             * CGR2 / 2. / (BNES(I + 1, J) + BNES(I, J));
+    d.grt[t] = CGR3 / (FNHS(I, J, L) + FNHS(I + 1, J, L)) / 2. / (BNES(I, J) + BNES(I + 1, J))
+               / (RLZ(I) + 0.5 * MDR);
+  }
+  double gpt = 0, gre = 0, gpe = 0, ze = 0, wet = 0, gmr = 0, gmp = 0, zm = 0, hm = 0, cmu0 = 0;
+  if (I >= 2) {
+    const double R = RLZ(I);
+    // DRIFTP (src/ModRamDrift.f90:232-237), J = 2..NT only
+    if (J >= 2) {
+      int Jp = J + 1;
+      if (J == d.nt) Jp = 2;
+      double GPA1 = FNIS(I, J, L) + FNIS(I, Jp, L)
+                    + (FNIS(I + 1, Jp, L) + FNIS(I + 1, J, L) - FNIS(I - 1, J, L) - FNIS(I - 1, Jp, L)) * R / 2. / MDR;
+      double GPA2 = R / 4. / MDR * (FNIS(I, J, L) + FNIS(I, Jp, L) - 2 * FNHS(I, J, L) - 2 * FNHS(I, Jp, L))
+                    * (BNES(I + 1, Jp) + BNES(I + 1, J) - BNES(I - 1, J) - BNES(I - 1, Jp)) / (BNES(I, J) + BNES(I, Jp));
+      gpt = -(GPA1 + GPA2) / (FNHS(I, J, L) + FNHS(I, Jp, L)) / (BNES(I, J) + BNES(I, Jp));
+    }
+    // DRIFTE (src/ModRamDrift.f90:323-341), J2 = J1
+    {
+      const double fis = FNIS(I, J, L), fhs = FNHS(I, J, L), b = BNES(I, J);
+      double GPA = (1. - fis / 2. / fhs) / b;
+      double GPR1 = GPA * (BNES(I + 1, J) - BNES(I - 1, J)) / 2. / MDR;
+      double GPR2 = -fis / fhs / R;
+      double GPR3 = -(FNIS(I + 1, J, L) - FNIS(I - 1, J, L)) / 2. / MDR / fhs;
+      double GPP1 = GPA * (BNES(I, J1) - BNES(I, J0)) / 2. / DPHI;
+      double GPP2 = -(FNIS(I, J1, L) - FNIS(I, J0, L)) / 2. / DPHI / fhs;
+      double DRD2 = (FNIS(I, J1, L) - FNIS(I, J0, L)) / 2. / DPHI
+                    + (fis - 2 * fhs) * (BNES(I, J1) - BNES(I, J0)) / 4 / b / DPHI;
+      double DPD2 = fis + (FNIS(I + 1, J, L) - FNIS(I - 1, J, L)) * R / 2 / MDR
+                    + R * (fis - 2 * fhs) / 4 / MDR * (BNES(I + 1, J) - BNES(I - 1, J)) / b;
+      double dBdt1 = DBDT(I, J) * (1. - fis / 2. / fhs) * R / b;
+      double dIdt1 = -DIDT(I, J, L) * R / fhs;
+      gre = GPR1 + GPR2 + GPR3;
+      gpe = GPP1 + GPP2;
+      ze = dBdt1 + dIdt1;
+      // EDT1 = eb(K)/(FNHS*RLZ*BNES); inner = UE + eb(K)*wet
+      wet = (gre * DRD2 * R - gpe * DPD2) / fhs / R / b;
+    }
+    // DRIFTMU (src/ModRamDrift.f90:418-433)
+    {
+      const double bis = BOUNIS(I, J, L), bhs = BOUNHS(I, J, L), b = BNES(I, J);
+      cmu0 = bis / bhs;
+      double GMR1 = (BNES(I + 1, J) - BNES(I - 1, J)) / 4 / MDR / b;
+      double GMR2 = 1 / R;
+      double GMR3 = (BOUNIS(I + 1, J, L) - BOUNIS(I - 1, J, L)) / 2 / MDR / bis;
+      double GMP1 = (BNES(I, J1) - BNES(I, J0)) / 4 / DPHI / b;
+      double GMP2 = (BOUNIS(I, J1, L) - BOUNIS(I, J0, L)) / 2 / DPHI / bis;
+      double DRM2 = (BOUNIS(I, J1, L) - BOUNIS(I, J0, L)) / 2 / DPHI
+                    + (bis - 2 * bhs) * (BNES(I, J1) - BNES(I, J0)) / 4 / b / DPHI;
+      double DPM2 = bis + (BOUNIS(I + 1, J, L) - BOUNIS(I - 1, J, L)) * R / 2 / MDR
+                    + (bis - 2 * bhs) * R / 4 / MDR * (BNES(I + 1, J) - BNES(I - 1, J)) / b;
+      double dBdt2 = DBDT(I, J) / 2. / b * R;
+      double dIbndt2 = DIBNDT(I, J, L) * R / bis;
+      gmr = GMR1 + GMR2 + GMR3;
+      gmp = GMP1 + GMP2;
+      zm = dBdt2 + dIbndt2;
+      hm = (gmr * DRM2 * R - gmp * DPM2) / bhs / R / b;
+    }
+    if (L == 1) d.rho[(long long)(J - 1) * d.nr + (I - 1)] =
+        FNHS(I, J, d.npa) * MU(d.npa) / FNHS(I, J, d.npa - 1) / MU(d.npa - 1);
+  } else if (L == 1) {
+    d.rho[(long long)(J - 1) * d.nr] = 0.0;
+  }
+  d.gpt[t] = gpt;
+  d.gre[t] = gre; d.gpe[t] = gpe; d.ze[t] = ze; d.wet[t] = wet;
+  d.gmr[t] = gmr; d.gmp[t] = gmp; d.zm[t] = zm; d.hm[t] = hm; d.cmu0[t] = cmu0;
+}
+
+void launch_field_tables(const Dev& d, cudaStream_t st) {
+  long long n = (long long)d.nr * d.nt * d.npa;
+  k_field_tables<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
+}
+
+// ------------------------------------------------------- species constants
+__global__ void k_species_static(Dev d) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.ns * d.ne) return;
+  const int s = t / d.ne, K = 1 + t % d.ne;
+  const double* grel = d.grel + s * d.ne;
+  const double* grbnd = d.grbnd + s * d.ne;
+  const double QS = (double)d.qs[s];
+  d.eb[t] = EBND(K) * 1e3 * (grbnd[K - 1] + 1) / 2 / grbnd[K - 1] / QS;
+  d.ek[t] = EKEV(K) * 1e3 * (grel[K - 1] + 1) / 2 / grel[K - 1] / QS;
+  if (K == 1) {
+    const double G1 = grel[0], G2 = grel[1];
+    d.kap[2 * s + 1] = G1 / G2 * sqrt((G2 * G2 - 1) / (G1 * G1 - 1));
+    const double EZERO = EKEV(1) - WE(1);
+    const double GRZERO = 1. + EZERO * 1000. * kQ / d.rmas[s] / kCS / kCS;
+    d.kap[2 * s + 0] = GRZERO / G1 * sqrt((G1 * G1 - 1) / (GRZERO * GRZERO - 1));
+  }
+}
+
+// ANISCH weights ERNM/EPMA/EPME of src/ModRamRun.f90:372-374, per species.
+__global__ void k_moment_weights(Dev d) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)d.ns * d.ncell) return;
+  const int s = (int)(t / d.ncell);
+  const long long c = t % d.ncell;
+  const int I = 1 + (int)(c % d.nr);
+  const int J = 1 + (int)((c / d.nr) % d.nt);
+  const int K = 1 + (int)((c / ((long long)d.nr * d.nt)) % d.ne);
+  const int L = 1 + (int)(c / ((long long)d.nr * d.nt * d.ne));
+  double me = 0.0, ma = 0.0;
+  if (I >= 2 && K >= 2 && L <= d.upa_mom[I - 1]) {
+    const double ff = d.ffactor[(long long)s * d.nr * d.ne * d.npa + (((long long)L - 1) * d.ne + (K - 1)) * d.nr + (I - 1)];
+    const double ERNM = WMU(L) / ff / FNHS(I, J, L);
+    const double EPMA = ERNM * MU(L) * MU(L);
+    me = ERNM - EPMA;
+    ma = EPMA;
+  }
+  d.epme[t] = me;
+  d.epma[t] = ma;
+}
+
+void launch_species_static(const Dev& d, cudaStream_t st) {
+  int n = d.ns * d.ne;
+  k_species_static<<<(n + 127) / 128, 128, 0, st>>>(d);
+  long long nc = (long long)d.ns * d.ncell;
+  k_moment_weights<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(d);
+}
+
+// ------------------------------------------------------------- DTs tables
+__global__ void k_dts_small(Dev d, double DTs) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.ns * d.ne * d.nr) return;
+  const int i = t % d.nr, k = (t / d.nr) % d.ne, s = t / (d.nr * d.ne);
+  const int I = i + 1, K = k + 1;
+  const double g = d.grel[s * d.ne + k], gb = d.grbnd[s * d.ne + k];
+  const double QS = (double)d.qs[s];
+  const double MDR = d.mdr, DPHI = d.dphi;
+  if (i == 0) d.p4[s * d.ne + k] = DTs * EKEV(K) * 1000.0 * (g + 1) / g / DPHI / MDR / QS;
+  d.p2[t] = DTs * EKEV(K) * 1000 * (g + 1) / g / (RLZ(I) * RLZ(I)) / DPHI / QS;
+  d.edot[t] = EBND(K) * DTs / RLZ(I) * (gb + 1) / gb / 2.;
+}
+
+__global__ void k_dts_cells(Dev d, double DTs) {
+  const long long n = (long long)d.nr * d.nt * d.npa;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int I = 1 + (int)(t % d.nr);
+  const int L = 1 + (int)(t / ((long long)d.nr * d.nt));
+  double mudot = 0.0;
+  if (L < d.npa) {
+    const double MUBOUN = MU(L) + 0.5 * WMU(L);
+    mudot = (1. - MUBOUN * MUBOUN) * DTs / 2 / MUBOUN / RLZ(I);
+  }
+  const double cm = mudot * d.cmu0[t];
+  d.cmudot[t] = cm;
+  d.wm[t] = -cm * d.hm[t];
+}
+
+// CEPARA analytic cross sections and ATMOL factor, per species and cell.
+__global__ void k_dts_loss(Dev d, double DTs) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)d.ns * d.ncell) return;
+  const int s = (int)(t / d.ncell);
+  const long long c = t % d.ncell;
+  const int I = 1 + (int)(c % d.nr);
+  const int J = 1 + (int)((c / d.nr) % d.nt);
+  const int K = 1 + (int)((c / ((long long)d.nr * d.nt)) % d.ne);
+  const int L = 1 + (int)(c / ((long long)d.nr * d.nt * d.ne));
+  const double V = d.vel[s * d.ne + K - 1];
+  double ch = 1.0, at = 1.0;
+  const int kind = d.cex_kind[s];
+  if (kind >= 1 && kind <= 3 && L >= 2 && K >= 2 && I >= 2) {
+    double X = log10(EKEV(K));
+    if (X < -2.) X = -2.;
+    const double X2 = X * X, X3 = X2 * X, X4 = X2 * X2;
+    double Y;
+    if (kind == 1) Y = -18.767 - 0.11017 * X - 3.8173e-2 * X2 - 0.1232 * X3 - 5.0488e-2 * X4;
+    else if (kind == 2) Y = -20.789 + 0.92316 * X - 0.68017 * X2 + 0.66153 * X3 - 0.20998 * X4;
+    else Y = -18.987 - 0.10613 * X - 5.4841E-3 * X2 - 1.6262E-2 * X3 - 7.0554E-3 * X4;
+    const double ALPHA = pow(10., Y) * V * HDNS(I, J, L) * DTs;
+    ch = exp(-ALPHA);
+  }
+  if (!(d.flags & 2u) && K >= 2 && I >= 2 && L >= d.upa_atm[I - 1]) {
+    const double TAUB = 2 * RLZ(I) / V;
+    const double ATLOS = exp(-DTs / TAUB);
+    at = pow(ATLOS, 1 / FNHS(I, J, L));
+  }
+  d.charge[t] = ch;
+  d.atm[t] = at;
+  d.loss1[t] = ch * at;
+  d.loss2[t] = ((ch * at) * at) * ch;
+}
+
+void launch_dts_tables(const Dev& d, double dts, cudaStream_t st) {
+  int n = d.ns * d.ne * d.nr;
+  k_dts_small<<<(n + 127) / 128, 128, 0, st>>>(d, dts);
+  long long nc = (long long)d.nr * d.nt * d.npa;
+  k_dts_cells<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(d, dts);
+  long long nl = (long long)d.ns * d.ncell;
+  k_dts_loss<<<(unsigned)((nl + 255) / 256), 256, 0, st>>>(d, dts);
+}
+
+// ------------------------------------------------ per-member (VT) tables
+__global__ void k_vt(Dev d) {
+  const int nv = d.nf * d.nt;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)d.nm * nv) return;
+  const int m = (int)(t / nv);
+  if (d.vt_mode[m] != 1) return;
+  const int I = 1 + (int)(t % nv) % d.nf;
+  const int J = 1 + (int)(t % nv) / d.nf;
+  const double KP = d.kp[m];
+  const double tt = 1. - 0.159 * KP + 0.0093 * (KP * KP);
+  const double AVS = 7.05E-6 / (tt * tt * tt) / kRE;
+  const double PHIOFS = 0 * kPI / 12.;
+  const double lr = LZ(I) * kRE;
+  d.vt[t] = AVS * (lr * lr) * sin(d.phi[J - 1] - PHIOFS);
+}
+
+__global__ void k_member_coef(Dev d, double DTs) {
+  const long long per = (long long)d.nr * d.nt * d.npa;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)d.nm * per) return;
+  const int m = (int)(t / per);
+  const long long c = t % per;
+  const int I = 1 + (int)(c % d.nr);
+  const int J = 1 + (int)((c / d.nr) % d.nt);
+  const int L = 1 + (int)(c / ((long long)d.nr * d.nt));
+  const double* vt = d.vt + (long long)m * d.nf * d.nt;
+#define VT(I, J) vt[BIX(I, J)]
+  const double MDR = d.mdr, DPHI = d.dphi;
+  int J0, J1;
+  wrapj(J, d.nt, J0, J1);
+  if (L == 1) {
+    const long long ij = (long long)m * d.nr * d.nt + (long long)(J - 1) * d.nr + (I - 1);
+    // DRIFTR E x B (src/ModRamDrift.f90:118-127) with VR from DRIFTPARA
+    const double VR = DTs / MDR / (RLZ(I) + 0.5 * MDR) / 2 / DPHI;
+    const double den = BNES(I, J) + BNES(I + 1, J);
+    d.cr[ij] = VR * (VT(I, J0) + VT(I + 1, J0) - VT(I, J1) - VT(I + 1, J1)) / den
+               + (EIP(I, J) + EIP(I + 1, J)) / den * DTs / MDR;
+    double ca = 0.0;
+    if (I >= 2 && J >= 2) {  // DRIFTP E x B, EIR and corotation terms
+      const double P1 = DTs / DPHI / 2 / MDR / RLZ(I);
+      ca = ((VT(I + 1, J) + VT(I + 1, J1) - VT(I - 1, J) - VT(I - 1, J1)) * P1
+            - (EIR(I, J1) + EIR(I, J)) / RLZ(I) * DTs / DPHI) / (BNES(I, J) + BNES(I, J1))
+           + kOME * DTs / DPHI;
+    }
+    d.ca[ij] = ca;
+  }
+  double ue = 0.0, um = 0.0;
+  if (I >= 2) {
+    const double R = RLZ(I);
+    const double DRD1 = (EIP(I, J) * R - (VT(I, J1) - VT(I, J0)) / 2. / DPHI) / BNES(I, J);
+    const double DPD1 = kOME * R + ((VT(I + 1, J) - VT(I - 1, J)) / 2 / MDR - EIR(I, J)) / BNES(I, J);
+    ue = d.gre[c] * DRD1 + d.gpe[c] * DPD1 + d.ze[c];
+    um = -d.cmudot[c] * (d.gmr[c] * DRD1 + d.gmp[c] * DPD1 + d.zm[c]);
+  }
+  d.ue[t] = ue;
+  d.um[t] = um;
+#undef VT
+}
+
+void launch_member_coef(const Dev& d, double dts, cudaStream_t st) {
+  long long nv = (long long)d.nm * d.nf * d.nt;
+  k_vt<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(d);
+  long long n = (long long)d.nm * d.nr * d.nt * d.npa;
+  k_member_coef<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, dts);
+}
+
+// ---------------------------------------------------- DRIFTR ghost planes
+// Plane p = (K-1)*NPA + (L-1) in the reference's K->L loop order.
+__global__ void k_ghost_planes(Dev d) {
+  const int np = d.ne * d.npa;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int2 item = d.items[blockIdx.y];
+  const int m = item.x, s = item.y, slot = m * d.ns + s;
+  if (p >= np) return;
+  const int k = p / d.npa, l = p % d.npa;
+  const double p4 = d.p4[s * d.ne + k];
+  int has = 0;
+  double v = 0.0;
+  for (int jj = d.nt - 1; jj >= 0; --jj)
+    if (inflow_line(d, m, jj, l, p4)) {
+      has = 1;
+      v = ghost_value(d, slot, jj, k, l, d.conf1);
+      break;
+    }
+  d.plane_has[(long long)slot * np + p] = has;
+  d.plane_last[(long long)slot * np + p] = v;
+}
+
+// Exclusive "last defined" scan over planes: one block per work item.
+__global__ void __launch_bounds__(1024) k_ghost_scan(Dev d) {
+  __shared__ int s_has[1024];
+  __shared__ double s_val[1024];
+  const int np = d.ne * d.npa;
+  const int2 item = d.items[blockIdx.x];
+  const int slot = item.x * d.ns + item.y;
+  const int* has = d.plane_has + (long long)slot * np;
+  const double* last = d.plane_last + (long long)slot * np;
+  double* carry = d.plane_carry + (long long)slot * np;
+  const int nt = blockDim.x;
+  const int cs = (np + nt - 1) / nt;
+  const int p0 = threadIdx.x * cs, p1 = min(np, p0 + cs);
+  int h = 0;
+  double v = 0.0;
+  for (int p = p0; p < p1; ++p)
+    if (has[p]) { h = 1; v = last[p]; }
+  s_has[threadIdx.x] = h;
+  s_val[threadIdx.x] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {  // serial exclusive scan over the block's chunks
+    int ch = 0;
+    double cv = 0.0;
+    for (int t = 0; t < nt; ++t) {
+      int th = s_has[t];
+      double tv = s_val[t];
+      s_has[t] = ch;
+      s_val[t] = cv;
+      if (th) { ch = 1; cv = tv; }
+    }
+  }
+  __syncthreads();
+  double run = s_val[threadIdx.x];
+  for (int p = p0; p < p1; ++p) {
+    carry[p] = run;
+    if (has[p]) run = last[p];
+  }
+}
+
+void launch_ghost(const Dev& d, cudaStream_t st) {
+  const int np = d.ne * d.npa;
+  k_ghost_planes<<<dim3((np + 127) / 128, d.nitems), 128, 0, st>>>(d);
+  k_ghost_scan<<<d.nitems, 1024, 0, st>>>(d);
+}
+
+// -------------------------------------------------- loss factor (bookkeeping path)
+__global__ void k_loss_apply(Dev d, const double* __restrict__ table) {
+  const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= d.ncell) return;
+  const int2 item = d.items[blockIdx.y];
+  const int slot = item.x * d.ns + item.y;
+  double* f = d.f2 + (long long)slot * d.ncell + c;
+  *f = *f * table[(long long)item.y * d.ncell + c];
+}
+
+void launch_loss_apply(const Dev& d, const double* table, cudaStream_t st) {
+  k_loss_apply<<<dim3((unsigned)((d.ncell + 255) / 256), d.nitems), 256, 0, st>>>(d, table);
+}
+
+// ------------------------------------ periodic copy + magnetopause mask
+__global__ void k_finish(Dev d, int any_outside) {
+  const long long n = (long long)d.nr * d.ne * d.npa;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int2 item = d.items[blockIdx.y];
+  const int slot = item.x * d.ns + item.y;
+  const int i = (int)(t % d.nr);
+  const long long kl = t / d.nr;  // K + NE*L
+  double* f = d.f2 + (long long)slot * d.ncell + kl * d.nt * d.nr + i;
+  f[(long long)(d.nt - 1) * d.nr] = f[0];  // F2(:,:,NT,:,:) = F2(:,:,1,:,:)
+  if (any_outside)
+    for (int j = 0; j < d.nt; ++j)
+      if (d.outside[(long long)j * d.nr + i] == 1) f[(long long)j * d.nr] = 1.e-31;
+}
+
+void launch_finish(const Dev& d, cudaStream_t st) {
+  // any_outside is folded into the flags word bit 31 by the host
+  long long n = (long long)d.nr * d.ne * d.npa;
+  k_finish<<<dim3((unsigned)((n + 255) / 256), d.nitems), 256, 0, st>>>(d, (d.flags >> 31) & 1u);
+}
+
+// ---------------------------------------------------------- ANISCH moments
+// Stage 1: one thread per (I>=2, J, K>=2): the L=1 side effect and the
+// pitch-angle sums SUME(K), SUMA(K) of src/ModRamRun.f90:366-378.
+__global__ void k_moments_part(Dev d) {
+  const int nr1 = d.nr - 1, ne1 = d.ne - 1;
+  const long long n = (long long)nr1 * d.nt * ne1;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int2 item = d.items[blockIdx.y];
+  const int s = item.y, slot = item.x * d.ns + s;
+  const int i = 1 + (int)(t % nr1);
+  const int j = (int)((t / nr1) % d.nt);
+  const int k = 1 + (int)(t / ((long long)nr1 * d.nt));
+  const long long st = (long long)d.ne * d.nt * d.nr;
+  const long long off = ((long long)k * d.nt + j) * d.nr + i;
+  double* f = d.f2 + (long long)slot * d.ncell + off;
+  const double* we = d.epme + (long long)s * d.ncell + off;
+  const double* wa = d.epma + (long long)s * d.ncell + off;
+  const double f2 = f[st];
+  f[0] = f2;  // F2(S,I,J,K,1) = F2(S,I,J,K,2)
+  double sume = 0.0, suma = 0.0;
+  const int u = d.upa_mom[i];
+  for (int L = 1; L <= u; ++L) {
+    const double v = (L == 1) ? f2 : f[(long long)(L - 1) * st];
+    sume = fma(v, we[(long long)(L - 1) * st], sume);
+    suma = fma(v, wa[(long long)(L - 1) * st], suma);
+  }
+  double* part = d.mom_part + (long long)slot * d.nr * d.nt * d.ne * 2;
+  const long long pi = (((long long)k * d.nt + j) * d.nr + i) * 2;
+  part[pi] = sume;
+  part[pi + 1] = suma;
+}
+
+// Stage 2: one thread per (I>=2, J): the energy-band sums and RFAC factors.
+__global__ void k_moments_reduce(Dev d) {
+  const int nr1 = d.nr - 1;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nr1 * d.nt) return;
+  const int2 item = d.items[blockIdx.y];
+  const int s = item.y, slot = item.x * d.ns + s;
+  const int i = 1 + t % nr1, j = t / nr1;
+  const double cv = kCS * 100;
+  const double RFAC = 4 * kPI / cv;
+  const double* part = d.mom_part + (long long)slot * d.nr * d.nt * d.ne * 2;
+  const double* epp = d.epp + s * d.ne;
+  int khi[5] = {6, 10, 25, 30, 35};
+  khi[4] = d.ne;
+  int klo = 2;
+  double ppert = 0., ppart = 0.;
+  for (int iwa = 0; iwa < 5; ++iwa) {
+    double PPER = 0., PPAR = 0.;
+    for (int K = klo; K <= khi[iwa]; ++K) {
+      const long long pi = (((long long)(K - 1) * d.nt + j) * d.nr + i) * 2;
+      PPER = PPER + epp[K - 1] * part[pi];
+      PPAR = PPAR + epp[K - 1] * part[pi + 1];
+    }
+    PPAR = 2 * RFAC * PPAR;
+    PPER = RFAC * PPER;
+    klo = khi[iwa] + 1;
+    ppert = ppert + PPER;
+    ppart = ppart + PPAR;
+  }
+  const long long o = (long long)slot * d.nr * d.nt + (long long)j * d.nr + i;
+  d.ppert[o] = ppert;
+  d.ppart[o] = ppart;
+}
+
+void launch_moments(const Dev& d, cudaStream_t st) {
+  long long n = (long long)(d.nr - 1) * d.nt * (d.ne - 1);
+  k_moments_part<<<dim3((unsigned)((n + 127) / 128), d.nitems), 128, 0, st>>>(d);
+  int n2 = (d.nr - 1) * d.nt;
+  k_moments_reduce<<<dim3((n2 + 127) / 128, d.nitems), 128, 0, st>>>(d);
+}
+
+// ------------------------------------------------------------------ SUMRC
+// Per-block partial sums of EKEV*F2*WE*WMU over I=2..NR, J=1..NT-1,
+// K=2..NE, L=2..NPA (src/ModRamRun.f90:246-255).  part: (nitems, nblk).
+__global__ void __launch_bounds__(256) k_sumrc(Dev d, double* part, int nblk) {
+  __shared__ double sh[256];
+  const int2 item = d.items[blockIdx.y];
+  const int slot = item.x * d.ns + item.y;
+  const double* f = d.f2 + (long long)slot * d.ncell;
+  double acc = 0.0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < d.ncell;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int I = 1 + (int)(c % d.nr);
+    const int J = 1 + (int)((c / d.nr) % d.nt);
+    const int K = 1 + (int)((c / ((long long)d.nr * d.nt)) % d.ne);
+    const int L = 1 + (int)(c / ((long long)d.nr * d.nt * d.ne));
+    if (I >= 2 && J <= d.nt - 1 && K >= 2 && L >= 2) {
+      const double WEIGHT = f[c] * WE(K) * WMU(L);
+      acc = acc + EKEV(K) * WEIGHT;
+    }
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[(long long)blockIdx.y * nblk + blockIdx.x] = sh[0];
+}
+
+void launch_sumrc(const Dev& d, double* part, int nblk, cudaStream_t st) {
+  k_sumrc<<<dim3(nblk, d.nitems), 256, 0, st>>>(d, part, nblk);
+}
+
+// ------------------------------------------------------------------- FLUX
+__global__ void k_flux(Dev d, int slot, int s, double* out) {
+  const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= d.ncell) return;
+  const int I = 1 + (int)(c % d.nr);
+  const int J = 1 + (int)((c / d.nr) % d.nt);
+  const int K = 1 + (int)((c / ((long long)d.nr * d.nt)) % d.ne);
+  const int L = 1 + (int)(c / ((long long)d.nr * d.nt * d.ne));
+  double v = 0.0;
+  if (I >= 2 && K >= 2 && L >= 2 && J <= d.nt - 1) {
+    const double ff = d.ffactor[(long long)s * d.nr * d.ne * d.npa + (((long long)L - 1) * d.ne + (K - 1)) * d.nr + (I - 1)];
+    v = d.f2[(long long)slot * d.ncell + c] / ff / FNHS(I, J, L);
+  }
+  out[c] = v;
+}
+
+void launch_flux(const Dev& d, int slot, int s, double* out, cudaStream_t st) {
+  k_flux<<<(unsigned)((d.ncell + 255) / 256), 256, 0, st>>>(d, slot, s, out);
+}
+
+}  // namespace ramgpu

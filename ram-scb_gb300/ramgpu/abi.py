@@ -1,0 +1,288 @@
+"""ctypes binding of the C ABI in include/ramgpu.h.
+
+``RamGpu`` mirrors the reference's interface for this path: the RAM state
+(F2 per species, field tables, FGEOS, VT) lives in the context, ``ram_run``
+advances it by one call of src/ModRamRun.f90:16-225, and the outputs
+(PPERT/PPART, FLUX, DtsNext, SUMRC losses) are read back afterwards.
+Arrays cross the boundary in the reference's Fortran layout.  There is no
+CPU fallback: if the CUDA library is missing the constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+RAMGPU_OK = 0
+ERRORS = {-1: "RAMGPU_ERR_ARG", -2: "RAMGPU_ERR_CUDA", -3: "RAMGPU_ERR_STATE",
+          -4: "RAMGPU_ERR_NUMERIC", -5: "RAMGPU_ERR_NOMEM"}
+FLAG_CLOSED, FLAG_NO_ATMOL, FLAG_LOSSES = 1, 2, 4
+
+# Every symbol include/ramgpu.h declares.
+EXPORTS = (
+    "ramgpu_create", "ramgpu_destroy", "ramgpu_last_error", "ramgpu_set_stream",
+    "ramgpu_set_species", "ramgpu_set_grid", "ramgpu_set_fields", "ramgpu_set_boundary",
+    "ramgpu_set_potential", "ramgpu_set_kp", "ramgpu_set_member_species",
+    "ramgpu_set_member_active", "ramgpu_upload_f2", "ramgpu_download_f2",
+    "ramgpu_upload_f2_all", "ramgpu_download_f2_all", "ramgpu_f2_device_ptr",
+    "ramgpu_ram_run", "ramgpu_half_step", "ramgpu_ram_run_async", "ramgpu_moments",
+    "ramgpu_flux", "ramgpu_cfl", "ramgpu_losses", "ramgpu_reset_losses", "ramgpu_launch_count",
+    "ramgpu_apply_op", "ramgpu_set_timing", "ramgpu_kernel_times",
+)
+KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
+          "anisch", "dts_tables", "sumrc")
+OP_DRIFTR, OP_DRIFTP, OP_DRIFTE, OP_DRIFTMU, OP_CHAREXCHANGE, OP_ATMOL, OP_ANISCH = range(7)
+
+
+class RamGpuError(RuntimeError):
+    pass
+
+
+class Config(C.Structure):
+    _fields_ = [("nr", C.c_int), ("nt", C.c_int), ("ne", C.c_int), ("npa", C.c_int),
+                ("ns", C.c_int), ("n_members", C.c_int), ("betalim", C.c_double),
+                ("fraccfl", C.c_double), ("dtsmin", C.c_double), ("flags", C.c_uint)]
+
+
+_P = C.POINTER(C.c_double)
+
+
+class GridStruct(C.Structure):
+    _fields_ = [("lz", _P), ("rlz", _P), ("phi", _P), ("dl1", C.c_double), ("mdr", C.c_double),
+                ("dphi", C.c_double), ("conf1", C.c_double), ("conf2", C.c_double),
+                ("ekev", _P), ("ebnd", _P), ("we", _P), ("de", _P), ("mu", _P), ("dmu", _P),
+                ("wmu", _P), ("upa", _P), ("rmas", _P), ("grel", _P), ("grbnd", _P), ("v", _P),
+                ("epp", _P), ("ernh", _P), ("ffactor", _P)]
+
+
+_lib = None
+
+
+def load_library(path: str | Path | None = None, build_if_missing: bool = False):
+    """Load libramgpu.so; raise if it is absent (no fallback path exists)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else _build.LIB_PATH
+    if not p.exists():
+        if build_if_missing:
+            _build.build_library()
+        else:
+            raise RamGpuError(f"CUDA library {p} not built; run __graft_entry__.build()")
+    lib = C.CDLL(str(p))
+    vp = C.c_void_p
+    i, d, u = C.c_int, C.c_double, C.c_uint
+    dp = _P
+    ip = C.POINTER(C.c_int)
+    sig = {
+        "ramgpu_create": ([C.POINTER(Config), C.POINTER(vp)], i),
+        "ramgpu_destroy": ([vp], i),
+        "ramgpu_last_error": ([vp, C.c_char_p, C.c_size_t], i),
+        "ramgpu_set_stream": ([vp, vp], i),
+        "ramgpu_set_species": ([vp, i, i, i], i),
+        "ramgpu_set_grid": ([vp, C.POINTER(GridStruct)], i),
+        "ramgpu_set_fields": ([vp] + [dp] * 11 + [ip], i),
+        "ramgpu_set_boundary": ([vp, i, i, dp], i),
+        "ramgpu_set_potential": ([vp, i, dp], i),
+        "ramgpu_set_kp": ([vp, i, d], i),
+        "ramgpu_set_member_species": ([vp, i, i, ip], i),
+        "ramgpu_set_member_active": ([vp, i, i], i),
+        "ramgpu_upload_f2": ([vp, i, i, dp], i),
+        "ramgpu_download_f2": ([vp, i, i, dp], i),
+        "ramgpu_upload_f2_all": ([vp, i, dp], i),
+        "ramgpu_download_f2_all": ([vp, i, dp], i),
+        "ramgpu_f2_device_ptr": ([vp, i, i, C.POINTER(dp)], i),
+        "ramgpu_ram_run": ([vp, d], i),
+        "ramgpu_half_step": ([vp, d, i], i),
+        "ramgpu_ram_run_async": ([vp, d], i),
+        "ramgpu_moments": ([vp, i, i, dp, dp], i),
+        "ramgpu_flux": ([vp, i, i, dp], i),
+        "ramgpu_cfl": ([vp, i, i, dp], i),
+        "ramgpu_losses": ([vp, i, i, dp], i),
+        "ramgpu_reset_losses": ([vp], i),
+        "ramgpu_launch_count": ([vp], C.c_longlong),
+        "ramgpu_apply_op": ([vp, d, i, i], i),
+        "ramgpu_set_timing": ([vp, i], i),
+        "ramgpu_kernel_times": ([vp, dp, C.POINTER(C.c_longlong)], i),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(_P)
+
+
+def _fort(a, dtype=np.float64):
+    return np.asfortranarray(np.asarray(a, dtype=dtype))
+
+
+class RamGpu:
+    """One GPU context holding the RAM state of ``n_members`` runs.
+
+    grid, fields: ``ramgpu.workload.Grid`` / ``Fields``.  Species are taken
+    from ``grid.species`` (charge and CEPARA branch)."""
+
+    def __init__(self, grid, fields, n_members: int = 1, betalim: float = 1.5,
+                 fraccfl: float = 0.8, dtsmin: float = 0.1, flags: int = 0, lib=None):
+        self.lib = lib or load_library()
+        self.grid = grid
+        self.ns = len(grid.species)
+        self.n_members = n_members
+        cfg = Config(grid.nr, grid.nt, grid.ne, grid.npa, self.ns, n_members, betalim, fraccfl,
+                     dtsmin, flags)
+        h = C.c_void_p()
+        rc = self.lib.ramgpu_create(C.byref(cfg), C.byref(h))
+        if rc != RAMGPU_OK:
+            buf = C.create_string_buffer(512)
+            self.lib.ramgpu_last_error(None, buf, 512)
+            raise RamGpuError(f"ramgpu_create: {ERRORS.get(rc, rc)}: {buf.value.decode()}")
+        self.h = h
+        for s, sp in enumerate(grid.species):
+            self._ck(self.lib.ramgpu_set_species(self.h, s, sp.charge, sp.cex_kind), "set_species")
+        self.set_grid(grid)
+        self.set_fields(fields)
+
+    # -------------------------------------------------------------- plumbing
+    def _ck(self, rc, what):
+        if rc != RAMGPU_OK:
+            buf = C.create_string_buffer(512)
+            self.lib.ramgpu_last_error(self.h, buf, 512)
+            raise RamGpuError(f"{what}: {ERRORS.get(rc, rc)}: {buf.value.decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ramgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---------------------------------------------------------------- inputs
+    def set_grid(self, g):
+        keep = {k: _fort(getattr(g, k)) for k in ("lz", "rlz", "phi", "ekev", "ebnd", "we", "de", "mu",
+                                                  "dmu", "wmu", "upa", "rmas", "grel", "grbnd", "v",
+                                                  "epp", "ernh", "ffactor")}
+        gs = GridStruct()
+        for k, a in keep.items():
+            setattr(gs, k, _dptr(a))
+        gs.dl1, gs.mdr, gs.dphi, gs.conf1, gs.conf2 = g.dl1, g.mdr, g.dphi, g.conf1, g.conf2
+        self._ck(self.lib.ramgpu_set_grid(self.h, C.byref(gs)), "set_grid")
+
+    def set_fields(self, f):
+        arrs = [_fort(getattr(f, k)) for k in ("fnhs", "fnis", "bounhs", "bounis", "hdns", "didt",
+                                               "dibndt", "bnes", "dbdt", "eir", "eip")]
+        out = _fort(f.outside, np.int32)
+        self._ck(self.lib.ramgpu_set_fields(self.h, *[_dptr(a) for a in arrs],
+                                            out.ctypes.data_as(C.POINTER(C.c_int))), "set_fields")
+
+    def set_boundary(self, member: int, s: int, fgeos):
+        a = _fort(fgeos)
+        self._ck(self.lib.ramgpu_set_boundary(self.h, member, s, _dptr(a)), "set_boundary")
+
+    def set_kp(self, member: int, kp: float):
+        self._ck(self.lib.ramgpu_set_kp(self.h, member, float(kp)), "set_kp")
+
+    def set_potential(self, member: int, vt):
+        a = _fort(vt)
+        self._ck(self.lib.ramgpu_set_potential(self.h, member, _dptr(a)), "set_potential")
+
+    def set_member_species(self, member: int, species_list):
+        a = np.asarray(species_list, dtype=np.int32)
+        self._ck(self.lib.ramgpu_set_member_species(self.h, member, a.size,
+                                                    a.ctypes.data_as(C.POINTER(C.c_int))),
+                 "set_member_species")
+
+    def set_member_active(self, member: int, active: bool):
+        self._ck(self.lib.ramgpu_set_member_active(self.h, member, int(bool(active))), "set_member_active")
+
+    # ----------------------------------------------------------------- state
+    def upload_f2(self, member: int, s: int, f2):
+        a = _fort(f2)
+        self._ck(self.lib.ramgpu_upload_f2(self.h, member, s, _dptr(a)), "upload_f2")
+
+    def download_f2(self, member: int, s: int) -> np.ndarray:
+        g = self.grid
+        a = np.empty((g.nr, g.nt, g.ne, g.npa), order="F")
+        self._ck(self.lib.ramgpu_download_f2(self.h, member, s, _dptr(a)), "download_f2")
+        return a
+
+    def f2_device_ptr(self, member: int, s: int) -> int:
+        p = _P()
+        self._ck(self.lib.ramgpu_f2_device_ptr(self.h, member, s, C.byref(p)), "f2_device_ptr")
+        return C.cast(p, C.c_void_p).value
+
+    # ------------------------------------------------------------------ step
+    def ram_run(self, dts: float):
+        self._ck(self.lib.ramgpu_ram_run(self.h, float(dts)), "ram_run")
+
+    def ram_run_async(self, dts: float):
+        self._ck(self.lib.ramgpu_ram_run_async(self.h, float(dts)), "ram_run_async")
+
+    def half_step(self, dts: float, order: int):
+        self._ck(self.lib.ramgpu_half_step(self.h, float(dts), int(order)), "half_step")
+
+    def apply_op(self, dts: float, op: int, cfl: bool = False):
+        """One reference operator (DRIFTR..ANISCH) on every active item."""
+        self._ck(self.lib.ramgpu_apply_op(self.h, float(dts), int(op), int(bool(cfl))), "apply_op")
+
+    # --------------------------------------------------------------- outputs
+    def moments(self, member: int, s: int):
+        g = self.grid
+        pe = np.empty((g.nr, g.nt), order="F")
+        pa = np.empty((g.nr, g.nt), order="F")
+        self._ck(self.lib.ramgpu_moments(self.h, member, s, _dptr(pe), _dptr(pa)), "moments")
+        return pe, pa
+
+    def flux(self, member: int, s: int) -> np.ndarray:
+        g = self.grid
+        a = np.empty((g.nr, g.nt, g.ne, g.npa), order="F")
+        self._ck(self.lib.ramgpu_flux(self.h, member, s, _dptr(a)), "flux")
+        return a
+
+    def cfl(self, member: int, s: int) -> np.ndarray:
+        a = np.empty(5)
+        self._ck(self.lib.ramgpu_cfl(self.h, member, s, _dptr(a)), "cfl")
+        return a
+
+    def losses(self, member: int, s: int) -> np.ndarray:
+        a = np.empty(4)
+        self._ck(self.lib.ramgpu_losses(self.h, member, s, _dptr(a)), "losses")
+        return a
+
+    def reset_losses(self):
+        self._ck(self.lib.ramgpu_reset_losses(self.h), "reset_losses")
+
+    def set_timing(self, enable: bool):
+        self._ck(self.lib.ramgpu_set_timing(self.h, int(bool(enable))), "set_timing")
+
+    def kernel_times(self):
+        """{class: (total_ms, launches)} of the launches timed since the last call."""
+        ms = np.zeros(16)
+        cnt = np.zeros(16, dtype=np.int64)
+        self._ck(self.lib.ramgpu_kernel_times(self.h, _dptr(ms), cnt.ctypes.data_as(C.POINTER(C.c_longlong))),
+                 "kernel_times")
+        return {KCLASS[k]: (float(ms[k]), int(cnt[k])) for k in range(len(KCLASS)) if cnt[k]}
+
+    def set_stream(self, stream_ptr: int):
+        self._ck(self.lib.ramgpu_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")
+
+    def launch_count(self) -> int:
+        return int(self.lib.ramgpu_launch_count(self.h))

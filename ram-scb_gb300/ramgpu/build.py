@@ -1,0 +1,69 @@
+"""In-tree build of the CUDA library (sm_103a only).
+
+The translation units compile concurrently, then link into
+``ram-scb_gb300/lib/libramgpu.so``.  No cmake, no torch extension
+machinery: the library exposes a plain C ABI (include/ramgpu.h).
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG_ROOT = Path(__file__).resolve().parent.parent          # ram-scb_gb300/
+REPO_ROOT = PKG_ROOT.parent
+CSRC = PKG_ROOT / "csrc"
+LIB_DIR = PKG_ROOT / "lib"
+LIB_PATH = LIB_DIR / "libramgpu.so"
+SOURCES = ["abi.cu", "sweeps.cu", "tables.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+
+
+def nvcc_path() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found: the ramgpu CUDA library cannot be built")
+
+
+def _stale(target: Path, deps) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(Path(p).stat().st_mtime > t for p in deps)
+
+
+def build_library(force: bool = False, verbose: bool = False) -> Path:
+    """Compile csrc/*.cu for sm_103a and link libramgpu.so (in-tree)."""
+    nvcc = nvcc_path()
+    obj_dir = LIB_DIR / "obj"
+    obj_dir.mkdir(parents=True, exist_ok=True)
+    headers = list(CSRC.glob("*.cuh")) + [REPO_ROOT / "include" / "ramgpu.h"]
+    jobs = []
+    for src in SOURCES:
+        s = CSRC / src
+        o = obj_dir / (src + ".o")
+        if force or _stale(o, [s] + headers):
+            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, "-I", str(REPO_ROOT / "include"), "-c", str(s), "-o", str(o)])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd))
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        return r
+
+    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        list(ex.map(run, jobs))
+    objs = [str(obj_dir / (s + ".o")) for s in SOURCES]
+    if force or jobs or _stale(LIB_PATH, objs):
+        run([nvcc, *ARCH, "-shared", "-o", str(LIB_PATH), *objs, "-lcudart"])
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build_library(force=True, verbose=True))

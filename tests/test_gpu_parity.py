@@ -1,0 +1,150 @@
+"""GPU parity: every operator and the full ram_run against the CPU oracle.
+
+Bar (from the specification of this path): FP64 results within 1e-12
+relative max-norm per step, i.e. max|gpu - ref| / max|ref| <= 1e-12 for F2
+of every species after one step started from the same state.  Moments,
+FLUX and DtsNext use the same tolerance.
+"""
+import numpy as np
+import pytest
+
+from ramgpu import abi, workload as W
+import pyoracle
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def rel(a, b):
+    den = np.max(np.abs(b))
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / (den if den > 0 else 1.0))
+
+
+@pytest.fixture(scope="module")
+def single():
+    return W.make_workload("single_h")
+
+
+@pytest.fixture(scope="module")
+def tiny():
+    return W.make_workload("tiny")
+
+
+@pytest.fixture(scope="module")
+def four():
+    return W.make_workload("four_sp")
+
+
+def _setup(wl, kp, members=1, flags=0):
+    g = wl.grid
+    gpu = abi.RamGpu(g, wl.fields, n_members=members, flags=flags)
+    for m in range(members):
+        for s in range(len(g.species)):
+            gpu.upload_f2(m, s, wl.f2[s])
+            gpu.set_boundary(m, s, wl.fgeos[s])
+        gpu.set_kp(m, kp)
+    return gpu
+
+
+SWEEPS = [("R", abi.OP_DRIFTR, 0), ("P", abi.OP_DRIFTP, 1), ("E", abi.OP_DRIFTE, 2),
+          ("MU", abi.OP_DRIFTMU, 3)]
+
+
+@pytest.mark.parametrize("name,op,slot", SWEEPS)
+@pytest.mark.parametrize("kp", [3.0, 6.5])
+def test_single_sweep(single, name, op, slot, kp):
+    wl = single
+    o = pyoracle.Oracle(wl.grid, wl.fields)
+    gpu = _setup(wl, kp)
+    vt = o.vt_vols(kp)
+    ref = np.asfortranarray(wl.f2[0]).copy(order="F")
+    dt_ref = o.sweep(name, 0, ref, vt, wl.dts, fgeos=wl.fgeos[0])
+    gpu.apply_op(wl.dts, op, cfl=True)
+    out = gpu.download_f2(0, 0)
+    assert rel(out, ref) <= TOL, f"{name}: {rel(out, ref)}"
+    dt_gpu = gpu.cfl(0, 0)[slot]
+    assert abs(dt_gpu - dt_ref) <= 1e-12 * dt_ref, (dt_gpu, dt_ref)
+
+
+@pytest.mark.parametrize("op,name", [(abi.OP_CHAREXCHANGE, "cex"), (abi.OP_ATMOL, "atmol")])
+def test_losses_ops(tiny, op, name):
+    wl = tiny
+    g = wl.grid
+    o = pyoracle.Oracle(g, wl.fields)
+    gpu = _setup(wl, 3.0)
+    gpu.apply_op(wl.dts, op)
+    for s in range(len(g.species)):
+        ref = np.asfortranarray(wl.f2[s]).copy(order="F")
+        charge, atlos = o.cepara(s, wl.dts)
+        if op == abi.OP_CHAREXCHANGE:
+            o.lib.ro_charexchange(pyoracle.C.byref(o.rg), pyoracle._p(ref), pyoracle._p(charge))
+        else:
+            o.lib.ro_atmol(pyoracle.C.byref(o.rg), pyoracle._p(ref), pyoracle._p(atlos))
+        assert rel(gpu.download_f2(0, s), ref) <= TOL, (name, s)
+
+
+@pytest.mark.parametrize("order", [0, 1])
+def test_half_step(tiny, order):
+    wl = tiny
+    g = wl.grid
+    o = pyoracle.Oracle(g, wl.fields)
+    gpu = _setup(wl, 4.0)
+    vt = o.vt_vols(4.0)
+    gpu.half_step(wl.dts, order)
+    for s in range(len(g.species)):
+        ref = np.asfortranarray(wl.f2[s]).copy(order="F")
+        o.half_step(s, ref, vt, wl.fgeos[s], wl.dts, order)
+        assert rel(gpu.download_f2(0, s), ref) <= TOL, (order, s)
+
+
+def _compare_ram_run(wl, kp, steps=1, flags=0):
+    g = wl.grid
+    o = pyoracle.Oracle(g, wl.fields)
+    gpu = _setup(wl, kp, flags=flags)
+    ref = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    worst = 0.0
+    for step in range(steps):
+        # per-step parity: both start the step from the oracle's state
+        for s in range(len(g.species)):
+            gpu.upload_f2(0, s, ref[s])
+        gpu.ram_run(wl.dts)
+        out = o.ram_run(ref, wl.fgeos, wl.dts, kp=kp, want_flux=True)
+        for s in range(len(g.species)):
+            e = rel(gpu.download_f2(0, s), ref[s])
+            worst = max(worst, e)
+            assert e <= TOL, (step, s, e)
+            pe, pa = gpu.moments(0, s)
+            assert rel(pe, out["ppert"][s]) <= TOL
+            assert rel(pa, out["ppart"][s]) <= TOL
+            assert rel(gpu.flux(0, s), out["flux"][s]) <= TOL
+        dn = gpu.cfl(0, 0)[4]
+        assert abs(dn - out["dts_next"]) <= 1e-12 * out["dts_next"], (dn, out["dts_next"])
+    return worst
+
+
+def test_ram_run_single_species(single):
+    _compare_ram_run(single, 3.0, steps=3)
+
+
+def test_ram_run_four_species_tiny(tiny):
+    _compare_ram_run(tiny, 5.0, steps=3)
+
+
+def test_ram_run_four_species_full(four):
+    _compare_ram_run(four, 2.0, steps=2)
+
+
+def test_strong_convection_inflow_mix(four):
+    """Kp=8: strong E x B makes most outer-boundary lines inflow, exercising
+    the ghost cells and the stale-ghost lines of DRIFTR."""
+    _compare_ram_run(four, 8.0, steps=1)
+
+
+def test_no_nan_and_positive(tiny):
+    gpu = _setup(tiny, 3.0)
+    for _ in range(5):
+        gpu.ram_run(tiny.dts)
+    for s in range(len(tiny.grid.species)):
+        f = gpu.download_f2(0, s)
+        assert np.isfinite(f).all()
+        assert (f >= 0).all()
