@@ -173,7 +173,8 @@ int ramgpu_flux(ramgpu_ctx *ctx, int member, int s, double *flux_s);
  * species of the member (src/ModRamRun.f90:204-205).  out: 5 doubles. */
 int ramgpu_cfl(ramgpu_ctx *ctx, int member, int s, double *out5);
 /* SUMRC bookkeeping (needs RAMGPU_FLAG_LOSSES): SETRC, LSDR, LSCHA, LSATM
- * accumulated since the last ramgpu_reset_losses.  out: 4 doubles. */
+ * accumulated since the last ramgpu_reset_losses, which zeroes the losses
+ * and takes SETRC of the current state as the starting ENOLD.  out: 4 doubles. */
 int ramgpu_losses(ramgpu_ctx *ctx, int member, int s, double *out4);
 int ramgpu_reset_losses(ramgpu_ctx *ctx);
 
@@ -188,6 +189,10 @@ long long ramgpu_launch_count(const ramgpu_ctx *ctx);
  * adds the elapsed times of completed launches into ms[16] and counts[16]
  * (caller-zeroed) and forgets them. */
 #define RAMGPU_NKCLASS 16
+/* Measured FP64 fma throughput of the current device in lane-operations
+ * per second (a dependent-free fma loop over 8 x SMs x 256 threads); the
+ * denominator of the FP64 roofline this path is bound by on GB300. */
+int ramgpu_probe_fp64(double *lane_ops_per_s);
 int ramgpu_set_timing(ramgpu_ctx *ctx, int enable);
 int ramgpu_kernel_times(ramgpu_ctx *ctx, double *ms, long long *counts);
 

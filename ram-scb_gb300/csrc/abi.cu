@@ -266,6 +266,17 @@ static int enqueue_ram_run(ramgpu_ctx* ctx, double dts) {
   return RAMGPU_OK;
 }
 
+// FP64 fma throughput probe: 8 independent chains per thread.
+__global__ void k_probe_dfma(double* out, double a, double b, int iters) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
 // =================================================================== ABI
 extern "C" {
 
@@ -726,11 +737,54 @@ int ramgpu_losses(ramgpu_ctx* ctx, int member, int s, double* out4) {
 int ramgpu_reset_losses(ramgpu_ctx* ctx) {
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
   CK(cudaMemsetAsync(ctx->losses, 0, sizeof(double) * 5 * ctx->d.nm * ctx->d.ns, ctx->stream));
+  // baseline SETRC of the current state (the ENOLD of the next SUMRC)
+  if (ctx->have_grid && ctx->have_fields) {
+    if (ctx->items_dirty) {
+      int rc = rebuild_items(ctx);
+      if (rc) return rc;
+    }
+    if (ctx->d.nitems > 0) {
+      int rc = sumrc_stage(ctx, kSumrcStages - 1, -1);
+      if (rc) return rc;
+    }
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   return RAMGPU_OK;
 }
 
 long long ramgpu_launch_count(const ramgpu_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int ramgpu_probe_fp64(double* lane_ops_per_s) {
+  if (!lane_ops_per_s) return RAMGPU_ERR_ARG;
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return fail(nullptr, RAMGPU_ERR_CUDA, "no CUDA device");
+  const int block = 256, grid = nsm * 8, iters = 4096;
+  double* out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * block * grid) != cudaSuccess)
+    return fail(nullptr, RAMGPU_ERR_NOMEM, "probe allocation failed");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int r = 0; r < 4; ++r) {
+    cudaEventRecord(e0, 0);
+    k_probe_dfma<<<grid, block>>>(out, 0.999999, 1e-7, iters);
+    cudaEventRecord(e1, 0);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (r > 0 && ms < best) best = ms;
+  }
+  cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return fail(nullptr, RAMGPU_ERR_CUDA, cudaGetErrorString(e));
+  *lane_ops_per_s = 8.0 * iters * (double)block * grid / (best * 1e-3);
+  return RAMGPU_OK;
+}
 
 int ramgpu_set_timing(ramgpu_ctx* ctx, int enable) {
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;

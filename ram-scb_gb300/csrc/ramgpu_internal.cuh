@@ -10,10 +10,10 @@
 // One thread advances one line of a sweep; the line is streamed through a
 // rolling register window, so no line buffer is kept.
 //
-// Cost model: on GB300 the FP64 add/mul/fma pipe issues ~0.5 T lane-ops/s
-// while FP64 min/max, integer and FP32 pipes are 16-70x faster, so every
-// sign test, threshold test and select is done on the integer bit pattern
-// and the limiter uses fmin/fmax, leaving 8-9 FP64 add/mul/fma per face.
+// Cost model: on GB300 the FP64 pipe (add/mul/fma, and also FP64 min/max and
+// compares) issues ~0.53 T lane-ops/s while the integer and FP32 pipes are
+// ~35-70x faster, so every sign test, threshold test, min/max and select is
+// done on the integer bit pattern, leaving 8-9 FP64 add/mul/fma per face.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -110,29 +110,49 @@ __device__ __forceinline__ bool same_sign_nonzero(double d, double x) {
   return ((long long)(bd ^ bx) >= 0) && ((bd << 1) != 0) && ((bx << 1) != 0);
 }
 
+// min / max of non-negative doubles on their bit patterns (integer pipe).
+// For x, y >= +0 the IEEE-754 encodings order like the values; FP64
+// fmin/fmax would issue on the slow FP64 pipe.
+__device__ __forceinline__ unsigned long long umin64(unsigned long long a, unsigned long long b) {
+  return a < b ? a : b;
+}
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
+  return a > b ? a : b;
+}
+constexpr unsigned long long kAbsMask = 0x7FFFFFFFFFFFFFFFULL;
+constexpr unsigned long long kSignMask = 0x8000000000000000ULL;
+
 // Flux-limited face value of the reference sweeps (src/ModRamDrift.f90:169-183):
 //   FUP = upwind value; if |X|<=1e-27 or R<=0: FBND=FUP
 //   else FBND = FUP + LIMITER(R)*CORR, LIMITER = max(min(beta R,1),min(R,beta)),
 //        CORR = -0.5*(Cd - s)*X = a*X,  R = D/X.
 // Division-free: for D*X>0, LIMITER*X = sign(X)*max(min(beta|D|,|X|),min(|D|,beta|X|)).
 // bx = beta*|x|, bd = beta*|d| (the neighbour face's bx).  One FP64 fma.
+// The min/max run on bit patterns of the non-negative magnitudes, so a face
+// costs one FP64 fma here.
 __device__ __forceinline__ double face_value(double x, double bx, double d, double bd,
                                              double fup, double a) {
-  double ax = fabs(x), ad = fabs(d);
-  double lx = fmax(fmin(bd, ax), fmin(ad, bx));
-  lx = copysign(lx, x);
+  const unsigned long long ux = dbits(x), ud = dbits(d);
+  const unsigned long long m = umax64(umin64(dbits(bd), ux & kAbsMask), umin64(ud & kAbsMask, dbits(bx)));
+  const double lx = __longlong_as_double((long long)(m | (ux & kSignMask)));
   double fb = fma(a, lx, fup);
   bool act = abs_gt_1em27(x) && same_sign_nonzero(d, x);
   return act ? fb : fup;
 }
+
+// Running CFL quotient max(|C|, floor) as bits (integer max).
+__device__ __forceinline__ unsigned long long cfl_bits(double c, unsigned long long floor_bits) {
+  return umax64(dbits(c) & kAbsMask, floor_bits);
+}
+constexpr unsigned long long kBits1em10 = 0x3DDB7CDFD9D7BDBBULL;  // 1.0E-10
+constexpr unsigned long long kBits1em32 = 0x3949F623D5A8A733ULL;  // 1.0E-32
 
 // F2 < 0 -> 1e-15 (src/ModRamDrift.f90:187-190)
 __device__ __forceinline__ double clip(double v) { return is_neg(v) ? 1E-15 : v; }
 
 // 64-bit max-reduction of a non-negative double across a warp, then one
 // atomicMax on the bit pattern (order-independent, hence deterministic).
-__device__ __forceinline__ void warp_atomic_max(unsigned long long *slot, double q) {
-  unsigned long long v = dbits(q);
+__device__ __forceinline__ void warp_atomic_max(unsigned long long *slot, unsigned long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);

@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(128) k_sweep_r(Dev d, double dts) {
   const int2 item = d.items[blockIdx.y];
   const int m = item.x, s = item.y, slot = m * d.ns + s;
   const int line = blockIdx.x * blockDim.x + threadIdx.x;
-  double q = 0.0;
+  unsigned long long q = 0ULL;  // CFL quotient bits
   if (line < nlines) {
     const int j = line % nt;
     const int l = line / (nt * ne);
@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(128) k_sweep_r(Dev d, double dts) {
     }
     double gm = fl[0], g0 = fl[1], gp = fl[2];
     double c = fma(grt[0], p4, cr[0]);
-    if (kCfl && outside[0] == 0) q = fmax(q, fmax(fabs(c), 1E-10));
+    if (kCfl && outside[0] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
     // face 1: FBND(1) = 0 (outflow) or F(2) (inflow)
     double phi_prev = c * ((inflow && !closed) ? g0 : 0.0);
     double xm = g0 - gm, bxm = beta * fabs(xm);
@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(128) k_sweep_r(Dev d, double dts) {
       const double gpp = (f + 2 <= nr) ? fl[f + 1] : g1;
       const double xp = gpp - gp, bxp = beta * fabs(xp);
       c = fma(grt[f - 1], p4, cr[f - 1]);
-      if (kCfl && outside[f - 1] == 0) q = fmax(q, fmax(fabs(c), 1E-10));
+      if (kCfl && outside[f - 1] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
       const bool neg = is_neg(c);
       const double a = fma(c, -0.5, neg ? -0.5 : 0.5);
       const double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(128) k_sweep_r(Dev d, double dts) {
       xm = x; bxm = bx; x = xp; bx = bxp;
     }
     // face NR (g0 = F(NR), gp = F(NR+1), x = X(NR))
-    if (kCfl && outside[nr - 1] == 0) q = fmax(q, fmax(fabs(cN), 1E-10));
+    if (kCfl && outside[nr - 1] == 0) q = umax64(q, cfl_bits(cN, kBits1em10));
     double fbn;
     if (!inflow) {
       fbn = g0;
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(128) k_sweep_p(Dev d, double dts) {
   const int2 item = d.items[blockIdx.y];
   const int m = item.x, s = item.y, slot = m * d.ns + s;
   const int line = blockIdx.x * blockDim.x + threadIdx.x;
-  double q = 0.0;
+  unsigned long long q = 0ULL;  // CFL quotient bits
   if (line < nlines) {
     const int i = 1 + line % (nr - 1);
     const int kl = line / (nr - 1);
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(128) k_sweep_p(Dev d, double dts) {
     const double XN = G2 - GN, bXN = beta * fabs(XN);
     // face NT first: its flux enters cell 2 through FBND(1)=FBND(NT)
     const double cN = CJ(nt);
-    if (kCfl && outside[(long long)(nt - 1) * nr] == 0) q = fmax(q, fmax(fabs(cN), 1E-10));
+    if (kCfl && outside[(long long)(nt - 1) * nr] == 0) q = umax64(q, cfl_bits(cN, kBits1em10));
     double phiN;
     {
       const bool neg = is_neg(cN);
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(128) k_sweep_p(Dev d, double dts) {
         bxp = bX1;
       }
       const double c = CJ(J);
-      if (kCfl && outside[(long long)(J - 1) * nr] == 0) q = fmax(q, fmax(fabs(c), 1E-10));
+      if (kCfl && outside[(long long)(J - 1) * nr] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
       const bool neg = is_neg(c);
       const double a = fma(c, -0.5, neg ? -0.5 : 0.5);
       const double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(128) k_sweep_e(Dev d, double dts) {
   const int2 item = d.items[blockIdx.y];
   const int m = item.x, s = item.y, slot = m * d.ns + s;
   const int line = blockIdx.x * blockDim.x + threadIdx.x;
-  double q = 0.0;
+  unsigned long long q = 0ULL;  // CFL quotient bits
   if (line < nlines) {
     const int i = 1 + line % (nr - 1);
     const int jl = line / (nr - 1);
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(128) k_sweep_e(Dev d, double dts) {
     double phi_prev;
     {
       const double c = CK(1);
-      if (kCfl && inside) q = fmax(q, fmax(fabs(c), 1E-10) * d.ide[0]);
+      if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em10)) * d.ide[0]));
       const bool neg = is_neg(c);
       const double a = fma(c, mhde[0], neg ? -0.5 : 0.5);
       double fb = face_value(X1, bX1, neg ? X2 : X0, neg ? bX2 : bX0, neg ? G2 : G1, a);
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(128) k_sweep_e(Dev d, double dts) {
       const double gpp = (K + 2 <= ne) ? GK(K + 2) : 0.0;
       const double xp = gpp - gp, bxp = beta * fabs(xp);
       const double c = CK(K);
-      if (kCfl && inside) q = fmax(q, fmax(fabs(c), 1E-10) * d.ide[K - 1]);
+      if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em10)) * d.ide[K - 1]));
       const bool neg = is_neg(c);
       const double a = fma(c, mhde[K - 1], neg ? -0.5 : 0.5);
       double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(128) k_sweep_mu(Dev d, double dts, const doubl
   const int2 item = d.items[blockIdx.y];
   const int m = item.x, s = item.y, slot = m * d.ns + s;
   const int line = blockIdx.x * blockDim.x + threadIdx.x;
-  double q = 0.0;
+  unsigned long long q = 0ULL;  // CFL quotient bits
   if (line < nlines) {
     const int i = 1 + line % (nr - 1);
     const int jk = line / (nr - 1);
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(128) k_sweep_mu(Dev d, double dts, const doubl
       if (kLoss == 2) gpp *= LA(L + 2);
       const double xp = gpp - gp, bxp = beta * fabs(xp);
       const double c = CL(L);
-      if (kCfl && inside) q = fmax(q, fmax(fabs(c), 1E-32) * d.idmu[L - 1]);
+      if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
       const bool neg = is_neg(c);
       const double a = fma(c, mhdmu[L - 1], neg ? -0.5 : 0.5);
       const double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(128) k_sweep_mu(Dev d, double dts, const doubl
     {
       const int L = npa - 1;
       const double c = CL(L);
-      if (kCfl && inside) q = fmax(q, fmax(fabs(c), 1E-32) * d.idmu[L - 1]);
+      if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
       const double phi = c * (closed ? 0.0 : gp);
       const double v = clip(fma(phi_prev - phi, iwmu[L - 1], g0));
       const double vN = v * d.rho[fij];
@@ -326,21 +326,21 @@ void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st) {
   else k_sweep_p<false><<<g, 128, 0, st>>>(d, dts);
 }
 void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st) {
-  dim3 g = grid_for((d.nr - 1) * d.nt * d.npa, d.nitems, 128);
-  if (cfl) k_sweep_e<true><<<g, 128, 0, st>>>(d, dts);
-  else k_sweep_e<false><<<g, 128, 0, st>>>(d, dts);
+  dim3 g = grid_for((d.nr - 1) * d.nt * d.npa, d.nitems, 64);
+  if (cfl) k_sweep_e<true><<<g, 64, 0, st>>>(d, dts);
+  else k_sweep_e<false><<<g, 64, 0, st>>>(d, dts);
 }
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
                      cudaStream_t st) {
-  dim3 g = grid_for((d.nr - 1) * d.nt * d.ne, d.nitems, 128);
+  dim3 g = grid_for((d.nr - 1) * d.nt * d.ne, d.nitems, 64);
   if (cfl) {
-    if (loss_mode == 1) k_sweep_mu<true, 1><<<g, 128, 0, st>>>(d, dts, loss);
-    else if (loss_mode == 2) k_sweep_mu<true, 2><<<g, 128, 0, st>>>(d, dts, loss);
-    else k_sweep_mu<true, 0><<<g, 128, 0, st>>>(d, dts, nullptr);
+    if (loss_mode == 1) k_sweep_mu<true, 1><<<g, 64, 0, st>>>(d, dts, loss);
+    else if (loss_mode == 2) k_sweep_mu<true, 2><<<g, 64, 0, st>>>(d, dts, loss);
+    else k_sweep_mu<true, 0><<<g, 64, 0, st>>>(d, dts, nullptr);
   } else {
-    if (loss_mode == 1) k_sweep_mu<false, 1><<<g, 128, 0, st>>>(d, dts, loss);
-    else if (loss_mode == 2) k_sweep_mu<false, 2><<<g, 128, 0, st>>>(d, dts, loss);
-    else k_sweep_mu<false, 0><<<g, 128, 0, st>>>(d, dts, nullptr);
+    if (loss_mode == 1) k_sweep_mu<false, 1><<<g, 64, 0, st>>>(d, dts, loss);
+    else if (loss_mode == 2) k_sweep_mu<false, 2><<<g, 64, 0, st>>>(d, dts, loss);
+    else k_sweep_mu<false, 0><<<g, 64, 0, st>>>(d, dts, nullptr);
   }
 }
 

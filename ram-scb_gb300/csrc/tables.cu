@@ -328,25 +328,34 @@ void launch_member_coef(const Dev& d, double dts, cudaStream_t st) {
 }
 
 // ---------------------------------------------------- DRIFTR ghost planes
-// Plane p = (K-1)*NPA + (L-1) in the reference's K->L loop order.
+// Plane p = (K-1)*NPA + (L-1) in the reference's K->L loop order.  One warp
+// per plane: lanes test 32 lines J at a time from the top, a ballot finds
+// the highest inflow J.
 __global__ void k_ghost_planes(Dev d) {
   const int np = d.ne * d.npa;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int2 item = d.items[blockIdx.y];
   const int m = item.x, s = item.y, slot = m * d.ns + s;
-  if (p >= np) return;
+  if (p >= np) return;  // uniform per warp
   const int k = p / d.npa, l = p % d.npa;
   const double p4 = d.p4[s * d.ne + k];
   int has = 0;
   double v = 0.0;
-  for (int jj = d.nt - 1; jj >= 0; --jj)
-    if (inflow_line(d, m, jj, l, p4)) {
+  for (int top = d.nt - 1; top >= 0; top -= 32) {
+    const int jj = top - lane;
+    const bool inf = jj >= 0 && inflow_line(d, m, jj, l, p4);
+    const unsigned b = __ballot_sync(0xffffffffu, inf);
+    if (b) {
       has = 1;
-      v = ghost_value(d, slot, jj, k, l, d.conf1);
+      v = ghost_value(d, slot, top - (__ffs(b) - 1), k, l, d.conf1);
       break;
     }
-  d.plane_has[(long long)slot * np + p] = has;
-  d.plane_last[(long long)slot * np + p] = v;
+  }
+  if (lane == 0) {
+    d.plane_has[(long long)slot * np + p] = has;
+    d.plane_last[(long long)slot * np + p] = v;
+  }
 }
 
 // Exclusive "last defined" scan over planes: one block per work item.
@@ -390,7 +399,7 @@ __global__ void __launch_bounds__(1024) k_ghost_scan(Dev d) {
 
 void launch_ghost(const Dev& d, cudaStream_t st) {
   const int np = d.ne * d.npa;
-  k_ghost_planes<<<dim3((np + 127) / 128, d.nitems), 128, 0, st>>>(d);
+  k_ghost_planes<<<dim3((np + 3) / 4, d.nitems), 128, 0, st>>>(d);
   k_ghost_scan<<<d.nitems, 1024, 0, st>>>(d);
 }
 

@@ -30,7 +30,7 @@ EXPORTS = (
     "ramgpu_upload_f2_all", "ramgpu_download_f2_all", "ramgpu_f2_device_ptr",
     "ramgpu_ram_run", "ramgpu_half_step", "ramgpu_ram_run_async", "ramgpu_moments",
     "ramgpu_flux", "ramgpu_cfl", "ramgpu_losses", "ramgpu_reset_losses", "ramgpu_launch_count",
-    "ramgpu_apply_op", "ramgpu_set_timing", "ramgpu_kernel_times",
+    "ramgpu_apply_op", "ramgpu_set_timing", "ramgpu_kernel_times", "ramgpu_probe_fp64",
 )
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
           "anisch", "dts_tables", "sumrc")
@@ -107,6 +107,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_apply_op": ([vp, d, i, i], i),
         "ramgpu_set_timing": ([vp, i], i),
         "ramgpu_kernel_times": ([vp, dp, C.POINTER(C.c_longlong)], i),
+        "ramgpu_probe_fp64": ([dp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -115,6 +116,16 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
     if path is None:
         _lib = lib
     return lib
+
+
+def probe_fp64() -> float:
+    """FP64 fma lane-operations per second of the current GPU."""
+    lib = load_library()
+    v = C.c_double()
+    rc = lib.ramgpu_probe_fp64(C.byref(v))
+    if rc != RAMGPU_OK:
+        raise RamGpuError(f"ramgpu_probe_fp64: {ERRORS.get(rc, rc)}")
+    return v.value
 
 
 def _dptr(a: np.ndarray):

@@ -360,6 +360,45 @@ def dipole_fields(g: Grid, seed: int = 1234, hdns_sigma: float = 0.1) -> Fields:
                   outside=np.zeros((g.nr, nt), dtype=np.int32))
 
 
+def perturbed_fields(g: Grid, seed: int = 99, compress: float = 0.15, efield: float = 2e-4,
+                     rates: float = 1.0, outside_cells: int = 3) -> Fields:
+    """Non-dipole tables that switch on every term the dipole zeroes: a
+    day-night compressed B and h/I (so the gradient-curvature drift and its
+    J derivatives are nonzero), seeded induced fields EIR/EIP [V/m], time
+    derivatives dBdt, dIdt, dIbndt, and a few outer cells outside the
+    magnetopause.  Used to exercise the DRIFTR stale-ghost lines and the
+    magnetopause paths."""
+    f = dipole_fields(g, seed=seed)
+    nf, nt, npa = g.nr + 1, g.nt, g.npa
+    rng = np.random.Generator(np.random.PCG64(seed + 1))
+    lz = g.lz[:, None]
+    cphi = np.cos(g.phi)[None, :]
+    bfac = 1.0 + compress * cphi * (lz / 6.5) ** 3
+    f.bnes = f.bnes * bfac
+    hfac = (1.0 + 0.5 * compress * cphi[:, :, None] * (lz[:, :, None] / 6.5) ** 2
+            * (1.0 - g.mu[None, None, :] ** 2))
+    for k in ("fnhs", "fnis", "bounhs", "bounis"):
+        setattr(f, k, getattr(f, k) * hfac)
+    smooth = lambda a: 0.5 * (a + np.roll(a, 1, axis=1))  # noqa: E731
+    f.eir = efield * smooth(rng.standard_normal((nf, nt)))
+    f.eip = efield * smooth(rng.standard_normal((nf, nt)))
+    f.dbdt = rates * 1e-12 * smooth(rng.standard_normal((nf, nt)))
+    f.didt = rates * 1e-6 * rng.standard_normal((nf, nt, npa))
+    f.dibndt = rates * 1e-6 * rng.standard_normal((nf, nt, npa))
+    for k in ("bnes", "eir", "eip", "dbdt"):
+        a = getattr(f, k)
+        a[:, nt - 1] = a[:, 0]
+    for k in ("fnhs", "fnis", "bounhs", "bounis", "didt", "dibndt"):
+        a = getattr(f, k)
+        a[:, nt - 1, :] = a[:, 0, :]
+    out = np.zeros((g.nr, nt), dtype=np.int32)
+    jmid = (nt - 1) // 2  # noon side
+    for c in range(outside_cells):
+        out[g.nr - 1, (jmid + c) % (nt - 1)] = 1
+    f.outside = out
+    return f
+
+
 # ------------------------------------------------------------------ state
 def kappa_flux(e_kev, kt=5.0, kappa=3.0, amp=1.0e5):
     """Kappa differential flux [1/cm2/s/sr/keV] (shape only; amp sets scale)."""
@@ -432,6 +471,8 @@ def make_workload(name: str, seed: int = 2024) -> Workload:
       four_sp    : e-,H+,He+,O+, 20x25x35x72, Kp 1->6 over 4320 steps, dt=5 s
       refined    : four species, 40x49x70x144, Kp 1->6, dt=2.5 s, 1440 steps
       tiny       : four species on a reduced 6x9x35x72 grid (tests)
+      tiny_pert  : tiny with perturbed_fields (non-dipole, E_ind, dB/dt,
+                   magnetopause cells) for coverage of the zero-in-dipole terms
     """
     if name == "single_h":
         sp = [HYDROGEN]
@@ -439,9 +480,9 @@ def make_workload(name: str, seed: int = 2024) -> Workload:
         params = [(5.0, 1.0)]
         kp = lambda step: 3.0  # noqa: E731
         dts, steps = 5.0, 720
-    elif name in ("four_sp", "tiny"):
+    elif name in ("four_sp", "tiny", "tiny_pert"):
         sp = [SPECIES[c] for c, _, _ in FOUR_SPECIES]
-        if name == "tiny":
+        if name in ("tiny", "tiny_pert"):
             g = arrays(6, 9, 35, 72, species=tuple(sp), mu_grid_nr=20)
         else:
             g = arrays(20, 25, 35, 72, species=tuple(sp))
@@ -458,7 +499,7 @@ def make_workload(name: str, seed: int = 2024) -> Workload:
         dts = 2.5
     else:
         raise ValueError(f"unknown workload {name!r}")
-    fl = dipole_fields(g, seed=seed)
+    fl = perturbed_fields(g, seed=seed) if name == "tiny_pert" else dipole_fields(g, seed=seed)
     f2 = [initial_f2(g, fl, s, seed=seed + 17 * (s + 1), kt=params[s][0], density_scale=params[s][1])
           for s in range(len(sp))]
     fg = [boundary_fgeos(g, s, kt=params[s][0], density_scale=params[s][1]) for s in range(len(sp))]

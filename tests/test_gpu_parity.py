@@ -66,6 +66,25 @@ def test_single_sweep(single, name, op, slot, kp):
     assert abs(dt_gpu - dt_ref) <= 1e-12 * dt_ref, (dt_gpu, dt_ref)
 
 
+@pytest.mark.parametrize("name,op,slot", SWEEPS)
+@pytest.mark.parametrize("kp,dts", [(3.0, 5.0), (8.0, 1.0)])
+def test_single_sweep_four_species(four, name, op, slot, kp, dts):
+    """Each sweep for e-, H+, He+, O+ (charge sign and mass enter the
+    gradient-curvature and energy terms)."""
+    wl = four
+    o = pyoracle.Oracle(wl.grid, wl.fields)
+    gpu = _setup(wl, kp)
+    vt = o.vt_vols(kp)
+    gpu.apply_op(dts, op, cfl=True)
+    for s in range(len(wl.grid.species)):
+        ref = np.asfortranarray(wl.f2[s]).copy(order="F")
+        dt_ref = o.sweep(name, s, ref, vt, dts, fgeos=wl.fgeos[s])
+        e = rel(gpu.download_f2(0, s), ref)
+        assert e <= TOL, (name, s, e)
+        dt_gpu = gpu.cfl(0, s)[slot]
+        assert abs(dt_gpu - dt_ref) <= 1e-12 * dt_ref, (name, s, dt_gpu, dt_ref)
+
+
 @pytest.mark.parametrize("op,name", [(abi.OP_CHAREXCHANGE, "cex"), (abi.OP_ATMOL, "atmol")])
 def test_losses_ops(tiny, op, name):
     wl = tiny
@@ -97,8 +116,9 @@ def test_half_step(tiny, order):
         assert rel(gpu.download_f2(0, s), ref) <= TOL, (order, s)
 
 
-def _compare_ram_run(wl, kp, steps=1, flags=0):
+def _compare_ram_run(wl, kp, steps=1, flags=0, dts=None):
     g = wl.grid
+    dts = wl.dts if dts is None else dts
     o = pyoracle.Oracle(g, wl.fields)
     gpu = _setup(wl, kp, flags=flags)
     ref = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
@@ -107,8 +127,11 @@ def _compare_ram_run(wl, kp, steps=1, flags=0):
         # per-step parity: both start the step from the oracle's state
         for s in range(len(g.species)):
             gpu.upload_f2(0, s, ref[s])
-        gpu.ram_run(wl.dts)
-        out = o.ram_run(ref, wl.fgeos, wl.dts, kp=kp, want_flux=True)
+        gpu.ram_run(dts)
+        out = o.ram_run(ref, wl.fgeos, dts, kp=kp, want_flux=True)
+        # the scheme is run inside its stability limit, as the reference's
+        # driver ensures through DtsNext (src/ModRamScbRun.f90:49-61)
+        assert dts <= out["dts_next"] / 0.8 + 1e-12
         for s in range(len(g.species)):
             e = rel(gpu.download_f2(0, s), ref[s])
             worst = max(worst, e)
@@ -136,8 +159,9 @@ def test_ram_run_four_species_full(four):
 
 def test_strong_convection_inflow_mix(four):
     """Kp=8: strong E x B makes most outer-boundary lines inflow, exercising
-    the ghost cells and the stale-ghost lines of DRIFTR."""
-    _compare_ram_run(four, 8.0, steps=1)
+    the ghost cells and the stale-ghost lines of DRIFTR.  DTs=1 s, the step
+    the reference's driver takes for Kp>6 (src/ModRamScbRun.f90:57-59)."""
+    _compare_ram_run(four, 8.0, steps=2, dts=1.0)
 
 
 def test_no_nan_and_positive(tiny):

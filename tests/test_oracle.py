@@ -1,0 +1,361 @@
+"""Pinning the CPU oracle without the Fortran reference.
+
+The reference ships no per-routine golden vectors for this path and no
+Fortran compiler is available, so the C oracle is pinned by
+  * known values of the ARRAYS grid (src/ModRamInit.f90:392-583),
+  * exact properties: identity at zero drift, phi periodicity, closed-face
+    conservation, the ANISCH L=1 side effect,
+  * an independent pure-Python restatement of the sweep line updates of
+    src/ModRamDrift.f90 (written from the Fortran text, including DRIFTR's
+    F(NR+1:NR+2) persistence across lines), which must agree with the C
+    oracle bit for bit and exercise every limiter branch,
+  * an independent NumPy evaluation of the CEPARA cross sections.
+"""
+import dataclasses
+import math
+
+import numpy as np
+import pytest
+
+from ramgpu import workload as W
+import pyoracle
+
+
+@pytest.fixture(scope="module")
+def tiny():
+    return W.make_workload("tiny")
+
+
+@pytest.fixture(scope="module")
+def tiny_pert():
+    return W.make_workload("tiny_pert")
+
+
+@pytest.fixture(scope="module")
+def std_grid():
+    return W.arrays(20, 25, 35, 72, species=(W.HYDROGEN,))
+
+
+# ------------------------------------------------------------------ ARRAYS
+def test_arrays_known_values(std_grid):
+    g = std_grid
+    assert g.we[0] == 3e-2 and g.ekev[0] == 0.1 + 0.5 * 3e-2 and g.ebnd[0] == 0.1 + 3e-2
+    assert g.we[1] == 3e-2 * 1.27
+    assert g.de[34] == 0.5 * g.we[34] * (1. + 1.27)
+    assert g.mu[0] == 0.0 and g.mu[71] == 1.0 and g.wmu[0] == 1.0 / 32
+    assert g.pa[47] == 18.7 and g.pa[49] == 16.0 and g.pa[71] == 0.0
+    assert list(g.pa[68:72]) == [2.5, 1.5, 1.0, 0.0]
+    assert g.dl1 == 0.25 and g.lz[0] == 1.75 and g.lz[20] == 6.75
+    assert g.conf1 == ((6.5 + 0.25) / 6.5) ** 2
+    assert g.dphi == 2 * math.pi / 24
+    assert np.all(np.diff(g.mu) > 0) and np.all(g.wmu > 0)
+    assert np.all(np.diff(g.upa) >= 0) and g.upa.min() >= 2
+    assert np.array_equal(g.ffactor[:, :, :, 0], g.ffactor[:, :, :, 1])
+    # ERNH/EPP (src/ModRamInit.f90:573-577)
+    gr = g.grel[0, 5]
+    assert g.ernh[0, 5] == g.we[5] * gr / math.sqrt((gr - 1.) * (gr + 1.))
+
+
+def test_refined_grid_shape():
+    g = W.refined_arrays(40, 49, 70, 144, species=(W.HYDROGEN,))
+    assert g.mu.size == 144 and g.ekev.size == 70
+    assert np.all(np.diff(g.mu) > 0) and np.all(g.wmu > 0) and np.all(g.dmu > 0)
+    assert abs(g.ebnd[-1] - 400.0) / 400.0 < 0.2
+    assert abs(g.we[0] + g.we[1] - 3e-2) < 1e-15
+
+
+# ------------------------------------------------------- exact properties
+def test_zero_drift_is_identity(tiny):
+    """VT = 0, EIP = 0 and J-independent dipole tables make CDriftR vanish up
+    to the rounding of the CGR1 sum ((a+b)-a)-b, so DRIFTR leaves F2
+    unchanged to 1e-14 of its maximum."""
+    wl = tiny
+    o = pyoracle.Oracle(wl.grid, wl.fields)
+    f2 = np.asfortranarray(wl.f2[1]).copy(order="F")
+    before = f2.copy(order="F")
+    vt = np.zeros((wl.grid.nr + 1, wl.grid.nt), order="F")
+    cd = np.zeros_like(f2, order="F")
+    o.sweep("R", 1, f2, vt, wl.dts, fgeos=wl.fgeos[1], cdrift=cd)
+    assert np.max(np.abs(cd)) < 1e-14
+    assert np.max(np.abs(f2 - before)) <= 1e-14 * np.max(before)
+
+
+def test_driftp_periodic(tiny):
+    wl = tiny
+    o = pyoracle.Oracle(wl.grid, wl.fields)
+    f2 = np.asfortranarray(wl.f2[1]).copy(order="F")
+    o.sweep("P", 1, f2, o.vt_vols(4.0), wl.dts)
+    assert np.array_equal(f2[1:, 0], f2[1:, -1])
+
+
+def test_anisch_side_effect(tiny):
+    wl = tiny
+    o = pyoracle.Oracle(wl.grid, wl.fields)
+    f2 = np.asfortranarray(wl.f2[2]).copy(order="F")
+    f2[:, :, :, 0] = -7.0
+    pe, pa = o.anisch(2, f2)
+    assert np.array_equal(f2[1:, :, 1:, 0], f2[1:, :, 1:, 1])
+    assert np.all(f2[0, :, :, 0] == -7.0) and np.all(f2[:, :, 0, 0] == -7.0)
+    assert np.all(pe[1:] > 0) and np.all(pa[1:] > 0)
+
+
+def _closed_species(grid):
+    sp = tuple(dataclasses.replace(s, cex_kind=W.CEX_NONE) for s in grid.species)
+    return dataclasses.replace(grid, species=sp)
+
+
+def content_q(g, f2):
+    w = g.we[None, None, 1:, None] * g.wmu[None, None, None, 1:-1]
+    return float(np.sum(f2[1:, :-1, 1:, 1:-1] * w))
+
+
+def test_closed_conservation_oracle(tiny):
+    wl = tiny
+    g = _closed_species(wl.grid)
+    o = pyoracle.Oracle(g, wl.fields)
+    f2 = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    q0 = [content_q(g, a) for a in f2]
+    for step in range(3):
+        o.ram_run(f2, wl.fgeos, 1.0, kp=4.0, closed=True, do_atmol=False)
+    for s in range(len(f2)):
+        assert abs(content_q(g, f2[s]) - q0[s]) <= 1e-13 * q0[s], s
+
+
+def test_cex_against_numpy(tiny):
+    wl = tiny
+    g = wl.grid
+    o = pyoracle.Oracle(g, wl.fields)
+    coefs = {1: (-18.767, -0.11017, -3.8173e-2, -0.1232, -5.0488e-2),
+             2: (-20.789, 0.92316, -0.68017, 0.66153, -0.20998),
+             3: (-18.987, -0.10613, -5.4841E-3, -1.6262E-2, -7.0554E-3)}
+    for s, sp in enumerate(g.species):
+        charge, atlos = o.cepara(s, wl.dts)
+        if sp.cex_kind == 0:
+            assert np.all(charge == 1.0)
+            continue
+        x = np.maximum(np.log10(g.ekev), -2.0)
+        c = coefs[sp.cex_kind]
+        y = c[0] + c[1] * x + c[2] * x ** 2 + c[3] * x ** 3 + c[4] * x ** 4
+        sig_v = 10.0 ** y * g.v[s]
+        hd = wl.fields.hdns[:g.nr]                              # (I, J, L)
+        ref = np.exp(-(sig_v[None, None, :, None] * hd[:, :, None, :] * wl.dts))
+        np.testing.assert_allclose(charge[1:, :, 1:, 1:], ref[1:, :, 1:, 1:], rtol=1e-13, atol=0)
+        assert np.all(charge[0] == 1.0) and np.all(charge[:, :, 0] == 1.0) and np.all(charge[..., 0] == 1.0)
+        taub = 2 * g.rlz[:g.nr, None] / g.v[s][None, :]
+        np.testing.assert_allclose(atlos[1:, 1:], np.exp(-wl.dts / taub)[1:, 1:], rtol=1e-14)
+
+
+# ------------------------------------ independent restatement of the sweeps
+BETA = 1.5
+
+
+def _face(F, I, s, X, C, beta, counts, I1=None, N=None):
+    """FBND(I) for the reference's limiter block, literal.  I1 is the right
+    cell (I+1, or the periodic J1) and N the upwind index."""
+    I1 = I + 1 if I1 is None else I1
+    FUP = 0.5 * (F[I] + F[I1] - s * X)
+    if abs(X) <= 1.e-27:
+        counts["small"] += 1
+        return FUP
+    if N is None:
+        N = I + 1 - s
+    R = (F[N] - F[N - 1]) / X
+    if R <= 0:
+        counts["fup"] += 1
+        return FUP
+    a, b = min(beta * R, 1.), min(R, beta)
+    LIM = max(a, b)
+    counts["betaR" if LIM == beta * R and beta * R < 1 else
+           "one" if LIM == 1. and R <= 1 else
+           "R" if LIM == R and R < beta else "beta"] += 1
+    CORR = -0.5 * (C - s) * X
+    return FUP + LIM * CORR
+
+
+def python_driftr(g, f2, cd, fgeos, fnhs, outside, counts):
+    """DRIFTR line updates with F(NR+1:NR+2) persisting across lines
+    (src/ModRamDrift.f90:130-194); 1-based lists, C from the oracle's CDriftR."""
+    NR, NT, NE, NPA = f2.shape
+    out = f2.copy(order="F")
+    F = [0.0] * (NR + 3)
+    for K in range(NE):
+        for L in range(NPA):
+            for J in range(NT):
+                for I in range(NR):
+                    F[I + 1] = float(f2[I, J, K, L])
+                C = [0.0] + [float(cd[I, J, K, L]) for I in range(NR)]
+                sgn = [0] + [(-1 if C[I] < 0 else 1) for I in range(1, NR + 1)]
+                FB = [0.0] * (NR + 1)
+                if sgn[NR] == 1:
+                    FB[1] = 0.
+                    FB[NR] = F[NR]
+                    UR = NR - 1
+                else:
+                    FB[1] = F[2]
+                    UR = NR
+                    if outside[NR - 1, J] == 1:
+                        F[NR + 1] = 0.
+                        F[NR + 2] = 0.
+                    else:
+                        F[NR + 1] = fgeos[J, K, L] * g.conf1 * fnhs[NR - 1, J, L]
+                        F[NR + 2] = fgeos[J, K, L] * g.conf2 * fnhs[NR - 1, J, L]
+                for I in range(2, UR + 1):
+                    FB[I] = _face(F, I, sgn[I], F[I + 1] - F[I], C[I], BETA, counts)
+                for I in range(2, NR + 1):
+                    v = f2[I - 1, J, K, L] - C[I] * FB[I] + C[I - 1] * FB[I - 1]
+                    out[I - 1, J, K, L] = 1E-15 if v < 0 else v
+    return out
+
+
+def python_driftmu(g, f2, cd, fnhs, counts):
+    """DRIFTMU line updates (src/ModRamDrift.f90:406-467) from CDriftMu."""
+    NR, NT, NE, NPA = f2.shape
+    out = f2.copy(order="F")
+    for K in range(NE):
+        for J in range(NT):
+            for I in range(1, NR):
+                F = [0.0] + [float(f2[I, J, K, L]) for L in range(NPA)]
+                F[1] = F[2]
+                C = [0.0] + [float(cd[I, J, K, L]) for L in range(NPA)]
+                FB = [0.0] * (NPA + 1)
+                for L in range(2, NPA - 1):
+                    s = -1 if C[L] < 0.0 else 1
+                    FB[L] = _face(F, L, s, F[L + 1] - F[L], C[L] / g.dmu[L - 1], BETA, counts)
+                C[1] = 0.
+                FB[1] = 0.
+                FB[NPA - 1] = F[NPA]
+                for L in range(2, NPA):
+                    v = (f2[I, J, K, L - 1] - C[L] / g.wmu[L - 1] * FB[L]
+                         + C[L - 1] / g.wmu[L - 1] * FB[L - 1])
+                    out[I, J, K, L - 1] = 1E-15 if v < 0 else v
+                out[I, J, K, NPA - 1] = (out[I, J, K, NPA - 2] * fnhs[I, J, NPA - 1] * g.mu[NPA - 1]
+                                         / fnhs[I, J, NPA - 2] / g.mu[NPA - 2])
+    return out
+
+
+def python_driftp(g, f2, cd, counts):
+    """DRIFTP line updates with the periodic wrap (src/ModRamDrift.f90:225-273)."""
+    NR, NT, NE, NPA = f2.shape
+    out = f2.copy(order="F")
+    for L in range(NPA):
+        for K in range(NE):
+            for I in range(1, NR):
+                F = [0.0] + [float(f2[I, J, K, L]) for J in range(NT)]
+                C = [0.0] + [float(cd[I, J, K, L]) for J in range(NT)]
+                FB = [0.0] * (NT + 1)
+                for J in range(2, NT + 1):
+                    J1 = 2 if J == NT else J + 1
+                    s = -1 if C[J] < 0 else 1
+                    N = J + 1 - s
+                    if N > NT:
+                        N = N - NT + 1
+                    FB[J] = _face(F, J, s, F[J1] - F[J], C[J], BETA, counts, I1=J1, N=N)
+                C[1] = C[NT]
+                FB[1] = FB[NT]
+                for J in range(2, NT + 1):
+                    v = f2[I, J - 1, K, L] - C[J] * FB[J] + C[J - 1] * FB[J - 1]
+                    out[I, J - 1, K, L] = 1E-15 if v < 0 else v
+                out[I, 0, K, L] = out[I, NT - 1, K, L]
+    return out
+
+
+def python_drifte(g, s_idx, f2, cd, counts):
+    """DRIFTE line updates with the extrapolated F(0), F(1) and zero F(NE+1:NE+2)
+    (src/ModRamDrift.f90:305-370)."""
+    NR, NT, NE, NPA = f2.shape
+    out = f2.copy(order="F")
+    grel = g.grel[s_idx]
+    EZERO = g.ekev[0] - g.we[0]
+    GRZERO = 1. + EZERO * 1000. * W.Q / g.rmas[s_idx] / W.CS / W.CS
+    for J in range(NT):
+        for I in range(1, NR):
+            for L in range(NPA):
+                F = [0.0] * (NE + 3)
+                for K in range(NE):
+                    F[K + 1] = float(f2[I, J, K, L])
+                F[1] = F[2] * grel[0] / grel[1] * math.sqrt((grel[1] ** 2 - 1) / (grel[0] ** 2 - 1))
+                F[0] = F[1] * GRZERO / grel[0] * math.sqrt((grel[0] ** 2 - 1) / (GRZERO ** 2 - 1))
+                C = [0.0] + [float(cd[I, J, K, L]) for K in range(NE)]
+                FB = [0.0] * (NE + 1)
+                for K in range(1, NE + 1):
+                    s = -1 if C[K] < 0 else 1
+                    FB[K] = _face(F, K, s, F[K + 1] - F[K], C[K] / g.de[K - 1], BETA, counts)
+                for K in range(2, NE + 1):
+                    v = (f2[I, J, K - 1, L] - C[K] / g.we[K - 1] * FB[K]
+                         + C[K - 1] / g.we[K - 1] * FB[K - 1])
+                    out[I, J, K - 1, L] = 1E-15 if v < 0 else v
+    return out
+
+
+@pytest.mark.parametrize("which", ["P", "E"])
+@pytest.mark.parametrize("name", ["tiny", "tiny_pert"])
+def test_driftp_drifte_match_independent_restatement(which, name, tiny, tiny_pert):
+    wl = {"tiny": tiny, "tiny_pert": tiny_pert}[name]
+    g = wl.grid
+    o = pyoracle.Oracle(g, wl.fields)
+    s = 3
+    f2 = np.asfortranarray(wl.f2[s]).copy(order="F")
+    cd = np.zeros_like(f2, order="F")
+    f_in = f2.copy(order="F")
+    o.sweep(which, s, f2, o.vt_vols(5.0), wl.dts, cdrift=cd)
+    counts = {k: 0 for k in ("small", "fup", "betaR", "one", "R", "beta")}
+    if which == "P":
+        ref = python_driftp(g, f_in, cd, counts)
+    else:
+        ref = python_drifte(g, s, f_in, cd, counts)
+    assert np.array_equal(f2[1:], ref[1:])
+    assert counts["fup"] > 0 and counts["R"] + counts["one"] + counts["betaR"] + counts["beta"] > 0
+
+
+@pytest.mark.parametrize("name,kp", [("tiny", 7.0), ("tiny_pert", 4.0)])
+def test_driftr_matches_independent_restatement(name, kp, tiny, tiny_pert):
+    wl = {"tiny": tiny, "tiny_pert": tiny_pert}[name]
+    g = wl.grid
+    o = pyoracle.Oracle(g, wl.fields)
+    s = 1
+    # a potential strong enough that both inflow and outflow lines exist
+    vt = o.vt_vols(kp)
+    f2 = np.asfortranarray(wl.f2[s]).copy(order="F")
+    cd = np.zeros_like(f2, order="F")
+    f_in = f2.copy(order="F")
+    o.sweep("R", s, f2, vt, wl.dts, fgeos=wl.fgeos[s], cdrift=cd)
+    counts = {k: 0 for k in ("small", "fup", "betaR", "one", "R", "beta")}
+    ref = python_driftr(g, f_in, cd, wl.fgeos[s], wl.fields.fnhs, wl.fields.outside, counts)
+    assert np.array_equal(f2, ref)
+    for k in ("fup", "betaR", "one", "R", "beta"):
+        assert counts[k] > 0, counts
+    # both boundary cases occur
+    assert (cd[-1] < 0).any() and (cd[-1] >= 0).any()
+
+
+def test_stale_ghost_scenario_exercised(tiny_pert):
+    """Lines that are outflow at NR but upwinded from the right at NR-1 read
+    F(NR+1) left by the previous inflow line.  With the non-dipole tables
+    such lines exist, so the bitwise match of the restatement above covers
+    them (with the pure dipole the sign of CDriftR depends on J only)."""
+    wl = tiny_pert
+    g = wl.grid
+    o = pyoracle.Oracle(g, wl.fields)
+    vt = o.vt_vols(4.0)
+    f2 = np.asfortranarray(wl.f2[1]).copy(order="F")
+    cd = np.zeros_like(f2, order="F")
+    o.sweep("R", 1, f2, vt, wl.dts, fgeos=wl.fgeos[1], cdrift=cd)
+    stale = (cd[-1] >= 0) & (cd[-2] < 0)
+    inflow = cd[-1] < 0
+    assert stale.any() and inflow.any()
+
+
+@pytest.mark.parametrize("name", ["tiny", "tiny_pert"])
+def test_driftmu_matches_independent_restatement(name, tiny, tiny_pert):
+    wl = {"tiny": tiny, "tiny_pert": tiny_pert}[name]
+    g = wl.grid
+    o = pyoracle.Oracle(g, wl.fields)
+    s = 2
+    f2 = np.asfortranarray(wl.f2[s]).copy(order="F")
+    cd = np.zeros_like(f2, order="F")
+    f_in = f2.copy(order="F")
+    o.sweep("MU", s, f2, o.vt_vols(4.0), wl.dts, cdrift=cd)
+    counts = {k: 0 for k in ("small", "fup", "betaR", "one", "R", "beta")}
+    ref = python_driftmu(g, f_in, cd, wl.fields.fnhs, counts)
+    assert np.array_equal(f2[1:], ref[1:])
+    assert counts["fup"] > 0 and counts["R"] + counts["one"] + counts["betaR"] + counts["beta"] > 0
