@@ -1,0 +1,127 @@
+!==============================================================================
+! ModRamGpu -- iso_c_binding interface of the GB300 RAM kinetic step
+! (include/ramgpu.h).  A RAM-SCB build that links libramgpu.so uses it from
+! ModRamRun to replace the species loop of ram_run and its tail
+! (src/ModRamRun.f90:64-222 of the reference).  Compiled only where a
+! Fortran compiler exists; the C ABI itself is tested through ctypes.
+!==============================================================================
+module ModRamGpu
+
+  use iso_c_binding
+  implicit none
+
+  integer(c_int), parameter :: RAMGPU_OK = 0
+  integer(c_int), parameter :: RAMGPU_FLAG_CLOSED = 1, RAMGPU_FLAG_NO_ATMOL = 2, &
+                               RAMGPU_FLAG_LOSSES = 4
+  integer(c_int), parameter :: RAMGPU_CEX_NONE = 0, RAMGPU_CEX_HYDROGEN = 1, &
+                               RAMGPU_CEX_HELIUM1 = 2, RAMGPU_CEX_OXYGEN1 = 3
+
+  type, bind(C) :: ramgpu_config
+     integer(c_int) :: nr, nt, ne, npa, ns, n_members
+     real(c_double) :: betalim, fraccfl, dtsmin
+     integer(c_int) :: flags
+  end type ramgpu_config
+
+  type, bind(C) :: ramgpu_grid
+     type(c_ptr)    :: lz, rlz, phi
+     real(c_double) :: dl1, mdr, dphi, conf1, conf2
+     type(c_ptr)    :: ekev, ebnd, we, de, mu, dmu, wmu, upa, rmas
+     type(c_ptr)    :: grel, grbnd, v, epp, ernh, ffactor
+  end type ramgpu_grid
+
+  interface
+     integer(c_int) function ramgpu_create(cfg, ctx) bind(C, name="ramgpu_create")
+       import :: c_int, c_ptr, ramgpu_config
+       type(ramgpu_config), intent(in) :: cfg
+       type(c_ptr), intent(out) :: ctx
+     end function
+     integer(c_int) function ramgpu_destroy(ctx) bind(C, name="ramgpu_destroy")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function ramgpu_set_species(ctx, s, charge, cex_kind) &
+          bind(C, name="ramgpu_set_species")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: s, charge, cex_kind
+     end function
+     integer(c_int) function ramgpu_set_grid(ctx, grid) bind(C, name="ramgpu_set_grid")
+       import :: c_int, c_ptr, ramgpu_grid
+       type(c_ptr), value :: ctx
+       type(ramgpu_grid), intent(in) :: grid
+     end function
+     integer(c_int) function ramgpu_set_fields(ctx, fnhs, fnis, bounhs, bounis, hdns, &
+          didt, dibndt, bnes, dbdt, eir, eip, outside_mgnp) bind(C, name="ramgpu_set_fields")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: fnhs(*), fnis(*), bounhs(*), bounis(*), hdns(*), &
+                                     didt(*), dibndt(*), bnes(*), dbdt(*), eir(*), eip(*)
+       integer(c_int), intent(in) :: outside_mgnp(*)
+     end function
+     integer(c_int) function ramgpu_set_boundary(ctx, member, s, fgeos_s) &
+          bind(C, name="ramgpu_set_boundary")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member, s
+       real(c_double), intent(in) :: fgeos_s(*)
+     end function
+     integer(c_int) function ramgpu_set_potential(ctx, member, vt) &
+          bind(C, name="ramgpu_set_potential")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member
+       real(c_double), intent(in) :: vt(*)
+     end function
+     integer(c_int) function ramgpu_set_kp(ctx, member, kp) bind(C, name="ramgpu_set_kp")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member
+       real(c_double), value :: kp
+     end function
+     integer(c_int) function ramgpu_upload_f2_all(ctx, member, f2) &
+          bind(C, name="ramgpu_upload_f2_all")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member
+       real(c_double), intent(in) :: f2(*)
+     end function
+     integer(c_int) function ramgpu_download_f2_all(ctx, member, f2) &
+          bind(C, name="ramgpu_download_f2_all")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member
+       real(c_double), intent(out) :: f2(*)
+     end function
+     integer(c_int) function ramgpu_ram_run(ctx, dts) bind(C, name="ramgpu_ram_run")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), value :: dts
+     end function
+     integer(c_int) function ramgpu_moments(ctx, member, s, ppert, ppart) &
+          bind(C, name="ramgpu_moments")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member, s
+       real(c_double), intent(out) :: ppert(*), ppart(*)
+     end function
+     integer(c_int) function ramgpu_flux(ctx, member, s, flux_s) bind(C, name="ramgpu_flux")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member, s
+       real(c_double), intent(out) :: flux_s(*)
+     end function
+     integer(c_int) function ramgpu_cfl(ctx, member, s, out5) bind(C, name="ramgpu_cfl")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member, s
+       real(c_double), intent(out) :: out5(5)
+     end function
+     integer(c_int) function ramgpu_last_error(ctx, buf, len) bind(C, name="ramgpu_last_error")
+       import :: c_int, c_ptr, c_char, c_size_t
+       type(c_ptr), value :: ctx
+       character(kind=c_char), intent(out) :: buf(*)
+       integer(c_size_t), value :: len
+     end function
+  end interface
+
+end module ModRamGpu
