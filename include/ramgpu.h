@@ -196,6 +196,28 @@ int ramgpu_probe_fp64(double *lane_ops_per_s);
 int ramgpu_set_timing(ramgpu_ctx *ctx, int enable);
 int ramgpu_kernel_times(ramgpu_ctx *ctx, double *ms, long long *counts);
 
+/* ---- no-allocation variant --------------------------------------------- */
+
+/* SETRC = sum EKEV*F2*WE*WMU (the energy-content sum of SUMRC) of one
+ * species' F2 already on the device, for callers that cannot allocate
+ * device memory: a host model that gives every device byte to its own pool
+ * and forbids libraries to call cudaMalloc, or code that must not call
+ * allocation APIs (cudaMalloc may synchronise the device) while work is in
+ * flight.  It allocates nothing: its only scratch is a fixed 36 KiB array in
+ * this library's device image, so NE and NPA are limited to 1024 and larger
+ * sizes are rejected with RAMGPU_ERR_ARG.
+ *   f2_dev : device pointer, (NR,NT,NE,NPA) Fortran order (e.g. from
+ *            ramgpu_f2_device_ptr);  we, wmu, ekev : host arrays (NE)/(NPA)/(NE)
+ *   stream : cudaStream_t or NULL;  setrc : host, receives the sum.
+ * The first call on a device looks up the scratch address on that device
+ * (make it before any stream capture).  Every call reuses the same scratch,
+ * which keeps the last call's contents; calls that overlap on the GPU race.
+ * Errors are reported by ramgpu_last_error(NULL, ...).  No counterpart in the
+ * reference: it exists only for callers that cannot allocate. */
+int ramgpu_sumrc_noalloc(const double *f2_dev, int nr, int nt, int ne, int npa,
+                         const double *we, const double *wmu, const double *ekev,
+                         void *stream, double *setrc);
+
 #ifdef __cplusplus
 }
 #endif

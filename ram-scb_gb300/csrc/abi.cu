@@ -59,6 +59,10 @@ struct ramgpu_ctx {
   std::vector<Span> spans;
 };
 
+namespace ramgpu {
+void set_thread_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace ramgpu
+
 // ------------------------------------------------------------------ helpers
 static cudaEvent_t take_event(ramgpu_ctx* c) {
   cudaEvent_t e = nullptr;

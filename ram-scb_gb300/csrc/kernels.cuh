@@ -1,5 +1,7 @@
 // kernels.cuh -- launchers shared between the kernel files and the C ABI.
 #pragma once
+#include <string>
+
 #include "ramgpu_internal.cuh"
 
 namespace ramgpu {
@@ -30,6 +32,9 @@ __device__ __forceinline__ double stale_ghost(const Dev& d, int m, int slot, int
     if (inflow_line(d, m, jj, l, p4)) return ghost_value(d, slot, jj, k, l, d.conf1);
   return d.plane_carry[(long long)slot * d.ne * d.npa + (long long)k * d.npa + l];
 }
+
+// Thread-local error text returned by ramgpu_last_error(NULL, ...).
+void set_thread_error(const std::string& msg);
 
 void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st);
 void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st);

@@ -31,6 +31,7 @@ EXPORTS = (
     "ramgpu_ram_run", "ramgpu_half_step", "ramgpu_ram_run_async", "ramgpu_moments",
     "ramgpu_flux", "ramgpu_cfl", "ramgpu_losses", "ramgpu_reset_losses", "ramgpu_launch_count",
     "ramgpu_apply_op", "ramgpu_set_timing", "ramgpu_kernel_times", "ramgpu_probe_fp64",
+    "ramgpu_sumrc_noalloc",
 )
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
           "anisch", "dts_tables", "sumrc")
@@ -108,6 +109,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_set_timing": ([vp, i], i),
         "ramgpu_kernel_times": ([vp, dp, C.POINTER(C.c_longlong)], i),
         "ramgpu_probe_fp64": ([dp], i),
+        "ramgpu_sumrc_noalloc": ([vp, i, i, i, i, dp, dp, dp, vp, dp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
