@@ -49,6 +49,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--flush-mb", type=int, default=256)
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--members", type=int, default=256, help="ensemble members (0: skip)")
+    ap.add_argument("--ensemble-steps", type=int, default=6)
+    ap.add_argument("--loop-members", type=int, default=16)
     return ap.parse_args()
 
 
@@ -164,6 +169,86 @@ def run_reference(args, rank, world):
 
 
 # ------------------------------------------------------------ GPU leg
+def run_ensemble(args, torch, dev, stream):
+    """Batched ensemble (256 uneven members on the standard grid) against
+    looping the plain single-member GPU step; returns a dict for the line."""
+    import numpy as np
+
+    from ramgpu import abi, workload as W
+
+    ens = W.make_ensemble(args.members)
+    base = ens.base
+    g = base.grid
+    gpu = abi.RamGpu(g, base.fields, n_members=ens.members)
+    gpu.set_stream(stream.cuda_stream)
+    for m in range(ens.members):
+        gpu.set_member_species(m, ens.species[m])
+        for s in ens.species[m]:
+            gpu.upload_f2(m, s, base.f2[s] * ens.scale[m])
+            gpu.set_boundary(m, s, base.fgeos[s] * ens.scale[m])
+    t0 = 356  # sample from DTs step 356 on: members with length < t0 + 2K retire inside it
+    gpu.set_kp_all(ens.kp(t0))
+    shapes, _ = gpu.autotune(base.dts)
+    gpu.set_graph(True)
+    flush = torch.empty(max(1, args.flush_mb) << 20, dtype=torch.uint8, device=dev)
+    for w in range(2):  # warm-up (captures the graph)
+        gpu.ram_run(base.dts)
+    K = max(2, min(args.ensemble_steps, 20))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    member_steps = 0
+    cell_updates = 0
+    dead = set()
+    for k in range(K):
+        step = t0 + 2 * k
+        for m in range(ens.members):  # finished members retire
+            if step >= ens.length[m] and m not in dead:
+                gpu.set_member_active(m, False)
+                dead.add(m)
+        active = [m for m in range(ens.members) if step < ens.length[m]]
+        member_steps += 2 * len(active)
+        cell_updates += 2 * g.ncell * sum(len(ens.species[m]) for m in active)
+        gpu.set_kp_all(ens.kp(step))
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+        ev[k][0].record(stream)
+        gpu.ram_run_async(base.dts)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    batched_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    retired = len(dead)
+    # looped: the plain single-member step (direct launches), one member at a time
+    gpu.set_graph(False)
+    sub = list(range(0, ens.members, max(1, ens.members // args.loop_members)))[:args.loop_members]
+    for m in range(ens.members):
+        gpu.set_member_active(m, False)
+    lev = []
+    for m in sub:
+        gpu.set_member_active(m, True)
+        gpu.set_kp_all(ens.kp(t0))
+        gpu.ram_run(base.dts)  # warm (rebuilds the work list)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.fill_(m & 0xFF)
+        a.record(stream)
+        gpu.ram_run_async(base.dts)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        lev.append(a.elapsed_time(b) / 1e3)
+        gpu.set_member_active(m, False)
+    looped_per_member = statistics.mean(lev)
+    gpu.close()
+    batched = member_steps / batched_s
+    looped = 2.0 / looped_per_member
+    return {"members": ens.members, "member_species": int(sum(len(x) for x in ens.species)),
+            "steps": K, "retired_in_sample": retired,
+            "member_steps_per_s_batched": batched, "member_steps_per_s_looped": looped,
+            "batched_over_looped": batched / looped,
+            "cell_updates_per_s_batched": cell_updates / batched_s,
+            "looped_sample_members": len(sub), "launch_shapes": shapes,
+            "notes": "batched: one graph-replayed ram_run per step for all active members; "
+                     "looped: the plain direct-launch step of one member at a time"}
+
+
 def run_gb300(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -187,7 +272,10 @@ def run_gb300(args, rank, world, local_rank):
     def kp_at(step):
         return wl.kp(2 * step)
 
-    # warm-up (also builds the DTs tables)
+    gpu.set_kp(-1, kp_at(0))
+    shapes, _ = gpu.autotune(wl.dts) if not args.no_autotune else (gpu.launch_shape(), None)
+    gpu.set_graph(not args.no_graph)
+    # warm-up (builds the DTs tables, captures the graph)
     for w in range(args.warmup):
         gpu.set_kp(-1, kp_at(w))
         gpu.ram_run(wl.dts)
@@ -197,8 +285,6 @@ def run_gb300(args, rank, world, local_rank):
     clocks = ClockSampler(local_rank)
     clocks.start()
     time.sleep(0.3)
-    gpu.set_timing(True)
-    gpu.kernel_times()
     launches0 = gpu.launch_count()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     torch.cuda.synchronize(dev)
@@ -213,8 +299,6 @@ def run_gb300(args, rank, world, local_rank):
     torch.cuda.synchronize(dev)
     wall = time.perf_counter() - wall0
     launches = gpu.launch_count() - launches0
-    ktimes = gpu.kernel_times()
-    gpu.set_timing(False)
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(step_ms)
@@ -224,7 +308,25 @@ def run_gb300(args, rank, world, local_rank):
         total_ms = float(t.item())
     value = world * cells_per_step * args.steps / (total_ms / 1e3)
 
-    # dominant kernel and its roofline (per launch, from the events above)
+    # per-kernel durations: a second timed pass with events around every
+    # launch group on the launching stream (timing mode bypasses the graph)
+    gpu.set_timing(True)
+    gpu.kernel_times()
+    kt_ms = []
+    for k in range(max(3, min(args.steps, 10))):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+        gpu.set_kp(-1, kp_at(k))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        gpu.ram_run_async(wl.dts)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        kt_ms.append(a.elapsed_time(b))
+    ktimes = gpu.kernel_times()
+    gpu.set_timing(False)
+
+    # dominant kernel and its roofline (per launch)
     hbm_peak, peak_kind = measured_peaks()
     sweep = {k: v for k, v in ktimes.items() if k.startswith("drift")}
     dom = max(sweep, key=lambda k: sweep[k][0])
@@ -234,7 +336,6 @@ def run_gb300(args, rank, world, local_rank):
     achieved = bytes_per_launch / (dom_ms / 1e3) / 1e9
     nfaces = g.ncell * nitems
     fp64 = FP64_OPS_PER_FACE[dom] * nfaces / (dom_ms / 1e3) / 1e9
-
     fp64_peak = abi.probe_fp64() / 1e9
 
     # end-to-end through the C ABI with host buffers (pinned), full F2 in and out
@@ -259,6 +360,11 @@ def run_gb300(args, rank, world, local_rank):
            "d2h_bytes_per_step": 8 * g.ncell * ns + 16 * g.nr * g.nt,
            "path": "ramgpu_upload_f2 (pinned host) + ramgpu_set_kp + ramgpu_ram_run + "
                    "ramgpu_download_f2 + ramgpu_moments, every step"}
+    gpu.close()
+
+    ensemble = None
+    if rank == 0 and args.members > 0:
+        ensemble = run_ensemble(args, torch, dev, stream)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -266,7 +372,6 @@ def run_gb300(args, rank, world, local_rank):
         cpu = {"value": v, "unit": UNIT, "cores": min(ns, os.cpu_count() or 1), "kind": "port",
                "sample": f"{n} ram_run calls of the same workload in {el:.1f} s (C restatement of the "
                          f"reference routines, OpenMP over species as the reference)"}
-    gpu.close()
     if rank != 0:
         return
     line = {
@@ -275,6 +380,7 @@ def run_gb300(args, rank, world, local_rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": workload_desc(wl), "step": "one ram_run call = 2 DTs steps",
                    "cells_per_step": cells_per_step, "l2": "flushed between timed steps (256 MB write)",
+                   "graph": not args.no_graph, "launch_shapes": shapes,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": None, "kernel": dom,
@@ -283,8 +389,9 @@ def run_gb300(args, rank, world, local_rank):
                               "frac": fp64 / fp64_peak, "ops_per_face": FP64_OPS_PER_FACE[dom],
                               "peak_kind": "measured live (fma loop, ramgpu_probe_fp64)"}},
         "kernels_ms": {k: round(v[0] / v[1], 5) for k, v in ktimes.items()},
+        "kernel_pass_ms_per_step": statistics.mean(kt_ms),
         "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
-        "wall_s": wall,
+        "ensemble": ensemble, "wall_s": wall,
     }
     print(json.dumps(line), flush=True)
 

@@ -115,6 +115,8 @@ int ramgpu_set_potential(ramgpu_ctx *ctx, int member, const double *vt);
 /* Kp for the Volland-Stern potential computed on the device
  * (src/ModRamRun.f90:45-54).  member < 0 sets every member. */
 int ramgpu_set_kp(ramgpu_ctx *ctx, int member, double kp);
+/* Kp of every member at once (n_members values), VOLS mode for all. */
+int ramgpu_set_kp_all(ramgpu_ctx *ctx, const double *kp);
 /* Species a member advances (default: all ns).  list holds 0-based species. */
 int ramgpu_set_member_species(ramgpu_ctx *ctx, int member, int n, const int *list);
 /* Retire (0) or re-activate (1) a member; retired members are not advanced. */
@@ -177,6 +179,26 @@ int ramgpu_cfl(ramgpu_ctx *ctx, int member, int s, double *out5);
  * and takes SETRC of the current state as the starting ENOLD.  out: 4 doubles. */
 int ramgpu_losses(ramgpu_ctx *ctx, int member, int s, double *out4);
 int ramgpu_reset_losses(ramgpu_ctx *ctx);
+
+/* ---- execution tuning (no reference counterpart) ------------------------ */
+
+/* Replay ram_run / ram_run_async from a CUDA graph captured on first use and
+ * re-captured when dts, the active (member, species) list, the flags or the
+ * launch shapes change.  Inputs (F2, Kp/VT, FGEOS, fields) are read when the
+ * graph runs, so set_* calls between steps take effect.  Timing mode
+ * (ramgpu_set_timing) bypasses the graph. */
+int ramgpu_set_graph(ramgpu_ctx *ctx, int enable);
+/* Launch shape of sweep w (0 DRIFTR, 1 DRIFTP, 2 DRIFTE, 3 DRIFTMU):
+ * threads per CTA (32..256, multiple of 32) and, when persistent_ctas > 0,
+ * a persistent grid of that many CTAs looping over (item, line-block) units. */
+int ramgpu_set_launch_shape(ramgpu_ctx *ctx, int sweep, int threads, int persistent_ctas);
+int ramgpu_get_launch_shape(ramgpu_ctx *ctx, int *threads4, int *persistent4);
+/* Autotuner: times every sweep at 32/64/128/256 threads per CTA, each with a
+ * one-unit-per-CTA grid and a persistent grid (resident CTAs x SMs), on the
+ * context's active items, keeps the fastest, and restores F2 afterwards
+ * (it allocates a temporary snapshot).  best_ms4 (may be NULL) receives the
+ * chosen average launch times. */
+int ramgpu_autotune(ramgpu_ctx *ctx, double dts, int reps, double *best_ms4);
 
 /* Number of kernel launches this context has issued (diagnostics). */
 long long ramgpu_launch_count(const ramgpu_ctx *ctx);

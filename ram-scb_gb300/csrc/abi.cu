@@ -52,6 +52,17 @@ struct ramgpu_ctx {
   double* sumrc_part = nullptr;
   double* upa_h_dummy = nullptr;
   long long launches = 0;
+  long long graph_launch_count = 0;
+  // CUDA graph of the ram_run sequence, replayed while (dts, items, flags)
+  // are unchanged; inputs (Kp, VT, FGEOS, F2) are read at execution time
+  bool graph_on = false;
+  cudaGraphExec_t graph_exec = nullptr;
+  double graph_dts = -1.0;
+  long long graph_items = -1;
+  unsigned graph_flags = 0;
+  int graph_shape = -1;
+  long long items_version = 0;
+  int shape_version = 0;
   // optional per-kernel-class timing
   bool timing = false;
   std::vector<cudaEvent_t> ev_free;
@@ -145,6 +156,7 @@ static int rebuild_items(ramgpu_ctx* ctx) {
   ctx->d.items = ctx->items_d;
   ctx->d.nitems = (int)ctx->items_h.size();
   ctx->items_dirty = false;
+  ctx->items_version += 1;
   return RAMGPU_OK;
 }
 
@@ -234,14 +246,11 @@ static int enqueue_reverse(ramgpu_ctx* ctx, double dts, bool loss_fused, const d
   return RAMGPU_OK;
 }
 
-static int enqueue_ram_run(ramgpu_ctx* ctx, double dts) {
-  int rc = prepare(ctx, dts);
-  if (rc) return rc;
-  ctx->last_dts = dts;
-  if (ctx->d.nitems == 0) return RAMGPU_OK;
+static int enqueue_body(ramgpu_ctx* ctx, double dts) {
+  int rc = RAMGPU_OK;
   { Timed t(ctx, 0); launch_member_coef(ctx->d, dts, ctx->stream); }
   { Timed t(ctx, 1); launch_ghost(ctx->d, ctx->stream); }
-  ctx->launches += 4;
+  ctx->launches += 5;
   CKL("member tables");
   const bool losses = ctx->cfg.flags & RAMGPU_FLAG_LOSSES;
   if (!losses) {
@@ -267,6 +276,49 @@ static int enqueue_ram_run(ramgpu_ctx* ctx, double dts) {
   { Timed t(ctx, 7); launch_moments(ctx->d, ctx->stream); }
   ctx->launches += 3;
   CKL("finish/moments");
+  return RAMGPU_OK;
+}
+
+static void drop_graph(ramgpu_ctx* ctx) {
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  ctx->graph_exec = nullptr;
+}
+
+static int enqueue_ram_run(ramgpu_ctx* ctx, double dts) {
+  int rc = prepare(ctx, dts);
+  if (rc) return rc;
+  ctx->last_dts = dts;
+  if (ctx->d.nitems == 0) return RAMGPU_OK;
+  if (!ctx->graph_on || ctx->timing) return enqueue_body(ctx, dts);
+  // CUDA graph: capture once per (dts, work list, flags, launch shapes), replay
+  if (!ctx->graph_exec || ctx->graph_dts != dts || ctx->graph_items != ctx->items_version ||
+      ctx->graph_flags != ctx->d.flags || ctx->graph_shape != ctx->shape_version) {
+    drop_graph(ctx);
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const long long l0 = ctx->launches;
+    rc = enqueue_body(ctx, dts);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph capture");
+    e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      ctx->graph_exec = nullptr;
+      return cuda_fail(ctx, e, "graph instantiate");
+    }
+    ctx->graph_launch_count = ctx->launches - l0;
+    ctx->launches = l0;
+    ctx->graph_dts = dts;
+    ctx->graph_items = ctx->items_version;
+    ctx->graph_flags = ctx->d.flags;
+    ctx->graph_shape = ctx->shape_version;
+  }
+  CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+  ctx->launches += ctx->graph_launch_count;
   return RAMGPU_OK;
 }
 
@@ -303,6 +355,8 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   d.nr = cfg->nr; d.nt = cfg->nt; d.ne = cfg->ne; d.npa = cfg->npa;
   d.ns = cfg->ns; d.nm = cfg->n_members; d.ncell = ncell; d.nf = cfg->nr + 1;
   d.betalim = ctx->cfg.betalim;
+  const int blk0[4] = {128, 128, 64, 64};
+  for (int w = 0; w < 4; ++w) { d.blk[w] = blk0[w]; d.pers[w] = 0; }
   const size_t nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa, ns = d.ns, nm = d.nm, nf = d.nf;
   const size_t nijl = nr * nt * npa, nfield = nf * nt * npa, nslot = nm * ns;
   bool ok = true;
@@ -310,6 +364,7 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   ctx->own_stream = ok;
   d.lz = dalloc<double>(ctx, nf, &ok); d.rlz = dalloc<double>(ctx, nf, &ok);
   d.phi = dalloc<double>(ctx, nt, &ok);
+  d.lr2 = dalloc<double>(ctx, nf, &ok); d.sinphi = dalloc<double>(ctx, nt, &ok);
   d.ekev = dalloc<double>(ctx, ne, &ok); d.ebnd = dalloc<double>(ctx, ne, &ok);
   d.we = dalloc<double>(ctx, ne, &ok); d.de = dalloc<double>(ctx, ne, &ok);
   d.mu = dalloc<double>(ctx, npa, &ok); d.dmu = dalloc<double>(ctx, npa, &ok);
@@ -350,13 +405,14 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   d.vt = dalloc<double>(ctx, nm * nf * nt, &ok);
   d.cr = dalloc<double>(ctx, nm * nr * nt, &ok); d.ca = dalloc<double>(ctx, nm * nr * nt, &ok);
   d.ue = dalloc<double>(ctx, nm * nijl, &ok); d.um = dalloc<double>(ctx, nm * nijl, &ok);
+  d.drd1 = dalloc<double>(ctx, nm * nr * nt, &ok); d.dpd1 = dalloc<double>(ctx, nm * nr * nt, &ok);
   d.f2 = dalloc<double>(ctx, nslot * ncell, &ok);
   d.fgeos = dalloc<double>(ctx, nslot * nt * ne * npa, &ok);
   d.plane_last = dalloc<double>(ctx, nslot * ne * npa, &ok);
   d.plane_has = dalloc<int>(ctx, nslot * ne * npa, &ok);
   d.plane_carry = dalloc<double>(ctx, nslot * ne * npa, &ok);
   d.cflq = dalloc<unsigned long long>(ctx, nslot * 4, &ok);
-  d.mom_part = dalloc<double>(ctx, nslot * nr * nt * ne * 2, &ok);
+  d.mom_part = dalloc<double>(ctx, nslot * 4 * nr * nt * ne * 2, &ok);
   d.ppert = dalloc<double>(ctx, nslot * nr * nt, &ok);
   d.ppart = dalloc<double>(ctx, nslot * nr * nt, &ok);
   ctx->items_d = dalloc<int2>(ctx, nslot, &ok);
@@ -385,6 +441,7 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
 int ramgpu_destroy(ramgpu_ctx* ctx) {
   if (!ctx) return RAMGPU_ERR_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  drop_graph(ctx);
   for (void* p : ctx->allocs) cudaFree(p);
   for (auto& sp : ctx->spans) { cudaEventDestroy(sp.a); cudaEventDestroy(sp.b); }
   for (cudaEvent_t e : ctx->ev_free) cudaEventDestroy(e);
@@ -438,6 +495,13 @@ int ramgpu_set_grid(ramgpu_ctx* ctx, const ramgpu_grid* g) {
     return cudaMemcpy((void*)dst, src, n * sizeof(double), cudaMemcpyHostToDevice);
   };
   CK(up(d.lz, G.lz, nr + 1)); CK(up(d.rlz, G.rlz, nr + 1)); CK(up(d.phi, G.phi, nt));
+  {  // VOLS factors (src/ModRamRun.f90:51): (LZ(I)*RE)**2 and SIN(PHI(J)-PHIOFS), PHIOFS = 0
+    std::vector<double> lr2(nr + 1), sp(nt);
+    for (int i = 0; i <= nr; ++i) { const double lr = G.lz[i] * kRE; lr2[i] = lr * lr; }
+    for (int j = 0; j < nt; ++j) sp[j] = sin(G.phi[j] - 0.0);
+    CK(up(d.lr2, lr2.data(), nr + 1));
+    CK(up(d.sinphi, sp.data(), nt));
+  }
   CK(up(d.ekev, G.ekev, ne)); CK(up(d.ebnd, G.ebnd, ne)); CK(up(d.we, G.we, ne)); CK(up(d.de, G.de, ne));
   CK(up(d.mu, G.mu, npa)); CK(up(d.dmu, G.dmu, npa)); CK(up(d.wmu, G.wmu, npa));
   CK(up(d.rmas, G.rmas, ns));
@@ -534,6 +598,18 @@ int ramgpu_set_kp(ramgpu_ctx* ctx, int member, double kp) {
     CK(cudaMemcpyAsync(ctx->d.vt_mode + m, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
   }
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_kp_all(ramgpu_ctx* ctx, const double* kp) {
+  if (check_ctx(ctx) || !kp) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  const int nm = ctx->cfg.n_members;
+  for (int m = 0; m < nm; ++m)
+    if (!isfinite(kp[m])) return fail(ctx, RAMGPU_ERR_ARG, "kp must be finite");
+  std::vector<int> one(nm, 1);
+  CK(cudaMemcpyAsync(ctx->d.kp, kp, sizeof(double) * nm, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d.vt_mode, one.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   return RAMGPU_OK;
 }
 
@@ -634,7 +710,7 @@ int ramgpu_half_step(ramgpu_ctx* ctx, double dts, int order) {
   if (ctx->d.nitems == 0) return RAMGPU_OK;
   launch_member_coef(ctx->d, dts, ctx->stream);
   launch_ghost(ctx->d, ctx->stream);
-  ctx->launches += 4;
+  ctx->launches += 5;
   CKL("member tables");
   if (order == 0) rc = enqueue_forward(ctx, dts, true, ctx->d.loss1);
   else rc = enqueue_reverse(ctx, dts, true, ctx->d.loss1);
@@ -652,7 +728,7 @@ int ramgpu_apply_op(ramgpu_ctx* ctx, double dts, int op, int cfl) {
   if (ctx->d.nitems == 0) return RAMGPU_OK;
   launch_member_coef(ctx->d, dts, ctx->stream);
   launch_ghost(ctx->d, ctx->stream);
-  ctx->launches += 4;
+  ctx->launches += 5;
   if (cfl) CK(cudaMemsetAsync(ctx->d.cflq, 0, sizeof(unsigned long long) * 4 * ctx->d.nm * ctx->d.ns, ctx->stream));
   switch (op) {
     case 0: launch_sweep_r(ctx->d, dts, cfl != 0, ctx->stream); break;
@@ -662,6 +738,7 @@ int ramgpu_apply_op(ramgpu_ctx* ctx, double dts, int op, int cfl) {
     case 4: launch_loss_apply(ctx->d, ctx->d.charge, ctx->stream); break;
     case 5: launch_loss_apply(ctx->d, ctx->d.atm, ctx->stream); break;
     case 6: launch_moments(ctx->d, ctx->stream); ctx->launches += 1; break;
+    default: break;
   }
   ctx->launches += 1;
   CKL("apply_op");
@@ -787,6 +864,108 @@ int ramgpu_probe_fp64(double* lane_ops_per_s) {
   cudaFree(out);
   if (e != cudaSuccess) return fail(nullptr, RAMGPU_ERR_CUDA, cudaGetErrorString(e));
   *lane_ops_per_s = 8.0 * iters * (double)block * grid / (best * 1e-3);
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_graph(ramgpu_ctx* ctx, int enable) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  ctx->graph_on = enable != 0;
+  if (!ctx->graph_on) drop_graph(ctx);
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_launch_shape(ramgpu_ctx* ctx, int sweep, int threads, int persistent_ctas) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (sweep < 0 || sweep > 3) return fail(ctx, RAMGPU_ERR_ARG, "sweep must be 0..3");
+  if (threads < 32 || threads > 256 || (threads % 32)) return fail(ctx, RAMGPU_ERR_ARG, "threads must be 32..256, multiple of 32");
+  if (persistent_ctas < 0) return fail(ctx, RAMGPU_ERR_ARG, "persistent_ctas must be >= 0");
+  ctx->d.blk[sweep] = threads;
+  ctx->d.pers[sweep] = persistent_ctas;
+  ctx->shape_version += 1;
+  return RAMGPU_OK;
+}
+
+int ramgpu_get_launch_shape(ramgpu_ctx* ctx, int* threads4, int* persistent4) {
+  if (check_ctx(ctx) || !threads4 || !persistent4) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  for (int w = 0; w < 4; ++w) { threads4[w] = ctx->d.blk[w]; persistent4[w] = ctx->d.pers[w]; }
+  return RAMGPU_OK;
+}
+
+int ramgpu_autotune(ramgpu_ctx* ctx, double dts, int reps, double* best_ms4) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (reps < 1) reps = 3;
+  int rc = prepare(ctx, dts);
+  if (rc) return rc;
+  if (ctx->d.nitems == 0) return RAMGPU_OK;
+  launch_member_coef(ctx->d, dts, ctx->stream);
+  launch_ghost(ctx->d, ctx->stream);
+  ctx->launches += 5;
+  // the trials advance F2: keep a copy of every active slot and restore it
+  const size_t ncell = ctx->d.ncell;
+  double* snap = nullptr;
+  CK(cudaMalloc(&snap, sizeof(double) * ncell * ctx->items_h.size()));
+  for (size_t i = 0; i < ctx->items_h.size(); ++i) {
+    const int slot = ctx->items_h[i].x * ctx->d.ns + ctx->items_h[i].y;
+    CK(cudaMemcpyAsync(snap + i * ncell, ctx->d.f2 + (size_t)slot * ncell, sizeof(double) * ncell,
+                       cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  int nsm = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int cand_blk[4] = {32, 64, 128, 256};
+  for (int w = 0; w < 4; ++w) {
+    float best = 1e30f;
+    int bb = ctx->d.blk[w], bp = ctx->d.pers[w];
+    for (int ib = 0; ib < 4; ++ib) {
+      for (int persist = 0; persist < 2; ++persist) {
+        const int blk = cand_blk[ib];
+        int pc = 0;
+        if (persist) {
+          const int per_sm = sweep_max_blocks_per_sm(w, blk);
+          if (per_sm <= 0) continue;
+          pc = per_sm * nsm;
+        }
+        ctx->d.blk[w] = blk;
+        ctx->d.pers[w] = pc;
+        float tot = 0.f;
+        for (int r = 0; r <= reps; ++r) {
+          cudaEventRecord(e0, ctx->stream);
+          switch (w) {
+            case 0: launch_sweep_r(ctx->d, dts, false, ctx->stream); break;
+            case 1: launch_sweep_p(ctx->d, dts, false, ctx->stream); break;
+            case 2: launch_sweep_e(ctx->d, dts, false, ctx->stream); break;
+            default: launch_sweep_mu(ctx->d, dts, false, 0, nullptr, ctx->stream); break;
+          }
+          cudaEventRecord(e1, ctx->stream);
+          cudaEventSynchronize(e1);
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          if (r > 0) tot += ms;  // first launch is a warm-up
+          ctx->launches += 1;
+        }
+        const float avg = tot / reps;
+        if (avg < best) { best = avg; bb = blk; bp = pc; }
+      }
+    }
+    ctx->d.blk[w] = bb;
+    ctx->d.pers[w] = bp;
+    if (best_ms4) best_ms4[w] = best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (size_t i = 0; i < ctx->items_h.size(); ++i) {
+    const int slot = ctx->items_h[i].x * ctx->d.ns + ctx->items_h[i].y;
+    cudaMemcpyAsync(ctx->d.f2 + (size_t)slot * ncell, snap + i * ncell, sizeof(double) * ncell,
+                    cudaMemcpyDeviceToDevice, ctx->stream);
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(snap);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "autotune");
+  ctx->shape_version += 1;
   return RAMGPU_OK;
 }
 

@@ -42,6 +42,8 @@ void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st);
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
                      cudaStream_t st);
 
+int sweep_max_blocks_per_sm(int w, int blk);
+
 void launch_field_tables(const Dev& d, cudaStream_t st);
 void launch_species_static(const Dev& d, cudaStream_t st);
 void launch_dts_tables(const Dev& d, double dts, cudaStream_t st);

@@ -36,6 +36,7 @@ struct Dev {
   unsigned flags;
   // grid vectors
   const double *lz, *rlz, *phi, *ekev, *ebnd, *we, *de, *mu, *dmu, *wmu;
+  const double *lr2, *sinphi;  // (LZ(I)*RE)**2 (NR+1) and SIN(PHI(J)-PHIOFS) (NT) of the VOLS formula
   const int *upa_atm;   // int(UPA(I)): first loss-cone L (1-based), NR
   const int *upa_mom;   // int(UPA(I)-1): last L of the ANISCH sum, NR
   // reciprocal grid tables: -0.5/DE, 1/WE, 1/DE (NE); -0.5/DMU, 1/WMU, 1/DMU (NPA)
@@ -76,6 +77,7 @@ struct Dev {
   double *cr;             // (nm, NR, NT)
   double *ca;             // (nm, NR, NT)
   double *ue, *um;        // (nm, NR, NT, NPA)
+  double *drd1, *dpd1;    // (nm, NR, NT): DRD1 = DRM1, DPD1 = DPM1 of DRIFTE/DRIFTMU
   // per (member, species) slot
   double *f2;             // (nm*ns, ncell)
   double *fgeos;          // (nm*ns, NT*NE*NPA)
@@ -83,12 +85,16 @@ struct Dev {
   int *plane_has;         // (nm*ns, NE*NPA): plane (K,L) has an inflow line
   double *plane_carry;    // (nm*ns, NE*NPA): F(NR+1) left by planes before (K,L) in K->L order
   unsigned long long *cflq;  // (nm*ns, 4): max over cells of the CFL quotient, as bits
-  double *mom_part;       // (nm*ns, NR, NT, NE, 2) per-K moment partials
+  double *mom_part;       // (nm*ns, 4 chunks, NE, NT, NR, 2) per-K moment partials
   double *ppert, *ppart;  // (nm*ns, NR, NT)
   double *sumrc_part;     // (nm*ns, nblk) SUMRC partial sums
   // work list
   const int2 *items;      // (member, species)
   int nitems;
+  // launch shape of the sweeps R, P, E, MU: threads per CTA and, when > 0,
+  // a persistent grid of that many CTAs looping over (item, line-block) units
+  int blk[4];
+  int pers[4];
 };
 
 // ---------------------------------------------------------------- bit tests

@@ -19,215 +19,236 @@ namespace ramgpu {
 // ----------------------------------------------------------------- DRIFTR
 // Line (J,K,L) along I = 1..NR.  Faces 2..NR-1 (and NR on inflow lines).
 template <bool kCfl>
-__global__ void __launch_bounds__(128) k_sweep_r(Dev d, double dts) {
+__global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = nt * ne * d.npa;
-  const int2 item = d.items[blockIdx.y];
-  const int m = item.x, s = item.y, slot = m * d.ns + s;
-  const int line = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long q = 0ULL;  // CFL quotient bits
-  if (line < nlines) {
-    const int j = line % nt;
-    const int l = line / (nt * ne);
-    double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + (long long)line * nr;
-    const double* __restrict__ grt = d.grt + ((long long)l * nt + j) * nr;
-    const double* __restrict__ cr = d.cr + ((long long)m * nt + j) * nr;
-    const int* __restrict__ outside = d.outside + (long long)j * nr;
-    const double p4 = d.p4[s * ne + (line / nt) % ne];
-    const double beta = d.betalim;
-    const bool closed = d.flags & 1u;
+  // Work units are (item, block of lines).  A grid of (blocks per item,
+  // items) gives one unit per CTA; a persistent grid loops over them.
+  const int bpi = (nlines + blockDim.x - 1) / blockDim.x;
+  const long long nunits = (long long)bpi * d.nitems;
+  for (long long u = blockIdx.x + (long long)blockIdx.y * gridDim.x; u < nunits;
+       u += (long long)gridDim.x * gridDim.y) {
+    const int2 item = d.items[u / bpi];
+    const int m = item.x, s = item.y, slot = m * d.ns + s;
+    const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
+    unsigned long long q = 0ULL;  // CFL quotient bits
+    if (line < nlines) {
+      const int j = line % nt;
+      const int l = line / (nt * ne);
+      double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + (long long)line * nr;
+      const double* __restrict__ grt = d.grt + ((long long)l * nt + j) * nr;
+      const double* __restrict__ cr = d.cr + ((long long)m * nt + j) * nr;
+      const int* __restrict__ outside = d.outside + (long long)j * nr;
+      const double p4 = d.p4[s * ne + (line / nt) % ne];
+      const double beta = d.betalim;
+      const bool closed = d.flags & 1u;
 
-    const int k = (line / nt) % ne;
-    const double cN = fma(grt[nr - 1], p4, cr[nr - 1]);
-    const double cNm = fma(grt[nr - 2], p4, cr[nr - 2]);
-    const bool inflow = is_neg(cN);
-    // F(NR+1), F(NR+2): boundary ghosts on inflow lines.  On an outflow line
-    // F(NR+1) is read only by face NR-1 when it is upwinded from the right,
-    // and then it is the stale value of the most recent inflow line in the
-    // reference's K->L->J loop order (F persists across lines in DRIFTR).
-    double g1 = 0.0, g2 = 0.0;
-    if (inflow) {  // line index = (L*NE+K)*NT+J, the layout of FGEOS(J,K,L)
-      g1 = ghost_value(d, slot, j, k, l, d.conf1);
-      g2 = ghost_value(d, slot, j, k, l, d.conf2);
-    } else if (is_neg(cNm)) {
-      g1 = stale_ghost(d, m, slot, j, k, l, p4);
+      const int k = (line / nt) % ne;
+      const double cN = fma(grt[nr - 1], p4, cr[nr - 1]);
+      const double cNm = fma(grt[nr - 2], p4, cr[nr - 2]);
+      const bool inflow = is_neg(cN);
+      // F(NR+1), F(NR+2): boundary ghosts on inflow lines.  On an outflow line
+      // F(NR+1) is read only by face NR-1 when it is upwinded from the right,
+      // and then it is the stale value of the most recent inflow line in the
+      // reference's K->L->J loop order (F persists across lines in DRIFTR).
+      double g1 = 0.0, g2 = 0.0;
+      if (inflow) {  // line index = (L*NE+K)*NT+J, the layout of FGEOS(J,K,L)
+        g1 = ghost_value(d, slot, j, k, l, d.conf1);
+        g2 = ghost_value(d, slot, j, k, l, d.conf2);
+      } else if (is_neg(cNm)) {
+        g1 = stale_ghost(d, m, slot, j, k, l, p4);
+      }
+      double gm = fl[0], g0 = fl[1], gp = fl[2];
+      double c = fma(grt[0], p4, cr[0]);
+      if (kCfl && outside[0] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
+      // face 1: FBND(1) = 0 (outflow) or F(2) (inflow)
+      double phi_prev = c * ((inflow && !closed) ? g0 : 0.0);
+      double xm = g0 - gm, bxm = beta * fabs(xm);
+      double x = gp - g0, bx = beta * fabs(x);
+      for (int f = 2; f <= nr - 1; ++f) {  // 1-based face f, updates cell f
+        const double gpp = (f + 2 <= nr) ? fl[f + 1] : g1;
+        const double xp = gpp - gp, bxp = beta * fabs(xp);
+        c = fma(grt[f - 1], p4, cr[f - 1]);
+        if (kCfl && outside[f - 1] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
+        const bool neg = is_neg(c);
+        const double a = fma(c, -0.5, neg ? -0.5 : 0.5);
+        const double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
+        const double phi = c * fb;
+        fl[f - 1] = clip((g0 - phi) + phi_prev);
+        phi_prev = phi;
+        gm = g0; g0 = gp; gp = gpp;
+        xm = x; bxm = bx; x = xp; bx = bxp;
+      }
+      // face NR (g0 = F(NR), gp = F(NR+1), x = X(NR))
+      if (kCfl && outside[nr - 1] == 0) q = umax64(q, cfl_bits(cN, kBits1em10));
+      double fbn;
+      if (!inflow) {
+        fbn = g0;
+      } else {
+        const double xp = g2 - g1, bxp = beta * fabs(xp);
+        fbn = face_value(x, bx, xp, bxp, g1, fma(cN, -0.5, -0.5));
+      }
+      if (closed) fbn = 0.0;
+      const double phin = cN * fbn;
+      fl[nr - 1] = clip((g0 - phin) + phi_prev);
     }
-    double gm = fl[0], g0 = fl[1], gp = fl[2];
-    double c = fma(grt[0], p4, cr[0]);
-    if (kCfl && outside[0] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
-    // face 1: FBND(1) = 0 (outflow) or F(2) (inflow)
-    double phi_prev = c * ((inflow && !closed) ? g0 : 0.0);
-    double xm = g0 - gm, bxm = beta * fabs(xm);
-    double x = gp - g0, bx = beta * fabs(x);
-    for (int f = 2; f <= nr - 1; ++f) {  // 1-based face f, updates cell f
-      const double gpp = (f + 2 <= nr) ? fl[f + 1] : g1;
-      const double xp = gpp - gp, bxp = beta * fabs(xp);
-      c = fma(grt[f - 1], p4, cr[f - 1]);
-      if (kCfl && outside[f - 1] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
-      const bool neg = is_neg(c);
-      const double a = fma(c, -0.5, neg ? -0.5 : 0.5);
-      const double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
-      const double phi = c * fb;
-      fl[f - 1] = clip((g0 - phi) + phi_prev);
-      phi_prev = phi;
-      gm = g0; g0 = gp; gp = gpp;
-      xm = x; bxm = bx; x = xp; bx = bxp;
-    }
-    // face NR (g0 = F(NR), gp = F(NR+1), x = X(NR))
-    if (kCfl && outside[nr - 1] == 0) q = umax64(q, cfl_bits(cN, kBits1em10));
-    double fbn;
-    if (!inflow) {
-      fbn = g0;
-    } else {
-      const double xp = g2 - g1, bxp = beta * fabs(xp);
-      fbn = face_value(x, bx, xp, bxp, g1, fma(cN, -0.5, -0.5));
-    }
-    if (closed) fbn = 0.0;
-    const double phin = cN * fbn;
-    fl[nr - 1] = clip((g0 - phin) + phi_prev);
+    if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 0], q);
   }
-  if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 0], q);
 }
 
 // ----------------------------------------------------------------- DRIFTP
 // Line (I,K,L), I = 2..NR, along J = 1..NT, periodic with J=1 == J=NT.
 template <bool kCfl>
-__global__ void __launch_bounds__(128) k_sweep_p(Dev d, double dts) {
+__global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * ne * d.npa;
-  const int2 item = d.items[blockIdx.y];
-  const int m = item.x, s = item.y, slot = m * d.ns + s;
-  const int line = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long q = 0ULL;  // CFL quotient bits
-  if (line < nlines) {
-    const int i = 1 + line % (nr - 1);
-    const int kl = line / (nr - 1);
-    const int k = kl % ne, l = kl / ne;
-    const long long st = nr;  // stride between consecutive J
-    double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + ((long long)kl * nt) * nr + i;
-    const double* __restrict__ gpt = d.gpt + ((long long)l * nt) * nr + i;
-    const double* __restrict__ ca = d.ca + ((long long)m * nt) * nr + i;
-    const int* __restrict__ outside = d.outside + i;
-    const double p2 = d.p2[((long long)s * ne + k) * nr + i];
-    const double beta = d.betalim;
-#define GJ(J) fl[(long long)((J)-1) * st]
-#define CJ(J) fma(gpt[(long long)((J)-1) * nr], p2, ca[(long long)((J)-1) * nr])
-    const double G1 = GJ(1), G2 = GJ(2), G3 = GJ(3), GNm = GJ(nt - 1), GN = GJ(nt);
-    const double X1 = G2 - G1, bX1 = beta * fabs(X1);
-    const double X2 = G3 - G2, bX2 = beta * fabs(X2);
-    const double XNm = GN - GNm, bXNm = beta * fabs(XNm);
-    const double XN = G2 - GN, bXN = beta * fabs(XN);
-    // face NT first: its flux enters cell 2 through FBND(1)=FBND(NT)
-    const double cN = CJ(nt);
-    if (kCfl && outside[(long long)(nt - 1) * nr] == 0) q = umax64(q, cfl_bits(cN, kBits1em10));
-    double phiN;
-    {
-      const bool neg = is_neg(cN);
-      const double a = fma(cN, -0.5, neg ? -0.5 : 0.5);
-      phiN = cN * face_value(XN, bXN, neg ? X2 : XNm, neg ? bX2 : bXNm, neg ? G2 : GN, a);
-    }
-    double phi_prev = phiN;
-    double g0 = G2, gp = G3, xm = X1, bxm = bX1, x = X2, bx = bX2;
-    for (int J = 2; J <= nt - 1; ++J) {
-      double gpp = 0.0, xp, bxp;
-      if (J <= nt - 3) {
-        gpp = GJ(J + 2);
-        xp = gpp - gp;
-        bxp = beta * fabs(xp);
-      } else if (J == nt - 2) {
-        gpp = GN;
-        xp = XNm;
-        bxp = bXNm;
-      } else {  // J = NT-1: N = NT+1 wraps to 2, D = F(2)-F(1)
-        xp = X1;
-        bxp = bX1;
+  // Work units are (item, block of lines).  A grid of (blocks per item,
+  // items) gives one unit per CTA; a persistent grid loops over them.
+  const int bpi = (nlines + blockDim.x - 1) / blockDim.x;
+  const long long nunits = (long long)bpi * d.nitems;
+  for (long long u = blockIdx.x + (long long)blockIdx.y * gridDim.x; u < nunits;
+       u += (long long)gridDim.x * gridDim.y) {
+    const int2 item = d.items[u / bpi];
+    const int m = item.x, s = item.y, slot = m * d.ns + s;
+    const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
+    unsigned long long q = 0ULL;  // CFL quotient bits
+    if (line < nlines) {
+      const int i = 1 + line % (nr - 1);
+      const int kl = line / (nr - 1);
+      const int k = kl % ne, l = kl / ne;
+      const long long st = nr;  // stride between consecutive J
+      double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + ((long long)kl * nt) * nr + i;
+      const double* __restrict__ gpt = d.gpt + ((long long)l * nt) * nr + i;
+      const double* __restrict__ ca = d.ca + ((long long)m * nt) * nr + i;
+      const int* __restrict__ outside = d.outside + i;
+      const double p2 = d.p2[((long long)s * ne + k) * nr + i];
+      const double beta = d.betalim;
+  #define GJ(J) fl[(long long)((J)-1) * st]
+  #define CJ(J) fma(gpt[(long long)((J)-1) * nr], p2, ca[(long long)((J)-1) * nr])
+      const double G1 = GJ(1), G2 = GJ(2), G3 = GJ(3), GNm = GJ(nt - 1), GN = GJ(nt);
+      const double X1 = G2 - G1, bX1 = beta * fabs(X1);
+      const double X2 = G3 - G2, bX2 = beta * fabs(X2);
+      const double XNm = GN - GNm, bXNm = beta * fabs(XNm);
+      const double XN = G2 - GN, bXN = beta * fabs(XN);
+      // face NT first: its flux enters cell 2 through FBND(1)=FBND(NT)
+      const double cN = CJ(nt);
+      if (kCfl && outside[(long long)(nt - 1) * nr] == 0) q = umax64(q, cfl_bits(cN, kBits1em10));
+      double phiN;
+      {
+        const bool neg = is_neg(cN);
+        const double a = fma(cN, -0.5, neg ? -0.5 : 0.5);
+        phiN = cN * face_value(XN, bXN, neg ? X2 : XNm, neg ? bX2 : bXNm, neg ? G2 : GN, a);
       }
-      const double c = CJ(J);
-      if (kCfl && outside[(long long)(J - 1) * nr] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
-      const bool neg = is_neg(c);
-      const double a = fma(c, -0.5, neg ? -0.5 : 0.5);
-      const double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
-      const double phi = c * fb;
-      GJ(J) = clip((g0 - phi) + phi_prev);
-      phi_prev = phi;
-      g0 = gp; gp = gpp;
-      xm = x; bxm = bx; x = xp; bx = bxp;
+      double phi_prev = phiN;
+      double g0 = G2, gp = G3, xm = X1, bxm = bX1, x = X2, bx = bX2;
+      for (int J = 2; J <= nt - 1; ++J) {
+        double gpp = 0.0, xp, bxp;
+        if (J <= nt - 3) {
+          gpp = GJ(J + 2);
+          xp = gpp - gp;
+          bxp = beta * fabs(xp);
+        } else if (J == nt - 2) {
+          gpp = GN;
+          xp = XNm;
+          bxp = bXNm;
+        } else {  // J = NT-1: N = NT+1 wraps to 2, D = F(2)-F(1)
+          xp = X1;
+          bxp = bX1;
+        }
+        const double c = CJ(J);
+        if (kCfl && outside[(long long)(J - 1) * nr] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
+        const bool neg = is_neg(c);
+        const double a = fma(c, -0.5, neg ? -0.5 : 0.5);
+        const double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
+        const double phi = c * fb;
+        GJ(J) = clip((g0 - phi) + phi_prev);
+        phi_prev = phi;
+        g0 = gp; gp = gpp;
+        xm = x; bxm = bx; x = xp; bx = bxp;
+      }
+      const double vN = clip((GN - phiN) + phi_prev);
+      GJ(nt) = vN;
+      GJ(1) = vN;
+  #undef GJ
+  #undef CJ
     }
-    const double vN = clip((GN - phiN) + phi_prev);
-    GJ(nt) = vN;
-    GJ(1) = vN;
-#undef GJ
-#undef CJ
+    if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 1], q);
   }
-  if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 1], q);
 }
 
 // ----------------------------------------------------------------- DRIFTE
 // Line (I,J,L), I = 2..NR, along K = 1..NE with extrapolated F(0), F(1)
 // and F(NE+1) = F(NE+2) = 0.  Cell K = 1 is never written.
 template <bool kCfl>
-__global__ void __launch_bounds__(128) k_sweep_e(Dev d, double dts) {
+__global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * nt * d.npa;
-  const int2 item = d.items[blockIdx.y];
-  const int m = item.x, s = item.y, slot = m * d.ns + s;
-  const int line = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long q = 0ULL;  // CFL quotient bits
-  if (line < nlines) {
-    const int i = 1 + line % (nr - 1);
-    const int jl = line / (nr - 1);
-    const int j = jl % nt, l = jl / nt;
-    const long long st = (long long)nt * nr;  // stride between consecutive K
-    double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + ((long long)l * ne * nt + j) * nr + i;
-    const long long fij = ((long long)l * nt + j) * nr + i;
-    const double wet = d.wet[fij];
-    const double ue = d.ue[(long long)m * nr * nt * d.npa + fij];
-    const double* __restrict__ edot = d.edot + (long long)s * ne * nr + i;
-    const double* __restrict__ eb = d.eb + s * ne;
-    const double* __restrict__ mhde = d.mhde;
-    const double* __restrict__ iwe = d.iwe;
-    const bool inside = d.outside[(long long)j * nr + i] == 0;
-    const double beta = d.betalim;
-    const bool closed = d.flags & 1u;
-#define GK(K) fl[(long long)((K)-1) * st]
-#define CK(K) (edot[(long long)((K)-1) * nr] * fma(eb[(K)-1], wet, ue))
-    const double F2v = GK(2);
-    const double G1 = d.kap[2 * s + 1] * F2v;
-    const double G0 = d.kap[2 * s + 0] * G1;
-    const double G2 = F2v, G3 = GK(3);
-    const double X0 = G1 - G0, bX0 = beta * fabs(X0);
-    const double X1 = G2 - G1, bX1 = beta * fabs(X1);
-    const double X2 = G3 - G2, bX2 = beta * fabs(X2);
-    double phi_prev;
-    {
-      const double c = CK(1);
-      if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em10)) * d.ide[0]));
-      const bool neg = is_neg(c);
-      const double a = fma(c, mhde[0], neg ? -0.5 : 0.5);
-      double fb = face_value(X1, bX1, neg ? X2 : X0, neg ? bX2 : bX0, neg ? G2 : G1, a);
-      if (closed) fb = 0.0;
-      phi_prev = c * fb;
+  // Work units are (item, block of lines).  A grid of (blocks per item,
+  // items) gives one unit per CTA; a persistent grid loops over them.
+  const int bpi = (nlines + blockDim.x - 1) / blockDim.x;
+  const long long nunits = (long long)bpi * d.nitems;
+  for (long long u = blockIdx.x + (long long)blockIdx.y * gridDim.x; u < nunits;
+       u += (long long)gridDim.x * gridDim.y) {
+    const int2 item = d.items[u / bpi];
+    const int m = item.x, s = item.y, slot = m * d.ns + s;
+    const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
+    unsigned long long q = 0ULL;  // CFL quotient bits
+    if (line < nlines) {
+      const int i = 1 + line % (nr - 1);
+      const int jl = line / (nr - 1);
+      const int j = jl % nt, l = jl / nt;
+      const long long st = (long long)nt * nr;  // stride between consecutive K
+      double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + ((long long)l * ne * nt + j) * nr + i;
+      const long long fij = ((long long)l * nt + j) * nr + i;
+      const double wet = d.wet[fij];
+      const double ue = d.ue[(long long)m * nr * nt * d.npa + fij];
+      const double* __restrict__ edot = d.edot + (long long)s * ne * nr + i;
+      const double* __restrict__ eb = d.eb + s * ne;
+      const double* __restrict__ mhde = d.mhde;
+      const double* __restrict__ iwe = d.iwe;
+      const bool inside = d.outside[(long long)j * nr + i] == 0;
+      const double beta = d.betalim;
+      const bool closed = d.flags & 1u;
+  #define GK(K) fl[(long long)((K)-1) * st]
+  #define CK(K) (edot[(long long)((K)-1) * nr] * fma(eb[(K)-1], wet, ue))
+      const double F2v = GK(2);
+      const double G1 = d.kap[2 * s + 1] * F2v;
+      const double G0 = d.kap[2 * s + 0] * G1;
+      const double G2 = F2v, G3 = GK(3);
+      const double X0 = G1 - G0, bX0 = beta * fabs(X0);
+      const double X1 = G2 - G1, bX1 = beta * fabs(X1);
+      const double X2 = G3 - G2, bX2 = beta * fabs(X2);
+      double phi_prev;
+      {
+        const double c = CK(1);
+        if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em10)) * d.ide[0]));
+        const bool neg = is_neg(c);
+        const double a = fma(c, mhde[0], neg ? -0.5 : 0.5);
+        double fb = face_value(X1, bX1, neg ? X2 : X0, neg ? bX2 : bX0, neg ? G2 : G1, a);
+        if (closed) fb = 0.0;
+        phi_prev = c * fb;
+      }
+      double g0 = G2, gp = G3, xm = X1, bxm = bX1, x = X2, bx = bX2;
+      for (int K = 2; K <= ne; ++K) {
+        const double gpp = (K + 2 <= ne) ? GK(K + 2) : 0.0;
+        const double xp = gpp - gp, bxp = beta * fabs(xp);
+        const double c = CK(K);
+        if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em10)) * d.ide[K - 1]));
+        const bool neg = is_neg(c);
+        const double a = fma(c, mhde[K - 1], neg ? -0.5 : 0.5);
+        double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
+        if (closed && K == ne) fb = 0.0;
+        const double phi = c * fb;
+        GK(K) = clip(fma(phi_prev - phi, iwe[K - 1], g0));
+        phi_prev = phi;
+        g0 = gp; gp = gpp;
+        xm = x; bxm = bx; x = xp; bx = bxp;
+      }
+  #undef GK
+  #undef CK
     }
-    double g0 = G2, gp = G3, xm = X1, bxm = bX1, x = X2, bx = bX2;
-    for (int K = 2; K <= ne; ++K) {
-      const double gpp = (K + 2 <= ne) ? GK(K + 2) : 0.0;
-      const double xp = gpp - gp, bxp = beta * fabs(xp);
-      const double c = CK(K);
-      if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em10)) * d.ide[K - 1]));
-      const bool neg = is_neg(c);
-      const double a = fma(c, mhde[K - 1], neg ? -0.5 : 0.5);
-      double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
-      if (closed && K == ne) fb = 0.0;
-      const double phi = c * fb;
-      GK(K) = clip(fma(phi_prev - phi, iwe[K - 1], g0));
-      phi_prev = phi;
-      g0 = gp; gp = gpp;
-      xm = x; bxm = bx; x = xp; bx = bxp;
-    }
-#undef GK
-#undef CK
+    if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 2], q);
   }
-  if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 2], q);
 }
 
 // ---------------------------------------------------------------- DRIFTMU
@@ -236,112 +257,144 @@ __global__ void __launch_bounds__(128) k_sweep_e(Dev d, double dts) {
 // kLoss: 0 none, 1 multiply the result by table lossA (loss after the sweep),
 //        2 multiply the input by lossA (loss before the sweep).
 template <bool kCfl, int kLoss>
-__global__ void __launch_bounds__(128) k_sweep_mu(Dev d, double dts, const double* __restrict__ lossA) {
+__global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const double* __restrict__ lossA) {
   const int nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa;
   const int nlines = (nr - 1) * nt * ne;
-  const int2 item = d.items[blockIdx.y];
-  const int m = item.x, s = item.y, slot = m * d.ns + s;
-  const int line = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long q = 0ULL;  // CFL quotient bits
-  if (line < nlines) {
-    const int i = 1 + line % (nr - 1);
-    const int jk = line / (nr - 1);
-    const int j = jk % nt;
-    const long long st = (long long)ne * nt * nr;  // stride between consecutive L
-    const long long off = (long long)jk * nr + i;  // (K*NT + J)*NR + I
-    double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + off;
-    const double* __restrict__ la = lossA ? lossA + (long long)s * d.ncell + off : nullptr;
-    const long long sij = (long long)nt * nr;     // stride of (I,J,L) tables in L
-    const long long fij = (long long)j * nr + i;
-    const double* __restrict__ wm = d.wm + fij;
-    const double* __restrict__ um = d.um + (long long)m * nt * nr * npa + fij;
-    const double ekv = d.ek[s * ne + jk / nt];
-    const double* __restrict__ mhdmu = d.mhdmu;
-    const double* __restrict__ iwmu = d.iwmu;
-    const bool inside = d.outside[fij] == 0;
-    const double beta = d.betalim;
-    const bool closed = d.flags & 1u;
-#define GL(L) fl[(long long)((L)-1) * st]
-#define LA(L) la[(long long)((L)-1) * st]
-#define CL(L) fma(ekv, wm[(long long)((L)-1) * sij], um[(long long)((L)-1) * sij])
-    double G2 = GL(2), G3 = GL(3);
-    if (kLoss == 2) { G2 *= LA(2); G3 *= LA(3); }
-    const double X1 = 0.0, bX1 = 0.0;  // F(2) - F(1) with F(1) = F(2)
-    double phi_prev = 0.0;              // CDriftMu(1) = 0, FBND(1) = 0
-    double g0 = G2, gp = G3, xm = X1, bxm = bX1;
-    double x = G3 - G2, bx = beta * fabs(x);
-    for (int L = 2; L <= npa - 2; ++L) {
-      double gpp = GL(L + 2);
-      if (kLoss == 2) gpp *= LA(L + 2);
-      const double xp = gpp - gp, bxp = beta * fabs(xp);
-      const double c = CL(L);
-      if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
-      const bool neg = is_neg(c);
-      const double a = fma(c, mhdmu[L - 1], neg ? -0.5 : 0.5);
-      const double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
-      const double phi = c * fb;
-      double v = clip(fma(phi_prev - phi, iwmu[L - 1], g0));
-      if (kLoss == 1) v *= LA(L);
-      GL(L) = v;
-      phi_prev = phi;
-      g0 = gp; gp = gpp;
-      xm = x; bxm = bx; x = xp; bx = bxp;
-    }
-    // face NPA-1: FBND = F(NPA); cell NPA-1; then the F2(NPA) ghost
-    {
-      const int L = npa - 1;
-      const double c = CL(L);
-      if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
-      const double phi = c * (closed ? 0.0 : gp);
-      const double v = clip(fma(phi_prev - phi, iwmu[L - 1], g0));
-      const double vN = v * d.rho[fij];
-      if (kLoss == 1) {
-        GL(L) = v * LA(L);
-        GL(npa) = vN * LA(npa);
-      } else {
+  // Work units are (item, block of lines).  A grid of (blocks per item,
+  // items) gives one unit per CTA; a persistent grid loops over them.
+  const int bpi = (nlines + blockDim.x - 1) / blockDim.x;
+  const long long nunits = (long long)bpi * d.nitems;
+  for (long long u = blockIdx.x + (long long)blockIdx.y * gridDim.x; u < nunits;
+       u += (long long)gridDim.x * gridDim.y) {
+    const int2 item = d.items[u / bpi];
+    const int m = item.x, s = item.y, slot = m * d.ns + s;
+    const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
+    unsigned long long q = 0ULL;  // CFL quotient bits
+    if (line < nlines) {
+      const int i = 1 + line % (nr - 1);
+      const int jk = line / (nr - 1);
+      const int j = jk % nt;
+      const long long st = (long long)ne * nt * nr;  // stride between consecutive L
+      const long long off = (long long)jk * nr + i;  // (K*NT + J)*NR + I
+      double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + off;
+      const double* __restrict__ la = lossA ? lossA + (long long)s * d.ncell + off : nullptr;
+      const long long sij = (long long)nt * nr;     // stride of (I,J,L) tables in L
+      const long long fij = (long long)j * nr + i;
+      const double* __restrict__ wm = d.wm + fij;
+      const double* __restrict__ um = d.um + (long long)m * nt * nr * npa + fij;
+      const double ekv = d.ek[s * ne + jk / nt];
+      const double* __restrict__ mhdmu = d.mhdmu;
+      const double* __restrict__ iwmu = d.iwmu;
+      const bool inside = d.outside[fij] == 0;
+      const double beta = d.betalim;
+      const bool closed = d.flags & 1u;
+  #define GL(L) fl[(long long)((L)-1) * st]
+  #define LA(L) la[(long long)((L)-1) * st]
+  #define CL(L) fma(ekv, wm[(long long)((L)-1) * sij], um[(long long)((L)-1) * sij])
+      double G2 = GL(2), G3 = GL(3);
+      if (kLoss == 2) { G2 *= LA(2); G3 *= LA(3); }
+      const double X1 = 0.0, bX1 = 0.0;  // F(2) - F(1) with F(1) = F(2)
+      double phi_prev = 0.0;              // CDriftMu(1) = 0, FBND(1) = 0
+      double g0 = G2, gp = G3, xm = X1, bxm = bX1;
+      double x = G3 - G2, bx = beta * fabs(x);
+      for (int L = 2; L <= npa - 2; ++L) {
+        double gpp = GL(L + 2);
+        if (kLoss == 2) gpp *= LA(L + 2);
+        const double xp = gpp - gp, bxp = beta * fabs(xp);
+        const double c = CL(L);
+        if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
+        const bool neg = is_neg(c);
+        const double a = fma(c, mhdmu[L - 1], neg ? -0.5 : 0.5);
+        const double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
+        const double phi = c * fb;
+        double v = clip(fma(phi_prev - phi, iwmu[L - 1], g0));
+        if (kLoss == 1) v *= LA(L);
         GL(L) = v;
-        GL(npa) = vN;
+        phi_prev = phi;
+        g0 = gp; gp = gpp;
+        xm = x; bxm = bx; x = xp; bx = bxp;
       }
+      // face NPA-1: FBND = F(NPA); cell NPA-1; then the F2(NPA) ghost
+      {
+        const int L = npa - 1;
+        const double c = CL(L);
+        if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
+        const double phi = c * (closed ? 0.0 : gp);
+        const double v = clip(fma(phi_prev - phi, iwmu[L - 1], g0));
+        const double vN = v * d.rho[fij];
+        if (kLoss == 1) {
+          GL(L) = v * LA(L);
+          GL(npa) = vN * LA(npa);
+        } else {
+          GL(L) = v;
+          GL(npa) = vN;
+        }
+      }
+  #undef GL
+  #undef LA
+  #undef CL
     }
-#undef GL
-#undef LA
-#undef CL
+    if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 3], q);
   }
-  if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 3], q);
 }
 
 // ---------------------------------------------------------------- launchers
-static inline dim3 grid_for(int nlines, int nitems, int block) {
-  return dim3((nlines + block - 1) / block, nitems, 1);
+// Grid: (blocks per item, items), or a persistent grid of d.pers[w] CTAs.
+static inline dim3 grid_for(const Dev& d, int w, int nlines) {
+  const int blk = d.blk[w];
+  if (d.pers[w] > 0) return dim3(d.pers[w], 1, 1);
+  return dim3((nlines + blk - 1) / blk, d.nitems, 1);
+}
+static inline int nlines_of(const Dev& d, int w) {
+  switch (w) {
+    case 0: return d.nt * d.ne * d.npa;
+    case 1: return (d.nr - 1) * d.ne * d.npa;
+    case 2: return (d.nr - 1) * d.nt * d.npa;
+    default: return (d.nr - 1) * d.nt * d.ne;
+  }
 }
 
 void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st) {
-  dim3 g = grid_for(d.nt * d.ne * d.npa, d.nitems, 128);
-  if (cfl) k_sweep_r<true><<<g, 128, 0, st>>>(d, dts);
-  else k_sweep_r<false><<<g, 128, 0, st>>>(d, dts);
+  dim3 g = grid_for(d, 0, nlines_of(d, 0));
+  if (cfl) k_sweep_r<true><<<g, d.blk[0], 0, st>>>(d, dts);
+  else k_sweep_r<false><<<g, d.blk[0], 0, st>>>(d, dts);
 }
 void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st) {
-  dim3 g = grid_for((d.nr - 1) * d.ne * d.npa, d.nitems, 128);
-  if (cfl) k_sweep_p<true><<<g, 128, 0, st>>>(d, dts);
-  else k_sweep_p<false><<<g, 128, 0, st>>>(d, dts);
+  dim3 g = grid_for(d, 1, nlines_of(d, 1));
+  if (cfl) k_sweep_p<true><<<g, d.blk[1], 0, st>>>(d, dts);
+  else k_sweep_p<false><<<g, d.blk[1], 0, st>>>(d, dts);
 }
 void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st) {
-  dim3 g = grid_for((d.nr - 1) * d.nt * d.npa, d.nitems, 64);
-  if (cfl) k_sweep_e<true><<<g, 64, 0, st>>>(d, dts);
-  else k_sweep_e<false><<<g, 64, 0, st>>>(d, dts);
+  dim3 g = grid_for(d, 2, nlines_of(d, 2));
+  if (cfl) k_sweep_e<true><<<g, d.blk[2], 0, st>>>(d, dts);
+  else k_sweep_e<false><<<g, d.blk[2], 0, st>>>(d, dts);
 }
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
                      cudaStream_t st) {
-  dim3 g = grid_for((d.nr - 1) * d.nt * d.ne, d.nitems, 64);
+  dim3 g = grid_for(d, 3, nlines_of(d, 3));
+  const int b = d.blk[3];
   if (cfl) {
-    if (loss_mode == 1) k_sweep_mu<true, 1><<<g, 64, 0, st>>>(d, dts, loss);
-    else if (loss_mode == 2) k_sweep_mu<true, 2><<<g, 64, 0, st>>>(d, dts, loss);
-    else k_sweep_mu<true, 0><<<g, 64, 0, st>>>(d, dts, nullptr);
+    if (loss_mode == 1) k_sweep_mu<true, 1><<<g, b, 0, st>>>(d, dts, loss);
+    else if (loss_mode == 2) k_sweep_mu<true, 2><<<g, b, 0, st>>>(d, dts, loss);
+    else k_sweep_mu<true, 0><<<g, b, 0, st>>>(d, dts, nullptr);
   } else {
-    if (loss_mode == 1) k_sweep_mu<false, 1><<<g, 64, 0, st>>>(d, dts, loss);
-    else if (loss_mode == 2) k_sweep_mu<false, 2><<<g, 64, 0, st>>>(d, dts, loss);
-    else k_sweep_mu<false, 0><<<g, 64, 0, st>>>(d, dts, nullptr);
+    if (loss_mode == 1) k_sweep_mu<false, 1><<<g, b, 0, st>>>(d, dts, loss);
+    else if (loss_mode == 2) k_sweep_mu<false, 2><<<g, b, 0, st>>>(d, dts, loss);
+    else k_sweep_mu<false, 0><<<g, b, 0, st>>>(d, dts, nullptr);
   }
+}
+
+// Resident CTAs per SM of sweep w at block size blk (for persistent grids).
+int sweep_max_blocks_per_sm(int w, int blk) {
+  int n = 0;
+  cudaError_t e = cudaSuccess;
+  switch (w) {
+    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_r<false>, blk, 0); break;
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_p<false>, blk, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_e<false>, blk, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_mu<false, 0>, blk, 0); break;
+  }
+  return e == cudaSuccess ? n : 0;
 }
 
 }  // namespace ramgpu

@@ -267,64 +267,78 @@ __global__ void k_vt(Dev d) {
   if (t >= (long long)d.nm * nv) return;
   const int m = (int)(t / nv);
   if (d.vt_mode[m] != 1) return;
-  const int I = 1 + (int)(t % nv) % d.nf;
-  const int J = 1 + (int)(t % nv) / d.nf;
+  const int i = (int)(t % nv) % d.nf;
+  const int j = (int)(t % nv) / d.nf;
   const double KP = d.kp[m];
   const double tt = 1. - 0.159 * KP + 0.0093 * (KP * KP);
   const double AVS = 7.05E-6 / (tt * tt * tt) / kRE;
-  const double PHIOFS = 0 * kPI / 12.;
-  const double lr = LZ(I) * kRE;
-  d.vt[t] = AVS * (lr * lr) * sin(d.phi[J - 1] - PHIOFS);
+  // VT = AVS*(LZ*RE)**2*SIN(PHI-PHIOFS), with (LZ*RE)**2 and SIN(PHI) tabulated
+  d.vt[t] = AVS * d.lr2[i] * d.sinphi[j];
 }
 
-__global__ void k_member_coef(Dev d, double DTs) {
-  const long long per = (long long)d.nr * d.nt * d.npa;
+// Per (member, I, J): the E x B terms of DRIFTR and DRIFTP and the
+// DRD1/DPD1 (= DRM1/DPM1) factors of DRIFTE/DRIFTMU.
+__global__ void k_member_ij(Dev d, double DTs) {
+  const long long per = (long long)d.nr * d.nt;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= (long long)d.nm * per) return;
   const int m = (int)(t / per);
-  const long long c = t % per;
-  const int I = 1 + (int)(c % d.nr);
-  const int J = 1 + (int)((c / d.nr) % d.nt);
-  const int L = 1 + (int)(c / ((long long)d.nr * d.nt));
+  const int I = 1 + (int)((t % per) % d.nr);
+  const int J = 1 + (int)((t % per) / d.nr);
   const double* vt = d.vt + (long long)m * d.nf * d.nt;
 #define VT(I, J) vt[BIX(I, J)]
   const double MDR = d.mdr, DPHI = d.dphi;
   int J0, J1;
   wrapj(J, d.nt, J0, J1);
-  if (L == 1) {
-    const long long ij = (long long)m * d.nr * d.nt + (long long)(J - 1) * d.nr + (I - 1);
-    // DRIFTR E x B (src/ModRamDrift.f90:118-127) with VR from DRIFTPARA
-    const double VR = DTs / MDR / (RLZ(I) + 0.5 * MDR) / 2 / DPHI;
-    const double den = BNES(I, J) + BNES(I + 1, J);
-    d.cr[ij] = VR * (VT(I, J0) + VT(I + 1, J0) - VT(I, J1) - VT(I + 1, J1)) / den
-               + (EIP(I, J) + EIP(I + 1, J)) / den * DTs / MDR;
-    double ca = 0.0;
-    if (I >= 2 && J >= 2) {  // DRIFTP E x B, EIR and corotation terms
-      const double P1 = DTs / DPHI / 2 / MDR / RLZ(I);
-      ca = ((VT(I + 1, J) + VT(I + 1, J1) - VT(I - 1, J) - VT(I - 1, J1)) * P1
-            - (EIR(I, J1) + EIR(I, J)) / RLZ(I) * DTs / DPHI) / (BNES(I, J) + BNES(I, J1))
-           + kOME * DTs / DPHI;
-    }
-    d.ca[ij] = ca;
-  }
-  double ue = 0.0, um = 0.0;
+  // DRIFTR E x B (src/ModRamDrift.f90:118-127) with VR from DRIFTPARA
+  const double VR = DTs / MDR / (RLZ(I) + 0.5 * MDR) / 2 / DPHI;
+  const double den = BNES(I, J) + BNES(I + 1, J);
+  d.cr[t] = VR * (VT(I, J0) + VT(I + 1, J0) - VT(I, J1) - VT(I + 1, J1)) / den
+            + (EIP(I, J) + EIP(I + 1, J)) / den * DTs / MDR;
+  double ca = 0.0, drd1 = 0.0, dpd1 = 0.0;
   if (I >= 2) {
     const double R = RLZ(I);
-    const double DRD1 = (EIP(I, J) * R - (VT(I, J1) - VT(I, J0)) / 2. / DPHI) / BNES(I, J);
-    const double DPD1 = kOME * R + ((VT(I + 1, J) - VT(I - 1, J)) / 2 / MDR - EIR(I, J)) / BNES(I, J);
-    ue = d.gre[c] * DRD1 + d.gpe[c] * DPD1 + d.ze[c];
-    um = -d.cmudot[c] * (d.gmr[c] * DRD1 + d.gmp[c] * DPD1 + d.zm[c]);
+    if (J >= 2) {  // DRIFTP E x B, EIR and corotation terms
+      const double P1 = DTs / DPHI / 2 / MDR / R;
+      ca = ((VT(I + 1, J) + VT(I + 1, J1) - VT(I - 1, J) - VT(I - 1, J1)) * P1
+            - (EIR(I, J1) + EIR(I, J)) / R * DTs / DPHI) / (BNES(I, J) + BNES(I, J1))
+           + kOME * DTs / DPHI;
+    }
+    drd1 = (EIP(I, J) * R - (VT(I, J1) - VT(I, J0)) / 2. / DPHI) / BNES(I, J);
+    dpd1 = kOME * R + ((VT(I + 1, J) - VT(I - 1, J)) / 2 / MDR - EIR(I, J)) / BNES(I, J);
+  }
+  d.ca[t] = ca;
+  d.drd1[t] = drd1;
+  d.dpd1[t] = dpd1;
+#undef VT
+}
+
+// Per (member, I, J, L): UE and UM from the (I,J) factors, two fmas each.
+__global__ void k_member_ijl(Dev d) {
+  const long long per = (long long)d.nr * d.nt * d.npa;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)d.nm * per) return;
+  const int m = (int)(t / per);
+  const long long c = t % per;
+  const int i = (int)(c % d.nr);
+  const long long ij = (long long)m * d.nr * d.nt + (c % ((long long)d.nr * d.nt));
+  double ue = 0.0, um = 0.0;
+  if (i >= 1) {
+    const double drd1 = d.drd1[ij], dpd1 = d.dpd1[ij];
+    ue = d.gre[c] * drd1 + d.gpe[c] * dpd1 + d.ze[c];
+    um = -d.cmudot[c] * (d.gmr[c] * drd1 + d.gmp[c] * dpd1 + d.zm[c]);
   }
   d.ue[t] = ue;
   d.um[t] = um;
-#undef VT
 }
 
 void launch_member_coef(const Dev& d, double dts, cudaStream_t st) {
   long long nv = (long long)d.nm * d.nf * d.nt;
   k_vt<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(d);
+  long long nij = (long long)d.nm * d.nr * d.nt;
+  k_member_ij<<<(unsigned)((nij + 127) / 128), 128, 0, st>>>(d, dts);
   long long n = (long long)d.nm * d.nr * d.nt * d.npa;
-  k_member_coef<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, dts);
+  k_member_ijl<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
 }
 
 // ---------------------------------------------------- DRIFTR ghost planes
@@ -359,38 +373,54 @@ __global__ void k_ghost_planes(Dev d) {
 }
 
 // Exclusive "last defined" scan over planes: one block per work item.
+// combine(left, right) = right if right has a value else left (associative),
+// scanned with warp shuffles, then across the 32 warp totals.
+__device__ __forceinline__ void last_scan_warp(int& h, double& v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int lh = __shfl_up_sync(0xffffffffu, h, o);
+    const double lv = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o && !h) { h = lh; v = lv; }
+  }
+}
+
 __global__ void __launch_bounds__(1024) k_ghost_scan(Dev d) {
-  __shared__ int s_has[1024];
-  __shared__ double s_val[1024];
+  __shared__ int s_h[32];
+  __shared__ double s_v[32];
   const int np = d.ne * d.npa;
   const int2 item = d.items[blockIdx.x];
   const int slot = item.x * d.ns + item.y;
   const int* has = d.plane_has + (long long)slot * np;
   const double* last = d.plane_last + (long long)slot * np;
   double* carry = d.plane_carry + (long long)slot * np;
-  const int nt = blockDim.x;
-  const int cs = (np + nt - 1) / nt;
-  const int p0 = threadIdx.x * cs, p1 = min(np, p0 + cs);
+  const int nth = blockDim.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int cs = (np + nth - 1) / nth;
+  const int p0 = min(np, threadIdx.x * cs), p1 = min(np, p0 + cs);
   int h = 0;
   double v = 0.0;
   for (int p = p0; p < p1; ++p)
     if (has[p]) { h = 1; v = last[p]; }
-  s_has[threadIdx.x] = h;
-  s_val[threadIdx.x] = v;
+  // inclusive scan within the warp
+  int ih = h;
+  double iv = v;
+  last_scan_warp(ih, iv);
+  if (lane == 31) { s_h[warp] = ih; s_v[warp] = iv; }
   __syncthreads();
-  if (threadIdx.x == 0) {  // serial exclusive scan over the block's chunks
-    int ch = 0;
-    double cv = 0.0;
-    for (int t = 0; t < nt; ++t) {
-      int th = s_has[t];
-      double tv = s_val[t];
-      s_has[t] = ch;
-      s_val[t] = cv;
-      if (th) { ch = 1; cv = tv; }
-    }
+  if (warp == 0) {
+    int wh = lane < (nth >> 5) ? s_h[lane] : 0;
+    double wv = lane < (nth >> 5) ? s_v[lane] : 0.0;
+    last_scan_warp(wh, wv);  // inclusive over warps
+    s_h[lane] = wh;
+    s_v[lane] = wv;
   }
   __syncthreads();
-  double run = s_val[threadIdx.x];
+  // exclusive value for this thread: inclusive of the previous thread
+  int eh = __shfl_up_sync(0xffffffffu, ih, 1);
+  double ev = __shfl_up_sync(0xffffffffu, iv, 1);
+  if (lane == 0) { eh = 0; ev = 0.0; }
+  if (!eh && warp > 0) { eh = s_h[warp - 1]; ev = s_v[warp - 1]; }
+  double run = eh ? ev : 0.0;
   for (int p = p0; p < p1; ++p) {
     carry[p] = run;
     if (has[p]) run = last[p];
@@ -440,77 +470,105 @@ void launch_finish(const Dev& d, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------- ANISCH moments
-// Stage 1: one thread per (I>=2, J, K>=2): the L=1 side effect and the
-// pitch-angle sums SUME(K), SUMA(K) of src/ModRamRun.f90:366-378.
+// Stage 1: one thread per (I>=2, J, K>=2, L-chunk): the L=1 side effect
+// (chunk 0) and partial pitch-angle sums SUME(K), SUMA(K) over L in the
+// chunk (src/ModRamRun.f90:366-378).  Partials (slot, chunk, K, J, I, 2).
+constexpr int kMomChunks = 4;
 __global__ void k_moments_part(Dev d) {
   const int nr1 = d.nr - 1, ne1 = d.ne - 1;
-  const long long n = (long long)nr1 * d.nt * ne1;
+  const long long n = (long long)nr1 * d.nt * ne1 * kMomChunks;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int2 item = d.items[blockIdx.y];
   const int s = item.y, slot = item.x * d.ns + s;
   const int i = 1 + (int)(t % nr1);
   const int j = (int)((t / nr1) % d.nt);
-  const int k = 1 + (int)(t / ((long long)nr1 * d.nt));
+  const int k = 1 + (int)((t / ((long long)nr1 * d.nt)) % ne1);
+  const int ch = (int)(t / ((long long)nr1 * d.nt * ne1));
   const long long st = (long long)d.ne * d.nt * d.nr;
   const long long off = ((long long)k * d.nt + j) * d.nr + i;
   double* f = d.f2 + (long long)slot * d.ncell + off;
   const double* we = d.epme + (long long)s * d.ncell + off;
   const double* wa = d.epma + (long long)s * d.ncell + off;
   const double f2 = f[st];
-  f[0] = f2;  // F2(S,I,J,K,1) = F2(S,I,J,K,2)
-  double sume = 0.0, suma = 0.0;
+  if (ch == 0) f[0] = f2;  // F2(S,I,J,K,1) = F2(S,I,J,K,2)
   const int u = d.upa_mom[i];
-  for (int L = 1; L <= u; ++L) {
+  const int cl = (d.npa + kMomChunks - 1) / kMomChunks;
+  const int l0 = 1 + ch * cl, l1 = min(u, (ch + 1) * cl);
+  double sume = 0.0, suma = 0.0;
+  for (int L = l0; L <= l1; ++L) {
     const double v = (L == 1) ? f2 : f[(long long)(L - 1) * st];
     sume = fma(v, we[(long long)(L - 1) * st], sume);
     suma = fma(v, wa[(long long)(L - 1) * st], suma);
   }
-  double* part = d.mom_part + (long long)slot * d.nr * d.nt * d.ne * 2;
-  const long long pi = (((long long)k * d.nt + j) * d.nr + i) * 2;
+  double* part = d.mom_part + (long long)slot * kMomChunks * d.nr * d.nt * d.ne * 2;
+  const long long pi = ((((long long)ch * d.ne + k) * d.nt + j) * d.nr + i) * 2;
   part[pi] = sume;
   part[pi + 1] = suma;
 }
 
-// Stage 2: one thread per (I>=2, J): the energy-band sums and RFAC factors.
+// Stage 2: one warp per (I>=2, J).  Lanes combine the chunk partials of 32
+// energies at a time; lane 0 then adds them in the reference's band order
+// (khi = 6,10,25,30,NE) with the RFAC factors.
 __global__ void k_moments_reduce(Dev d) {
   const int nr1 = d.nr - 1;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nr1 * d.nt) return;
+  const int lane = threadIdx.x & 31;
+  const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (t >= nr1 * d.nt) return;  // uniform per warp
   const int2 item = d.items[blockIdx.y];
   const int s = item.y, slot = item.x * d.ns + s;
   const int i = 1 + t % nr1, j = t / nr1;
   const double cv = kCS * 100;
   const double RFAC = 4 * kPI / cv;
-  const double* part = d.mom_part + (long long)slot * d.nr * d.nt * d.ne * 2;
+  const long long cstride = (long long)d.nr * d.nt * d.ne * 2;
+  const double* part = d.mom_part + (long long)slot * kMomChunks * cstride;
   const double* epp = d.epp + s * d.ne;
   int khi[5] = {6, 10, 25, 30, 35};
   khi[4] = d.ne;
-  int klo = 2;
-  double ppert = 0., ppart = 0.;
-  for (int iwa = 0; iwa < 5; ++iwa) {
-    double PPER = 0., PPAR = 0.;
-    for (int K = klo; K <= khi[iwa]; ++K) {
+  int iwa = 0;
+  double PPER = 0., PPAR = 0., ppert = 0., ppart = 0.;
+  for (int base = 2; base <= d.ne; base += 32) {
+    const int K = base + lane;
+    double pe = 0.0, pa = 0.0;
+    if (K <= d.ne) {
       const long long pi = (((long long)(K - 1) * d.nt + j) * d.nr + i) * 2;
-      PPER = PPER + epp[K - 1] * part[pi];
-      PPAR = PPAR + epp[K - 1] * part[pi + 1];
+      double sume = 0.0, suma = 0.0;
+      for (int c = 0; c < kMomChunks; ++c) {
+        sume += part[c * cstride + pi];
+        suma += part[c * cstride + pi + 1];
+      }
+      pe = epp[K - 1] * sume;
+      pa = epp[K - 1] * suma;
     }
-    PPAR = 2 * RFAC * PPAR;
-    PPER = RFAC * PPER;
-    klo = khi[iwa] + 1;
-    ppert = ppert + PPER;
-    ppart = ppart + PPAR;
+    const int kmax = min(32, d.ne - base + 1);
+    for (int q = 0; q < kmax; ++q) {
+      const double ve = __shfl_sync(0xffffffffu, pe, q);
+      const double va = __shfl_sync(0xffffffffu, pa, q);
+      PPER = PPER + ve;
+      PPAR = PPAR + va;
+      if (base + q == khi[iwa]) {  // close the band
+        PPAR = 2 * RFAC * PPAR;
+        PPER = RFAC * PPER;
+        ppert = ppert + PPER;
+        ppart = ppart + PPAR;
+        PPER = 0.;
+        PPAR = 0.;
+        iwa = min(iwa + 1, 4);
+      }
+    }
   }
-  const long long o = (long long)slot * d.nr * d.nt + (long long)j * d.nr + i;
-  d.ppert[o] = ppert;
-  d.ppart[o] = ppart;
+  if (lane == 0) {
+    const long long o = (long long)slot * d.nr * d.nt + (long long)j * d.nr + i;
+    d.ppert[o] = ppert;
+    d.ppart[o] = ppart;
+  }
 }
 
 void launch_moments(const Dev& d, cudaStream_t st) {
-  long long n = (long long)(d.nr - 1) * d.nt * (d.ne - 1);
+  long long n = (long long)(d.nr - 1) * d.nt * (d.ne - 1) * kMomChunks;
   k_moments_part<<<dim3((unsigned)((n + 127) / 128), d.nitems), 128, 0, st>>>(d);
   int n2 = (d.nr - 1) * d.nt;
-  k_moments_reduce<<<dim3((n2 + 127) / 128, d.nitems), 128, 0, st>>>(d);
+  k_moments_reduce<<<dim3((n2 + 3) / 4, d.nitems), 128, 0, st>>>(d);
 }
 
 // ------------------------------------------------------------------ SUMRC

@@ -31,7 +31,8 @@ EXPORTS = (
     "ramgpu_ram_run", "ramgpu_half_step", "ramgpu_ram_run_async", "ramgpu_moments",
     "ramgpu_flux", "ramgpu_cfl", "ramgpu_losses", "ramgpu_reset_losses", "ramgpu_launch_count",
     "ramgpu_apply_op", "ramgpu_set_timing", "ramgpu_kernel_times", "ramgpu_probe_fp64",
-    "ramgpu_sumrc_noalloc",
+    "ramgpu_sumrc_noalloc", "ramgpu_set_graph", "ramgpu_set_launch_shape",
+    "ramgpu_get_launch_shape", "ramgpu_autotune", "ramgpu_set_kp_all",
 )
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
           "anisch", "dts_tables", "sumrc")
@@ -110,6 +111,11 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_kernel_times": ([vp, dp, C.POINTER(C.c_longlong)], i),
         "ramgpu_probe_fp64": ([dp], i),
         "ramgpu_sumrc_noalloc": ([vp, i, i, i, i, dp, dp, dp, vp, dp], i),
+        "ramgpu_set_graph": ([vp, i], i),
+        "ramgpu_set_launch_shape": ([vp, i, i, i], i),
+        "ramgpu_get_launch_shape": ([vp, ip, ip], i),
+        "ramgpu_autotune": ([vp, d, i, dp], i),
+        "ramgpu_set_kp_all": ([vp, dp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -213,6 +219,12 @@ class RamGpu:
     def set_kp(self, member: int, kp: float):
         self._ck(self.lib.ramgpu_set_kp(self.h, member, float(kp)), "set_kp")
 
+    def set_kp_all(self, kp):
+        a = np.ascontiguousarray(kp, dtype=np.float64)
+        if a.size != self.n_members:
+            raise ValueError("need one Kp per member")
+        self._ck(self.lib.ramgpu_set_kp_all(self.h, _dptr(a)), "set_kp_all")
+
     def set_potential(self, member: int, vt):
         a = _fort(vt)
         self._ck(self.lib.ramgpu_set_potential(self.h, member, _dptr(a)), "set_potential")
@@ -293,6 +305,27 @@ class RamGpu:
         self._ck(self.lib.ramgpu_kernel_times(self.h, _dptr(ms), cnt.ctypes.data_as(C.POINTER(C.c_longlong))),
                  "kernel_times")
         return {KCLASS[k]: (float(ms[k]), int(cnt[k])) for k in range(len(KCLASS)) if cnt[k]}
+
+    def set_graph(self, enable: bool):
+        self._ck(self.lib.ramgpu_set_graph(self.h, int(bool(enable))), "set_graph")
+
+    def set_launch_shape(self, sweep: int, threads: int, persistent_ctas: int = 0):
+        self._ck(self.lib.ramgpu_set_launch_shape(self.h, sweep, threads, persistent_ctas),
+                 "set_launch_shape")
+
+    def launch_shape(self):
+        t = np.zeros(4, dtype=np.int32)
+        p = np.zeros(4, dtype=np.int32)
+        self._ck(self.lib.ramgpu_get_launch_shape(self.h, t.ctypes.data_as(C.POINTER(C.c_int)),
+                                                  p.ctypes.data_as(C.POINTER(C.c_int))), "launch_shape")
+        return [(int(a), int(b)) for a, b in zip(t, p)]
+
+    def autotune(self, dts: float, reps: int = 3):
+        """Pick threads/CTA and persistent-vs-plain grid per sweep by timing;
+        returns the chosen shapes and their average launch times [ms]."""
+        ms = np.zeros(4)
+        self._ck(self.lib.ramgpu_autotune(self.h, float(dts), int(reps), _dptr(ms)), "autotune")
+        return self.launch_shape(), ms
 
     def set_stream(self, stream_ptr: int):
         self._ck(self.lib.ramgpu_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")

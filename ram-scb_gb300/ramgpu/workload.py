@@ -505,3 +505,45 @@ def make_workload(name: str, seed: int = 2024) -> Workload:
     fg = [boundary_fgeos(g, s, kt=params[s][0], density_scale=params[s][1]) for s in range(len(sp))]
     return Workload(name=name, grid=g, fields=fl, f2=f2, fgeos=fg, kp=kp, dts=dts, steps=steps,
                     meta={"seed": seed, "species": [s.name for s in sp]})
+
+
+# ---------------------------------------------------------------- ensembles
+@dataclass
+class Ensemble:
+    """Members of the batched-ensemble workload on the standard grid:
+    species subsets of size uniform 1-4, Kp drivers piecewise linear with
+    knots every 30 min drawn uniform 1-7, initial-density scale lognormal
+    (sigma 0.5), run lengths uniform 360-1440 DTs steps."""
+    base: Workload
+    species: list        # per member: sorted species indices
+    kp_knots: np.ndarray  # (members, nknots)
+    scale: np.ndarray     # (members,)
+    length: np.ndarray    # (members,) DTs steps
+    knot_steps: int       # DTs steps between knots (30 min / DTs)
+
+    @property
+    def members(self) -> int:
+        return len(self.species)
+
+    def kp(self, step: int) -> np.ndarray:
+        """Kp of every member at DTs step `step` (piecewise linear)."""
+        x = step / self.knot_steps
+        i = min(int(x), self.kp_knots.shape[1] - 2)
+        w = x - i
+        return (1.0 - w) * self.kp_knots[:, i] + w * self.kp_knots[:, i + 1]
+
+
+def make_ensemble(members: int = 256, seed: int = 4242) -> Ensemble:
+    base = make_workload("four_sp", seed=seed)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    species = []
+    for _ in range(members):
+        n = int(rng.integers(1, 5))
+        species.append(sorted(rng.choice(4, size=n, replace=False).tolist()))
+    knot_steps = int(round(1800.0 / base.dts))
+    nknots = 1440 // knot_steps + 2
+    kp_knots = rng.uniform(1.0, 7.0, size=(members, nknots))
+    scale = rng.lognormal(0.0, 0.5, size=members)
+    length = rng.integers(360, 1441, size=members)
+    return Ensemble(base=base, species=species, kp_knots=kp_knots, scale=scale, length=length,
+                    knot_steps=knot_steps)

@@ -172,3 +172,51 @@ def test_api_errors(tiny):
         gpu.set_member_species(0, [1, 1])
     gpu.ram_run(wl.dts)  # context still usable after the errors
     assert np.isfinite(gpu.download_f2(0, 1)).all()
+
+
+def test_graph_replay_matches_direct(tiny):
+    """ram_run from a captured CUDA graph equals direct launches bitwise, with
+    Kp changing between steps (inputs are read when the graph runs)."""
+    wl = tiny
+    a = _gpu(wl, 2.0)
+    b = _gpu(wl, 2.0)
+    b.set_graph(True)
+    for step, kp in enumerate([2.0, 3.0, 4.5, 4.5, 6.0]):
+        a.set_kp(0, kp)
+        b.set_kp(0, kp)
+        a.ram_run(wl.dts)
+        b.ram_run(wl.dts)
+    for s in range(len(wl.grid.species)):
+        assert np.array_equal(a.download_f2(0, s), b.download_f2(0, s)), s
+        pa, pb = a.moments(0, s), b.moments(0, s)
+        assert np.array_equal(pa[0], pb[0]) and np.array_equal(pa[1], pb[1])
+
+
+@pytest.mark.parametrize("shape", [(32, 0), (256, 0), (64, 1), (128, 1)])
+def test_launch_shapes_bitwise(tiny, shape):
+    threads, persistent = shape
+    wl = tiny
+    ref = _gpu(wl, 3.0)
+    alt = _gpu(wl, 3.0)
+    for w in range(4):
+        alt.set_launch_shape(w, threads, 2 * 152 if persistent else 0)
+    for _ in range(2):
+        ref.ram_run(wl.dts)
+        alt.ram_run(wl.dts)
+    for s in range(len(wl.grid.species)):
+        assert np.array_equal(ref.download_f2(0, s), alt.download_f2(0, s))
+    assert np.array_equal(ref.cfl(0, 1), alt.cfl(0, 1))
+
+
+def test_autotune_restores_state_and_keeps_results(tiny):
+    wl = tiny
+    ref = _gpu(wl, 3.0)
+    tun = _gpu(wl, 3.0)
+    shapes, ms = tun.autotune(wl.dts, reps=2)
+    assert all(t in (32, 64, 128, 256) for t, _ in shapes) and np.all(ms > 0)
+    for s in range(len(wl.grid.species)):
+        assert np.array_equal(tun.download_f2(0, s), np.asfortranarray(wl.f2[s]))
+    ref.ram_run(wl.dts)
+    tun.ram_run(wl.dts)
+    for s in range(len(wl.grid.species)):
+        assert np.array_equal(ref.download_f2(0, s), tun.download_f2(0, s))
