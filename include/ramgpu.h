@@ -218,6 +218,46 @@ int ramgpu_probe_fp64(double *lane_ops_per_s);
 int ramgpu_set_timing(ramgpu_ctx *ctx, int enable);
 int ramgpu_kernel_times(ramgpu_ctx *ctx, double *ms, long long *counts);
 
+/* ---- frozen-limiter adjoint (no reference counterpart) ------------------- */
+
+/* One log-flux observation: FLUX = F2/FFACTOR/FNHS of (member, s) at
+ * energy bin k and pitch-angle bin l (0-based, both >= 1 as FLUX is defined
+ * for K, L >= 2), bilinear in L-shell (between LZ(I), I >= 2) and in MLT
+ * (periodic), taken after ram_run call `call` (0-based) of the window.
+ * The misfit is J = sum over observations of (log flux_model - log_obs)^2. */
+typedef struct {
+    int member, s, call, k, l;
+    double lshell;   /* [RE] */
+    double mlt;      /* [h] */
+    double log_obs;
+} ramgpu_obs;
+
+/* Forward pass of a window of ncalls ram_run calls of length dts from the
+ * current F2, with Kp of call c and member m in kp[c*n_members + m] (VOLS).
+ * Saves a checkpoint of F2 every k_ckpt calls, evaluates J per member into
+ * J[n_members] and leaves F2 at the end of the window.  Every limiter branch
+ * and clip is recorded; ramgpu_adj_digest returns a digest of the pattern.
+ * Allocates its checkpoint and record buffers (k_ckpt*8 bytes per cell and
+ * item for the record). */
+int ramgpu_adj_forward(ramgpu_ctx *ctx, int ncalls, double dts, const double *kp, int k_ckpt,
+                       const ramgpu_obs *obs, int nobs, double *J);
+/* Backward pass: gradients of J with respect to the window's initial F2
+ * (grad_f2: n_members*ns*NR*NT*NE*NPA, per (member, s) the Fortran-order
+ * F2(S,:,:,:,:)) and to FGEOS (grad_fgeos: n_members*ns*NT*NE*NPA), with the
+ * limiter branches frozen as recorded.  Each checkpoint segment is
+ * recomputed with recording and then transposed call by call.  Either
+ * output may be NULL.  On return F2 is the window's initial state again. */
+int ramgpu_adj_backward(ramgpu_ctx *ctx, double *grad_f2, double *grad_fgeos);
+/* Digest of every branch recorded by the last ramgpu_adj_forward: equal
+ * digests mean the same frozen-limiter pattern. */
+int ramgpu_adj_digest(ramgpu_ctx *ctx, unsigned long long *digest);
+/* Copy of the branch record of one call of the last checkpoint segment of
+ * the last ramgpu_adj_forward: 8 sweeps (R,P,E,MU,MU,E,P,R) x active items x
+ * NR*NT*NE*NPA bytes, per face the limiter case (bits 0-2: 0 upwind only,
+ * 1 beta*D, 2 X, 3 D, 4 beta*X) and bit 3 set when the updated cell was
+ * clipped (diagnostics). */
+int ramgpu_adj_record(ramgpu_ctx *ctx, int call, unsigned char *out);
+
 /* ---- no-allocation variant --------------------------------------------- */
 
 /* SETRC = sum EKEV*F2*WE*WMU (the energy-content sum of SUMRC) of one

@@ -63,6 +63,19 @@ struct ramgpu_ctx {
   int graph_shape = -1;
   long long items_version = 0;
   int shape_version = 0;
+  // frozen-limiter adjoint window
+  struct Adj {
+    bool ready = false;
+    int ncalls = 0, k = 0, nseg = 0, nobs = 0;
+    double dts = 0.0;
+    long long items_version = -1;
+    std::vector<double> kp;          // ncalls * nm
+    ObsDev* obs = nullptr;
+    double *fm = nullptr, *J = nullptr, *J2 = nullptr, *ckpt = nullptr;
+    unsigned char* rec = nullptr;
+    unsigned long long* digest = nullptr;
+    size_t rec_call = 0;             // bytes of one call's record (8 sweeps)
+  } adj;
   // optional per-kernel-class timing
   bool timing = false;
   std::vector<cudaEvent_t> ev_free;
@@ -279,6 +292,55 @@ static int enqueue_body(ramgpu_ctx* ctx, double dts) {
   return RAMGPU_OK;
 }
 
+static void adj_free(ramgpu_ctx* ctx) {
+  auto& a = ctx->adj;
+  cudaFree(a.obs); cudaFree(a.fm); cudaFree(a.J); cudaFree(a.J2); cudaFree(a.ckpt);
+  cudaFree(a.rec); cudaFree(a.digest);
+  a.obs = nullptr; a.fm = a.J = a.J2 = a.ckpt = nullptr; a.rec = nullptr; a.digest = nullptr;
+  a.ready = false;
+}
+
+// One ram_run call with every sweep recording its branches into rec
+// (8 instances of nitems*ncell bytes: R,P,E,MU forward, MU,E,P,R reverse).
+static int enqueue_call_rec(ramgpu_ctx* ctx, double dts, unsigned char* rec) {
+  const size_t isz = (size_t)ctx->d.nitems * ctx->d.ncell;
+  // positions no sweep writes (e.g. cell 1 of a DRIFTR line) stay zero
+  CK(cudaMemsetAsync(rec, 0, 8 * isz, ctx->stream));
+  launch_member_coef(ctx->d, dts, ctx->stream);
+  launch_ghost(ctx->d, ctx->stream);
+  launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 0 * isz);
+  launch_sweep_p(ctx->d, dts, false, ctx->stream, rec + 1 * isz);
+  launch_sweep_e(ctx->d, dts, false, ctx->stream, rec + 2 * isz);
+  launch_sweep_mu(ctx->d, dts, false, 1, ctx->d.loss2, ctx->stream, rec + 3 * isz);
+  launch_sweep_mu(ctx->d, dts, false, 0, nullptr, ctx->stream, rec + 4 * isz);
+  launch_sweep_e(ctx->d, dts, false, ctx->stream, rec + 5 * isz);
+  launch_sweep_p(ctx->d, dts, false, ctx->stream, rec + 6 * isz);
+  launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 7 * isz);
+  launch_finish(ctx->d, ctx->stream);
+  launch_moments(ctx->d, ctx->stream);
+  ctx->launches += 15;
+  CKL("recorded ram_run");
+  return RAMGPU_OK;
+}
+
+static int adj_copy_items(ramgpu_ctx* ctx, double* dst, bool to_ckpt) {
+  const size_t n = ctx->d.ncell;
+  for (size_t i = 0; i < ctx->items_h.size(); ++i) {
+    const int slot = ctx->items_h[i].x * ctx->d.ns + ctx->items_h[i].y;
+    double* f = ctx->d.f2 + (size_t)slot * n;
+    CK(cudaMemcpyAsync(to_ckpt ? dst + i * n : f, to_ckpt ? f : dst + i * n, sizeof(double) * n,
+                       cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  return RAMGPU_OK;
+}
+
+static int adj_set_kp(ramgpu_ctx* ctx, int call) {
+  const int nm = ctx->cfg.n_members;
+  CK(cudaMemcpyAsync(ctx->d.kp, ctx->adj.kp.data() + (size_t)call * nm, sizeof(double) * nm,
+                     cudaMemcpyHostToDevice, ctx->stream));
+  return RAMGPU_OK;
+}
+
 static void drop_graph(ramgpu_ctx* ctx) {
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   ctx->graph_exec = nullptr;
@@ -411,6 +473,10 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   d.plane_last = dalloc<double>(ctx, nslot * ne * npa, &ok);
   d.plane_has = dalloc<int>(ctx, nslot * ne * npa, &ok);
   d.plane_carry = dalloc<double>(ctx, nslot * ne * npa, &ok);
+  d.plane_last_src = dalloc<int>(ctx, nslot * ne * npa, &ok);
+  d.lam = dalloc<double>(ctx, nslot * ncell, &ok);
+  d.gfg = dalloc<double>(ctx, nslot * nt * ne * npa, &ok);
+  d.plane_carry_src = dalloc<int>(ctx, nslot * ne * npa, &ok);
   d.cflq = dalloc<unsigned long long>(ctx, nslot * 4, &ok);
   d.mom_part = dalloc<double>(ctx, nslot * 4 * nr * nt * ne * 2, &ok);
   d.ppert = dalloc<double>(ctx, nslot * nr * nt, &ok);
@@ -442,6 +508,7 @@ int ramgpu_destroy(ramgpu_ctx* ctx) {
   if (!ctx) return RAMGPU_ERR_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   drop_graph(ctx);
+  adj_free(ctx);
   for (void* p : ctx->allocs) cudaFree(p);
   for (auto& sp : ctx->spans) { cudaEventDestroy(sp.a); cudaEventDestroy(sp.b); }
   for (cudaEvent_t e : ctx->ev_free) cudaEventDestroy(e);
@@ -966,6 +1033,159 @@ int ramgpu_autotune(ramgpu_ctx* ctx, double dts, int reps, double* best_ms4) {
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "autotune");
   ctx->shape_version += 1;
+  return RAMGPU_OK;
+}
+
+int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp, int k_ckpt,
+                       const ramgpu_obs* obs, int nobs, double* J) {
+  if (check_ctx(ctx) || !kp || (nobs > 0 && !obs)) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (ncalls < 1 || k_ckpt < 1 || nobs < 0) return fail(ctx, RAMGPU_ERR_ARG, "ncalls, k_ckpt >= 1, nobs >= 0");
+  if (ctx->cfg.flags & RAMGPU_FLAG_LOSSES)
+    return fail(ctx, RAMGPU_ERR_ARG, "the adjoint window runs without RAMGPU_FLAG_LOSSES");
+  Dev& d = ctx->d;
+  if (d.nr > 160 || d.nt > 160 || d.ne > 160 || d.npa > 160)
+    return fail(ctx, RAMGPU_ERR_ARG, "the adjoint supports NR, NT, NE, NPA <= 160");
+  int rc = prepare(ctx, dts);
+  if (rc) return rc;
+  if (d.nitems == 0) return fail(ctx, RAMGPU_ERR_STATE, "no active (member, species)");
+  const int nm = ctx->cfg.n_members;
+  for (long long i = 0; i < (long long)ncalls * nm; ++i)
+    if (!isfinite(kp[i])) return fail(ctx, RAMGPU_ERR_ARG, "kp must be finite");
+  // observations -> device form (corners and weights of the bilinear stencil)
+  std::vector<ObsDev> oh(nobs);
+  std::vector<double> lz(d.nf), phi(d.nt);
+  CK(cudaMemcpy(lz.data(), d.lz, sizeof(double) * d.nf, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(phi.data(), d.phi, sizeof(double) * d.nt, cudaMemcpyDeviceToHost));
+  for (int t = 0; t < nobs; ++t) {
+    const ramgpu_obs& o = obs[t];
+    if (int r2 = check_ms(ctx, o.member, o.s)) return r2;
+    if (o.call < 0 || o.call >= ncalls || o.k < 1 || o.k >= d.ne || o.l < 1 || o.l >= d.npa ||
+        !isfinite(o.lshell) || !isfinite(o.mlt) || !isfinite(o.log_obs))
+      return fail(ctx, RAMGPU_ERR_ARG, "observation out of range");
+    bool found = false;
+    for (auto& it : ctx->items_h) found |= (it.x == o.member && it.y == o.s);
+    if (!found) return fail(ctx, RAMGPU_ERR_ARG, "observation of an inactive (member, species)");
+    ObsDev& q = oh[t];
+    q.member = o.member; q.slot = o.member * d.ns + o.s; q.call = o.call; q.k = o.k; q.l = o.l;
+    q.log_obs = o.log_obs;
+    int i0 = 1;  // I >= 2 (FLUX is defined for I >= 2)
+    while (i0 + 1 < d.nr - 1 && lz[i0 + 1] <= o.lshell) ++i0;
+    q.i0 = i0;
+    q.wi = fmin(1.0, fmax(0.0, (o.lshell - lz[i0]) / (lz[i0 + 1] - lz[i0])));
+    const double twopi = 2.0 * kPI;
+    double ph = fmod(o.mlt * kPI / 12.0, twopi);
+    if (ph < 0) ph += twopi;
+    int j0 = (int)(ph / d.dphi);
+    if (j0 > d.nt - 2) j0 = d.nt - 2;
+    q.j0 = j0;
+    q.j1 = (j0 + 1 == d.nt - 1) ? 0 : j0 + 1;  // J = NT is J = 1
+    q.wj = fmin(1.0, fmax(0.0, (ph - phi[j0]) / d.dphi));
+  }
+  adj_free(ctx);
+  auto& a = ctx->adj;
+  a.ncalls = ncalls; a.k = k_ckpt; a.nseg = (ncalls + k_ckpt - 1) / k_ckpt; a.nobs = nobs; a.dts = dts;
+  a.kp.assign(kp, kp + (size_t)ncalls * nm);
+  a.items_version = ctx->items_version;
+  a.rec_call = (size_t)8 * d.nitems * d.ncell;
+  const int kseg = k_ckpt < ncalls ? k_ckpt : ncalls;
+  bool ok = cudaMalloc(&a.ckpt, sizeof(double) * a.nseg * d.nitems * d.ncell) == cudaSuccess;
+  ok = ok && cudaMalloc(&a.rec, a.rec_call * kseg) == cudaSuccess;
+  ok = ok && cudaMalloc(&a.obs, sizeof(ObsDev) * (nobs > 0 ? nobs : 1)) == cudaSuccess;
+  ok = ok && cudaMalloc(&a.fm, sizeof(double) * (nobs > 0 ? nobs : 1)) == cudaSuccess;
+  ok = ok && cudaMalloc(&a.J, sizeof(double) * nm) == cudaSuccess;
+  ok = ok && cudaMalloc(&a.J2, sizeof(double) * nm) == cudaSuccess;
+  ok = ok && cudaMalloc(&a.digest, sizeof(unsigned long long)) == cudaSuccess;
+  if (!ok) {
+    adj_free(ctx);
+    return fail(ctx, RAMGPU_ERR_NOMEM, "adjoint buffers: device allocation failed");
+  }
+  if (nobs > 0) CK(cudaMemcpy(a.obs, oh.data(), sizeof(ObsDev) * nobs, cudaMemcpyHostToDevice));
+  std::vector<int> one(nm, 1);
+  CK(cudaMemcpyAsync(d.vt_mode, one.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(a.J, 0, sizeof(double) * nm, ctx->stream));
+  CK(cudaMemsetAsync(a.digest, 0, sizeof(unsigned long long), ctx->stream));
+  for (int c = 0; c < ncalls; ++c) {
+    if (c % k_ckpt == 0)
+      if ((rc = adj_copy_items(ctx, a.ckpt + (size_t)(c / k_ckpt) * d.nitems * d.ncell, true))) return rc;
+    if ((rc = adj_set_kp(ctx, c))) return rc;
+    unsigned char* r = a.rec + (size_t)(c % k_ckpt) * a.rec_call;
+    if ((rc = enqueue_call_rec(ctx, dts, r))) return rc;
+    launch_digest(r, (long long)a.rec_call, a.digest, ctx->stream);
+    launch_obs_fwd(d, a.obs, nobs, c, a.fm, a.J, ctx->stream);
+    ctx->launches += 2;
+    CKL("adjoint forward");
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (J) CK(cudaMemcpy(J, a.J, sizeof(double) * nm, cudaMemcpyDeviceToHost));
+  ctx->last_dts = dts;
+  a.ready = true;
+  return RAMGPU_OK;
+}
+
+int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  auto& a = ctx->adj;
+  if (!a.ready) return fail(ctx, RAMGPU_ERR_STATE, "ramgpu_adj_forward must run first");
+  if (ctx->items_dirty || a.items_version != ctx->items_version)
+    return fail(ctx, RAMGPU_ERR_STATE, "active members/species changed since ramgpu_adj_forward");
+  Dev& d = ctx->d;
+  int rc = prepare(ctx, a.dts);
+  if (rc) return rc;
+  const size_t nslot = (size_t)d.nm * d.ns, nfg = (size_t)d.nt * d.ne * d.npa;
+  const size_t isz = (size_t)d.nitems * d.ncell;
+  CK(cudaMemsetAsync(d.lam, 0, sizeof(double) * nslot * d.ncell, ctx->stream));
+  CK(cudaMemsetAsync(d.gfg, 0, sizeof(double) * nslot * nfg, ctx->stream));
+  for (int seg = a.nseg - 1; seg >= 0; --seg) {
+    const int c0 = seg * a.k, c1 = (c0 + a.k < a.ncalls) ? c0 + a.k : a.ncalls;
+    if ((rc = adj_copy_items(ctx, a.ckpt + (size_t)seg * isz, false))) return rc;
+    for (int c = c0; c < c1; ++c) {  // recompute the segment, recording branches
+      if ((rc = adj_set_kp(ctx, c))) return rc;
+      if ((rc = enqueue_call_rec(ctx, a.dts, a.rec + (size_t)(c - c0) * a.rec_call))) return rc;
+      launch_obs_fwd(d, a.obs, a.nobs, c, a.fm, a.J2, ctx->stream);
+    }
+    for (int c = c1 - 1; c >= c0; --c) {  // transpose call c
+      const unsigned char* r = a.rec + (size_t)(c - c0) * a.rec_call;
+      launch_obs_adj(d, a.obs, a.nobs, c, a.fm, ctx->stream);
+      if ((rc = adj_set_kp(ctx, c))) return rc;
+      launch_member_coef(d, a.dts, ctx->stream);
+      launch_ghost(d, ctx->stream);
+      launch_adj_tail(d, ctx->stream);
+      launch_adj_sweep(d, 0, r + 7 * isz, ctx->stream);
+      launch_adj_sweep(d, 1, r + 6 * isz, ctx->stream);
+      launch_adj_sweep(d, 2, r + 5 * isz, ctx->stream);
+      launch_adj_sweep(d, 3, r + 4 * isz, ctx->stream);
+      launch_scale_lam(d, d.loss2, ctx->stream);
+      launch_adj_sweep(d, 3, r + 3 * isz, ctx->stream);
+      launch_adj_sweep(d, 2, r + 2 * isz, ctx->stream);
+      launch_adj_sweep(d, 1, r + 1 * isz, ctx->stream);
+      launch_adj_sweep(d, 0, r + 0 * isz, ctx->stream);
+      ctx->launches += 17;
+      CKL("adjoint backward");
+    }
+  }
+  if ((rc = adj_copy_items(ctx, a.ckpt, false))) return rc;  // F2 back to the initial state
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (grad_f2) CK(cudaMemcpy(grad_f2, d.lam, sizeof(double) * nslot * d.ncell, cudaMemcpyDeviceToHost));
+  if (grad_fgeos) CK(cudaMemcpy(grad_fgeos, d.gfg, sizeof(double) * nslot * nfg, cudaMemcpyDeviceToHost));
+  return RAMGPU_OK;
+}
+
+int ramgpu_adj_record(ramgpu_ctx* ctx, int call, unsigned char* out) {
+  if (check_ctx(ctx) || !out) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  auto& a = ctx->adj;
+  if (!a.ready) return fail(ctx, RAMGPU_ERR_STATE, "ramgpu_adj_forward must run first");
+  if (call < 0 || call >= a.ncalls || (a.ncalls > a.k && call / a.k != a.nseg - 1))
+    return fail(ctx, RAMGPU_ERR_ARG, "only calls of the last checkpoint segment are kept");
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(out, a.rec + (size_t)(call % a.k) * a.rec_call, a.rec_call, cudaMemcpyDeviceToHost));
+  return RAMGPU_OK;
+}
+
+int ramgpu_adj_digest(ramgpu_ctx* ctx, unsigned long long* digest) {
+  if (check_ctx(ctx) || !digest) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (!ctx->adj.ready) return fail(ctx, RAMGPU_ERR_STATE, "ramgpu_adj_forward must run first");
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(digest, ctx->adj.digest, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
   return RAMGPU_OK;
 }
 

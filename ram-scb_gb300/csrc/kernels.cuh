@@ -36,11 +36,23 @@ __device__ __forceinline__ double stale_ghost(const Dev& d, int m, int slot, int
 // Thread-local error text returned by ramgpu_last_error(NULL, ...).
 void set_thread_error(const std::string& msg);
 
-void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st);
-void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st);
-void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st);
+// rec (may be null): per-face branch record of the frozen-limiter adjoint,
+// (items, ncell) bytes for this sweep instance.
+// FGEOS index (L*NE+K)*NT+J of the inflow line whose F(NR+1) outflow line
+// (J,K,L) reads as its stale ghost, or -1 (value 0) -- the source that
+// stale_ghost() takes its value from.
+__device__ __forceinline__ int stale_ghost_src(const Dev& d, int m, int slot, int j, int k, int l,
+                                               double p4) {
+  for (int jj = j - 1; jj >= 0; --jj)
+    if (inflow_line(d, m, jj, l, p4)) return (l * d.ne + k) * d.nt + jj;
+  return d.plane_carry_src[(long long)slot * d.ne * d.npa + (long long)k * d.npa + l];
+}
+
+void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr);
+void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr);
+void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr);
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
-                     cudaStream_t st);
+                     cudaStream_t st, unsigned char* rec = nullptr);
 
 int sweep_max_blocks_per_sm(int w, int blk);
 
@@ -54,5 +66,21 @@ void launch_finish(const Dev& d, cudaStream_t st);
 void launch_moments(const Dev& d, cudaStream_t st);
 void launch_sumrc(const Dev& d, double* part, int nblk, cudaStream_t st);
 void launch_flux(const Dev& d, int slot, int s, double* out, cudaStream_t st);
+
+// ---- frozen-limiter adjoint (adjoint.cu)
+struct ObsDev {
+  int member, slot, call, k, l;
+  int i0, j0, j1;      // 0-based corner indices: I = i0, i0+1; J = j0, j1
+  double wi, wj;       // bilinear weights of the upper corners
+  double log_obs;
+};
+void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_t st);
+void launch_adj_tail(const Dev& d, cudaStream_t st);
+void launch_scale_lam(const Dev& d, const double* table, cudaStream_t st);
+void launch_obs_fwd(const Dev& d, const ObsDev* obs, int nobs, int call, double* fm, double* J,
+                    cudaStream_t st);
+void launch_obs_adj(const Dev& d, const ObsDev* obs, int nobs, int call, const double* fm,
+                    cudaStream_t st);
+void launch_digest(const unsigned char* rec, long long n, unsigned long long* out, cudaStream_t st);
 
 }  // namespace ramgpu

@@ -84,6 +84,11 @@ struct Dev {
   double *plane_last;     // (nm*ns, NE*NPA): DRIFTR F(NR+1) of the last inflow line of plane (K,L)
   int *plane_has;         // (nm*ns, NE*NPA): plane (K,L) has an inflow line
   double *plane_carry;    // (nm*ns, NE*NPA): F(NR+1) left by planes before (K,L) in K->L order
+  int *plane_last_src;    // (nm*ns, NE*NPA): FGEOS index (L*NE+K)*NT+J of that last inflow line
+  int *plane_carry_src;   // (nm*ns, NE*NPA): FGEOS index behind plane_carry, -1 if none
+  // frozen-limiter adjoint: lambda (same layout as f2) and dJ/dFGEOS per slot
+  double *lam;            // (nm*ns, ncell)
+  double *gfg;            // (nm*ns, NT*NE*NPA)
   unsigned long long *cflq;  // (nm*ns, 4): max over cells of the CFL quotient, as bits
   double *mom_part;       // (nm*ns, 4 chunks, NE, NT, NR, 2) per-K moment partials
   double *ppert, *ppart;  // (nm*ns, NR, NT)
@@ -145,6 +150,22 @@ __device__ __forceinline__ double face_value(double x, double bx, double d, doub
   bool act = abs_gt_1em27(x) && same_sign_nonzero(d, x);
   return act ? fb : fup;
 }
+
+// Same face value, also reporting which limiter candidate was taken, for
+// the frozen-limiter adjoint: 0 upwind only, 1 beta*D, 2 X, 3 D, 4 beta*X.
+__device__ __forceinline__ double face_value_case(double x, double bx, double d, double bd,
+                                                  double fup, double a, int& cs) {
+  const unsigned long long ux = dbits(x), ud = dbits(d);
+  const unsigned long long m1 = umin64(dbits(bd), ux & kAbsMask);
+  const unsigned long long m2 = umin64(ud & kAbsMask, dbits(bx));
+  const unsigned long long m = umax64(m1, m2);
+  const double lx = __longlong_as_double((long long)(m | (ux & kSignMask)));
+  const double fb = fma(a, lx, fup);
+  const bool act = abs_gt_1em27(x) && same_sign_nonzero(d, x);
+  cs = !act ? 0 : (m == m1 ? (m1 == dbits(bd) ? 1 : 2) : (m2 == (ud & kAbsMask) ? 3 : 4));
+  return act ? fb : fup;
+}
+constexpr int kClipBit = 8;  // recorded with the case: the updated cell was clipped
 
 // Running CFL quotient max(|C|, floor) as bits (integer max).
 __device__ __forceinline__ unsigned long long cfl_bits(double c, unsigned long long floor_bits) {

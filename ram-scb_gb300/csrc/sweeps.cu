@@ -18,8 +18,8 @@ namespace ramgpu {
 
 // ----------------------------------------------------------------- DRIFTR
 // Line (J,K,L) along I = 1..NR.  Faces 2..NR-1 (and NR on inflow lines).
-template <bool kCfl>
-__global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts) {
+template <bool kCfl, bool kRec>
+__global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = nt * ne * d.npa;
   // Work units are (item, block of lines).  A grid of (blocks per item,
@@ -36,6 +36,8 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts) {
       const int j = line % nt;
       const int l = line / (nt * ne);
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + (long long)line * nr;
+      // branch record of the frozen-limiter adjoint: one byte per face/cell
+      unsigned char* __restrict__ rl = kRec ? rec + (u / bpi) * d.ncell + (long long)line * nr : nullptr;
       const double* __restrict__ grt = d.grt + ((long long)l * nt + j) * nr;
       const double* __restrict__ cr = d.cr + ((long long)m * nt + j) * nr;
       const int* __restrict__ outside = d.outside + (long long)j * nr;
@@ -72,9 +74,12 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts) {
         if (kCfl && outside[f - 1] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
         const bool neg = is_neg(c);
         const double a = fma(c, -0.5, neg ? -0.5 : 0.5);
-        const double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
+        int cs;
+        const double fb = face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         const double phi = c * fb;
-        fl[f - 1] = clip((g0 - phi) + phi_prev);
+        const double raw = (g0 - phi) + phi_prev;
+        fl[f - 1] = clip(raw);
+        if (kRec) rl[f - 1] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         gm = g0; g0 = gp; gp = gpp;
         xm = x; bxm = bx; x = xp; bx = bxp;
@@ -82,15 +87,18 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts) {
       // face NR (g0 = F(NR), gp = F(NR+1), x = X(NR))
       if (kCfl && outside[nr - 1] == 0) q = umax64(q, cfl_bits(cN, kBits1em10));
       double fbn;
+      int csn = 0;
       if (!inflow) {
         fbn = g0;
       } else {
         const double xp = g2 - g1, bxp = beta * fabs(xp);
-        fbn = face_value(x, bx, xp, bxp, g1, fma(cN, -0.5, -0.5));
+        fbn = face_value_case(x, bx, xp, bxp, g1, fma(cN, -0.5, -0.5), csn);
       }
       if (closed) fbn = 0.0;
       const double phin = cN * fbn;
-      fl[nr - 1] = clip((g0 - phin) + phi_prev);
+      const double rawn = (g0 - phin) + phi_prev;
+      fl[nr - 1] = clip(rawn);
+      if (kRec) rl[nr - 1] = (unsigned char)(csn | (is_neg(rawn) ? kClipBit : 0));
     }
     if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 0], q);
   }
@@ -98,8 +106,8 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts) {
 
 // ----------------------------------------------------------------- DRIFTP
 // Line (I,K,L), I = 2..NR, along J = 1..NT, periodic with J=1 == J=NT.
-template <bool kCfl>
-__global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts) {
+template <bool kCfl, bool kRec>
+__global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * ne * d.npa;
   // Work units are (item, block of lines).  A grid of (blocks per item,
@@ -118,6 +126,8 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts) {
       const int k = kl % ne, l = kl / ne;
       const long long st = nr;  // stride between consecutive J
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + ((long long)kl * nt) * nr + i;
+      unsigned char* __restrict__ rl =
+          kRec ? rec + (u / bpi) * d.ncell + ((long long)kl * nt) * nr + i : nullptr;
       const double* __restrict__ gpt = d.gpt + ((long long)l * nt) * nr + i;
       const double* __restrict__ ca = d.ca + ((long long)m * nt) * nr + i;
       const int* __restrict__ outside = d.outside + i;
@@ -134,10 +144,11 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts) {
       const double cN = CJ(nt);
       if (kCfl && outside[(long long)(nt - 1) * nr] == 0) q = umax64(q, cfl_bits(cN, kBits1em10));
       double phiN;
+      int csN;
       {
         const bool neg = is_neg(cN);
         const double a = fma(cN, -0.5, neg ? -0.5 : 0.5);
-        phiN = cN * face_value(XN, bXN, neg ? X2 : XNm, neg ? bX2 : bXNm, neg ? G2 : GN, a);
+        phiN = cN * face_value_case(XN, bXN, neg ? X2 : XNm, neg ? bX2 : bXNm, neg ? G2 : GN, a, csN);
       }
       double phi_prev = phiN;
       double g0 = G2, gp = G3, xm = X1, bxm = bX1, x = X2, bx = bX2;
@@ -159,16 +170,21 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts) {
         if (kCfl && outside[(long long)(J - 1) * nr] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
         const bool neg = is_neg(c);
         const double a = fma(c, -0.5, neg ? -0.5 : 0.5);
-        const double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
+        int cs;
+        const double fb = face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         const double phi = c * fb;
-        GJ(J) = clip((g0 - phi) + phi_prev);
+        const double raw = (g0 - phi) + phi_prev;
+        GJ(J) = clip(raw);
+        if (kRec) rl[(long long)(J - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         g0 = gp; gp = gpp;
         xm = x; bxm = bx; x = xp; bx = bxp;
       }
-      const double vN = clip((GN - phiN) + phi_prev);
+      const double rawN = (GN - phiN) + phi_prev;
+      const double vN = clip(rawN);
       GJ(nt) = vN;
       GJ(1) = vN;
+      if (kRec) rl[(long long)(nt - 1) * st] = (unsigned char)(csN | (is_neg(rawN) ? kClipBit : 0));
   #undef GJ
   #undef CJ
     }
@@ -179,8 +195,8 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts) {
 // ----------------------------------------------------------------- DRIFTE
 // Line (I,J,L), I = 2..NR, along K = 1..NE with extrapolated F(0), F(1)
 // and F(NE+1) = F(NE+2) = 0.  Cell K = 1 is never written.
-template <bool kCfl>
-__global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts) {
+template <bool kCfl, bool kRec>
+__global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * nt * d.npa;
   // Work units are (item, block of lines).  A grid of (blocks per item,
@@ -199,6 +215,8 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts) {
       const int j = jl % nt, l = jl / nt;
       const long long st = (long long)nt * nr;  // stride between consecutive K
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + ((long long)l * ne * nt + j) * nr + i;
+      unsigned char* __restrict__ rl =
+          kRec ? rec + (u / bpi) * d.ncell + ((long long)l * ne * nt + j) * nr + i : nullptr;
       const long long fij = ((long long)l * nt + j) * nr + i;
       const double wet = d.wet[fij];
       const double ue = d.ue[(long long)m * nr * nt * d.npa + fij];
@@ -224,8 +242,10 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts) {
         if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em10)) * d.ide[0]));
         const bool neg = is_neg(c);
         const double a = fma(c, mhde[0], neg ? -0.5 : 0.5);
-        double fb = face_value(X1, bX1, neg ? X2 : X0, neg ? bX2 : bX0, neg ? G2 : G1, a);
+        int cs;
+        double fb = face_value_case(X1, bX1, neg ? X2 : X0, neg ? bX2 : bX0, neg ? G2 : G1, a, cs);
         if (closed) fb = 0.0;
+        if (kRec) rl[0] = (unsigned char)cs;
         phi_prev = c * fb;
       }
       double g0 = G2, gp = G3, xm = X1, bxm = bX1, x = X2, bx = bX2;
@@ -236,10 +256,13 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts) {
         if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em10)) * d.ide[K - 1]));
         const bool neg = is_neg(c);
         const double a = fma(c, mhde[K - 1], neg ? -0.5 : 0.5);
-        double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
+        int cs;
+        double fb = face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         if (closed && K == ne) fb = 0.0;
         const double phi = c * fb;
-        GK(K) = clip(fma(phi_prev - phi, iwe[K - 1], g0));
+        const double raw = fma(phi_prev - phi, iwe[K - 1], g0);
+        GK(K) = clip(raw);
+        if (kRec) rl[(long long)(K - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         g0 = gp; gp = gpp;
         xm = x; bxm = bx; x = xp; bx = bxp;
@@ -256,8 +279,9 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts) {
 // faces 2..NPA-2, FBND(NPA-1) = F(NPA), then the F2(NPA) extrapolation.
 // kLoss: 0 none, 1 multiply the result by table lossA (loss after the sweep),
 //        2 multiply the input by lossA (loss before the sweep).
-template <bool kCfl, int kLoss>
-__global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const double* __restrict__ lossA) {
+template <bool kCfl, int kLoss, bool kRec>
+__global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const double* __restrict__ lossA,
+                                                   unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa;
   const int nlines = (nr - 1) * nt * ne;
   // Work units are (item, block of lines).  A grid of (blocks per item,
@@ -277,6 +301,7 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
       const long long st = (long long)ne * nt * nr;  // stride between consecutive L
       const long long off = (long long)jk * nr + i;  // (K*NT + J)*NR + I
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + off;
+      unsigned char* __restrict__ rl = kRec ? rec + (u / bpi) * d.ncell + off : nullptr;
       const double* __restrict__ la = lossA ? lossA + (long long)s * d.ncell + off : nullptr;
       const long long sij = (long long)nt * nr;     // stride of (I,J,L) tables in L
       const long long fij = (long long)j * nr + i;
@@ -305,9 +330,12 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
         const bool neg = is_neg(c);
         const double a = fma(c, mhdmu[L - 1], neg ? -0.5 : 0.5);
-        const double fb = face_value(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a);
+        int cs;
+        const double fb = face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         const double phi = c * fb;
-        double v = clip(fma(phi_prev - phi, iwmu[L - 1], g0));
+        const double raw = fma(phi_prev - phi, iwmu[L - 1], g0);
+        if (kRec) rl[(long long)(L - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
+        double v = clip(raw);
         if (kLoss == 1) v *= LA(L);
         GL(L) = v;
         phi_prev = phi;
@@ -320,7 +348,9 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         const double c = CL(L);
         if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
         const double phi = c * (closed ? 0.0 : gp);
-        const double v = clip(fma(phi_prev - phi, iwmu[L - 1], g0));
+        const double raw = fma(phi_prev - phi, iwmu[L - 1], g0);
+        if (kRec) rl[(long long)(L - 1) * st] = (unsigned char)(is_neg(raw) ? kClipBit : 0);
+        const double v = clip(raw);
         const double vN = v * d.rho[fij];
         if (kLoss == 1) {
           GL(L) = v * LA(L);
@@ -354,33 +384,40 @@ static inline int nlines_of(const Dev& d, int w) {
   }
 }
 
-void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st) {
+void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec) {
   dim3 g = grid_for(d, 0, nlines_of(d, 0));
-  if (cfl) k_sweep_r<true><<<g, d.blk[0], 0, st>>>(d, dts);
-  else k_sweep_r<false><<<g, d.blk[0], 0, st>>>(d, dts);
+  if (rec) k_sweep_r<false, true><<<g, d.blk[0], 0, st>>>(d, dts, rec);
+  else if (cfl) k_sweep_r<true, false><<<g, d.blk[0], 0, st>>>(d, dts, nullptr);
+  else k_sweep_r<false, false><<<g, d.blk[0], 0, st>>>(d, dts, nullptr);
 }
-void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st) {
+void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec) {
   dim3 g = grid_for(d, 1, nlines_of(d, 1));
-  if (cfl) k_sweep_p<true><<<g, d.blk[1], 0, st>>>(d, dts);
-  else k_sweep_p<false><<<g, d.blk[1], 0, st>>>(d, dts);
+  if (rec) k_sweep_p<false, true><<<g, d.blk[1], 0, st>>>(d, dts, rec);
+  else if (cfl) k_sweep_p<true, false><<<g, d.blk[1], 0, st>>>(d, dts, nullptr);
+  else k_sweep_p<false, false><<<g, d.blk[1], 0, st>>>(d, dts, nullptr);
 }
-void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st) {
+void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec) {
   dim3 g = grid_for(d, 2, nlines_of(d, 2));
-  if (cfl) k_sweep_e<true><<<g, d.blk[2], 0, st>>>(d, dts);
-  else k_sweep_e<false><<<g, d.blk[2], 0, st>>>(d, dts);
+  if (rec) k_sweep_e<false, true><<<g, d.blk[2], 0, st>>>(d, dts, rec);
+  else if (cfl) k_sweep_e<true, false><<<g, d.blk[2], 0, st>>>(d, dts, nullptr);
+  else k_sweep_e<false, false><<<g, d.blk[2], 0, st>>>(d, dts, nullptr);
 }
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
-                     cudaStream_t st) {
+                     cudaStream_t st, unsigned char* rec) {
   dim3 g = grid_for(d, 3, nlines_of(d, 3));
   const int b = d.blk[3];
-  if (cfl) {
-    if (loss_mode == 1) k_sweep_mu<true, 1><<<g, b, 0, st>>>(d, dts, loss);
-    else if (loss_mode == 2) k_sweep_mu<true, 2><<<g, b, 0, st>>>(d, dts, loss);
-    else k_sweep_mu<true, 0><<<g, b, 0, st>>>(d, dts, nullptr);
+  if (rec) {
+    if (loss_mode == 1) k_sweep_mu<false, 1, true><<<g, b, 0, st>>>(d, dts, loss, rec);
+    else if (loss_mode == 2) k_sweep_mu<false, 2, true><<<g, b, 0, st>>>(d, dts, loss, rec);
+    else k_sweep_mu<false, 0, true><<<g, b, 0, st>>>(d, dts, nullptr, rec);
+  } else if (cfl) {
+    if (loss_mode == 1) k_sweep_mu<true, 1, false><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+    else if (loss_mode == 2) k_sweep_mu<true, 2, false><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+    else k_sweep_mu<true, 0, false><<<g, b, 0, st>>>(d, dts, nullptr, nullptr);
   } else {
-    if (loss_mode == 1) k_sweep_mu<false, 1><<<g, b, 0, st>>>(d, dts, loss);
-    else if (loss_mode == 2) k_sweep_mu<false, 2><<<g, b, 0, st>>>(d, dts, loss);
-    else k_sweep_mu<false, 0><<<g, b, 0, st>>>(d, dts, nullptr);
+    if (loss_mode == 1) k_sweep_mu<false, 1, false><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+    else if (loss_mode == 2) k_sweep_mu<false, 2, false><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+    else k_sweep_mu<false, 0, false><<<g, b, 0, st>>>(d, dts, nullptr, nullptr);
   }
 }
 
@@ -389,10 +426,10 @@ int sweep_max_blocks_per_sm(int w, int blk) {
   int n = 0;
   cudaError_t e = cudaSuccess;
   switch (w) {
-    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_r<false>, blk, 0); break;
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_p<false>, blk, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_e<false>, blk, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_mu<false, 0>, blk, 0); break;
+    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_r<false, false>, blk, 0); break;
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_p<false, false>, blk, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_e<false, false>, blk, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_mu<false, 0, false>, blk, 0); break;
   }
   return e == cudaSuccess ? n : 0;
 }

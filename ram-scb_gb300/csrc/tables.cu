@@ -354,7 +354,7 @@ __global__ void k_ghost_planes(Dev d) {
   if (p >= np) return;  // uniform per warp
   const int k = p / d.npa, l = p % d.npa;
   const double p4 = d.p4[s * d.ne + k];
-  int has = 0;
+  int has = 0, src = -1;
   double v = 0.0;
   for (int top = d.nt - 1; top >= 0; top -= 32) {
     const int jj = top - lane;
@@ -362,68 +362,80 @@ __global__ void k_ghost_planes(Dev d) {
     const unsigned b = __ballot_sync(0xffffffffu, inf);
     if (b) {
       has = 1;
-      v = ghost_value(d, slot, top - (__ffs(b) - 1), k, l, d.conf1);
+      const int jsel = top - (__ffs(b) - 1);
+      v = ghost_value(d, slot, jsel, k, l, d.conf1);
+      src = (l * d.ne + k) * d.nt + jsel;
       break;
     }
   }
   if (lane == 0) {
     d.plane_has[(long long)slot * np + p] = has;
     d.plane_last[(long long)slot * np + p] = v;
+    d.plane_last_src[(long long)slot * np + p] = src;
   }
 }
 
 // Exclusive "last defined" scan over planes: one block per work item.
 // combine(left, right) = right if right has a value else left (associative),
 // scanned with warp shuffles, then across the 32 warp totals.
-__device__ __forceinline__ void last_scan_warp(int& h, double& v) {
+__device__ __forceinline__ void last_scan_warp(int& h, double& v, int& src) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const int lh = __shfl_up_sync(0xffffffffu, h, o);
     const double lv = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= o && !h) { h = lh; v = lv; }
+    const int ls = __shfl_up_sync(0xffffffffu, src, o);
+    if (lane >= o && !h) { h = lh; v = lv; src = ls; }
   }
 }
 
 __global__ void __launch_bounds__(1024) k_ghost_scan(Dev d) {
   __shared__ int s_h[32];
   __shared__ double s_v[32];
+  __shared__ int s_s[32];
   const int np = d.ne * d.npa;
   const int2 item = d.items[blockIdx.x];
   const int slot = item.x * d.ns + item.y;
   const int* has = d.plane_has + (long long)slot * np;
   const double* last = d.plane_last + (long long)slot * np;
   double* carry = d.plane_carry + (long long)slot * np;
+  const int* lsrc = d.plane_last_src + (long long)slot * np;
+  int* csrc = d.plane_carry_src + (long long)slot * np;
   const int nth = blockDim.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int cs = (np + nth - 1) / nth;
   const int p0 = min(np, threadIdx.x * cs), p1 = min(np, p0 + cs);
-  int h = 0;
+  int h = 0, sc = -1;
   double v = 0.0;
   for (int p = p0; p < p1; ++p)
-    if (has[p]) { h = 1; v = last[p]; }
+    if (has[p]) { h = 1; v = last[p]; sc = lsrc[p]; }
   // inclusive scan within the warp
-  int ih = h;
+  int ih = h, is = sc;
   double iv = v;
-  last_scan_warp(ih, iv);
-  if (lane == 31) { s_h[warp] = ih; s_v[warp] = iv; }
+  last_scan_warp(ih, iv, is);
+  if (lane == 31) { s_h[warp] = ih; s_v[warp] = iv; s_s[warp] = is; }
   __syncthreads();
   if (warp == 0) {
     int wh = lane < (nth >> 5) ? s_h[lane] : 0;
     double wv = lane < (nth >> 5) ? s_v[lane] : 0.0;
-    last_scan_warp(wh, wv);  // inclusive over warps
+    int ws = lane < (nth >> 5) ? s_s[lane] : -1;
+    last_scan_warp(wh, wv, ws);  // inclusive over warps
     s_h[lane] = wh;
     s_v[lane] = wv;
+    s_s[lane] = ws;
   }
   __syncthreads();
   // exclusive value for this thread: inclusive of the previous thread
   int eh = __shfl_up_sync(0xffffffffu, ih, 1);
   double ev = __shfl_up_sync(0xffffffffu, iv, 1);
-  if (lane == 0) { eh = 0; ev = 0.0; }
-  if (!eh && warp > 0) { eh = s_h[warp - 1]; ev = s_v[warp - 1]; }
+  int es = __shfl_up_sync(0xffffffffu, is, 1);
+  if (lane == 0) { eh = 0; ev = 0.0; es = -1; }
+  if (!eh && warp > 0) { eh = s_h[warp - 1]; ev = s_v[warp - 1]; es = s_s[warp - 1]; }
   double run = eh ? ev : 0.0;
+  int rsrc = eh ? es : -1;
   for (int p = p0; p < p1; ++p) {
     carry[p] = run;
-    if (has[p]) run = last[p];
+    csrc[p] = rsrc;
+    if (has[p]) { run = last[p]; rsrc = lsrc[p]; }
   }
 }
 

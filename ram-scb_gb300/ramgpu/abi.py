@@ -33,6 +33,7 @@ EXPORTS = (
     "ramgpu_apply_op", "ramgpu_set_timing", "ramgpu_kernel_times", "ramgpu_probe_fp64",
     "ramgpu_sumrc_noalloc", "ramgpu_set_graph", "ramgpu_set_launch_shape",
     "ramgpu_get_launch_shape", "ramgpu_autotune", "ramgpu_set_kp_all",
+    "ramgpu_adj_forward", "ramgpu_adj_backward", "ramgpu_adj_digest", "ramgpu_adj_record",
 )
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
           "anisch", "dts_tables", "sumrc")
@@ -58,6 +59,11 @@ class GridStruct(C.Structure):
                 ("ekev", _P), ("ebnd", _P), ("we", _P), ("de", _P), ("mu", _P), ("dmu", _P),
                 ("wmu", _P), ("upa", _P), ("rmas", _P), ("grel", _P), ("grbnd", _P), ("v", _P),
                 ("epp", _P), ("ernh", _P), ("ffactor", _P)]
+
+
+class ObsStruct(C.Structure):
+    _fields_ = [("member", C.c_int), ("s", C.c_int), ("call", C.c_int), ("k", C.c_int),
+                ("l", C.c_int), ("lshell", C.c_double), ("mlt", C.c_double), ("log_obs", C.c_double)]
 
 
 _lib = None
@@ -116,6 +122,10 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_get_launch_shape": ([vp, ip, ip], i),
         "ramgpu_autotune": ([vp, d, i, dp], i),
         "ramgpu_set_kp_all": ([vp, dp], i),
+        "ramgpu_adj_forward": ([vp, i, d, dp, i, C.POINTER(ObsStruct), i, dp], i),
+        "ramgpu_adj_backward": ([vp, dp, dp], i),
+        "ramgpu_adj_digest": ([vp, C.POINTER(C.c_ulonglong)], i),
+        "ramgpu_adj_record": ([vp, i, C.POINTER(C.c_ubyte)], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -326,6 +336,49 @@ class RamGpu:
         ms = np.zeros(4)
         self._ck(self.lib.ramgpu_autotune(self.h, float(dts), int(reps), _dptr(ms)), "autotune")
         return self.launch_shape(), ms
+
+    # --------------------------------------------------------------- adjoint
+    def adj_forward(self, ncalls: int, dts: float, kp, k_ckpt: int, obs):
+        """Checkpointed forward pass of a window; kp: (ncalls, n_members) or
+        (ncalls,) Kp; obs: list of dicts with member, s, call, k, l (0-based),
+        lshell [RE], mlt [h], log_obs.  Returns J per member."""
+        kpa = np.asarray(kp, dtype=np.float64)
+        if kpa.ndim == 1:
+            kpa = np.repeat(kpa[:, None], self.n_members, axis=1)
+        kpa = np.ascontiguousarray(kpa.reshape(ncalls, self.n_members))
+        arr = (ObsStruct * max(1, len(obs)))()
+        for t, o in enumerate(obs):
+            arr[t] = ObsStruct(o["member"], o["s"], o["call"], o["k"], o["l"], o["lshell"], o["mlt"],
+                               o["log_obs"])
+        J = np.zeros(self.n_members)
+        self._ck(self.lib.ramgpu_adj_forward(self.h, int(ncalls), float(dts), _dptr(kpa), int(k_ckpt),
+                                             arr, len(obs), _dptr(J)), "adj_forward")
+        return J
+
+    def adj_backward(self):
+        """(dJ/dF2 at the window start, dJ/dFGEOS): arrays of shape
+        (members, ns, NR, NT, NE, NPA) and (members, ns, NT, NE, NPA), each
+        trailing block in Fortran order like F2(S,:,:,:,:) / FGEOS(S,:,:,:)."""
+        g = self.grid
+        gf = np.zeros(self.n_members * self.ns * g.ncell)
+        gb = np.zeros(self.n_members * self.ns * g.nt * g.ne * g.npa)
+        self._ck(self.lib.ramgpu_adj_backward(self.h, _dptr(gf), _dptr(gb)), "adj_backward")
+        gf = gf.reshape(self.n_members, self.ns, g.npa, g.ne, g.nt, g.nr).transpose(0, 1, 5, 4, 3, 2)
+        gb = gb.reshape(self.n_members, self.ns, g.npa, g.ne, g.nt).transpose(0, 1, 4, 3, 2)
+        return gf, gb
+
+    def adj_record(self, call: int, nitems: int) -> np.ndarray:
+        """Branch record of one call: (8 sweeps, items, NR*NT*NE*NPA) bytes."""
+        g = self.grid
+        out = np.zeros((8, nitems, g.ncell), dtype=np.uint8)
+        self._ck(self.lib.ramgpu_adj_record(self.h, int(call), out.ctypes.data_as(C.POINTER(C.c_ubyte))),
+                 "adj_record")
+        return out
+
+    def adj_digest(self) -> int:
+        v = C.c_ulonglong()
+        self._ck(self.lib.ramgpu_adj_digest(self.h, C.byref(v)), "adj_digest")
+        return int(v.value)
 
     def set_stream(self, stream_ptr: int):
         self._ck(self.lib.ramgpu_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")

@@ -1,0 +1,202 @@
+"""GPU frozen-limiter adjoint: finite differences, checkpointing, batching.
+
+J = sum (log flux_model - log flux_obs)^2 over virtual-spacecraft samples
+of FLUX (src/ModRamRun.f90:214) at pitch-angle bin L=2, bilinear in
+(L-shell, MLT).  The observations come from a seed-perturbed "truth" run.
+Finite differences use relative perturbations x0*(1 +- eps*r) small enough
+that the recorded branch pattern (digest) is unchanged, so the scheme is
+linear between the two runs and the directional derivative must agree with
+the adjoint to 1e-6 relative.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from ramgpu import abi, workload as W
+
+pytestmark = pytest.mark.gpu
+
+
+def interp_flux(g, flux, o):
+    """Python mirror of the device observation operator."""
+    lz = g.lz
+    i0 = 1
+    while i0 + 1 < g.nr - 1 and lz[i0 + 1] <= o["lshell"]:
+        i0 += 1
+    wi = min(1.0, max(0.0, (o["lshell"] - lz[i0]) / (lz[i0 + 1] - lz[i0])))
+    ph = math.fmod(o["mlt"] * math.pi / 12.0, 2 * math.pi)
+    j0 = min(int(ph / g.dphi), g.nt - 2)
+    j1 = 0 if j0 + 1 == g.nt - 1 else j0 + 1
+    wj = min(1.0, max(0.0, (ph - g.phi[j0]) / g.dphi))
+    v = 0.0
+    for a in (0, 1):
+        for b in (0, 1):
+            w = (wi if a else 1 - wi) * (wj if b else 1 - wj)
+            v += w * flux[i0 + a, j1 if b else j0, o["k"], o["l"]]
+    return v
+
+
+def make_case(wl, members, ncalls, nobs, seed, species_lists=None, outer=0):
+    g = wl.grid
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ns = len(g.species)
+    species_lists = species_lists or [list(range(ns))] * members
+    kp = rng.uniform(2.0, 5.0, size=(ncalls, members))
+    obs = []
+    for t in range(nobs):
+        m = int(rng.integers(members))
+        s = int(rng.choice(species_lists[m]))
+        # the last `outer` samples sit next to the outer boundary, where FGEOS acts
+        lo, hi = (g.lz[g.nr - 2], g.lz[g.nr - 1] - 1e-6) if t >= nobs - outer else (2.6, 5.9)
+        obs.append({"member": m, "s": s, "call": int(rng.integers(ncalls)), "k": int(rng.integers(8, 28)),
+                    "l": 1, "lshell": float(rng.uniform(lo, hi)), "mlt": float(rng.uniform(0, 24)),
+                    "log_obs": 0.0})
+    # truth: a seed-perturbed initial state, same drivers
+    truth = abi.RamGpu(g, wl.fields, n_members=members)
+    for m in range(members):
+        truth.set_member_species(m, species_lists[m])
+        for s in range(ns):
+            truth.upload_f2(m, s, np.asarray(wl.f2[s]) * rng.lognormal(0.0, 0.05, size=wl.f2[s].shape))
+            truth.set_boundary(m, s, wl.fgeos[s])
+    for c in range(ncalls):
+        for m in range(members):
+            truth.set_kp(m, kp[c, m])
+        truth.ram_run(wl.dts)
+        for o in obs:
+            if o["call"] == c:
+                o["log_obs"] = math.log(interp_flux(g, truth.flux(o["member"], o["s"]), o))
+    truth.close()
+    model = abi.RamGpu(g, wl.fields, n_members=members)
+    for m in range(members):
+        model.set_member_species(m, species_lists[m])
+        for s in range(ns):
+            model.upload_f2(m, s, wl.f2[s])
+            model.set_boundary(m, s, wl.fgeos[s])
+    return model, kp, obs
+
+
+@pytest.fixture(scope="module")
+def tiny():
+    return W.make_workload("tiny")
+
+
+@pytest.fixture(scope="module")
+def case(tiny):
+    model, kp, obs = make_case(tiny, 1, 4, 30, seed=11, outer=10)
+    J = model.adj_forward(NCALLS, tiny.dts, kp, 2, obs)
+    digest = model.adj_digest()
+    gf, gb = model.adj_backward()
+    return tiny, model, kp, obs, J, digest, gf, gb
+
+
+def _set_f2(model, wl, scale):
+    for s in range(len(wl.grid.species)):
+        model.upload_f2(0, s, np.asarray(wl.f2[s]) * scale[s])
+
+
+NCALLS = 4
+
+
+def _records(model, ns):
+    return np.stack([model.adj_record(c, ns) for c in range(NCALLS)])
+
+
+def _run(model, wl, kp, obs, f2_scale=None, fg_scale=None):
+    """J and the branch record of the window for scaled F2 / FGEOS."""
+    ns = len(wl.grid.species)
+    for s in range(ns):
+        model.upload_f2(0, s, np.asarray(wl.f2[s]) * (1.0 if f2_scale is None else f2_scale[s]))
+        model.set_boundary(0, s, wl.fgeos[s] * (1.0 if fg_scale is None else fg_scale[s]))
+    J = model.adj_forward(NCALLS, wl.dts, kp, NCALLS, obs)[0]
+    return J, _records(model, ns)
+
+
+def _fd_check(case, directions, make_r, use_f2, seed, eps_list):
+    """Central differences along x0*(1 +- eps*r) for each eps in eps_list,
+    with the branch record of both runs compared byte by byte against the
+    unperturbed run.  Faces whose limiter sits on a kink (R at 1/beta, 1 or
+    beta, where adjacent linear pieces give equal values) flip for any eps,
+    in numbers proportional to eps; being continuous, they do not bias the
+    central difference.  The best eps (truncation vs rounding noise) must
+    agree with the adjoint to 1e-6, with kink crossings below 1e-3 of the
+    faces."""
+    wl, model, kp, obs, J0, dig0, gf, gb = case
+    ns = len(wl.grid.species)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    _, rec0 = _run(model, wl, kp, obs)
+    nfaces = rec0.size
+    worst, flips_max = 0.0, 0
+    try:
+        for direction in range(directions):
+            r = make_r(rng)
+            if use_f2:
+                ad = sum(float(np.sum(gf[0, s] * np.asarray(wl.f2[s]) * r[s])) for s in range(ns))
+            else:
+                ad = sum(float(np.sum(gb[0, s] * wl.fgeos[s] * r[s])) for s in range(ns))
+            trials = []
+            for eps in eps_list:
+                sp = [1.0 + eps * x for x in r]
+                sm = [1.0 - eps * x for x in r]
+                jp, recp = _run(model, wl, kp, obs, **({"f2_scale": sp} if use_f2 else {"fg_scale": sp}))
+                jm, recm = _run(model, wl, kp, obs, **({"f2_scale": sm} if use_f2 else {"fg_scale": sm}))
+                flips = int(np.count_nonzero(recp != rec0) + np.count_nonzero(recm != rec0))
+                fd = (jp - jm) / (2 * eps)
+                trials.append((abs(fd - ad) / abs(ad), flips, eps))
+            print(direction, [(f"{e:.0e}", f, f"{er:.2e}") for er, f, e in trials])
+            err, flips, eps = min(trials)
+            worst = max(worst, err)
+            flips_max = max(flips_max, flips)
+            assert err <= 1e-6, (direction, eps, err, flips)
+            assert flips <= 1e-3 * nfaces, (direction, flips, nfaces)
+    finally:
+        _run(model, wl, kp, obs)
+    print(f"FD {'F2' if use_f2 else 'FGEOS'}: {directions} directions, worst relative error {worst:.2e}, "
+          f"most flipped faces {flips_max} of {nfaces}")
+
+
+def test_gradient_finite_differences_f2(case):
+    wl, model, kp, obs, J0, dig0, gf, _ = case
+    ns = len(wl.grid.species)
+    assert J0[0] > 0 and np.isfinite(gf).all()
+    # two identical runs record identical branches
+    model.adj_forward(NCALLS, wl.dts, kp, 2, obs)
+    assert model.adj_digest() == dig0
+    _fd_check(case, 16, lambda rng: [rng.uniform(-1.0, 1.0, size=wl.f2[s].shape) for s in range(ns)],
+              True, 5, (1e-6, 1e-7))
+
+
+def test_gradient_finite_differences_fgeos(case):
+    wl, model, kp, obs, J0, dig0, _, gb = case
+    ns = len(wl.grid.species)
+    assert np.abs(gb).max() > 0
+    _fd_check(case, 4, lambda rng: [rng.uniform(-1.0, 1.0, size=wl.fgeos[s].shape) for s in range(ns)],
+              False, 6, (1e-4, 1e-5, 1e-6))
+
+
+def test_checkpoint_spacing_invariant(case):
+    wl, model, kp, obs, J0, _, gf, gb = case
+    _set_f2(model, wl, [1.0] * len(wl.grid.species))
+    J1 = model.adj_forward(4, wl.dts, kp, 1, obs)
+    gf1, gb1 = model.adj_backward()
+    assert abs(J1[0] - J0[0]) <= 1e-13 * J0[0]
+    assert np.max(np.abs(gf1 - gf)) <= 1e-12 * np.max(np.abs(gf))
+    assert np.max(np.abs(gb1 - gb)) <= 1e-12 * np.max(np.abs(gb))
+    # after the backward pass F2 is the window's initial state
+    assert np.array_equal(model.download_f2(0, 1), np.asfortranarray(wl.f2[1]))
+
+
+def test_batched_gradients_equal_solo(tiny):
+    lists = [[0, 1, 2, 3], [1, 3], [2]]
+    model, kp, obs = make_case(tiny, 3, 3, 24, seed=21, species_lists=lists)
+    J = model.adj_forward(3, tiny.dts, kp, 2, obs)
+    gf, gb = model.adj_backward()
+    for m in range(3):
+        solo, _, _ = make_case(tiny, 1, 3, 0, seed=99, species_lists=[lists[m]])
+        obs_m = [dict(o, member=0) for o in obs if o["member"] == m]
+        Jm = solo.adj_forward(3, tiny.dts, kp[:, m], 2, obs_m)
+        gfm, gbm = solo.adj_backward()
+        assert abs(Jm[0] - J[m]) <= 1e-13 * max(J[m], 1e-300)
+        assert np.max(np.abs(gfm[0] - gf[m])) <= 1e-12 * max(np.max(np.abs(gf[m])), 1e-300)
+        assert np.max(np.abs(gbm[0] - gb[m])) <= 1e-12 * max(np.max(np.abs(gb[m])), 1e-300)
+        solo.close()
