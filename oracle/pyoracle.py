@@ -8,6 +8,7 @@ no per-routine golden vectors in the reference); see ram_oracle.h.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 from pathlib import Path
@@ -90,6 +91,17 @@ def load():
         lib.ro_ram_run.argtypes = [gp, C.c_int, sp, pp, C.c_double, _P, _P, PP, PP, PP, PP, PP,
                                    C.POINTER(RoLosses), _P, C.c_int]
         lib.ro_half_step.argtypes = [gp, sp, pp, dpp, _P, _P, _P, _P, _P, C.c_int]
+        U8 = C.POINTER(C.c_ubyte)
+        lib.ro_driftr_rec.argtypes = [gp, sp, pp, dpp, _P, _P, _P, _P, U8, _IP]
+        lib.ro_driftr_rec.restype = C.c_double
+        for n in ("ro_driftp_rec", "ro_drifte_rec", "ro_driftmu_rec"):
+            f = getattr(lib, n)
+            f.argtypes = [gp, sp, pp, dpp, _P, _P, _P, U8]
+            f.restype = C.c_double
+        lib.ro_driftr_adj.argtypes = [gp, pp, _P, U8, _IP, _P, _P]
+        lib.ro_driftp_adj.argtypes = [gp, pp, _P, U8, _P]
+        lib.ro_drifte_adj.argtypes = [gp, sp, pp, _P, U8, _P]
+        lib.ro_driftmu_adj.argtypes = [gp, pp, _P, U8, _P]
         _lib = lib
     return _lib
 
@@ -100,6 +112,32 @@ def _f(a, dtype=np.float64):
 
 def _p(a):
     return a.ctypes.data_as(_P) if a is not None else None
+
+
+def _u8(a):
+    return a.ctypes.data_as(C.POINTER(C.c_ubyte))
+
+
+def _ip(a):
+    return a.ctypes.data_as(_IP)
+
+
+def obs_cells(grid, o):
+    """Bilinear (L-shell, MLT) stencil of one observation: four (i, j, weight)
+    over I >= 2 (0-based i >= 1) with J = NT folded onto J = 1."""
+    lz, nr, nt, dphi = grid.lz, grid.nr, grid.nt, grid.dphi
+    i0 = 1
+    while i0 + 1 < nr - 1 and lz[i0 + 1] <= o["lshell"]:
+        i0 += 1
+    wi = min(1.0, max(0.0, (o["lshell"] - lz[i0]) / (lz[i0 + 1] - lz[i0])))
+    ph = math.fmod(o["mlt"] * math.pi / 12.0, 2 * math.pi)
+    if ph < 0:
+        ph += 2 * math.pi
+    j0 = min(int(ph / dphi), nt - 2)
+    j1 = 0 if j0 + 1 == nt - 1 else j0 + 1
+    wj = min(1.0, max(0.0, (ph - grid.phi[j0]) / dphi))
+    return [(i0 + a, j1 if b else j0, (wi if a else 1 - wi) * (wj if b else 1 - wj))
+            for a in (0, 1) for b in (0, 1)]
 
 
 class Oracle:
@@ -236,3 +274,135 @@ class Oracle:
         if fl:
             out["flux"] = dict(zip(idx, fl))
         return out
+
+    # ------------------------------------------------------------- adjoint
+    _REC = {"R": "ro_driftr_rec", "P": "ro_driftp_rec", "E": "ro_drifte_rec", "MU": "ro_driftmu_rec"}
+
+    def sweep_rec(self, which, s, f2, vt, dts, fgeos=None, closed=False):
+        """One DRIFT* routine (in place) that also records its frozen branches.
+        Returns a tape entry (which, s, cdrift, rec, gsrc|None)."""
+        g = self.grid
+        shape = (g.nr, g.nt, g.ne, g.npa)
+        dp = self.driftpara(s, dts)
+        p = self.params(dts, closed)
+        cd = np.zeros(shape, order="F")
+        rec = np.zeros(shape, dtype=np.uint8, order="F")
+        args = [C.byref(self.rg), C.byref(self.sp[s]), C.byref(p), C.byref(dp["_struct"]), _p(vt)]
+        if which == "R":
+            gsrc = np.full((g.nt, g.ne, g.npa), -1, dtype=np.int32, order="F")
+            self.lib.ro_driftr_rec(*args, _p(_f(fgeos)), _p(f2), _p(cd), _u8(rec), _ip(gsrc))
+            return ("R", s, cd, rec, gsrc)
+        getattr(self.lib, self._REC[which])(*args, _p(f2), _p(cd), _u8(rec))
+        return (which, s, cd, rec, None)
+
+    def sweep_adj(self, tape, lam, dts, gfgeos=None, closed=False):
+        """Transpose of a recorded sweep applied to lam (Fortran, in place);
+        DRIFTR adds its FGEOS gradient into gfgeos."""
+        which, s, cd, rec, gsrc = tape
+        p = self.params(dts, closed)
+        rg = C.byref(self.rg)
+        if which == "R":
+            self.lib.ro_driftr_adj(rg, C.byref(p), _p(cd), _u8(rec), _ip(gsrc), _p(lam), _p(gfgeos))
+        elif which == "P":
+            self.lib.ro_driftp_adj(rg, C.byref(p), _p(cd), _u8(rec), _p(lam))
+        elif which == "E":
+            self.lib.ro_drifte_adj(rg, C.byref(self.sp[s]), C.byref(p), _p(cd), _u8(rec), _p(lam))
+        else:
+            self.lib.ro_driftmu_adj(rg, C.byref(p), _p(cd), _u8(rec), _p(lam))
+
+    def loss_factor(self, s, dts, do_atmol=True):
+        """Per-cell factor of CHAREXCHANGE, ATMOL, ATMOL, CHAREXCHANGE as
+        ram_run applies them between the two sweep halves."""
+        g = self.grid
+        charge, atlos = self.cepara(s, dts, do_atmol)
+        at = np.ones((g.nr, g.nt, g.ne, g.npa), order="F")
+        if do_atmol:
+            self.lib.ro_atmol(C.byref(self.rg), _p(at), _p(atlos))
+        ch = charge if self.grid.species[s].cex_kind else np.ones_like(at)
+        return ch, at
+
+    def window_gradient(self, f2s, fgeos, dts, kps, obs, species=None, closed=False, do_atmol=True,
+                        records=None):
+        """Scalar adjoint of a window of len(kps) ram_run calls for one member.
+
+        J = sum over obs of (log flux - log_obs)^2 with flux = F2/FFACTOR/FNHS
+        (src/ModRamRun.f90:214) after call o["call"], bilinear in (L-shell,
+        MLT) at 0-based bins (o["k"], o["l"]).  Forward: the reference call
+        sequence of ram_run (src/ModRamRun.f90:77-225) with every sweep
+        recorded; backward: the transposes in reverse order.  f2s is not
+        modified.  With ``records`` a list, each call's branch record is
+        appended as an (8 sweeps, species, NR*NT*NE*NPA) uint8 array.
+        Returns (J, {s: dJ/dF2}, {s: dJ/dFGEOS})."""
+        g = self.grid
+        idx = list(range(self.ns)) if species is None else list(species)
+        f = {s: np.array(f2s[s], dtype=np.float64, order="F", copy=True) for s in idx}
+        fg = {s: _f(fgeos[s]) for s in idx}
+        fac = {s: self.loss_factor(s, dts, do_atmol) for s in idx}
+        out = np.asarray(self._keep["outside"]) == 1
+        fnhs = self._keep["f_fnhs"]
+        tapes, fm = [], {}
+        J = 0.0
+        for c, kp in enumerate(kps):
+            vt = self.vt_vols(kp)
+            tc = {}
+            for s in idx:
+                t = [self.sweep_rec("R", s, f[s], vt, dts, fg[s], closed),
+                     self.sweep_rec("P", s, f[s], vt, dts, closed=closed),
+                     self.sweep_rec("E", s, f[s], vt, dts, closed=closed),
+                     self.sweep_rec("MU", s, f[s], vt, dts, closed=closed)]
+                ch, at = fac[s]
+                f[s] *= ch
+                f[s] *= at
+                f[s] *= at
+                f[s] *= ch
+                t += [self.sweep_rec("MU", s, f[s], vt, dts, closed=closed),
+                      self.sweep_rec("E", s, f[s], vt, dts, closed=closed),
+                      self.sweep_rec("P", s, f[s], vt, dts, closed=closed),
+                      self.sweep_rec("R", s, f[s], vt, dts, fg[s], closed)]
+                tc[s] = t
+                f[s][:, g.nt - 1] = f[s][:, 0]
+                f[s][out] = 1e-31
+                self.anisch(s, f[s])
+            tapes.append(tc)
+            if records is not None:
+                records.append(np.stack([np.stack([tc[s][q][3].reshape(-1, order="F") for s in idx])
+                                         for q in range(8)]))
+            for n, o in enumerate(obs):
+                if o["call"] != c:
+                    continue
+                ff = np.asarray(self.grid.ffactor[o["s"]])
+                v = sum(w * (f[o["s"]][i, j, o["k"], o["l"]] / ff[i, o["k"], o["l"]] / fnhs[i, j, o["l"]])
+                        for i, j, w in obs_cells(g, o))
+                fm[n] = v
+                J += (math.log(v) - o["log_obs"]) ** 2
+        lam = {s: np.zeros((g.nr, g.nt, g.ne, g.npa), order="F") for s in idx}
+        gfg = {s: np.zeros((g.nt, g.ne, g.npa), order="F") for s in idx}
+        for c in range(len(kps) - 1, -1, -1):
+            for n, o in enumerate(obs):
+                if o["call"] != c:
+                    continue
+                v = fm[n]
+                gr = 2.0 * (math.log(v) - o["log_obs"]) / v
+                ff = np.asarray(self.grid.ffactor[o["s"]])
+                for i, j, w in obs_cells(g, o):
+                    lam[o["s"]][i, j, o["k"], o["l"]] += gr * w / (ff[i, o["k"], o["l"]] * fnhs[i, j, o["l"]])
+            for s in idx:
+                lm = lam[s]
+                # ANISCH: F2(I,J,K,1) = F2(I,J,K,2), I >= 2, K >= 2
+                lm[1:, :, 1:, 1] += lm[1:, :, 1:, 0]
+                lm[1:, :, 1:, 0] = 0.0
+                lm[out] = 0.0
+                lm[:, 0] += lm[:, g.nt - 1]
+                lm[:, g.nt - 1] = 0.0
+                t = tapes[c][s]
+                for e in t[7:3:-1]:
+                    self.sweep_adj(e, lm, dts, gfg[s], closed)
+                ch, at = fac[s]
+                lm *= ch
+                lm *= at
+                lm *= at
+                lm *= ch
+                for e in t[3::-1]:
+                    self.sweep_adj(e, lm, dts, gfg[s], closed)
+            tapes[c] = None
+        return J, lam, gfg

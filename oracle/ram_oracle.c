@@ -130,11 +130,41 @@ void ro_driftpara(const ro_grid *g, const ro_species *sp, const ro_params *p, ro
     }
 }
 
+/* Frozen-limiter branch of one face (for the adjoint): 0 upwind only,
+ * 1 LIMITER = BetaLim*R, 2 LIMITER = 1, 3 LIMITER = R, 4 LIMITER = BetaLim,
+ * following MAX(MIN(BetaLim*R,1.),MIN(R,BetaLim)) literally. */
+static int limiter_case(double betalim, double r)
+{
+    double a = dmin(betalim * r, 1.), b = dmin(r, betalim);
+    if (dmax(a, b) == a && !(b > a)) return (betalim * r < 1.) ? 1 : 2;
+    return (r < betalim) ? 3 : 4;
+}
+#define REC_CLIP 8
+
 /* ------------------------------------------------------------------ DRIFTR */
+static double driftr_impl(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                          const ro_driftpara_t *dp, const double *vt, const double *fgeos,
+                          double *f2, double *cdrift, unsigned char *rec, int *gsrc);
+
 double ro_driftr(const ro_grid *g, const ro_species *sp, const ro_params *p,
                  const ro_driftpara_t *dp, const double *vt, const double *fgeos,
                  double *f2, double *cdrift)
 {
+    return driftr_impl(g, sp, p, dp, vt, fgeos, f2, cdrift, NULL, NULL);
+}
+
+double ro_driftr_rec(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                     const ro_driftpara_t *dp, const double *vt, const double *fgeos,
+                     double *f2, double *cdrift, unsigned char *rec, int *gsrc)
+{
+    return driftr_impl(g, sp, p, dp, vt, fgeos, f2, cdrift, rec, gsrc);
+}
+
+static double driftr_impl(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                          const ro_driftpara_t *dp, const double *vt, const double *fgeos,
+                          double *f2, double *cdrift, unsigned char *rec, int *gsrc)
+{
+    int last_src = -1; /* line whose F(NR+1) is currently held, -1: none or 0 outside */
     const double DTs = p->dts, MDR = g->mdr, DPHI = g->dphi, BetaLim = p->betalim;
     const int QS = sp->qs;
     double DtDriftR = 100000.0;
@@ -184,6 +214,8 @@ double ro_driftr(const ro_grid *g, const ro_species *sp, const ro_params *p,
                     if (CD[I - 1] < 0) SG(I, J) = -1;
                 }
                 int UR;
+                if (rec)
+                    for (int I = 1; I <= NR; ++I) rec[IX4(I, J, K, L)] = 0;
                 if (SG(NR, J) == 1) {
                     FB(1) = 0.;
                     FB(NR) = FF(NR);
@@ -194,15 +226,19 @@ double ro_driftr(const ro_grid *g, const ro_species *sp, const ro_params *p,
                     if (OUTSIDE(NR, J) == 1) {
                         FF(NR + 1) = 0.;
                         FF(NR + 2) = 0.;
+                        last_src = -1;
                     } else {
                         FF(NR + 1) = fgeos[IXG(J, K, L)] * g->conf1 * FNHS(NR, J, L);
                         FF(NR + 2) = fgeos[IXG(J, K, L)] * g->conf2 * FNHS(NR, J, L);
+                        last_src = (int)IXG(J, K, L);
                     }
                 }
+                if (gsrc) gsrc[IXG(J, K, L)] = last_src;
                 for (int I = 2; I <= UR; ++I) {
                     int s = SG(I, J);
                     double X = FF(I + 1) - FF(I);
                     double FUP = 0.5 * (FF(I) + FF(I + 1) - s * X);
+                    int cs = 0;
                     if (fabs(X) <= 1.E-27) FB(I) = FUP;
                     if (fabs(X) > 1.E-27) {
                         int N = I + 1 - s;
@@ -212,8 +248,10 @@ double ro_driftr(const ro_grid *g, const ro_species *sp, const ro_params *p,
                             double LIM = limiter(BetaLim, R);
                             double CORR = -0.5 * (CD[I - 1] - s) * X;
                             FB(I) = FUP + LIM * CORR;
+                            cs = limiter_case(BetaLim, R);
                         }
                     }
+                    if (rec) rec[IX4(I, J, K, L)] = (unsigned char)cs;
                 }
                 if (p->closed) {
                     FB(1) = 0.;
@@ -221,7 +259,10 @@ double ro_driftr(const ro_grid *g, const ro_species *sp, const ro_params *p,
                 }
                 for (int I = 2; I <= NR; ++I) {
                     F2(I, J, K, L) = F2(I, J, K, L) - CD[I - 1] * FB(I) + CD[I - 2] * FB(I - 1);
-                    if (F2(I, J, K, L) < 0) F2(I, J, K, L) = 1E-15;
+                    if (F2(I, J, K, L) < 0) {
+                        F2(I, J, K, L) = 1E-15;
+                        if (rec) rec[IX4(I, J, K, L)] |= REC_CLIP;
+                    }
                 }
                 if (cdrift)
                     for (int I = 1; I <= NR; ++I) cdrift[IX4(I, J, K, L)] = CD[I - 1];
@@ -239,8 +280,23 @@ double ro_driftr(const ro_grid *g, const ro_species *sp, const ro_params *p,
 }
 
 /* ------------------------------------------------------------------ DRIFTP */
+static double driftp_impl(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                          const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift,
+                          unsigned char *rec);
 double ro_driftp(const ro_grid *g, const ro_species *sp, const ro_params *p,
                  const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift)
+{
+    return driftp_impl(g, sp, p, dp, vt, f2, cdrift, NULL);
+}
+double ro_driftp_rec(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                     const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift,
+                     unsigned char *rec)
+{
+    return driftp_impl(g, sp, p, dp, vt, f2, cdrift, rec);
+}
+static double driftp_impl(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                          const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift,
+                          unsigned char *rec)
 {
     const double DTs = p->dts, MDR = g->mdr, DPHI = g->dphi, BetaLim = p->betalim;
     double DtDriftP = 100000.0;
@@ -277,6 +333,7 @@ double ro_driftp(const ro_grid *g, const ro_species *sp, const ro_params *p,
                     if (C(J) < 0) s = -1;
                     double X = FF(J1) - FF(J);
                     double FUP = 0.5 * (FF(J) + FF(J1) - s * X);
+                    int cs = 0;
                     if (fabs(X) <= 1.E-27) FB(J) = FUP;
                     if (fabs(X) > 1.E-27) {
                         int N = J + 1 - s;
@@ -287,14 +344,20 @@ double ro_driftp(const ro_grid *g, const ro_species *sp, const ro_params *p,
                             double LIM = limiter(BetaLim, R);
                             double CORR = -0.5 * (C(J) - s) * X;
                             FB(J) = FUP + LIM * CORR;
+                            cs = limiter_case(BetaLim, R);
                         }
                     }
+                    if (rec) rec[IX4(I, J, K, L)] = (unsigned char)cs;
                 }
                 C(1) = C(NT);
                 FB(1) = FB(NT);
+                if (rec) rec[IX4(I, 1, K, L)] = 0;
                 for (int J = 2; J <= NT; ++J) {
                     F2(I, J, K, L) = F2(I, J, K, L) - C(J) * FB(J) + C(J - 1) * FB(J - 1);
-                    if (F2(I, J, K, L) < 0) F2(I, J, K, L) = 1E-15;
+                    if (F2(I, J, K, L) < 0) {
+                        F2(I, J, K, L) = 1E-15;
+                        if (rec) rec[IX4(I, J, K, L)] |= REC_CLIP;
+                    }
                 }
                 F2(I, 1, K, L) = F2(I, NT, K, L);
                 if (cdrift)
@@ -310,8 +373,23 @@ double ro_driftp(const ro_grid *g, const ro_species *sp, const ro_params *p,
 }
 
 /* ------------------------------------------------------------------ DRIFTE */
+static double drifte_impl(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                          const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift,
+                          unsigned char *rec);
 double ro_drifte(const ro_grid *g, const ro_species *sp, const ro_params *p,
                  const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift)
+{
+    return drifte_impl(g, sp, p, dp, vt, f2, cdrift, NULL);
+}
+double ro_drifte_rec(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                     const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift,
+                     unsigned char *rec)
+{
+    return drifte_impl(g, sp, p, dp, vt, f2, cdrift, rec);
+}
+static double drifte_impl(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                          const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift,
+                          unsigned char *rec)
 {
     const double DTs = p->dts, MDR = g->mdr, DPHI = g->dphi, BetaLim = p->betalim;
     const int QS = sp->qs;
@@ -365,6 +443,7 @@ double ro_drifte(const ro_grid *g, const ro_species *sp, const ro_params *p,
                     if (C(K) < 0) s = -1;
                     double X = FF(K + 1) - FF(K);
                     double FUP = 0.5 * (FF(K) + FF(K + 1) - s * X);
+                    int cs = 0;
                     if (fabs(X) <= 1.E-27) FB(K) = FUP;
                     if (fabs(X) > 1.E-27) {
                         int N = K + 1 - s;
@@ -374,8 +453,10 @@ double ro_drifte(const ro_grid *g, const ro_species *sp, const ro_params *p,
                             double LIM = limiter(BetaLim, R);
                             double CORR = -0.5 * (C(K) / DE(K) - s) * X;
                             FB(K) = FUP + LIM * CORR;
+                            cs = limiter_case(BetaLim, R);
                         }
                     }
+                    if (rec) rec[IX4(I, J, K, L)] = (unsigned char)cs;
                 }
                 if (p->closed) {
                     FB(1) = 0.;
@@ -383,7 +464,10 @@ double ro_drifte(const ro_grid *g, const ro_species *sp, const ro_params *p,
                 }
                 for (int K = 2; K <= NE; ++K) {
                     F2(I, J, K, L) = F2(I, J, K, L) - C(K) / WE(K) * FB(K) + C(K - 1) / WE(K) * FB(K - 1);
-                    if (F2(I, J, K, L) < 0) F2(I, J, K, L) = 1E-15;
+                    if (F2(I, J, K, L) < 0) {
+                        F2(I, J, K, L) = 1E-15;
+                        if (rec) rec[IX4(I, J, K, L)] |= REC_CLIP;
+                    }
                 }
                 if (cdrift)
                     for (int K = 1; K <= NE; ++K) cdrift[IX4(I, J, K, L)] = C(K);
@@ -400,8 +484,23 @@ double ro_drifte(const ro_grid *g, const ro_species *sp, const ro_params *p,
 }
 
 /* ----------------------------------------------------------------- DRIFTMU */
+static double driftmu_impl(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                           const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift,
+                           unsigned char *rec);
 double ro_driftmu(const ro_grid *g, const ro_species *sp, const ro_params *p,
                   const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift)
+{
+    return driftmu_impl(g, sp, p, dp, vt, f2, cdrift, NULL);
+}
+double ro_driftmu_rec(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                      const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift,
+                      unsigned char *rec)
+{
+    return driftmu_impl(g, sp, p, dp, vt, f2, cdrift, rec);
+}
+static double driftmu_impl(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                           const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift,
+                           unsigned char *rec)
 {
     const double DTs = p->dts, MDR = g->mdr, DPHI = g->dphi, BetaLim = p->betalim;
     const int QS = sp->qs;
@@ -447,6 +546,7 @@ double ro_driftmu(const ro_grid *g, const ro_species *sp, const ro_params *p,
                     }
                     int s = 1;
                     if (C(L) < 0.0) s = -1;
+                    if (rec) rec[IX4(I, J, K, L)] = 0;
                     if (L <= NPA - 2) {
                         double X = FF(L + 1) - FF(L);
                         double FUP = 0.5 * (FF(L) + FF(L + 1) - s * X);
@@ -459,6 +559,7 @@ double ro_driftmu(const ro_grid *g, const ro_species *sp, const ro_params *p,
                                 double LIM = limiter(BetaLim, R);
                                 double CORR = -0.5 * (C(L) / DMU(L) - s) * X;
                                 FB(L) = FUP + LIM * CORR;
+                                if (rec) rec[IX4(I, J, K, L)] = (unsigned char)limiter_case(BetaLim, R);
                             }
                         }
                     }
@@ -469,7 +570,10 @@ double ro_driftmu(const ro_grid *g, const ro_species *sp, const ro_params *p,
                 if (p->closed) FB(NPA - 1) = 0.;
                 for (int L = 2; L <= NPA - 1; ++L) {
                     F2(I, J, K, L) = F2(I, J, K, L) - C(L) / WMU(L) * FB(L) + C(L - 1) / WMU(L) * FB(L - 1);
-                    if (F2(I, J, K, L) < 0) F2(I, J, K, L) = 1E-15;
+                    if (F2(I, J, K, L) < 0) {
+                        F2(I, J, K, L) = 1E-15;
+                        if (rec) rec[IX4(I, J, K, L)] |= REC_CLIP;
+                    }
                 }
                 F2(I, J, K, NPA) = F2(I, J, K, NPA - 1) * FNHS(I, J, NPA) * MU(NPA) / FNHS(I, J, NPA - 1) / MU(NPA - 1);
                 if (cdrift)
@@ -727,4 +831,197 @@ int ro_ram_run(const ro_grid *g, int ns, const ro_species *sp_all, const ro_para
     free(vt);
     (void)HMIN_UNUSED;
     return 0;
+}
+
+/* ==================================================================== adjoint
+ * Scalar adjoint of the frozen-limiter scheme.  The forward sweeps are run
+ * through the *_rec variants, which record per face the limiter case of
+ * MAX(MIN(BetaLim*R,1.),MIN(R,BetaLim)) (0: upwind only, 1: BetaLim*R,
+ * 2: 1, 3: R, 4: BetaLim) and REC_CLIP when the updated cell was clipped,
+ * and (DRIFTR) per line the FGEOS index that F(NR+1) came from.  With those
+ * frozen, each line update is linear in F:
+ *   FUP = 0.5*(F(I)+F(I+1)-s*X)     -> weights 0.5*(1+s), 0.5*(1-s)
+ *   LIMITER*CORR = a * (LIMITER*X),  a = -0.5*(C[/DE|/DMU] - s),
+ *   LIMITER*X = BetaLim*D | X | D | BetaLim*X,  D = F(N)-F(N-1), N = I+1-s,
+ * and the functions below apply its transpose to lam (in place). */
+
+static void adj_face(double *Gb, int I, int I1, int N, int s, int cs, double a, double FBb,
+                     double beta)
+{
+    Gb[I] += 0.5 * (1 + s) * FBb;
+    Gb[I1] += 0.5 * (1 - s) * FBb;
+    if (!cs) return;
+    double Lb = a * FBb;
+    switch (cs) {
+    case 1: Gb[N] += beta * Lb; Gb[N - 1] -= beta * Lb; break;
+    case 2: Gb[I1] += Lb; Gb[I] -= Lb; break;
+    case 3: Gb[N] += Lb; Gb[N - 1] -= Lb; break;
+    default: Gb[I1] += beta * Lb; Gb[I] -= beta * Lb; break;
+    }
+}
+
+void ro_driftr_adj(const ro_grid *g, const ro_params *p, const double *cd, const unsigned char *rec,
+                   const int *gsrc, double *lam, double *gfgeos)
+{
+    const double beta = p->betalim;
+    double *Gb = (double *)malloc(sizeof(double) * (NR + 3));
+    double *Pb = (double *)malloc(sizeof(double) * (NR + 1));
+    for (int K = 1; K <= NE; ++K)
+        for (int L = 1; L <= NPA; ++L)
+            for (int J = 1; J <= NT; ++J) {
+                for (int i = 0; i <= NR + 2; ++i) Gb[i] = 0.;
+                for (int i = 0; i <= NR; ++i) Pb[i] = 0.;
+#define CC(I) cd[IX4(I, J, K, L)]
+#define RC(I) rec[IX4(I, J, K, L)]
+                const int inflow = CC(NR) < 0;
+                Gb[1] = lam[IX4(1, J, K, L)];
+                for (int I = 2; I <= NR; ++I) {
+                    double le = (RC(I) & REC_CLIP) ? 0. : lam[IX4(I, J, K, L)];
+                    Gb[I] += le;       /* F2new(I) = F2(I) - C(I)FB(I) + C(I-1)FB(I-1) */
+                    Pb[I] -= le;
+                    Pb[I - 1] += le;
+                }
+                if (inflow && !p->closed) Gb[2] += CC(1) * Pb[1]; /* FBND(1) = F(2) */
+                int UR = inflow ? NR : NR - 1;
+                for (int I = 2; I <= UR; ++I) {
+                    if (p->closed && I == NR) continue;
+                    int s = CC(I) < 0 ? -1 : 1;
+                    adj_face(Gb, I, I + 1, I + 1 - s, s, RC(I) & 7, -0.5 * (CC(I) - s), CC(I) * Pb[I], beta);
+                }
+                if (!inflow && !p->closed) Gb[NR] += CC(NR) * Pb[NR]; /* FBND(NR) = F(NR) */
+                int src = gsrc[IXG(J, K, L)];
+                if (src >= 0) {
+                    int jj = src % NT + 1, ll = src / (NT * NE) + 1;
+                    gfgeos[src] += g->conf1 * FNHS(NR, jj, ll) * Gb[NR + 1];
+                    if (inflow) gfgeos[src] += g->conf2 * FNHS(NR, jj, ll) * Gb[NR + 2];
+                }
+                for (int I = 1; I <= NR; ++I) lam[IX4(I, J, K, L)] = Gb[I];
+#undef CC
+#undef RC
+            }
+    free(Gb);
+    free(Pb);
+}
+
+void ro_driftp_adj(const ro_grid *g, const ro_params *p, const double *cd, const unsigned char *rec,
+                   double *lam)
+{
+    const double beta = p->betalim;
+    double *Gb = (double *)malloc(sizeof(double) * (NT + 3));
+    double *Pb = (double *)malloc(sizeof(double) * (NT + 1));
+    double *lv = (double *)malloc(sizeof(double) * (NT + 1));
+    for (int L = 1; L <= NPA; ++L)
+        for (int K = 1; K <= NE; ++K)
+            for (int I = 2; I <= NR; ++I) {
+#define CC(J) cd[IX4(I, J, K, L)]
+#define RC(J) rec[IX4(I, J, K, L)]
+                for (int J = 0; J <= NT + 2; ++J) Gb[J] = 0.;
+                for (int J = 0; J <= NT; ++J) Pb[J] = 0.;
+                for (int J = 1; J <= NT; ++J) lv[J] = lam[IX4(I, J, K, L)];
+                lv[NT] += lv[1]; /* F2(I,1) = F2new(I,NT) */
+                lv[1] = 0.;
+                for (int J = 2; J <= NT; ++J) {
+                    double le = (RC(J) & REC_CLIP) ? 0. : lv[J];
+                    Gb[J] += le;
+                    Pb[J] -= le;
+                    Pb[J - 1] += le;
+                }
+                Pb[NT] += Pb[1]; /* FBND(1) = FBND(NT), CDriftP(1) = CDriftP(NT) */
+                for (int J = 2; J <= NT; ++J) {
+                    int s = CC(J) < 0 ? -1 : 1;
+                    int J1 = (J == NT) ? 2 : J + 1;
+                    int N = J + 1 - s;
+                    if (N > NT) N = N - NT + 1;
+                    adj_face(Gb, J, J1, N, s, RC(J) & 7, -0.5 * (CC(J) - s), CC(J) * Pb[J], beta);
+                }
+                for (int J = 1; J <= NT; ++J) lam[IX4(I, J, K, L)] = Gb[J];
+#undef CC
+#undef RC
+            }
+    free(Gb);
+    free(Pb);
+    free(lv);
+}
+
+void ro_drifte_adj(const ro_grid *g, const ro_species *sp, const ro_params *p, const double *cd,
+                   const unsigned char *rec, double *lam)
+{
+    const double beta = p->betalim;
+    double *Gb = (double *)malloc(sizeof(double) * (NE + 3)); /* F(0:NE+2) */
+    double *FBb = (double *)malloc(sizeof(double) * (NE + 1));
+    const double EZERO = EKEV(1) - WE(1);
+    const double GRZERO = 1. + EZERO * 1000. * Q / sp->rmas / CS / CS;
+    /* F(1) = F(2)*k1, F(0) = F(1)*k0 (src/ModRamDrift.f90:334-335) */
+    const double k1 = GREL(1) / GREL(2) * sqrt((GREL(2) * GREL(2) - 1) / (GREL(1) * GREL(1) - 1));
+    const double k0 = GRZERO / GREL(1) * sqrt((GREL(1) * GREL(1) - 1) / (GRZERO * GRZERO - 1));
+    for (int J = 1; J <= NT; ++J)
+        for (int I = 2; I <= NR; ++I)
+            for (int L = 1; L <= NPA; ++L) {
+#define CC(K) cd[IX4(I, J, K, L)]
+#define RC(K) rec[IX4(I, J, K, L)]
+                for (int K = 0; K <= NE + 2; ++K) Gb[K] = 0.;
+                for (int K = 0; K <= NE; ++K) FBb[K] = 0.;
+                double out1 = lam[IX4(I, J, 1, L)];
+                for (int K = 2; K <= NE; ++K) {
+                    double le = (RC(K) & REC_CLIP) ? 0. : lam[IX4(I, J, K, L)];
+                    Gb[K] += le; /* F2 - C(K)/WE(K)*FB(K) + C(K-1)/WE(K)*FB(K-1) */
+                    FBb[K] -= CC(K) / WE(K) * le;
+                    FBb[K - 1] += CC(K - 1) / WE(K) * le;
+                }
+                for (int K = 1; K <= NE; ++K) {
+                    if (p->closed && (K == 1 || K == NE)) continue;
+                    int s = CC(K) < 0 ? -1 : 1;
+                    adj_face(Gb, K, K + 1, K + 1 - s, s, RC(K) & 7, -0.5 * (CC(K) / DE(K) - s), FBb[K], beta);
+                }
+                double g1 = Gb[1] + k0 * Gb[0];
+                lam[IX4(I, J, 1, L)] = out1;
+                lam[IX4(I, J, 2, L)] = Gb[2] + k1 * g1;
+                for (int K = 3; K <= NE; ++K) lam[IX4(I, J, K, L)] = Gb[K];
+#undef CC
+#undef RC
+            }
+    free(Gb);
+    free(FBb);
+}
+
+void ro_driftmu_adj(const ro_grid *g, const ro_params *p, const double *cd, const unsigned char *rec,
+                    double *lam)
+{
+    const double beta = p->betalim;
+    double *Gb = (double *)malloc(sizeof(double) * (NPA + 3));
+    double *FBb = (double *)malloc(sizeof(double) * (NPA + 1));
+    double *lv = (double *)malloc(sizeof(double) * (NPA + 1));
+    for (int K = 1; K <= NE; ++K)
+        for (int J = 1; J <= NT; ++J)
+            for (int I = 2; I <= NR; ++I) {
+#define CC(L) cd[IX4(I, J, K, L)]
+#define RC(L) rec[IX4(I, J, K, L)]
+                for (int L = 0; L <= NPA + 2; ++L) Gb[L] = 0.;
+                for (int L = 0; L <= NPA; ++L) FBb[L] = 0.;
+                for (int L = 1; L <= NPA; ++L) lv[L] = lam[IX4(I, J, K, L)];
+                /* F2(NPA) = F2new(NPA-1)*FNHS(NPA)*MU(NPA)/FNHS(NPA-1)/MU(NPA-1) */
+                double rho = 1.0 * FNHS(I, J, NPA) * MU(NPA) / FNHS(I, J, NPA - 1) / MU(NPA - 1);
+                lv[NPA - 1] += rho * lv[NPA];
+                lv[NPA] = 0.;
+                double out1 = lv[1];
+                for (int L = 2; L <= NPA - 1; ++L) {
+                    double le = (RC(L) & REC_CLIP) ? 0. : lv[L];
+                    Gb[L] += le;
+                    FBb[L] -= CC(L) / WMU(L) * le;
+                    FBb[L - 1] += CC(L - 1) / WMU(L) * le;
+                }
+                for (int L = 2; L <= NPA - 2; ++L) {
+                    int s = CC(L) < 0.0 ? -1 : 1;
+                    adj_face(Gb, L, L + 1, L + 1 - s, s, RC(L) & 7, -0.5 * (CC(L) / DMU(L) - s), FBb[L], beta);
+                }
+                if (!p->closed) Gb[NPA] += FBb[NPA - 1]; /* FBND(NPA-1) = F(NPA) */
+                Gb[2] += Gb[1];                           /* F(1) = F(2) */
+                lam[IX4(I, J, K, 1)] = out1;
+                for (int L = 2; L <= NPA; ++L) lam[IX4(I, J, K, L)] = Gb[L];
+#undef CC
+#undef RC
+            }
+    free(Gb);
+    free(FBb);
+    free(lv);
 }

@@ -136,6 +136,34 @@ void ro_half_step(const ro_grid *g, const ro_species *sp, const ro_params *p,
                   const ro_driftpara_t *dp, const double *vt, const double *fgeos,
                   const double *charge, const double *atlos, double *f2, int order);
 
+/* ---- frozen-limiter adjoint (new; the reference has no adjoint) ---------
+ * *_rec: the sweeps above, also recording per face the limiter case
+ * (0 upwind, 1 BetaLim*R, 2 one, 3 R, 4 BetaLim; bit 3: the updated cell was
+ * clipped) into rec (NR,NT,NE,NPA) and, for DRIFTR, per line the FGEOS index
+ * (NT,NE,NPA layout) that F(NR+1) came from, -1 if none, into gsrc.
+ * *_adj: transpose of that frozen line map applied to lam in place, with
+ * cd the CDrift* output of the recorded call; DRIFTR adds dJ/dFGEOS. */
+double ro_driftr_rec(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                     const ro_driftpara_t *dp, const double *vt, const double *fgeos,
+                     double *f2, double *cdrift, unsigned char *rec, int *gsrc);
+double ro_driftp_rec(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                     const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift,
+                     unsigned char *rec);
+double ro_drifte_rec(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                     const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift,
+                     unsigned char *rec);
+double ro_driftmu_rec(const ro_grid *g, const ro_species *sp, const ro_params *p,
+                      const ro_driftpara_t *dp, const double *vt, double *f2, double *cdrift,
+                      unsigned char *rec);
+void ro_driftr_adj(const ro_grid *g, const ro_params *p, const double *cd, const unsigned char *rec,
+                   const int *gsrc, double *lam, double *gfgeos);
+void ro_driftp_adj(const ro_grid *g, const ro_params *p, const double *cd, const unsigned char *rec,
+                   double *lam);
+void ro_drifte_adj(const ro_grid *g, const ro_species *sp, const ro_params *p, const double *cd,
+                   const unsigned char *rec, double *lam);
+void ro_driftmu_adj(const ro_grid *g, const ro_params *p, const double *cd, const unsigned char *rec,
+                    double *lam);
+
 #ifdef __cplusplus
 }
 #endif
