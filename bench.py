@@ -54,6 +54,12 @@ def parse():
     ap.add_argument("--members", type=int, default=256, help="ensemble members (0: skip)")
     ap.add_argument("--ensemble-steps", type=int, default=6)
     ap.add_argument("--loop-members", type=int, default=16)
+    ap.add_argument("--adj-calls", type=int, default=720,
+                    help="adjoint window in ram_run calls (720 = 1440 DTs steps = 2 h); 0: skip")
+    ap.add_argument("--adj-ckpt", type=int, default=32, help="checkpoint spacing in calls (32 = 64 steps)")
+    ap.add_argument("--adj-fd", type=int, default=2, help="finite-difference directions on the full window")
+    ap.add_argument("--adj-members", type=int, default=64, help="batched-gradient members (0: skip)")
+    ap.add_argument("--adj-member-calls", type=int, default=36)
     return ap.parse_args()
 
 
@@ -249,6 +255,188 @@ def run_ensemble(args, torch, dev, stream):
                      "looped: the plain direct-launch step of one member at a time"}
 
 
+def _truth_observations(gpu, wl, kp, obs, ncalls, species, seed):
+    """Fill log_obs from a seed-perturbed forward run sampled by the
+    virtual-spacecraft flyer; kp: (ncalls, members)."""
+    import numpy as np
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    for m in range(gpu.n_members):
+        gpu.set_member_species(m, species[m])
+        for s in species[m]:
+            gpu.upload_f2(m, s, np.asarray(wl.f2[s]) * rng.lognormal(0.0, 0.05, size=wl.f2[s].shape))
+            gpu.set_boundary(m, s, wl.fgeos[s])
+    gpu.set_graph(True)
+    bycall = {}
+    for o in obs:
+        bycall.setdefault(o["call"], []).append(o)
+    for c in range(ncalls):
+        gpu.set_kp_all(kp[c])
+        gpu.ram_run(wl.dts)
+        if c in bycall:
+            sf, _ = gpu.fly_sats([(o["member"], o["lshell"], o["mlt"]) for o in bycall[c]])
+            for t, o in enumerate(bycall[c]):
+                o["log_obs"] = math.log(sf[t, o["s"], o["k"], o["l"]])
+
+
+def run_adjoint(args, torch, dev, stream):
+    """Adjoint window on the four-species standard grid: 1440 DTs steps
+    (720 ram_run calls, Kp 1->6 ramp), 50 virtual-spacecraft samples on
+    circular equatorial orbits at L = 4-6, 10-200 keV, pitch-angle bin 2;
+    checkpoints every 64 steps.  Reports adjoint cost over the plain forward,
+    finite-difference checks on the full window, and a 64-member batched
+    gradient against looping single-member gradients."""
+    import numpy as np
+
+    from ramgpu import abi, sats, workload as W
+
+    wl = W.make_workload("four_sp")
+    g = wl.grid
+    ns = len(g.species)
+    nc, kc = args.adj_calls, args.adj_ckpt
+    kp = np.array([[wl.kp(2 * c)] for c in range(nc)])
+    obs = sats.orbit_observations(g, nc, wl.dts, 50, seed=505)
+    truth = abi.RamGpu(g, wl.fields)
+    truth.set_stream(stream.cuda_stream)
+    _truth_observations(truth, wl, kp, obs, nc, [list(range(ns))], seed=606)
+    truth.close()
+    gpu = abi.RamGpu(g, wl.fields)
+    gpu.set_stream(stream.cuda_stream)
+
+    def reset():
+        for s in range(ns):
+            gpu.upload_f2(0, s, wl.f2[s])
+            gpu.set_boundary(0, s, wl.fgeos[s])
+
+    reset()
+    gpu.autotune(wl.dts)
+    gpu.set_graph(True)
+    for c in range(2):
+        gpu.set_kp(-1, kp[c, 0])
+        gpu.ram_run(wl.dts)
+    reset()
+    torch.cuda.synchronize(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for c in range(nc):
+        gpu.set_kp(-1, kp[c, 0])
+        gpu.ram_run_async(wl.dts)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    fwd_s = a.elapsed_time(b) / 1e3
+    reset()
+    gpu.adj_forward(2, wl.dts, kp[:2], 1, [])  # warm-up of the adjoint buffers and kernels
+    gpu.adj_backward()
+    reset()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    J = gpu.adj_forward(nc, wl.dts, kp, kc, obs)[0]
+    t1 = time.perf_counter()
+    gf, gb = gpu.adj_backward()
+    t2 = time.perf_counter()
+    # finite differences along x0*(1 +- eps*r), best of two eps per direction
+    rng = np.random.Generator(np.random.PCG64(707))
+    fd = []
+    for d in range(max(0, args.adj_fd)):
+        r = [rng.uniform(-1.0, 1.0, size=wl.f2[s].shape) for s in range(ns)]
+        ad = sum(float(np.sum(gf[0, s] * np.asarray(wl.f2[s]) * r[s])) for s in range(ns))
+        errs = []
+        for eps in (1e-6, 1e-7):
+            jj = []
+            for sign in (1.0, -1.0):
+                for s in range(ns):
+                    gpu.upload_f2(0, s, np.asarray(wl.f2[s]) * (1.0 + sign * eps * r[s]))
+                jj.append(gpu.adj_forward(nc, wl.dts, kp, kc, obs)[0])
+            errs.append(abs((jj[0] - jj[1]) / (2 * eps) - ad) / abs(ad))
+        fd.append(min(errs))
+    reset()
+    gpu.close()
+    out = {"window_calls": nc, "window_dts_steps": 2 * nc, "checkpoint_calls": kc, "observations": len(obs),
+           "J": J, "forward_s": fwd_s, "adj_forward_s": t1 - t0, "adj_backward_s": t2 - t1,
+           "adjoint_over_forward": (t2 - t0) / fwd_s,
+           "fd_directions": len(fd), "fd_max_rel_err": max(fd) if fd else None,
+           "forward": "graph-replayed ram_run per call",
+           "adjoint": "recording forward with checkpoints + segment recompute + transposed sweeps"}
+    if args.adj_members > 0:
+        out["batched"] = run_adjoint_batched(args, torch, dev, stream)
+    return out
+
+
+def run_adjoint_batched(args, torch, dev, stream):
+    import numpy as np
+
+    from ramgpu import abi, sats, workload as W
+
+    ens = W.make_ensemble(args.adj_members, seed=808)
+    base = ens.base
+    g = base.grid
+    nm, nc = ens.members, args.adj_member_calls
+    kc = max(1, nc // 3)
+    kp = np.stack([ens.kp(2 * c) for c in range(nc)])
+    obs = sats.orbit_observations(g, nc, base.dts, 10 * nm, seed=909, members=nm, species=ens.species)
+    truth = abi.RamGpu(g, base.fields, n_members=nm)
+    truth.set_stream(stream.cuda_stream)
+    _truth_observations(truth, base, kp, obs, nc, ens.species, seed=910)
+    truth.close()
+    gpu = abi.RamGpu(g, base.fields, n_members=nm)
+    gpu.set_stream(stream.cuda_stream)
+
+    def reset(model, members):
+        for mi, m in enumerate(members):
+            model.set_member_species(mi, ens.species[m])
+            for s in ens.species[m]:
+                model.upload_f2(mi, s, np.asarray(base.f2[s]) * ens.scale[m])
+                model.set_boundary(mi, s, base.fgeos[s] * ens.scale[m])
+
+    reset(gpu, range(nm))
+    gpu.set_graph(True)
+    gpu.set_kp_all(kp[0])
+    gpu.ram_run(base.dts)
+    reset(gpu, range(nm))
+    torch.cuda.synchronize(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for c in range(nc):
+        gpu.set_kp_all(kp[c])
+        gpu.ram_run_async(base.dts)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    fwd_s = a.elapsed_time(b) / 1e3
+    reset(gpu, range(nm))
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    J = gpu.adj_forward(nc, base.dts, kp, kc, obs)
+    gf, gb = gpu.adj_backward()
+    batched_s = time.perf_counter() - t0
+    gpu.close()
+    # looped: the same gradients one member at a time
+    sub = list(range(0, nm, max(1, nm // 4)))[:4]
+    solo = abi.RamGpu(g, base.fields, n_members=1)
+    solo.set_stream(stream.cuda_stream)
+    loop_s, agree = [], 0.0
+    for m in sub:
+        reset(solo, [m])
+        obs_m = [dict(o, member=0) for o in obs if o["member"] == m]
+        solo.adj_forward(1, base.dts, kp[:1, m], 1, [])  # warm-up
+        solo.adj_backward()
+        reset(solo, [m])
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        Jm = solo.adj_forward(nc, base.dts, kp[:, m], kc, obs_m)
+        gfm, _ = solo.adj_backward()
+        loop_s.append(time.perf_counter() - t0)
+        for s in ens.species[m]:
+            agree = max(agree, float(np.max(np.abs(gfm[0, s] - gf[m, s])) / max(np.max(np.abs(gf[m, s])), 1e-300)))
+    solo.close()
+    looped = 1.0 / statistics.mean(loop_s)
+    return {"members": nm, "member_species": int(sum(len(x) for x in ens.species)), "window_calls": nc,
+            "checkpoint_calls": kc, "observations": len(obs), "forward_s": fwd_s, "adjoint_s": batched_s,
+            "adjoint_over_forward": batched_s / fwd_s,
+            "member_gradients_per_s_batched": nm / batched_s, "member_gradients_per_s_looped": looped,
+            "batched_over_looped": (nm / batched_s) / looped,
+            "solo_vs_batched_max_rel_diff": agree, "looped_sample_members": len(sub)}
+
+
 def run_gb300(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -365,6 +553,9 @@ def run_gb300(args, rank, world, local_rank):
     ensemble = None
     if rank == 0 and args.members > 0:
         ensemble = run_ensemble(args, torch, dev, stream)
+    adjoint = None
+    if rank == 0 and args.adj_calls > 0:
+        adjoint = run_adjoint(args, torch, dev, stream)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -391,7 +582,7 @@ def run_gb300(args, rank, world, local_rank):
         "kernels_ms": {k: round(v[0] / v[1], 5) for k, v in ktimes.items()},
         "kernel_pass_ms_per_step": statistics.mean(kt_ms),
         "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
-        "ensemble": ensemble, "wall_s": wall,
+        "ensemble": ensemble, "adjoint": adjoint, "wall_s": wall,
     }
     print(json.dumps(line), flush=True)
 

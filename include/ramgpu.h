@@ -108,7 +108,7 @@ int ramgpu_set_fields(ramgpu_ctx *ctx, const double *fnhs, const double *fnis,
                       const double *dbdt, const double *eir, const double *eip,
                       const int *outside_mgnp);
 /* GEOSB output FGEOS(S,:,:,:) of one species (src/ModRamBoundary.f90:241-319):
- * (NT,NE,NPA).  member < 0 sets it for every member. */
+ * (NT,NE,NPA), host or device memory.  member < 0 sets it for every member. */
 int ramgpu_set_boundary(ramgpu_ctx *ctx, int member, int s, const double *fgeos_s);
 /* Potential VT(NR+1,NT) for a member (the non-VOLS branch, src/ModRamRun.f90:49). */
 int ramgpu_set_potential(ramgpu_ctx *ctx, int member, const double *vt);
@@ -124,7 +124,8 @@ int ramgpu_set_member_active(ramgpu_ctx *ctx, int member, int active);
 
 /* ---- state --------------------------------------------------------------- */
 
-/* F2(S,:,:,:,:) of one species as a contiguous (NR,NT,NE,NPA) array. */
+/* F2(S,:,:,:,:) of one species as a contiguous (NR,NT,NE,NPA) array in host
+ * or device memory (unified addressing decides the copy direction). */
 int ramgpu_upload_f2(ramgpu_ctx *ctx, int member, int s, const double *f2_s);
 int ramgpu_download_f2(ramgpu_ctx *ctx, int member, int s, double *f2_s);
 /* The whole reference array F2(NS,NR,NT,NE,NPA) of one member. */
@@ -179,6 +180,36 @@ int ramgpu_cfl(ramgpu_ctx *ctx, int member, int s, double *out5);
  * and takes SETRC of the current state as the starting ENOLD.  out: 4 doubles. */
 int ramgpu_losses(ramgpu_ctx *ctx, int member, int s, double *out4);
 int ramgpu_reset_losses(ramgpu_ctx *ctx);
+
+/* Virtual spacecraft on the equatorial plane.  FLUX of the current state
+ * (src/ModRamRun.f90:208-222) sampled at (L-shell [RE], MLT [h]) for every
+ * species, energy and pitch-angle bin, the RAM-grid counterpart of the flux
+ * part of fly_sats (src/ModRamSats.f90:640-666):
+ *   SatFlux(S,E,PA): bilinear in (R, MLT) over the four FLUX cells around
+ *     the point (J = NT folded onto J = 1); BadDataFlag (-1e10,
+ *     src/ModRamSats.f90:35) unless all four are > 0, which also makes the
+ *     E = 1 and PA = 1 bins and species outside the member BadDataFlag;
+ *   OmnFlux(S,E) = sum over PA of SatFlux*4*pi*WMU(PA) for SatFlux > 0, and
+ *     BadDataFlag when that sum is not > 0.
+ * The reference interpolates flux3DEQ on the SCB mesh with GSL
+ * natural-neighbour weights; without SCB the sampling mesh is RAM's own
+ * equatorial grid.  Trajectory interpolation in time is the caller's.
+ * sat_flux: nsat*NS*NE*NPA, per satellite SatFlux(NS,NE,NPA) in Fortran
+ * order; omni_flux: nsat*NS*NE, per satellite OmnFlux(NS,NE).  Either
+ * output may be NULL (not both). */
+typedef struct {
+    int member;
+    double lshell;   /* [RE] */
+    double mlt;      /* [h] */
+} ramgpu_sat;
+int ramgpu_fly_sats(ramgpu_ctx *ctx, const ramgpu_sat *sats, int nsat, double *sat_flux,
+                    double *omni_flux);
+
+/* SCB hand-off, ram_sum_pressure (src/ModRamFunctions.f90:272-297):
+ * PAllSum(I,J) = sum_S (2/3 PPERT(S,I,J) + 1/3 PPART(S,I,J)) and
+ * PParSum(I,J) = sum_S PPART(S,I,J) over the member's species, in species
+ * order, from the moments of the last ram_run.  Outputs (NR,NT) each. */
+int ramgpu_sum_pressure(ramgpu_ctx *ctx, int member, double *pallsum, double *pparsum);
 
 /* ---- execution tuning (no reference counterpart) ------------------------ */
 
@@ -246,7 +277,8 @@ int ramgpu_adj_forward(ramgpu_ctx *ctx, int ncalls, double dts, const double *kp
  * F2(S,:,:,:,:)) and to FGEOS (grad_fgeos: n_members*ns*NT*NE*NPA), with the
  * limiter branches frozen as recorded.  Each checkpoint segment is
  * recomputed with recording and then transposed call by call.  Either
- * output may be NULL.  On return F2 is the window's initial state again. */
+ * output may be NULL; both may be host or device memory.  On return F2 is
+ * the window's initial state again. */
 int ramgpu_adj_backward(ramgpu_ctx *ctx, double *grad_f2, double *grad_fgeos);
 /* Digest of every branch recorded by the last ramgpu_adj_forward: equal
  * digests mean the same frozen-limiter pattern. */

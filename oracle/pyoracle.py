@@ -406,3 +406,52 @@ class Oracle:
                     self.sweep_adj(e, lm, dts, gfg[s], closed)
             tapes[c] = None
         return J, lam, gfg
+
+
+# ----------------------------------------------------------- output products
+BAD_DATA = -1.0E10  # BadDataFlag, src/ModRamSats.f90:35
+
+
+def sat_samples(grid, flux, sats, species_of=None):
+    """Virtual-spacecraft samples restated from fly_sats' flux block
+    (src/ModRamSats.f90:640-666) on the equatorial RAM grid: SatFlux(S,E,PA)
+    bilinear in (R, MLT) over the FLUX cells of obs_cells (BadDataFlag unless
+    all four corners are > 0) and OmnFlux(S,E) = sum_PA SatFlux*4*pi*WMU for
+    SatFlux > 0 (BadDataFlag if not > 0).  flux: {s: FLUX (NR,NT,NE,NPA)};
+    sats: [(member, lshell, mlt)]; species_of: {member: species list}."""
+    ns, ne, npa = len(grid.species), grid.ne, grid.npa
+    wmu = np.asarray(grid.wmu)
+    sf = np.full((len(sats), ns, ne, npa), BAD_DATA)
+    om = np.full((len(sats), ns, ne), BAD_DATA)
+    for t, (m, lsh, mlt) in enumerate(sats):
+        cells = obs_cells(grid, {"lshell": lsh, "mlt": mlt})
+        for s in range(ns):
+            if species_of is not None and s not in species_of[m]:
+                continue
+            acc = np.zeros((ne, npa))
+            pos = np.ones((ne, npa), dtype=bool)
+            for i, j, w in cells:
+                fl = np.asarray(flux[s])[i, j]
+                pos &= fl > 0.0
+                acc = acc + w * fl
+            v = np.where(pos, acc, BAD_DATA)
+            v[0, :] = BAD_DATA
+            v[:, 0] = BAD_DATA
+            sf[t, s] = v
+            o = np.zeros(ne)
+            for l in range(npa):
+                o = np.where(v[:, l] > 0.0, o + v[:, l] * 4.0 * math.pi * wmu[l], o)
+            om[t, s] = np.where(o > 0.0, o, BAD_DATA)
+    return sf, om
+
+
+def sum_pressure(ppert, ppart, species):
+    """ram_sum_pressure (src/ModRamFunctions.f90:272-297) over `species`:
+    PAllSum = sum_S 2/3 PPERT + 1/3 PPART, PParSum = sum_S PPART."""
+    onethird, twothird = 1.0 / 3.0, 2.0 / 3.0
+    pall = np.zeros_like(ppert[species[0]])
+    ppar = np.zeros_like(ppart[species[0]])
+    for s in species:
+        pall = pall + twothird * ppert[s] + onethird * ppart[s]
+        ppar = ppar + ppart[s]
+    return pall, ppar

@@ -638,7 +638,7 @@ int ramgpu_set_boundary(ramgpu_ctx* ctx, int member, int s, const double* fgeos_
   for (int m = m0; m < m1; ++m) {
     if (int rc = check_ms(ctx, m, s)) return rc;
     CK(cudaMemcpy(ctx->d.fgeos + (size_t)(m * ctx->d.ns + s) * n, fgeos_s, n * sizeof(double),
-                  cudaMemcpyHostToDevice));
+                  cudaMemcpyDefault));
   }
   return RAMGPU_OK;
 }
@@ -709,7 +709,7 @@ int ramgpu_upload_f2(ramgpu_ctx* ctx, int member, int s, const double* f2_s) {
   if (int rc = check_ms(ctx, member, s)) return rc;
   const size_t n = ctx->d.ncell;
   CK(cudaMemcpyAsync(ctx->d.f2 + (size_t)(member * ctx->d.ns + s) * n, f2_s, n * sizeof(double),
-                     cudaMemcpyHostToDevice, ctx->stream));
+                     cudaMemcpyDefault, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return RAMGPU_OK;
 }
@@ -719,7 +719,7 @@ int ramgpu_download_f2(ramgpu_ctx* ctx, int member, int s, double* f2_s) {
   if (int rc = check_ms(ctx, member, s)) return rc;
   const size_t n = ctx->d.ncell;
   CK(cudaMemcpyAsync(f2_s, ctx->d.f2 + (size_t)(member * ctx->d.ns + s) * n, n * sizeof(double),
-                     cudaMemcpyDeviceToHost, ctx->stream));
+                     cudaMemcpyDefault, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return RAMGPU_OK;
 }
@@ -828,8 +828,6 @@ int ramgpu_flux(ramgpu_ctx* ctx, int member, int s, double* flux_s) {
   if (int rc = check_ms(ctx, member, s)) return rc;
   if (!ctx->have_grid || !ctx->have_fields) return fail(ctx, RAMGPU_ERR_STATE, "grid/fields not set");
   const size_t n = ctx->d.ncell;
-  // The moment-partial buffer of this slot is reused as staging only when
-  // large enough; otherwise a temporary device buffer is used.
   double* tmp = nullptr;
   CK(cudaMalloc(&tmp, n * sizeof(double)));
   launch_flux(ctx->d, member * ctx->d.ns + s, s, tmp, ctx->stream);
@@ -1036,6 +1034,100 @@ int ramgpu_autotune(ramgpu_ctx* ctx, double dts, int reps, double* best_ms4) {
   return RAMGPU_OK;
 }
 
+// Bit s set when species s belongs to the member (retired members keep
+// their last state and are still sampled).
+static unsigned species_mask(const ramgpu_ctx* ctx, int member) {
+  unsigned m = 0u;
+  for (int s : ctx->member_species[member]) m |= 1u << s;
+  return m;
+}
+
+// Bilinear stencil of an equatorial point (L-shell [RE], MLT [h]) on the
+// FLUX grid: corners I = i0, i0+1 (0-based, I >= 2 where FLUX is defined)
+// and J = j0, j1 with J = NT folded onto J = 1; weights of the upper
+// corners clamped to [0,1] (points beyond the grid take the edge value).
+static void equatorial_stencil(const Dev& d, const std::vector<double>& lz, const std::vector<double>& phi,
+                               double lshell, double mlt, int* i0o, double* wi, int* j0o, int* j1o,
+                               double* wj) {
+  int i0 = 1;
+  while (i0 + 1 < d.nr - 1 && lz[i0 + 1] <= lshell) ++i0;
+  *i0o = i0;
+  *wi = fmin(1.0, fmax(0.0, (lshell - lz[i0]) / (lz[i0 + 1] - lz[i0])));
+  const double twopi = 2.0 * kPI;
+  double ph = fmod(mlt * kPI / 12.0, twopi);
+  if (ph < 0) ph += twopi;
+  int j0 = (int)(ph / d.dphi);
+  if (j0 > d.nt - 2) j0 = d.nt - 2;
+  *j0o = j0;
+  *j1o = (j0 + 1 == d.nt - 1) ? 0 : j0 + 1;
+  *wj = fmin(1.0, fmax(0.0, (ph - phi[j0]) / d.dphi));
+}
+
+int ramgpu_fly_sats(ramgpu_ctx* ctx, const ramgpu_sat* sats, int nsat, double* sat_flux, double* omni_flux) {
+  if (check_ctx(ctx) || (nsat > 0 && !sats) || (!sat_flux && !omni_flux))
+    return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (nsat < 0) return fail(ctx, RAMGPU_ERR_ARG, "nsat >= 0");
+  if (!ctx->have_grid || !ctx->have_fields) return fail(ctx, RAMGPU_ERR_STATE, "grid/fields not set");
+  if (nsat == 0) return RAMGPU_OK;
+  Dev& d = ctx->d;
+  if (d.ns > 32) return fail(ctx, RAMGPU_ERR_ARG, "fly_sats supports ns <= 32");
+  std::vector<double> lz(d.nf), phi(d.nt);
+  CK(cudaMemcpy(lz.data(), d.lz, sizeof(double) * d.nf, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(phi.data(), d.phi, sizeof(double) * d.nt, cudaMemcpyDeviceToHost));
+  std::vector<SatDev> sh(nsat);
+  for (int t = 0; t < nsat; ++t) {
+    const ramgpu_sat& o = sats[t];
+    if (o.member < 0 || o.member >= ctx->cfg.n_members || !isfinite(o.lshell) || !isfinite(o.mlt))
+      return fail(ctx, RAMGPU_ERR_ARG, "satellite member or position out of range");
+    SatDev& q = sh[t];
+    q.member = o.member;
+    q.active_mask = 0u;
+    q.active_mask = species_mask(ctx, o.member);
+    equatorial_stencil(d, lz, phi, o.lshell, o.mlt, &q.i0, &q.wi, &q.j0, &q.j1, &q.wj);
+  }
+  const size_t nfl = (size_t)nsat * d.ns * d.ne * d.npa, nom = (size_t)nsat * d.ns * d.ne;
+  void* buf = nullptr;
+  const size_t bytes = sizeof(SatDev) * nsat + sizeof(double) * (nfl + nom);
+  CK(cudaMalloc(&buf, bytes));
+  SatDev* qd = (SatDev*)buf;
+  double* fl = (double*)((char*)buf + sizeof(SatDev) * nsat);
+  double* om = fl + nfl;
+  cudaError_t e = cudaMemcpyAsync(qd, sh.data(), sizeof(SatDev) * nsat, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) {
+    launch_fly_sats(d, qd, nsat, fl, om, ctx->stream);
+    ctx->launches += 1;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && sat_flux)
+    e = cudaMemcpyAsync(sat_flux, fl, sizeof(double) * nfl, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess && omni_flux)
+    e = cudaMemcpyAsync(omni_flux, om, sizeof(double) * nom, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "fly_sats");
+  return RAMGPU_OK;
+}
+
+int ramgpu_sum_pressure(ramgpu_ctx* ctx, int member, double* pallsum, double* pparsum) {
+  if (check_ctx(ctx) || !pallsum || !pparsum) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, RAMGPU_ERR_ARG, "member out of range");
+  Dev& d = ctx->d;
+  if (d.ns > 32) return fail(ctx, RAMGPU_ERR_ARG, "sum_pressure supports ns <= 32");
+  const unsigned mask = species_mask(ctx, member);
+  const size_t n = (size_t)d.nr * d.nt;
+  double* buf = nullptr;
+  CK(cudaMalloc(&buf, 2 * n * sizeof(double)));
+  launch_sum_pressure(d, member, mask, buf, buf + n, ctx->stream);
+  ctx->launches += 1;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(pallsum, buf, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(pparsum, buf + n, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "sum_pressure");
+  return RAMGPU_OK;
+}
+
 int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp, int k_ckpt,
                        const ramgpu_obs* obs, int nobs, double* J) {
   if (check_ctx(ctx) || !kp || (nobs > 0 && !obs)) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
@@ -1068,18 +1160,7 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
     ObsDev& q = oh[t];
     q.member = o.member; q.slot = o.member * d.ns + o.s; q.call = o.call; q.k = o.k; q.l = o.l;
     q.log_obs = o.log_obs;
-    int i0 = 1;  // I >= 2 (FLUX is defined for I >= 2)
-    while (i0 + 1 < d.nr - 1 && lz[i0 + 1] <= o.lshell) ++i0;
-    q.i0 = i0;
-    q.wi = fmin(1.0, fmax(0.0, (o.lshell - lz[i0]) / (lz[i0 + 1] - lz[i0])));
-    const double twopi = 2.0 * kPI;
-    double ph = fmod(o.mlt * kPI / 12.0, twopi);
-    if (ph < 0) ph += twopi;
-    int j0 = (int)(ph / d.dphi);
-    if (j0 > d.nt - 2) j0 = d.nt - 2;
-    q.j0 = j0;
-    q.j1 = (j0 + 1 == d.nt - 1) ? 0 : j0 + 1;  // J = NT is J = 1
-    q.wj = fmin(1.0, fmax(0.0, (ph - phi[j0]) / d.dphi));
+    equatorial_stencil(d, lz, phi, o.lshell, o.mlt, &q.i0, &q.wi, &q.j0, &q.j1, &q.wj);
   }
   adj_free(ctx);
   auto& a = ctx->adj;
@@ -1165,8 +1246,8 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
   }
   if ((rc = adj_copy_items(ctx, a.ckpt, false))) return rc;  // F2 back to the initial state
   CK(cudaStreamSynchronize(ctx->stream));
-  if (grad_f2) CK(cudaMemcpy(grad_f2, d.lam, sizeof(double) * nslot * d.ncell, cudaMemcpyDeviceToHost));
-  if (grad_fgeos) CK(cudaMemcpy(grad_fgeos, d.gfg, sizeof(double) * nslot * nfg, cudaMemcpyDeviceToHost));
+  if (grad_f2) CK(cudaMemcpy(grad_f2, d.lam, sizeof(double) * nslot * d.ncell, cudaMemcpyDefault));
+  if (grad_fgeos) CK(cudaMemcpy(grad_fgeos, d.gfg, sizeof(double) * nslot * nfg, cudaMemcpyDefault));
   return RAMGPU_OK;
 }
 

@@ -83,4 +83,16 @@ void launch_obs_adj(const Dev& d, const ObsDev* obs, int nobs, int call, const d
                     cudaStream_t st);
 void launch_digest(const unsigned char* rec, long long n, unsigned long long* out, cudaStream_t st);
 
+// virtual spacecraft and SCB hand-off (outputs.cu)
+struct SatDev {
+  int member;
+  unsigned active_mask;  // bit s: (member, s) is active
+  int i0, j0, j1;        // bilinear stencil, as ObsDev
+  double wi, wj;
+};
+void launch_fly_sats(const Dev& d, const SatDev* sats, int nsat, double* sat_flux, double* omni,
+                     cudaStream_t st);
+void launch_sum_pressure(const Dev& d, int member, unsigned mask, double* pall, double* ppar,
+                         cudaStream_t st);
+
 }  // namespace ramgpu

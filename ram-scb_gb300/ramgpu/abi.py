@@ -34,7 +34,9 @@ EXPORTS = (
     "ramgpu_sumrc_noalloc", "ramgpu_set_graph", "ramgpu_set_launch_shape",
     "ramgpu_get_launch_shape", "ramgpu_autotune", "ramgpu_set_kp_all",
     "ramgpu_adj_forward", "ramgpu_adj_backward", "ramgpu_adj_digest", "ramgpu_adj_record",
+    "ramgpu_fly_sats", "ramgpu_sum_pressure",
 )
+BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
           "anisch", "dts_tables", "sumrc")
 OP_DRIFTR, OP_DRIFTP, OP_DRIFTE, OP_DRIFTMU, OP_CHAREXCHANGE, OP_ATMOL, OP_ANISCH = range(7)
@@ -64,6 +66,10 @@ class GridStruct(C.Structure):
 class ObsStruct(C.Structure):
     _fields_ = [("member", C.c_int), ("s", C.c_int), ("call", C.c_int), ("k", C.c_int),
                 ("l", C.c_int), ("lshell", C.c_double), ("mlt", C.c_double), ("log_obs", C.c_double)]
+
+
+class SatStruct(C.Structure):
+    _fields_ = [("member", C.c_int), ("lshell", C.c_double), ("mlt", C.c_double)]
 
 
 _lib = None
@@ -126,6 +132,8 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_adj_backward": ([vp, dp, dp], i),
         "ramgpu_adj_digest": ([vp, C.POINTER(C.c_ulonglong)], i),
         "ramgpu_adj_record": ([vp, i, C.POINTER(C.c_ubyte)], i),
+        "ramgpu_fly_sats": ([vp, C.POINTER(SatStruct), i, dp, dp], i),
+        "ramgpu_sum_pressure": ([vp, i, dp, dp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -166,6 +174,7 @@ class RamGpu:
         self.grid = grid
         self.ns = len(grid.species)
         self.n_members = n_members
+        self.member_species = [list(range(self.ns)) for _ in range(n_members)]
         cfg = Config(grid.nr, grid.nt, grid.ne, grid.npa, self.ns, n_members, betalim, fraccfl,
                      dtsmin, flags)
         h = C.c_void_p()
@@ -244,6 +253,7 @@ class RamGpu:
         self._ck(self.lib.ramgpu_set_member_species(self.h, member, a.size,
                                                     a.ctypes.data_as(C.POINTER(C.c_int))),
                  "set_member_species")
+        self.member_species[member] = sorted(int(x) for x in a)
 
     def set_member_active(self, member: int, active: bool):
         self._ck(self.lib.ramgpu_set_member_active(self.h, member, int(bool(active))), "set_member_active")
@@ -291,6 +301,27 @@ class RamGpu:
         a = np.empty((g.nr, g.nt, g.ne, g.npa), order="F")
         self._ck(self.lib.ramgpu_flux(self.h, member, s, _dptr(a)), "flux")
         return a
+
+    def fly_sats(self, sats):
+        """Virtual-spacecraft samples of the current state.  sats: iterable of
+        (member, lshell [RE], mlt [h]).  Returns (SatFlux, OmnFlux) with shapes
+        (nsat, NS, NE, NPA) and (nsat, NS, NE); BadDataFlag where undefined."""
+        g = self.grid
+        sats = list(sats)
+        arr = (SatStruct * max(1, len(sats)))(*[SatStruct(int(m), float(lv), float(t)) for m, lv, t in sats])
+        fl = np.zeros(len(sats) * self.ns * g.ne * g.npa)
+        om = np.zeros(len(sats) * self.ns * g.ne)
+        self._ck(self.lib.ramgpu_fly_sats(self.h, arr, len(sats), _dptr(fl), _dptr(om)), "fly_sats")
+        return (fl.reshape(len(sats), g.npa, g.ne, self.ns).transpose(0, 3, 2, 1),
+                om.reshape(len(sats), g.ne, self.ns).transpose(0, 2, 1))
+
+    def sum_pressure(self, member: int = 0):
+        """(PAllSum, PParSum), each (NR, NT), from the moments of the last ram_run."""
+        g = self.grid
+        pa = np.empty((g.nr, g.nt), order="F")
+        pp = np.empty((g.nr, g.nt), order="F")
+        self._ck(self.lib.ramgpu_sum_pressure(self.h, int(member), _dptr(pa), _dptr(pp)), "sum_pressure")
+        return pa, pp
 
     def cfl(self, member: int, s: int) -> np.ndarray:
         a = np.empty(5)

@@ -241,3 +241,30 @@ def test_gradient_matches_cpu_adjoint():
         eb = np.max(np.abs(gb[0, s] - cb[s])) / max(np.max(np.abs(cb[s])), 1e-300)
         print(f"species {s}: dJ/dF2 {ef:.2e}  dJ/dFGEOS {eb:.2e}  record mismatches {mism}")
         assert ef <= 1e-9 and eb <= 1e-9, (s, ef, eb)
+
+
+def test_autograd_function_matches_c_abi(tiny):
+    """The torch.autograd.Function wrapper: same J as ramgpu_adj_forward, and
+    backward() delivers the C-ABI gradients scaled by the upstream weights."""
+    import torch
+
+    from ramgpu import autograd as A
+
+    model, kp, obs = make_case(tiny, 2, 3, 20, seed=31)
+    try:
+        J = model.adj_forward(3, tiny.dts, kp, 2, obs)
+        gf, gb = model.adj_backward()
+        f2, fg = A.device_state(model, tiny.f2, tiny.fgeos, "cuda")
+        Jt = A.window_misfit(model, f2, fg, 3, tiny.dts, kp, 2, obs)
+        assert np.allclose(Jt.cpu().numpy(), J, rtol=1e-13, atol=0)
+        w = torch.tensor([1.0, -2.5], dtype=torch.float64, device="cuda")
+        (Jt * w).sum().backward()
+        gt, gbt = f2.grad.cpu().numpy(), fg.grad.cpu().numpy()
+        for m, wm in enumerate((1.0, -2.5)):
+            for s in range(len(tiny.grid.species)):
+                ref = wm * gf[m, s]
+                assert np.max(np.abs(gt[m, s].transpose(3, 2, 1, 0) - ref)) <= 1e-13 * np.max(np.abs(ref))
+                refb = wm * gb[m, s]
+                assert np.max(np.abs(gbt[m, s].transpose(2, 1, 0) - refb)) <= 1e-13 * max(np.max(np.abs(refb)), 1e-300)
+    finally:
+        model.close()
