@@ -131,14 +131,25 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU legs
-def cpu_time_oracle(wl, seconds, nthreads):
+def cpu_threads(ns):
+    """(species threads, line threads per species) using every host core:
+    the reference's OpenMP loop over species, each species' independent
+    lines threaded inside it."""
+    cores = os.cpu_count() or 1
+    outer = max(1, min(ns, cores))
+    return outer, max(1, cores // outer)
+
+
+def cpu_time_oracle(wl, seconds, nthreads, inner=1):
     """Time the CPU oracle (the reference's routines restated in C, species
-    loop under OpenMP like the reference) on this workload; returns
-    (cell-updates/s, steps, elapsed)."""
+    loop under OpenMP like the reference, `inner` threads over independent
+    lines inside each routine) on this workload; returns (cell-updates/s,
+    calls, elapsed)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import numpy as np
     import pyoracle
 
+    pyoracle.set_inner_threads(inner)
     o = pyoracle.Oracle(wl.grid, wl.fields)
     f2 = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
     cells = 2 * wl.grid.ncell * len(wl.grid.species)
@@ -150,6 +161,7 @@ def cpu_time_oracle(wl, seconds, nthreads):
         el = time.perf_counter() - t0
         if el >= seconds or n >= 1000:
             break
+    pyoracle.set_inner_threads(1)
     return cells * n / el, n, el
 
 
@@ -160,16 +172,18 @@ def run_reference(args, rank, world):
         return
     wl = W.make_workload(args.workload)
     ns = len(wl.grid.species)
-    threads = min(ns, os.cpu_count() or 1)
+    outer, inner = cpu_threads(ns)
     budget = max(5.0, min(60.0, 0.4 * max(args.steps, 1)))
-    v, n, el = cpu_time_oracle(wl, budget, threads)
+    v, n, el = cpu_time_oracle(wl, budget, outer, inner)
     sample = (f"{n} ram_run calls of the workload ({workload_desc(wl)}), {el:.1f} s; "
-              f"C restatement of the reference routines (no Fortran compiler), OpenMP over species")
+              f"C restatement of the reference routines (no Fortran compiler), OpenMP over "
+              f"{outer} species x {inner} line threads")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": n, "warmup": 1, "ms_per_step": 1e3 * el / n, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": workload_desc(wl), "step": "one ram_run call (2 DTs steps)"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": outer * inner, "kind": "port",
+                             "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -334,6 +348,15 @@ def run_adjoint(args, torch, dev, stream):
     t1 = time.perf_counter()
     gf, gb = gpu.adj_backward()
     t2 = time.perf_counter()
+    # the same window with every call's record kept (one segment: no recompute)
+    reset()
+    torch.cuda.synchronize(dev)
+    t3 = time.perf_counter()
+    gpu.adj_forward(nc, wl.dts, kp, nc, obs)
+    t4 = time.perf_counter()
+    gpu.adj_backward()
+    t5 = time.perf_counter()
+    reset()
     # finite differences along x0*(1 +- eps*r), best of two eps per direction
     rng = np.random.Generator(np.random.PCG64(707))
     fd = []
@@ -354,6 +377,9 @@ def run_adjoint(args, torch, dev, stream):
     out = {"window_calls": nc, "window_dts_steps": 2 * nc, "checkpoint_calls": kc, "observations": len(obs),
            "J": J, "forward_s": fwd_s, "adj_forward_s": t1 - t0, "adj_backward_s": t2 - t1,
            "adjoint_over_forward": (t2 - t0) / fwd_s,
+           "full_record": {"adj_forward_s": t4 - t3, "adj_backward_s": t5 - t4,
+                           "adjoint_over_forward": (t5 - t3) / fwd_s,
+                           "record_bytes": 8 * g.ncell * ns * nc},
            "fd_directions": len(fd), "fd_max_rel_err": max(fd) if fd else None,
            "forward": "graph-replayed ram_run per call",
            "adjoint": "recording forward with checkpoints + segment recompute + transposed sweeps"}
@@ -559,10 +585,12 @@ def run_gb300(args, rank, world, local_rank):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, n, el = cpu_time_oracle(wl, args.cpu_seconds, min(ns, os.cpu_count() or 1))
-        cpu = {"value": v, "unit": UNIT, "cores": min(ns, os.cpu_count() or 1), "kind": "port",
+        outer, inner = cpu_threads(ns)
+        v, n, el = cpu_time_oracle(wl, args.cpu_seconds, outer, inner)
+        cpu = {"value": v, "unit": UNIT, "cores": outer * inner, "kind": "port",
                "sample": f"{n} ram_run calls of the same workload in {el:.1f} s (C restatement of the "
-                         f"reference routines, OpenMP over species as the reference)"}
+                         f"reference routines; OpenMP over {outer} species as the reference, "
+                         f"{inner} threads over independent lines inside each routine)"}
     if rank != 0:
         return
     line = {

@@ -275,8 +275,10 @@ int ramgpu_adj_forward(ramgpu_ctx *ctx, int ncalls, double dts, const double *kp
 /* Backward pass: gradients of J with respect to the window's initial F2
  * (grad_f2: n_members*ns*NR*NT*NE*NPA, per (member, s) the Fortran-order
  * F2(S,:,:,:,:)) and to FGEOS (grad_fgeos: n_members*ns*NT*NE*NPA), with the
- * limiter branches frozen as recorded.  Each checkpoint segment is
- * recomputed with recording and then transposed call by call.  Either
+ * limiter branches frozen as recorded.  Each checkpoint segment but the
+ * last (whose record the forward pass kept) is recomputed from its
+ * checkpoint with recording, then transposed call by call; with k_ckpt >=
+ * ncalls nothing is recomputed.  Either
  * output may be NULL; both may be host or device memory.  On return F2 is
  * the window's initial state again. */
 int ramgpu_adj_backward(ramgpu_ctx *ctx, double *grad_f2, double *grad_fgeos);
@@ -287,7 +289,8 @@ int ramgpu_adj_digest(ramgpu_ctx *ctx, unsigned long long *digest);
  * the last ramgpu_adj_forward: 8 sweeps (R,P,E,MU,MU,E,P,R) x active items x
  * NR*NT*NE*NPA bytes, per face the limiter case (bits 0-2: 0 upwind only,
  * 1 beta*D, 2 X, 3 D, 4 beta*X) and bit 3 set when the updated cell was
- * clipped (diagnostics). */
+ * clipped (diagnostics).  Available until a ramgpu_adj_backward that had to
+ * recompute earlier segments (more than one segment) replaces it. */
 int ramgpu_adj_record(ramgpu_ctx *ctx, int call, unsigned char *out);
 
 /* ---- no-allocation variant --------------------------------------------- */

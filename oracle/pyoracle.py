@@ -72,6 +72,7 @@ def load():
         lib = C.CDLL(str(LIB_PATH))
         gp, sp, pp = C.POINTER(RoGrid), C.POINTER(RoSpecies), C.POINTER(RoParams)
         dpp = C.POINTER(RoDriftPara)
+        lib.ro_set_inner_threads.argtypes = [C.c_int]
         lib.ro_vt_vols.argtypes = [gp, C.c_double, _P]
         lib.ro_driftpara.argtypes = [gp, sp, pp, dpp]
         lib.ro_driftr.argtypes = [gp, sp, pp, dpp, _P, _P, _P, _P]
@@ -104,6 +105,11 @@ def load():
         lib.ro_driftmu_adj.argtypes = [gp, pp, _P, U8, _P]
         _lib = lib
     return _lib
+
+
+def set_inner_threads(n: int):
+    """Threads for the independent-line loops inside each oracle routine."""
+    load().ro_set_inner_threads(int(n))
 
 
 def _f(a, dtype=np.float64):

@@ -88,6 +88,11 @@ static const double PI = 3.1415926535897932384626433832795;
 #define EDOT(I, K) dp->edot[IXRK(I, K)]
 #define MUDOT(I, L) dp->mudot[IXRL(I, L)]
 
+/* Threads for the loops over independent lines inside one routine (the
+ * reference runs them serially; the results do not depend on this). */
+static int g_inner = 1;
+void ro_set_inner_threads(int n) { g_inner = n < 1 ? 1 : n; }
+
 static inline double dmax(double a, double b) { return a > b ? a : b; }
 static inline double dmin(double a, double b) { return a < b ? a : b; }
 /* Fortran MAX/MIN for the limiter: MAX(MIN(B*R,1.),MIN(R,B)) */
@@ -160,23 +165,36 @@ double ro_driftr_rec(const ro_grid *g, const ro_species *sp, const ro_params *p,
     return driftr_impl(g, sp, p, dp, vt, fgeos, f2, cdrift, rec, gsrc);
 }
 
+/* CGR of DRIFTR (src/ModRamDrift.f90:139-144) for face I of line (J,K,L). */
+static double driftr_cgr(const ro_grid *g, double P4, double MDR, int I, int J, int J0, int J1, int L)
+{
+    double CGR1 = FNIS(I + 1, J1, L) + FNIS(I, J1, L) - FNIS(I + 1, J0, L) - FNIS(I, J0, L);
+    double CGR2 = BNES(I + 1, J1) + BNES(I, J1) - BNES(I + 1, J0) - BNES(I, J0);
+    double CGR3 = CGR1 + (FNIS(I + 1, J, L) + FNIS(I, J, L) - 2 * FNHS(I + 1, J, L)
+                          - 2 * FNHS(I, J, L)) * CGR2 / 2. / (BNES(I + 1, J) + BNES(I, J));
+    return CGR3 / (FNHS(I, J, L) + FNHS(I + 1, J, L)) * P4 / 2.
+           / (BNES(I, J) + BNES(I + 1, J)) / (RLZ(I) + 0.5 * MDR);
+}
+
+static double driftr_p4(const ro_grid *g, const ro_species *sp, double DTs, double DPHI, double MDR,
+                        int QS, int K)
+{
+    return DTs * EKEV(K) * 1000.0 * (GREL(K) + 1) / GREL(K) / DPHI / MDR / QS;
+}
+
 static double driftr_impl(const ro_grid *g, const ro_species *sp, const ro_params *p,
                           const ro_driftpara_t *dp, const double *vt, const double *fgeos,
                           double *f2, double *cdrift, unsigned char *rec, int *gsrc)
 {
-    int last_src = -1; /* line whose F(NR+1) is currently held, -1: none or 0 outside */
     const double DTs = p->dts, MDR = g->mdr, DPHI = g->dphi, BetaLim = p->betalim;
     const int QS = sp->qs;
     double DtDriftR = 100000.0;
-    int *sgn = (int *)malloc(sizeof(int) * NR * NT);
     double *CR = (double *)calloc((size_t)NR * NT, sizeof(double));
-    double *F = (double *)calloc((size_t)NR + 2, sizeof(double)); /* F(1:NR+2) -> F[0..NR+1] */
-    double *FBND = (double *)calloc((size_t)NR, sizeof(double));
-    double *CD = (double *)malloc(sizeof(double) * NR); /* CDriftR(:,J,K,L) of the current line */
-#define FF(n) F[(n)-1]
-#define FB(n) FBND[(n)-1]
-#define SG(i, j) sgn[IXM(i, j)]
-    for (int i = 0; i < NR * NT; ++i) sgn[i] = 1;
+    /* FGEOS index of the line whose ghost F(NR+1:NR+2) is held when plane
+     * (K,L) starts, in the reference's K->L->J line order; -1: none yet, or
+     * the last inflow line was outside the magnetopause (ghost 0).  Lines
+     * are otherwise independent, so planes may run in parallel. */
+    int *plane_src = (int *)malloc(sizeof(int) * (size_t)NE * NPA);
 
     for (int I = 1; I <= NR; ++I)
         for (int J = 1; J <= NT; ++J) {
@@ -188,94 +206,130 @@ static double driftr_impl(const ro_grid *g, const ro_species *sp, const ro_param
             CR[IXM(I, J)] = VR(I) * (VT(I, J0) + VT(I + 1, J0) - VT(I, J1) - VT(I + 1, J1)) / den
                           + (EIP(I, J) + EIP(I + 1, J)) / den * DTs / MDR;
         }
+    {
+        int src = -1;
+        for (int K = 1; K <= NE; ++K) {
+            double P4 = driftr_p4(g, sp, DTs, DPHI, MDR, QS, K);
+            for (int L = 1; L <= NPA; ++L) {
+                plane_src[(size_t)(L - 1) * NE + (K - 1)] = src;
+                for (int J = 1; J <= NT; ++J) {
+                    int J0 = J - 1;
+                    if (J == 1) J0 = NT - 1;
+                    int J1 = J + 1;
+                    if (J == NT) J1 = 2;
+                    double cnr = CR[IXM(NR, J)] + driftr_cgr(g, P4, MDR, NR, J, J0, J1, L);
+                    if (cnr < 0) src = (OUTSIDE(NR, J) == 1) ? -1 : (int)IXG(J, K, L);
+                }
+            }
+        }
+    }
 
-    for (int K = 1; K <= NE; ++K) {
-        double P4 = DTs * EKEV(K) * 1000.0 * (GREL(K) + 1) / GREL(K) / DPHI / MDR / QS;
-        for (int L = 1; L <= NPA; ++L)
-            for (int J = 1; J <= NT; ++J) {
-                for (int I = 1; I <= NR; ++I) FF(I) = F2(I, J, K, L);
-                int J0 = J - 1;
-                if (J == 1) J0 = NT - 1;
-                int J1 = J + 1;
-                if (J == NT) J1 = 2;
-                for (int I = 1; I <= NR; ++I) {
-                    double CGR1 = FNIS(I + 1, J1, L) + FNIS(I, J1, L) - FNIS(I + 1, J0, L) - FNIS(I, J0, L);
-                    double CGR2 = BNES(I + 1, J1) + BNES(I, J1) - BNES(I + 1, J0) - BNES(I, J0);
-                    double CGR3 = CGR1 + (FNIS(I + 1, J, L) + FNIS(I, J, L) - 2 * FNHS(I + 1, J, L)
-                                          - 2 * FNHS(I, J, L)) * CGR2 / 2. / (BNES(I + 1, J) + BNES(I, J));
-                    double CGR = CGR3 / (FNHS(I, J, L) + FNHS(I + 1, J, L)) * P4 / 2.
-                                 / (BNES(I, J) + BNES(I + 1, J)) / (RLZ(I) + 0.5 * MDR);
-                    CD[I - 1] = CR[IXM(I, J)] + CGR;
-                    if (OUTSIDE(I, J) == 0) {
-                        double ctemp = dmax(fabs(CD[I - 1]), 1E-10);
-                        DtDriftR = dmin(DtDriftR, p->fraccfl * DTs / ctemp);
-                    }
-                    SG(I, J) = 1;
-                    if (CD[I - 1] < 0) SG(I, J) = -1;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_inner) reduction(min : DtDriftR)
+#endif
+    {
+        int *sgn = (int *)malloc(sizeof(int) * NR * NT);
+        double *F = (double *)calloc((size_t)NR + 2, sizeof(double)); /* F(1:NR+2) -> F[0..NR+1] */
+        double *FBND = (double *)calloc((size_t)NR, sizeof(double));
+        double *CD = (double *)malloc(sizeof(double) * NR); /* CDriftR(:,J,K,L) of the current line */
+#define FF(n) F[(n)-1]
+#define FB(n) FBND[(n)-1]
+#define SG(i, j) sgn[IXM(i, j)]
+        for (int i = 0; i < NR * NT; ++i) sgn[i] = 1;
+#ifdef _OPENMP
+#pragma omp for collapse(2) schedule(static)
+#endif
+        for (int K = 1; K <= NE; ++K)
+            for (int L = 1; L <= NPA; ++L) {
+                double P4 = driftr_p4(g, sp, DTs, DPHI, MDR, QS, K);
+                int last_src = plane_src[(size_t)(L - 1) * NE + (K - 1)];
+                FF(NR + 1) = 0.;
+                FF(NR + 2) = 0.;
+                if (last_src >= 0) {
+                    int jj = last_src % NT + 1, ll = last_src / (NT * NE) + 1;
+                    FF(NR + 1) = fgeos[last_src] * g->conf1 * FNHS(NR, jj, ll);
+                    FF(NR + 2) = fgeos[last_src] * g->conf2 * FNHS(NR, jj, ll);
                 }
-                int UR;
-                if (rec)
-                    for (int I = 1; I <= NR; ++I) rec[IX4(I, J, K, L)] = 0;
-                if (SG(NR, J) == 1) {
-                    FB(1) = 0.;
-                    FB(NR) = FF(NR);
-                    UR = NR - 1;
-                } else {
-                    FB(1) = FF(2);
-                    UR = NR;
-                    if (OUTSIDE(NR, J) == 1) {
-                        FF(NR + 1) = 0.;
-                        FF(NR + 2) = 0.;
-                        last_src = -1;
+                for (int J = 1; J <= NT; ++J) {
+                    for (int I = 1; I <= NR; ++I) FF(I) = F2(I, J, K, L);
+                    int J0 = J - 1;
+                    if (J == 1) J0 = NT - 1;
+                    int J1 = J + 1;
+                    if (J == NT) J1 = 2;
+                    for (int I = 1; I <= NR; ++I) {
+                        CD[I - 1] = CR[IXM(I, J)] + driftr_cgr(g, P4, MDR, I, J, J0, J1, L);
+                        if (OUTSIDE(I, J) == 0) {
+                            double ctemp = dmax(fabs(CD[I - 1]), 1E-10);
+                            DtDriftR = dmin(DtDriftR, p->fraccfl * DTs / ctemp);
+                        }
+                        SG(I, J) = 1;
+                        if (CD[I - 1] < 0) SG(I, J) = -1;
+                    }
+                    int UR;
+                    if (rec)
+                        for (int I = 1; I <= NR; ++I) rec[IX4(I, J, K, L)] = 0;
+                    if (SG(NR, J) == 1) {
+                        FB(1) = 0.;
+                        FB(NR) = FF(NR);
+                        UR = NR - 1;
                     } else {
-                        FF(NR + 1) = fgeos[IXG(J, K, L)] * g->conf1 * FNHS(NR, J, L);
-                        FF(NR + 2) = fgeos[IXG(J, K, L)] * g->conf2 * FNHS(NR, J, L);
-                        last_src = (int)IXG(J, K, L);
-                    }
-                }
-                if (gsrc) gsrc[IXG(J, K, L)] = last_src;
-                for (int I = 2; I <= UR; ++I) {
-                    int s = SG(I, J);
-                    double X = FF(I + 1) - FF(I);
-                    double FUP = 0.5 * (FF(I) + FF(I + 1) - s * X);
-                    int cs = 0;
-                    if (fabs(X) <= 1.E-27) FB(I) = FUP;
-                    if (fabs(X) > 1.E-27) {
-                        int N = I + 1 - s;
-                        double R = (FF(N) - FF(N - 1)) / X;
-                        if (R <= 0) FB(I) = FUP;
-                        if (R > 0) {
-                            double LIM = limiter(BetaLim, R);
-                            double CORR = -0.5 * (CD[I - 1] - s) * X;
-                            FB(I) = FUP + LIM * CORR;
-                            cs = limiter_case(BetaLim, R);
+                        FB(1) = FF(2);
+                        UR = NR;
+                        if (OUTSIDE(NR, J) == 1) {
+                            FF(NR + 1) = 0.;
+                            FF(NR + 2) = 0.;
+                            last_src = -1;
+                        } else {
+                            FF(NR + 1) = fgeos[IXG(J, K, L)] * g->conf1 * FNHS(NR, J, L);
+                            FF(NR + 2) = fgeos[IXG(J, K, L)] * g->conf2 * FNHS(NR, J, L);
+                            last_src = (int)IXG(J, K, L);
                         }
                     }
-                    if (rec) rec[IX4(I, J, K, L)] = (unsigned char)cs;
-                }
-                if (p->closed) {
-                    FB(1) = 0.;
-                    FB(NR) = 0.;
-                }
-                for (int I = 2; I <= NR; ++I) {
-                    F2(I, J, K, L) = F2(I, J, K, L) - CD[I - 1] * FB(I) + CD[I - 2] * FB(I - 1);
-                    if (F2(I, J, K, L) < 0) {
-                        F2(I, J, K, L) = 1E-15;
-                        if (rec) rec[IX4(I, J, K, L)] |= REC_CLIP;
+                    if (gsrc) gsrc[IXG(J, K, L)] = last_src;
+                    for (int I = 2; I <= UR; ++I) {
+                        int s = SG(I, J);
+                        double X = FF(I + 1) - FF(I);
+                        double FUP = 0.5 * (FF(I) + FF(I + 1) - s * X);
+                        int cs = 0;
+                        if (fabs(X) <= 1.E-27) FB(I) = FUP;
+                        if (fabs(X) > 1.E-27) {
+                            int N = I + 1 - s;
+                            double R = (FF(N) - FF(N - 1)) / X;
+                            if (R <= 0) FB(I) = FUP;
+                            if (R > 0) {
+                                double LIM = limiter(BetaLim, R);
+                                double CORR = -0.5 * (CD[I - 1] - s) * X;
+                                FB(I) = FUP + LIM * CORR;
+                                cs = limiter_case(BetaLim, R);
+                            }
+                        }
+                        if (rec) rec[IX4(I, J, K, L)] = (unsigned char)cs;
                     }
+                    if (p->closed) {
+                        FB(1) = 0.;
+                        FB(NR) = 0.;
+                    }
+                    for (int I = 2; I <= NR; ++I) {
+                        F2(I, J, K, L) = F2(I, J, K, L) - CD[I - 1] * FB(I) + CD[I - 2] * FB(I - 1);
+                        if (F2(I, J, K, L) < 0) {
+                            F2(I, J, K, L) = 1E-15;
+                            if (rec) rec[IX4(I, J, K, L)] |= REC_CLIP;
+                        }
+                    }
+                    if (cdrift)
+                        for (int I = 1; I <= NR; ++I) cdrift[IX4(I, J, K, L)] = CD[I - 1];
                 }
-                if (cdrift)
-                    for (int I = 1; I <= NR; ++I) cdrift[IX4(I, J, K, L)] = CD[I - 1];
             }
-    }
 #undef FF
 #undef FB
 #undef SG
-    free(sgn);
+        free(sgn);
+        free(F);
+        free(FBND);
+        free(CD);
+    }
     free(CR);
-    free(F);
-    free(FBND);
-    free(CD);
+    free(plane_src);
     return DtDriftR;
 }
 
@@ -301,12 +355,19 @@ static double driftp_impl(const ro_grid *g, const ro_species *sp, const ro_param
     const double DTs = p->dts, MDR = g->mdr, DPHI = g->dphi, BetaLim = p->betalim;
     double DtDriftP = 100000.0;
     const double OME = 7.3E-5;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_inner) reduction(min : DtDriftP)
+#endif
+    {
     double *F = (double *)calloc((size_t)NT, sizeof(double));
     double *FBND = (double *)calloc((size_t)NT, sizeof(double));
     double *CD = (double *)calloc((size_t)NT, sizeof(double));
 #define FF(n) F[(n)-1]
 #define FB(n) FBND[(n)-1]
 #define C(n) CD[(n)-1]
+#ifdef _OPENMP
+#pragma omp for collapse(2) schedule(static)
+#endif
     for (int L = 1; L <= NPA; ++L)
         for (int K = 1; K <= NE; ++K)
             for (int I = 2; I <= NR; ++I) {
@@ -369,6 +430,7 @@ static double driftp_impl(const ro_grid *g, const ro_species *sp, const ro_param
     free(F);
     free(FBND);
     free(CD);
+    }
     return DtDriftP;
 }
 
@@ -396,22 +458,29 @@ static double drifte_impl(const ro_grid *g, const ro_species *sp, const ro_param
     double DtDriftE = 10000.0;
     const double OME = 7.3E-5;
     /* F(0:NE+2) -> F[0..NE+2] */
+    double EZERO = EKEV(1) - WE(1);
+    double GRZERO = 1. + EZERO * 1000. * Q / sp->rmas / CS / CS;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_inner) reduction(min : DtDriftE)
+#endif
+    {
     double *F = (double *)calloc((size_t)NE + 3, sizeof(double));
     double *FBND = (double *)calloc((size_t)NE, sizeof(double));
     double *CD = (double *)calloc((size_t)NE, sizeof(double));
 #define FF(n) F[(n)]
 #define FB(n) FBND[(n)-1]
 #define C(n) CD[(n)-1]
-    double EZERO = EKEV(1) - WE(1);
-    double GRZERO = 1. + EZERO * 1000. * Q / sp->rmas / CS / CS;
     FF(NE + 1) = 0.;
     FF(NE + 2) = 0.;
+#ifdef _OPENMP
+#pragma omp for collapse(2) schedule(static)
+#endif
     for (int J = 1; J <= NT; ++J) {
-        int J0 = J - 1;
-        if (J == 1) J0 = NT - 1;
-        int J2 = J + 1;
-        if (J == NT) J2 = 2;
         for (int I = 2; I <= NR; ++I) {
+            int J0 = J - 1;
+            if (J == 1) J0 = NT - 1;
+            int J2 = J + 1;
+            if (J == NT) J2 = 2;
             double DRD1 = (EIP(I, J) * RLZ(I) - (VT(I, J2) - VT(I, J0)) / 2. / DPHI) / BNES(I, J);
             double DPD1 = OME * RLZ(I) + ((VT(I + 1, J) - VT(I - 1, J)) / 2 / MDR - EIR(I, J)) / BNES(I, J);
             for (int L = 1; L <= NPA; ++L) {
@@ -480,6 +549,7 @@ static double drifte_impl(const ro_grid *g, const ro_species *sp, const ro_param
     free(F);
     free(FBND);
     free(CD);
+    }
     return DtDriftE;
 }
 
@@ -506,19 +576,26 @@ static double driftmu_impl(const ro_grid *g, const ro_species *sp, const ro_para
     const int QS = sp->qs;
     double DtDriftMu = 10000.0;
     const double OME = 7.3E-5;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_inner) reduction(min : DtDriftMu)
+#endif
+    {
     double *F = (double *)calloc((size_t)NPA, sizeof(double));
     double *FBND = (double *)calloc((size_t)NPA, sizeof(double));
     double *CD = (double *)calloc((size_t)NPA, sizeof(double));
 #define FF(n) F[(n)-1]
 #define FB(n) FBND[(n)-1]
 #define C(n) CD[(n)-1]
+#ifdef _OPENMP
+#pragma omp for collapse(2) schedule(static)
+#endif
     for (int K = 1; K <= NE; ++K)
         for (int J = 1; J <= NT; ++J) {
-            int J0 = J - 1;
-            if (J == 1) J0 = NT - 1;
-            int J1 = J + 1;
-            if (J == NT) J1 = 2;
             for (int I = 2; I <= NR; ++I) {
+                int J0 = J - 1;
+                if (J == 1) J0 = NT - 1;
+                int J1 = J + 1;
+                if (J == NT) J1 = 2;
                 for (int L = 1; L <= NPA; ++L) FF(L) = F2(I, J, K, L);
                 FF(1) = FF(2);
                 double DRM1 = (EIP(I, J) * RLZ(I) - (VT(I, J1) - VT(I, J0)) / 2 / DPHI) / BNES(I, J);
@@ -586,6 +663,7 @@ static double driftmu_impl(const ro_grid *g, const ro_species *sp, const ro_para
     free(F);
     free(FBND);
     free(CD);
+    }
     return DtDriftMu;
 }
 
@@ -596,6 +674,9 @@ void ro_cepara(const ro_grid *g, const ro_species *sp, const ro_params *p, doubl
     size_t n = (size_t)NR * NT * NE * NPA;
     for (size_t i = 0; i < n; ++i) charge[i] = 1.;
     if (sp->cex_kind >= 1 && sp->cex_kind <= 3) {
+#ifdef _OPENMP
+#pragma omp parallel for collapse(2) num_threads(g_inner) schedule(static)
+#endif
         for (int L = 2; L <= NPA; ++L)
             for (int K = 2; K <= NE; ++K)
                 for (int I = 2; I <= NR; ++I)
@@ -622,6 +703,9 @@ void ro_cepara(const ro_grid *g, const ro_species *sp, const ro_params *p, doubl
 
 void ro_charexchange(const ro_grid *g, double *f2, const double *charge)
 {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(g_inner) schedule(static)
+#endif
     for (int K = 2; K <= NE; ++K)
         for (int J = 1; J <= NT; ++J)
             for (int I = 2; I <= NR; ++I)
@@ -630,6 +714,9 @@ void ro_charexchange(const ro_grid *g, double *f2, const double *charge)
 
 void ro_atmol(const ro_grid *g, double *f2, const double *atlos)
 {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(g_inner) schedule(static)
+#endif
     for (int K = 2; K <= NE; ++K)
         for (int J = 1; J <= NT; ++J)
             for (int I = 2; I <= NR; ++I) {
@@ -658,6 +745,9 @@ void ro_anisch(const ro_grid *g, const ro_species *sp, double *f2, double *ppert
     const double RFAC = 4 * PI / cv;
     int khi[5] = {6, 10, 25, 30, 35};
     khi[4] = NE;
+#ifdef _OPENMP
+#pragma omp parallel for collapse(2) num_threads(g_inner) schedule(static)
+#endif
     for (int I = 2; I <= NR; ++I)
         for (int J = 1; J <= NT; ++J) {
             int klo = 2;
@@ -694,6 +784,9 @@ void ro_anisch(const ro_grid *g, const ro_species *sp, double *f2, double *ppert
 
 void ro_flux(const ro_grid *g, const ro_species *sp, const double *f2, double *flux)
 {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(g_inner) schedule(static)
+#endif
     for (int I = 2; I <= NR; ++I)
         for (int K = 2; K <= NE; ++K)
             for (int L = 2; L <= NPA; ++L)
@@ -757,6 +850,7 @@ int ro_ram_run(const ro_grid *g, int ns, const ro_species *sp_all, const ro_para
     size_t ncell = (size_t)NR * NT * NE * NPA;
 #ifdef _OPENMP
     if (nthreads < 1) nthreads = 1;
+    if (g_inner > 1 && nthreads > 1) omp_set_max_active_levels(2);
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 1)
 #endif
     for (int iS = 0; iS < ns; ++iS) {

@@ -82,6 +82,11 @@ typedef struct {
     double lsdr, lscha, lsatm;  /* ELORC accumulated into LSDR/LSCHA/LSATM */
 } ro_losses;
 
+/* Threads for the loops over independent lines inside each routine
+ * (default 1, the reference's serial loops); ro_ram_run nests them inside
+ * its per-species threads.  Results are identical for every setting. */
+void ro_set_inner_threads(int n);
+
 /* VOLS potential, src/ModRamRun.f90:45-54.  vt: (NR+1, NT). */
 void ro_vt_vols(const ro_grid *g, double kp, double *vt);
 

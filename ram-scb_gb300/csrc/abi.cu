@@ -70,11 +70,13 @@ struct ramgpu_ctx {
     double dts = 0.0;
     long long items_version = -1;
     std::vector<double> kp;          // ncalls * nm
+    double* kp_d = nullptr;          // the same on the device (copied per call device-to-device)
     ObsDev* obs = nullptr;
     double *fm = nullptr, *J = nullptr, *J2 = nullptr, *ckpt = nullptr;
     unsigned char* rec = nullptr;
     unsigned long long* digest = nullptr;
     size_t rec_call = 0;             // bytes of one call's record (8 sweeps)
+    bool rec_stale = false;          // the record ring no longer holds the last segment
   } adj;
   // optional per-kernel-class timing
   bool timing = false;
@@ -295,8 +297,8 @@ static int enqueue_body(ramgpu_ctx* ctx, double dts) {
 static void adj_free(ramgpu_ctx* ctx) {
   auto& a = ctx->adj;
   cudaFree(a.obs); cudaFree(a.fm); cudaFree(a.J); cudaFree(a.J2); cudaFree(a.ckpt);
-  cudaFree(a.rec); cudaFree(a.digest);
-  a.obs = nullptr; a.fm = a.J = a.J2 = a.ckpt = nullptr; a.rec = nullptr; a.digest = nullptr;
+  cudaFree(a.rec); cudaFree(a.digest); cudaFree(a.kp_d);
+  a.obs = nullptr; a.fm = a.J = a.J2 = a.ckpt = a.kp_d = nullptr; a.rec = nullptr; a.digest = nullptr;
   a.ready = false;
 }
 
@@ -334,10 +336,12 @@ static int adj_copy_items(ramgpu_ctx* ctx, double* dst, bool to_ckpt) {
   return RAMGPU_OK;
 }
 
+// Kp of every member for one call of the window, device to device (the host
+// does not wait for the stream).
 static int adj_set_kp(ramgpu_ctx* ctx, int call) {
   const int nm = ctx->cfg.n_members;
-  CK(cudaMemcpyAsync(ctx->d.kp, ctx->adj.kp.data() + (size_t)call * nm, sizeof(double) * nm,
-                     cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d.kp, ctx->adj.kp_d + (size_t)call * nm, sizeof(double) * nm,
+                     cudaMemcpyDeviceToDevice, ctx->stream));
   return RAMGPU_OK;
 }
 
@@ -1135,8 +1139,8 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
   if (ctx->cfg.flags & RAMGPU_FLAG_LOSSES)
     return fail(ctx, RAMGPU_ERR_ARG, "the adjoint window runs without RAMGPU_FLAG_LOSSES");
   Dev& d = ctx->d;
-  if (d.nr > 160 || d.nt > 160 || d.ne > 160 || d.npa > 160)
-    return fail(ctx, RAMGPU_ERR_ARG, "the adjoint supports NR, NT, NE, NPA <= 160");
+  if (d.nr < 4 || d.nt < 7 || d.ne < 4 || d.npa < 6)
+    return fail(ctx, RAMGPU_ERR_ARG, "the adjoint needs NR >= 4, NT >= 7, NE >= 4, NPA >= 6");
   int rc = prepare(ctx, dts);
   if (rc) return rc;
   if (d.nitems == 0) return fail(ctx, RAMGPU_ERR_STATE, "no active (member, species)");
@@ -1176,11 +1180,13 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
   ok = ok && cudaMalloc(&a.J, sizeof(double) * nm) == cudaSuccess;
   ok = ok && cudaMalloc(&a.J2, sizeof(double) * nm) == cudaSuccess;
   ok = ok && cudaMalloc(&a.digest, sizeof(unsigned long long)) == cudaSuccess;
+  ok = ok && cudaMalloc(&a.kp_d, sizeof(double) * (size_t)ncalls * nm) == cudaSuccess;
   if (!ok) {
     adj_free(ctx);
     return fail(ctx, RAMGPU_ERR_NOMEM, "adjoint buffers: device allocation failed");
   }
   if (nobs > 0) CK(cudaMemcpy(a.obs, oh.data(), sizeof(ObsDev) * nobs, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(a.kp_d, a.kp.data(), sizeof(double) * (size_t)ncalls * nm, cudaMemcpyHostToDevice));
   std::vector<int> one(nm, 1);
   CK(cudaMemcpyAsync(d.vt_mode, one.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemsetAsync(a.J, 0, sizeof(double) * nm, ctx->stream));
@@ -1200,6 +1206,7 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
   if (J) CK(cudaMemcpy(J, a.J, sizeof(double) * nm, cudaMemcpyDeviceToHost));
   ctx->last_dts = dts;
   a.ready = true;
+  a.rec_stale = false;
   return RAMGPU_OK;
 }
 
@@ -1218,11 +1225,15 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
   CK(cudaMemsetAsync(d.gfg, 0, sizeof(double) * nslot * nfg, ctx->stream));
   for (int seg = a.nseg - 1; seg >= 0; --seg) {
     const int c0 = seg * a.k, c1 = (c0 + a.k < a.ncalls) ? c0 + a.k : a.ncalls;
-    if ((rc = adj_copy_items(ctx, a.ckpt + (size_t)seg * isz, false))) return rc;
-    for (int c = c0; c < c1; ++c) {  // recompute the segment, recording branches
-      if ((rc = adj_set_kp(ctx, c))) return rc;
-      if ((rc = enqueue_call_rec(ctx, a.dts, a.rec + (size_t)(c - c0) * a.rec_call))) return rc;
-      launch_obs_fwd(d, a.obs, a.nobs, c, a.fm, a.J2, ctx->stream);
+    // The record of the last segment is still the forward pass's own (the
+    // observation values fm are kept from it for every call); earlier
+    // segments are recomputed from their checkpoint, recording branches.
+    if (seg != a.nseg - 1 || a.rec_stale) {
+      if ((rc = adj_copy_items(ctx, a.ckpt + (size_t)seg * isz, false))) return rc;
+      for (int c = c0; c < c1; ++c) {
+        if ((rc = adj_set_kp(ctx, c))) return rc;
+        if ((rc = enqueue_call_rec(ctx, a.dts, a.rec + (size_t)(c - c0) * a.rec_call))) return rc;
+      }
     }
     for (int c = c1 - 1; c >= c0; --c) {  // transpose call c
       const unsigned char* r = a.rec + (size_t)(c - c0) * a.rec_call;
@@ -1245,6 +1256,7 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
     }
   }
   if ((rc = adj_copy_items(ctx, a.ckpt, false))) return rc;  // F2 back to the initial state
+  a.rec_stale = a.nseg > 1;  // the ring now holds segment 0
   CK(cudaStreamSynchronize(ctx->stream));
   if (grad_f2) CK(cudaMemcpy(grad_f2, d.lam, sizeof(double) * nslot * d.ncell, cudaMemcpyDefault));
   if (grad_fgeos) CK(cudaMemcpy(grad_fgeos, d.gfg, sizeof(double) * nslot * nfg, cudaMemcpyDefault));
@@ -1257,6 +1269,8 @@ int ramgpu_adj_record(ramgpu_ctx* ctx, int call, unsigned char* out) {
   if (!a.ready) return fail(ctx, RAMGPU_ERR_STATE, "ramgpu_adj_forward must run first");
   if (call < 0 || call >= a.ncalls || (a.ncalls > a.k && call / a.k != a.nseg - 1))
     return fail(ctx, RAMGPU_ERR_ARG, "only calls of the last checkpoint segment are kept");
+  if (a.rec_stale)
+    return fail(ctx, RAMGPU_ERR_STATE, "the record was replaced by ramgpu_adj_backward's recomputation");
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemcpy(out, a.rec + (size_t)(call % a.k) * a.rec_call, a.rec_call, cudaMemcpyDeviceToHost));
   return RAMGPU_OK;

@@ -19,25 +19,32 @@
 
 namespace ramgpu {
 
-constexpr int kMaxLine = 160;  // longest line of the adjoint (NR, NT, NE, NPA <= 160)
+// Transposed sweeps.  With the record frozen, one face f contributes
+//   FBb(f) = dJ/dFBND(f) = C(f) * (w(f+1) le(f+1) - w(f) le(f))
+// (le = lambda of an updated, unclipped cell, w the update weight: 1 for R
+// and P, 1/WE, 1/WMU for E and MU) and scatters it to the cells of
+// FBND(f) = FUP + a LX:  the upwind cell, and for LX = beta D | X | D |
+// beta X the two cells of D (f-1,f for s=+1; f+1,f+2 for s=-1) or of X
+// (f,f+1).  Every face touches cells f-1..f+2 only, so each line is
+// streamed once with a rolling window of four cell accumulators in
+// registers: after face f, cell f-1 is final and is written out.
 
-// Scatter of one face: FBb = dJ/dFBND(f).  up is the upwind cell, cs the
-// recorded case, a the CORR factor, (f, f+1) the face's cells and
-// (dm, dp) the cells of D = G(dp) - G(dm).
-__device__ __forceinline__ void scatter_face(double* Gb, double FBb, int up, int cs, double a,
-                                             double beta, int f, int f1, int dm, int dp) {
-  Gb[up] += FBb;
+// Scatter of one face into the window (cm1, c0, c1, c2) = cells f-1..f+2.
+__device__ __forceinline__ void face_adj(double FBb, bool neg, int cs, double a, double beta,
+                                         double& cm1, double& c0, double& c1, double& c2) {
+  if (neg) c1 += FBb; else c0 += FBb;  // FUP = F(f) or F(f+1)
   if (cs) {
     const double Lb = a * FBb;
     const double Vb = (cs == 1 || cs == 4) ? beta * Lb : Lb;
-    if (cs == 2 || cs == 4) {  // V = X = G(f1) - G(f)
-      Gb[f1] += Vb;
-      Gb[f] -= Vb;
-    } else {                   // V = D
-      Gb[dp] += Vb;
-      Gb[dm] -= Vb;
-    }
+    if (cs == 2 || cs == 4) { c1 += Vb; c0 -= Vb; }  // X = F(f+1) - F(f)
+    else if (!neg) { c0 += Vb; cm1 -= Vb; }          // D = F(f) - F(f-1)
+    else { c2 += Vb; c1 -= Vb; }                     // D = F(f+2) - F(f+1)
   }
+}
+
+// lambda of cell c of a line (stride st) masked by the clip bit
+__device__ __forceinline__ double masked(const double* lam, const unsigned char* rl, long long off) {
+  return (rl[off] & kClipBit) ? 0.0 : lam[off];
 }
 
 #define WORK_LOOP(NLINES)                                                          \
@@ -47,7 +54,11 @@ __device__ __forceinline__ void scatter_face(double* Gb, double FBb, int up, int
        u += (long long)gridDim.x * gridDim.y)
 
 // ------------------------------------------------------------------ DRIFTR^T
-__global__ void __launch_bounds__(64) k_adj_r(Dev d, const unsigned char* __restrict__ rec) {
+// Cells 1..NR, ghosts NR+1, NR+2.  new(1) = F(1); faces 2..NR-1 (and NR on
+// inflow lines); FBND(1) = F(2) on inflow lines, FBND(NR) = F(NR) on outflow
+// lines (both 0 when closed).  The ghosts' adjoints go to dJ/dFGEOS, for an
+// outflow line to the FGEOS cell its stale ghost came from.
+__global__ void __launch_bounds__(128) k_adj_r(Dev d, const unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = nt * ne * d.npa;
   WORK_LOOP(nlines) {
@@ -64,55 +75,55 @@ __global__ void __launch_bounds__(64) k_adj_r(Dev d, const unsigned char* __rest
     const double beta = d.betalim;
     const bool closed = d.flags & 1u;
     const int n = nr;
-    double C[kMaxLine + 1], Gb[kMaxLine + 3], Pb[kMaxLine + 1];
-    for (int i = 1; i <= n; ++i) {
-      C[i] = fma(grt[i - 1], p4, cr[i - 1]);
-      Gb[i] = 0.0;
-      Pb[i] = 0.0;
-    }
-    Gb[0] = Gb[n + 1] = Gb[n + 2] = 0.0;
-    const bool inflow = is_neg(C[n]);
-    Gb[1] = lam[0];  // cell 1 is not updated
-    for (int i = 2; i <= n; ++i) {
-      const double le = (rl[i - 1] & kClipBit) ? 0.0 : lam[i - 1];
-      Gb[i] += le;
-      Pb[i] -= le;
-      Pb[i - 1] += le;
-    }
-    if (inflow && !closed) Gb[2] += C[1] * Pb[1];  // FBND(1) = F(2)
+    const double cN = fma(grt[n - 1], p4, cr[n - 1]);
+    const bool inflow = is_neg(cN);
     const int UR = inflow ? n : n - 1;
-    for (int f = 2; f <= UR; ++f) {
-      if (closed && f == n) continue;
-      const double FBb = C[f] * Pb[f];
-      const bool neg = is_neg(C[f]);
-      const double a = fma(C[f], -0.5, neg ? -0.5 : 0.5);
-      scatter_face(Gb, FBb, neg ? f + 1 : f, rl[f - 1] & 7, a, beta, f, f + 1, neg ? f + 1 : f - 1,
-                   neg ? f + 2 : f);
+    // le(i) for i = 2..NR (0 outside); window cells 1..4
+    double le0 = masked(lam, rl, 1);                  // le(f), f = 2
+    double le1 = (3 <= n) ? masked(lam, rl, 2) : 0.0;  // le(f+1)
+    double le2 = (4 <= n) ? masked(lam, rl, 3) : 0.0;  // le(f+2)
+    double cm1 = lam[0], c0 = le0, c1 = le1, c2 = le2;
+    if (inflow && !closed) c0 += fma(grt[0], p4, cr[0]) * le0;  // FBND(1) = F(2)
+    for (int f = 2; f <= n; ++f) {
+      const double C = (f == n) ? cN : fma(grt[f - 1], p4, cr[f - 1]);
+      if (f <= UR && !(closed && f == n)) {
+        const bool neg = is_neg(C);
+        const double a = fma(C, -0.5, neg ? -0.5 : 0.5);
+        face_adj(C * (le1 - le0), neg, rl[f - 1] & 7, a, beta, cm1, c0, c1, c2);
+      }
+      if (f == n && !inflow && !closed) c0 -= cN * le0;  // FBND(NR) = F(NR)
+      lam[f - 2] = cm1;
+      const double le3 = (f + 3 <= n) ? masked(lam, rl, f + 2) : 0.0;
+      cm1 = c0; c0 = c1; c1 = c2; c2 = le3;
+      le0 = le1; le1 = le2; le2 = le3;
     }
-    if (!inflow && !closed) Gb[n] += C[n] * Pb[n];  // FBND(NR) = F(NR)
-    // ghost cells -> dJ/dFGEOS
+    lam[n - 1] = cm1;
+    const double gN1 = c0, gN2 = c1;  // ghosts F(NR+1), F(NR+2)
     const long long nfg = (long long)nt * ne * d.npa;
     if (inflow) {
       if (d.outside[(long long)j * nr + n - 1] != 1) {
         const double fh = d.fnhs[((long long)l * nt + j) * d.nf + n - 1];
-        atomicAdd(&d.gfg[slot * nfg + line], d.conf1 * fh * Gb[n + 1] + d.conf2 * fh * Gb[n + 2]);
+        atomicAdd(&d.gfg[slot * nfg + line], d.conf1 * fh * gN1 + d.conf2 * fh * gN2);
       }
-    } else if (Gb[n + 1] != 0.0) {
+    } else if (gN1 != 0.0) {
       const int src = stale_ghost_src(d, m, slot, j, k, l, p4);
       if (src >= 0) {
         const int jj = src % nt, ll = src / (nt * ne);
         if (d.outside[(long long)jj * nr + n - 1] != 1) {
           const double fh = d.fnhs[((long long)ll * nt + jj) * d.nf + n - 1];
-          atomicAdd(&d.gfg[slot * nfg + src], d.conf1 * fh * Gb[n + 1]);
+          atomicAdd(&d.gfg[slot * nfg + src], d.conf1 * fh * gN1);
         }
       }
     }
-    for (int i = 1; i <= n; ++i) lam[i - 1] = Gb[i];
   }
 }
 
 // ------------------------------------------------------------------ DRIFTP^T
-__global__ void __launch_bounds__(64) k_adj_p(Dev d, const unsigned char* __restrict__ rec) {
+// Cells 1..NT with J = 1 == J = NT: new(1) is overwritten by new(NT), faces
+// J = 2..NT with FBND(1) = FBND(NT).  Faces NT-1 and NT wrap onto cells
+// 1..3; they are transposed first, their contributions held in registers
+// and added when the window reaches those cells (NT >= 7).
+__global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * ne * d.npa;
   WORK_LOOP(nlines) {
@@ -123,6 +134,7 @@ __global__ void __launch_bounds__(64) k_adj_p(Dev d, const unsigned char* __rest
     const int i = 1 + line % (nr - 1);
     const int kl = line / (nr - 1);
     const int k = kl % ne, l = kl / ne;
+    const long long st = nr;
     const long long base = ((long long)kl * nt) * nr + i;
     double* lam = d.lam + (long long)slot * d.ncell + base;
     const unsigned char* rl = rec + (u / bpi) * d.ncell + base;
@@ -131,40 +143,74 @@ __global__ void __launch_bounds__(64) k_adj_p(Dev d, const unsigned char* __rest
     const double p2 = d.p2[((long long)s * ne + k) * nr + i];
     const double beta = d.betalim;
     const int n = nt;
-    double C[kMaxLine + 1], Gb[kMaxLine + 3], Pb[kMaxLine + 1], lv[kMaxLine + 1];
-    for (int J = 1; J <= n; ++J) {
-      C[J] = (J >= 2) ? fma(gpt[(long long)(J - 1) * nr], p2, ca[(long long)(J - 1) * nr]) : 0.0;
-      lv[J] = lam[(long long)(J - 1) * nr];
-      Gb[J] = 0.0;
-      Pb[J] = 0.0;
+#define PC(J) fma(gpt[(long long)((J)-1) * nr], p2, ca[(long long)((J)-1) * nr])
+#define PLE(J) masked(lam, rl, (long long)((J)-1) * st)
+    // le(NT) takes lambda of cell 1 too (F2(1) = F2new(NT))
+    const double leN = (rl[(long long)(n - 1) * st] & kClipBit) ? 0.0 : lam[(long long)(n - 1) * st] + lam[0];
+    const double leNm = PLE(n - 1), le2 = PLE(2);
+    // w1..w3: contributions to cells 1..3, tNm2..tN: to cells NT-2..NT
+    double w1 = 0.0, w2 = 0.0, w3 = 0.0, tNm2 = 0.0, tNm1 = 0.0, tN = 0.0;
+    {  // face NT-1: X = F(NT)-F(NT-1); D = F(NT-1)-F(NT-2) (s=+1) or F(2)-F(1) (s=-1)
+      const double C = PC(n - 1);
+      const bool neg = is_neg(C);
+      const double a = fma(C, -0.5, neg ? -0.5 : 0.5);
+      const double FBb = C * (leN - leNm);
+      const int cs = rl[(long long)(n - 2) * st] & 7;
+      if (neg) tN += FBb; else tNm1 += FBb;
+      if (cs) {
+        const double Lb = a * FBb;
+        const double Vb = (cs == 1 || cs == 4) ? beta * Lb : Lb;
+        if (cs == 2 || cs == 4) { tN += Vb; tNm1 -= Vb; }
+        else if (!neg) { tNm1 += Vb; tNm2 -= Vb; }
+        else { w2 += Vb; w1 -= Vb; }
+      }
     }
-    lv[n] += lv[1];  // F2(1) = F2new(NT)
-    lv[1] = 0.0;
-    for (int J = 2; J <= n; ++J) {
-      const double le = (rl[(long long)(J - 1) * nr] & kClipBit) ? 0.0 : lv[J];
-      Gb[J] += le;
-      Pb[J] -= le;
-      Pb[J - 1] += le;
+    {  // face NT: X = F(2)-F(NT); D = F(NT)-F(NT-1) (s=+1) or F(3)-F(2) (s=-1)
+      const double C = PC(n);
+      const bool neg = is_neg(C);
+      const double a = fma(C, -0.5, neg ? -0.5 : 0.5);
+      const double FBb = C * (le2 - leN);  // Pb(NT) = -le(NT) + Pb(1), Pb(1) = le(2)
+      const int cs = rl[(long long)(n - 1) * st] & 7;
+      if (neg) w2 += FBb; else tN += FBb;
+      if (cs) {
+        const double Lb = a * FBb;
+        const double Vb = (cs == 1 || cs == 4) ? beta * Lb : Lb;
+        if (cs == 2 || cs == 4) { w2 += Vb; tN -= Vb; }
+        else if (!neg) { tN += Vb; tNm1 -= Vb; }
+        else { w3 += Vb; w2 -= Vb; }
+      }
     }
-    Pb[n] += Pb[1];  // FBND(1) = FBND(NT), CDriftP(1) = CDriftP(NT)
-    for (int J = 2; J <= n; ++J) {
-      const double FBb = C[J] * Pb[J];
-      const bool neg = is_neg(C[J]);
-      const double a = fma(C[J], -0.5, neg ? -0.5 : 0.5);
-      const int J1 = (J == n) ? 2 : J + 1;
-      int dm, dp;
-      if (!neg) { dm = J - 1; dp = J; }
-      else if (J <= n - 2) { dm = J + 1; dp = J + 2; }
-      else if (J == n - 1) { dm = 1; dp = 2; }
-      else { dm = 2; dp = 3; }
-      scatter_face(Gb, FBb, neg ? J1 : J, rl[(long long)(J - 1) * nr] & 7, a, beta, J, J1, dm, dp);
+    // faces 2..NT-2 streamed; window cells 1..4 (cell 1 has no own term)
+    double le0 = le2, le1 = PLE(3), lnext = PLE(4);
+    double cm1 = w1, c0 = le2 + w2, c1 = le1 + w3, c2 = lnext;
+    for (int J = 2; J <= n - 2; ++J) {
+      const double C = PC(J);
+      const bool neg = is_neg(C);
+      const double a = fma(C, -0.5, neg ? -0.5 : 0.5);
+      face_adj(C * (le1 - le0), neg, rl[(long long)(J - 1) * st] & 7, a, beta, cm1, c0, c1, c2);
+      lam[(long long)(J - 2) * st] = cm1;
+      const int cn = J + 3;  // cell entering the window
+      const double lec = (cn < n) ? PLE(cn) : (cn == n ? leN : 0.0);
+      double add = lec;
+      if (cn == n - 2) add += tNm2;
+      if (cn == n - 1) add += tNm1;
+      if (cn == n) add += tN;
+      cm1 = c0; c0 = c1; c1 = c2; c2 = add;
+      le0 = le1; le1 = lnext; lnext = lec;
     }
-    for (int J = 1; J <= n; ++J) lam[(long long)(J - 1) * nr] = Gb[J];
+    lam[(long long)(n - 3) * st] = cm1;
+    lam[(long long)(n - 2) * st] = c0;
+    lam[(long long)(n - 1) * st] = c1;
+#undef PC
+#undef PLE
   }
 }
 
 // ------------------------------------------------------------------ DRIFTE^T
-__global__ void __launch_bounds__(64) k_adj_e(Dev d, const unsigned char* __restrict__ rec) {
+// Cells 0..NE+2: G(1) = kap1 F(2) and G(0) = kap0 G(1) are extrapolated,
+// G(NE+1) = G(NE+2) = 0; faces 1..NE (not 1 and NE when closed); cell 1
+// is never updated.
+__global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * nt * d.npa;
   WORK_LOOP(nlines) {
@@ -187,39 +233,42 @@ __global__ void __launch_bounds__(64) k_adj_e(Dev d, const unsigned char* __rest
     const double beta = d.betalim;
     const bool closed = d.flags & 1u;
     const int n = ne;
-    double C[kMaxLine + 1], Gb[kMaxLine + 3], Pb[kMaxLine + 1];
+#define EC(K) (edot[(long long)((K)-1) * nr] * fma(eb[(K)-1], wet, ue))
+#define ELE(K) masked(lam, rl, (long long)((K)-1) * st)
+    const double out1 = lam[0];
+    // wl(K) = le(K)/WE(K) for K = 2..NE, 0 elsewhere; window cells 0..3
+    double le2 = ELE(2), le3 = ELE(3);
+    double wl0 = 0.0, wl1 = le2 * d.iwe[1], wl2 = le3 * d.iwe[2];
+    double cm1 = 0.0, c0 = 0.0, c1 = le2, c2 = le3;
+    double g0 = 0.0, g1 = 0.0;
     for (int K = 1; K <= n; ++K) {
-      C[K] = edot[(long long)(K - 1) * nr] * fma(eb[K - 1], wet, ue);
-      Gb[K] = 0.0;
-      Pb[K] = 0.0;
+      if (!(closed && (K == 1 || K == n))) {
+        const double C = EC(K);
+        const bool neg = is_neg(C);
+        const double a = fma(C, d.mhde[K - 1], neg ? -0.5 : 0.5);
+        face_adj(C * (wl1 - wl0), neg, rl[(long long)(K - 1) * st] & 7, a, beta, cm1, c0, c1, c2);
+      }
+      // cell K-1 is final
+      if (K == 1) g0 = cm1;
+      else if (K == 2) g1 = cm1 + d.kap[2 * s + 0] * g0;
+      else if (K == 3) lam[st] = cm1 + d.kap[2 * s + 1] * g1;
+      else lam[(long long)(K - 2) * st] = cm1;
+      const int cn = K + 3;
+      const double lec = (cn <= n) ? ELE(cn) : 0.0;
+      cm1 = c0; c0 = c1; c1 = c2; c2 = lec;
+      wl0 = wl1; wl1 = wl2; wl2 = (cn <= n) ? lec * d.iwe[cn - 1] : 0.0;
     }
-    Gb[0] = Gb[n + 1] = Gb[n + 2] = 0.0;
-    const double out1 = lam[0];  // cell K = 1 is not updated
-    for (int K = 2; K <= n; ++K) {
-      const double le = (rl[(long long)(K - 1) * st] & kClipBit) ? 0.0 : lam[(long long)(K - 1) * st];
-      const double w = d.iwe[K - 1];
-      Gb[K] += le;
-      Pb[K] -= w * le;
-      Pb[K - 1] += w * le;
-    }
-    for (int K = 1; K <= n; ++K) {
-      if (closed && (K == 1 || K == n)) continue;
-      const double FBb = C[K] * Pb[K];
-      const bool neg = is_neg(C[K]);
-      const double a = fma(C[K], d.mhde[K - 1], neg ? -0.5 : 0.5);
-      scatter_face(Gb, FBb, neg ? K + 1 : K, rl[(long long)(K - 1) * st] & 7, a, beta, K, K + 1,
-                   neg ? K + 1 : K - 1, neg ? K + 2 : K);
-    }
-    // G(1) = kap1 F(2), G(0) = kap0 G(1); G(NE+1) = G(NE+2) = 0
-    const double g1 = Gb[1] + d.kap[2 * s + 0] * Gb[0];
+    lam[(long long)(n - 1) * st] = cm1;  // cell NE (NE >= 4)
     lam[0] = out1;
-    lam[st] = Gb[2] + d.kap[2 * s + 1] * g1;
-    for (int K = 3; K <= n; ++K) lam[(long long)(K - 1) * st] = Gb[K];
+#undef EC
+#undef ELE
   }
 }
 
 // ----------------------------------------------------------------- DRIFTMU^T
-__global__ void __launch_bounds__(64) k_adj_mu(Dev d, const unsigned char* __restrict__ rec) {
+// Cells 1..NPA: G(1) = F(2); faces 2..NPA-2; FBND(NPA-1) = F(NPA) (0 when
+// closed); cells 2..NPA-1 updated; then F2(NPA) = F2new(NPA-1)*rho.
+__global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa;
   const int nlines = (nr - 1) * nt * ne;
   WORK_LOOP(nlines) {
@@ -242,40 +291,44 @@ __global__ void __launch_bounds__(64) k_adj_mu(Dev d, const unsigned char* __res
     const double beta = d.betalim;
     const bool closed = d.flags & 1u;
     const int n = npa;
-    double C[kMaxLine + 1], Gb[kMaxLine + 3], Pb[kMaxLine + 1], lv[kMaxLine + 1];
-    for (int L = 1; L <= n; ++L) {
-      C[L] = (L >= 2 && L <= n - 1) ? fma(ekv, wm[(long long)(L - 1) * sij], um[(long long)(L - 1) * sij]) : 0.0;
-      lv[L] = lam[(long long)(L - 1) * st];
-      Gb[L] = 0.0;
-      Pb[L] = 0.0;
-    }
-    Gb[n + 1] = Gb[n + 2] = 0.0;
-    lv[n - 1] += d.rho[fij] * lv[n];  // F2(NPA) = F2new(NPA-1) * rho
-    lv[n] = 0.0;
-    const double out1 = lv[1];       // cell L = 1 is not updated
-    for (int L = 2; L <= n - 1; ++L) {
-      const double le = (rl[(long long)(L - 1) * st] & kClipBit) ? 0.0 : lv[L];
-      const double w = d.iwmu[L - 1];
-      Gb[L] += le;
-      Pb[L] -= w * le;
-      Pb[L - 1] += w * le;
-    }
+#define MC(L) fma(ekv, wm[(long long)((L)-1) * sij], um[(long long)((L)-1) * sij])
+#define MLE(L) masked(lam, rl, (long long)((L)-1) * st)
+    const double out1 = lam[0];
+    // le(NPA-1) takes rho * lambda(NPA) (F2(NPA) = F2new(NPA-1)*rho)
+    const double leNm = (rl[(long long)(n - 2) * st] & kClipBit)
+                            ? 0.0 : lam[(long long)(n - 2) * st] + d.rho[fij] * lam[(long long)(n - 1) * st];
+#define MLV(L) ((L) == n - 1 ? leNm : MLE(L))
+    double le2 = MLV(2), le3 = MLV(3), le4 = MLV(4);
+    double wl0 = le2 * d.iwmu[1], wl1 = le3 * d.iwmu[2], wl2 = le4 * d.iwmu[3];
+    double cm1 = 0.0, c0 = le2, c1 = le3, c2 = le4;
+    double gb1 = 0.0;
     for (int L = 2; L <= n - 2; ++L) {
-      const double FBb = C[L] * Pb[L];
-      const bool neg = is_neg(C[L]);
-      const double a = fma(C[L], d.mhdmu[L - 1], neg ? -0.5 : 0.5);
-      scatter_face(Gb, FBb, neg ? L + 1 : L, rl[(long long)(L - 1) * st] & 7, a, beta, L, L + 1,
-                   neg ? L + 1 : L - 1, neg ? L + 2 : L);
+      const double C = MC(L);
+      const bool neg = is_neg(C);
+      const double a = fma(C, d.mhdmu[L - 1], neg ? -0.5 : 0.5);
+      face_adj(C * (wl1 - wl0), neg, rl[(long long)(L - 1) * st] & 7, a, beta, cm1, c0, c1, c2);
+      if (L == 2) gb1 = cm1;                              // cell 1 -> cell 2 (G(1) = F(2))
+      else if (L == 3) lam[st] = cm1 + gb1;
+      else lam[(long long)(L - 2) * st] = cm1;
+      const int cn = L + 3;
+      const double lec = (cn <= n - 1) ? MLV(cn) : 0.0;
+      cm1 = c0; c0 = c1; c1 = c2; c2 = lec;
+      wl0 = wl1; wl1 = wl2; wl2 = (cn <= n - 1) ? lec * d.iwmu[cn - 1] : 0.0;
     }
-    if (!closed) Gb[n] += C[n - 1] * Pb[n - 1];  // FBND(NPA-1) = F(NPA)
-    Gb[2] += Gb[1];                               // F(1) = F(2)
+    // window: cells NPA-2, NPA-1, NPA
+    if (!closed) c1 += MC(n - 1) * (-wl0);  // FBND(NPA-1) = F(NPA): Pb(NPA-1) = -le(NPA-1)/WMU
+    lam[(long long)(n - 3) * st] = cm1;
+    lam[(long long)(n - 2) * st] = c0;
+    lam[(long long)(n - 1) * st] = c1;
     lam[0] = out1;
-    for (int L = 2; L <= n; ++L) lam[(long long)(L - 1) * st] = Gb[L];
+#undef MC
+#undef MLE
+#undef MLV
   }
 }
 
 void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_t st) {
-  const int blk = 64;
+  const int blk = 128;
   int nl;
   switch (w) {
     case 0: nl = d.nt * d.ne * d.npa; break;

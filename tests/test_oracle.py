@@ -359,3 +359,25 @@ def test_driftmu_matches_independent_restatement(name, tiny, tiny_pert):
     ref = python_driftmu(g, f_in, cd, wl.fields.fnhs, counts)
     assert np.array_equal(f2[1:], ref[1:])
     assert counts["fup"] > 0 and counts["R"] + counts["one"] + counts["betaR"] + counts["beta"] > 0
+
+
+def test_threaded_oracle_is_bitwise_serial():
+    """Threading the oracle's independent lines (and nesting them under the
+    species threads) leaves every result bit-identical, including DRIFTR's
+    stale ghosts on the perturbed grid and the DtDrift minima."""
+    wl = W.make_workload("tiny_pert")
+    o = pyoracle.Oracle(wl.grid, wl.fields)
+    runs = []
+    for inner, outer in ((1, 1), (4, 4), (3, 2)):
+        pyoracle.set_inner_threads(inner)
+        f = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+        outs = [o.ram_run(f, wl.fgeos, wl.dts, kp=3.0 + c, nthreads=outer, want_flux=True) for c in range(2)]
+        runs.append((f, outs))
+    pyoracle.set_inner_threads(1)
+    f0, o0 = runs[0]
+    for f, outs in runs[1:]:
+        for s in range(len(f)):
+            assert np.array_equal(f[s], f0[s])
+            assert np.array_equal(outs[1]["ppert"][s], o0[1]["ppert"][s])
+            assert np.array_equal(outs[1]["flux"][s], o0[1]["flux"][s])
+        assert outs[1]["dts_next"] == o0[1]["dts_next"]
