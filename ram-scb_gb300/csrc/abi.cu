@@ -440,6 +440,7 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   d.ide = dalloc<double>(ctx, ne, &ok);
   d.mhdmu = dalloc<double>(ctx, npa, &ok); d.iwmu = dalloc<double>(ctx, npa, &ok);
   d.idmu = dalloc<double>(ctx, npa, &ok);
+  d.bmhde = dalloc<double>(ctx, ne, &ok); d.bmhdmu = dalloc<double>(ctx, npa, &ok);
   d.grel = dalloc<double>(ctx, ns * ne, &ok); d.grbnd = dalloc<double>(ctx, ns * ne, &ok);
   d.vel = dalloc<double>(ctx, ns * ne, &ok); d.epp = dalloc<double>(ctx, ns * ne, &ok);
   d.rmas = dalloc<double>(ctx, ns, &ok);
@@ -589,6 +590,9 @@ int ramgpu_set_grid(ramgpu_ctx* ctx, const ramgpu_grid* g) {
   for (int l = 0; l < npa; ++l) { q1[l] = -0.5 / G.dmu[l]; q2[l] = 1.0 / G.wmu[l]; q3[l] = 1.0 / G.dmu[l]; }
   CK(up(d.mhde, r1.data(), ne)); CK(up(d.iwe, r2.data(), ne)); CK(up(d.ide, r3.data(), ne));
   CK(up(d.mhdmu, q1.data(), npa)); CK(up(d.iwmu, q2.data(), npa)); CK(up(d.idmu, q3.data(), npa));
+  for (int k = 0; k < ne; ++k) r1[k] *= d.betalim;
+  for (int l = 0; l < npa; ++l) q1[l] *= d.betalim;
+  CK(up(d.bmhde, r1.data(), ne)); CK(up(d.bmhdmu, q1.data(), npa));
   // (NS,NE) Fortran -> [s][k]
   std::vector<double> t(ns * ne);
   auto tr2 = [&](const double* dst, const double* src) {

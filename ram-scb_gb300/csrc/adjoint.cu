@@ -29,17 +29,36 @@ namespace ramgpu {
 // streamed once with a rolling window of four cell accumulators in
 // registers: after face f, cell f-1 is final and is written out.
 
-// Scatter of one face into the window (cm1, c0, c1, c2) = cells f-1..f+2.
-__device__ __forceinline__ void face_adj(double FBb, bool neg, int cs, double a, double beta,
-                                         double& cm1, double& c0, double& c1, double& c2) {
-  if (neg) c1 += FBb; else c0 += FBb;  // FUP = F(f) or F(f+1)
-  if (cs) {
-    const double Lb = a * FBb;
-    const double Vb = (cs == 1 || cs == 4) ? beta * Lb : Lb;
-    if (cs == 2 || cs == 4) { c1 += Vb; c0 -= Vb; }  // X = F(f+1) - F(f)
-    else if (!neg) { c0 += Vb; cm1 -= Vb; }          // D = F(f) - F(f-1)
-    else { c2 += Vb; c1 -= Vb; }                     // D = F(f+2) - F(f+1)
-  }
+// Scatter of one face into the window (cm1, c0, c1, c2) = cells f-1..f+2:
+// the upwind cell gets FBb, the two cells of LX get +-ak*FBb with ak = a
+// (cases 2, 3) or beta*a (cases 1, 4).  Every coefficient is picked by
+// integer selects, so a face costs 2 adds and 4 fma on the FP64 pipe
+// whatever its case.
+__device__ __forceinline__ void face_acc(double FBb, bool neg, int cs, double ak, double& cm1,
+                                         double& c0, double& c1, double& c2) {
+  const bool xt = (cs == 2) | (cs == 4);  // LX = X (f, f+1)
+  const bool dt = (cs == 1) | (cs == 3);  // LX = D (f-1, f) or (f+1, f+2)
+  const double pos = (xt | dt) ? ak : 0.0;
+  const double ngv = __longlong_as_double(__double_as_longlong(pos) ^ (long long)kSignMask);
+  const double sm1 = (dt & !neg) ? ngv : 0.0;
+  const double s0 = xt ? ngv : ((dt & !neg) ? pos : 0.0);
+  const double s1 = xt ? pos : ((dt & neg) ? ngv : 0.0);
+  const double s2 = (dt & neg) ? pos : 0.0;
+  const double f0 = neg ? s0 : s0 + 1.0;  // FUP = F(f) for s = +1
+  const double f1 = neg ? s1 + 1.0 : s1;  // FUP = F(f+1) for s = -1
+  cm1 = fma(sm1, FBb, cm1);
+  c0 = fma(f0, FBb, c0);
+  c1 = fma(f1, FBb, c1);
+  c2 = fma(s2, FBb, c2);
+}
+
+// ak = LIMITER weight times the CORR factor a = -0.5*(C*q - s) of a face:
+// fma(C, -0.5*k*q, 0.5*k*s) with k = beta for cases 1, 4 and 1 otherwise
+// (q = 1 for R and P; -0.5*q comes from the -0.5/DE, -0.5/DMU tables).
+__device__ __forceinline__ double face_ak(double C, bool neg, int cs, double mh, double bmh, double beta) {
+  const bool kb = (cs == 1) | (cs == 4);
+  const double hk = kb ? 0.5 * beta : 0.5;
+  return fma(C, kb ? bmh : mh, neg ? -hk : hk);
 }
 
 // lambda of cell c of a line (stride st) masked by the clip bit
@@ -72,7 +91,7 @@ __global__ void __launch_bounds__(128) k_adj_r(Dev d, const unsigned char* __res
     const double* grt = d.grt + ((long long)l * nt + j) * nr;
     const double* cr = d.cr + ((long long)m * nt + j) * nr;
     const double p4 = d.p4[s * ne + k];
-    const double beta = d.betalim;
+    const double beta = d.betalim, bmh = -0.5 * beta;
     const bool closed = d.flags & 1u;
     const int n = nr;
     const double cN = fma(grt[n - 1], p4, cr[n - 1]);
@@ -88,8 +107,8 @@ __global__ void __launch_bounds__(128) k_adj_r(Dev d, const unsigned char* __res
       const double C = (f == n) ? cN : fma(grt[f - 1], p4, cr[f - 1]);
       if (f <= UR && !(closed && f == n)) {
         const bool neg = is_neg(C);
-        const double a = fma(C, -0.5, neg ? -0.5 : 0.5);
-        face_adj(C * (le1 - le0), neg, rl[f - 1] & 7, a, beta, cm1, c0, c1, c2);
+        const int cs = rl[f - 1] & 7;
+        face_acc(C * (le1 - le0), neg, cs, face_ak(C, neg, cs, -0.5, bmh, beta), cm1, c0, c1, c2);
       }
       if (f == n && !inflow && !closed) c0 -= cN * le0;  // FBND(NR) = F(NR)
       lam[f - 2] = cm1;
@@ -141,7 +160,7 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
     const double* gpt = d.gpt + ((long long)l * nt) * nr + i;
     const double* ca = d.ca + ((long long)m * nt) * nr + i;
     const double p2 = d.p2[((long long)s * ne + k) * nr + i];
-    const double beta = d.betalim;
+    const double beta = d.betalim, bmh = -0.5 * beta;
     const int n = nt;
 #define PC(J) fma(gpt[(long long)((J)-1) * nr], p2, ca[(long long)((J)-1) * nr])
 #define PLE(J) masked(lam, rl, (long long)((J)-1) * st)
@@ -186,8 +205,8 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
     for (int J = 2; J <= n - 2; ++J) {
       const double C = PC(J);
       const bool neg = is_neg(C);
-      const double a = fma(C, -0.5, neg ? -0.5 : 0.5);
-      face_adj(C * (le1 - le0), neg, rl[(long long)(J - 1) * st] & 7, a, beta, cm1, c0, c1, c2);
+      const int cs = rl[(long long)(J - 1) * st] & 7;
+      face_acc(C * (le1 - le0), neg, cs, face_ak(C, neg, cs, -0.5, bmh, beta), cm1, c0, c1, c2);
       lam[(long long)(J - 2) * st] = cm1;
       const int cn = J + 3;  // cell entering the window
       const double lec = (cn < n) ? PLE(cn) : (cn == n ? leN : 0.0);
@@ -245,8 +264,9 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
       if (!(closed && (K == 1 || K == n))) {
         const double C = EC(K);
         const bool neg = is_neg(C);
-        const double a = fma(C, d.mhde[K - 1], neg ? -0.5 : 0.5);
-        face_adj(C * (wl1 - wl0), neg, rl[(long long)(K - 1) * st] & 7, a, beta, cm1, c0, c1, c2);
+        const int cs = rl[(long long)(K - 1) * st] & 7;
+        face_acc(C * (wl1 - wl0), neg, cs, face_ak(C, neg, cs, d.mhde[K - 1], d.bmhde[K - 1], beta), cm1,
+                 c0, c1, c2);
       }
       // cell K-1 is final
       if (K == 1) g0 = cm1;
@@ -305,8 +325,9 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
     for (int L = 2; L <= n - 2; ++L) {
       const double C = MC(L);
       const bool neg = is_neg(C);
-      const double a = fma(C, d.mhdmu[L - 1], neg ? -0.5 : 0.5);
-      face_adj(C * (wl1 - wl0), neg, rl[(long long)(L - 1) * st] & 7, a, beta, cm1, c0, c1, c2);
+      const int cs = rl[(long long)(L - 1) * st] & 7;
+      face_acc(C * (wl1 - wl0), neg, cs, face_ak(C, neg, cs, d.mhdmu[L - 1], d.bmhdmu[L - 1], beta), cm1,
+               c0, c1, c2);
       if (L == 2) gb1 = cm1;                              // cell 1 -> cell 2 (G(1) = F(2))
       else if (L == 3) lam[st] = cm1 + gb1;
       else lam[(long long)(L - 2) * st] = cm1;
@@ -457,21 +478,44 @@ void launch_obs_adj(const Dev& d, const ObsDev* obs, int nobs, int call, const d
   if (nobs > 0) k_obs_adj<<<(nobs + 127) / 128, 128, 0, st>>>(d, obs, nobs, call, fm);
 }
 
-// Order-independent digest of a branch record (sum of mixed position*code
-// terms modulo 2^64): equal digests of two runs mean an unchanged pattern
-// with overwhelming probability.
+// Order-independent digest of a branch record: two sums (mod 2^32) of
+// position-mixed 32-bit hashes of its 32-bit words, read 16 bytes at a time
+// (a ragged tail byte by byte).  Equal digests of two runs mean an
+// unchanged pattern with overwhelming probability.
+__device__ __forceinline__ unsigned mix32(unsigned w, unsigned long long i, unsigned c1, unsigned c2) {
+  unsigned h = (w + (unsigned)i * 0x9E3779B9u + (unsigned)(i >> 32)) * c1;
+  h ^= h >> 15;
+  h *= c2;
+  return h ^ (h >> 13);
+}
+
 __global__ void k_digest(const unsigned char* __restrict__ rec, long long n, unsigned long long* out) {
-  unsigned long long acc = 0ULL;
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-       c += (long long)gridDim.x * blockDim.x) {
-    unsigned long long x = (unsigned long long)c * 0x9E3779B97F4A7C15ULL + rec[c];
-    x ^= x >> 29;
-    x *= 0xBF58476D1CE4E5B9ULL;
-    x ^= x >> 32;
-    acc += x * (rec[c] + 1ULL);
+  unsigned lo = 0u, hi = 0u;
+  const bool al = ((unsigned long long)rec & 15ULL) == 0ULL;
+  const long long n16 = al ? n / 16 : 0;
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long nth = (long long)gridDim.x * blockDim.x;
+  const uint4* r4 = reinterpret_cast<const uint4*>(rec);
+  for (long long c = tid; c < n16; c += nth) {
+    const uint4 v = r4[c];
+    const unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const unsigned long long i = 4ULL * c + q;
+      lo += mix32(w[q], i, 0x85EBCA6Bu, 0xC2B2AE35u);
+      hi += mix32(w[q], i, 0x27D4EB2Fu, 0x165667B1u);
+    }
   }
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+  for (long long b = 16 * n16 + tid; b < n; b += nth) {
+    const unsigned long long i = 0x100000000ULL + (unsigned long long)b;
+    lo += mix32(rec[b], i, 0x85EBCA6Bu, 0xC2B2AE35u);
+    hi += mix32(rec[b], i, 0x27D4EB2Fu, 0x165667B1u);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo += __shfl_xor_sync(0xffffffffu, lo, o);
+    hi += __shfl_xor_sync(0xffffffffu, hi, o);
+  }
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, ((unsigned long long)hi << 32) + lo);
 }
 
 void launch_digest(const unsigned char* rec, long long n, unsigned long long* out, cudaStream_t st) {

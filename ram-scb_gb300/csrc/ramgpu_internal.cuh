@@ -41,6 +41,7 @@ struct Dev {
   const int *upa_mom;   // int(UPA(I)-1): last L of the ANISCH sum, NR
   // reciprocal grid tables: -0.5/DE, 1/WE, 1/DE (NE); -0.5/DMU, 1/WMU, 1/DMU (NPA)
   const double *mhde, *iwe, *ide, *mhdmu, *iwmu, *idmu;
+  const double *bmhde, *bmhdmu;  // BetaLim times -0.5/DE and -0.5/DMU (adjoint)
   // per-species grid (ns x NE)
   const double *grel, *grbnd, *vel;
   const double *epp;

@@ -242,7 +242,27 @@ def test_gradient_matches_cpu_adjoint():
         print(f"species {s}: dJ/dF2 {ef:.2e}  dJ/dFGEOS {eb:.2e}  record mismatches {mism}")
         errs.append((s, ef, eb))
     assert all(ef <= 1e-9 and eb <= 1e-9 for _, ef, eb in errs), errs
-    assert mism <= 1e-4 * recs[2].size * 2, mism
+    # Branch codes may differ only next to the magnetopause-outside cells:
+    # there F2 sits at the 1e-31 mask / 1e-15 floor, where the two
+    # evaluations of the limiter ratio part at rounding level, and the masked
+    # adjoint is zero, so the choice does not reach the gradient.
+    out = np.asarray(wl.fields.outside) == 1
+    phys = out[:, : g.nt - 1].copy()  # J = NT is J = 1
+    phys[:, 0] |= out[:, g.nt - 1]
+    nearp = np.zeros_like(phys)
+    for di in range(-2, 3):
+        sh = np.zeros_like(phys)
+        if di >= 0:
+            sh[di:] = phys[: g.nr - di]
+        else:
+            sh[:di] = phys[-di:]
+        for dj in range(-2, 3):
+            nearp |= np.roll(sh, dj, axis=1)
+    near = np.concatenate([nearp, nearp[:, :1]], axis=1)
+    for i, c in enumerate((2, 3)):
+        q, s_, cell = np.nonzero(recg[i] != recs[c])
+        I, J = cell % g.nr, (cell // g.nr) % g.nt
+        assert near[I, J].all(), (c, list(zip(q[~near[I, J]][:5], I[~near[I, J]][:5], J[~near[I, J]][:5])))
 
 
 def test_autograd_function_matches_c_abi(tiny):
@@ -258,7 +278,7 @@ def test_autograd_function_matches_c_abi(tiny):
         gf, gb = model.adj_backward()
         f2, fg = A.device_state(model, tiny.f2, tiny.fgeos, "cuda")
         Jt = A.window_misfit(model, f2, fg, 3, tiny.dts, kp, 2, obs)
-        assert np.allclose(Jt.cpu().numpy(), J, rtol=1e-13, atol=0)
+        assert np.allclose(Jt.detach().cpu().numpy(), J, rtol=1e-13, atol=0)
         w = torch.tensor([1.0, -2.5], dtype=torch.float64, device="cuda")
         (Jt * w).sum().backward()
         gt, gbt = f2.grad.cpu().numpy(), fg.grad.cpu().numpy()
