@@ -328,7 +328,7 @@ class Oracle:
         return ch, at
 
     def window_gradient(self, f2s, fgeos, dts, kps, obs, species=None, closed=False, do_atmol=True,
-                        records=None):
+                        records=None, states=None):
         """Scalar adjoint of a window of len(kps) ram_run calls for one member.
 
         J = sum over obs of (log flux - log_obs)^2 with flux = F2/FFACTOR/FNHS
@@ -337,7 +337,8 @@ class Oracle:
         sequence of ram_run (src/ModRamRun.f90:77-225) with every sweep
         recorded; backward: the transposes in reverse order.  f2s is not
         modified.  With ``records`` a list, each call's branch record is
-        appended as an (8 sweeps, species, NR*NT*NE*NPA) uint8 array.
+        appended as an (8 sweeps, species, NR*NT*NE*NPA) uint8 array; with
+        ``states`` a list, each call's starting F2 as (species, NR*NT*NE*NPA).
         Returns (J, {s: dJ/dF2}, {s: dJ/dFGEOS})."""
         g = self.grid
         idx = list(range(self.ns)) if species is None else list(species)
@@ -351,6 +352,8 @@ class Oracle:
         for c, kp in enumerate(kps):
             vt = self.vt_vols(kp)
             tc = {}
+            if states is not None:
+                states.append(np.stack([f[s].reshape(-1, order="F").copy() for s in idx]))
             for s in idx:
                 t = [self.sweep_rec("R", s, f[s], vt, dts, fg[s], closed),
                      self.sweep_rec("P", s, f[s], vt, dts, closed=closed),

@@ -230,9 +230,9 @@ def test_gradient_matches_cpu_adjoint():
     finally:
         model.close()
     o = pyoracle.Oracle(g, wl.fields)
-    recs = []
+    recs, states = [], []
     Jc, cf, cb = o.window_gradient([np.asfortranarray(a) for a in wl.f2], [np.asfortranarray(a) for a in wl.fgeos],
-                                   wl.dts, kp[:, 0], obs, records=recs)
+                                   wl.dts, kp[:, 0], obs, records=recs, states=states)
     assert abs(Jg - Jc) <= 1e-12 * Jc, (Jg, Jc)
     mism = sum(int(np.count_nonzero(recg[i][:, :, :] != recs[c])) for i, c in enumerate((2, 3)))
     errs = []
@@ -242,27 +242,27 @@ def test_gradient_matches_cpu_adjoint():
         print(f"species {s}: dJ/dF2 {ef:.2e}  dJ/dFGEOS {eb:.2e}  record mismatches {mism}")
         errs.append((s, ef, eb))
     assert all(ef <= 1e-9 and eb <= 1e-9 for _, ef, eb in errs), errs
-    # Branch codes may differ only next to the magnetopause-outside cells:
-    # there F2 sits at the 1e-31 mask / 1e-15 floor, where the two
-    # evaluations of the limiter ratio part at rounding level, and the masked
-    # adjoint is zero, so the choice does not reach the gradient.
-    out = np.asarray(wl.fields.outside) == 1
-    phys = out[:, : g.nt - 1].copy()  # J = NT is J = 1
-    phys[:, 0] |= out[:, g.nt - 1]
-    nearp = np.zeros_like(phys)
-    for di in range(-2, 3):
-        sh = np.zeros_like(phys)
-        if di >= 0:
-            sh[di:] = phys[: g.nr - di]
-        else:
-            sh[:di] = phys[-di:]
-        for dj in range(-2, 3):
-            nearp |= np.roll(sh, dj, axis=1)
-    near = np.concatenate([nearp, nearp[:, :1]], axis=1)
+    # Branch codes may differ only where F2 is tiny next to its species'
+    # maximum (the mask and clip floors, far tails of the distribution): there
+    # the 1e-12-relative differences of the two forward evaluations exceed
+    # the cell values themselves and move the limiter ratio or the 1e-27
+    # threshold, while the adjoint weight of such faces does not reach the
+    # gradient at the tolerance above.
     for i, c in enumerate((2, 3)):
         q, s_, cell = np.nonzero(recg[i] != recs[c])
-        I, J = cell % g.nr, (cell // g.nr) % g.nt
-        assert near[I, J].all(), (c, list(zip(q[~near[I, J]][:5], I[~near[I, J]][:5], J[~near[I, J]][:5])))
+        if cell.size == 0:
+            continue
+        st = states[c]
+        rel = []
+        for qq, ss, cc in zip(q, s_, cell):
+            # neighbourhood along every axis within two cells
+            idx = [cc + o for o in (-2, -1, 0, 1, 2)]
+            for stride in (g.nr, g.nr * g.nt, g.nr * g.nt * g.ne):
+                idx += [cc + o * stride for o in (-2, -1, 1, 2)]
+            idx = [x for x in idx if 0 <= x < st.shape[1]]
+            rel.append(np.min(np.abs(st[ss, idx])) / np.max(np.abs(st[ss])))
+        print(f"call {c}: {cell.size} differing codes, local/max F2 at most {max(rel):.1e}")
+        assert max(rel) < 1e-6, (c, sorted(rel)[-5:])
 
 
 def test_autograd_function_matches_c_abi(tiny):
