@@ -1143,8 +1143,8 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
   if (ctx->cfg.flags & RAMGPU_FLAG_LOSSES)
     return fail(ctx, RAMGPU_ERR_ARG, "the adjoint window runs without RAMGPU_FLAG_LOSSES");
   Dev& d = ctx->d;
-  if (d.nr < 4 || d.nt < 7 || d.ne < 4 || d.npa < 6)
-    return fail(ctx, RAMGPU_ERR_ARG, "the adjoint needs NR >= 4, NT >= 7, NE >= 4, NPA >= 6");
+  if (d.nr < 4 || d.nt < 7 || d.ne < 6 || d.npa < 9)
+    return fail(ctx, RAMGPU_ERR_ARG, "the adjoint needs NR >= 4, NT >= 7, NE >= 6, NPA >= 9");
   int rc = prepare(ctx, dts);
   if (rc) return rc;
   if (d.nitems == 0) return fail(ctx, RAMGPU_ERR_STATE, "no active (member, species)");

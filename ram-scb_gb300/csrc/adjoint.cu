@@ -72,6 +72,10 @@ __device__ __forceinline__ double masked(const double* lam, const unsigned char*
   for (long long u = blockIdx.x + (long long)blockIdx.y * gridDim.x; u < nunits;   \
        u += (long long)gridDim.x * gridDim.y)
 
+// The loops below are peeled so that no floating-point operation in the
+// main loop depends on the position along the line (the FP64 pipe is the
+// bottleneck and predicated-off branches would still cost issue slots).
+
 // ------------------------------------------------------------------ DRIFTR^T
 // Cells 1..NR, ghosts NR+1, NR+2.  new(1) = F(1); faces 2..NR-1 (and NR on
 // inflow lines); FBND(1) = F(2) on inflow lines, FBND(NR) = F(NR) on outflow
@@ -93,31 +97,40 @@ __global__ void __launch_bounds__(128) k_adj_r(Dev d, const unsigned char* __res
     const double p4 = d.p4[s * ne + k];
     const double beta = d.betalim, bmh = -0.5 * beta;
     const bool closed = d.flags & 1u;
-    const int n = nr;
+    const int n = nr;  // >= 4
     const double cN = fma(grt[n - 1], p4, cr[n - 1]);
     const bool inflow = is_neg(cN);
-    const int UR = inflow ? n : n - 1;
-    // le(i) for i = 2..NR (0 outside); window cells 1..4
-    double le0 = masked(lam, rl, 1);                  // le(f), f = 2
-    double le1 = (3 <= n) ? masked(lam, rl, 2) : 0.0;  // le(f+1)
-    double le2 = (4 <= n) ? masked(lam, rl, 3) : 0.0;  // le(f+2)
+    // le(i) = lambda of updated, unclipped cell i (i = 2..NR); window = cells f-1..f+2
+    double le0 = masked(lam, rl, 1), le1 = masked(lam, rl, 2), le2 = masked(lam, rl, 3);
     double cm1 = lam[0], c0 = le0, c1 = le1, c2 = le2;
     if (inflow && !closed) c0 += fma(grt[0], p4, cr[0]) * le0;  // FBND(1) = F(2)
-    for (int f = 2; f <= n; ++f) {
-      const double C = (f == n) ? cN : fma(grt[f - 1], p4, cr[f - 1]);
-      if (f <= UR && !(closed && f == n)) {
-        const bool neg = is_neg(C);
-        const int cs = rl[f - 1] & 7;
-        face_acc(C * (le1 - le0), neg, cs, face_ak(C, neg, cs, -0.5, bmh, beta), cm1, c0, c1, c2);
-      }
-      if (f == n && !inflow && !closed) c0 -= cN * le0;  // FBND(NR) = F(NR)
+    auto face = [&](int f, double C) {
+      const bool neg = is_neg(C);
+      const int cs = rl[f - 1] & 7;
+      face_acc(C * (le1 - le0), neg, cs, face_ak(C, neg, cs, -0.5, bmh, beta), cm1, c0, c1, c2);
+    };
+    auto advance = [&](int f, double le3) {  // cell f-1 is final; cell f+3 enters
       lam[f - 2] = cm1;
-      const double le3 = (f + 3 <= n) ? masked(lam, rl, f + 2) : 0.0;
       cm1 = c0; c0 = c1; c1 = c2; c2 = le3;
       le0 = le1; le1 = le2; le2 = le3;
+    };
+    int f = 2;
+    for (; f <= n - 3; ++f) {
+      face(f, fma(grt[f - 1], p4, cr[f - 1]));
+      advance(f, masked(lam, rl, f + 2));
     }
-    lam[n - 1] = cm1;
-    const double gN1 = c0, gN2 = c1;  // ghosts F(NR+1), F(NR+2)
+    for (; f <= n - 1; ++f) {
+      face(f, fma(grt[f - 1], p4, cr[f - 1]));
+      advance(f, 0.0);
+    }
+    // face NR: transposed on inflow lines, FBND(NR) = F(NR) on outflow lines
+    if (!closed) {
+      if (inflow) face(n, cN);
+      else c0 -= cN * le0;
+    }
+    lam[n - 2] = cm1;
+    lam[n - 1] = c0;
+    const double gN1 = c1, gN2 = c2;  // ghosts F(NR+1), F(NR+2)
     const long long nfg = (long long)nt * ne * d.npa;
     if (inflow) {
       if (d.outside[(long long)j * nr + n - 1] != 1) {
@@ -172,51 +185,45 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
     {  // face NT-1: X = F(NT)-F(NT-1); D = F(NT-1)-F(NT-2) (s=+1) or F(2)-F(1) (s=-1)
       const double C = PC(n - 1);
       const bool neg = is_neg(C);
-      const double a = fma(C, -0.5, neg ? -0.5 : 0.5);
-      const double FBb = C * (leN - leNm);
       const int cs = rl[(long long)(n - 2) * st] & 7;
+      const double FBb = C * (leN - leNm);
+      const double V = face_ak(C, neg, cs, -0.5, bmh, beta) * FBb;
       if (neg) tN += FBb; else tNm1 += FBb;
-      if (cs) {
-        const double Lb = a * FBb;
-        const double Vb = (cs == 1 || cs == 4) ? beta * Lb : Lb;
-        if (cs == 2 || cs == 4) { tN += Vb; tNm1 -= Vb; }
-        else if (!neg) { tNm1 += Vb; tNm2 -= Vb; }
-        else { w2 += Vb; w1 -= Vb; }
-      }
+      if (cs == 2 || cs == 4) { tN += V; tNm1 -= V; }
+      else if (cs && !neg) { tNm1 += V; tNm2 -= V; }
+      else if (cs) { w2 += V; w1 -= V; }
     }
     {  // face NT: X = F(2)-F(NT); D = F(NT)-F(NT-1) (s=+1) or F(3)-F(2) (s=-1)
       const double C = PC(n);
       const bool neg = is_neg(C);
-      const double a = fma(C, -0.5, neg ? -0.5 : 0.5);
-      const double FBb = C * (le2 - leN);  // Pb(NT) = -le(NT) + Pb(1), Pb(1) = le(2)
       const int cs = rl[(long long)(n - 1) * st] & 7;
+      const double FBb = C * (le2 - leN);  // Pb(NT) = -le(NT) + Pb(1), Pb(1) = le(2)
+      const double V = face_ak(C, neg, cs, -0.5, bmh, beta) * FBb;
       if (neg) w2 += FBb; else tN += FBb;
-      if (cs) {
-        const double Lb = a * FBb;
-        const double Vb = (cs == 1 || cs == 4) ? beta * Lb : Lb;
-        if (cs == 2 || cs == 4) { w2 += Vb; tN -= Vb; }
-        else if (!neg) { tN += Vb; tNm1 -= Vb; }
-        else { w3 += Vb; w2 -= Vb; }
-      }
+      if (cs == 2 || cs == 4) { w2 += V; tN -= V; }
+      else if (cs && !neg) { tN += V; tNm1 -= V; }
+      else if (cs) { w3 += V; w2 -= V; }
     }
     // faces 2..NT-2 streamed; window cells 1..4 (cell 1 has no own term)
     double le0 = le2, le1 = PLE(3), lnext = PLE(4);
     double cm1 = w1, c0 = le2 + w2, c1 = le1 + w3, c2 = lnext;
-    for (int J = 2; J <= n - 2; ++J) {
+    auto step = [&](int J, double add, double lec) {  // face J, then cell J+3 enters
       const double C = PC(J);
       const bool neg = is_neg(C);
       const int cs = rl[(long long)(J - 1) * st] & 7;
       face_acc(C * (le1 - le0), neg, cs, face_ak(C, neg, cs, -0.5, bmh, beta), cm1, c0, c1, c2);
       lam[(long long)(J - 2) * st] = cm1;
-      const int cn = J + 3;  // cell entering the window
-      const double lec = (cn < n) ? PLE(cn) : (cn == n ? leN : 0.0);
-      double add = lec;
-      if (cn == n - 2) add += tNm2;
-      if (cn == n - 1) add += tNm1;
-      if (cn == n) add += tN;
       cm1 = c0; c0 = c1; c1 = c2; c2 = add;
       le0 = le1; le1 = lnext; lnext = lec;
+    };
+    for (int J = 2; J <= n - 6; ++J) {
+      const double lec = PLE(J + 3);
+      step(J, lec, lec);
     }
+    { const double lec = PLE(n - 2); step(n - 5, lec + tNm2, lec); }
+    step(n - 4, leNm + tNm1, leNm);
+    step(n - 3, leN + tN, leN);
+    step(n - 2, 0.0, 0.0);
     lam[(long long)(n - 3) * st] = cm1;
     lam[(long long)(n - 2) * st] = c0;
     lam[(long long)(n - 1) * st] = c1;
@@ -228,7 +235,7 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
 // ------------------------------------------------------------------ DRIFTE^T
 // Cells 0..NE+2: G(1) = kap1 F(2) and G(0) = kap0 G(1) are extrapolated,
 // G(NE+1) = G(NE+2) = 0; faces 1..NE (not 1 and NE when closed); cell 1
-// is never updated.
+// is never updated (NE >= 6).
 __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * nt * d.npa;
@@ -255,30 +262,45 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
 #define EC(K) (edot[(long long)((K)-1) * nr] * fma(eb[(K)-1], wet, ue))
 #define ELE(K) masked(lam, rl, (long long)((K)-1) * st)
     const double out1 = lam[0];
-    // wl(K) = le(K)/WE(K) for K = 2..NE, 0 elsewhere; window cells 0..3
-    double le2 = ELE(2), le3 = ELE(3);
+    // wl(K) = le(K)/WE(K) for K = 2..NE, 0 elsewhere; window = cells K-1..K+2
+    const double le2 = ELE(2), le3 = ELE(3);
     double wl0 = 0.0, wl1 = le2 * d.iwe[1], wl2 = le3 * d.iwe[2];
     double cm1 = 0.0, c0 = 0.0, c1 = le2, c2 = le3;
-    double g0 = 0.0, g1 = 0.0;
-    for (int K = 1; K <= n; ++K) {
-      if (!(closed && (K == 1 || K == n))) {
-        const double C = EC(K);
-        const bool neg = is_neg(C);
-        const int cs = rl[(long long)(K - 1) * st] & 7;
-        face_acc(C * (wl1 - wl0), neg, cs, face_ak(C, neg, cs, d.mhde[K - 1], d.bmhde[K - 1], beta), cm1,
-                 c0, c1, c2);
-      }
-      // cell K-1 is final
-      if (K == 1) g0 = cm1;
-      else if (K == 2) g1 = cm1 + d.kap[2 * s + 0] * g0;
-      else if (K == 3) lam[st] = cm1 + d.kap[2 * s + 1] * g1;
-      else lam[(long long)(K - 2) * st] = cm1;
-      const int cn = K + 3;
-      const double lec = (cn <= n) ? ELE(cn) : 0.0;
+    auto face = [&](int K) {
+      const double C = EC(K);
+      const bool neg = is_neg(C);
+      const int cs = rl[(long long)(K - 1) * st] & 7;
+      face_acc(C * (wl1 - wl0), neg, cs, face_ak(C, neg, cs, d.mhde[K - 1], d.bmhde[K - 1], beta), cm1, c0,
+               c1, c2);
+    };
+    auto shift = [&](double lec, double wl) {
       cm1 = c0; c0 = c1; c1 = c2; c2 = lec;
-      wl0 = wl1; wl1 = wl2; wl2 = (cn <= n) ? lec * d.iwe[cn - 1] : 0.0;
+      wl0 = wl1; wl1 = wl2; wl2 = wl;
+    };
+    if (!closed) face(1);
+    const double g0 = cm1;  // cell 0
+    { const double lec = ELE(4); shift(lec, lec * d.iwe[3]); }
+    face(2);
+    const double g1 = fma(d.kap[2 * s + 0], g0, cm1);  // cell 1 (+ kap0 * cell 0)
+    { const double lec = ELE(5); shift(lec, lec * d.iwe[4]); }
+    face(3);
+    lam[st] = fma(d.kap[2 * s + 1], g1, cm1);  // cell 2 (+ kap1 * cell 1)
+    { const double lec = ELE(6); shift(lec, lec * d.iwe[5]); }
+    int K = 4;
+    for (; K <= n - 3; ++K) {
+      face(K);
+      lam[(long long)(K - 2) * st] = cm1;
+      const double lec = ELE(K + 3);
+      shift(lec, lec * d.iwe[K + 2]);
     }
-    lam[(long long)(n - 1) * st] = cm1;  // cell NE (NE >= 4)
+    for (; K <= n - 1; ++K) {
+      face(K);
+      lam[(long long)(K - 2) * st] = cm1;
+      shift(0.0, 0.0);
+    }
+    if (!closed) face(n);
+    lam[(long long)(n - 2) * st] = cm1;
+    lam[(long long)(n - 1) * st] = c0;
     lam[0] = out1;
 #undef EC
 #undef ELE
@@ -287,7 +309,8 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
 
 // ----------------------------------------------------------------- DRIFTMU^T
 // Cells 1..NPA: G(1) = F(2); faces 2..NPA-2; FBND(NPA-1) = F(NPA) (0 when
-// closed); cells 2..NPA-1 updated; then F2(NPA) = F2new(NPA-1)*rho.
+// closed); cells 2..NPA-1 updated; then F2(NPA) = F2new(NPA-1)*rho
+// (NPA >= 9).
 __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa;
   const int nlines = (nr - 1) * nt * ne;
@@ -316,35 +339,50 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
     const double out1 = lam[0];
     // le(NPA-1) takes rho * lambda(NPA) (F2(NPA) = F2new(NPA-1)*rho)
     const double leNm = (rl[(long long)(n - 2) * st] & kClipBit)
-                            ? 0.0 : lam[(long long)(n - 2) * st] + d.rho[fij] * lam[(long long)(n - 1) * st];
-#define MLV(L) ((L) == n - 1 ? leNm : MLE(L))
-    double le2 = MLV(2), le3 = MLV(3), le4 = MLV(4);
+                            ? 0.0 : fma(d.rho[fij], lam[(long long)(n - 1) * st], lam[(long long)(n - 2) * st]);
+    const double le2 = MLE(2), le3 = MLE(3), le4 = MLE(4);
     double wl0 = le2 * d.iwmu[1], wl1 = le3 * d.iwmu[2], wl2 = le4 * d.iwmu[3];
     double cm1 = 0.0, c0 = le2, c1 = le3, c2 = le4;
-    double gb1 = 0.0;
-    for (int L = 2; L <= n - 2; ++L) {
+    auto face = [&](int L) {
       const double C = MC(L);
       const bool neg = is_neg(C);
       const int cs = rl[(long long)(L - 1) * st] & 7;
       face_acc(C * (wl1 - wl0), neg, cs, face_ak(C, neg, cs, d.mhdmu[L - 1], d.bmhdmu[L - 1], beta), cm1,
                c0, c1, c2);
-      if (L == 2) gb1 = cm1;                              // cell 1 -> cell 2 (G(1) = F(2))
-      else if (L == 3) lam[st] = cm1 + gb1;
-      else lam[(long long)(L - 2) * st] = cm1;
-      const int cn = L + 3;
-      const double lec = (cn <= n - 1) ? MLV(cn) : 0.0;
+    };
+    auto shift = [&](double lec, double wl) {
       cm1 = c0; c0 = c1; c1 = c2; c2 = lec;
-      wl0 = wl1; wl1 = wl2; wl2 = (cn <= n - 1) ? lec * d.iwmu[cn - 1] : 0.0;
+      wl0 = wl1; wl1 = wl2; wl2 = wl;
+    };
+    face(2);
+    const double gb1 = cm1;  // cell 1 -> cell 2 (G(1) = F(2))
+    { const double lec = MLE(5); shift(lec, lec * d.iwmu[4]); }
+    face(3);
+    lam[st] = cm1 + gb1;
+    { const double lec = MLE(6); shift(lec, lec * d.iwmu[5]); }
+    int L = 4;
+    for (; L <= n - 5; ++L) {
+      face(L);
+      lam[(long long)(L - 2) * st] = cm1;
+      const double lec = MLE(L + 3);
+      shift(lec, lec * d.iwmu[L + 2]);
     }
-    // window: cells NPA-2, NPA-1, NPA
-    if (!closed) c1 += MC(n - 1) * (-wl0);  // FBND(NPA-1) = F(NPA): Pb(NPA-1) = -le(NPA-1)/WMU
+    face(n - 4);  // cell NPA-1 enters
+    lam[(long long)(n - 6) * st] = cm1;
+    shift(leNm, leNm * d.iwmu[n - 2]);
+    for (L = n - 3; L <= n - 2; ++L) {
+      face(L);
+      lam[(long long)(L - 2) * st] = cm1;
+      shift(0.0, 0.0);
+    }
+    // window: cells NPA-2, NPA-1, NPA; FBND(NPA-1) = F(NPA): Pb(NPA-1) = -le(NPA-1)/WMU
+    if (!closed) c1 -= MC(n - 1) * wl0;
     lam[(long long)(n - 3) * st] = cm1;
     lam[(long long)(n - 2) * st] = c0;
     lam[(long long)(n - 1) * st] = c1;
     lam[0] = out1;
 #undef MC
 #undef MLE
-#undef MLV
   }
 }
 
