@@ -292,6 +292,15 @@ int ramgpu_adj_digest(ramgpu_ctx *ctx, unsigned long long *digest);
  * clipped (diagnostics).  Available until a ramgpu_adj_backward that had to
  * recompute earlier segments (more than one segment) replaces it. */
 int ramgpu_adj_record(ramgpu_ctx *ctx, int call, unsigned char *out);
+/* The last window run again from the current F2 with every limiter branch
+ * and clip taken from the record (the frozen-limiter scheme that
+ * ramgpu_adj_backward differentiates, which is affine in F2 and FGEOS):
+ * J[n_members] of that run; F2 ends at the window's end.  Needs every call's
+ * record, i.e. ramgpu_adj_forward with k_ckpt >= ncalls.  With the recorded
+ * F2 it reproduces the recorded run bit for bit; it exists to check the
+ * adjoint by finite differences on long windows, where unfrozen
+ * perturbations cross limiter kinks. */
+int ramgpu_adj_replay(ramgpu_ctx *ctx, double *J);
 
 /* ---- no-allocation variant --------------------------------------------- */
 

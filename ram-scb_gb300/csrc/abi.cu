@@ -72,7 +72,7 @@ struct ramgpu_ctx {
     std::vector<double> kp;          // ncalls * nm
     double* kp_d = nullptr;          // the same on the device (copied per call device-to-device)
     ObsDev* obs = nullptr;
-    double *fm = nullptr, *J = nullptr, *J2 = nullptr, *ckpt = nullptr;
+    double *fm = nullptr, *fm2 = nullptr, *J = nullptr, *J2 = nullptr, *ckpt = nullptr;
     unsigned char* rec = nullptr;
     unsigned long long* digest = nullptr;
     size_t rec_call = 0;             // bytes of one call's record (8 sweeps)
@@ -296,9 +296,9 @@ static int enqueue_body(ramgpu_ctx* ctx, double dts) {
 
 static void adj_free(ramgpu_ctx* ctx) {
   auto& a = ctx->adj;
-  cudaFree(a.obs); cudaFree(a.fm); cudaFree(a.J); cudaFree(a.J2); cudaFree(a.ckpt);
+  cudaFree(a.obs); cudaFree(a.fm); cudaFree(a.fm2); cudaFree(a.J); cudaFree(a.J2); cudaFree(a.ckpt);
   cudaFree(a.rec); cudaFree(a.digest); cudaFree(a.kp_d);
-  a.obs = nullptr; a.fm = a.J = a.J2 = a.ckpt = a.kp_d = nullptr; a.rec = nullptr; a.digest = nullptr;
+  a.obs = nullptr; a.fm = a.fm2 = a.J = a.J2 = a.ckpt = a.kp_d = nullptr; a.rec = nullptr; a.digest = nullptr;
   a.ready = false;
 }
 
@@ -322,6 +322,27 @@ static int enqueue_call_rec(ramgpu_ctx* ctx, double dts, unsigned char* rec) {
   launch_moments(ctx->d, ctx->stream);
   ctx->launches += 15;
   CKL("recorded ram_run");
+  return RAMGPU_OK;
+}
+
+// One ram_run call with every sweep taking its branches and clips from rec
+// (the frozen-limiter scheme of a recorded call, applied to the current F2).
+static int enqueue_call_replay(ramgpu_ctx* ctx, double dts, unsigned char* rec) {
+  const size_t isz = (size_t)ctx->d.nitems * ctx->d.ncell;
+  launch_member_coef(ctx->d, dts, ctx->stream);
+  launch_ghost(ctx->d, ctx->stream);
+  launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 0 * isz, true);
+  launch_sweep_p(ctx->d, dts, false, ctx->stream, rec + 1 * isz, true);
+  launch_sweep_e(ctx->d, dts, false, ctx->stream, rec + 2 * isz, true);
+  launch_sweep_mu(ctx->d, dts, false, 1, ctx->d.loss2, ctx->stream, rec + 3 * isz, true);
+  launch_sweep_mu(ctx->d, dts, false, 0, nullptr, ctx->stream, rec + 4 * isz, true);
+  launch_sweep_e(ctx->d, dts, false, ctx->stream, rec + 5 * isz, true);
+  launch_sweep_p(ctx->d, dts, false, ctx->stream, rec + 6 * isz, true);
+  launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 7 * isz, true);
+  launch_finish(ctx->d, ctx->stream);
+  launch_moments(ctx->d, ctx->stream);
+  ctx->launches += 12;
+  CKL("replayed ram_run");
   return RAMGPU_OK;
 }
 
@@ -1181,6 +1202,7 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
   ok = ok && cudaMalloc(&a.rec, a.rec_call * kseg) == cudaSuccess;
   ok = ok && cudaMalloc(&a.obs, sizeof(ObsDev) * (nobs > 0 ? nobs : 1)) == cudaSuccess;
   ok = ok && cudaMalloc(&a.fm, sizeof(double) * (nobs > 0 ? nobs : 1)) == cudaSuccess;
+  ok = ok && cudaMalloc(&a.fm2, sizeof(double) * (nobs > 0 ? nobs : 1)) == cudaSuccess;
   ok = ok && cudaMalloc(&a.J, sizeof(double) * nm) == cudaSuccess;
   ok = ok && cudaMalloc(&a.J2, sizeof(double) * nm) == cudaSuccess;
   ok = ok && cudaMalloc(&a.digest, sizeof(unsigned long long)) == cudaSuccess;
@@ -1264,6 +1286,30 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
   CK(cudaStreamSynchronize(ctx->stream));
   if (grad_f2) CK(cudaMemcpy(grad_f2, d.lam, sizeof(double) * nslot * d.ncell, cudaMemcpyDefault));
   if (grad_fgeos) CK(cudaMemcpy(grad_fgeos, d.gfg, sizeof(double) * nslot * nfg, cudaMemcpyDefault));
+  return RAMGPU_OK;
+}
+
+int ramgpu_adj_replay(ramgpu_ctx* ctx, double* J) {
+  if (check_ctx(ctx) || !J) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  auto& a = ctx->adj;
+  if (!a.ready) return fail(ctx, RAMGPU_ERR_STATE, "ramgpu_adj_forward must run first");
+  if (a.nseg != 1 || a.rec_stale)
+    return fail(ctx, RAMGPU_ERR_STATE, "replay needs every call's record: ramgpu_adj_forward with k_ckpt >= ncalls");
+  if (ctx->items_dirty || a.items_version != ctx->items_version)
+    return fail(ctx, RAMGPU_ERR_STATE, "active members/species changed since ramgpu_adj_forward");
+  int rc = prepare(ctx, a.dts);
+  if (rc) return rc;
+  Dev& d = ctx->d;
+  const int nm = ctx->cfg.n_members;
+  CK(cudaMemsetAsync(a.J2, 0, sizeof(double) * nm, ctx->stream));
+  for (int c = 0; c < a.ncalls; ++c) {
+    if ((rc = adj_set_kp(ctx, c))) return rc;
+    if ((rc = enqueue_call_replay(ctx, a.dts, a.rec + (size_t)c * a.rec_call))) return rc;
+    launch_obs_fwd(d, a.obs, a.nobs, c, a.fm2, a.J2, ctx->stream);
+    ctx->launches += 1;
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(J, a.J2, sizeof(double) * nm, cudaMemcpyDeviceToHost));
   return RAMGPU_OK;
 }
 

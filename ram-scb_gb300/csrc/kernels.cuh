@@ -48,11 +48,16 @@ __device__ __forceinline__ int stale_ghost_src(const Dev& d, int m, int slot, in
   return d.plane_carry_src[(long long)slot * d.ne * d.npa + (long long)k * d.npa + l];
 }
 
-void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr);
-void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr);
-void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr);
+// rec: branch record of the sweep, written (replay false) or, with replay
+// true, read back to run the sweep with those branches and clips frozen.
+void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr,
+                    bool replay = false);
+void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr,
+                    bool replay = false);
+void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr,
+                    bool replay = false);
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
-                     cudaStream_t st, unsigned char* rec = nullptr);
+                     cudaStream_t st, unsigned char* rec = nullptr, bool replay = false);
 
 int sweep_max_blocks_per_sm(int w, int blk);
 

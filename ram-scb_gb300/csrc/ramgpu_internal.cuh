@@ -168,6 +168,17 @@ __device__ __forceinline__ double face_value_case(double x, double bx, double d,
 }
 constexpr int kClipBit = 8;  // recorded with the case: the updated cell was clipped
 
+// Face value with the branch taken from a record (frozen-limiter replay):
+// LIMITER*X = beta*D | X | D | beta*X for cases 1..4, FUP for case 0.  For
+// the recorded branch this equals face_value_case bit for bit.
+__device__ __forceinline__ double face_value_frozen(double x, double d, double fup, double a, double beta,
+                                                    int cs) {
+  const double lx = cs == 1 ? beta * d : cs == 2 ? x : cs == 3 ? d : beta * x;
+  return cs ? fma(a, lx, fup) : fup;
+}
+// F2 < 0 -> 1e-15 applied as recorded
+__device__ __forceinline__ double clip_frozen(double v, unsigned char r) { return (r & kClipBit) ? 1E-15 : v; }
+
 // Running CFL quotient max(|C|, floor) as bits (integer max).
 __device__ __forceinline__ unsigned long long cfl_bits(double c, unsigned long long floor_bits) {
   return umax64(dbits(c) & kAbsMask, floor_bits);

@@ -18,7 +18,7 @@ namespace ramgpu {
 
 // ----------------------------------------------------------------- DRIFTR
 // Line (J,K,L) along I = 1..NR.  Faces 2..NR-1 (and NR on inflow lines).
-template <bool kCfl, bool kRec>
+template <bool kCfl, int kRec>
 __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = nt * ne * d.npa;
@@ -75,11 +75,13 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
         const bool neg = is_neg(c);
         const double a = fma(c, -0.5, neg ? -0.5 : 0.5);
         int cs;
-        const double fb = face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
+        const double fb = (kRec == 2)
+            ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = rl[f - 1] & 7)
+            : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         const double phi = c * fb;
         const double raw = (g0 - phi) + phi_prev;
-        fl[f - 1] = clip(raw);
-        if (kRec) rl[f - 1] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
+        fl[f - 1] = (kRec == 2) ? clip_frozen(raw, rl[f - 1]) : clip(raw);
+        if (kRec == 1) rl[f - 1] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         gm = g0; g0 = gp; gp = gpp;
         xm = x; bxm = bx; x = xp; bx = bxp;
@@ -92,13 +94,14 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
         fbn = g0;
       } else {
         const double xp = g2 - g1, bxp = beta * fabs(xp);
-        fbn = face_value_case(x, bx, xp, bxp, g1, fma(cN, -0.5, -0.5), csn);
+        fbn = (kRec == 2) ? face_value_frozen(x, xp, g1, fma(cN, -0.5, -0.5), beta, csn = rl[nr - 1] & 7)
+                          : face_value_case(x, bx, xp, bxp, g1, fma(cN, -0.5, -0.5), csn);
       }
       if (closed) fbn = 0.0;
       const double phin = cN * fbn;
       const double rawn = (g0 - phin) + phi_prev;
-      fl[nr - 1] = clip(rawn);
-      if (kRec) rl[nr - 1] = (unsigned char)(csn | (is_neg(rawn) ? kClipBit : 0));
+      fl[nr - 1] = (kRec == 2) ? clip_frozen(rawn, rl[nr - 1]) : clip(rawn);
+      if (kRec == 1) rl[nr - 1] = (unsigned char)(csn | (is_neg(rawn) ? kClipBit : 0));
     }
     if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 0], q);
   }
@@ -106,7 +109,7 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
 
 // ----------------------------------------------------------------- DRIFTP
 // Line (I,K,L), I = 2..NR, along J = 1..NT, periodic with J=1 == J=NT.
-template <bool kCfl, bool kRec>
+template <bool kCfl, int kRec>
 __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * ne * d.npa;
@@ -148,7 +151,9 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
       {
         const bool neg = is_neg(cN);
         const double a = fma(cN, -0.5, neg ? -0.5 : 0.5);
-        phiN = cN * face_value_case(XN, bXN, neg ? X2 : XNm, neg ? bX2 : bXNm, neg ? G2 : GN, a, csN);
+        phiN = cN * ((kRec == 2)
+            ? face_value_frozen(XN, neg ? X2 : XNm, neg ? G2 : GN, a, beta, csN = rl[(long long)(nt - 1) * st] & 7)
+            : face_value_case(XN, bXN, neg ? X2 : XNm, neg ? bX2 : bXNm, neg ? G2 : GN, a, csN));
       }
       double phi_prev = phiN;
       double g0 = G2, gp = G3, xm = X1, bxm = bX1, x = X2, bx = bX2;
@@ -171,20 +176,23 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
         const bool neg = is_neg(c);
         const double a = fma(c, -0.5, neg ? -0.5 : 0.5);
         int cs;
-        const double fb = face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
+        const unsigned char* rj = kRec ? rl + (long long)(J - 1) * st : nullptr;
+        const double fb = (kRec == 2)
+            ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rj & 7)
+            : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         const double phi = c * fb;
         const double raw = (g0 - phi) + phi_prev;
-        GJ(J) = clip(raw);
-        if (kRec) rl[(long long)(J - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
+        GJ(J) = (kRec == 2) ? clip_frozen(raw, *rj) : clip(raw);
+        if (kRec == 1) rl[(long long)(J - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         g0 = gp; gp = gpp;
         xm = x; bxm = bx; x = xp; bx = bxp;
       }
       const double rawN = (GN - phiN) + phi_prev;
-      const double vN = clip(rawN);
+      const double vN = (kRec == 2) ? clip_frozen(rawN, rl[(long long)(nt - 1) * st]) : clip(rawN);
       GJ(nt) = vN;
       GJ(1) = vN;
-      if (kRec) rl[(long long)(nt - 1) * st] = (unsigned char)(csN | (is_neg(rawN) ? kClipBit : 0));
+      if (kRec == 1) rl[(long long)(nt - 1) * st] = (unsigned char)(csN | (is_neg(rawN) ? kClipBit : 0));
   #undef GJ
   #undef CJ
     }
@@ -195,7 +203,7 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
 // ----------------------------------------------------------------- DRIFTE
 // Line (I,J,L), I = 2..NR, along K = 1..NE with extrapolated F(0), F(1)
 // and F(NE+1) = F(NE+2) = 0.  Cell K = 1 is never written.
-template <bool kCfl, bool kRec>
+template <bool kCfl, int kRec>
 __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * nt * d.npa;
@@ -243,9 +251,10 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
         const bool neg = is_neg(c);
         const double a = fma(c, mhde[0], neg ? -0.5 : 0.5);
         int cs;
-        double fb = face_value_case(X1, bX1, neg ? X2 : X0, neg ? bX2 : bX0, neg ? G2 : G1, a, cs);
+        double fb = (kRec == 2) ? face_value_frozen(X1, neg ? X2 : X0, neg ? G2 : G1, a, beta, cs = rl[0] & 7)
+                                : face_value_case(X1, bX1, neg ? X2 : X0, neg ? bX2 : bX0, neg ? G2 : G1, a, cs);
         if (closed) fb = 0.0;
-        if (kRec) rl[0] = (unsigned char)cs;
+        if (kRec == 1) rl[0] = (unsigned char)cs;
         phi_prev = c * fb;
       }
       double g0 = G2, gp = G3, xm = X1, bxm = bX1, x = X2, bx = bX2;
@@ -257,12 +266,14 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
         const bool neg = is_neg(c);
         const double a = fma(c, mhde[K - 1], neg ? -0.5 : 0.5);
         int cs;
-        double fb = face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
+        const unsigned char* rk = kRec ? rl + (long long)(K - 1) * st : nullptr;
+        double fb = (kRec == 2) ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rk & 7)
+                                : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         if (closed && K == ne) fb = 0.0;
         const double phi = c * fb;
         const double raw = fma(phi_prev - phi, iwe[K - 1], g0);
-        GK(K) = clip(raw);
-        if (kRec) rl[(long long)(K - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
+        GK(K) = (kRec == 2) ? clip_frozen(raw, *rk) : clip(raw);
+        if (kRec == 1) rl[(long long)(K - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         g0 = gp; gp = gpp;
         xm = x; bxm = bx; x = xp; bx = bxp;
@@ -279,7 +290,7 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
 // faces 2..NPA-2, FBND(NPA-1) = F(NPA), then the F2(NPA) extrapolation.
 // kLoss: 0 none, 1 multiply the result by table lossA (loss after the sweep),
 //        2 multiply the input by lossA (loss before the sweep).
-template <bool kCfl, int kLoss, bool kRec>
+template <bool kCfl, int kLoss, int kRec>
 __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const double* __restrict__ lossA,
                                                    unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa;
@@ -331,11 +342,13 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         const bool neg = is_neg(c);
         const double a = fma(c, mhdmu[L - 1], neg ? -0.5 : 0.5);
         int cs;
-        const double fb = face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
+        const unsigned char* rq = kRec ? rl + (long long)(L - 1) * st : nullptr;
+        const double fb = (kRec == 2) ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rq & 7)
+                                      : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         const double phi = c * fb;
         const double raw = fma(phi_prev - phi, iwmu[L - 1], g0);
-        if (kRec) rl[(long long)(L - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
-        double v = clip(raw);
+        if (kRec == 1) rl[(long long)(L - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
+        double v = (kRec == 2) ? clip_frozen(raw, *rq) : clip(raw);
         if (kLoss == 1) v *= LA(L);
         GL(L) = v;
         phi_prev = phi;
@@ -349,8 +362,8 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
         const double phi = c * (closed ? 0.0 : gp);
         const double raw = fma(phi_prev - phi, iwmu[L - 1], g0);
-        if (kRec) rl[(long long)(L - 1) * st] = (unsigned char)(is_neg(raw) ? kClipBit : 0);
-        const double v = clip(raw);
+        if (kRec == 1) rl[(long long)(L - 1) * st] = (unsigned char)(is_neg(raw) ? kClipBit : 0);
+        const double v = (kRec == 2) ? clip_frozen(raw, rl[(long long)(L - 1) * st]) : clip(raw);
         const double vN = v * d.rho[fij];
         if (kLoss == 1) {
           GL(L) = v * LA(L);
@@ -384,40 +397,47 @@ static inline int nlines_of(const Dev& d, int w) {
   }
 }
 
-void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec) {
+void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay) {
   dim3 g = grid_for(d, 0, nlines_of(d, 0));
-  if (rec) k_sweep_r<false, true><<<g, d.blk[0], 0, st>>>(d, dts, rec);
-  else if (cfl) k_sweep_r<true, false><<<g, d.blk[0], 0, st>>>(d, dts, nullptr);
-  else k_sweep_r<false, false><<<g, d.blk[0], 0, st>>>(d, dts, nullptr);
+  if (rec && replay) k_sweep_r<false, 2><<<g, d.blk[0], 0, st>>>(d, dts, rec);
+  else if (rec) k_sweep_r<false, 1><<<g, d.blk[0], 0, st>>>(d, dts, rec);
+  else if (cfl) k_sweep_r<true, 0><<<g, d.blk[0], 0, st>>>(d, dts, nullptr);
+  else k_sweep_r<false, 0><<<g, d.blk[0], 0, st>>>(d, dts, nullptr);
 }
-void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec) {
+void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay) {
   dim3 g = grid_for(d, 1, nlines_of(d, 1));
-  if (rec) k_sweep_p<false, true><<<g, d.blk[1], 0, st>>>(d, dts, rec);
-  else if (cfl) k_sweep_p<true, false><<<g, d.blk[1], 0, st>>>(d, dts, nullptr);
-  else k_sweep_p<false, false><<<g, d.blk[1], 0, st>>>(d, dts, nullptr);
+  if (rec && replay) k_sweep_p<false, 2><<<g, d.blk[1], 0, st>>>(d, dts, rec);
+  else if (rec) k_sweep_p<false, 1><<<g, d.blk[1], 0, st>>>(d, dts, rec);
+  else if (cfl) k_sweep_p<true, 0><<<g, d.blk[1], 0, st>>>(d, dts, nullptr);
+  else k_sweep_p<false, 0><<<g, d.blk[1], 0, st>>>(d, dts, nullptr);
 }
-void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec) {
+void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay) {
   dim3 g = grid_for(d, 2, nlines_of(d, 2));
-  if (rec) k_sweep_e<false, true><<<g, d.blk[2], 0, st>>>(d, dts, rec);
-  else if (cfl) k_sweep_e<true, false><<<g, d.blk[2], 0, st>>>(d, dts, nullptr);
-  else k_sweep_e<false, false><<<g, d.blk[2], 0, st>>>(d, dts, nullptr);
+  if (rec && replay) k_sweep_e<false, 2><<<g, d.blk[2], 0, st>>>(d, dts, rec);
+  else if (rec) k_sweep_e<false, 1><<<g, d.blk[2], 0, st>>>(d, dts, rec);
+  else if (cfl) k_sweep_e<true, 0><<<g, d.blk[2], 0, st>>>(d, dts, nullptr);
+  else k_sweep_e<false, 0><<<g, d.blk[2], 0, st>>>(d, dts, nullptr);
 }
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
-                     cudaStream_t st, unsigned char* rec) {
+                     cudaStream_t st, unsigned char* rec, bool replay) {
   dim3 g = grid_for(d, 3, nlines_of(d, 3));
   const int b = d.blk[3];
-  if (rec) {
-    if (loss_mode == 1) k_sweep_mu<false, 1, true><<<g, b, 0, st>>>(d, dts, loss, rec);
-    else if (loss_mode == 2) k_sweep_mu<false, 2, true><<<g, b, 0, st>>>(d, dts, loss, rec);
-    else k_sweep_mu<false, 0, true><<<g, b, 0, st>>>(d, dts, nullptr, rec);
+  if (rec && replay) {
+    if (loss_mode == 1) k_sweep_mu<false, 1, 2><<<g, b, 0, st>>>(d, dts, loss, rec);
+    else if (loss_mode == 2) k_sweep_mu<false, 2, 2><<<g, b, 0, st>>>(d, dts, loss, rec);
+    else k_sweep_mu<false, 0, 2><<<g, b, 0, st>>>(d, dts, nullptr, rec);
+  } else if (rec) {
+    if (loss_mode == 1) k_sweep_mu<false, 1, 1><<<g, b, 0, st>>>(d, dts, loss, rec);
+    else if (loss_mode == 2) k_sweep_mu<false, 2, 1><<<g, b, 0, st>>>(d, dts, loss, rec);
+    else k_sweep_mu<false, 0, 1><<<g, b, 0, st>>>(d, dts, nullptr, rec);
   } else if (cfl) {
-    if (loss_mode == 1) k_sweep_mu<true, 1, false><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-    else if (loss_mode == 2) k_sweep_mu<true, 2, false><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-    else k_sweep_mu<true, 0, false><<<g, b, 0, st>>>(d, dts, nullptr, nullptr);
+    if (loss_mode == 1) k_sweep_mu<true, 1, 0><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+    else if (loss_mode == 2) k_sweep_mu<true, 2, 0><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+    else k_sweep_mu<true, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr, nullptr);
   } else {
-    if (loss_mode == 1) k_sweep_mu<false, 1, false><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-    else if (loss_mode == 2) k_sweep_mu<false, 2, false><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-    else k_sweep_mu<false, 0, false><<<g, b, 0, st>>>(d, dts, nullptr, nullptr);
+    if (loss_mode == 1) k_sweep_mu<false, 1, 0><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+    else if (loss_mode == 2) k_sweep_mu<false, 2, 0><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+    else k_sweep_mu<false, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr, nullptr);
   }
 }
 
@@ -426,10 +446,10 @@ int sweep_max_blocks_per_sm(int w, int blk) {
   int n = 0;
   cudaError_t e = cudaSuccess;
   switch (w) {
-    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_r<false, false>, blk, 0); break;
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_p<false, false>, blk, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_e<false, false>, blk, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_mu<false, 0, false>, blk, 0); break;
+    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_r<false, 0>, blk, 0); break;
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_p<false, 0>, blk, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_e<false, 0>, blk, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_mu<false, 0, 0>, blk, 0); break;
   }
   return e == cudaSuccess ? n : 0;
 }

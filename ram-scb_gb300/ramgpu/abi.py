@@ -34,7 +34,7 @@ EXPORTS = (
     "ramgpu_sumrc_noalloc", "ramgpu_set_graph", "ramgpu_set_launch_shape",
     "ramgpu_get_launch_shape", "ramgpu_autotune", "ramgpu_set_kp_all",
     "ramgpu_adj_forward", "ramgpu_adj_backward", "ramgpu_adj_digest", "ramgpu_adj_record",
-    "ramgpu_fly_sats", "ramgpu_sum_pressure",
+    "ramgpu_fly_sats", "ramgpu_sum_pressure", "ramgpu_adj_replay",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
@@ -133,6 +133,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_adj_digest": ([vp, C.POINTER(C.c_ulonglong)], i),
         "ramgpu_adj_record": ([vp, i, C.POINTER(C.c_ubyte)], i),
         "ramgpu_fly_sats": ([vp, C.POINTER(SatStruct), i, dp, dp], i),
+        "ramgpu_adj_replay": ([vp, dp], i),
         "ramgpu_sum_pressure": ([vp, i, dp, dp], i),
     }
     for name, (args, res) in sig.items():
@@ -405,6 +406,13 @@ class RamGpu:
         self._ck(self.lib.ramgpu_adj_record(self.h, int(call), out.ctypes.data_as(C.POINTER(C.c_ubyte))),
                  "adj_record")
         return out
+
+    def adj_replay(self) -> np.ndarray:
+        """J per member of the last window replayed from the current F2 with
+        the recorded branches frozen (needs k_ckpt >= ncalls)."""
+        J = np.zeros(self.n_members)
+        self._ck(self.lib.ramgpu_adj_replay(self.h, _dptr(J)), "adj_replay")
+        return J
 
     def adj_digest(self) -> int:
         v = C.c_ulonglong()

@@ -290,3 +290,48 @@ def test_autograd_function_matches_c_abi(tiny):
                 assert np.max(np.abs(gbt[m, s].transpose(2, 1, 0) - refb)) <= 1e-13 * max(np.max(np.abs(refb)), 1e-300)
     finally:
         model.close()
+
+
+def test_frozen_replay_and_finite_differences(tiny):
+    """ramgpu_adj_replay reruns the window with the recorded branches frozen:
+    from the same F2 it reproduces the recorded run bit for bit, and since
+    the frozen scheme is affine in F2 and FGEOS its J is smooth, so central
+    differences with large steps agree with the adjoint to 1e-8 whatever
+    kinks the unfrozen scheme would cross."""
+    model, kp, obs = make_case(tiny, 1, 4, 30, seed=12, outer=10)
+    ns = len(tiny.grid.species)
+    try:
+        J0 = model.adj_forward(4, tiny.dts, kp, 4, obs)[0]
+        end = [model.download_f2(0, s) for s in range(ns)]
+        gf, gb = model.adj_backward()
+        _set_f2(model, tiny, [1.0] * ns)
+        Jr = model.adj_replay()[0]
+        assert abs(Jr - J0) <= 1e-14 * J0
+        for s in range(ns):
+            assert np.array_equal(model.download_f2(0, s), end[s])
+        rng = np.random.Generator(np.random.PCG64(8))
+        for use_f2 in (True, False):
+            for _ in range(3):
+                shp = [(tiny.f2[s] if use_f2 else tiny.fgeos[s]).shape for s in range(ns)]
+                r = [rng.uniform(-1.0, 1.0, size=shp[s]) for s in range(ns)]
+                base = tiny.f2 if use_f2 else tiny.fgeos
+                grad = gf[0] if use_f2 else gb[0]
+                ad = sum(float(np.sum(grad[s] * np.asarray(base[s]) * r[s])) for s in range(ns))
+                jj = []
+                eps = 1e-4
+                for sign in (1.0, -1.0):
+                    for s in range(ns):
+                        x = np.asarray(base[s]) * (1.0 + sign * eps * r[s])
+                        if use_f2:
+                            model.upload_f2(0, s, x)
+                        else:
+                            model.upload_f2(0, s, tiny.f2[s])
+                            model.set_boundary(0, s, x)
+                    jj.append(model.adj_replay()[0])
+                err = abs((jj[0] - jj[1]) / (2 * eps) - ad) / abs(ad)
+                print("frozen FD", "F2" if use_f2 else "FGEOS", f"{err:.2e}")
+                assert err <= 1e-8, err
+        for s in range(ns):
+            model.set_boundary(0, s, tiny.fgeos[s])
+    finally:
+        model.close()
