@@ -36,6 +36,11 @@ UNIT = "cell-updates/s"
 # the source: coefficient, a-term, X, beta|X|, face fma, flux, two update ops;
 # DRIFTE's coefficient is two ops; the CFL-tracking forward E/MU add one.
 FP64_OPS_PER_FACE = {"driftr": 8, "driftp": 8, "drifte": 9.5, "driftmu": 8.5}
+# DRAM bytes (read + write) per launch of each sweep on the four-species
+# standard grid, from one ncu capture (profiles/sweeps_four_sp.md, current
+# kernels): F2 is read once; the written lines stay in L2 within a launch,
+# and k_sweep_mu also reads the fused CEX/ATMOL factor.
+NCU_DRAM_BYTES = {"four_sp": {"driftr": 44.3e6, "driftp": 40.6e6, "drifte": 39.8e6, "driftmu": 81.7e6}}
 
 
 def parse():
@@ -617,7 +622,8 @@ def run_gb300(args, rank, world, local_rank):
                    "graph": not args.no_graph, "launch_shapes": shapes,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None, "kernel": dom,
+                     "frac": achieved / hbm_peak,
+                     "traffic": NCU_DRAM_BYTES.get(args.workload, {}).get(dom), "kernel": dom,
                      "kernel_ms": dom_ms, "peak_kind": peak_kind,
                      "fp64": {"achieved": fp64, "peak": fp64_peak, "unit": "G lane-ops/s",
                               "frac": fp64 / fp64_peak, "ops_per_face": FP64_OPS_PER_FACE[dom],

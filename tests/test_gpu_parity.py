@@ -116,7 +116,7 @@ def test_half_step(tiny, order):
         assert rel(gpu.download_f2(0, s), ref) <= TOL, (order, s)
 
 
-def _compare_ram_run(wl, kp, steps=1, flags=0, dts=None):
+def _compare_ram_run(wl, kp, steps=1, flags=0, dts=None, nthreads=1):
     g = wl.grid
     dts = wl.dts if dts is None else dts
     o = pyoracle.Oracle(g, wl.fields)
@@ -128,7 +128,7 @@ def _compare_ram_run(wl, kp, steps=1, flags=0, dts=None):
         for s in range(len(g.species)):
             gpu.upload_f2(0, s, ref[s])
         gpu.ram_run(dts)
-        out = o.ram_run(ref, wl.fgeos, dts, kp=kp, want_flux=True)
+        out = o.ram_run(ref, wl.fgeos, dts, kp=kp, want_flux=True, nthreads=nthreads)
         # the scheme is run inside its stability limit, as the reference's
         # driver ensures through DtsNext (src/ModRamScbRun.f90:49-61)
         assert dts <= out["dts_next"] / 0.8 + 1e-12
@@ -155,6 +155,17 @@ def test_ram_run_four_species_tiny(tiny):
 
 def test_ram_run_four_species_full(four):
     _compare_ram_run(four, 2.0, steps=2)
+
+
+def test_ram_run_refined_grid():
+    """The refined 40x49x70x144 grid (19.8 M cells per species, 632 MB of F2
+    for the four species, larger than L2): one full ram_run step."""
+    wl = W.make_workload("refined")
+    pyoracle.set_inner_threads(4)
+    try:
+        _compare_ram_run(wl, 3.0, steps=1, nthreads=4)
+    finally:
+        pyoracle.set_inner_threads(1)
 
 
 def test_strong_convection_inflow_mix(four):
