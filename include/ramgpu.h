@@ -266,7 +266,8 @@ typedef struct {
 /* Forward pass of a window of ncalls ram_run calls of length dts from the
  * current F2, with Kp of call c and member m in kp[c*n_members + m] (VOLS).
  * Saves a checkpoint of F2 every k_ckpt calls, evaluates J per member into
- * J[n_members] and leaves F2 at the end of the window.  Every limiter branch
+ * J[n_members] and leaves F2 at the end of the window (the moments are
+ * those of the window's last call).  Every limiter branch
  * and clip is recorded; ramgpu_adj_digest returns a digest of the pattern.
  * Allocates its checkpoint and record buffers (k_ckpt*8 bytes per cell and
  * item for the record). */

@@ -304,7 +304,7 @@ static void adj_free(ramgpu_ctx* ctx) {
 
 // One ram_run call with every sweep recording its branches into rec
 // (8 instances of nitems*ncell bytes: R,P,E,MU forward, MU,E,P,R reverse).
-static int enqueue_call_rec(ramgpu_ctx* ctx, double dts, unsigned char* rec) {
+static int enqueue_call_rec(ramgpu_ctx* ctx, double dts, unsigned char* rec, bool moments) {
   const size_t isz = (size_t)ctx->d.nitems * ctx->d.ncell;
   // positions no sweep writes (e.g. cell 1 of a DRIFTR line) stay zero
   CK(cudaMemsetAsync(rec, 0, 8 * isz, ctx->stream));
@@ -319,8 +319,9 @@ static int enqueue_call_rec(ramgpu_ctx* ctx, double dts, unsigned char* rec) {
   launch_sweep_p(ctx->d, dts, false, ctx->stream, rec + 6 * isz);
   launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 7 * isz);
   launch_finish(ctx->d, ctx->stream);
-  launch_moments(ctx->d, ctx->stream);
-  ctx->launches += 15;
+  if (moments) launch_moments(ctx->d, ctx->stream);
+  else launch_anisch_state(ctx->d, ctx->stream);
+  ctx->launches += moments ? 15 : 14;
   CKL("recorded ram_run");
   return RAMGPU_OK;
 }
@@ -340,7 +341,7 @@ static int enqueue_call_replay(ramgpu_ctx* ctx, double dts, unsigned char* rec) 
   launch_sweep_p(ctx->d, dts, false, ctx->stream, rec + 6 * isz, true);
   launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 7 * isz, true);
   launch_finish(ctx->d, ctx->stream);
-  launch_moments(ctx->d, ctx->stream);
+  launch_anisch_state(ctx->d, ctx->stream);
   ctx->launches += 12;
   CKL("replayed ram_run");
   return RAMGPU_OK;
@@ -1222,7 +1223,7 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
       if ((rc = adj_copy_items(ctx, a.ckpt + (size_t)(c / k_ckpt) * d.nitems * d.ncell, true))) return rc;
     if ((rc = adj_set_kp(ctx, c))) return rc;
     unsigned char* r = a.rec + (size_t)(c % k_ckpt) * a.rec_call;
-    if ((rc = enqueue_call_rec(ctx, dts, r))) return rc;
+    if ((rc = enqueue_call_rec(ctx, dts, r, c == ncalls - 1))) return rc;
     launch_digest(r, (long long)a.rec_call, a.digest, ctx->stream);
     launch_obs_fwd(d, a.obs, nobs, c, a.fm, a.J, ctx->stream);
     ctx->launches += 2;
@@ -1258,7 +1259,7 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
       if ((rc = adj_copy_items(ctx, a.ckpt + (size_t)seg * isz, false))) return rc;
       for (int c = c0; c < c1; ++c) {
         if ((rc = adj_set_kp(ctx, c))) return rc;
-        if ((rc = enqueue_call_rec(ctx, a.dts, a.rec + (size_t)(c - c0) * a.rec_call))) return rc;
+        if ((rc = enqueue_call_rec(ctx, a.dts, a.rec + (size_t)(c - c0) * a.rec_call, false))) return rc;
       }
     }
     for (int c = c1 - 1; c >= c0; --c) {  // transpose call c

@@ -55,10 +55,11 @@ __device__ __forceinline__ void face_acc(double FBb, bool neg, int cs, double ak
 // ak = LIMITER weight times the CORR factor a = -0.5*(C*q - s) of a face:
 // fma(C, -0.5*k*q, 0.5*k*s) with k = beta for cases 1, 4 and 1 otherwise
 // (q = 1 for R and P; -0.5*q comes from the -0.5/DE, -0.5/DMU tables).
-__device__ __forceinline__ double face_ak(double C, bool neg, int cs, double mh, double bmh, double beta) {
+__device__ __forceinline__ double face_ak(double C, bool neg, int cs, double mh, double bmh, double hb) {
   const bool kb = (cs == 1) | (cs == 4);
-  const double hk = kb ? 0.5 * beta : 0.5;
-  return fma(C, kb ? bmh : mh, neg ? -hk : hk);
+  const double hk = kb ? hb : 0.5;  // hb = 0.5*beta
+  const double shk = __longlong_as_double(__double_as_longlong(hk) ^ (neg ? (long long)kSignMask : 0LL));
+  return fma(C, kb ? bmh : mh, shk);
 }
 
 // lambda of cell c of a line (stride st) masked by the clip bit
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(128) k_adj_r(Dev d, const unsigned char* __res
     const double* grt = d.grt + ((long long)l * nt + j) * nr;
     const double* cr = d.cr + ((long long)m * nt + j) * nr;
     const double p4 = d.p4[s * ne + k];
-    const double beta = d.betalim, bmh = -0.5 * beta;
+    const double hb = 0.5 * d.betalim, bmh = -hb;
     const bool closed = d.flags & 1u;
     const int n = nr;  // >= 4
     const double cN = fma(grt[n - 1], p4, cr[n - 1]);
@@ -107,7 +108,7 @@ __global__ void __launch_bounds__(128) k_adj_r(Dev d, const unsigned char* __res
     auto face = [&](int f, double C) {
       const bool neg = is_neg(C);
       const int cs = rl[f - 1] & 7;
-      face_acc(C * (le1 - le0), neg, cs, face_ak(C, neg, cs, -0.5, bmh, beta), cm1, c0, c1, c2);
+      face_acc(C * (le1 - le0), neg, cs, face_ak(C, neg, cs, -0.5, bmh, hb), cm1, c0, c1, c2);
     };
     auto advance = [&](int f, double le3) {  // cell f-1 is final; cell f+3 enters
       lam[f - 2] = cm1;
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
     const double* gpt = d.gpt + ((long long)l * nt) * nr + i;
     const double* ca = d.ca + ((long long)m * nt) * nr + i;
     const double p2 = d.p2[((long long)s * ne + k) * nr + i];
-    const double beta = d.betalim, bmh = -0.5 * beta;
+    const double hb = 0.5 * d.betalim, bmh = -hb;
     const int n = nt;
 #define PC(J) fma(gpt[(long long)((J)-1) * nr], p2, ca[(long long)((J)-1) * nr])
 #define PLE(J) masked(lam, rl, (long long)((J)-1) * st)
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
       const bool neg = is_neg(C);
       const int cs = rl[(long long)(n - 2) * st] & 7;
       const double FBb = C * (leN - leNm);
-      const double V = face_ak(C, neg, cs, -0.5, bmh, beta) * FBb;
+      const double V = face_ak(C, neg, cs, -0.5, bmh, hb) * FBb;
       if (neg) tN += FBb; else tNm1 += FBb;
       if (cs == 2 || cs == 4) { tN += V; tNm1 -= V; }
       else if (cs && !neg) { tNm1 += V; tNm2 -= V; }
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
       const bool neg = is_neg(C);
       const int cs = rl[(long long)(n - 1) * st] & 7;
       const double FBb = C * (le2 - leN);  // Pb(NT) = -le(NT) + Pb(1), Pb(1) = le(2)
-      const double V = face_ak(C, neg, cs, -0.5, bmh, beta) * FBb;
+      const double V = face_ak(C, neg, cs, -0.5, bmh, hb) * FBb;
       if (neg) w2 += FBb; else tN += FBb;
       if (cs == 2 || cs == 4) { w2 += V; tN -= V; }
       else if (cs && !neg) { tN += V; tNm1 -= V; }
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
       const double C = PC(J);
       const bool neg = is_neg(C);
       const int cs = rl[(long long)(J - 1) * st] & 7;
-      face_acc(C * (le1 - le0), neg, cs, face_ak(C, neg, cs, -0.5, bmh, beta), cm1, c0, c1, c2);
+      face_acc(C * (le1 - le0), neg, cs, face_ak(C, neg, cs, -0.5, bmh, hb), cm1, c0, c1, c2);
       lam[(long long)(J - 2) * st] = cm1;
       cm1 = c0; c0 = c1; c1 = c2; c2 = add;
       le0 = le1; le1 = lnext; lnext = lec;
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
     const double ue = d.ue[(long long)m * nr * nt * d.npa + fij];
     const double* edot = d.edot + (long long)s * ne * nr + i;
     const double* eb = d.eb + s * ne;
-    const double beta = d.betalim;
+    const double hb = 0.5 * d.betalim;
     const bool closed = d.flags & 1u;
     const int n = ne;
 #define EC(K) (edot[(long long)((K)-1) * nr] * fma(eb[(K)-1], wet, ue))
@@ -270,7 +271,7 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
       const double C = EC(K);
       const bool neg = is_neg(C);
       const int cs = rl[(long long)(K - 1) * st] & 7;
-      face_acc(C * (wl1 - wl0), neg, cs, face_ak(C, neg, cs, d.mhde[K - 1], d.bmhde[K - 1], beta), cm1, c0,
+      face_acc(C * (wl1 - wl0), neg, cs, face_ak(C, neg, cs, d.mhde[K - 1], d.bmhde[K - 1], hb), cm1, c0,
                c1, c2);
     };
     auto shift = [&](double lec, double wl) {
@@ -331,7 +332,7 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
     const double* wm = d.wm + fij;
     const double* um = d.um + (long long)m * nt * nr * npa + fij;
     const double ekv = d.ek[s * ne + jk / nt];
-    const double beta = d.betalim;
+    const double hb = 0.5 * d.betalim;
     const bool closed = d.flags & 1u;
     const int n = npa;
 #define MC(L) fma(ekv, wm[(long long)((L)-1) * sij], um[(long long)((L)-1) * sij])
@@ -347,7 +348,7 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
       const double C = MC(L);
       const bool neg = is_neg(C);
       const int cs = rl[(long long)(L - 1) * st] & 7;
-      face_acc(C * (wl1 - wl0), neg, cs, face_ak(C, neg, cs, d.mhdmu[L - 1], d.bmhdmu[L - 1], beta), cm1,
+      face_acc(C * (wl1 - wl0), neg, cs, face_ak(C, neg, cs, d.mhdmu[L - 1], d.bmhdmu[L - 1], hb), cm1,
                c0, c1, c2);
     };
     auto shift = [&](double lec, double wl) {

@@ -69,6 +69,7 @@ void launch_ghost(const Dev& d, cudaStream_t st);
 void launch_loss_apply(const Dev& d, const double* table, cudaStream_t st);
 void launch_finish(const Dev& d, cudaStream_t st);
 void launch_moments(const Dev& d, cudaStream_t st);
+void launch_anisch_state(const Dev& d, cudaStream_t st);
 void launch_sumrc(const Dev& d, double* part, int nblk, cudaStream_t st);
 void launch_flux(const Dev& d, int slot, int s, double* out, cudaStream_t st);
 

@@ -583,6 +583,28 @@ void launch_moments(const Dev& d, cudaStream_t st) {
   k_moments_reduce<<<dim3((n2 + 3) / 4, d.nitems), 128, 0, st>>>(d);
 }
 
+// ANISCH's only effect on F2, F2(I,J,K,1) = F2(I,J,K,2) for I, K >= 2
+// (src/ModRamRun.f90:366), for runs that need the state but not the
+// moments (the adjoint's forward and recomputation passes).
+__global__ void k_anisch_state(Dev d) {
+  const int nr1 = d.nr - 1, ne1 = d.ne - 1;
+  const long long n = (long long)nr1 * d.nt * ne1;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int2 item = d.items[blockIdx.y];
+  const int slot = item.x * d.ns + item.y;
+  const int i = 1 + (int)(t % nr1);
+  const int j = (int)((t / nr1) % d.nt);
+  const int k = 1 + (int)(t / ((long long)nr1 * d.nt));
+  double* f = d.f2 + (long long)slot * d.ncell + ((long long)k * d.nt + j) * d.nr + i;
+  f[0] = f[(long long)d.ne * d.nt * d.nr];
+}
+
+void launch_anisch_state(const Dev& d, cudaStream_t st) {
+  const long long n = (long long)(d.nr - 1) * d.nt * (d.ne - 1);
+  k_anisch_state<<<dim3((unsigned)((n + 255) / 256), d.nitems), 256, 0, st>>>(d);
+}
+
 // ------------------------------------------------------------------ SUMRC
 // Per-block partial sums of EKEV*F2*WE*WMU over I=2..NR, J=1..NT-1,
 // K=2..NE, L=2..NPA (src/ModRamRun.f90:246-255).  part: (nitems, nblk).
