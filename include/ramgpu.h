@@ -107,6 +107,17 @@ int ramgpu_set_fields(ramgpu_ctx *ctx, const double *fnhs, const double *fnis,
                       const double *didt, const double *dibndt, const double *bnes,
                       const double *dbdt, const double *eir, const double *eip,
                       const int *outside_mgnp);
+/* Implicit pitch-angle diffusion of species s, the scheme WPADIF
+ * (src/ModRamWPI.f90:643-714) and FLCscatter (src/ModRamLoss.f90:512-575)
+ * share, with coefficient daa = D(I,J,K,L) (NR,NT,NE,NPA), host or device
+ * memory: ATAW+ATAC for electrons (chorus and hiss), ATAW_emic_h +
+ * ATAW_emic_he for EMIC, FLC_coef(S,:,:,:,:) for FLC.  While a coefficient
+ * is set, ramgpu_ram_run applies the diffusion to species s after the
+ * forward drifts and again before the reverse ones, where ram_run calls
+ * WPADIF (src/ModRamRun.f90:91-107,144-158); RAMGPU_OP_PADIF applies it
+ * once.  daa = NULL removes it.  The adjoint does not cover it. */
+int ramgpu_set_pa_diffusion(ramgpu_ctx *ctx, int s, const double *daa);
+
 /* GEOSB output FGEOS(S,:,:,:) of one species (src/ModRamBoundary.f90:241-319):
  * (NT,NE,NPA), host or device memory.  member < 0 sets it for every member. */
 int ramgpu_set_boundary(ramgpu_ctx *ctx, int member, int s, const double *fgeos_s);
@@ -163,6 +174,7 @@ int ramgpu_ram_run_async(ramgpu_ctx *ctx, double dts);
 #define RAMGPU_OP_CHAREXCHANGE 4
 #define RAMGPU_OP_ATMOL 5
 #define RAMGPU_OP_ANISCH 6
+#define RAMGPU_OP_PADIF 7   /* one implicit pitch-angle diffusion (WPADIF / FLCscatter) */
 int ramgpu_apply_op(ramgpu_ctx *ctx, double dts, int op, int cfl);
 
 /* ---- outputs ------------------------------------------------------------- */
@@ -179,6 +191,9 @@ int ramgpu_cfl(ramgpu_ctx *ctx, int member, int s, double *out5);
  * accumulated since the last ramgpu_reset_losses, which zeroes the losses
  * and takes SETRC of the current state as the starting ENOLD.  out: 4 doubles. */
 int ramgpu_losses(ramgpu_ctx *ctx, int member, int s, double *out4);
+/* LSWAE (src/ModRamRun.f90:99,106,150,157): the ELORC of the pitch-angle
+ * diffusion accumulated since the last ramgpu_reset_losses. */
+int ramgpu_loss_wae(ramgpu_ctx *ctx, int member, int s, double *lswae);
 int ramgpu_reset_losses(ramgpu_ctx *ctx);
 
 /* Virtual spacecraft on the equatorial plane.  FLUX of the current state

@@ -50,7 +50,7 @@ class RoDriftPara(C.Structure):
 
 class RoLosses(C.Structure):
     _fields_ = [("setrc", C.c_double), ("lsdr", C.c_double), ("lscha", C.c_double),
-                ("lsatm", C.c_double)]
+                ("lsatm", C.c_double), ("lswae", C.c_double)]
 
 
 def build(force: bool = False) -> Path:
@@ -92,6 +92,9 @@ def load():
         lib.ro_ram_run.argtypes = [gp, C.c_int, sp, pp, C.c_double, _P, _P, PP, PP, PP, PP, PP,
                                    C.POINTER(RoLosses), _P, C.c_int]
         lib.ro_half_step.argtypes = [gp, sp, pp, dpp, _P, _P, _P, _P, _P, C.c_int]
+        lib.ro_ram_run2.argtypes = [gp, C.c_int, sp, pp, C.c_double, _P, _P, PP, PP, PP, PP, PP,
+                                    C.POINTER(RoLosses), _P, C.c_int, PP]
+        lib.ro_padif.argtypes = [gp, pp, _P, _P]
         U8 = C.POINTER(C.c_ubyte)
         lib.ro_driftr_rec.argtypes = [gp, sp, pp, dpp, _P, _P, _P, _P, U8, _IP]
         lib.ro_driftr_rec.restype = C.c_double
@@ -215,6 +218,11 @@ class Oracle:
         fn = {"P": self.lib.ro_driftp, "E": self.lib.ro_drifte, "MU": self.lib.ro_driftmu}[which]
         return fn(*args, _p(f2), cd)
 
+    def padif(self, f2, daa, dts):
+        """WPADIF / FLCscatter on one species (Fortran array, in place)."""
+        p = self.params(dts)
+        self.lib.ro_padif(C.byref(self.rg), C.byref(p), _p(_f(daa)), _p(f2))
+
     def cepara(self, s, dts, do_atmol=True):
         g = self.grid
         charge = np.zeros((g.nr, g.nt, g.ne, g.npa), order="F")
@@ -247,9 +255,11 @@ class Oracle:
                               _p(vt), _p(_f(fgeos)), _p(charge), _p(atlos), _p(f2), int(order))
 
     def ram_run(self, f2s, fgeos, dts, kp=None, vt=None, closed=False, do_atmol=True,
-                losses=None, want_flux=False, nthreads=1, species=None):
+                losses=None, want_flux=False, nthreads=1, species=None, daa=None):
         """One ram_run call over the species in ``species`` (default all);
-        f2s/fgeos are lists indexed by species."""
+        f2s/fgeos are lists indexed by species.  daa: optional {species:
+        pitch-angle diffusion coefficient (NR,NT,NE,NPA)}, applied as WPADIF
+        on both sides of the loss processes."""
         g = self.grid
         idx = list(range(self.ns)) if species is None else list(species)
         n = len(idx)
@@ -269,14 +279,16 @@ class Oracle:
             for t, s in enumerate(idx):
                 ls[t].setrc, ls[t].lsdr, ls[t].lscha, ls[t].lsatm = losses[s]
         dn = C.c_double()
-        self.lib.ro_ram_run(C.byref(self.rg), n, sp_arr, C.byref(p), float(kp if kp is not None else 0.0),
-                            _p(vt_in), _p(vt_out), PArr(*[_p(a) for a in fg]),
-                            PArr(*[_p(f2s[s]) for s in idx]), PArr(*[_p(a) for a in pe]),
-                            PArr(*[_p(a) for a in pa]), PArr(*[_p(a) for a in fl]) if fl else None,
-                            ls, C.byref(dn), int(nthreads))
+        dl = [_f(daa[s]) if daa is not None and s in daa else None for s in idx]
+        self.lib.ro_ram_run2(C.byref(self.rg), n, sp_arr, C.byref(p), float(kp if kp is not None else 0.0),
+                             _p(vt_in), _p(vt_out), PArr(*[_p(a) for a in fg]),
+                             PArr(*[_p(f2s[s]) for s in idx]), PArr(*[_p(a) for a in pe]),
+                             PArr(*[_p(a) for a in pa]), PArr(*[_p(a) for a in fl]) if fl else None,
+                             ls, C.byref(dn), int(nthreads), PArr(*[_p(a) for a in dl]))
         out = {"vt": vt_out, "ppert": dict(zip(idx, pe)), "ppart": dict(zip(idx, pa)),
                "dts_next": dn.value,
-               "losses": {s: (ls[t].setrc, ls[t].lsdr, ls[t].lscha, ls[t].lsatm) for t, s in enumerate(idx)}}
+               "losses": {s: (ls[t].setrc, ls[t].lsdr, ls[t].lscha, ls[t].lsatm) for t, s in enumerate(idx)},
+               "lswae": {s: ls[t].lswae for t, s in enumerate(idx)}}
         if fl:
             out["flux"] = dict(zip(idx, fl))
         return out

@@ -838,6 +838,18 @@ int ro_ram_run(const ro_grid *g, int ns, const ro_species *sp_all, const ro_para
                double *const *ppert, double *const *ppart, double *const *flux,
                ro_losses *losses, double *dts_next, int nthreads)
 {
+    return ro_ram_run2(g, ns, sp_all, p, kp, vt_in, vt_out, fgeos, f2s, ppert, ppart, flux, losses,
+                       dts_next, nthreads, NULL);
+}
+
+void ro_padif(const ro_grid *g, const ro_params *p, const double *daa, double *f2);
+
+int ro_ram_run2(const ro_grid *g, int ns, const ro_species *sp_all, const ro_params *p,
+                double kp, const double *vt_in, double *vt_out,
+                const double *const *fgeos, double *const *f2s,
+                double *const *ppert, double *const *ppart, double *const *flux,
+                ro_losses *losses, double *dts_next, int nthreads, const double *const *daa)
+{
     size_t nvt = (size_t)(NR + 1) * NT;
     double *vt = (double *)malloc(sizeof(double) * nvt);
     if (vt_in)
@@ -864,13 +876,18 @@ int ro_ram_run(const ro_grid *g, int ns, const ro_species *sp_all, const ro_para
         ro_cepara(g, sp, p, charge, atlos);
         ro_driftpara(g, sp, p, dp);
         double setrc = losses ? losses[iS].setrc : 0., s1;
-        double lsdr = 0., lscha = 0., lsatm = 0.;
+        double lsdr = 0., lscha = 0., lsatm = 0., lswae = 0.;
         /* forward half */
         dtr[iS * 4 + 0] = ro_driftr(g, sp, p, dp, vt, fgeos[iS], f2, NULL);
         dtr[iS * 4 + 1] = ro_driftp(g, sp, p, dp, vt, f2, NULL);
         dtr[iS * 4 + 2] = ro_drifte(g, sp, p, dp, vt, f2, NULL);
         dtr[iS * 4 + 3] = ro_driftmu(g, sp, p, dp, vt, f2, NULL);
         s1 = ro_sumrc(g, f2); lsdr += setrc - s1; setrc = s1;
+        const double *dps = daa ? daa[iS] : NULL;
+        if (dps) { /* WPADIF after the drifts (src/ModRamRun.f90:91-107) */
+            ro_padif(g, p, dps, f2);
+            s1 = ro_sumrc(g, f2); lswae += setrc - s1; setrc = s1;
+        }
         if (sp->cex_kind) {
             ro_charexchange(g, f2, charge);
             s1 = ro_sumrc(g, f2); lscha += setrc - s1; setrc = s1;
@@ -886,6 +903,10 @@ int ro_ram_run(const ro_grid *g, int ns, const ro_species *sp_all, const ro_para
             ro_charexchange(g, f2, charge);
             s1 = ro_sumrc(g, f2); lscha += setrc - s1; setrc = s1;
         }
+        if (dps) { /* and before the reverse drifts (src/ModRamRun.f90:144-158) */
+            ro_padif(g, p, dps, f2);
+            s1 = ro_sumrc(g, f2); lswae += setrc - s1; setrc = s1;
+        }
         ro_driftmu(g, sp, p, dp, vt, f2, NULL);
         ro_drifte(g, sp, p, dp, vt, f2, NULL);
         ro_driftp(g, sp, p, dp, vt, f2, NULL);
@@ -896,6 +917,7 @@ int ro_ram_run(const ro_grid *g, int ns, const ro_species *sp_all, const ro_para
             losses[iS].lsdr += lsdr;
             losses[iS].lscha += lscha;
             losses[iS].lsatm += lsatm;
+            losses[iS].lswae += lswae;
         }
         free_dp(dp);
         free(charge);
@@ -1118,4 +1140,60 @@ void ro_driftmu_adj(const ro_grid *g, const ro_params *p, const double *cd, cons
     free(Gb);
     free(FBb);
     free(lv);
+}
+
+/* ---------------------------------------------------- implicit PA diffusion
+ * WPADIF (src/ModRamWPI.f90:643-714) and FLCscatter (src/ModRamLoss.f90:
+ * 512-575) share one implicit scheme; daa is their coefficient, D(I,J,K,L):
+ * ATAW+ATAC for electrons, ATAW_emic_h+ATAW_emic_he for EMIC, FLC_coef(S,..)
+ * for FLC.  The diagnostic file written when a row is not diagonally
+ * dominant is left out. */
+void ro_padif(const ro_grid *g, const ro_params *p, const double *daa, double *f2)
+{
+    const double DTs = p->dts;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_inner)
+#endif
+    {
+        double *F = (double *)calloc((size_t)NPA + 1, sizeof(double));
+        double *RK = (double *)calloc((size_t)NPA + 1, sizeof(double));
+        double *RL = (double *)calloc((size_t)NPA + 1, sizeof(double));
+        double *FACMU = (double *)calloc((size_t)NPA + 1, sizeof(double));
+#define D(I, J, K, L) daa[IX4(I, J, K, L)]
+#ifdef _OPENMP
+#pragma omp for collapse(2) schedule(static)
+#endif
+        for (int J = 1; J <= NT; ++J)
+            for (int I = 2; I <= NR; ++I)
+                for (int K = 2; K <= NE; ++K) {
+                    for (int L = 2; L <= NPA; ++L) {
+                        FACMU[L] = FNHS(I, J, L) * MU(L);
+                        F[L] = F2(I, J, K, L) / FACMU[L];
+                    }
+                    FACMU[1] = FNHS(I, J, 1) * MU(1);
+                    F[1] = F[2];
+                    RK[1] = 0.;
+                    RL[1] = -1.;
+                    for (int L = 2; L <= NPA - 1; ++L) {
+                        double AN = D(I, J, K, L) / DMU(L);
+                        double GN = D(I, J, K, L - 1) / DMU(L - 1);
+                        AN = AN * DTs / FACMU[L] / WMU(L);
+                        GN = GN * DTs / FACMU[L] / WMU(L);
+                        double BN = AN + GN;
+                        double RP = F[L];
+                        double DENOM = BN + GN * RL[L - 1] + 1;
+                        RK[L] = (RP + GN * RK[L - 1]) / DENOM;
+                        RL[L] = -AN / DENOM;
+                    }
+                    F2(I, J, K, NPA - 1) = RK[NPA - 1] / (1 + RL[NPA - 1]);
+                    for (int L = NPA - 2; L >= 1; --L) F2(I, J, K, L) = RK[L] - RL[L] * F2(I, J, K, L + 1);
+                    F2(I, J, K, NPA) = F2(I, J, K, NPA - 1);
+                    for (int L = 1; L <= NPA; ++L) F2(I, J, K, L) = F2(I, J, K, L) * FACMU[L];
+                }
+#undef D
+        free(F);
+        free(RK);
+        free(RL);
+        free(FACMU);
+    }
 }

@@ -80,6 +80,7 @@ typedef struct {
 typedef struct {
     double setrc;               /* SETRC after the call */
     double lsdr, lscha, lsatm;  /* ELORC accumulated into LSDR/LSCHA/LSATM */
+    double lswae;               /* ELORC of the pitch-angle diffusion (LSWAE) */
 } ro_losses;
 
 /* Threads for the loops over independent lines inside each routine
@@ -133,6 +134,20 @@ int ro_ram_run(const ro_grid *g, int ns, const ro_species *sp, const ro_params *
                const double *const *fgeos, double *const *f2,
                double *const *ppert, double *const *ppart, double *const *flux,
                ro_losses *losses, double *dts_next, int nthreads);
+
+/* ro_ram_run with WPADIF (src/ModRamRun.f90:91-107,144-158) for every
+ * species s with daa[s] != NULL (daa may be NULL): daa[s] is the
+ * pitch-angle diffusion coefficient D(I,J,K,L) of ro_padif. */
+int ro_ram_run2(const ro_grid *g, int ns, const ro_species *sp, const ro_params *p,
+                double kp, const double *vt_in, double *vt_out,
+                const double *const *fgeos, double *const *f2,
+                double *const *ppert, double *const *ppart, double *const *flux,
+                ro_losses *losses, double *dts_next, int nthreads, const double *const *daa);
+
+/* Implicit pitch-angle diffusion of WPADIF (src/ModRamWPI.f90:643-714) and
+ * FLCscatter (src/ModRamLoss.f90:512-575), one species in place, with
+ * coefficient daa = D(I,J,K,L) (NR,NT,NE,NPA). */
+void ro_padif(const ro_grid *g, const ro_params *p, const double *daa, double *f2);
 
 /* One DTs half of ram_run for one species (the measurement "step"):
  * order 0 = R,P,E,MU,[CEX],[ATMOL]; order 1 = [ATMOL],[CEX],MU,E,P,R.

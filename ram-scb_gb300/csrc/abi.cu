@@ -25,7 +25,7 @@ using namespace ramgpu;
 namespace {
 thread_local std::string g_create_error;
 constexpr int kSumrcBlocks = 64;
-constexpr int kSumrcStages = 7;
+constexpr int kSumrcStages = 9;  // 0-5 ram_run, 6-7 pitch-angle diffusion, 8 reset
 }  // namespace
 
 struct ramgpu_ctx {
@@ -45,6 +45,11 @@ struct ramgpu_ctx {
   bool have_grid = false, have_fields = false;
   bool field_dirty = true, static_dirty = true;
   double tables_dts = -1.0;
+  // implicit pitch-angle diffusion: species with a coefficient, tables state
+  std::vector<int> pd_on_h;
+  bool pd_alloc = false, pd_dirty = false;
+  double pd_dts = -1.0;
+  int pd_any() const { for (int v : pd_on_h) if (v) return 1; return 0; }
   int any_outside = 0;
   double last_dts = 0.0;
   // loss bookkeeping on the device: per slot {SETRC, LSDR, LSCHA, LSATM, valid}
@@ -193,6 +198,7 @@ static int prepare(ramgpu_ctx* ctx, double dts) {
     ctx->field_dirty = false;
     ctx->static_dirty = true;
     ctx->tables_dts = -1.0;
+    ctx->pd_dirty = true;
   }
   if (ctx->static_dirty) {
     launch_species_static(ctx->d, ctx->stream);
@@ -207,6 +213,13 @@ static int prepare(ramgpu_ctx* ctx, double dts) {
     CKL("dts tables");
     ctx->tables_dts = dts;
   }
+  if (ctx->pd_any() && (ctx->pd_dirty || ctx->pd_dts != dts)) {
+    launch_padif_tables(ctx->d, dts, ctx->stream);
+    ctx->launches += 2;
+    CKL("pitch-angle diffusion tables");
+    ctx->pd_dirty = false;
+    ctx->pd_dts = dts;
+  }
   if (ctx->items_dirty) {
     int rc = rebuild_items(ctx);
     if (rc) return rc;
@@ -215,7 +228,8 @@ static int prepare(ramgpu_ctx* ctx, double dts) {
 }
 
 // SUMRC of every item into stage buffer `stage`, then fold into the device
-// accumulators: which = -1 (set SETRC only), 1 LSDR, 2 LSCHA, 3 LSATM.
+// accumulators: which = -1 (set SETRC only), 1 LSDR, 2 LSCHA, 3 LSATM,
+// 5 LSWAE (index 4 marks a valid SETRC).
 __global__ void k_losses_fold(Dev d, const double* part, int nblk, double* losses, int which) {
   const int it = blockIdx.x * blockDim.x + threadIdx.x;
   if (it >= d.nitems) return;
@@ -223,7 +237,7 @@ __global__ void k_losses_fold(Dev d, const double* part, int nblk, double* losse
   const int slot = item.x * d.ns + item.y;
   double s = 0.0;
   for (int b = 0; b < nblk; ++b) s += part[(long long)it * nblk + b];
-  double* L = losses + (long long)slot * 5;
+  double* L = losses + (long long)slot * 6;
   if (which >= 1 && L[4] != 0.0) L[which] += L[0] - s;  // ELORC = ENOLD - SETRC
   L[0] = s;
   L[4] = 1.0;
@@ -268,13 +282,27 @@ static int enqueue_body(ramgpu_ctx* ctx, double dts) {
   ctx->launches += 5;
   CKL("member tables");
   const bool losses = ctx->cfg.flags & RAMGPU_FLAG_LOSSES;
-  if (!losses) {
+  const bool pd = ctx->pd_any();
+  if (!losses && !pd) {
     // R,P,E,MU then CEX,ATMOL,ATMOL,CEX folded into the MU store
     if ((rc = enqueue_forward(ctx, dts, true, ctx->d.loss2))) return rc;
+    if ((rc = enqueue_reverse(ctx, dts, false, nullptr))) return rc;
+  } else if (!losses) {
+    // R,P,E,MU, WPADIF, CEX,ATMOL,ATMOL,CEX (folded into WPADIF's store), WPADIF, MU,E,P,R
+    if ((rc = enqueue_forward(ctx, dts, false, nullptr))) return rc;
+    { Timed t(ctx, 9); launch_padif(ctx->d, ctx->d.loss2, ctx->stream); }
+    { Timed t(ctx, 9); launch_padif(ctx->d, nullptr, ctx->stream); }
+    ctx->launches += 2;
+    CKL("pitch-angle diffusion");
     if ((rc = enqueue_reverse(ctx, dts, false, nullptr))) return rc;
   } else {
     if ((rc = enqueue_forward(ctx, dts, false, nullptr))) return rc;
     if ((rc = sumrc_stage(ctx, 0, 1))) return rc;
+    if (pd) {
+      { Timed t(ctx, 9); launch_padif(ctx->d, nullptr, ctx->stream); }
+      ctx->launches += 1;
+      if ((rc = sumrc_stage(ctx, 6, 5))) return rc;
+    }
     { Timed t(ctx, 9); launch_loss_apply(ctx->d, ctx->d.charge, ctx->stream); }
     if ((rc = sumrc_stage(ctx, 1, 2))) return rc;
     { Timed t(ctx, 9); launch_loss_apply(ctx->d, ctx->d.atm, ctx->stream); }
@@ -284,6 +312,11 @@ static int enqueue_body(ramgpu_ctx* ctx, double dts) {
     { Timed t(ctx, 9); launch_loss_apply(ctx->d, ctx->d.charge, ctx->stream); }
     if ((rc = sumrc_stage(ctx, 4, 2))) return rc;
     ctx->launches += 4;
+    if (pd) {
+      { Timed t(ctx, 9); launch_padif(ctx->d, nullptr, ctx->stream); }
+      ctx->launches += 1;
+      if ((rc = sumrc_stage(ctx, 7, 5))) return rc;
+    }
     if ((rc = enqueue_reverse(ctx, dts, false, nullptr))) return rc;
     if ((rc = sumrc_stage(ctx, 5, 1))) return rc;
   }
@@ -509,7 +542,7 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   d.ppert = dalloc<double>(ctx, nslot * nr * nt, &ok);
   d.ppart = dalloc<double>(ctx, nslot * nr * nt, &ok);
   ctx->items_d = dalloc<int2>(ctx, nslot, &ok);
-  ctx->losses = dalloc<double>(ctx, nslot * 5, &ok);
+  ctx->losses = dalloc<double>(ctx, nslot * 6, &ok);
   ctx->sumrc_part = dalloc<double>(ctx, (size_t)kSumrcStages * nslot * kSumrcBlocks, &ok);
   if (!ok) {
     ramgpu_destroy(ctx);
@@ -673,6 +706,33 @@ int ramgpu_set_boundary(ramgpu_ctx* ctx, int member, int s, const double* fgeos_
   return RAMGPU_OK;
 }
 
+int ramgpu_set_pa_diffusion(ramgpu_ctx* ctx, int s, const double* daa) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (s < 0 || s >= ctx->cfg.ns) return fail(ctx, RAMGPU_ERR_ARG, "species out of range");
+  Dev& d = ctx->d;
+  if (ctx->pd_on_h.empty()) ctx->pd_on_h.assign(d.ns, 0);
+  if (daa && !ctx->pd_alloc) {
+    bool ok = true;
+    d.pd_on = dalloc<int>(ctx, d.ns, &ok);
+    d.pd_d = dalloc<double>(ctx, (size_t)d.ns * d.ncell, &ok);
+    d.pd_gn = dalloc<double>(ctx, (size_t)d.ns * d.ncell, &ok);
+    d.pd_inv = dalloc<double>(ctx, (size_t)d.ns * d.ncell, &ok);
+    d.pd_rl = dalloc<double>(ctx, (size_t)d.ns * d.ncell, &ok);
+    d.pd_fac = dalloc<double>(ctx, (size_t)d.nr * d.nt * d.npa, &ok);
+    d.pd_ifac = dalloc<double>(ctx, (size_t)d.nr * d.nt * d.npa, &ok);
+    if (!ok) return fail(ctx, RAMGPU_ERR_NOMEM, "pitch-angle diffusion tables: device allocation failed");
+    ctx->pd_alloc = true;
+  }
+  if (daa)
+    CK(cudaMemcpy((void*)(d.pd_d + (size_t)s * d.ncell), daa, sizeof(double) * d.ncell, cudaMemcpyDefault));
+  ctx->pd_on_h[s] = daa ? 1 : 0;
+  if (ctx->pd_alloc)
+    CK(cudaMemcpy((void*)d.pd_on, ctx->pd_on_h.data(), sizeof(int) * d.ns, cudaMemcpyHostToDevice));
+  ctx->pd_dirty = true;
+  ctx->shape_version += 1;  // the ram_run launch sequence changes: recapture the graph
+  return RAMGPU_OK;
+}
+
 int ramgpu_set_potential(ramgpu_ctx* ctx, int member, const double* vt) {
   if (check_ctx(ctx) || !vt) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
   if (int rc = check_ms(ctx, member, 0)) return rc;
@@ -818,7 +878,7 @@ int ramgpu_half_step(ramgpu_ctx* ctx, double dts, int order) {
 
 int ramgpu_apply_op(ramgpu_ctx* ctx, double dts, int op, int cfl) {
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
-  if (op < 0 || op > 6) return fail(ctx, RAMGPU_ERR_ARG, "unknown op");
+  if (op < 0 || op > 7) return fail(ctx, RAMGPU_ERR_ARG, "unknown op");
   int rc = prepare(ctx, dts);
   if (rc) return rc;
   ctx->last_dts = dts;
@@ -835,6 +895,7 @@ int ramgpu_apply_op(ramgpu_ctx* ctx, double dts, int op, int cfl) {
     case 4: launch_loss_apply(ctx->d, ctx->d.charge, ctx->stream); break;
     case 5: launch_loss_apply(ctx->d, ctx->d.atm, ctx->stream); break;
     case 6: launch_moments(ctx->d, ctx->stream); ctx->launches += 1; break;
+    case 7: launch_padif(ctx->d, nullptr, ctx->stream); break;
     default: break;
   }
   ctx->launches += 1;
@@ -903,16 +964,25 @@ int ramgpu_cfl(ramgpu_ctx* ctx, int member, int s, double* out5) {
 int ramgpu_losses(ramgpu_ctx* ctx, int member, int s, double* out4) {
   if (check_ctx(ctx) || !out4) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
   if (int rc = check_ms(ctx, member, s)) return rc;
-  double v[5];
+  double v[6];
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaMemcpy(v, ctx->losses + (size_t)(member * ctx->d.ns + s) * 5, sizeof(v), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(v, ctx->losses + (size_t)(member * ctx->d.ns + s) * 6, sizeof(v), cudaMemcpyDeviceToHost));
   for (int i = 0; i < 4; ++i) out4[i] = v[i];
+  return RAMGPU_OK;
+}
+
+int ramgpu_loss_wae(ramgpu_ctx* ctx, int member, int s, double* lswae) {
+  if (check_ctx(ctx) || !lswae) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (int rc = check_ms(ctx, member, s)) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(lswae, ctx->losses + (size_t)(member * ctx->d.ns + s) * 6 + 5, sizeof(double),
+                cudaMemcpyDeviceToHost));
   return RAMGPU_OK;
 }
 
 int ramgpu_reset_losses(ramgpu_ctx* ctx) {
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
-  CK(cudaMemsetAsync(ctx->losses, 0, sizeof(double) * 5 * ctx->d.nm * ctx->d.ns, ctx->stream));
+  CK(cudaMemsetAsync(ctx->losses, 0, sizeof(double) * 6 * ctx->d.nm * ctx->d.ns, ctx->stream));
   // baseline SETRC of the current state (the ENOLD of the next SUMRC)
   if (ctx->have_grid && ctx->have_fields) {
     if (ctx->items_dirty) {
@@ -1164,6 +1234,8 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
   if (ncalls < 1 || k_ckpt < 1 || nobs < 0) return fail(ctx, RAMGPU_ERR_ARG, "ncalls, k_ckpt >= 1, nobs >= 0");
   if (ctx->cfg.flags & RAMGPU_FLAG_LOSSES)
     return fail(ctx, RAMGPU_ERR_ARG, "the adjoint window runs without RAMGPU_FLAG_LOSSES");
+  if (ctx->pd_any())
+    return fail(ctx, RAMGPU_ERR_ARG, "the adjoint does not cover the pitch-angle diffusion");
   Dev& d = ctx->d;
   if (d.nr < 4 || d.nt < 7 || d.ne < 6 || d.npa < 9)
     return fail(ctx, RAMGPU_ERR_ARG, "the adjoint needs NR >= 4, NT >= 7, NE >= 6, NPA >= 9");

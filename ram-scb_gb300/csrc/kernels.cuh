@@ -89,6 +89,10 @@ void launch_obs_adj(const Dev& d, const ObsDev* obs, int nobs, int call, const d
                     cudaStream_t st);
 void launch_digest(const unsigned char* rec, long long n, unsigned long long* out, cudaStream_t st);
 
+// implicit pitch-angle diffusion (padif.cu)
+void launch_padif_tables(const Dev& d, double dts, cudaStream_t st);
+void launch_padif(const Dev& d, const double* loss, cudaStream_t st);
+
 // virtual spacecraft and SCB hand-off (outputs.cu)
 struct SatDev {
   int member;

@@ -71,6 +71,12 @@ struct Dev {
   double *loss1;          // (ns, ncell): CHARGE*ATLOS^(1/FNHS) (one half step)
   double *loss2;          // (ns, ncell): ((CHARGE*ATM)*ATM)*CHARGE (both halves)
   double *charge, *atm;   // (ns, ncell): separate factors for the bookkeeping path
+  // implicit pitch-angle diffusion (WPADIF / FLCscatter): per species the
+  // coefficient D and the elimination tables; FACMU and 1/FACMU (NR,NT,NPA)
+  const int *pd_on;       // (ns): species has a coefficient
+  const double *pd_d;     // (ns, ncell)
+  double *pd_gn, *pd_inv, *pd_rl;  // (ns, ncell)
+  double *pd_fac, *pd_ifac;        // (NR, NT, NPA)
   // per-member VT-dependent tables
   double *kp;             // (nm)
   int *vt_mode;           // (nm): 1 = VOLS from kp, 0 = explicit VT

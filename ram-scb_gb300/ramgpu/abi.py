@@ -34,12 +34,13 @@ EXPORTS = (
     "ramgpu_sumrc_noalloc", "ramgpu_set_graph", "ramgpu_set_launch_shape",
     "ramgpu_get_launch_shape", "ramgpu_autotune", "ramgpu_set_kp_all",
     "ramgpu_adj_forward", "ramgpu_adj_backward", "ramgpu_adj_digest", "ramgpu_adj_record",
-    "ramgpu_fly_sats", "ramgpu_sum_pressure", "ramgpu_adj_replay",
+    "ramgpu_fly_sats", "ramgpu_sum_pressure", "ramgpu_adj_replay", "ramgpu_set_pa_diffusion",
+    "ramgpu_loss_wae",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
           "anisch", "dts_tables", "sumrc")
-OP_DRIFTR, OP_DRIFTP, OP_DRIFTE, OP_DRIFTMU, OP_CHAREXCHANGE, OP_ATMOL, OP_ANISCH = range(7)
+OP_DRIFTR, OP_DRIFTP, OP_DRIFTE, OP_DRIFTMU, OP_CHAREXCHANGE, OP_ATMOL, OP_ANISCH, OP_PADIF = range(8)
 
 
 class RamGpuError(RuntimeError):
@@ -134,6 +135,8 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_adj_record": ([vp, i, C.POINTER(C.c_ubyte)], i),
         "ramgpu_fly_sats": ([vp, C.POINTER(SatStruct), i, dp, dp], i),
         "ramgpu_adj_replay": ([vp, dp], i),
+        "ramgpu_set_pa_diffusion": ([vp, i, dp], i),
+        "ramgpu_loss_wae": ([vp, i, i, dp], i),
         "ramgpu_sum_pressure": ([vp, i, dp, dp], i),
     }
     for name, (args, res) in sig.items():
@@ -323,6 +326,19 @@ class RamGpu:
         pp = np.empty((g.nr, g.nt), order="F")
         self._ck(self.lib.ramgpu_sum_pressure(self.h, int(member), _dptr(pa), _dptr(pp)), "sum_pressure")
         return pa, pp
+
+    def set_pa_diffusion(self, s: int, daa=None):
+        """Pitch-angle diffusion coefficient D(I,J,K,L) of species s (None removes it)."""
+        if daa is None:
+            self._ck(self.lib.ramgpu_set_pa_diffusion(self.h, s, None), "set_pa_diffusion")
+        else:
+            a = _fort(daa)
+            self._ck(self.lib.ramgpu_set_pa_diffusion(self.h, s, _dptr(a)), "set_pa_diffusion")
+
+    def loss_wae(self, member: int, s: int) -> float:
+        v = C.c_double()
+        self._ck(self.lib.ramgpu_loss_wae(self.h, member, s, C.byref(v)), "loss_wae")
+        return v.value
 
     def cfl(self, member: int, s: int) -> np.ndarray:
         a = np.empty(5)

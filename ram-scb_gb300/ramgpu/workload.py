@@ -435,6 +435,23 @@ def boundary_fgeos(g: Grid, s: int, kt=5.0, kappa=3.0, amp=1.0e5, density_scale=
     return out
 
 
+def pa_diffusion(g: Grid, f: Fields, seed: int = 7, d0: float = 2.0e-5) -> np.ndarray:
+    """Synthetic pitch-angle diffusion coefficient D(I,J,K,L) in RAM's form
+    D_mumu*mu*h (the coefficient WPADIF and FLCscatter divide by DMU): a
+    (1-mu^2) profile, decreasing with energy, log-normal in space.  d0 sets
+    the implicit step's off-diagonal weight AN ~ d0*DTs*(1-mu^2)/(DMU*WMU)
+    near O(0.1-1) on the standard grid.  C order (I,J,K,L)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nr, nt, ne, npa = g.nr, g.nt, g.ne, g.npa
+    mu = np.asarray(g.mu)
+    prof = (1.0 - mu ** 2) * mu
+    ek = (np.asarray(g.ekev) / 10.0) ** -0.5
+    d = (d0 * ek[None, None, :, None] * prof[None, None, None, :] * f.fnhs[:nr, :, None, :]
+         * rng.lognormal(0.0, 0.3, size=(nr, nt, ne, npa)))
+    d[:, nt - 1] = d[:, 0]
+    return np.ascontiguousarray(d)
+
+
 def vols_vt(g: Grid, kp: float) -> np.ndarray:
     """VT(I,J), I=1..NR+1 (src/ModRamRun.f90:45-54).  C order (I,J)."""
     t = 1. - 0.159 * kp + 0.0093 * (kp * kp)
