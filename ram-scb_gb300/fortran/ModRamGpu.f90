@@ -29,6 +29,14 @@ module ModRamGpu
      type(c_ptr)    :: grel, grbnd, v, epp, ernh, ffactor
   end type ramgpu_grid
 
+  ! virtual spacecraft position for ramgpu_fly_sats (equatorial)
+  type, bind(C) :: ramgpu_sat
+     integer(c_int) :: member
+     real(c_double) :: lshell, mlt
+  end type ramgpu_sat
+
+  integer(c_int), parameter :: RAMGPU_OP_PADIF = 7
+
   interface
      integer(c_int) function ramgpu_create(cfg, ctx) bind(C, name="ramgpu_create")
        import :: c_int, c_ptr, ramgpu_config
@@ -115,6 +123,59 @@ module ModRamGpu
        type(c_ptr), value :: ctx
        integer(c_int), value :: member, s
        real(c_double), intent(out) :: out5(5)
+     end function
+     integer(c_int) function ramgpu_half_step(ctx, dts, order) bind(C, name="ramgpu_half_step")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), value :: dts
+       integer(c_int), value :: order
+     end function
+     integer(c_int) function ramgpu_apply_op(ctx, dts, op, cfl) bind(C, name="ramgpu_apply_op")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), value :: dts
+       integer(c_int), value :: op, cfl
+     end function
+     integer(c_int) function ramgpu_losses(ctx, member, s, out4) bind(C, name="ramgpu_losses")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member, s
+       real(c_double), intent(out) :: out4(4)
+     end function
+     integer(c_int) function ramgpu_loss_wae(ctx, member, s, lswae) bind(C, name="ramgpu_loss_wae")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member, s
+       real(c_double), intent(out) :: lswae
+     end function
+     integer(c_int) function ramgpu_reset_losses(ctx) bind(C, name="ramgpu_reset_losses")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     ! WPADIF / FLCscatter coefficient of species s (ATAW+ATAC, ATAW_emic_h+
+     ! ATAW_emic_he or FLC_coef(S,:,:,:,:)); pass c_null_ptr through a
+     ! separate interface to remove it
+     integer(c_int) function ramgpu_set_pa_diffusion(ctx, s, daa) &
+          bind(C, name="ramgpu_set_pa_diffusion")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: s
+       real(c_double), intent(in) :: daa(*)
+     end function
+     integer(c_int) function ramgpu_fly_sats(ctx, sats, nsat, sat_flux, omni_flux) &
+          bind(C, name="ramgpu_fly_sats")
+       import :: c_int, c_ptr, c_double, ramgpu_sat
+       type(c_ptr), value :: ctx
+       type(ramgpu_sat), intent(in) :: sats(*)
+       integer(c_int), value :: nsat
+       real(c_double), intent(out) :: sat_flux(*), omni_flux(*)
+     end function
+     integer(c_int) function ramgpu_sum_pressure(ctx, member, pallsum, pparsum) &
+          bind(C, name="ramgpu_sum_pressure")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member
+       real(c_double), intent(out) :: pallsum(*), pparsum(*)
      end function
      integer(c_int) function ramgpu_last_error(ctx, buf, len) bind(C, name="ramgpu_last_error")
        import :: c_int, c_ptr, c_char, c_size_t
