@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--adj-fd", type=int, default=4, help="finite-difference directions on the full window")
     ap.add_argument("--adj-members", type=int, default=64, help="batched-gradient members (0: skip)")
     ap.add_argument("--adj-member-calls", type=int, default=36)
+    ap.add_argument("--only", choices=["adjoint"], default=None,
+                    help="run one section alone (profiling); prints its result as JSON")
     return ap.parse_args()
 
 
@@ -491,6 +493,10 @@ def run_gb300(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
+    if args.only == "adjoint":
+        stream = torch.cuda.Stream(device=dev)
+        print(json.dumps({"adjoint": run_adjoint(args, torch, dev, stream)}), flush=True)
+        return
     wl = W.make_workload(args.workload)
     g = wl.grid
     ns = len(g.species)

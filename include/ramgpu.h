@@ -220,6 +220,22 @@ typedef struct {
 int ramgpu_fly_sats(ramgpu_ctx *ctx, const ramgpu_sat *sats, int nsat, double *sat_flux,
                     double *omni_flux);
 
+/* Bounce integrals of computehI (src/ModRamScb.f90:378-406, with
+ * integrator_c and bounceaverage_c of src/RamGSL.c:452-606) on field lines
+ * through the RAM grid: line (I,J), I = 1..NR, is the one through LZ(I+1).
+ * Inputs (host or device memory): chi (nthe), the field-line coordinate;
+ * x, y, z, b, dens (nthe, NR, NT), positions [RE], |B| and the density to
+ * bounce-average (dens may be NULL); ieq = nThetaEquator (1-based).  The
+ * equator fix of :388-395 is applied to a copy of b.  The integrals of the
+ * reference's linearly interpolated integrands are evaluated exactly
+ * (the reference's GSL cquad runs at 1e-3 tolerance).  Outputs (NR,NT,NPA):
+ * h = H_cart, fi = I_cart, hdens = HDens_cart (needs dens; may be NULL),
+ * bmirror = the mirror field of each pitch angle as the integrals used it
+ * (may be NULL).  Lines with outsideMGNP (ramgpu_set_fields) set give 0. */
+int ramgpu_bounce_integrals(ramgpu_ctx *ctx, int nthe, const double *chi, const double *x,
+                            const double *y, const double *z, const double *b, const double *dens,
+                            int ieq, double *h, double *fi, double *hdens, double *bmirror);
+
 /* SCB hand-off, ram_sum_pressure (src/ModRamFunctions.f90:272-297):
  * PAllSum(I,J) = sum_S (2/3 PPERT(S,I,J) + 1/3 PPART(S,I,J)) and
  * PParSum(I,J) = sum_S PPART(S,I,J) over the member's species, in species

@@ -95,6 +95,7 @@ def load():
         lib.ro_ram_run2.argtypes = [gp, C.c_int, sp, pp, C.c_double, _P, _P, PP, PP, PP, PP, PP,
                                     C.POINTER(RoLosses), _P, C.c_int, PP]
         lib.ro_padif.argtypes = [gp, pp, _P, _P]
+        lib.ro_bounce_integrals.argtypes = [gp, C.c_int, _P, _P, _P, _P, _P, _P, C.c_int, _P, _P, _P, _P]
         U8 = C.POINTER(C.c_ubyte)
         lib.ro_driftr_rec.argtypes = [gp, sp, pp, dpp, _P, _P, _P, _P, U8, _IP]
         lib.ro_driftr_rec.restype = C.c_double
@@ -222,6 +223,18 @@ class Oracle:
         """WPADIF / FLCscatter on one species (Fortran array, in place)."""
         p = self.params(dts)
         self.lib.ro_padif(C.byref(self.rg), C.byref(p), _p(_f(daa)), _p(f2))
+
+    def bounce_integrals(self, lines):
+        """computehI's bounce integrals on field lines (workload.FieldLines):
+        (H_cart, I_cart, HDens_cart, mirror B), each (NR, NT, NPA)."""
+        g = self.grid
+        shp = (g.nr, g.nt, g.npa)
+        h, fi, hd, bm = (np.zeros(shp, order="F") for _ in range(4))
+        b = _f(lines.b).copy(order="F")
+        self.lib.ro_bounce_integrals(C.byref(self.rg), int(lines.chi.size), _p(_f(lines.chi)), _p(_f(lines.x)),
+                                     _p(_f(lines.y)), _p(_f(lines.z)), _p(b), _p(_f(lines.dens)),
+                                     int(lines.ieq), _p(h), _p(fi), _p(hd), _p(bm))
+        return h, fi, hd, bm
 
     def cepara(self, s, dts, do_atmol=True):
         g = self.grid

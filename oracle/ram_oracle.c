@@ -1197,3 +1197,154 @@ void ro_padif(const ro_grid *g, const ro_params *p, const double *daa, double *f
         free(FACMU);
     }
 }
+
+/* ------------------------------------------------------------ computehI
+ * Bounce integrals of computehI (src/ModRamScb.f90:378-406) with
+ * integrator_c and bounceaverage_c (src/RamGSL.c:452-606).  The reference
+ * integrates, with GSL cquad at 1e-3 tolerance, integrands built on the
+ * LINEAR interpolant of B (and of the density) between the field-line
+ * nodes (integral_interpolate, src/RamGSL.c:295-322); here those same
+ * integrals are evaluated exactly, segment by segment, in closed form:
+ * with u = Bm - B linear on a segment, a = sqrt(u0), b = sqrt(u1),
+ *   int sqrt(u) = (2/3) dchi (a^2+ab+b^2)/(a+b),  int 1/sqrt(u) = 2 dchi/(a+b),
+ *   int (n0 + dn t)/sqrt(u) = dchi (n0 H1 + dn H2), H1 = 2/(a+b),
+ *   H2 = 2(b+2a)/(3(a+b)^2),
+ * and the part of a segment where B >= Bm (integrand 0) cut off at u = 0. */
+static void seg_integrals(double c0, double c1, double B0, double B1, double n0, double n1, double bm,
+                          double *yi, double *yh, double *yd)
+{
+    double u0 = bm - B0, u1 = bm - B1, dchi = c1 - c0;
+    if (u0 <= 0 && u1 <= 0) return;
+    double a, b, na, nb, w;
+    if (u0 > 0 && u1 > 0) {
+        a = sqrt(u0); b = sqrt(u1); na = n0; nb = n1; w = dchi;
+    } else if (u0 > 0) { /* positive from the segment start to u = 0 */
+        double f = u0 / (u0 - u1);
+        a = sqrt(u0); b = 0.; na = n0; nb = n0 + (n1 - n0) * f; w = dchi * f;
+    } else {             /* positive from u = 0 to the segment end */
+        double f = u1 / (u1 - u0);
+        a = 0.; b = sqrt(u1); na = n1 + (n0 - n1) * f; nb = n1; w = dchi * f;
+    }
+    double s = a + b;
+    *yi += (2. / 3.) * w * (a * a + a * b + b * b) / s;
+    *yh += 2. * w / s;
+    if (yd) *yd += w * (na * (2. / s) + (nb - na) * (2. * (b + 2. * a) / (3. * s * s)));
+}
+
+static void line_integrals(int nthe, const double *chi, const double *bf, const double *var, double bm,
+                           int i0, int i1, double *yi, double *yh, double *yd)
+{
+    *yi = 0.; *yh = 0.;
+    if (yd) *yd = 0.;
+    for (int k = i0; k < i1; ++k)
+        seg_integrals(chi[k], chi[k + 1], bf[k], bf[k + 1], var ? var[k] : 0., var ? var[k + 1] : 0., bm, yi,
+                      yh, yd);
+}
+
+/* Mirror-point bracket of integrator_c/bounceaverage_c (src/RamGSL.c:546-563). */
+static void mirror_bracket(int nT, const double *chi, const double *bf, double m, int *lh, int *rh, double *a,
+                           double *b)
+{
+    *a = 0; *b = 0; *lh = 0; *rh = 0;
+    for (int i = 1; i < nT - 1; i++)
+        if (m <= bf[i - 1] && m >= bf[i]) { *a = chi[i - 1]; *lh = i - 1; break; }
+    for (int i = nT - 2; i > 0; i--)
+        if (m >= bf[i - 1] && m <= bf[i]) { *b = chi[i]; *rh = i; break; }
+}
+
+static int index_of(int nT, const double *chi, double v)
+{
+    for (int i = 0; i < nT; ++i)
+        if (chi[i] == v) return i;
+    return 0;
+}
+
+/* integrator_c (src/RamGSL.c:538-606) with exact segment integrals.
+ * var != NULL gives bounceaverage_c (src/RamGSL.c:452-508) instead (yV in yi). */
+static void ro_integrator(int nT, int nPa, double *mirror, const double *chi, const double *bf, const double *var,
+                          double *yI, double *yH)
+{
+    int LH[512], RH[512];
+    double a[512], b[512], dummy;
+    for (int L = 1; L < nPa - 1; L++) mirror_bracket(nT, chi, bf, mirror[L], &LH[L], &RH[L], &a[L], &b[L]);
+    if (var) line_integrals(nT, chi, bf, var, mirror[nPa - 1], 0, nT - 1, &dummy, &dummy, &yI[nPa - 1]);
+    else line_integrals(nT, chi, bf, NULL, mirror[nPa - 1], 0, nT - 1, &yI[nPa - 1], &yH[nPa - 1], NULL);
+    for (int L = nPa - 2; L > 0; L--) {
+        if (mirror[L] >= bf[1] || a[L] == 0) a[L] = chi[0];
+        if (mirror[L] >= bf[nT - 1] || b[L] == 0) b[L] = chi[nT - 1];
+        if (a[L] <= chi[0] || b[L] >= chi[nT - 1]) {
+            mirror[L] = mirror[nPa - 1];
+            yI[L] = yI[nPa - 1];
+            if (!var) yH[L] = yH[nPa - 1];
+        } else {
+            if ((RH[L] - LH[L]) <= 4) {
+                yI[L] = yI[L + 1];
+                if (!var) yH[L] = yH[L + 1];
+                continue;
+            }
+            int i0 = index_of(nT, chi, a[L]), i1 = index_of(nT, chi, b[L]);
+            if (var) {
+                line_integrals(nT, chi, bf, var, mirror[L], i0, i1, &dummy, &dummy, &yI[L]);
+                if (yI[L] <= 0) yI[L] = yI[L + 1];
+            } else {
+                line_integrals(nT, chi, bf, NULL, mirror[L], i0, i1, &yI[L], &yH[L], NULL);
+                if (yI[L] <= 0) yI[L] = yI[L + 1];
+                if (yH[L] <= 0) yH[L] = yH[L + 1];
+            }
+        }
+    }
+    if (var) {
+        yI[0] = yI[1];
+    } else {
+        yI[0] = 0;
+        yH[0] = yH[1];
+    }
+}
+
+void ro_bounce_integrals(const ro_grid *g, int nthe, const double *chi, const double *x, const double *y,
+                         const double *z, double *bline, const double *dens, int ieq, double *h, double *fi,
+                         double *hd, double *bm)
+{
+    const double pi_d = 3.141592653589793238462643383279502884197;
+    double *mirror = (double *)malloc(sizeof(double) * NPA);
+    double *yI = (double *)malloc(sizeof(double) * NPA), *yH = (double *)malloc(sizeof(double) * NPA);
+    double *yD = (double *)malloc(sizeof(double) * NPA);
+    for (int i = 1; i <= NR; ++i)
+        for (int j = 1; j <= NT; ++j) {
+            size_t ln = ((size_t)(j - 1) * NR + (i - 1)) * nthe;
+            double *bf = bline + ln;
+            const double *xl = x + ln, *yl = y + ln, *zl = z + ln;
+            for (int L = 1; L <= NPA; ++L) {
+                size_t o = ((size_t)(L - 1) * NT + (j - 1)) * NR + (i - 1);
+                h[o] = 0.; fi[o] = 0.;
+                if (hd) hd[o] = 0.;
+                if (bm) bm[o] = 0.;
+            }
+            if (OUTSIDE(i, j) != 0) continue;
+            double length = 0.;
+            for (int k = 1; k < nthe; ++k) {
+                double dx = xl[k] - xl[k - 1], dy = yl[k] - yl[k - 1], dz = zl[k] - zl[k - 1];
+                length = length + sqrt(dx * dx + dy * dy + dz * dz);
+            }
+            const int e = ieq - 1;
+            double r0 = sqrt(xl[e] * xl[e] + yl[e] * yl[e]);
+            double bmin = bf[0];
+            for (int k = 1; k < nthe; ++k) bmin = dmin(bmin, bf[k]);
+            if (fabs(bf[e] - bmin) > 1e-9) {
+                if (2. * bmin - bf[e] > 0.) bf[e] = 2. * bmin - bf[e];
+                else bf[e] = bmin - 0.01;
+            }
+            for (int L = 1; L <= NPA - 1; ++L) mirror[L - 1] = bf[e] / (1. - MU(L) * MU(L));
+            mirror[NPA - 1] = bf[nthe - 1];
+            ro_integrator(nthe, NPA, mirror, chi, bf, NULL, yI, yH);
+            if (hd) ro_integrator(nthe, NPA, mirror, chi, bf, dens + ln, yD, NULL);
+            for (int L = 1; L <= NPA; ++L) {
+                size_t o = ((size_t)(L - 1) * NT + (j - 1)) * NR + (i - 1);
+                fi[o] = (length / (pi_d * r0)) * yI[L - 1] / sqrt(mirror[L - 1]);
+                h[o] = (length / (pi_d * 2 * r0)) * yH[L - 1] * sqrt(mirror[L - 1]);
+                if (hd) hd[o] = yD[L - 1] / yH[L - 1];
+                if (bm) bm[o] = mirror[L - 1];
+            }
+        }
+    free(mirror); free(yI); free(yH); free(yD);
+}

@@ -149,6 +149,18 @@ int ro_ram_run2(const ro_grid *g, int ns, const ro_species *sp, const ro_params 
  * coefficient daa = D(I,J,K,L) (NR,NT,NE,NPA). */
 void ro_padif(const ro_grid *g, const ro_params *p, const double *daa, double *f2);
 
+/* Bounce integrals of computehI (src/ModRamScb.f90:378-406; integrator_c and
+ * bounceaverage_c of src/RamGSL.c) on RAM-grid field lines, the integrals of
+ * the linearly interpolated integrands evaluated exactly.  Inputs per line
+ * (I,J): nthe nodes of chi (shared), x, y, z, B (bline, modified in place by
+ * the equator fix of :388-395) and density (dens, may be NULL), all
+ * (nthe, NR, NT); ieq = nThetaEquator (1-based).  Outputs (NR,NT,NPA):
+ * h = H_cart, fi = I_cart, hd = HDens_cart (may be NULL), bm = the mirror
+ * field used (may be NULL); lines with outsideMGNP set are zero. */
+void ro_bounce_integrals(const ro_grid *g, int nthe, const double *chi, const double *x, const double *y,
+                         const double *z, double *bline, const double *dens, int ieq, double *h, double *fi,
+                         double *hd, double *bm);
+
 /* One DTs half of ram_run for one species (the measurement "step"):
  * order 0 = R,P,E,MU,[CEX],[ATMOL]; order 1 = [ATMOL],[CEX],MU,E,P,R.
  * charge/atlos from ro_cepara. */

@@ -1208,6 +1208,72 @@ int ramgpu_fly_sats(ramgpu_ctx* ctx, const ramgpu_sat* sats, int nsat, double* s
   return RAMGPU_OK;
 }
 
+int ramgpu_bounce_integrals(ramgpu_ctx* ctx, int nthe, const double* chi, const double* x, const double* y,
+                            const double* z, const double* b, const double* dens, int ieq, double* h,
+                            double* fi, double* hdens, double* bmirror) {
+  if (check_ctx(ctx) || !chi || !x || !y || !z || !b || !h || !fi || (hdens && !dens))
+    return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (!ctx->have_grid || !ctx->have_fields) return fail(ctx, RAMGPU_ERR_STATE, "grid/fields not set");
+  if (nthe < 3 || ieq < 1 || ieq > nthe) return fail(ctx, RAMGPU_ERR_ARG, "nthe >= 3 and 1 <= ieq <= nthe");
+  Dev& d = ctx->d;
+  const size_t nl = (size_t)d.nr * d.nt, nln = nl * nthe, na = nl * d.npa;
+  // one device block: lines (x,y,z,b,dens), chi, per-line and per-angle scratch, outputs
+  const size_t nd = 5 * nln + nthe + 2 * nl + 5 * na + 4 * na;
+  double* buf = nullptr;
+  unsigned char* sbuf = nullptr;
+  int* okb = nullptr;
+  CK(cudaMalloc(&buf, nd * sizeof(double)));
+  cudaError_t e = cudaMalloc(&sbuf, 2 * na);
+  if (e == cudaSuccess) e = cudaMalloc(&okb, nl * sizeof(int));
+  BounceDev q{};
+  q.nr = d.nr; q.nt = d.nt; q.npa = d.npa; q.nthe = nthe; q.ieq = ieq;
+  double* p = buf;
+  double *dx = p; p += nln;
+  double *dy = p; p += nln;
+  double *dz = p; p += nln;
+  double *db = p; p += nln;
+  double *dd = p; p += nln;
+  double *dchi = p; p += nthe;
+  q.length = p; p += nl;
+  q.r0 = p; p += nl;
+  q.mirror = p; p += na;
+  q.mirror2 = p; p += na;
+  q.yi = p; p += na;
+  q.yh = p; p += na;
+  q.yd = p; p += na;
+  q.h_out = p; p += na;
+  q.i_out = p; p += na;
+  q.d_out = p; p += na;
+  q.m_out = p; p += na;
+  q.x = dx; q.y = dy; q.z = dz; q.b = db; q.chi = dchi; q.mu = d.mu; q.outside = d.outside;
+  q.dens = dens ? dd : nullptr;
+  if (!dens) q.yd = nullptr;
+  q.st = sbuf; q.sd = sbuf + na; q.line_ok = okb;
+  const size_t bytes = nln * sizeof(double);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, bytes, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dy, y, bytes, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dz, z, bytes, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(db, b, bytes, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess && dens) e = cudaMemcpyAsync(dd, dens, bytes, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dchi, chi, nthe * sizeof(double), cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) {
+    launch_bounce(q, ctx->stream);
+    ctx->launches += 3;
+    e = cudaGetLastError();
+  }
+  const size_t ob = na * sizeof(double);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, q.h_out, ob, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(fi, q.i_out, ob, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess && hdens) e = cudaMemcpyAsync(hdens, q.d_out, ob, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess && bmirror) e = cudaMemcpyAsync(bmirror, q.m_out, ob, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(buf);
+  cudaFree(sbuf);
+  cudaFree(okb);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "bounce_integrals");
+  return RAMGPU_OK;
+}
+
 int ramgpu_sum_pressure(ramgpu_ctx* ctx, int member, double* pallsum, double* pparsum) {
   if (check_ctx(ctx) || !pallsum || !pparsum) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
   if (member < 0 || member >= ctx->cfg.n_members) return fail(ctx, RAMGPU_ERR_ARG, "member out of range");

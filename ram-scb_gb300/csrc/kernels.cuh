@@ -93,6 +93,21 @@ void launch_digest(const unsigned char* rec, long long n, unsigned long long* ou
 void launch_padif_tables(const Dev& d, double dts, cudaStream_t st);
 void launch_padif(const Dev& d, const double* loss, cudaStream_t st);
 
+// bounce integrals of computehI (bounce.cu); line arrays (nthe, NR, NT),
+// per-angle arrays (NR*NT lines, NPA), outputs (NR, NT, NPA)
+struct BounceDev {
+  int nr, nt, npa, nthe, ieq;
+  const double *chi, *x, *y, *z, *dens, *mu;
+  double* b;                     // copied in, equator-fixed in place
+  const int* outside;            // (NR, NT)
+  int* line_ok;
+  double *length, *r0;           // per line
+  double *mirror, *mirror2, *yi, *yh, *yd;
+  unsigned char *st, *sd;
+  double *h_out, *i_out, *d_out, *m_out;
+};
+void launch_bounce(const BounceDev& q, cudaStream_t st);
+
 // virtual spacecraft and SCB hand-off (outputs.cu)
 struct SatDev {
   int member;

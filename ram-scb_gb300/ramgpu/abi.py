@@ -35,7 +35,7 @@ EXPORTS = (
     "ramgpu_get_launch_shape", "ramgpu_autotune", "ramgpu_set_kp_all",
     "ramgpu_adj_forward", "ramgpu_adj_backward", "ramgpu_adj_digest", "ramgpu_adj_record",
     "ramgpu_fly_sats", "ramgpu_sum_pressure", "ramgpu_adj_replay", "ramgpu_set_pa_diffusion",
-    "ramgpu_loss_wae",
+    "ramgpu_loss_wae", "ramgpu_bounce_integrals",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
@@ -137,6 +137,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_adj_replay": ([vp, dp], i),
         "ramgpu_set_pa_diffusion": ([vp, i, dp], i),
         "ramgpu_loss_wae": ([vp, i, i, dp], i),
+        "ramgpu_bounce_integrals": ([vp, i, dp, dp, dp, dp, dp, dp, i, dp, dp, dp, dp], i),
         "ramgpu_sum_pressure": ([vp, i, dp, dp], i),
     }
     for name, (args, res) in sig.items():
@@ -326,6 +327,18 @@ class RamGpu:
         pp = np.empty((g.nr, g.nt), order="F")
         self._ck(self.lib.ramgpu_sum_pressure(self.h, int(member), _dptr(pa), _dptr(pp)), "sum_pressure")
         return pa, pp
+
+    def bounce_integrals(self, lines):
+        """computehI's bounce integrals on field lines (workload.FieldLines):
+        (H_cart, I_cart, HDens_cart, mirror B), each (NR, NT, NPA)."""
+        g = self.grid
+        shp = (g.nr, g.nt, g.npa)
+        h, fi, hd, bm = (np.zeros(shp, order="F") for _ in range(4))
+        arrs = [_fort(a) for a in (lines.chi, lines.x, lines.y, lines.z, lines.b, lines.dens)]
+        self._ck(self.lib.ramgpu_bounce_integrals(self.h, int(lines.chi.size), *[_dptr(a) for a in arrs],
+                                                  int(lines.ieq), _dptr(h), _dptr(fi), _dptr(hd), _dptr(bm)),
+                 "bounce_integrals")
+        return h, fi, hd, bm
 
     def set_pa_diffusion(self, s: int, daa=None):
         """Pitch-angle diffusion coefficient D(I,J,K,L) of species s (None removes it)."""

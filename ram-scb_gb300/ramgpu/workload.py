@@ -452,6 +452,58 @@ def pa_diffusion(g: Grid, f: Fields, seed: int = 7, d0: float = 2.0e-5) -> np.nd
     return np.ascontiguousarray(d)
 
 
+def rairden_density(dist):
+    """Rairden-like hydrogen geocorona density [m^-3] against geocentric
+    distance [RE], the RAIRDEN mode of computehI (src/ModRamScb.f90:364-369)."""
+    d = np.asarray(dist)
+    return 10 ** (13.326 - 3.6908 * d + 1.1362 * d ** 2 - 0.16984 * d ** 3 + 0.009553 * d ** 4)
+
+
+@dataclass
+class FieldLines:
+    """Field lines through the RAM grid points, the input of the bounce
+    integrals: chi (nthe) and x, y, z, B, density (nthe, NR, NT), lines
+    I = 1..NR at L-shell LZ(I+1) (they fill FNHS(I+1,...)); ieq is the
+    1-based equator node."""
+    chi: np.ndarray
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    b: np.ndarray
+    dens: np.ndarray
+    ieq: int
+
+
+def dipole_lines(g: Grid, nthe: int = 201) -> FieldLines:
+    """Dipole field lines (B in units of the surface equatorial field) from
+    foot to foot, nodes equally spaced in arc length; chi = pi*s/length."""
+    if nthe % 2 == 0:
+        raise ValueError("nthe must be odd (a node on the equator)")
+    nr, nt = g.nr, g.nt
+    x = np.zeros((nthe, nr, nt)); y = np.zeros_like(x); z = np.zeros_like(x); b = np.zeros_like(x)
+    chi = np.zeros(nthe)
+    for i in range(nr):
+        lsh = g.lz[i + 1]
+        lam0 = math.acos(math.sqrt(1.0 / lsh))
+        lam = np.linspace(-lam0, lam0, 20001)
+        ds = lsh * np.cos(lam) * np.sqrt(1 + 3 * np.sin(lam) ** 2)
+        s = np.concatenate([[0.0], np.cumsum(0.5 * (ds[1:] + ds[:-1]) * np.diff(lam))])
+        sk = np.linspace(0.0, s[-1], nthe)
+        lk = np.interp(sk, s, lam)
+        lk[(nthe - 1) // 2] = 0.0
+        r = lsh * np.cos(lk) ** 2
+        bb = np.sqrt(1 + 3 * np.sin(lk) ** 2) / r ** 3
+        chi = math.pi * sk / s[-1]
+        for j in range(nt):
+            ph = g.phi[j]
+            x[:, i, j] = r * np.cos(lk) * math.cos(ph)
+            y[:, i, j] = r * np.cos(lk) * math.sin(ph)
+            z[:, i, j] = r * np.sin(lk)
+            b[:, i, j] = bb
+    dens = rairden_density(np.sqrt(x ** 2 + y ** 2 + z ** 2))
+    return FieldLines(chi, x, y, z, b, dens, (nthe + 1) // 2)
+
+
 def vols_vt(g: Grid, kp: float) -> np.ndarray:
     """VT(I,J), I=1..NR+1 (src/ModRamRun.f90:45-54).  C order (I,J)."""
     t = 1. - 0.159 * kp + 0.0093 * (kp * kp)

@@ -407,3 +407,76 @@ def test_padif_identity_and_conservation():
     assert np.max(np.abs(f - f0)) > 1e-3 * np.max(np.abs(f0)) and f.min() >= 0
     # untouched: I = 1 and K = 1
     assert np.array_equal(f[0], f0[0]) and np.array_equal(f[:, :, 0], f0[:, :, 0])
+
+
+def _dipole_setup(nthe):
+    import dataclasses
+    wl = W.make_workload("single_h")
+    fl = dataclasses.replace(wl.fields, outside=np.zeros_like(wl.fields.outside))
+    return wl.grid, pyoracle.Oracle(wl.grid, fl), W.dipole_lines(wl.grid, nthe)
+
+
+def test_bounce_integrals_dipole_known_answer():
+    """computehI's h and I integrals on dipole field lines reproduce Ejiri's
+    h(y), I(y) (FUNT, FUNI, src/ModRamFunctions.f90:90-143) to their fit
+    accuracy wherever the mirror point lies above the surface."""
+    g, o, lines = _dipole_setup(1601)
+    h, fi, hd, bm = o.bounce_integrals(lines)
+    mu = np.asarray(g.mu)
+    beq = lines.b[lines.ieq - 1]     # (NR, NT)
+    bend = lines.b[-1]
+    checked = 0
+    for L in range(3, g.npa - 1):
+        # mirror point well above the surface (outside the loss cone); near
+        # 90 degrees the bracket spans too few nodes and the reference copies
+        # the neighbouring pitch angle, so L >= 4 (1-based) only
+        ok = beq / (1.0 - mu[L] ** 2) < 0.8 * bend
+        if not ok.any():
+            continue
+        t, u = W.funt(mu[L]), W.funi(mu[L])
+        assert abs(h[:, :, L][ok] / t - 1).max() < 2e-3, L
+        assert abs(fi[:, :, L][ok] / u - 1).max() < 2e-3, L
+        checked += int(ok.sum())
+    assert checked > 0.7 * g.nr * g.nt * (g.npa - 4)
+    assert np.all(fi[:, :, 0] == 0.0)  # I at 90 degrees
+    # bounce-averaged density lies between the equatorial and the foot values
+    assert np.all(hd[:, :, 1:] > 0)
+
+
+def test_bounce_integrals_exact_for_the_interpolant():
+    """The closed-form segment integrals equal adaptive quadrature of the
+    reference's integrands (linear interpolant of B and of the density,
+    cut off where B >= Bm) far below the reference's 1e-3 tolerance."""
+    from scipy import integrate
+
+    g, o, lines = _dipole_setup(101)
+    h, fi, hd, bm = o.bounce_integrals(lines)
+    chi = lines.chi
+    i, j = 7, 4
+    B = lines.b[:, i, j]
+    n = lines.dens[:, i, j]
+    xl, yl, zl = lines.x[:, i, j], lines.y[:, i, j], lines.z[:, i, j]
+    length = float(np.sum(np.sqrt(np.diff(xl) ** 2 + np.diff(yl) ** 2 + np.diff(zl) ** 2)))
+    e = lines.ieq - 1
+    r0 = math.hypot(xl[e], yl[e])
+    for L in (5, 17, 33, 48):
+        m = bm[i, j, L]
+        inside = np.nonzero(B < m)[0]
+        # crossings of the interpolant through Bm, as quadrature break points
+        pts = []
+        for k in range(len(B) - 1):
+            if (B[k] - m) * (B[k + 1] - m) < 0:
+                pts.append(chi[k] + (chi[k + 1] - chi[k]) * (m - B[k]) / (B[k + 1] - B[k]))
+        lo, hi = pts[0], pts[-1]
+        bi = lambda c: np.interp(c, chi, B)
+        ni = lambda c: np.interp(c, chi, n)
+        fh = lambda c: 1.0 / math.sqrt(max(m - bi(c), 1e-300)) if m > bi(c) else 0.0
+        fI = lambda c: math.sqrt(m - bi(c)) if m > bi(c) else 0.0
+        fd = lambda c: ni(c) * fh(c)
+        kw = dict(points=list(chi[inside[0]:inside[-1] + 1]), limit=500, epsabs=0, epsrel=1e-12)
+        yh = integrate.quad(fh, lo, hi, **kw)[0]
+        yi = integrate.quad(fI, lo, hi, **kw)[0]
+        yd = integrate.quad(fd, lo, hi, **kw)[0]
+        assert abs((length / (math.pi * 2 * r0)) * yh * math.sqrt(m) / h[i, j, L] - 1) < 1e-9, L
+        assert abs((length / (math.pi * r0)) * yi / math.sqrt(m) / fi[i, j, L] - 1) < 1e-9, L
+        assert abs((yd / yh) / hd[i, j, L] - 1) < 1e-8, L
