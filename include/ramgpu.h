@@ -139,6 +139,15 @@ int ramgpu_set_member_active(ramgpu_ctx *ctx, int member, int active);
  * or device memory (unified addressing decides the copy direction). */
 int ramgpu_upload_f2(ramgpu_ctx *ctx, int member, int s, const double *f2_s);
 int ramgpu_download_f2(ramgpu_ctx *ctx, int member, int s, double *f2_s);
+/* Stream-ordered forms: the copies (and the moment read-back) are queued on
+ * the context's stream behind or ahead of ramgpu_ram_run_async and do not
+ * wait; the caller keeps the buffers alive and unchanged until
+ * ramgpu_synchronize returns.  With page-locked host buffers they overlap
+ * nothing but run at full link speed and cost the host no round trips. */
+int ramgpu_upload_f2_async(ramgpu_ctx *ctx, int member, int s, const double *f2_s);
+int ramgpu_download_f2_async(ramgpu_ctx *ctx, int member, int s, double *f2_s);
+int ramgpu_moments_async(ramgpu_ctx *ctx, int member, int s, double *ppert, double *ppart);
+int ramgpu_synchronize(ramgpu_ctx *ctx);
 /* The whole reference array F2(NS,NR,NT,NE,NPA) of one member. */
 int ramgpu_upload_f2_all(ramgpu_ctx *ctx, int member, const double *f2);
 int ramgpu_download_f2_all(ramgpu_ctx *ctx, int member, double *f2);

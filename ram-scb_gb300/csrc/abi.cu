@@ -743,18 +743,23 @@ int ramgpu_set_potential(ramgpu_ctx* ctx, int member, const double* vt) {
   return RAMGPU_OK;
 }
 
+// Kp (VOLS mode) of members m0..m1-1, written in stream order by a tiny
+// kernel so that the host neither waits nor keeps a staging buffer alive.
+__global__ void k_set_kp(double* kp, int* vt_mode, int m0, int m1, double v) {
+  const int m = m0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < m1) { kp[m] = v; vt_mode[m] = 1; }
+}
+
 int ramgpu_set_kp(ramgpu_ctx* ctx, int member, double kp) {
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
   if (!isfinite(kp)) return fail(ctx, RAMGPU_ERR_ARG, "kp must be finite");
   int m0 = member, m1 = member + 1;
   if (member < 0) { m0 = 0; m1 = ctx->cfg.n_members; }
-  for (int m = m0; m < m1; ++m) {
-    if (int rc = check_ms(ctx, m, 0)) return rc;
-    int one = 1;
-    CK(cudaMemcpyAsync(ctx->d.kp + m, &kp, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->d.vt_mode + m, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-  }
+  if (int rc = check_ms(ctx, m0, 0)) return rc;
+  if (int rc = check_ms(ctx, m1 - 1, 0)) return rc;
+  k_set_kp<<<(m1 - m0 + 127) / 128, 128, 0, ctx->stream>>>(ctx->d.kp, ctx->d.vt_mode, m0, m1, kp);
+  ctx->launches += 1;
+  CKL("set_kp");
   return RAMGPU_OK;
 }
 
@@ -810,6 +815,39 @@ int ramgpu_download_f2(ramgpu_ctx* ctx, int member, int s, double* f2_s) {
   const size_t n = ctx->d.ncell;
   CK(cudaMemcpyAsync(f2_s, ctx->d.f2 + (size_t)(member * ctx->d.ns + s) * n, n * sizeof(double),
                      cudaMemcpyDefault, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return RAMGPU_OK;
+}
+
+int ramgpu_upload_f2_async(ramgpu_ctx* ctx, int member, int s, const double* f2_s) {
+  if (check_ctx(ctx) || !f2_s) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (int rc = check_ms(ctx, member, s)) return rc;
+  const size_t n = ctx->d.ncell;
+  CK(cudaMemcpyAsync(ctx->d.f2 + (size_t)(member * ctx->d.ns + s) * n, f2_s, n * sizeof(double),
+                     cudaMemcpyDefault, ctx->stream));
+  return RAMGPU_OK;
+}
+
+int ramgpu_download_f2_async(ramgpu_ctx* ctx, int member, int s, double* f2_s) {
+  if (check_ctx(ctx) || !f2_s) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (int rc = check_ms(ctx, member, s)) return rc;
+  const size_t n = ctx->d.ncell;
+  CK(cudaMemcpyAsync(f2_s, ctx->d.f2 + (size_t)(member * ctx->d.ns + s) * n, n * sizeof(double),
+                     cudaMemcpyDefault, ctx->stream));
+  return RAMGPU_OK;
+}
+
+int ramgpu_moments_async(ramgpu_ctx* ctx, int member, int s, double* ppert, double* ppart) {
+  if (check_ctx(ctx) || !ppert || !ppart) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (int rc = check_ms(ctx, member, s)) return rc;
+  const size_t n = (size_t)ctx->d.nr * ctx->d.nt, o = (size_t)(member * ctx->d.ns + s) * n;
+  CK(cudaMemcpyAsync(ppert, ctx->d.ppert + o, n * sizeof(double), cudaMemcpyDefault, ctx->stream));
+  CK(cudaMemcpyAsync(ppart, ctx->d.ppart + o, n * sizeof(double), cudaMemcpyDefault, ctx->stream));
+  return RAMGPU_OK;
+}
+
+int ramgpu_synchronize(ramgpu_ctx* ctx) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
   CK(cudaStreamSynchronize(ctx->stream));
   return RAMGPU_OK;
 }

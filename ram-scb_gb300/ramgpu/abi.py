@@ -35,7 +35,8 @@ EXPORTS = (
     "ramgpu_get_launch_shape", "ramgpu_autotune", "ramgpu_set_kp_all",
     "ramgpu_adj_forward", "ramgpu_adj_backward", "ramgpu_adj_digest", "ramgpu_adj_record",
     "ramgpu_fly_sats", "ramgpu_sum_pressure", "ramgpu_adj_replay", "ramgpu_set_pa_diffusion",
-    "ramgpu_loss_wae", "ramgpu_bounce_integrals",
+    "ramgpu_loss_wae", "ramgpu_bounce_integrals", "ramgpu_upload_f2_async", "ramgpu_download_f2_async",
+    "ramgpu_moments_async", "ramgpu_synchronize",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
@@ -138,6 +139,10 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_set_pa_diffusion": ([vp, i, dp], i),
         "ramgpu_loss_wae": ([vp, i, i, dp], i),
         "ramgpu_bounce_integrals": ([vp, i, dp, dp, dp, dp, dp, dp, i, dp, dp, dp, dp], i),
+        "ramgpu_upload_f2_async": ([vp, i, i, dp], i),
+        "ramgpu_download_f2_async": ([vp, i, i, dp], i),
+        "ramgpu_moments_async": ([vp, i, i, dp, dp], i),
+        "ramgpu_synchronize": ([vp], i),
         "ramgpu_sum_pressure": ([vp, i, dp, dp], i),
     }
     for name, (args, res) in sig.items():
