@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--flush-mb", type=int, default=256)
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-coef-store", action="store_true",
+                    help="recompute the face coefficients in the reverse half instead of storing them")
     ap.add_argument("--members", type=int, default=256, help="ensemble members (0: skip)")
     ap.add_argument("--ensemble-steps", type=int, default=6)
     ap.add_argument("--loop-members", type=int, default=16)
@@ -513,6 +515,7 @@ def run_gb300(args, rank, world, local_rank):
         return wl.kp(2 * step)
 
     gpu.set_kp(-1, kp_at(0))
+    gpu.set_coef_store(not args.no_coef_store)
     shapes, _ = gpu.autotune(wl.dts) if not args.no_autotune else (gpu.launch_shape(), None)
     gpu.set_graph(not args.no_graph)
     # warm-up (builds the DTs tables, captures the graph)
@@ -633,6 +636,7 @@ def run_gb300(args, rank, world, local_rank):
         "config": {"workload": workload_desc(wl), "step": "one ram_run call = 2 DTs steps",
                    "cells_per_step": cells_per_step, "l2": "flushed between timed steps (256 MB write)",
                    "graph": not args.no_graph, "launch_shapes": shapes,
+                   "coef_store": not args.no_coef_store,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak,

@@ -253,6 +253,14 @@ int ramgpu_sum_pressure(ramgpu_ctx *ctx, int member, double *pallsum, double *pp
 
 /* ---- execution tuning (no reference counterpart) ------------------------ */
 
+/* Keep each face's coefficient C and CORR factor from the forward sweeps of a
+ * ram_run call and read them back in its reverse sweeps (enable = 1, the
+ * default), instead of recomputing them: 64 bytes per cell and (member,
+ * species) of device memory, taken only while it fits in a quarter of the
+ * free memory, for about 2 FP64 operations per face less in the reverse
+ * half.  Results are identical either way. */
+int ramgpu_set_coef_store(ramgpu_ctx *ctx, int enable);
+
 /* Replay ram_run / ram_run_async from a CUDA graph captured on first use and
  * re-captured when dts, the active (member, species) list, the flags or the
  * launch shapes change.  Inputs (F2, Kp/VT, FGEOS, fields) are read when the

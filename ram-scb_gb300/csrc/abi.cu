@@ -45,6 +45,7 @@ struct ramgpu_ctx {
   bool have_grid = false, have_fields = false;
   bool field_dirty = true, static_dirty = true;
   double tables_dts = -1.0;
+  bool coef_enabled = true;  // store face coefficients between the two halves
   // implicit pitch-angle diffusion: species with a coefficient, tables state
   std::vector<int> pd_on_h;
   bool pd_alloc = false, pd_dirty = false;
@@ -224,6 +225,23 @@ static int prepare(ramgpu_ctx* ctx, double dts) {
     int rc = rebuild_items(ctx);
     if (rc) return rc;
   }
+  // face-coefficient store for the reverse half: 64 bytes per cell and item,
+  // kept only while it takes at most a quarter of the free device memory
+  if (ctx->coef_enabled && ctx->d.coef_items < ctx->d.nitems) {
+    cudaFree(ctx->d.coef);
+    ctx->d.coef = nullptr;
+    ctx->d.coef_items = 0;
+    const size_t need = (size_t)8 * ctx->d.nitems * ctx->d.ncell * sizeof(double);
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && need <= fr / 4 &&
+        cudaMalloc(&ctx->d.coef, need) == cudaSuccess) {
+      ctx->d.coef_items = ctx->d.nitems;
+    } else {
+      ctx->d.coef = nullptr;
+      cudaGetLastError();
+    }
+    ctx->shape_version += 1;  // launch sequence changed: recapture the graph
+  }
   return RAMGPU_OK;
 }
 
@@ -254,22 +272,29 @@ static int sumrc_stage(ramgpu_ctx* ctx, int stage, int which) {
   return RAMGPU_OK;
 }
 
+// Forward sweeps with the CFL reduction; when the coefficient store exists
+// they also keep each face's C and CORR factor for the reverse half.
 static int enqueue_forward(ramgpu_ctx* ctx, double dts, bool loss_fused, const double* loss_table) {
   CK(cudaMemsetAsync(ctx->d.cflq, 0, sizeof(unsigned long long) * 4 * ctx->d.nm * ctx->d.ns, ctx->stream));
-  { Timed t(ctx, 2); launch_sweep_r(ctx->d, dts, true, ctx->stream); }
-  { Timed t(ctx, 3); launch_sweep_p(ctx->d, dts, true, ctx->stream); }
-  { Timed t(ctx, 4); launch_sweep_e(ctx->d, dts, true, ctx->stream); }
-  { Timed t(ctx, 5); launch_sweep_mu(ctx->d, dts, true, loss_fused ? 1 : 0, loss_table, ctx->stream); }
+  const int co = ctx->d.coef ? 1 : 0;
+  { Timed t(ctx, 2); launch_sweep_r(ctx->d, dts, true, ctx->stream, nullptr, false, co); }
+  { Timed t(ctx, 3); launch_sweep_p(ctx->d, dts, true, ctx->stream, nullptr, false, co); }
+  { Timed t(ctx, 4); launch_sweep_e(ctx->d, dts, true, ctx->stream, nullptr, false, co); }
+  { Timed t(ctx, 5); launch_sweep_mu(ctx->d, dts, true, loss_fused ? 1 : 0, loss_table, ctx->stream, nullptr, false, co); }
   ctx->launches += 4;
   CKL("forward sweeps");
   return RAMGPU_OK;
 }
 
-static int enqueue_reverse(ramgpu_ctx* ctx, double dts, bool loss_fused, const double* loss_table) {
-  { Timed t(ctx, 5); launch_sweep_mu(ctx->d, dts, false, loss_fused ? 2 : 0, loss_table, ctx->stream); }
-  { Timed t(ctx, 4); launch_sweep_e(ctx->d, dts, false, ctx->stream); }
-  { Timed t(ctx, 3); launch_sweep_p(ctx->d, dts, false, ctx->stream); }
-  { Timed t(ctx, 2); launch_sweep_r(ctx->d, dts, false, ctx->stream); }
+// Reverse sweeps; after_forward: the forward half of the same call ran just
+// before, so its stored face coefficients are read back.
+static int enqueue_reverse(ramgpu_ctx* ctx, double dts, bool loss_fused, const double* loss_table,
+                           bool after_forward) {
+  const int co = (after_forward && ctx->d.coef) ? 2 : 0;
+  { Timed t(ctx, 5); launch_sweep_mu(ctx->d, dts, false, loss_fused ? 2 : 0, loss_table, ctx->stream, nullptr, false, co); }
+  { Timed t(ctx, 4); launch_sweep_e(ctx->d, dts, false, ctx->stream, nullptr, false, co); }
+  { Timed t(ctx, 3); launch_sweep_p(ctx->d, dts, false, ctx->stream, nullptr, false, co); }
+  { Timed t(ctx, 2); launch_sweep_r(ctx->d, dts, false, ctx->stream, nullptr, false, co); }
   ctx->launches += 4;
   CKL("reverse sweeps");
   return RAMGPU_OK;
@@ -286,7 +311,7 @@ static int enqueue_body(ramgpu_ctx* ctx, double dts) {
   if (!losses && !pd) {
     // R,P,E,MU then CEX,ATMOL,ATMOL,CEX folded into the MU store
     if ((rc = enqueue_forward(ctx, dts, true, ctx->d.loss2))) return rc;
-    if ((rc = enqueue_reverse(ctx, dts, false, nullptr))) return rc;
+    if ((rc = enqueue_reverse(ctx, dts, false, nullptr, true))) return rc;
   } else if (!losses) {
     // R,P,E,MU, WPADIF, CEX,ATMOL,ATMOL,CEX (folded into WPADIF's store), WPADIF, MU,E,P,R
     if ((rc = enqueue_forward(ctx, dts, false, nullptr))) return rc;
@@ -294,7 +319,7 @@ static int enqueue_body(ramgpu_ctx* ctx, double dts) {
     { Timed t(ctx, 9); launch_padif(ctx->d, nullptr, ctx->stream); }
     ctx->launches += 2;
     CKL("pitch-angle diffusion");
-    if ((rc = enqueue_reverse(ctx, dts, false, nullptr))) return rc;
+    if ((rc = enqueue_reverse(ctx, dts, false, nullptr, true))) return rc;
   } else {
     if ((rc = enqueue_forward(ctx, dts, false, nullptr))) return rc;
     if ((rc = sumrc_stage(ctx, 0, 1))) return rc;
@@ -317,7 +342,7 @@ static int enqueue_body(ramgpu_ctx* ctx, double dts) {
       ctx->launches += 1;
       if ((rc = sumrc_stage(ctx, 7, 5))) return rc;
     }
-    if ((rc = enqueue_reverse(ctx, dts, false, nullptr))) return rc;
+    if ((rc = enqueue_reverse(ctx, dts, false, nullptr, true))) return rc;
     if ((rc = sumrc_stage(ctx, 5, 1))) return rc;
   }
   { Timed t(ctx, 6); launch_finish(ctx->d, ctx->stream); }
@@ -569,6 +594,7 @@ int ramgpu_destroy(ramgpu_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   drop_graph(ctx);
   adj_free(ctx);
+  cudaFree(ctx->d.coef);
   for (void* p : ctx->allocs) cudaFree(p);
   for (auto& sp : ctx->spans) { cudaEventDestroy(sp.a); cudaEventDestroy(sp.b); }
   for (cudaEvent_t e : ctx->ev_free) cudaEventDestroy(e);
@@ -908,7 +934,7 @@ int ramgpu_half_step(ramgpu_ctx* ctx, double dts, int order) {
   ctx->launches += 5;
   CKL("member tables");
   if (order == 0) rc = enqueue_forward(ctx, dts, true, ctx->d.loss1);
-  else rc = enqueue_reverse(ctx, dts, true, ctx->d.loss1);
+  else rc = enqueue_reverse(ctx, dts, true, ctx->d.loss1, false);
   if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->stream));
   return RAMGPU_OK;
@@ -1067,6 +1093,19 @@ int ramgpu_probe_fp64(double* lane_ops_per_s) {
   cudaFree(out);
   if (e != cudaSuccess) return fail(nullptr, RAMGPU_ERR_CUDA, cudaGetErrorString(e));
   *lane_ops_per_s = 8.0 * iters * (double)block * grid / (best * 1e-3);
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_coef_store(ramgpu_ctx* ctx, int enable) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  ctx->coef_enabled = enable != 0;
+  if (!ctx->coef_enabled && ctx->d.coef) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->d.coef);
+    ctx->d.coef = nullptr;
+    ctx->d.coef_items = 0;
+    ctx->shape_version += 1;
+  }
   return RAMGPU_OK;
 }
 

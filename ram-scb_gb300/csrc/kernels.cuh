@@ -51,13 +51,13 @@ __device__ __forceinline__ int stale_ghost_src(const Dev& d, int m, int slot, in
 // rec: branch record of the sweep, written (replay false) or, with replay
 // true, read back to run the sweep with those branches and clips frozen.
 void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr,
-                    bool replay = false);
+                    bool replay = false, int co = 0);
 void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr,
-                    bool replay = false);
+                    bool replay = false, int co = 0);
 void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr,
-                    bool replay = false);
+                    bool replay = false, int co = 0);
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
-                     cudaStream_t st, unsigned char* rec = nullptr, bool replay = false);
+                     cudaStream_t st, unsigned char* rec = nullptr, bool replay = false, int co = 0);
 
 int sweep_max_blocks_per_sm(int w, int blk);
 

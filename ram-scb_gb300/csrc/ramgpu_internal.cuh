@@ -100,6 +100,10 @@ struct Dev {
   double *mom_part;       // (nm*ns, 4 chunks, NE, NT, NR, 2) per-K moment partials
   double *ppert, *ppart;  // (nm*ns, NR, NT)
   double *sumrc_part;     // (nm*ns, nblk) SUMRC partial sums
+  // face coefficients C and a of the forward sweeps, read back by the
+  // reverse ones: (4 sweeps, 2, coef_items, ncell); null when not allocated
+  double *coef;
+  long long coef_items;
   // work list
   const int2 *items;      // (member, species)
   int nitems;
@@ -173,6 +177,11 @@ __device__ __forceinline__ double face_value_case(double x, double bx, double d,
   return act ? fb : fup;
 }
 constexpr int kClipBit = 8;  // recorded with the case: the updated cell was clipped
+
+// Stored face coefficient array q (0: C, 1: a) of sweep w for work item `it`.
+__device__ __forceinline__ double* coef_ptr(const Dev& d, int w, int q, long long it) {
+  return d.coef + (((long long)(w * 2 + q) * d.coef_items) + it) * d.ncell;
+}
 
 // Face value with the branch taken from a record (frozen-limiter replay):
 // LIMITER*X = beta*D | X | D | beta*X for cases 1..4, FUP for case 0.  For

@@ -18,7 +18,7 @@ namespace ramgpu {
 
 // ----------------------------------------------------------------- DRIFTR
 // Line (J,K,L) along I = 1..NR.  Faces 2..NR-1 (and NR on inflow lines).
-template <bool kCfl, int kRec>
+template <bool kCfl, int kRec, int kCo>
 __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = nt * ne * d.npa;
@@ -38,6 +38,10 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + (long long)line * nr;
       // branch record of the frozen-limiter adjoint: one byte per face/cell
       unsigned char* __restrict__ rl = kRec ? rec + (u / bpi) * d.ncell + (long long)line * nr : nullptr;
+      // face coefficients C and CORR factor a: stored by the forward sweep,
+      // read back by the reverse one (same DTs, same potential)
+      double* __restrict__ cst = kCo ? coef_ptr(d, 0, 0, u / bpi) + (long long)line * nr : nullptr;
+      double* __restrict__ ast = kCo ? coef_ptr(d, 0, 1, u / bpi) + (long long)line * nr : nullptr;
       const double* __restrict__ grt = d.grt + ((long long)l * nt + j) * nr;
       const double* __restrict__ cr = d.cr + ((long long)m * nt + j) * nr;
       const int* __restrict__ outside = d.outside + (long long)j * nr;
@@ -46,8 +50,9 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
       const bool closed = d.flags & 1u;
 
       const int k = (line / nt) % ne;
-      const double cN = fma(grt[nr - 1], p4, cr[nr - 1]);
-      const double cNm = fma(grt[nr - 2], p4, cr[nr - 2]);
+      const double cN = (kCo == 2) ? cst[nr - 1] : fma(grt[nr - 1], p4, cr[nr - 1]);
+      const double cNm = (kCo == 2) ? cst[nr - 2] : fma(grt[nr - 2], p4, cr[nr - 2]);
+      if (kCo == 1) { cst[nr - 1] = cN; cst[nr - 2] = cNm; }
       const bool inflow = is_neg(cN);
       // F(NR+1), F(NR+2): boundary ghosts on inflow lines.  On an outflow line
       // F(NR+1) is read only by face NR-1 when it is upwinded from the right,
@@ -61,7 +66,8 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
         g1 = stale_ghost(d, m, slot, j, k, l, p4);
       }
       double gm = fl[0], g0 = fl[1], gp = fl[2];
-      double c = fma(grt[0], p4, cr[0]);
+      double c = (kCo == 2) ? cst[0] : fma(grt[0], p4, cr[0]);
+      if (kCo == 1) cst[0] = c;
       if (kCfl && outside[0] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
       // face 1: FBND(1) = 0 (outflow) or F(2) (inflow)
       double phi_prev = c * ((inflow && !closed) ? g0 : 0.0);
@@ -70,10 +76,11 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
       for (int f = 2; f <= nr - 1; ++f) {  // 1-based face f, updates cell f
         const double gpp = (f + 2 <= nr) ? fl[f + 1] : g1;
         const double xp = gpp - gp, bxp = beta * fabs(xp);
-        c = fma(grt[f - 1], p4, cr[f - 1]);
+        c = (kCo == 2) ? cst[f - 1] : ((f == nr - 1) ? cNm : fma(grt[f - 1], p4, cr[f - 1]));
         if (kCfl && outside[f - 1] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
         const bool neg = is_neg(c);
-        const double a = fma(c, -0.5, neg ? -0.5 : 0.5);
+        const double a = (kCo == 2) ? ast[f - 1] : fma(c, -0.5, neg ? -0.5 : 0.5);
+        if (kCo == 1) { cst[f - 1] = c; ast[f - 1] = a; }
         int cs;
         const double fb = (kRec == 2)
             ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = rl[f - 1] & 7)
@@ -109,7 +116,7 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
 
 // ----------------------------------------------------------------- DRIFTP
 // Line (I,K,L), I = 2..NR, along J = 1..NT, periodic with J=1 == J=NT.
-template <bool kCfl, int kRec>
+template <bool kCfl, int kRec, int kCo>
 __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * ne * d.npa;
@@ -131,6 +138,8 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + ((long long)kl * nt) * nr + i;
       unsigned char* __restrict__ rl =
           kRec ? rec + (u / bpi) * d.ncell + ((long long)kl * nt) * nr + i : nullptr;
+      double* __restrict__ cst = kCo ? coef_ptr(d, 1, 0, u / bpi) + ((long long)kl * nt) * nr + i : nullptr;
+      double* __restrict__ ast = kCo ? coef_ptr(d, 1, 1, u / bpi) + ((long long)kl * nt) * nr + i : nullptr;
       const double* __restrict__ gpt = d.gpt + ((long long)l * nt) * nr + i;
       const double* __restrict__ ca = d.ca + ((long long)m * nt) * nr + i;
       const int* __restrict__ outside = d.outside + i;
@@ -144,13 +153,14 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
       const double XNm = GN - GNm, bXNm = beta * fabs(XNm);
       const double XN = G2 - GN, bXN = beta * fabs(XN);
       // face NT first: its flux enters cell 2 through FBND(1)=FBND(NT)
-      const double cN = CJ(nt);
+      const double cN = (kCo == 2) ? cst[(long long)(nt - 1) * st] : CJ(nt);
       if (kCfl && outside[(long long)(nt - 1) * nr] == 0) q = umax64(q, cfl_bits(cN, kBits1em10));
       double phiN;
       int csN;
       {
         const bool neg = is_neg(cN);
-        const double a = fma(cN, -0.5, neg ? -0.5 : 0.5);
+        const double a = (kCo == 2) ? ast[(long long)(nt - 1) * st] : fma(cN, -0.5, neg ? -0.5 : 0.5);
+        if (kCo == 1) { cst[(long long)(nt - 1) * st] = cN; ast[(long long)(nt - 1) * st] = a; }
         phiN = cN * ((kRec == 2)
             ? face_value_frozen(XN, neg ? X2 : XNm, neg ? G2 : GN, a, beta, csN = rl[(long long)(nt - 1) * st] & 7)
             : face_value_case(XN, bXN, neg ? X2 : XNm, neg ? bX2 : bXNm, neg ? G2 : GN, a, csN));
@@ -171,10 +181,11 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
           xp = X1;
           bxp = bX1;
         }
-        const double c = CJ(J);
+        const double c = (kCo == 2) ? cst[(long long)(J - 1) * st] : CJ(J);
         if (kCfl && outside[(long long)(J - 1) * nr] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
         const bool neg = is_neg(c);
-        const double a = fma(c, -0.5, neg ? -0.5 : 0.5);
+        const double a = (kCo == 2) ? ast[(long long)(J - 1) * st] : fma(c, -0.5, neg ? -0.5 : 0.5);
+        if (kCo == 1) { cst[(long long)(J - 1) * st] = c; ast[(long long)(J - 1) * st] = a; }
         int cs;
         const unsigned char* rj = kRec ? rl + (long long)(J - 1) * st : nullptr;
         const double fb = (kRec == 2)
@@ -203,7 +214,7 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
 // ----------------------------------------------------------------- DRIFTE
 // Line (I,J,L), I = 2..NR, along K = 1..NE with extrapolated F(0), F(1)
 // and F(NE+1) = F(NE+2) = 0.  Cell K = 1 is never written.
-template <bool kCfl, int kRec>
+template <bool kCfl, int kRec, int kCo>
 __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * nt * d.npa;
@@ -225,6 +236,10 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + ((long long)l * ne * nt + j) * nr + i;
       unsigned char* __restrict__ rl =
           kRec ? rec + (u / bpi) * d.ncell + ((long long)l * ne * nt + j) * nr + i : nullptr;
+      double* __restrict__ cst =
+          kCo ? coef_ptr(d, 2, 0, u / bpi) + ((long long)l * ne * nt + j) * nr + i : nullptr;
+      double* __restrict__ ast =
+          kCo ? coef_ptr(d, 2, 1, u / bpi) + ((long long)l * ne * nt + j) * nr + i : nullptr;
       const long long fij = ((long long)l * nt + j) * nr + i;
       const double wet = d.wet[fij];
       const double ue = d.ue[(long long)m * nr * nt * d.npa + fij];
@@ -246,10 +261,11 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
       const double X2 = G3 - G2, bX2 = beta * fabs(X2);
       double phi_prev;
       {
-        const double c = CK(1);
+        const double c = (kCo == 2) ? cst[0] : CK(1);
         if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em10)) * d.ide[0]));
         const bool neg = is_neg(c);
-        const double a = fma(c, mhde[0], neg ? -0.5 : 0.5);
+        const double a = (kCo == 2) ? ast[0] : fma(c, mhde[0], neg ? -0.5 : 0.5);
+        if (kCo == 1) { cst[0] = c; ast[0] = a; }
         int cs;
         double fb = (kRec == 2) ? face_value_frozen(X1, neg ? X2 : X0, neg ? G2 : G1, a, beta, cs = rl[0] & 7)
                                 : face_value_case(X1, bX1, neg ? X2 : X0, neg ? bX2 : bX0, neg ? G2 : G1, a, cs);
@@ -261,10 +277,11 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
       for (int K = 2; K <= ne; ++K) {
         const double gpp = (K + 2 <= ne) ? GK(K + 2) : 0.0;
         const double xp = gpp - gp, bxp = beta * fabs(xp);
-        const double c = CK(K);
+        const double c = (kCo == 2) ? cst[(long long)(K - 1) * st] : CK(K);
         if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em10)) * d.ide[K - 1]));
         const bool neg = is_neg(c);
-        const double a = fma(c, mhde[K - 1], neg ? -0.5 : 0.5);
+        const double a = (kCo == 2) ? ast[(long long)(K - 1) * st] : fma(c, mhde[K - 1], neg ? -0.5 : 0.5);
+        if (kCo == 1) { cst[(long long)(K - 1) * st] = c; ast[(long long)(K - 1) * st] = a; }
         int cs;
         const unsigned char* rk = kRec ? rl + (long long)(K - 1) * st : nullptr;
         double fb = (kRec == 2) ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rk & 7)
@@ -290,7 +307,7 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
 // faces 2..NPA-2, FBND(NPA-1) = F(NPA), then the F2(NPA) extrapolation.
 // kLoss: 0 none, 1 multiply the result by table lossA (loss after the sweep),
 //        2 multiply the input by lossA (loss before the sweep).
-template <bool kCfl, int kLoss, int kRec>
+template <bool kCfl, int kLoss, int kRec, int kCo>
 __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const double* __restrict__ lossA,
                                                    unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa;
@@ -313,6 +330,8 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
       const long long off = (long long)jk * nr + i;  // (K*NT + J)*NR + I
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + off;
       unsigned char* __restrict__ rl = kRec ? rec + (u / bpi) * d.ncell + off : nullptr;
+      double* __restrict__ cst = kCo ? coef_ptr(d, 3, 0, u / bpi) + off : nullptr;
+      double* __restrict__ ast = kCo ? coef_ptr(d, 3, 1, u / bpi) + off : nullptr;
       const double* __restrict__ la = lossA ? lossA + (long long)s * d.ncell + off : nullptr;
       const long long sij = (long long)nt * nr;     // stride of (I,J,L) tables in L
       const long long fij = (long long)j * nr + i;
@@ -337,10 +356,11 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         double gpp = GL(L + 2);
         if (kLoss == 2) gpp *= LA(L + 2);
         const double xp = gpp - gp, bxp = beta * fabs(xp);
-        const double c = CL(L);
+        const double c = (kCo == 2) ? cst[(long long)(L - 1) * st] : CL(L);
         if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
         const bool neg = is_neg(c);
-        const double a = fma(c, mhdmu[L - 1], neg ? -0.5 : 0.5);
+        const double a = (kCo == 2) ? ast[(long long)(L - 1) * st] : fma(c, mhdmu[L - 1], neg ? -0.5 : 0.5);
+        if (kCo == 1) { cst[(long long)(L - 1) * st] = c; ast[(long long)(L - 1) * st] = a; }
         int cs;
         const unsigned char* rq = kRec ? rl + (long long)(L - 1) * st : nullptr;
         const double fb = (kRec == 2) ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rq & 7)
@@ -358,7 +378,8 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
       // face NPA-1: FBND = F(NPA); cell NPA-1; then the F2(NPA) ghost
       {
         const int L = npa - 1;
-        const double c = CL(L);
+        const double c = (kCo == 2) ? cst[(long long)(L - 1) * st] : CL(L);
+        if (kCo == 1) cst[(long long)(L - 1) * st] = c;
         if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
         const double phi = c * (closed ? 0.0 : gp);
         const double raw = fma(phi_prev - phi, iwmu[L - 1], g0);
@@ -397,48 +418,56 @@ static inline int nlines_of(const Dev& d, int w) {
   }
 }
 
-void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay) {
+// co: 0 compute the face coefficients, 1 compute and store them, 2 load
+// the stored ones (needs d.coef; the plain, store and load forms give
+// identical results).
+void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay, int co) {
   dim3 g = grid_for(d, 0, nlines_of(d, 0));
-  if (rec && replay) k_sweep_r<false, 2><<<g, d.blk[0], 0, st>>>(d, dts, rec);
-  else if (rec) k_sweep_r<false, 1><<<g, d.blk[0], 0, st>>>(d, dts, rec);
-  else if (cfl) k_sweep_r<true, 0><<<g, d.blk[0], 0, st>>>(d, dts, nullptr);
-  else k_sweep_r<false, 0><<<g, d.blk[0], 0, st>>>(d, dts, nullptr);
+  const int b = d.blk[0];
+  if (rec && replay) k_sweep_r<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec);
+  else if (rec) k_sweep_r<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec);
+  else if (co == 1) k_sweep_r<true, 0, 1><<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (co == 2) k_sweep_r<false, 0, 2><<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (cfl) k_sweep_r<true, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr);
+  else k_sweep_r<false, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr);
 }
-void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay) {
+void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay, int co) {
   dim3 g = grid_for(d, 1, nlines_of(d, 1));
-  if (rec && replay) k_sweep_p<false, 2><<<g, d.blk[1], 0, st>>>(d, dts, rec);
-  else if (rec) k_sweep_p<false, 1><<<g, d.blk[1], 0, st>>>(d, dts, rec);
-  else if (cfl) k_sweep_p<true, 0><<<g, d.blk[1], 0, st>>>(d, dts, nullptr);
-  else k_sweep_p<false, 0><<<g, d.blk[1], 0, st>>>(d, dts, nullptr);
+  const int b = d.blk[1];
+  if (rec && replay) k_sweep_p<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec);
+  else if (rec) k_sweep_p<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec);
+  else if (co == 1) k_sweep_p<true, 0, 1><<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (co == 2) k_sweep_p<false, 0, 2><<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (cfl) k_sweep_p<true, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr);
+  else k_sweep_p<false, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr);
 }
-void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay) {
+void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay, int co) {
   dim3 g = grid_for(d, 2, nlines_of(d, 2));
-  if (rec && replay) k_sweep_e<false, 2><<<g, d.blk[2], 0, st>>>(d, dts, rec);
-  else if (rec) k_sweep_e<false, 1><<<g, d.blk[2], 0, st>>>(d, dts, rec);
-  else if (cfl) k_sweep_e<true, 0><<<g, d.blk[2], 0, st>>>(d, dts, nullptr);
-  else k_sweep_e<false, 0><<<g, d.blk[2], 0, st>>>(d, dts, nullptr);
+  const int b = d.blk[2];
+  if (rec && replay) k_sweep_e<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec);
+  else if (rec) k_sweep_e<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec);
+  else if (co == 1) k_sweep_e<true, 0, 1><<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (co == 2) k_sweep_e<false, 0, 2><<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (cfl) k_sweep_e<true, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr);
+  else k_sweep_e<false, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr);
+}
+template <int kLoss>
+static void mu_launch(const Dev& d, dim3 g, int b, double dts, const double* loss, cudaStream_t st,
+                      unsigned char* rec, bool replay, bool cfl, int co) {
+  if (rec && replay) k_sweep_mu<false, kLoss, 2, 0><<<g, b, 0, st>>>(d, dts, loss, rec);
+  else if (rec) k_sweep_mu<false, kLoss, 1, 0><<<g, b, 0, st>>>(d, dts, loss, rec);
+  else if (co == 1) k_sweep_mu<true, kLoss, 0, 1><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+  else if (co == 2) k_sweep_mu<false, kLoss, 0, 2><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+  else if (cfl) k_sweep_mu<true, kLoss, 0, 0><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+  else k_sweep_mu<false, kLoss, 0, 0><<<g, b, 0, st>>>(d, dts, loss, nullptr);
 }
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
-                     cudaStream_t st, unsigned char* rec, bool replay) {
+                     cudaStream_t st, unsigned char* rec, bool replay, int co) {
   dim3 g = grid_for(d, 3, nlines_of(d, 3));
   const int b = d.blk[3];
-  if (rec && replay) {
-    if (loss_mode == 1) k_sweep_mu<false, 1, 2><<<g, b, 0, st>>>(d, dts, loss, rec);
-    else if (loss_mode == 2) k_sweep_mu<false, 2, 2><<<g, b, 0, st>>>(d, dts, loss, rec);
-    else k_sweep_mu<false, 0, 2><<<g, b, 0, st>>>(d, dts, nullptr, rec);
-  } else if (rec) {
-    if (loss_mode == 1) k_sweep_mu<false, 1, 1><<<g, b, 0, st>>>(d, dts, loss, rec);
-    else if (loss_mode == 2) k_sweep_mu<false, 2, 1><<<g, b, 0, st>>>(d, dts, loss, rec);
-    else k_sweep_mu<false, 0, 1><<<g, b, 0, st>>>(d, dts, nullptr, rec);
-  } else if (cfl) {
-    if (loss_mode == 1) k_sweep_mu<true, 1, 0><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-    else if (loss_mode == 2) k_sweep_mu<true, 2, 0><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-    else k_sweep_mu<true, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr, nullptr);
-  } else {
-    if (loss_mode == 1) k_sweep_mu<false, 1, 0><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-    else if (loss_mode == 2) k_sweep_mu<false, 2, 0><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-    else k_sweep_mu<false, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr, nullptr);
-  }
+  if (loss_mode == 1) mu_launch<1>(d, g, b, dts, loss, st, rec, replay, cfl, co);
+  else if (loss_mode == 2) mu_launch<2>(d, g, b, dts, loss, st, rec, replay, cfl, co);
+  else mu_launch<0>(d, g, b, dts, nullptr, st, rec, replay, cfl, co);
 }
 
 // Resident CTAs per SM of sweep w at block size blk (for persistent grids).
@@ -446,10 +475,10 @@ int sweep_max_blocks_per_sm(int w, int blk) {
   int n = 0;
   cudaError_t e = cudaSuccess;
   switch (w) {
-    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_r<false, 0>, blk, 0); break;
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_p<false, 0>, blk, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_e<false, 0>, blk, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_mu<false, 0, 0>, blk, 0); break;
+    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_r<false, 0, 0>, blk, 0); break;
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_p<false, 0, 0>, blk, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_e<false, 0, 0>, blk, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_mu<false, 0, 0, 0>, blk, 0); break;
   }
   return e == cudaSuccess ? n : 0;
 }

@@ -36,7 +36,7 @@ EXPORTS = (
     "ramgpu_adj_forward", "ramgpu_adj_backward", "ramgpu_adj_digest", "ramgpu_adj_record",
     "ramgpu_fly_sats", "ramgpu_sum_pressure", "ramgpu_adj_replay", "ramgpu_set_pa_diffusion",
     "ramgpu_loss_wae", "ramgpu_bounce_integrals", "ramgpu_upload_f2_async", "ramgpu_download_f2_async",
-    "ramgpu_moments_async", "ramgpu_synchronize",
+    "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
@@ -143,6 +143,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_download_f2_async": ([vp, i, i, dp], i),
         "ramgpu_moments_async": ([vp, i, i, dp, dp], i),
         "ramgpu_synchronize": ([vp], i),
+        "ramgpu_set_coef_store": ([vp, i], i),
         "ramgpu_sum_pressure": ([vp, i, dp, dp], i),
     }
     for name, (args, res) in sig.items():
@@ -381,6 +382,9 @@ class RamGpu:
         self._ck(self.lib.ramgpu_kernel_times(self.h, _dptr(ms), cnt.ctypes.data_as(C.POINTER(C.c_longlong))),
                  "kernel_times")
         return {KCLASS[k]: (float(ms[k]), int(cnt[k])) for k in range(len(KCLASS)) if cnt[k]}
+
+    def set_coef_store(self, enable: bool):
+        self._ck(self.lib.ramgpu_set_coef_store(self.h, int(bool(enable))), "set_coef_store")
 
     def set_graph(self, enable: bool):
         self._ck(self.lib.ramgpu_set_graph(self.h, int(bool(enable))), "set_graph")
