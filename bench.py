@@ -515,7 +515,8 @@ def run_gb300(args, rank, world, local_rank):
         return wl.kp(2 * step)
 
     gpu.set_kp(-1, kp_at(0))
-    gpu.set_coef_store(not args.no_coef_store)
+    if args.no_coef_store:
+        gpu.set_coef_store(0)
     shapes, _ = gpu.autotune(wl.dts) if not args.no_autotune else (gpu.launch_shape(), None)
     gpu.set_graph(not args.no_graph)
     # warm-up (builds the DTs tables, captures the graph)
@@ -636,7 +637,7 @@ def run_gb300(args, rank, world, local_rank):
         "config": {"workload": workload_desc(wl), "step": "one ram_run call = 2 DTs steps",
                    "cells_per_step": cells_per_step, "l2": "flushed between timed steps (256 MB write)",
                    "graph": not args.no_graph, "launch_shapes": shapes,
-                   "coef_store": not args.no_coef_store,
+                   "coef_store": "none" if args.no_coef_store else "DRIFTE",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak,

@@ -253,13 +253,14 @@ int ramgpu_sum_pressure(ramgpu_ctx *ctx, int member, double *pallsum, double *pp
 
 /* ---- execution tuning (no reference counterpart) ------------------------ */
 
-/* Keep each face's coefficient C and CORR factor from the forward sweeps of a
- * ram_run call and read them back in its reverse sweeps (enable = 1, the
- * default), instead of recomputing them: 64 bytes per cell and (member,
- * species) of device memory, taken only while it fits in a quarter of the
- * free memory, for about 2 FP64 operations per face less in the reverse
- * half.  Results are identical either way. */
-int ramgpu_set_coef_store(ramgpu_ctx *ctx, int enable);
+/* Sweeps whose face coefficient C and CORR factor the forward half of a
+ * ram_run call keeps for its reverse half, which then reads them instead of
+ * recomputing them: bit 0 R, 1 P, 2 E, 3 MU.  Each set bit costs 16 bytes
+ * per cell and (member, species) of device memory, taken only while it fits
+ * in a quarter of the free memory.  Default 4 (DRIFTE only, whose C costs
+ * two FP64 operations; for the other sweeps the stores cost more time than
+ * the FP64 work they save).  Results are identical for every mask. */
+int ramgpu_set_coef_store(ramgpu_ctx *ctx, int mask);
 
 /* Replay ram_run / ram_run_async from a CUDA graph captured on first use and
  * re-captured when dts, the active (member, species) list, the flags or the

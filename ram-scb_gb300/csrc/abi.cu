@@ -45,7 +45,11 @@ struct ramgpu_ctx {
   bool have_grid = false, have_fields = false;
   bool field_dirty = true, static_dirty = true;
   double tables_dts = -1.0;
-  bool coef_enabled = true;  // store face coefficients between the two halves
+  // sweeps (bit w: R, P, E, MU) whose face coefficients the forward half
+  // stores for the reverse half; measured on GB300, only DRIFTE (two FP64
+  // operations for C) gains, the others lose more to the stores than they
+  // save in FP64 work
+  unsigned coef_mask = 4u;
   // implicit pitch-angle diffusion: species with a coefficient, tables state
   std::vector<int> pd_on_h;
   bool pd_alloc = false, pd_dirty = false;
@@ -227,11 +231,13 @@ static int prepare(ramgpu_ctx* ctx, double dts) {
   }
   // face-coefficient store for the reverse half: 64 bytes per cell and item,
   // kept only while it takes at most a quarter of the free device memory
-  if (ctx->coef_enabled && ctx->d.coef_items < ctx->d.nitems) {
+  if (ctx->coef_mask && ctx->d.coef_items < ctx->d.nitems) {
     cudaFree(ctx->d.coef);
     ctx->d.coef = nullptr;
     ctx->d.coef_items = 0;
-    const size_t need = (size_t)8 * ctx->d.nitems * ctx->d.ncell * sizeof(double);
+    int nw = 0;
+    for (int w = 0; w < 4; ++w) ctx->d.coef_slot[w] = ((ctx->coef_mask >> w) & 1u) ? nw++ : -1;
+    const size_t need = (size_t)2 * nw * ctx->d.nitems * ctx->d.ncell * sizeof(double);
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && need <= fr / 4 &&
         cudaMalloc(&ctx->d.coef, need) == cudaSuccess) {
@@ -276,11 +282,12 @@ static int sumrc_stage(ramgpu_ctx* ctx, int stage, int which) {
 // they also keep each face's C and CORR factor for the reverse half.
 static int enqueue_forward(ramgpu_ctx* ctx, double dts, bool loss_fused, const double* loss_table) {
   CK(cudaMemsetAsync(ctx->d.cflq, 0, sizeof(unsigned long long) * 4 * ctx->d.nm * ctx->d.ns, ctx->stream));
-  const int co = ctx->d.coef ? 1 : 0;
-  { Timed t(ctx, 2); launch_sweep_r(ctx->d, dts, true, ctx->stream, nullptr, false, co); }
-  { Timed t(ctx, 3); launch_sweep_p(ctx->d, dts, true, ctx->stream, nullptr, false, co); }
-  { Timed t(ctx, 4); launch_sweep_e(ctx->d, dts, true, ctx->stream, nullptr, false, co); }
-  { Timed t(ctx, 5); launch_sweep_mu(ctx->d, dts, true, loss_fused ? 1 : 0, loss_table, ctx->stream, nullptr, false, co); }
+  const Dev& d = ctx->d;
+  auto co = [&](int w) { return (d.coef && d.coef_slot[w] >= 0) ? 1 : 0; };
+  { Timed t(ctx, 2); launch_sweep_r(d, dts, true, ctx->stream, nullptr, false, co(0)); }
+  { Timed t(ctx, 3); launch_sweep_p(d, dts, true, ctx->stream, nullptr, false, co(1)); }
+  { Timed t(ctx, 4); launch_sweep_e(d, dts, true, ctx->stream, nullptr, false, co(2)); }
+  { Timed t(ctx, 5); launch_sweep_mu(d, dts, true, loss_fused ? 1 : 0, loss_table, ctx->stream, nullptr, false, co(3)); }
   ctx->launches += 4;
   CKL("forward sweeps");
   return RAMGPU_OK;
@@ -290,11 +297,12 @@ static int enqueue_forward(ramgpu_ctx* ctx, double dts, bool loss_fused, const d
 // before, so its stored face coefficients are read back.
 static int enqueue_reverse(ramgpu_ctx* ctx, double dts, bool loss_fused, const double* loss_table,
                            bool after_forward) {
-  const int co = (after_forward && ctx->d.coef) ? 2 : 0;
-  { Timed t(ctx, 5); launch_sweep_mu(ctx->d, dts, false, loss_fused ? 2 : 0, loss_table, ctx->stream, nullptr, false, co); }
-  { Timed t(ctx, 4); launch_sweep_e(ctx->d, dts, false, ctx->stream, nullptr, false, co); }
-  { Timed t(ctx, 3); launch_sweep_p(ctx->d, dts, false, ctx->stream, nullptr, false, co); }
-  { Timed t(ctx, 2); launch_sweep_r(ctx->d, dts, false, ctx->stream, nullptr, false, co); }
+  const Dev& d = ctx->d;
+  auto co = [&](int w) { return (after_forward && d.coef && d.coef_slot[w] >= 0) ? 2 : 0; };
+  { Timed t(ctx, 5); launch_sweep_mu(d, dts, false, loss_fused ? 2 : 0, loss_table, ctx->stream, nullptr, false, co(3)); }
+  { Timed t(ctx, 4); launch_sweep_e(d, dts, false, ctx->stream, nullptr, false, co(2)); }
+  { Timed t(ctx, 3); launch_sweep_p(d, dts, false, ctx->stream, nullptr, false, co(1)); }
+  { Timed t(ctx, 2); launch_sweep_r(d, dts, false, ctx->stream, nullptr, false, co(0)); }
   ctx->launches += 4;
   CKL("reverse sweeps");
   return RAMGPU_OK;
@@ -1096,16 +1104,16 @@ int ramgpu_probe_fp64(double* lane_ops_per_s) {
   return RAMGPU_OK;
 }
 
-int ramgpu_set_coef_store(ramgpu_ctx* ctx, int enable) {
+int ramgpu_set_coef_store(ramgpu_ctx* ctx, int mask) {
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
-  ctx->coef_enabled = enable != 0;
-  if (!ctx->coef_enabled && ctx->d.coef) {
-    CK(cudaStreamSynchronize(ctx->stream));
-    cudaFree(ctx->d.coef);
-    ctx->d.coef = nullptr;
-    ctx->d.coef_items = 0;
-    ctx->shape_version += 1;
-  }
+  if (mask < 0 || mask > 15) return fail(ctx, RAMGPU_ERR_ARG, "mask: bits 0-3 (R, P, E, MU)");
+  if ((unsigned)mask == ctx->coef_mask) return RAMGPU_OK;
+  ctx->coef_mask = (unsigned)mask;
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(ctx->d.coef);  // reallocated for the new set by the next step
+  ctx->d.coef = nullptr;
+  ctx->d.coef_items = 0;
+  ctx->shape_version += 1;
   return RAMGPU_OK;
 }
 

@@ -101,9 +101,11 @@ struct Dev {
   double *ppert, *ppart;  // (nm*ns, NR, NT)
   double *sumrc_part;     // (nm*ns, nblk) SUMRC partial sums
   // face coefficients C and a of the forward sweeps, read back by the
-  // reverse ones: (4 sweeps, 2, coef_items, ncell); null when not allocated
+  // reverse ones: (stored sweeps, 2, coef_items, ncell); coef_slot[w] is
+  // sweep w's place or -1; null when not allocated
   double *coef;
   long long coef_items;
+  int coef_slot[4];
   // work list
   const int2 *items;      // (member, species)
   int nitems;
@@ -180,7 +182,7 @@ constexpr int kClipBit = 8;  // recorded with the case: the updated cell was cli
 
 // Stored face coefficient array q (0: C, 1: a) of sweep w for work item `it`.
 __device__ __forceinline__ double* coef_ptr(const Dev& d, int w, int q, long long it) {
-  return d.coef + (((long long)(w * 2 + q) * d.coef_items) + it) * d.ncell;
+  return d.coef + (((long long)(d.coef_slot[w] * 2 + q) * d.coef_items) + it) * d.ncell;
 }
 
 // Face value with the branch taken from a record (frozen-limiter replay):

@@ -383,8 +383,11 @@ class RamGpu:
                  "kernel_times")
         return {KCLASS[k]: (float(ms[k]), int(cnt[k])) for k in range(len(KCLASS)) if cnt[k]}
 
-    def set_coef_store(self, enable: bool):
-        self._ck(self.lib.ramgpu_set_coef_store(self.h, int(bool(enable))), "set_coef_store")
+    def set_coef_store(self, mask):
+        """Sweeps (bit 0 R, 1 P, 2 E, 3 MU; True = 4, False = 0) whose forward
+        face coefficients are kept for the reverse half."""
+        m = (4 if mask else 0) if isinstance(mask, bool) else int(mask)
+        self._ck(self.lib.ramgpu_set_coef_store(self.h, m), "set_coef_store")
 
     def set_graph(self, enable: bool):
         self._ck(self.lib.ramgpu_set_graph(self.h, int(bool(enable))), "set_graph")

@@ -228,7 +228,7 @@ def test_coefficient_store_is_bitwise_neutral(name):
     half gives the same bits as recomputing them (also with graph replay)."""
     wl = W.make_workload(name)
     outs = []
-    for store, graph in ((False, False), (True, False), (True, True)):
+    for store, graph in ((0, False), (15, False), (4, True), (15, True)):
         gpu = _gpu(wl, 4.0)
         gpu.set_coef_store(store)
         gpu.set_graph(graph)
