@@ -118,6 +118,13 @@ int ramgpu_set_fields(ramgpu_ctx *ctx, const double *fnhs, const double *fnis,
  * once.  daa = NULL removes it.  The adjoint does not cover it. */
 int ramgpu_set_pa_diffusion(ramgpu_ctx *ctx, int s, const double *daa);
 
+/* The field tables as the context holds them (for example after
+ * ramgpu_compute_hI), same shapes as ramgpu_set_fields; any output may be
+ * NULL. */
+int ramgpu_get_fields(ramgpu_ctx *ctx, double *fnhs, double *fnis, double *bounhs, double *bounis,
+                      double *hdns, double *didt, double *dibndt, double *bnes, double *dbdt,
+                      double *eir, double *eip);
+
 /* GEOSB output FGEOS(S,:,:,:) of one species (src/ModRamBoundary.f90:241-319):
  * (NT,NE,NPA), host or device memory.  member < 0 sets it for every member. */
 int ramgpu_set_boundary(ramgpu_ctx *ctx, int member, int s, const double *fgeos_s);
@@ -244,6 +251,22 @@ int ramgpu_fly_sats(ramgpu_ctx *ctx, const ramgpu_sat *sats, int nsat, double *s
 int ramgpu_bounce_integrals(ramgpu_ctx *ctx, int nthe, const double *chi, const double *x,
                             const double *y, const double *z, const double *b, const double *dens,
                             int ieq, double *h, double *fi, double *hdens, double *bmirror);
+
+/* computehI's producer on the device: the bounce integrals above, then the
+ * RAM-variable fill of src/ModRamScb.f90:458-463,520-632 written straight
+ * into the context's field tables -- lines outside the magnetopause take
+ * the previous radial point; FNHS, FNIS, HDNS for I = 2..NR+1 from line
+ * I-1; BOUNHS, BOUNIS from h and I interpolated in pitch angle at the bin
+ * boundaries PAbn (Steffen's monotone cubic, as the reference's default
+ * 1-D interpolation); BNES = equatorial B * bnormal / 1e9; dIdt, dIbndt,
+ * dBdt over dthi seconds (0 when |dthi| <= 1e-9); the I = 1 row (dipole
+ * BNES, EIR = EIP = 0) and the NaN repair.  pa, pabn: PA and PAbn of
+ * ARRAYS (NPA).  The SCB-to-RAM line conversion, the outside-SCB scaling
+ * and the optional Gaussian smoothing are the caller's.  The next step
+ * rebuilds every derived table. */
+int ramgpu_compute_hI(ramgpu_ctx *ctx, int nthe, const double *chi, const double *x, const double *y,
+                      const double *z, const double *b, const double *dens, int ieq, const double *pa,
+                      const double *pabn, double bnormal, double dthi);
 
 /* SCB hand-off, ram_sum_pressure (src/ModRamFunctions.f90:272-297):
  * PAllSum(I,J) = sum_S (2/3 PPERT(S,I,J) + 1/3 PPART(S,I,J)) and

@@ -96,6 +96,7 @@ def load():
                                     C.POINTER(RoLosses), _P, C.c_int, PP]
         lib.ro_padif.argtypes = [gp, pp, _P, _P]
         lib.ro_bounce_integrals.argtypes = [gp, C.c_int, _P, _P, _P, _P, _P, _P, C.c_int, _P, _P, _P, _P]
+        lib.ro_install_hI.argtypes = [gp, _P, _P, _P, _P, _P, _P, C.c_double, C.c_double] + [_P] * 11
         U8 = C.POINTER(C.c_ubyte)
         lib.ro_driftr_rec.argtypes = [gp, sp, pp, dpp, _P, _P, _P, _P, U8, _IP]
         lib.ro_driftr_rec.restype = C.c_double
@@ -235,6 +236,22 @@ class Oracle:
                                      _p(_f(lines.y)), _p(_f(lines.z)), _p(b), _p(_f(lines.dens)),
                                      int(lines.ieq), _p(h), _p(fi), _p(hd), _p(bm))
         return h, fi, hd, bm
+
+    def compute_hI(self, lines, bnormal=1.0, dthi=0.0, fields=None):
+        """computehI's integrals and RAM-variable fill: a dict of new field
+        tables (as Fields, Fortran order) starting from ``fields`` (default
+        this oracle's).  The oracle's own fields are left unchanged."""
+        g = self.grid
+        h, fi, hd, bm = self.bounce_integrals(lines)
+        beq = _f(bm[:, :, 0])
+        src = fields if fields is not None else {k[2:]: v for k, v in self._keep.items() if k.startswith("f_")}
+        out = {k: _f(src[k]).copy(order="F") for k in ("fnhs", "fnis", "hdns", "bounhs", "bounis", "bnes", "dbdt",
+                                                       "didt", "dibndt", "eir", "eip")}
+        self.lib.ro_install_hI(C.byref(self.rg), _p(_f(g.pa)), _p(_f(g.pabn)), _p(h), _p(fi), _p(hd), _p(beq),
+                               float(bnormal), float(dthi),
+                               *[_p(out[k]) for k in ("fnhs", "fnis", "hdns", "bounhs", "bounis", "bnes", "dbdt",
+                                                      "didt", "dibndt", "eir", "eip")])
+        return out
 
     def cepara(self, s, dts, do_atmol=True):
         g = self.grid

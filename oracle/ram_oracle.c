@@ -1348,3 +1348,150 @@ void ro_bounce_integrals(const ro_grid *g, int nthe, const double *chi, const do
         }
     free(mirror); free(yI); free(yH); free(yD);
 }
+
+/* Monotone cubic interpolation of Steffen (1990, A&A 239, 443): interior
+ * slopes by his eq. (11) -- the harmonic-limited average of the adjacent
+ * secants, zero at local extrema -- and the one-sided secants at the two
+ * ends (the simplest boundary choice of his section 2.2); Hermite cubics
+ * in between.  Outside [xa[0], xa[n-1]] the value is extrapolated
+ * linearly from the first or last two points, and xa is first reduced to
+ * its strictly increasing subsequence, as the reference's 1-D wrapper
+ * does (src/ModRamGSL.f90:261-311, src/RamGSL.c:111-175). */
+static double sgn1(double v) { return v < 0 ? -1.0 : 1.0; }
+
+static void steffen_eval(int n0, const double *xa0, const double *fa0, int nb, const double *xb, double *fb)
+{
+    double xa[512], fa[512], yp[512];
+    int n = 0;
+    for (int i = 0; i < n0; ++i)
+        if (n == 0 || xa0[i] > xa[n - 1]) { xa[n] = xa0[i]; fa[n] = fa0[i]; ++n; }
+    if (n < 2) {
+        for (int q = 0; q < nb; ++q) fb[q] = n ? fa[0] : 0.;
+        return;
+    }
+    yp[0] = (fa[1] - fa[0]) / (xa[1] - xa[0]);
+    for (int i = 1; i < n - 1; ++i) {
+        double hm = xa[i] - xa[i - 1], h = xa[i + 1] - xa[i];
+        double sm = (fa[i] - fa[i - 1]) / hm, s = (fa[i + 1] - fa[i]) / h;
+        double p = (sm * h + s * hm) / (hm + h);
+        double m = fabs(sm);
+        if (fabs(s) < m) m = fabs(s);
+        if (0.5 * fabs(p) < m) m = 0.5 * fabs(p);
+        yp[i] = (sgn1(sm) + sgn1(s)) * m;
+    }
+    yp[n - 1] = (fa[n - 1] - fa[n - 2]) / (xa[n - 1] - xa[n - 2]);
+    for (int q = 0; q < nb; ++q) {
+        double x = xb[q];
+        if (x <= xa[0]) { fb[q] = fa[0] + (x - xa[0]) / (xa[1] - xa[0]) * (fa[1] - fa[0]); continue; }
+        if (x >= xa[n - 1]) {
+            fb[q] = fa[n - 1] + (x - xa[n - 1]) / (xa[n - 2] - xa[n - 1]) * (fa[n - 2] - fa[n - 1]);
+            continue;
+        }
+        int i = 0;
+        while (i < n - 2 && xa[i + 1] <= x) ++i;
+        double h = xa[i + 1] - xa[i], s = (fa[i + 1] - fa[i]) / h;
+        double a = (yp[i] + yp[i + 1] - 2 * s) / h / h, b = (3 * s - 2 * yp[i] - yp[i + 1]) / h;
+        double t = x - xa[i];
+        fb[q] = fa[i] + t * (yp[i] + t * (b + t * a));
+    }
+}
+
+/* The RAM-variable fill of computehI (src/ModRamScb.f90:520-630) from the
+ * bounce integrals of ro_bounce_integrals: h and I interpolated in pitch
+ * angle to the bin boundaries PAbn (BOUNHS, BOUNIS, :520-531), lines
+ * outside the magnetopause given the previous radial point's values
+ * (:458-463), FNHS/FNIS/HDNS/BOUNHS/BOUNIS/BNES for I = 2..NR+1 from line
+ * I-1 with the time derivatives over dthi (:566-602), the I = 1 row (:603-
+ * 618) and the NaN repair (:620-632).  beq: equatorial B of each line in
+ * the units of b, bnormal converts them to nT.  The field arrays (the ones
+ * ro_grid points to) are updated in place. */
+void ro_install_hI(ro_grid *g, const double *pa, const double *pabn, const double *hc, const double *ic,
+                   const double *dc, const double *beq, double bnormal, double dthi, double *fnhs, double *fnis,
+                   double *hdns, double *bounhs, double *bounis, double *bnes, double *dbdt, double *didt,
+                   double *dibndt, double *eir, double *eip)
+{
+    size_t na = (size_t)NR * NT * NPA;
+    double *h = (double *)malloc(sizeof(double) * na), *fi = (double *)malloc(sizeof(double) * na);
+    double *hd = (double *)malloc(sizeof(double) * na), *hb = (double *)malloc(sizeof(double) * na);
+    double *ib = (double *)malloc(sizeof(double) * na), *be = (double *)malloc(sizeof(double) * NR * NT);
+    memcpy(h, hc, sizeof(double) * na); memcpy(fi, ic, sizeof(double) * na); memcpy(hd, dc, sizeof(double) * na);
+    memcpy(be, beq, sizeof(double) * NR * NT);
+#define A3(a, i, j, L) a[((size_t)((L)-1) * NT + (j)-1) * NR + (i)-1]
+    /* outside the magnetopause: the previous radial point */
+    for (int j = 1; j <= NT; ++j)
+        for (int i = 2; i <= NR; ++i)
+            if (OUTSIDE(i, j) == 1) {
+                for (int L = 1; L <= NPA; ++L) {
+                    A3(fi, i, j, L) = A3(fi, i - 1, j, L);
+                    A3(h, i, j, L) = A3(h, i - 1, j, L);
+                    A3(hd, i, j, L) = A3(hd, i - 1, j, L);
+                }
+                be[(size_t)(j - 1) * NR + i - 1] = be[(size_t)(j - 1) * NR + i - 2];
+            }
+    /* PA(NPA:1:-1) -> PAbn(NPA-1:2:-1) */
+    double xa[512], fa[512], xb[512], fb[512];
+    for (int L = 0; L < NPA; ++L) xa[L] = pa[NPA - 1 - L];
+    for (int q = 0; q < NPA - 2; ++q) xb[q] = pabn[NPA - 2 - q];
+    for (int i = 1; i <= NR; ++i)
+        for (int j = 1; j <= NT; ++j) {
+            for (int w = 0; w < 2; ++w) {
+                const double *src = w ? fi : h;
+                double *dst = w ? ib : hb;
+                for (int L = 0; L < NPA; ++L) fa[L] = A3(src, i, j, NPA - L);
+                steffen_eval(NPA, xa, fa, NPA - 2, xb, fb);
+                for (int q = 0; q < NPA - 2; ++q) A3(dst, i, j, NPA - 1 - q) = fb[q];
+                A3(dst, i, j, NPA) = A3(dst, i, j, NPA - 1);
+                A3(dst, i, j, 1) = A3(dst, i, j, 2);
+            }
+        }
+    const int nf = NR + 1;
+#define F3(a, I, J, L) a[((size_t)((L)-1) * NT + (J)-1) * nf + (I)-1]
+#define F2D(a, I, J) a[(size_t)((J)-1) * nf + (I)-1]
+    const int dt0 = fabs(dthi) <= 1e-9;
+    for (int I = 2; I <= NR + 1; ++I)
+        for (int J = 1; J <= NT; ++J) {
+            double bprev = F2D(bnes, I, J);
+            for (int L = 1; L <= NPA; ++L) {
+                double fip = F3(fnis, I, J, L), bip = F3(bounis, I, J, L);
+                F3(fnhs, I, J, L) = A3(h, I - 1, J, L);
+                F3(fnis, I, J, L) = A3(fi, I - 1, J, L);
+                F3(hdns, I, J, L) = A3(hd, I - 1, J, L);
+                F3(bounhs, I, J, L) = A3(hb, I - 1, J, L);
+                F3(bounis, I, J, L) = A3(ib, I - 1, J, L);
+                F3(didt, I, J, L) = dt0 ? 0. : (F3(fnis, I, J, L) - fip) / dthi;
+                F3(dibndt, I, J, L) = dt0 ? 0. : (F3(bounis, I, J, L) - bip) / dthi;
+            }
+            F2D(bnes, I, J) = be[(size_t)(J - 1) * NR + I - 2] * bnormal / 1e9;
+            F2D(dbdt, I, J) = dt0 ? 0. : (F2D(bnes, I, J) - bprev) / dthi;
+        }
+    for (int J = 1; J <= NT; ++J) {
+        F2D(bnes, 1, J) = 0.32 / (LZ(1) * LZ(1) * LZ(1)) / 1.e4;
+        F2D(dbdt, 1, J) = 0.;
+        F2D(eir, 1, J) = 0.;
+        F2D(eip, 1, J) = 0.;
+        for (int L = 1; L <= NPA; ++L) {
+            F3(fnhs, 1, J, L) = F3(fnhs, 2, J, L);
+            F3(fnis, 1, J, L) = F3(fnis, 2, J, L);
+            F3(bounhs, 1, J, L) = F3(bounhs, 2, J, L);
+            F3(bounis, 1, J, L) = F3(bounis, 2, J, L);
+            F3(hdns, 1, J, L) = F3(hdns, 2, J, L);
+            F3(didt, 1, J, L) = 0.;
+            F3(dibndt, 1, J, L) = 0.;
+        }
+    }
+    for (int I = 2; I <= NR + 1; ++I)
+        for (int J = 1; J <= NT; ++J)
+            for (int L = 1; L <= NPA; ++L) {
+                if (isnan(F3(fnis, I, J, L))) F3(fnis, I, J, L) = F3(fnis, I - 1, J, L);
+                if (isnan(F3(fnhs, I, J, L))) F3(fnhs, I, J, L) = F3(fnhs, I - 1, J, L);
+                if (isnan(F3(bounis, I, J, L))) F3(bounis, I, J, L) = F3(bounis, I - 1, J, L);
+                if (isnan(F3(bounhs, I, J, L))) F3(bounhs, I, J, L) = F3(bounhs, I - 1, J, L);
+                if (isnan(F3(hdns, I, J, L))) F3(hdns, I, J, L) = F3(hdns, I - 1, J, L);
+                if (isnan(F3(didt, I, J, L))) F3(didt, I, J, L) = 0.;
+                if (isnan(F3(dibndt, I, J, L))) F3(dibndt, I, J, L) = 0.;
+            }
+#undef A3
+#undef F3
+#undef F2D
+    free(h); free(fi); free(hd); free(hb); free(ib); free(be);
+}

@@ -161,6 +161,15 @@ void ro_bounce_integrals(const ro_grid *g, int nthe, const double *chi, const do
                          const double *z, double *bline, const double *dens, int ieq, double *h, double *fi,
                          double *hd, double *bm);
 
+/* The RAM-variable fill of computehI (src/ModRamScb.f90:458-463,520-632)
+ * from the bounce integrals (hc, ic, dc: (NR,NT,NPA); beq: (NR,NT)), with
+ * BOUNHS/BOUNIS by Steffen's monotone cubic in pitch angle at PAbn.  The
+ * field arrays passed are updated in place ((NR+1,NT,NPA) / (NR+1,NT)). */
+void ro_install_hI(ro_grid *g, const double *pa, const double *pabn, const double *hc, const double *ic,
+                   const double *dc, const double *beq, double bnormal, double dthi, double *fnhs, double *fnis,
+                   double *hdns, double *bounhs, double *bounis, double *bnes, double *dbdt, double *didt,
+                   double *dibndt, double *eir, double *eip);
+
 /* One DTs half of ram_run for one species (the measurement "step"):
  * order 0 = R,P,E,MU,[CEX],[ATMOL]; order 1 = [ATMOL],[CEX],MU,E,P,R.
  * charge/atlos from ro_cepara. */

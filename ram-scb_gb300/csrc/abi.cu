@@ -727,6 +727,24 @@ int ramgpu_set_fields(ramgpu_ctx* ctx, const double* fnhs, const double* fnis, c
   return RAMGPU_OK;
 }
 
+int ramgpu_get_fields(ramgpu_ctx* ctx, double* fnhs, double* fnis, double* bounhs, double* bounis,
+                      double* hdns, double* didt, double* dibndt, double* bnes, double* dbdt, double* eir,
+                      double* eip) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (!ctx->have_fields) return fail(ctx, RAMGPU_ERR_STATE, "fields not set");
+  Dev& d = ctx->d;
+  const size_t nfield = (size_t)d.nf * d.nt * d.npa, n2 = (size_t)d.nf * d.nt;
+  CK(cudaStreamSynchronize(ctx->stream));
+  auto dn = [&](double* dst, const double* src, size_t n) {
+    return dst ? cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyDefault) : cudaSuccess;
+  };
+  CK(dn(fnhs, d.fnhs, nfield)); CK(dn(fnis, d.fnis, nfield)); CK(dn(bounhs, d.bounhs, nfield));
+  CK(dn(bounis, d.bounis, nfield)); CK(dn(hdns, d.hdns, nfield)); CK(dn(didt, d.didt, nfield));
+  CK(dn(dibndt, d.dibndt, nfield));
+  CK(dn(bnes, d.bnes, n2)); CK(dn(dbdt, d.dbdt, n2)); CK(dn(eir, d.eir, n2)); CK(dn(eip, d.eip, n2));
+  return RAMGPU_OK;
+}
+
 int ramgpu_set_boundary(ramgpu_ctx* ctx, int member, int s, const double* fgeos_s) {
   if (check_ctx(ctx) || !fgeos_s) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
   const size_t n = (size_t)ctx->d.nt * ctx->d.ne * ctx->d.npa;
@@ -1356,6 +1374,87 @@ int ramgpu_bounce_integrals(ramgpu_ctx* ctx, int nthe, const double* chi, const 
   cudaFree(sbuf);
   cudaFree(okb);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "bounce_integrals");
+  return RAMGPU_OK;
+}
+
+int ramgpu_compute_hI(ramgpu_ctx* ctx, int nthe, const double* chi, const double* x, const double* y,
+                      const double* z, const double* b, const double* dens, int ieq, const double* pa,
+                      const double* pabn, double bnormal, double dthi) {
+  if (check_ctx(ctx) || !chi || !x || !y || !z || !b || !dens || !pa || !pabn)
+    return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (!ctx->have_grid || !ctx->have_fields) return fail(ctx, RAMGPU_ERR_STATE, "grid/fields not set");
+  if (nthe < 3 || ieq < 1 || ieq > nthe) return fail(ctx, RAMGPU_ERR_ARG, "nthe >= 3 and 1 <= ieq <= nthe");
+  Dev& d = ctx->d;
+  const size_t nl = (size_t)d.nr * d.nt, nln = nl * nthe, na = nl * d.npa;
+  const size_t nd = 5 * nln + nthe + 2 * nl + 9 * na + 2 * na + 6 * nl * d.npa + d.npa + d.npa;
+  double* buf = nullptr;
+  unsigned char* sbuf = nullptr;
+  int* okb = nullptr;
+  CK(cudaMalloc(&buf, nd * sizeof(double)));
+  cudaError_t e = cudaMalloc(&sbuf, 2 * na);
+  if (e == cudaSuccess) e = cudaMalloc(&okb, nl * sizeof(int));
+  BounceDev q{};
+  q.nr = d.nr; q.nt = d.nt; q.npa = d.npa; q.nthe = nthe; q.ieq = ieq;
+  double* p = buf;
+  double *dx = p; p += nln;
+  double *dy = p; p += nln;
+  double *dz = p; p += nln;
+  double *db = p; p += nln;
+  double *dd = p; p += nln;
+  double *dchi = p; p += nthe;
+  q.length = p; p += nl;
+  q.r0 = p; p += nl;
+  q.mirror = p; p += na;
+  q.mirror2 = p; p += na;
+  q.yi = p; p += na;
+  q.yh = p; p += na;
+  q.yd = p; p += na;
+  q.h_out = p; p += na;
+  q.i_out = p; p += na;
+  q.d_out = p; p += na;
+  q.m_out = p; p += na;
+  q.x = dx; q.y = dy; q.z = dz; q.b = db; q.chi = dchi; q.mu = d.mu; q.outside = d.outside;
+  q.dens = dd;
+  q.st = sbuf; q.sd = sbuf + na; q.line_ok = okb;
+  HiDev hq{};
+  hq.nr = d.nr; hq.nt = d.nt; hq.npa = d.npa; hq.dthi = dthi; hq.bnormal = bnormal;
+  hq.outside = d.outside;
+  hq.h = q.h_out; hq.fi = q.i_out; hq.hd = q.d_out; hq.beq = q.m_out;  // L = 1 mirror = equatorial B
+  hq.hb = p; p += na;
+  hq.ib = p; p += na;
+  hq.scratch = p; p += 6 * nl * d.npa;
+  double* dpa = p; p += d.npa;
+  double* dpr = p; p += d.npa;
+  hq.pa = dpa; hq.pabn_rev = dpr;
+  hq.fnhs = (double*)d.fnhs; hq.fnis = (double*)d.fnis; hq.hdns = (double*)d.hdns;
+  hq.bounhs = (double*)d.bounhs; hq.bounis = (double*)d.bounis; hq.didt = (double*)d.didt;
+  hq.dibndt = (double*)d.dibndt; hq.bnes = (double*)d.bnes; hq.dbdt = (double*)d.dbdt;
+  hq.eir = (double*)d.eir; hq.eip = (double*)d.eip;
+  std::vector<double> lz0(1), pr(d.npa, 0.0);
+  if (e == cudaSuccess) e = cudaMemcpy(lz0.data(), d.lz, sizeof(double), cudaMemcpyDeviceToHost);
+  hq.lz0 = lz0[0];
+  for (int qq = 0; qq < d.npa - 2; ++qq) pr[qq] = pabn[d.npa - 2 - qq];
+  const size_t bytes = nln * sizeof(double);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, bytes, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dy, y, bytes, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dz, z, bytes, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(db, b, bytes, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dd, dens, bytes, cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dchi, chi, nthe * sizeof(double), cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dpa, pa, d.npa * sizeof(double), cudaMemcpyDefault, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dpr, pr.data(), d.npa * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) {
+    launch_bounce(q, ctx->stream);
+    launch_hi_fill(hq, ctx->stream);
+    ctx->launches += 7;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(buf);
+  cudaFree(sbuf);
+  cudaFree(okb);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "compute_hI");
+  ctx->field_dirty = true;  // derived tables follow on the next step
   return RAMGPU_OK;
 }
 

@@ -197,3 +197,165 @@ void launch_bounce(const BounceDev& q, cudaStream_t st) {
 }
 
 }  // namespace ramgpu
+
+namespace ramgpu {
+
+// ------------------------------------------------------- the field-table fill
+// computehI's RAM-variable fill (src/ModRamScb.f90:458-463,520-632) on the
+// device, from the bounce integrals: BOUNHS/BOUNIS by Steffen's (1990)
+// monotone cubic in pitch angle at the bin boundaries PAbn (interior slopes
+// by his eq. (11), one-sided secants at the ends, linear extrapolation
+// outside the data, as the reference's 1-D interpolation wrapper), then
+// FNHS..BOUNIS, BNES and the time derivatives written into the context's
+// field tables, the I = 1 row and the NaN repair.
+
+namespace {
+__device__ double sgn1(double v) { return v < 0 ? -1.0 : 1.0; }
+
+// Steffen slopes and values at xb of data (xa ascending, distinct)
+__device__ void steffen_line(int n, const double* xa, const double* fa, double* yp, int nb, const double* xb,
+                             double* fb, long long fbs) {
+  yp[0] = (fa[1] - fa[0]) / (xa[1] - xa[0]);
+  for (int i = 1; i < n - 1; ++i) {
+    const double hm = xa[i] - xa[i - 1], h = xa[i + 1] - xa[i];
+    const double sm = (fa[i] - fa[i - 1]) / hm, s = (fa[i + 1] - fa[i]) / h;
+    const double p = (sm * h + s * hm) / (hm + h);
+    double m = fabs(sm);
+    if (fabs(s) < m) m = fabs(s);
+    if (0.5 * fabs(p) < m) m = 0.5 * fabs(p);
+    yp[i] = (sgn1(sm) + sgn1(s)) * m;
+  }
+  yp[n - 1] = (fa[n - 1] - fa[n - 2]) / (xa[n - 1] - xa[n - 2]);
+  for (int q = 0; q < nb; ++q) {
+    const double x = xb[q];
+    double v;
+    if (x <= xa[0]) {
+      v = fa[0] + (x - xa[0]) / (xa[1] - xa[0]) * (fa[1] - fa[0]);
+    } else if (x >= xa[n - 1]) {
+      v = fa[n - 1] + (x - xa[n - 1]) / (xa[n - 2] - xa[n - 1]) * (fa[n - 2] - fa[n - 1]);
+    } else {
+      int i = 0;
+      while (i < n - 2 && xa[i + 1] <= x) ++i;
+      const double h = xa[i + 1] - xa[i], s = (fa[i + 1] - fa[i]) / h;
+      const double a = (yp[i] + yp[i + 1] - 2 * s) / h / h, b = (3 * s - 2 * yp[i] - yp[i + 1]) / h;
+      const double t = x - xa[i];
+      v = fa[i] + t * (yp[i] + t * (b + t * a));
+    }
+    fb[(long long)q * fbs] = v;
+  }
+}
+}  // namespace
+
+// per J: lines outside the magnetopause take the previous radial point
+__global__ void k_hi_outside(HiDev q) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= q.nt) return;
+  const long long sl = (long long)q.nr * q.nt;
+  for (int i = 1; i < q.nr; ++i) {
+    if (q.outside[(long long)j * q.nr + i] != 1) continue;
+    for (int L = 0; L < q.npa; ++L) {
+      const long long o = (long long)L * sl + (long long)j * q.nr + i;
+      q.h[o] = q.h[o - 1];
+      q.fi[o] = q.fi[o - 1];
+      q.hd[o] = q.hd[o - 1];
+    }
+    q.beq[(long long)j * q.nr + i] = q.beq[(long long)j * q.nr + i - 1];
+  }
+}
+
+// per line: h and I interpolated to PAbn (x ascending: PA(NPA:1:-1))
+__global__ void k_hi_interp(HiDev q) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nl = q.nr * q.nt;
+  if (t >= 2 * nl) return;
+  const int w = t / nl, line = t % nl;
+  const int npa = q.npa;
+  const long long sl = nl;
+  const double* src = (w ? q.fi : q.h) + line;
+  double* dst = (w ? q.ib : q.hb) + line;
+  double* sc = q.scratch + (long long)t * 3 * npa;
+  double *fa = sc, *yp = sc + npa;
+  // data in ascending PA, reduced to strictly increasing x
+  int n = 0;
+  double* xa = sc + 2 * npa;
+  for (int L = 0; L < npa; ++L) {
+    const double x = q.pa[npa - 1 - L];
+    if (n == 0 || x > xa[n - 1]) { xa[n] = x; fa[n] = src[(long long)(npa - 1 - L) * sl]; ++n; }
+  }
+  // targets PAbn(NPA-1:2:-1) -> BOUN*(NPA-1 .. 2)
+  steffen_line(n, xa, fa, yp, npa - 2, q.pabn_rev, dst + (long long)(npa - 2) * sl, -sl);
+  dst[(long long)(npa - 1) * sl] = dst[(long long)(npa - 2) * sl];
+  dst[0] = dst[sl];
+}
+
+// per (I >= 2, J, L): the fields of row I from line I-1, with time derivatives
+__global__ void k_hi_fill(HiDev q) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long n = (long long)q.nr * q.nt * q.npa;
+  if (t >= n) return;
+  const int i = (int)(t % q.nr);                     // line index, row I = i+2 (1-based)
+  const int j = (int)((t / q.nr) % q.nt);
+  const int L = (int)(t / ((long long)q.nr * q.nt));
+  const int nf = q.nr + 1;
+  const long long f = ((long long)L * q.nt + j) * nf + (i + 1);
+  const double fip = q.fnis[f], bip = q.bounis[f];
+  const bool dt0 = fabs(q.dthi) <= 1e-9;
+  q.fnhs[f] = q.h[t];
+  q.fnis[f] = q.fi[t];
+  q.hdns[f] = q.hd[t];
+  q.bounhs[f] = q.hb[t];
+  q.bounis[f] = q.ib[t];
+  q.didt[f] = dt0 ? 0.0 : (q.fi[t] - fip) / q.dthi;
+  q.dibndt[f] = dt0 ? 0.0 : (q.ib[t] - bip) / q.dthi;
+  if (L == 0) {
+    const long long f2 = (long long)j * nf + (i + 1);
+    const double bprev = q.bnes[f2];
+    q.bnes[f2] = q.beq[(long long)j * q.nr + i] * q.bnormal / 1e9;
+    q.dbdt[f2] = dt0 ? 0.0 : (q.bnes[f2] - bprev) / q.dthi;
+  }
+}
+
+// per (J, L): the I = 1 row, then the NaN repair in increasing I
+__global__ void k_hi_rows(HiDev q) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= q.nt * q.npa) return;
+  const int j = t % q.nt, L = t / q.nt;
+  const int nf = q.nr + 1;
+  const long long b = ((long long)L * q.nt + j) * nf;
+  if (L == 0) {
+    const long long b2 = (long long)j * nf;
+    q.bnes[b2] = 0.32 / (q.lz0 * q.lz0 * q.lz0) / 1.e4;
+    q.dbdt[b2] = 0.0;
+    q.eir[b2] = 0.0;
+    q.eip[b2] = 0.0;
+  }
+  q.fnhs[b] = q.fnhs[b + 1];
+  q.fnis[b] = q.fnis[b + 1];
+  q.bounhs[b] = q.bounhs[b + 1];
+  q.bounis[b] = q.bounis[b + 1];
+  q.hdns[b] = q.hdns[b + 1];
+  q.didt[b] = 0.0;
+  q.dibndt[b] = 0.0;
+  for (int I = 1; I < nf; ++I) {
+    const long long c = b + I;
+    if (isnan(q.fnis[c])) q.fnis[c] = q.fnis[c - 1];
+    if (isnan(q.fnhs[c])) q.fnhs[c] = q.fnhs[c - 1];
+    if (isnan(q.bounis[c])) q.bounis[c] = q.bounis[c - 1];
+    if (isnan(q.bounhs[c])) q.bounhs[c] = q.bounhs[c - 1];
+    if (isnan(q.hdns[c])) q.hdns[c] = q.hdns[c - 1];
+    if (isnan(q.didt[c])) q.didt[c] = 0.0;
+    if (isnan(q.dibndt[c])) q.dibndt[c] = 0.0;
+  }
+}
+
+void launch_hi_fill(const HiDev& q, cudaStream_t st) {
+  k_hi_outside<<<(q.nt + 63) / 64, 64, 0, st>>>(q);
+  const int nl2 = 2 * q.nr * q.nt;
+  k_hi_interp<<<(nl2 + 63) / 64, 64, 0, st>>>(q);
+  const long long n = (long long)q.nr * q.nt * q.npa;
+  k_hi_fill<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(q);
+  const int nr2 = q.nt * q.npa;
+  k_hi_rows<<<(nr2 + 127) / 128, 128, 0, st>>>(q);
+}
+
+}  // namespace ramgpu

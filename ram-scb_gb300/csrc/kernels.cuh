@@ -107,6 +107,17 @@ struct BounceDev {
   double *h_out, *i_out, *d_out, *m_out;
 };
 void launch_bounce(const BounceDev& q, cudaStream_t st);
+// computehI's field-table fill: inputs h, fi, hd (NR,NT,NPA) and beq (NR,NT)
+// (modified: the outside-magnetopause copy), outputs the context's tables
+struct HiDev {
+  int nr, nt, npa;
+  double dthi, bnormal, lz0;
+  const int* outside;
+  const double *pa, *pabn_rev;   // PA (NPA); PAbn(NPA-1:2:-1) (NPA-2)
+  double *h, *fi, *hd, *beq, *hb, *ib, *scratch;
+  double *fnhs, *fnis, *hdns, *bounhs, *bounis, *didt, *dibndt, *bnes, *dbdt, *eir, *eip;
+};
+void launch_hi_fill(const HiDev& q, cudaStream_t st);
 
 // virtual spacecraft and SCB hand-off (outputs.cu)
 struct SatDev {

@@ -36,7 +36,8 @@ EXPORTS = (
     "ramgpu_adj_forward", "ramgpu_adj_backward", "ramgpu_adj_digest", "ramgpu_adj_record",
     "ramgpu_fly_sats", "ramgpu_sum_pressure", "ramgpu_adj_replay", "ramgpu_set_pa_diffusion",
     "ramgpu_loss_wae", "ramgpu_bounce_integrals", "ramgpu_upload_f2_async", "ramgpu_download_f2_async",
-    "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store",
+    "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store", "ramgpu_compute_hI",
+    "ramgpu_get_fields",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
@@ -144,6 +145,8 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_moments_async": ([vp, i, i, dp, dp], i),
         "ramgpu_synchronize": ([vp], i),
         "ramgpu_set_coef_store": ([vp, i], i),
+        "ramgpu_compute_hI": ([vp, i, dp, dp, dp, dp, dp, dp, i, dp, dp, d, d], i),
+        "ramgpu_get_fields": ([vp] + [dp] * 11, i),
         "ramgpu_sum_pressure": ([vp, i, dp, dp], i),
     }
     for name, (args, res) in sig.items():
@@ -345,6 +348,26 @@ class RamGpu:
                                                   int(lines.ieq), _dptr(h), _dptr(fi), _dptr(hd), _dptr(bm)),
                  "bounce_integrals")
         return h, fi, hd, bm
+
+    def compute_hI(self, lines, pa, pabn, bnormal: float = 1.0, dthi: float = 0.0):
+        """computehI on the device from field lines (workload.FieldLines):
+        fills the context's field tables."""
+        arrs = [_fort(a) for a in (lines.chi, lines.x, lines.y, lines.z, lines.b, lines.dens)]
+        pa_, pb_ = _fort(pa), _fort(pabn)
+        self._ck(self.lib.ramgpu_compute_hI(self.h, int(lines.chi.size), *[_dptr(a) for a in arrs],
+                                            int(lines.ieq), _dptr(pa_), _dptr(pb_), float(bnormal),
+                                            float(dthi)), "compute_hI")
+
+    def get_fields(self):
+        """The context's field tables: dict of FNHS, FNIS, BOUNHS, BOUNIS, HDNS,
+        dIdt, dIbndt (NR+1,NT,NPA) and BNES, dBdt, EIR, EIP (NR+1,NT)."""
+        g = self.grid
+        names3 = ("fnhs", "fnis", "bounhs", "bounis", "hdns", "didt", "dibndt")
+        names2 = ("bnes", "dbdt", "eir", "eip")
+        out = {n: np.zeros((g.nr + 1, g.nt, g.npa), order="F") for n in names3}
+        out.update({n: np.zeros((g.nr + 1, g.nt), order="F") for n in names2})
+        self._ck(self.lib.ramgpu_get_fields(self.h, *[_dptr(out[n]) for n in names3 + names2]), "get_fields")
+        return out
 
     def set_pa_diffusion(self, s: int, daa=None):
         """Pitch-angle diffusion coefficient D(I,J,K,L) of species s (None removes it)."""

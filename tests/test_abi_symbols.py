@@ -12,7 +12,7 @@ from ramgpu import abi, build
 
 def declared_symbols():
     text = (ROOT / "include" / "ramgpu.h").read_text()
-    return sorted(set(re.findall(r"\b(ramgpu_[a-z0-9_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(ramgpu_[A-Za-z0-9_]+)\s*\(", text)))
 
 
 def test_header_and_binding_agree():

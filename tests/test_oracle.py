@@ -480,3 +480,29 @@ def test_bounce_integrals_exact_for_the_interpolant():
         assert abs((length / (math.pi * 2 * r0)) * yh * math.sqrt(m) / h[i, j, L] - 1) < 1e-9, L
         assert abs((length / (math.pi * r0)) * yi / math.sqrt(m) / fi[i, j, L] - 1) < 1e-9, L
         assert abs((yd / yh) / hd[i, j, L] - 1) < 1e-8, L
+
+
+def test_compute_hI_fills_dipole_tables():
+    """computehI's fill on dipole field lines rebuilds the dipole tables that
+    ARRAYS-era RAM computes from Ejiri's fits: FNHS, FNIS and the bin-
+    boundary BOUNHS, BOUNIS agree in the trapped range; BNES is the dipole
+    equatorial field; row 1 copies row 2; no time derivatives at dthi = 0,
+    finite differences of the tables at dthi > 0."""
+    g, o, lines = _dipole_setup(401)
+    wl = W.make_workload("single_h")
+    f0 = {k: np.asarray(getattr(wl.fields, k)) for k in
+          ("fnhs", "fnis", "hdns", "bounhs", "bounis", "bnes", "dbdt", "didt", "dibndt", "eir", "eip")}
+    out = o.compute_hI(lines, bnormal=3.2e4, dthi=0.0, fields=f0)
+    for k in ("fnhs", "fnis", "bounhs", "bounis"):
+        # near 90 degrees a narrow mirror bracket makes the reference copy
+        # the neighbouring pitch angle (a 1 % effect on the outermost line)
+        r = np.abs(out[k][1:, :, 3:45] / f0[k][1:, :, 3:45] - 1)
+        assert np.median(r) < 2e-3 and r.max() < 1.5e-2, (k, np.median(r), r.max())
+    np.testing.assert_allclose(out["bnes"][1:], f0["bnes"][1:], rtol=1e-12)
+    for k in ("fnhs", "fnis", "bounhs", "bounis", "hdns"):
+        assert np.array_equal(out[k][0], out[k][1])
+    assert not out["didt"].any() and not out["dbdt"].any()
+    out2 = o.compute_hI(lines, bnormal=3.2e4, dthi=300.0, fields=f0)
+    np.testing.assert_allclose(out2["didt"][1:], (out2["fnis"][1:] - f0["fnis"][1:]) / 300.0, rtol=1e-12,
+                               atol=1e-300)
+    assert not out2["didt"][0].any()
