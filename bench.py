@@ -139,6 +139,15 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(value: float, device=None) -> float:
+    """The largest value over all ranks (the job's time is its slowest rank)."""
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ------------------------------------------------------------ CPU legs
 def cpu_threads(ns):
     """(species threads, line threads per species) using every host core:
@@ -547,9 +556,7 @@ def run_gb300(args, rank, world, local_rank):
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(step_ms)
     if world > 1:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms, dev)
     value = world * cells_per_step * args.steps / (total_ms / 1e3)
 
     # per-kernel durations: a second timed pass with events around every

@@ -183,3 +183,33 @@ def test_no_nan_and_positive(tiny):
         f = gpu.download_f2(0, s)
         assert np.isfinite(f).all()
         assert (f >= 0).all()
+
+
+def test_ram_run_matches_golden_fixture():
+    """The GPU step against the committed fixture (tests/golden), with no
+    CPU run: per-species sums, 256 sampled cells, moments, FLUX, DtsNext."""
+    import json
+    from conftest import ROOT
+    gd = json.loads((ROOT / "tests" / "golden" / "ram_run_tiny.json").read_text())
+    wl = W.make_workload(gd["workload"])
+    gpu = _setup(wl, gd["kp"])
+    try:
+        gpu.ram_run(gd["dts"])
+        assert abs(gpu.cfl(0, 0)[4] - gd["dts_next"]) <= 1e-12 * gd["dts_next"]
+        for s, sd in enumerate(gd["species"]):
+            f = gpu.download_f2(0, s)
+            assert abs(np.sum(f) - sd["sum"]) <= 1e-12 * abs(sd["sum"])
+            scale = max(abs(v) for _, v in sd["cells"])
+            for c, v in sd["cells"]:
+                assert abs(f[tuple(c)] - v) <= TOL * scale
+            pe, pa = gpu.moments(0, s)
+            for arr, key in ((pe, "ppert"), (pa, "ppart")):
+                sc = max(abs(v) for _, v in sd[key])
+                for c, v in sd[key]:
+                    assert abs(arr[tuple(c)] - v) <= TOL * sc
+            fl = gpu.flux(0, s)
+            sc = max(abs(v) for _, v in sd["flux"])
+            for c, v in sd["flux"]:
+                assert abs(fl[tuple(c)] - v) <= TOL * sc
+    finally:
+        gpu.close()

@@ -506,3 +506,30 @@ def test_compute_hI_fills_dipole_tables():
     np.testing.assert_allclose(out2["didt"][1:], (out2["fnis"][1:] - f0["fnis"][1:]) / 300.0, rtol=1e-12,
                                atol=1e-300)
     assert not out2["didt"][0].any()
+
+
+def _golden():
+    import json
+    from conftest import ROOT
+    return json.loads((ROOT / "tests" / "golden" / "ram_run_tiny.json").read_text())
+
+
+def test_oracle_matches_golden_fixture():
+    """The committed fixture (tests/golden/make_golden.py) pins the oracle's
+    ram_run on the non-dipole test grid; libm differences between machines
+    stay far inside 1e-12."""
+    gd = _golden()
+    wl = W.make_workload(gd["workload"])
+    o = pyoracle.Oracle(wl.grid, wl.fields)
+    f2 = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    out = o.ram_run(f2, wl.fgeos, gd["dts"], kp=gd["kp"], want_flux=True)
+    assert abs(out["dts_next"] - gd["dts_next"]) <= 1e-12 * gd["dts_next"]
+    for s, sd in enumerate(gd["species"]):
+        assert abs(np.sum(f2[s]) - sd["sum"]) <= 1e-12 * abs(sd["sum"])
+        scale = max(abs(v) for _, v in sd["cells"])
+        for c, v in sd["cells"]:
+            assert abs(f2[s][tuple(c)] - v) <= 1e-12 * scale
+        for key in ("ppert", "ppart"):
+            sc = max(abs(v) for _, v in sd[key])
+            for c, v in sd[key]:
+                assert abs(out[key][s][tuple(c)] - v) <= 1e-12 * sc

@@ -1,0 +1,64 @@
+"""The multi-GPU path is replicas only (species and members are independent;
+no exchange step): under torchrun every rank runs its own replica, times
+are combined by a max over ranks, and rank 0 alone prints the JSON line.
+These run on the CPU with the gloo backend and world size 2."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, values, out):
+    import torch
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    torch.distributed.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        sys.path.insert(0, str(ROOT))
+        import bench
+        out.put((rank, bench.max_over_ranks(values[rank])))
+    finally:
+        torch.distributed.destroy_process_group()
+
+
+def test_max_over_ranks_gloo():
+    torch = pytest.importorskip("torch")
+    mp = torch.multiprocessing.get_context("spawn")
+    q = mp.Queue()
+    port = _free_port()
+    vals = [3.5, 7.25]
+    ps = [mp.Process(target=_worker, args=(r, 2, port, vals, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    got = dict(q.get(timeout=120) for _ in ps)
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert got == {0: 7.25, 1: 7.25}
+
+
+def test_reference_arm_under_torchrun():
+    """bench.py --impl reference as the driver launches it for N = 2: rank 0
+    times the CPU path and prints one line, rank 1 exits cleanly."""
+    pytest.importorskip("torch")
+    port = _free_port()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"),
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1", "--workload", "single_h"]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
