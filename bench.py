@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--flush-mb", type=int, default=256)
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-padif", action="store_true", help="skip the step timed with WPADIF on")
     ap.add_argument("--no-coef-store", action="store_true",
                     help="recompute the face coefficients in the reverse half instead of storing them")
     ap.add_argument("--members", type=int, default=256, help="ensemble members (0: skip)")
@@ -618,6 +619,37 @@ def run_gb300(args, rank, world, local_rank):
            "d2h_bytes_per_step": 8 * g.ncell * ns + 16 * g.nr * g.nt,
            "path": "ramgpu_upload_f2_async x4 (page-locked host) + ramgpu_set_kp + ramgpu_ram_run_async + "
                    "ramgpu_download_f2_async x4 + ramgpu_moments_async + ramgpu_synchronize, every step"}
+    # the same step with WPADIF on the electrons (both halves), per-kernel timed
+    padif = None
+    if not args.no_padif:
+        gpu.set_pa_diffusion(0, W.pa_diffusion(g, wl.fields))
+        gpu.set_timing(True)
+        gpu.kernel_times()
+        pd_ms = []
+        for k in range(3):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+            gpu.set_kp(-1, kp_at(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            gpu.ram_run_async(wl.dts)
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            pd_ms.append(a.elapsed_time(b))
+        kt = gpu.kernel_times()
+        gpu.set_timing(False)
+        gpu.set_pa_diffusion(0, None)
+        pk = kt.get("padif", (0.0, 1))
+        per = pk[0] / max(pk[1], 1)
+        # algorithmic bytes of the two launches per step: the electrons' solve
+        # reads F2 and the three elimination tables and writes F2 (40 B per
+        # cell) in both; the first also applies the loss factor to the other
+        # three species (F2 and factor in, F2 out: 24 B per cell)
+        byts = 0.5 * (40.0 + 40.0 + 3 * 24.0) * g.ncell
+        padif = {"species": "Electron (WPADIF after the drifts and before the reverse drifts)",
+                 "step_ms": statistics.mean(pd_ms), "step_ms_without": statistics.mean(kt_ms),
+                 "kernel_ms_per_launch": per, "launches": pk[1],
+                 "algorithmic_GBps": byts / (per / 1e3) / 1e9 if per > 0 else None}
     gpu.close()
 
     ensemble = None
@@ -656,7 +688,7 @@ def run_gb300(args, rank, world, local_rank):
         "kernels_ms": {k: round(v[0] / v[1], 5) for k, v in ktimes.items()},
         "kernel_pass_ms_per_step": statistics.mean(kt_ms),
         "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
-        "ensemble": ensemble, "adjoint": adjoint, "wall_s": wall,
+        "padif": padif, "ensemble": ensemble, "adjoint": adjoint, "wall_s": wall,
     }
     print(json.dumps(line), flush=True)
 

@@ -310,7 +310,8 @@ long long ramgpu_launch_count(const ramgpu_ctx *ctx);
  * around every launch group (diagnostics; no reference counterpart).
  * Kernel classes: 0 member tables, 1 DRIFTR ghost planes, 2 DRIFTR, 3 DRIFTP,
  * 4 DRIFTE, 5 DRIFTMU (+fused loss), 6 periodic copy/mask, 7 ANISCH,
- * 8 DTs tables, 9 SUMRC/loss bookkeeping.  ramgpu_kernel_times synchronises,
+ * 8 DTs tables, 9 SUMRC/loss bookkeeping, 10 pitch-angle diffusion.
+ * ramgpu_kernel_times synchronises,
  * adds the elapsed times of completed launches into ms[16] and counts[16]
  * (caller-zeroed) and forgets them. */
 #define RAMGPU_NKCLASS 16

@@ -323,8 +323,8 @@ static int enqueue_body(ramgpu_ctx* ctx, double dts) {
   } else if (!losses) {
     // R,P,E,MU, WPADIF, CEX,ATMOL,ATMOL,CEX (folded into WPADIF's store), WPADIF, MU,E,P,R
     if ((rc = enqueue_forward(ctx, dts, false, nullptr))) return rc;
-    { Timed t(ctx, 9); launch_padif(ctx->d, ctx->d.loss2, ctx->stream); }
-    { Timed t(ctx, 9); launch_padif(ctx->d, nullptr, ctx->stream); }
+    { Timed t(ctx, 10); launch_padif(ctx->d, ctx->d.loss2, ctx->stream); }
+    { Timed t(ctx, 10); launch_padif(ctx->d, nullptr, ctx->stream); }
     ctx->launches += 2;
     CKL("pitch-angle diffusion");
     if ((rc = enqueue_reverse(ctx, dts, false, nullptr, true))) return rc;
@@ -332,7 +332,7 @@ static int enqueue_body(ramgpu_ctx* ctx, double dts) {
     if ((rc = enqueue_forward(ctx, dts, false, nullptr))) return rc;
     if ((rc = sumrc_stage(ctx, 0, 1))) return rc;
     if (pd) {
-      { Timed t(ctx, 9); launch_padif(ctx->d, nullptr, ctx->stream); }
+      { Timed t(ctx, 10); launch_padif(ctx->d, nullptr, ctx->stream); }
       ctx->launches += 1;
       if ((rc = sumrc_stage(ctx, 6, 5))) return rc;
     }
@@ -346,7 +346,7 @@ static int enqueue_body(ramgpu_ctx* ctx, double dts) {
     if ((rc = sumrc_stage(ctx, 4, 2))) return rc;
     ctx->launches += 4;
     if (pd) {
-      { Timed t(ctx, 9); launch_padif(ctx->d, nullptr, ctx->stream); }
+      { Timed t(ctx, 10); launch_padif(ctx->d, nullptr, ctx->stream); }
       ctx->launches += 1;
       if ((rc = sumrc_stage(ctx, 7, 5))) return rc;
     }

@@ -177,6 +177,45 @@ module ModRamGpu
        integer(c_int), value :: member
        real(c_double), intent(out) :: pallsum(*), pparsum(*)
      end function
+     ! computehI on the device: field lines (nthe, NR, NT) through the RAM grid
+     integer(c_int) function ramgpu_compute_hI(ctx, nthe, chi, x, y, z, b, dens, ieq, pa, pabn, &
+          bnormal, dthi) bind(C, name="ramgpu_compute_hI")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: nthe, ieq
+       real(c_double), intent(in) :: chi(*), x(*), y(*), z(*), b(*), dens(*), pa(*), pabn(*)
+       real(c_double), value :: bnormal, dthi
+     end function
+     integer(c_int) function ramgpu_get_fields(ctx, fnhs, fnis, bounhs, bounis, hdns, didt, &
+          dibndt, bnes, dbdt, eir, eip) bind(C, name="ramgpu_get_fields")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(out) :: fnhs(*), fnis(*), bounhs(*), bounis(*), hdns(*), &
+                                      didt(*), dibndt(*), bnes(*), dbdt(*), eir(*), eip(*)
+     end function
+     integer(c_int) function ramgpu_upload_f2_async(ctx, member, s, f2_s) &
+          bind(C, name="ramgpu_upload_f2_async")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member, s
+       real(c_double), intent(in) :: f2_s(*)
+     end function
+     integer(c_int) function ramgpu_download_f2_async(ctx, member, s, f2_s) &
+          bind(C, name="ramgpu_download_f2_async")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member, s
+       real(c_double), intent(out) :: f2_s(*)
+     end function
+     integer(c_int) function ramgpu_ram_run_async(ctx, dts) bind(C, name="ramgpu_ram_run_async")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), value :: dts
+     end function
+     integer(c_int) function ramgpu_synchronize(ctx) bind(C, name="ramgpu_synchronize")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
      integer(c_int) function ramgpu_last_error(ctx, buf, len) bind(C, name="ramgpu_last_error")
        import :: c_int, c_ptr, c_char, c_size_t
        type(c_ptr), value :: ctx

@@ -41,7 +41,7 @@ EXPORTS = (
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
-          "anisch", "dts_tables", "sumrc")
+          "anisch", "dts_tables", "sumrc", "padif")
 OP_DRIFTR, OP_DRIFTP, OP_DRIFTE, OP_DRIFTMU, OP_CHAREXCHANGE, OP_ATMOL, OP_ANISCH, OP_PADIF = range(8)
 
 
