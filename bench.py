@@ -37,10 +37,13 @@ UNIT = "cell-updates/s"
 # DRIFTE's coefficient is two ops; the CFL-tracking forward E/MU add one.
 FP64_OPS_PER_FACE = {"driftr": 8, "driftp": 8, "drifte": 9.5, "driftmu": 8.5}
 # DRAM bytes (read + write) per launch of each sweep on the four-species
-# standard grid, from one ncu capture (profiles/sweeps_four_sp.md, current
-# kernels): F2 is read once; the written lines stay in L2 within a launch,
-# and k_sweep_mu also reads the fused CEX/ATMOL factor.
-NCU_DRAM_BYTES = {"four_sp": {"driftr": 44.3e6, "driftp": 40.6e6, "drifte": 39.8e6, "driftmu": 81.7e6}}
+# standard grid, the mean of its forward and reverse launches in one ncu
+# capture (profiles/sweeps_four_sp.md, current kernels): F2 is read once
+# and the written lines stay in L2 within a launch; the forward MU also
+# reads the fused CEX/ATMOL factor, and DRIFTE stores and reloads its face
+# coefficients.
+NCU_DRAM_BYTES = {"four_sp": {"driftr": 0.5 * (44.6e6 + 44.4e6), "driftp": 0.5 * (40.7e6 + 40.6e6),
+                               "drifte": 0.5 * (109.0e6 + 129.7e6), "driftmu": 0.5 * (81.7e6 + 40.4e6)}}
 
 
 def parse():
