@@ -32,10 +32,14 @@ sys.path.insert(0, str(ROOT / "ram-scb_gb300"))
 
 METRIC = "FP64 cell-updates/s"
 UNIT = "cell-updates/s"
-# FP64 add/mul/fma per face of each sweep kernel (csrc/sweeps.cu), counted from
-# the source: coefficient, a-term, X, beta|X|, face fma, flux, two update ops;
-# DRIFTE's coefficient is two ops; the CFL-tracking forward E/MU add one.
-FP64_OPS_PER_FACE = {"driftr": 8, "driftp": 8, "drifte": 9.5, "driftmu": 8.5}
+# FP64 instructions per cell of each sweep kernel (csrc/sweeps.cu): ncu's
+# sm__inst_executed_pipe_fp64 x 32 lanes / cells, the mean of its forward
+# and reverse launches on the four-species standard grid (the forward E and
+# MU carry the CFL quotient's multiply; DRIFTE's forward computes and stores
+# its face coefficients, the reverse loads them).  Per face this is the
+# formulation's own count: X, beta*X, coefficient, a-term, face fma, flux
+# and the two update operations.
+FP64_OPS_PER_CELL = {"driftr": 8.18, "driftp": 7.53, "drifte": 0.5 * (9.58 + 5.78), "driftmu": 0.5 * (9.23 + 7.37)}
 # DRAM bytes (read + write) per launch of each sweep on the four-species
 # standard grid, the mean of its forward and reverse launches in one ncu
 # capture (profiles/sweeps_four_sp.md, current kernels): F2 is read once
@@ -590,7 +594,7 @@ def run_gb300(args, rank, world, local_rank):
     bytes_per_launch = 16.0 * g.ncell * nitems  # F2 read + write once per sweep
     achieved = bytes_per_launch / (dom_ms / 1e3) / 1e9
     nfaces = g.ncell * nitems
-    fp64 = FP64_OPS_PER_FACE[dom] * nfaces / (dom_ms / 1e3) / 1e9
+    fp64 = FP64_OPS_PER_CELL[dom] * nfaces / (dom_ms / 1e3) / 1e9
     fp64_peak = abi.probe_fp64() / 1e9
 
     # end-to-end through the C ABI with host buffers (pinned), full F2 in and out
@@ -686,7 +690,7 @@ def run_gb300(args, rank, world, local_rank):
                      "traffic": NCU_DRAM_BYTES.get(args.workload, {}).get(dom), "kernel": dom,
                      "kernel_ms": dom_ms, "peak_kind": peak_kind,
                      "fp64": {"achieved": fp64, "peak": fp64_peak, "unit": "G lane-ops/s",
-                              "frac": fp64 / fp64_peak, "ops_per_face": FP64_OPS_PER_FACE[dom],
+                              "frac": fp64 / fp64_peak, "ops_per_cell": FP64_OPS_PER_CELL[dom],
                               "peak_kind": "measured live (fma loop, ramgpu_probe_fp64)"}},
         "kernels_ms": {k: round(v[0] / v[1], 5) for k, v in ktimes.items()},
         "kernel_pass_ms_per_step": statistics.mean(kt_ms),

@@ -39,7 +39,7 @@ __device__ __forceinline__ void face_acc(double FBb, bool neg, int cs, double ak
   const bool xt = (cs == 2) | (cs == 4);  // LX = X (f, f+1)
   const bool dt = (cs == 1) | (cs == 3);  // LX = D (f-1, f) or (f+1, f+2)
   const double pos = (xt | dt) ? ak : 0.0;
-  const double ngv = __longlong_as_double(__double_as_longlong(pos) ^ (long long)kSignMask);
+  const double ngv = bitsd(dbits(pos) ^ kSignMask);
   const double sm1 = (dt & !neg) ? ngv : 0.0;
   const double s0 = xt ? ngv : ((dt & !neg) ? pos : 0.0);
   const double s1 = xt ? pos : ((dt & neg) ? ngv : 0.0);
@@ -65,7 +65,7 @@ __device__ __forceinline__ double face_ak(double C, bool neg, int cs, double mh,
   double shk;
   if (kXorSign) {
     const double hk = kb ? hb : 0.5;
-    shk = __longlong_as_double(__double_as_longlong(hk) ^ (neg ? (long long)kSignMask : 0LL));
+    shk = bitsd(dbits(hk) ^ (neg ? kSignMask : 0ULL));
   } else {
     shk = neg ? (kb ? -hb : -0.5) : (kb ? hb : 0.5);
   }

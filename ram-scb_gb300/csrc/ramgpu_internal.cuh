@@ -116,9 +116,25 @@ struct Dev {
 };
 
 // ---------------------------------------------------------------- bit tests
-__device__ __forceinline__ unsigned long long dbits(double x) {
-  return (unsigned long long)__double_as_longlong(x);
+// The bit pattern moves through an opaque PTX mov: with a plain bit cast
+// the compiler may fold the integer sign-bit masks and tests below back
+// into FP64 abs/negate/compare instructions, which issue on the FP64 pipe.
+using bits64 = unsigned long long;
+constexpr bits64 kAbsMask = 0x7FFFFFFFFFFFFFFFULL;
+constexpr bits64 kSignMask = 0x8000000000000000ULL;
+__device__ __forceinline__ bits64 dbits(double x) {
+  bits64 u;
+  asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+  return u;
 }
+__device__ __forceinline__ double bitsd(bits64 u) {
+  double x;
+  asm("mov.b64 %0, %1;" : "=d"(x) : "l"(u));
+  return x;
+}
+// beta*|x| as bits (beta > 0): the sign bit of beta*x cleared on the
+// integer pipe; IEEE rounding is symmetric, so this equals beta*fabs(x).
+__device__ __forceinline__ bits64 babs_bits(double beta, double x) { return dbits(beta * x) & kAbsMask; }
 // x < 0.0 exactly as the Fortran test `C.lt.0` (false for -0.0 and NaN with
 // the sign bit clear).
 __device__ __forceinline__ bool is_neg(double x) { return dbits(x) > 0x8000000000000000ULL; }
@@ -143,39 +159,26 @@ __device__ __forceinline__ unsigned long long umin64(unsigned long long a, unsig
 __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
   return a > b ? a : b;
 }
-constexpr unsigned long long kAbsMask = 0x7FFFFFFFFFFFFFFFULL;
-constexpr unsigned long long kSignMask = 0x8000000000000000ULL;
 
 // Flux-limited face value of the reference sweeps (src/ModRamDrift.f90:169-183):
 //   FUP = upwind value; if |X|<=1e-27 or R<=0: FBND=FUP
 //   else FBND = FUP + LIMITER(R)*CORR, LIMITER = max(min(beta R,1),min(R,beta)),
 //        CORR = -0.5*(Cd - s)*X = a*X,  R = D/X.
 // Division-free: for D*X>0, LIMITER*X = sign(X)*max(min(beta|D|,|X|),min(|D|,beta|X|)).
-// bx = beta*|x|, bd = beta*|d| (the neighbour face's bx).  One FP64 fma.
+// bx = beta*|x|, bd = beta*|d| as bits (bd is the neighbour face's bx).
 // The min/max run on bit patterns of the non-negative magnitudes, so a face
-// costs one FP64 fma here.
-__device__ __forceinline__ double face_value(double x, double bx, double d, double bd,
-                                             double fup, double a) {
-  const unsigned long long ux = dbits(x), ud = dbits(d);
-  const unsigned long long m = umax64(umin64(dbits(bd), ux & kAbsMask), umin64(ud & kAbsMask, dbits(bx)));
-  const double lx = __longlong_as_double((long long)(m | (ux & kSignMask)));
-  double fb = fma(a, lx, fup);
-  bool act = abs_gt_1em27(x) && same_sign_nonzero(d, x);
-  return act ? fb : fup;
-}
-
-// Same face value, also reporting which limiter candidate was taken, for
-// the frozen-limiter adjoint: 0 upwind only, 1 beta*D, 2 X, 3 D, 4 beta*X.
-__device__ __forceinline__ double face_value_case(double x, double bx, double d, double bd,
+// costs one FP64 fma here.  cs reports which limiter candidate was taken,
+// for the frozen-limiter adjoint: 0 upwind only, 1 beta*D, 2 X, 3 D, 4 beta*X.
+__device__ __forceinline__ double face_value_case(double x, bits64 bx, double d, bits64 bd,
                                                   double fup, double a, int& cs) {
-  const unsigned long long ux = dbits(x), ud = dbits(d);
-  const unsigned long long m1 = umin64(dbits(bd), ux & kAbsMask);
-  const unsigned long long m2 = umin64(ud & kAbsMask, dbits(bx));
-  const unsigned long long m = umax64(m1, m2);
-  const double lx = __longlong_as_double((long long)(m | (ux & kSignMask)));
+  const bits64 ux = dbits(x), ud = dbits(d);
+  const bits64 m1 = umin64(bd, ux & kAbsMask);
+  const bits64 m2 = umin64(ud & kAbsMask, bx);
+  const bits64 m = umax64(m1, m2);
+  const double lx = bitsd(m | (ux & kSignMask));
   const double fb = fma(a, lx, fup);
   const bool act = abs_gt_1em27(x) && same_sign_nonzero(d, x);
-  cs = !act ? 0 : (m == m1 ? (m1 == dbits(bd) ? 1 : 2) : (m2 == (ud & kAbsMask) ? 3 : 4));
+  cs = !act ? 0 : (m == m1 ? (m1 == bd ? 1 : 2) : (m2 == (ud & kAbsMask) ? 3 : 4));
   return act ? fb : fup;
 }
 constexpr int kClipBit = 8;  // recorded with the case: the updated cell was clipped

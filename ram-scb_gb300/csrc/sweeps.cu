@@ -71,11 +71,11 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
       if (kCfl && outside[0] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
       // face 1: FBND(1) = 0 (outflow) or F(2) (inflow)
       double phi_prev = c * ((inflow && !closed) ? g0 : 0.0);
-      double xm = g0 - gm, bxm = beta * fabs(xm);
-      double x = gp - g0, bx = beta * fabs(x);
+      double xm = g0 - gm; bits64 bxm = babs_bits(beta, xm);
+      double x = gp - g0; bits64 bx = babs_bits(beta, x);
       for (int f = 2; f <= nr - 1; ++f) {  // 1-based face f, updates cell f
         const double gpp = (f + 2 <= nr) ? fl[f + 1] : g1;
-        const double xp = gpp - gp, bxp = beta * fabs(xp);
+        const double xp = gpp - gp; const bits64 bxp = babs_bits(beta, xp);
         c = (kCo == 2) ? cst[f - 1] : ((f == nr - 1) ? cNm : fma(grt[f - 1], p4, cr[f - 1]));
         if (kCfl && outside[f - 1] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
         const bool neg = is_neg(c);
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
       if (!inflow) {
         fbn = g0;
       } else {
-        const double xp = g2 - g1, bxp = beta * fabs(xp);
+        const double xp = g2 - g1; const bits64 bxp = babs_bits(beta, xp);
         fbn = (kRec == 2) ? face_value_frozen(x, xp, g1, fma(cN, -0.5, -0.5), beta, csn = rl[nr - 1] & 7)
                           : face_value_case(x, bx, xp, bxp, g1, fma(cN, -0.5, -0.5), csn);
       }
@@ -148,10 +148,10 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
   #define GJ(J) fl[(long long)((J)-1) * st]
   #define CJ(J) fma(gpt[(long long)((J)-1) * nr], p2, ca[(long long)((J)-1) * nr])
       const double G1 = GJ(1), G2 = GJ(2), G3 = GJ(3), GNm = GJ(nt - 1), GN = GJ(nt);
-      const double X1 = G2 - G1, bX1 = beta * fabs(X1);
-      const double X2 = G3 - G2, bX2 = beta * fabs(X2);
-      const double XNm = GN - GNm, bXNm = beta * fabs(XNm);
-      const double XN = G2 - GN, bXN = beta * fabs(XN);
+      const double X1 = G2 - G1; const bits64 bX1 = babs_bits(beta, X1);
+      const double X2 = G3 - G2; const bits64 bX2 = babs_bits(beta, X2);
+      const double XNm = GN - GNm; const bits64 bXNm = babs_bits(beta, XNm);
+      const double XN = G2 - GN; const bits64 bXN = babs_bits(beta, XN);
       // face NT first: its flux enters cell 2 through FBND(1)=FBND(NT)
       const double cN = (kCo == 2) ? cst[(long long)(nt - 1) * st] : CJ(nt);
       if (kCfl && outside[(long long)(nt - 1) * nr] == 0) q = umax64(q, cfl_bits(cN, kBits1em10));
@@ -166,13 +166,15 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
             : face_value_case(XN, bXN, neg ? X2 : XNm, neg ? bX2 : bXNm, neg ? G2 : GN, a, csN));
       }
       double phi_prev = phiN;
-      double g0 = G2, gp = G3, xm = X1, bxm = bX1, x = X2, bx = bX2;
+      double g0 = G2, gp = G3, xm = X1, x = X2;
+      bits64 bxm = bX1, bx = bX2;
       for (int J = 2; J <= nt - 1; ++J) {
-        double gpp = 0.0, xp, bxp;
+        double gpp = 0.0, xp;
+        bits64 bxp;
         if (J <= nt - 3) {
           gpp = GJ(J + 2);
           xp = gpp - gp;
-          bxp = beta * fabs(xp);
+          bxp = babs_bits(beta, xp);
         } else if (J == nt - 2) {
           gpp = GN;
           xp = XNm;
@@ -256,13 +258,13 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
       const double G1 = d.kap[2 * s + 1] * F2v;
       const double G0 = d.kap[2 * s + 0] * G1;
       const double G2 = F2v, G3 = GK(3);
-      const double X0 = G1 - G0, bX0 = beta * fabs(X0);
-      const double X1 = G2 - G1, bX1 = beta * fabs(X1);
-      const double X2 = G3 - G2, bX2 = beta * fabs(X2);
+      const double X0 = G1 - G0; const bits64 bX0 = babs_bits(beta, X0);
+      const double X1 = G2 - G1; const bits64 bX1 = babs_bits(beta, X1);
+      const double X2 = G3 - G2; const bits64 bX2 = babs_bits(beta, X2);
       double phi_prev;
       {
         const double c = (kCo == 2) ? cst[0] : CK(1);
-        if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em10)) * d.ide[0]));
+        if (kCfl && inside) q = umax64(q, dbits(bitsd(cfl_bits(c, kBits1em10)) * d.ide[0]));
         const bool neg = is_neg(c);
         const double a = (kCo == 2) ? ast[0] : fma(c, mhde[0], neg ? -0.5 : 0.5);
         if (kCo == 1) { cst[0] = c; ast[0] = a; }
@@ -273,12 +275,13 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
         if (kRec == 1) rl[0] = (unsigned char)cs;
         phi_prev = c * fb;
       }
-      double g0 = G2, gp = G3, xm = X1, bxm = bX1, x = X2, bx = bX2;
+      double g0 = G2, gp = G3, xm = X1, x = X2;
+      bits64 bxm = bX1, bx = bX2;
       for (int K = 2; K <= ne; ++K) {
         const double gpp = (K + 2 <= ne) ? GK(K + 2) : 0.0;
-        const double xp = gpp - gp, bxp = beta * fabs(xp);
+        const double xp = gpp - gp; const bits64 bxp = babs_bits(beta, xp);
         const double c = (kCo == 2) ? cst[(long long)(K - 1) * st] : CK(K);
-        if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em10)) * d.ide[K - 1]));
+        if (kCfl && inside) q = umax64(q, dbits(bitsd(cfl_bits(c, kBits1em10)) * d.ide[K - 1]));
         const bool neg = is_neg(c);
         const double a = (kCo == 2) ? ast[(long long)(K - 1) * st] : fma(c, mhde[K - 1], neg ? -0.5 : 0.5);
         if (kCo == 1) { cst[(long long)(K - 1) * st] = c; ast[(long long)(K - 1) * st] = a; }
@@ -348,16 +351,18 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
   #define CL(L) fma(ekv, wm[(long long)((L)-1) * sij], um[(long long)((L)-1) * sij])
       double G2 = GL(2), G3 = GL(3);
       if (kLoss == 2) { G2 *= LA(2); G3 *= LA(3); }
-      const double X1 = 0.0, bX1 = 0.0;  // F(2) - F(1) with F(1) = F(2)
+      const double X1 = 0.0;  // F(2) - F(1) with F(1) = F(2)
+      const bits64 bX1 = 0;
       double phi_prev = 0.0;              // CDriftMu(1) = 0, FBND(1) = 0
-      double g0 = G2, gp = G3, xm = X1, bxm = bX1;
-      double x = G3 - G2, bx = beta * fabs(x);
+      double g0 = G2, gp = G3, xm = X1;
+      bits64 bxm = bX1;
+      double x = G3 - G2; bits64 bx = babs_bits(beta, x);
       for (int L = 2; L <= npa - 2; ++L) {
         double gpp = GL(L + 2);
         if (kLoss == 2) gpp *= LA(L + 2);
-        const double xp = gpp - gp, bxp = beta * fabs(xp);
+        const double xp = gpp - gp; const bits64 bxp = babs_bits(beta, xp);
         const double c = (kCo == 2) ? cst[(long long)(L - 1) * st] : CL(L);
-        if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
+        if (kCfl && inside) q = umax64(q, dbits(bitsd(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
         const bool neg = is_neg(c);
         const double a = (kCo == 2) ? ast[(long long)(L - 1) * st] : fma(c, mhdmu[L - 1], neg ? -0.5 : 0.5);
         if (kCo == 1) { cst[(long long)(L - 1) * st] = c; ast[(long long)(L - 1) * st] = a; }
@@ -380,7 +385,7 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         const int L = npa - 1;
         const double c = (kCo == 2) ? cst[(long long)(L - 1) * st] : CL(L);
         if (kCo == 1) cst[(long long)(L - 1) * st] = c;
-        if (kCfl && inside) q = umax64(q, dbits(__longlong_as_double(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
+        if (kCfl && inside) q = umax64(q, dbits(bitsd(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
         const double phi = c * (closed ? 0.0 : gp);
         const double raw = fma(phi_prev - phi, iwmu[L - 1], g0);
         if (kRec == 1) rl[(long long)(L - 1) * st] = (unsigned char)(is_neg(raw) ? kClipBit : 0);
