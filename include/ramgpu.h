@@ -177,6 +177,20 @@ int ramgpu_half_step(ramgpu_ctx *ctx, double dts, int order);
  * reads), for CUDA-graph capture and overlap.  Inputs set by the calls
  * above are read at execution time. */
 int ramgpu_ram_run_async(ramgpu_ctx *ctx, double dts);
+/* One ram_run call with F2 crossing the host boundary, as the reference's
+ * host array does every call: f2[slot] (slot = member*NS + species, host
+ * pointers, best page-locked) holds that item's F2(S,:,:,:,:) as in
+ * ramgpu_upload_f2; it is uploaded, advanced and written back in place.
+ * The active items are split into groups (ramgpu_set_pipeline_groups,
+ * default 4) that run on their own streams as their uploads land, so the
+ * copies of one group overlap the sweeps of the others.  ppert/ppart,
+ * when not NULL, receive each item's (NR,NT) moments (NULL entries are
+ * skipped), and so does f2 (a NULL entry leaves that item's F2 resident
+ * and unchanged on the host side).  Returns when every copy is back. */
+int ramgpu_ram_run_host(ramgpu_ctx *ctx, double dts, double *const *f2, double *const *ppert,
+                        double *const *ppart);
+/* Number of item groups ramgpu_ram_run_host pipelines (1..8). */
+int ramgpu_set_pipeline_groups(ramgpu_ctx *ctx, int groups);
 
 /* Diagnostic: one operator of the step on every active item, as the
  * reference routine of the same name (the coefficient tables for dts are
@@ -296,11 +310,12 @@ int ramgpu_set_graph(ramgpu_ctx *ctx, int enable);
  * a persistent grid of that many CTAs looping over (item, line-block) units. */
 int ramgpu_set_launch_shape(ramgpu_ctx *ctx, int sweep, int threads, int persistent_ctas);
 int ramgpu_get_launch_shape(ramgpu_ctx *ctx, int *threads4, int *persistent4);
-/* Autotuner: times every sweep at 32/64/128/256 threads per CTA, each with a
- * one-unit-per-CTA grid and a persistent grid (resident CTAs x SMs), on the
- * context's active items, keeps the fastest, and restores F2 afterwards
- * (it allocates a temporary snapshot).  best_ms4 (may be NULL) receives the
- * chosen average launch times. */
+/* Autotuner: for each sweep in turn, tries 32/64/128/256 threads per CTA,
+ * each with a one-unit-per-CTA grid and a persistent grid (resident CTAs x
+ * SMs), timing whole ram_run steps on the context's active items (best of
+ * reps), keeps the fastest, and restores F2 afterwards (it allocates a
+ * temporary snapshot).  best_ms4 (may be NULL) receives the best step time
+ * of each sweep's round. */
 int ramgpu_autotune(ramgpu_ctx *ctx, double dts, int reps, double *best_ms4);
 
 /* Number of kernel launches this context has issued (diagnostics). */

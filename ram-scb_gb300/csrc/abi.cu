@@ -14,6 +14,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -88,6 +89,17 @@ struct ramgpu_ctx {
     size_t rec_call = 0;             // bytes of one call's record (8 sweeps)
     bool rec_stale = false;          // the record ring no longer holds the last segment
   } adj;
+  // ramgpu_ram_run_host: item groups, their streams and events, and the
+  // graph of the whole pipeline for one set of host buffers
+  int pipe_groups = 4;
+  cudaGraphExec_t pipe_exec = nullptr;
+  std::vector<const void*> pipe_key;
+  double pipe_dts = -1.0;
+  long long pipe_items = -1, pipe_launches = 0;
+  unsigned pipe_flags = 0;
+  int pipe_shape = -1, pipe_g = 0;
+  std::vector<cudaStream_t> pipe_streams;
+  std::vector<cudaEvent_t> pipe_events;  // per group: uploads done, group done; then one for the tables
   // optional per-kernel-class timing
   bool timing = false;
   std::vector<cudaEvent_t> ev_free;
@@ -214,7 +226,7 @@ static int prepare(ramgpu_ctx* ctx, double dts) {
   }
   if (ctx->tables_dts != dts) {
     launch_dts_tables(ctx->d, dts, ctx->stream);
-    ctx->launches += 3;
+    ctx->launches += 4;
     CKL("dts tables");
     ctx->tables_dts = dts;
   }
@@ -280,8 +292,10 @@ static int sumrc_stage(ramgpu_ctx* ctx, int stage, int which) {
 
 // Forward sweeps with the CFL reduction; when the coefficient store exists
 // they also keep each face's C and CORR factor for the reverse half.
-static int enqueue_forward(ramgpu_ctx* ctx, double dts, bool loss_fused, const double* loss_table) {
-  CK(cudaMemsetAsync(ctx->d.cflq, 0, sizeof(unsigned long long) * 4 * ctx->d.nm * ctx->d.ns, ctx->stream));
+static int enqueue_forward(ramgpu_ctx* ctx, double dts, bool loss_fused, const double* loss_table,
+                           bool clear_cfl = true) {
+  if (clear_cfl)
+    CK(cudaMemsetAsync(ctx->d.cflq, 0, sizeof(unsigned long long) * 4 * ctx->d.nm * ctx->d.ns, ctx->stream));
   const Dev& d = ctx->d;
   auto co = [&](int w) { return (d.coef && d.coef_slot[w] >= 0) ? 1 : 0; };
   { Timed t(ctx, 2); launch_sweep_r(d, dts, true, ctx->stream, nullptr, false, co(0)); }
@@ -308,28 +322,27 @@ static int enqueue_reverse(ramgpu_ctx* ctx, double dts, bool loss_fused, const d
   return RAMGPU_OK;
 }
 
-static int enqueue_body(ramgpu_ctx* ctx, double dts) {
+// The sweeps, losses and tail of one ram_run call for the work items of
+// ctx->d (the per-member tables and ghost planes are enqueued before);
+// clear_cfl: reset the CFL accumulators first.
+static int enqueue_sweeps(ramgpu_ctx* ctx, double dts, bool clear_cfl) {
   int rc = RAMGPU_OK;
-  { Timed t(ctx, 0); launch_member_coef(ctx->d, dts, ctx->stream); }
-  { Timed t(ctx, 1); launch_ghost(ctx->d, ctx->stream); }
-  ctx->launches += 5;
-  CKL("member tables");
   const bool losses = ctx->cfg.flags & RAMGPU_FLAG_LOSSES;
   const bool pd = ctx->pd_any();
   if (!losses && !pd) {
     // R,P,E,MU then CEX,ATMOL,ATMOL,CEX folded into the MU store
-    if ((rc = enqueue_forward(ctx, dts, true, ctx->d.loss2))) return rc;
+    if ((rc = enqueue_forward(ctx, dts, true, ctx->d.loss2, clear_cfl))) return rc;
     if ((rc = enqueue_reverse(ctx, dts, false, nullptr, true))) return rc;
   } else if (!losses) {
     // R,P,E,MU, WPADIF, CEX,ATMOL,ATMOL,CEX (folded into WPADIF's store), WPADIF, MU,E,P,R
-    if ((rc = enqueue_forward(ctx, dts, false, nullptr))) return rc;
+    if ((rc = enqueue_forward(ctx, dts, false, nullptr, clear_cfl))) return rc;
     { Timed t(ctx, 10); launch_padif(ctx->d, ctx->d.loss2, ctx->stream); }
     { Timed t(ctx, 10); launch_padif(ctx->d, nullptr, ctx->stream); }
     ctx->launches += 2;
     CKL("pitch-angle diffusion");
     if ((rc = enqueue_reverse(ctx, dts, false, nullptr, true))) return rc;
   } else {
-    if ((rc = enqueue_forward(ctx, dts, false, nullptr))) return rc;
+    if ((rc = enqueue_forward(ctx, dts, false, nullptr, clear_cfl))) return rc;
     if ((rc = sumrc_stage(ctx, 0, 1))) return rc;
     if (pd) {
       { Timed t(ctx, 10); launch_padif(ctx->d, nullptr, ctx->stream); }
@@ -360,6 +373,19 @@ static int enqueue_body(ramgpu_ctx* ctx, double dts) {
   return RAMGPU_OK;
 }
 
+static int enqueue_tables(ramgpu_ctx* ctx, double dts) {
+  { Timed t(ctx, 0); launch_member_coef(ctx->d, dts, ctx->stream); }
+  { Timed t(ctx, 1); launch_ghost(ctx->d, ctx->stream); }
+  ctx->launches += 3;
+  CKL("member tables");
+  return RAMGPU_OK;
+}
+
+static int enqueue_body(ramgpu_ctx* ctx, double dts) {
+  if (int rc = enqueue_tables(ctx, dts)) return rc;
+  return enqueue_sweeps(ctx, dts, true);
+}
+
 static void adj_free(ramgpu_ctx* ctx) {
   auto& a = ctx->adj;
   cudaFree(a.obs); cudaFree(a.fm); cudaFree(a.fm2); cudaFree(a.J); cudaFree(a.J2); cudaFree(a.ckpt);
@@ -387,7 +413,7 @@ static int enqueue_call_rec(ramgpu_ctx* ctx, double dts, unsigned char* rec, boo
   launch_finish(ctx->d, ctx->stream);
   if (moments) launch_moments(ctx->d, ctx->stream);
   else launch_anisch_state(ctx->d, ctx->stream);
-  ctx->launches += moments ? 15 : 14;
+  ctx->launches += moments ? 13 : 12;
   CKL("recorded ram_run");
   return RAMGPU_OK;
 }
@@ -408,7 +434,7 @@ static int enqueue_call_replay(ramgpu_ctx* ctx, double dts, unsigned char* rec) 
   launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 7 * isz, true);
   launch_finish(ctx->d, ctx->stream);
   launch_anisch_state(ctx->d, ctx->stream);
-  ctx->launches += 12;
+  ctx->launches += 10;
   CKL("replayed ram_run");
   return RAMGPU_OK;
 }
@@ -549,7 +575,8 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   d.cmu0 = dalloc<double>(ctx, nijl, &ok); d.wm = dalloc<double>(ctx, nijl, &ok);
   d.cmudot = dalloc<double>(ctx, nijl, &ok);
   d.rho = dalloc<double>(ctx, nr * nt, &ok);
-  d.epme = dalloc<double>(ctx, ns * ncell, &ok); d.epma = dalloc<double>(ctx, ns * ncell, &ok);
+  d.mw_a = dalloc<double>(ctx, ns * npa * ne * nr, &ok);
+  d.mw_be = dalloc<double>(ctx, npa * nt * nr, &ok); d.mw_ba = dalloc<double>(ctx, npa * nt * nr, &ok);
   d.p4 = dalloc<double>(ctx, ns * ne, &ok);
   d.p2 = dalloc<double>(ctx, ns * ne * nr, &ok); d.edot = dalloc<double>(ctx, ns * ne * nr, &ok);
   d.eb = dalloc<double>(ctx, ns * ne, &ok); d.ek = dalloc<double>(ctx, ns * ne, &ok);
@@ -561,6 +588,7 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   d.cr = dalloc<double>(ctx, nm * nr * nt, &ok); d.ca = dalloc<double>(ctx, nm * nr * nt, &ok);
   d.ue = dalloc<double>(ctx, nm * nijl, &ok); d.um = dalloc<double>(ctx, nm * nijl, &ok);
   d.drd1 = dalloc<double>(ctx, nm * nr * nt, &ok); d.dpd1 = dalloc<double>(ctx, nm * nr * nt, &ok);
+  d.mij = dalloc<double>(ctx, 8 * nr * nt, &ok);
   d.f2 = dalloc<double>(ctx, nslot * ncell, &ok);
   d.fgeos = dalloc<double>(ctx, nslot * nt * ne * npa, &ok);
   d.plane_last = dalloc<double>(ctx, nslot * ne * npa, &ok);
@@ -606,6 +634,9 @@ int ramgpu_destroy(ramgpu_ctx* ctx) {
   for (void* p : ctx->allocs) cudaFree(p);
   for (auto& sp : ctx->spans) { cudaEventDestroy(sp.a); cudaEventDestroy(sp.b); }
   for (cudaEvent_t e : ctx->ev_free) cudaEventDestroy(e);
+  if (ctx->pipe_exec) cudaGraphExecDestroy(ctx->pipe_exec);
+  for (cudaStream_t st : ctx->pipe_streams) cudaStreamDestroy(st);
+  for (cudaEvent_t e : ctx->pipe_events) cudaEventDestroy(e);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return RAMGPU_OK;
@@ -940,6 +971,166 @@ int ramgpu_ram_run_async(ramgpu_ctx* ctx, double dts) {
   return enqueue_ram_run(ctx, dts);
 }
 
+int ramgpu_set_pipeline_groups(ramgpu_ctx* ctx, int groups) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (groups < 1 || groups > 8) return fail(ctx, RAMGPU_ERR_ARG, "groups must be 1..8");
+  ctx->pipe_groups = groups;
+  return RAMGPU_OK;
+}
+
+// Uploads, sweeps and read-back of ram_run pipelined over item groups.
+// Stream order: the context's stream (previous work) -> event -> group
+// uploads chained in group order (so the first group starts computing
+// first) ; the per-member tables, ghost planes and CFL reset on the
+// context's stream -> event ; group g: its uploads, the tables event, its
+// sweeps and tail on a view of the work list, its read-back -> event the
+// context's stream waits for.  The coefficient store is indexed by the
+// item's place in the full list (Dev::item0), so groups never share it.
+// Enqueue only (direct launches or inside a graph capture of the context's
+// stream, which the group streams join through the events).
+static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, double* const* ppert,
+                            double* const* ppart, int G) {
+  const int nit = ctx->d.nitems;
+  cudaEvent_t ev_prev = ctx->pipe_events[2 * G], ev_tab = ctx->pipe_events[2 * G + 1];
+  const size_t n = ctx->d.ncell, nm2 = (size_t)ctx->d.nr * ctx->d.nt;
+  const cudaStream_t main = ctx->stream;
+  const Dev full = ctx->d;
+  auto slot_of = [&](int it) { return ctx->items_h[it].x * full.ns + ctx->items_h[it].y; };
+  CK(cudaEventRecord(ev_prev, main));
+  // uploads, in group order
+  for (int g = 0; g < G; ++g) {
+    const int i0 = (int)((long long)nit * g / G), i1 = (int)((long long)nit * (g + 1) / G);
+    cudaStream_t st = ctx->pipe_streams[g];
+    CK(cudaStreamWaitEvent(st, g == 0 ? ev_prev : ctx->pipe_events[2 * (g - 1)], 0));
+    for (int it = i0; it < i1; ++it) {
+      const int slot = slot_of(it);
+      if (f2[slot])
+        CK(cudaMemcpyAsync(full.f2 + (size_t)slot * n, f2[slot], n * sizeof(double), cudaMemcpyDefault, st));
+    }
+    CK(cudaEventRecord(ctx->pipe_events[2 * g], st));
+  }
+  // per-member tables and ghost planes of every item, CFL accumulators
+  if (int rc = enqueue_tables(ctx, dts)) return rc;
+  CK(cudaMemsetAsync(full.cflq, 0, sizeof(unsigned long long) * 4 * full.nm * full.ns, main));
+  CK(cudaEventRecord(ev_tab, main));
+  for (int g = 0; g < G; ++g) {
+    const int i0 = (int)((long long)nit * g / G), i1 = (int)((long long)nit * (g + 1) / G);
+    cudaStream_t st = ctx->pipe_streams[g];
+    CK(cudaStreamWaitEvent(st, ev_tab, 0));
+    ctx->stream = st;
+    ctx->d.items = full.items + i0;
+    ctx->d.nitems = i1 - i0;
+    ctx->d.item0 = i0;
+    const int rc = enqueue_sweeps(ctx, dts, false);
+    ctx->d = full;
+    ctx->stream = main;
+    if (rc) return rc;
+    for (int it = i0; it < i1; ++it) {
+      const int slot = slot_of(it);
+      if (f2[slot])
+        CK(cudaMemcpyAsync(f2[slot], full.f2 + (size_t)slot * n, n * sizeof(double), cudaMemcpyDefault, st));
+      if (ppert && ppert[slot])
+        CK(cudaMemcpyAsync(ppert[slot], full.ppert + (size_t)slot * nm2, nm2 * sizeof(double), cudaMemcpyDefault, st));
+      if (ppart && ppart[slot])
+        CK(cudaMemcpyAsync(ppart[slot], full.ppart + (size_t)slot * nm2, nm2 * sizeof(double), cudaMemcpyDefault, st));
+    }
+    CK(cudaEventRecord(ctx->pipe_events[2 * g + 1], st));
+    CK(cudaStreamWaitEvent(main, ctx->pipe_events[2 * g + 1], 0));
+  }
+  return RAMGPU_OK;
+}
+
+int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* const* ppert,
+                        double* const* ppart) {
+  if (check_ctx(ctx) || !f2) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  int rc = prepare(ctx, dts);
+  if (rc) return rc;
+  ctx->last_dts = dts;
+  const int nit = ctx->d.nitems;
+  if (nit == 0) return RAMGPU_OK;
+  // the loss bookkeeping indexes its partial sums by list position: one group
+  const bool losses = ctx->cfg.flags & RAMGPU_FLAG_LOSSES;
+  const int G = losses ? 1 : std::min(ctx->pipe_groups, nit);
+  // group g's stream gets the g-th highest priority, so the block scheduler
+  // favours the groups in upload order
+  if ((int)ctx->pipe_streams.size() < G) {
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    while ((int)ctx->pipe_streams.size() < G) {
+      const int prio = std::min(least, greatest + (int)ctx->pipe_streams.size());
+      cudaStream_t st = nullptr;
+      CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio));
+      ctx->pipe_streams.push_back(st);
+    }
+  }
+  while ((int)ctx->pipe_events.size() < 2 * G + 2) {
+    cudaEvent_t e = nullptr;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ctx->pipe_events.push_back(e);
+  }
+  const bool timing = ctx->timing;
+  ctx->timing = false;
+  // a graph holds the copies' host addresses, so it is kept per buffer set
+  // and only for page-locked (or device) buffers: capturing a copy from
+  // pageable memory is not allowed
+  const int nslot = ctx->d.nm * ctx->d.ns;
+  std::vector<const void*> key;
+  bool capturable = ctx->graph_on;
+  for (double* const* tab : {f2, ppert, ppart}) {
+    for (int k = 0; k < nslot; ++k) {
+      const void* p = tab ? (const void*)tab[k] : nullptr;
+      key.push_back(p);
+      if (p && capturable) {
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, p) != cudaSuccess || at.type == cudaMemoryTypeUnregistered) {
+          cudaGetLastError();
+          capturable = false;
+        }
+      }
+    }
+  }
+  if (!capturable) {
+    rc = enqueue_pipeline(ctx, dts, f2, ppert, ppart, G);
+  } else {
+    if (!ctx->pipe_exec || ctx->pipe_key != key || ctx->pipe_dts != dts || ctx->pipe_items != ctx->items_version ||
+        ctx->pipe_flags != ctx->d.flags || ctx->pipe_shape != ctx->shape_version || ctx->pipe_g != G) {
+      if (ctx->pipe_exec) cudaGraphExecDestroy(ctx->pipe_exec);
+      ctx->pipe_exec = nullptr;
+      cudaGraph_t g = nullptr;
+      const long long l0 = ctx->launches;
+      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      rc = enqueue_pipeline(ctx, dts, f2, ppert, ppart, G);
+      cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+      ctx->pipe_launches = ctx->launches - l0;  // kernels per replay
+      ctx->launches = l0;
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        ctx->timing = timing;
+        return rc;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->pipe_exec, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        ctx->pipe_exec = nullptr;
+        ctx->timing = timing;
+        return cuda_fail(ctx, e, "pipeline graph");
+      }
+      ctx->pipe_key = key;
+      ctx->pipe_dts = dts;
+      ctx->pipe_items = ctx->items_version;
+      ctx->pipe_flags = ctx->d.flags;
+      ctx->pipe_shape = ctx->shape_version;
+      ctx->pipe_g = G;
+    }
+    CK(cudaGraphLaunch(ctx->pipe_exec, ctx->stream));
+    ctx->launches += ctx->pipe_launches;
+  }
+  ctx->timing = timing;
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return RAMGPU_OK;
+}
+
 int ramgpu_ram_run(ramgpu_ctx* ctx, double dts) {
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
   int rc = enqueue_ram_run(ctx, dts);
@@ -957,7 +1148,7 @@ int ramgpu_half_step(ramgpu_ctx* ctx, double dts, int order) {
   if (ctx->d.nitems == 0) return RAMGPU_OK;
   launch_member_coef(ctx->d, dts, ctx->stream);
   launch_ghost(ctx->d, ctx->stream);
-  ctx->launches += 5;
+  ctx->launches += 3;
   CKL("member tables");
   if (order == 0) rc = enqueue_forward(ctx, dts, true, ctx->d.loss1);
   else rc = enqueue_reverse(ctx, dts, true, ctx->d.loss1, false);
@@ -975,7 +1166,7 @@ int ramgpu_apply_op(ramgpu_ctx* ctx, double dts, int op, int cfl) {
   if (ctx->d.nitems == 0) return RAMGPU_OK;
   launch_member_coef(ctx->d, dts, ctx->stream);
   launch_ghost(ctx->d, ctx->stream);
-  ctx->launches += 5;
+  ctx->launches += 3;
   if (cfl) CK(cudaMemsetAsync(ctx->d.cflq, 0, sizeof(unsigned long long) * 4 * ctx->d.nm * ctx->d.ns, ctx->stream));
   switch (op) {
     case 0: launch_sweep_r(ctx->d, dts, cfl != 0, ctx->stream); break;
@@ -1167,7 +1358,7 @@ int ramgpu_autotune(ramgpu_ctx* ctx, double dts, int reps, double* best_ms4) {
   if (ctx->d.nitems == 0) return RAMGPU_OK;
   launch_member_coef(ctx->d, dts, ctx->stream);
   launch_ghost(ctx->d, ctx->stream);
-  ctx->launches += 5;
+  ctx->launches += 3;
   // the trials advance F2: keep a copy of every active slot and restore it
   const size_t ncell = ctx->d.ncell;
   double* snap = nullptr;
@@ -1198,24 +1389,26 @@ int ramgpu_autotune(ramgpu_ctx* ctx, double dts, int reps, double* best_ms4) {
         }
         ctx->d.blk[w] = blk;
         ctx->d.pers[w] = pc;
-        float tot = 0.f;
+        // one trial = a whole ram_run step (direct launches) with this
+        // sweep's shape and the others' current ones: the sweeps interact
+        // through L2 and the SM schedule, so isolated sweeps mislead; best
+        // of reps after one warm-up step
+        float tbest = 1e30f;
         for (int r = 0; r <= reps; ++r) {
           cudaEventRecord(e0, ctx->stream);
-          switch (w) {
-            case 0: launch_sweep_r(ctx->d, dts, false, ctx->stream); break;
-            case 1: launch_sweep_p(ctx->d, dts, false, ctx->stream); break;
-            case 2: launch_sweep_e(ctx->d, dts, false, ctx->stream); break;
-            default: launch_sweep_mu(ctx->d, dts, false, 0, nullptr, ctx->stream); break;
+          if (int rc2 = enqueue_body(ctx, dts)) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            cudaFree(snap);
+            return rc2;
           }
           cudaEventRecord(e1, ctx->stream);
           cudaEventSynchronize(e1);
           float ms = 0.f;
           cudaEventElapsedTime(&ms, e0, e1);
-          if (r > 0) tot += ms;  // first launch is a warm-up
-          ctx->launches += 1;
+          if (r > 0 && ms < tbest) tbest = ms;
         }
-        const float avg = tot / reps;
-        if (avg < best) { best = avg; bb = blk; bp = pc; }
+        if (tbest < best) { best = tbest; bb = blk; bp = pc; }
       }
     }
     ctx->d.blk[w] = bb;
@@ -1600,7 +1793,7 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
       launch_adj_sweep(d, 2, r + 2 * isz, ctx->stream);
       launch_adj_sweep(d, 1, r + 1 * isz, ctx->stream);
       launch_adj_sweep(d, 0, r + 0 * isz, ctx->stream);
-      ctx->launches += 17;
+      ctx->launches += 15;
       CKL("adjoint backward");
     }
   }

@@ -29,27 +29,33 @@ namespace ramgpu {
 // streamed once with a rolling window of four cell accumulators in
 // registers: after face f, cell f-1 is final and is written out.
 
-// Scatter of one face into the window (cm1, c0, c1, c2) = cells f-1..f+2:
-// the upwind cell gets FBb, the two cells of LX get +-ak*FBb with ak = a
-// (cases 2, 3) or beta*a (cases 1, 4).  Every coefficient is picked by
-// integer selects, so a face costs 2 adds and 4 fma on the FP64 pipe
-// whatever its case.
+// Scatter of one face into the window (cm1, c0, c1, c2) = cells f-1..f+2.
+// FBND(f) = FUP + a LX depends on three adjacent cells: (f-1, f, f+1) when
+// the face is upwinded from the left (C >= 0, FUP = F(f)) and (f, f+1, f+2)
+// from the right (FUP = F(f+1)); in that shifted window its derivatives are
+//   (-ak, 1+ak, 0)  for LX = D from the left or LX = X from the right,
+//   (0, 1-ak, ak)   for LX = X from the left or LX = D from the right,
+//   (0, 1, 0)       upwind only,
+// with ak = a (cases 2, 3) or beta*a (cases 1, 4).  The window and the
+// signed coefficient are picked by integer selects, so a face costs one add
+// and three fma on the FP64 pipe whatever its case.
 __device__ __forceinline__ void face_acc(double FBb, bool neg, int cs, double ak, double& cm1,
                                          double& c0, double& c1, double& c2) {
   const bool xt = (cs == 2) | (cs == 4);  // LX = X (f, f+1)
   const bool dt = (cs == 1) | (cs == 3);  // LX = D (f-1, f) or (f+1, f+2)
-  const double pos = (xt | dt) ? ak : 0.0;
-  const double ngv = bitsd(dbits(pos) ^ kSignMask);
-  const double sm1 = (dt & !neg) ? ngv : 0.0;
-  const double s0 = xt ? ngv : ((dt & !neg) ? pos : 0.0);
-  const double s1 = xt ? pos : ((dt & neg) ? ngv : 0.0);
-  const double s2 = (dt & neg) ? pos : 0.0;
-  const double f0 = neg ? s0 : s0 + 1.0;  // FUP = F(f) for s = +1
-  const double f1 = neg ? s1 + 1.0 : s1;  // FUP = F(f+1) for s = -1
-  cm1 = fma(sm1, FBb, cm1);
-  c0 = fma(f0, FBb, c0);
-  c1 = fma(f1, FBb, c1);
-  c2 = fma(s2, FBb, c2);
+  const bool left = (dt & !neg) | (xt & neg);
+  const bool right = (xt & !neg) | (dt & neg);
+  const double sak = left ? bitsd(dbits(ak) ^ kSignMask) : (right ? ak : 0.0);
+  const double a0 = left ? sak : 0.0, a2 = right ? sak : 0.0;
+  const double a1 = 1.0 - sak;
+  double t0 = neg ? c0 : cm1, t1 = neg ? c1 : c0, t2 = neg ? c2 : c1;
+  t0 = fma(a0, FBb, t0);
+  t1 = fma(a1, FBb, t1);
+  t2 = fma(a2, FBb, t2);
+  cm1 = neg ? cm1 : t0;
+  c0 = neg ? t0 : t1;
+  c1 = neg ? t1 : t2;
+  c2 = neg ? t2 : c2;
 }
 
 // ak = LIMITER weight times the CORR factor a = -0.5*(C*q - s) of a face:
@@ -72,9 +78,17 @@ __device__ __forceinline__ double face_ak(double C, bool neg, int cs, double mh,
   return fma(C, kb ? bmh : mh, shk);
 }
 
-// lambda of cell c of a line (stride st) masked by the clip bit
-__device__ __forceinline__ double masked(const double* lam, const unsigned char* rl, long long off) {
-  return (rl[off] & kClipBit) ? 0.0 : lam[off];
+// lambda of cell c of a line (stride st) masked by the clip bit.  Both
+// loads are issued unconditionally (the record through the read-only path)
+// so that the next cells' loads can run ahead of the window's arithmetic.
+// kNc: lambda too through the read-only path, for lines that own whole
+// 32-byte sectors and are read ahead of where they are written, so no
+// sector is read again after a write in the same launch.
+template <bool kNc = false>
+__device__ __forceinline__ double masked(const double* __restrict__ lam, const unsigned char* __restrict__ rl,
+                                         long long off) {
+  const double v = kNc ? __ldg(lam + off) : lam[off];
+  return (__ldg(rl + off) & kClipBit) ? 0.0 : v;
 }
 
 #define WORK_LOOP(NLINES)                                                          \
@@ -92,7 +106,12 @@ __device__ __forceinline__ double masked(const double* lam, const unsigned char*
 // inflow lines); FBND(1) = F(2) on inflow lines, FBND(NR) = F(NR) on outflow
 // lines (both 0 when closed).  The ghosts' adjoints go to dJ/dFGEOS, for an
 // outflow line to the FGEOS cell its stale ghost came from.
-__global__ void __launch_bounds__(128) k_adj_r(Dev d, const unsigned char* __restrict__ rec) {
+// kNc (NR a multiple of 4): a line is NR doubles at a multiple of NR, so it
+// owns whole sectors and lambda can be read ahead through the read-only path.
+// Six resident CTAs per SM as the register target: without it the compiler
+// aims at a higher occupancy and spills the window (measured slower).
+template <bool kNc>
+__global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = nt * ne * d.npa;
   WORK_LOOP(nlines) {
@@ -101,10 +120,10 @@ __global__ void __launch_bounds__(128) k_adj_r(Dev d, const unsigned char* __res
     const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
     if (line >= nlines) continue;
     const int j = line % nt, k = (line / nt) % ne, l = line / (nt * ne);
-    double* lam = d.lam + (long long)slot * d.ncell + (long long)line * nr;
-    const unsigned char* rl = rec + (u / bpi) * d.ncell + (long long)line * nr;
-    const double* grt = d.grt + ((long long)l * nt + j) * nr;
-    const double* cr = d.cr + ((long long)m * nt + j) * nr;
+    double* __restrict__ lam = d.lam + (long long)slot * d.ncell + (long long)line * nr;
+    const unsigned char* __restrict__ rl = rec + (u / bpi) * d.ncell + (long long)line * nr;
+    const double* __restrict__ grt = d.grt + ((long long)l * nt + j) * nr;
+    const double* __restrict__ cr = d.cr + ((long long)m * nt + j) * nr;
     const double p4 = d.p4[s * ne + k];
     const double hb = 0.5 * d.betalim, bmh = -hb;
     const bool closed = d.flags & 1u;
@@ -112,7 +131,7 @@ __global__ void __launch_bounds__(128) k_adj_r(Dev d, const unsigned char* __res
     const double cN = fma(grt[n - 1], p4, cr[n - 1]);
     const bool inflow = is_neg(cN);
     // le(i) = lambda of updated, unclipped cell i (i = 2..NR); window = cells f-1..f+2
-    double le0 = masked(lam, rl, 1), le1 = masked(lam, rl, 2), le2 = masked(lam, rl, 3);
+    double le0 = masked<kNc>(lam, rl, 1), le1 = masked<kNc>(lam, rl, 2), le2 = masked<kNc>(lam, rl, 3);
     double cm1 = lam[0], c0 = le0, c1 = le1, c2 = le2;
     if (inflow && !closed) c0 += fma(grt[0], p4, cr[0]) * le0;  // FBND(1) = F(2)
     auto face = [&](int f, double C) {
@@ -128,7 +147,7 @@ __global__ void __launch_bounds__(128) k_adj_r(Dev d, const unsigned char* __res
     int f = 2;
     for (; f <= n - 3; ++f) {
       face(f, fma(grt[f - 1], p4, cr[f - 1]));
-      advance(f, masked(lam, rl, f + 2));
+      advance(f, masked<kNc>(lam, rl, f + 2));
     }
     for (; f <= n - 1; ++f) {
       face(f, fma(grt[f - 1], p4, cr[f - 1]));
@@ -179,10 +198,10 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
     const int k = kl % ne, l = kl / ne;
     const long long st = nr;
     const long long base = ((long long)kl * nt) * nr + i;
-    double* lam = d.lam + (long long)slot * d.ncell + base;
-    const unsigned char* rl = rec + (u / bpi) * d.ncell + base;
-    const double* gpt = d.gpt + ((long long)l * nt) * nr + i;
-    const double* ca = d.ca + ((long long)m * nt) * nr + i;
+    double* __restrict__ lam = d.lam + (long long)slot * d.ncell + base;
+    const unsigned char* __restrict__ rl = rec + (u / bpi) * d.ncell + base;
+    const double* __restrict__ gpt = d.gpt + ((long long)l * nt) * nr + i;
+    const double* __restrict__ ca = d.ca + ((long long)m * nt) * nr + i;
     const double p2 = d.p2[((long long)s * ne + k) * nr + i];
     const double hb = 0.5 * d.betalim, bmh = -hb;
     const int n = nt;
@@ -260,13 +279,13 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
     const int j = jl % nt, l = jl / nt;
     const long long st = (long long)nt * nr;
     const long long base = ((long long)l * ne * nt + j) * nr + i;
-    double* lam = d.lam + (long long)slot * d.ncell + base;
-    const unsigned char* rl = rec + (u / bpi) * d.ncell + base;
+    double* __restrict__ lam = d.lam + (long long)slot * d.ncell + base;
+    const unsigned char* __restrict__ rl = rec + (u / bpi) * d.ncell + base;
     const long long fij = ((long long)l * nt + j) * nr + i;
     const double wet = d.wet[fij];
     const double ue = d.ue[(long long)m * nr * nt * d.npa + fij];
-    const double* edot = d.edot + (long long)s * ne * nr + i;
-    const double* eb = d.eb + s * ne;
+    const double* __restrict__ edot = d.edot + (long long)s * ne * nr + i;
+    const double* __restrict__ eb = d.eb + s * ne;
     const double hb = 0.5 * d.betalim;
     const bool closed = d.flags & 1u;
     const int n = ne;
@@ -335,12 +354,12 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
     const int j = jk % nt;
     const long long st = (long long)ne * nt * nr;
     const long long off = (long long)jk * nr + i;
-    double* lam = d.lam + (long long)slot * d.ncell + off;
-    const unsigned char* rl = rec + (u / bpi) * d.ncell + off;
+    double* __restrict__ lam = d.lam + (long long)slot * d.ncell + off;
+    const unsigned char* __restrict__ rl = rec + (u / bpi) * d.ncell + off;
     const long long sij = (long long)nt * nr;
     const long long fij = (long long)j * nr + i;
-    const double* wm = d.wm + fij;
-    const double* um = d.um + (long long)m * nt * nr * npa + fij;
+    const double* __restrict__ wm = d.wm + fij;
+    const double* __restrict__ um = d.um + (long long)m * nt * nr * npa + fij;
     const double ekv = d.ek[s * ne + jk / nt];
     const double hb = 0.5 * d.betalim;
     const bool closed = d.flags & 1u;
@@ -408,7 +427,10 @@ void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_
   }
   dim3 g((nl + blk - 1) / blk, d.nitems, 1);
   switch (w) {
-    case 0: k_adj_r<<<g, blk, 0, st>>>(d, rec); break;
+    case 0:
+      if (d.nr % 4 == 0) k_adj_r<true><<<g, blk, 0, st>>>(d, rec);
+      else k_adj_r<false><<<g, blk, 0, st>>>(d, rec);
+      break;
     case 1: k_adj_p<<<g, blk, 0, st>>>(d, rec); break;
     case 2: k_adj_e<<<g, blk, 0, st>>>(d, rec); break;
     default: k_adj_mu<<<g, blk, 0, st>>>(d, rec); break;

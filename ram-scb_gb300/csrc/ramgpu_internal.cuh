@@ -59,7 +59,8 @@ struct Dev {
   double *gre, *gpe, *ze, *wet;   // E: GPR1+2+3, GPP1+2, dBdt1+dIdt1, EDT1 factor
   double *gmr, *gmp, *zm, *hm, *cmu0;  // MU
   double *rho;            // (NR,NT): FNHS(NPA)*MU(NPA)/FNHS(NPA-1)/MU(NPA-1)
-  double *epme, *epma;    // (ns, ncell): ANISCH weights, exact reference formula
+  double *mw_a;           // (ns, NPA, NE, NR): ANISCH weight RFAC*EPP(K)/FFACTOR
+  double *mw_be, *mw_ba;  // (NPA, NT, NR): ANISCH weights WMU/FNHS*(1-MU^2), 2*WMU/FNHS*MU^2
   // DTs-dependent per-species small tables
   double *p4;             // (ns, NE)
   double *p2;             // (ns, NR, NE)
@@ -85,6 +86,7 @@ struct Dev {
   double *ca;             // (nm, NR, NT)
   double *ue, *um;        // (nm, NR, NT, NPA)
   double *drd1, *dpd1;    // (nm, NR, NT): DRD1 = DRM1, DPD1 = DPM1 of DRIFTE/DRIFTMU
+  double *mij;            // (8, NT, NR): VT-independent factors of cr, ca, drd1, dpd1 (DTs, fields)
   // per (member, species) slot
   double *f2;             // (nm*ns, ncell)
   double *fgeos;          // (nm*ns, NT*NE*NPA)
@@ -97,7 +99,7 @@ struct Dev {
   double *lam;            // (nm*ns, ncell)
   double *gfg;            // (nm*ns, NT*NE*NPA)
   unsigned long long *cflq;  // (nm*ns, 4): max over cells of the CFL quotient, as bits
-  double *mom_part;       // (nm*ns, 4 chunks, NE, NT, NR, 2) per-K moment partials
+  double *mom_part;       // (nm*ns, NT, NR, (NE-1)*4 chunks, 2) moment partials
   double *ppert, *ppart;  // (nm*ns, NR, NT)
   double *sumrc_part;     // (nm*ns, nblk) SUMRC partial sums
   // face coefficients C and a of the forward sweeps, read back by the
@@ -109,6 +111,7 @@ struct Dev {
   // work list
   const int2 *items;      // (member, species)
   int nitems;
+  int item0;              // position of items[0] in the full list (a group's view of it)
   // launch shape of the sweeps R, P, E, MU: threads per CTA and, when > 0,
   // a persistent grid of that many CTAs looping over (item, line-block) units
   int blk[4];
@@ -185,7 +188,7 @@ constexpr int kClipBit = 8;  // recorded with the case: the updated cell was cli
 
 // Stored face coefficient array q (0: C, 1: a) of sweep w for work item `it`.
 __device__ __forceinline__ double* coef_ptr(const Dev& d, int w, int q, long long it) {
-  return d.coef + (((long long)(d.coef_slot[w] * 2 + q) * d.coef_items) + it) * d.ncell;
+  return d.coef + (((long long)(d.coef_slot[w] * 2 + q) * d.coef_items) + d.item0 + it) * d.ncell;
 }
 
 // Face value with the branch taken from a record (frozen-limiter replay):

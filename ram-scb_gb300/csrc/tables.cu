@@ -3,8 +3,9 @@
 // The drift coefficients of the reference are recomputed per cell and per
 // call; here they are split into factors that change at different rates:
 //   fields only (set_fields)      : grt, gpt, gre, gpe, ze, wet, gmr, gmp, zm, hm, cmu0, rho
-//   species only (set_grid)       : eb, ek, kap, ANISCH weights epme/epma
+//   species only (set_grid)       : eb, ek, kap, ANISCH weights mw_a (mw_be, mw_ba: fields)
 //   DTs (when DTs changes)        : p4, p2, edot, cmudot, wm, CHARGE/ATMOL factors
+//   DTs and fields                : mij (E x B factors per I, J)
 //   potential VT (every ram_run)  : cr, ca, ue, um
 // so that a sweep face needs one or two FP64 operations for its coefficient.
 // Formulas restate src/ModRamDrift.f90:36-88 (DRIFTPARA), :118-146 (DRIFTR),
@@ -157,33 +158,46 @@ __global__ void k_species_static(Dev d) {
   }
 }
 
-// ANISCH weights ERNM/EPMA/EPME of src/ModRamRun.f90:372-374, per species.
+// ANISCH weights (src/ModRamRun.f90:372-374 and :380-389).  The reference's
+// ERNM = WMU(L)/FFACTOR(S,I,K,L)/FNHS(I,J,L), EPMA = ERNM*MU^2,
+// EPME = ERNM-EPMA, with the energy weight EPP(S,K) and the band factors
+// RFAC folded in, is the product of a species factor and a field factor:
+//   mw_a (S,L,K,I)  = RFAC*EPP(S,K)/FFACTOR(S,I,K,L)
+//   mw_be(L,J,I)    = WMU(L)/FNHS(I,J,L)*(1-MU(L)^2)   (as B - B*MU*MU)
+//   mw_ba(L,J,I)    = 2*WMU(L)/FNHS(I,J,L)*MU(L)^2
+// so PPERT = sum over K>=2, L<=u of (F2*mw_a)*mw_be and PPART likewise.
+// The reference sums the same products band by band (khi = 6,10,25,30,NE)
+// and scales each band by RFAC; the orders differ by rounding only.  Both
+// tables stay in L2 (NS*NPA*NE*NR and NPA*NT*NR doubles).
 __global__ void k_moment_weights(Dev d) {
+  const long long na = (long long)d.ns * d.npa * d.ne * d.nr;
+  const long long nb = (long long)d.npa * d.nt * d.nr;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)d.ns * d.ncell) return;
-  const int s = (int)(t / d.ncell);
-  const long long c = t % d.ncell;
-  const int I = 1 + (int)(c % d.nr);
-  const int J = 1 + (int)((c / d.nr) % d.nt);
-  const int K = 1 + (int)((c / ((long long)d.nr * d.nt)) % d.ne);
-  const int L = 1 + (int)(c / ((long long)d.nr * d.nt * d.ne));
-  double me = 0.0, ma = 0.0;
-  if (I >= 2 && K >= 2 && L <= d.upa_mom[I - 1]) {
+  if (t < na) {
+    const int I = 1 + (int)(t % d.nr);
+    const int K = 1 + (int)((t / d.nr) % d.ne);
+    const int L = 1 + (int)((t / ((long long)d.nr * d.ne)) % d.npa);
+    const int s = (int)(t / ((long long)d.nr * d.ne * d.npa));
     const double ff = d.ffactor[(long long)s * d.nr * d.ne * d.npa + (((long long)L - 1) * d.ne + (K - 1)) * d.nr + (I - 1)];
-    const double ERNM = WMU(L) / ff / FNHS(I, J, L);
-    const double EPMA = ERNM * MU(L) * MU(L);
-    me = ERNM - EPMA;
-    ma = EPMA;
+    const double RFAC = 4 * kPI / (kCS * 100);
+    d.mw_a[t] = RFAC * d.epp[s * d.ne + K - 1] / ff;
+  } else if (t < na + nb) {
+    const long long c = t - na;
+    const int I = 1 + (int)(c % d.nr);
+    const int J = 1 + (int)((c / d.nr) % d.nt);
+    const int L = 1 + (int)(c / ((long long)d.nr * d.nt));
+    const double B = WMU(L) / FNHS(I, J, L);
+    const double BA = B * MU(L) * MU(L);
+    d.mw_be[c] = B - BA;
+    d.mw_ba[c] = 2 * BA;
   }
-  d.epme[t] = me;
-  d.epma[t] = ma;
 }
 
 void launch_species_static(const Dev& d, cudaStream_t st) {
   int n = d.ns * d.ne;
   k_species_static<<<(n + 127) / 128, 128, 0, st>>>(d);
-  long long nc = (long long)d.ns * d.ncell;
-  k_moment_weights<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(d);
+  const long long nw = (long long)d.ns * d.npa * d.ne * d.nr + (long long)d.npa * d.nt * d.nr;
+  k_moment_weights<<<(unsigned)((nw + 255) / 256), 256, 0, st>>>(d);
 }
 
 // ------------------------------------------------------------- DTs tables
@@ -251,9 +265,45 @@ __global__ void k_dts_loss(Dev d, double DTs) {
   d.loss2[t] = ((ch * at) * at) * ch;
 }
 
+// VT-independent parts of the per-call E x B terms, per (I, J) (src/ModRamDrift.f90:118-127,
+// :232-239 and DRIFTPARA :60-75), so that each per-call term is one fma on
+// the VT combination:
+//   CR   = crk*(VT(I,J0)+VT(I+1,J0)-VT(I,J1)-VT(I+1,J1)) + cr0
+//   CA   = cak*(VT(I+1,J)+VT(I+1,J1)-VT(I-1,J)-VT(I-1,J1)) + ca0   (I, J >= 2)
+//   DRD1 = d1k*(VT(I,J1)-VT(I,J0)) + d10,  DPD1 = p1k*(VT(I+1,J)-VT(I-1,J)) + p10
+// (the reference's quotients regrouped; they agree to rounding).  mij is
+// (8, NT, NR) in that order: crk, cr0, cak, ca0, d1k, d10, p1k, p10.
+__global__ void k_dts_ij(Dev d, double DTs) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = d.nr * d.nt;
+  if (t >= n) return;
+  const int I = 1 + t % d.nr, J = 1 + t / d.nr;
+  int J0, J1;
+  wrapj(J, d.nt, J0, J1);
+  const double MDR = d.mdr, DPHI = d.dphi;
+  const double VR = DTs / MDR / (RLZ(I) + 0.5 * MDR) / 2 / DPHI;
+  const double den = BNES(I, J) + BNES(I + 1, J);
+  double v[8] = {VR / den, (EIP(I, J) + EIP(I + 1, J)) / den * DTs / MDR, 0., 0., 0., 0., 0., 0.};
+  if (I >= 2) {
+    const double R = RLZ(I);
+    if (J >= 2) {
+      const double denp = BNES(I, J) + BNES(I, J1);
+      v[2] = DTs / DPHI / 2 / MDR / R / denp;
+      v[3] = kOME * DTs / DPHI - (EIR(I, J1) + EIR(I, J)) / R * DTs / DPHI / denp;
+    }
+    v[4] = -0.5 / DPHI / BNES(I, J);
+    v[5] = EIP(I, J) * R / BNES(I, J);
+    v[6] = 0.5 / MDR / BNES(I, J);
+    v[7] = kOME * R - EIR(I, J) / BNES(I, J);
+  }
+  for (int q = 0; q < 8; ++q) d.mij[(long long)q * n + t] = v[q];
+}
+
 void launch_dts_tables(const Dev& d, double dts, cudaStream_t st) {
   int n = d.ns * d.ne * d.nr;
   k_dts_small<<<(n + 127) / 128, 128, 0, st>>>(d, dts);
+  const int nij = d.nr * d.nt;
+  k_dts_ij<<<(nij + 127) / 128, 128, 0, st>>>(d, dts);
   long long nc = (long long)d.nr * d.nt * d.npa;
   k_dts_cells<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(d, dts);
   long long nl = (long long)d.ns * d.ncell;
@@ -261,95 +311,59 @@ void launch_dts_tables(const Dev& d, double dts, cudaStream_t st) {
 }
 
 // ------------------------------------------------ per-member (VT) tables
-__global__ void k_vt(Dev d) {
-  const int nv = d.nf * d.nt;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)d.nm * nv) return;
-  const int m = (int)(t / nv);
-  if (d.vt_mode[m] != 1) return;
-  const int i = (int)(t % nv) % d.nf;
-  const int j = (int)(t % nv) / d.nf;
-  const double KP = d.kp[m];
-  const double tt = 1. - 0.159 * KP + 0.0093 * (KP * KP);
-  const double AVS = 7.05E-6 / (tt * tt * tt) / kRE;
-  // VT = AVS*(LZ*RE)**2*SIN(PHI-PHIOFS), with (LZ*RE)**2 and SIN(PHI) tabulated
-  d.vt[t] = AVS * d.lr2[i] * d.sinphi[j];
-}
+// VT(I,J) of member m: the VOLS formula (src/ModRamRun.f90:45-54)
+// AVS*(LZ*RE)**2*SIN(PHI-PHIOFS) with (LZ*RE)**2 and the sine tabulated, or
+// the explicit potential of ramgpu_set_potential.
+struct VtSource {
+  const double* vt;
+  double avs;
+  bool vols;
+  __device__ VtSource(const Dev& d, int m) : vt(d.vt + (long long)m * d.nf * d.nt), avs(0.0), vols(d.vt_mode[m] == 1) {
+    if (vols) {
+      const double KP = d.kp[m];
+      const double tt = 1. - 0.159 * KP + 0.0093 * (KP * KP);
+      avs = 7.05E-6 / (tt * tt * tt) / kRE;
+    }
+  }
+  __device__ double operator()(const Dev& d, int I, int J) const {
+    return vols ? avs * d.lr2[I - 1] * d.sinphi[J - 1] : vt[BIX(I, J)];
+  }
+};
 
 // Per (member, I, J): the E x B terms of DRIFTR and DRIFTP and the
-// DRD1/DPD1 (= DRM1/DPM1) factors of DRIFTE/DRIFTMU.
-__global__ void k_member_ij(Dev d, double DTs) {
-  const long long per = (long long)d.nr * d.nt;
+// DRD1/DPD1 (= DRM1/DPM1) factors of DRIFTE/DRIFTMU, one fma each on the
+// VT combination (k_dts_ij holds the rest).
+__global__ void k_member_ij(Dev d) {
+  const int per = d.nr * d.nt;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= (long long)d.nm * per) return;
   const int m = (int)(t / per);
-  const int I = 1 + (int)((t % per) % d.nr);
-  const int J = 1 + (int)((t % per) / d.nr);
-  const double* vt = d.vt + (long long)m * d.nf * d.nt;
-#define VT(I, J) vt[BIX(I, J)]
-  const double MDR = d.mdr, DPHI = d.dphi;
+  const int ij = (int)(t % per);
+  const int I = 1 + ij % d.nr;
+  const int J = 1 + ij / d.nr;
+  const VtSource VT(d, m);
+  const double* __restrict__ q = d.mij + ij;
   int J0, J1;
   wrapj(J, d.nt, J0, J1);
-  // DRIFTR E x B (src/ModRamDrift.f90:118-127) with VR from DRIFTPARA
-  const double VR = DTs / MDR / (RLZ(I) + 0.5 * MDR) / 2 / DPHI;
-  const double den = BNES(I, J) + BNES(I + 1, J);
-  d.cr[t] = VR * (VT(I, J0) + VT(I + 1, J0) - VT(I, J1) - VT(I + 1, J1)) / den
-            + (EIP(I, J) + EIP(I + 1, J)) / den * DTs / MDR;
+  d.cr[t] = fma(q[0], VT(d, I, J0) + VT(d, I + 1, J0) - VT(d, I, J1) - VT(d, I + 1, J1), q[per]);
   double ca = 0.0, drd1 = 0.0, dpd1 = 0.0;
   if (I >= 2) {
-    const double R = RLZ(I);
-    if (J >= 2) {  // DRIFTP E x B, EIR and corotation terms
-      const double P1 = DTs / DPHI / 2 / MDR / R;
-      ca = ((VT(I + 1, J) + VT(I + 1, J1) - VT(I - 1, J) - VT(I - 1, J1)) * P1
-            - (EIR(I, J1) + EIR(I, J)) / R * DTs / DPHI) / (BNES(I, J) + BNES(I, J1))
-           + kOME * DTs / DPHI;
-    }
-    drd1 = (EIP(I, J) * R - (VT(I, J1) - VT(I, J0)) / 2. / DPHI) / BNES(I, J);
-    dpd1 = kOME * R + ((VT(I + 1, J) - VT(I - 1, J)) / 2 / MDR - EIR(I, J)) / BNES(I, J);
+    if (J >= 2) ca = fma(q[2 * per], VT(d, I + 1, J) + VT(d, I + 1, J1) - VT(d, I - 1, J) - VT(d, I - 1, J1), q[3 * per]);
+    drd1 = fma(q[4 * per], VT(d, I, J1) - VT(d, I, J0), q[5 * per]);
+    dpd1 = fma(q[6 * per], VT(d, I + 1, J) - VT(d, I - 1, J), q[7 * per]);
   }
   d.ca[t] = ca;
   d.drd1[t] = drd1;
   d.dpd1[t] = dpd1;
-#undef VT
 }
 
-// Per (member, I, J, L): UE and UM from the (I,J) factors, two fmas each.
-__global__ void k_member_ijl(Dev d) {
-  const long long per = (long long)d.nr * d.nt * d.npa;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)d.nm * per) return;
-  const int m = (int)(t / per);
-  const long long c = t % per;
-  const int i = (int)(c % d.nr);
-  const long long ij = (long long)m * d.nr * d.nt + (c % ((long long)d.nr * d.nt));
-  double ue = 0.0, um = 0.0;
-  if (i >= 1) {
-    const double drd1 = d.drd1[ij], dpd1 = d.dpd1[ij];
-    ue = d.gre[c] * drd1 + d.gpe[c] * dpd1 + d.ze[c];
-    um = -d.cmudot[c] * (d.gmr[c] * drd1 + d.gmp[c] * dpd1 + d.zm[c]);
-  }
-  d.ue[t] = ue;
-  d.um[t] = um;
-}
-
-void launch_member_coef(const Dev& d, double dts, cudaStream_t st) {
-  long long nv = (long long)d.nm * d.nf * d.nt;
-  k_vt<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(d);
-  long long nij = (long long)d.nm * d.nr * d.nt;
-  k_member_ij<<<(unsigned)((nij + 127) / 128), 128, 0, st>>>(d, dts);
-  long long n = (long long)d.nm * d.nr * d.nt * d.npa;
-  k_member_ijl<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
-}
-
-// ---------------------------------------------------- DRIFTR ghost planes
-// Plane p = (K-1)*NPA + (L-1) in the reference's K->L loop order.  One warp
-// per plane: lanes test 32 lines J at a time from the top, a ballot finds
-// the highest inflow J.
-__global__ void k_ghost_planes(Dev d) {
+// DRIFTR ghost planes.  Plane p = (K-1)*NPA + (L-1) in the reference's
+// K->L loop order.  One warp per plane: lanes test 32 lines J at a time
+// from the top, a ballot finds the highest inflow J.
+__device__ __forceinline__ void ghost_plane(const Dev& d, int it, int p) {
   const int np = d.ne * d.npa;
   const int lane = threadIdx.x & 31;
-  const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int2 item = d.items[blockIdx.y];
+  const int2 item = d.items[it];
   const int m = item.x, s = item.y, slot = m * d.ns + s;
   if (p >= np) return;  // uniform per warp
   const int k = p / d.npa, l = p % d.npa;
@@ -373,6 +387,44 @@ __global__ void k_ghost_planes(Dev d) {
     d.plane_last[(long long)slot * np + p] = v;
     d.plane_last_src[(long long)slot * np + p] = src;
   }
+}
+
+// Per (member, I, J, L): UE and UM from the (I,J) factors; the blocks past
+// nb_ijl find the ghost planes of every work item (4 planes per block).
+__global__ void __launch_bounds__(128) k_member_ijl(Dev d, int nb_ijl) {
+  if ((int)blockIdx.x >= nb_ijl) {
+    const int np = d.ne * d.npa, bpi = (np + 3) / 4;
+    const int b = (int)blockIdx.x - nb_ijl;
+    ghost_plane(d, b / bpi, (b % bpi) * 4 + (threadIdx.x >> 5));
+    return;
+  }
+  const long long per = (long long)d.nr * d.nt * d.npa;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)d.nm * per) return;
+  const int m = (int)(t / per);
+  const long long c = t % per;
+  const int i = (int)(c % d.nr);
+  const long long ij = (long long)m * d.nr * d.nt + (c % ((long long)d.nr * d.nt));
+  double ue = 0.0, um = 0.0;
+  if (i >= 1) {
+    const double drd1 = d.drd1[ij], dpd1 = d.dpd1[ij];
+    ue = d.gre[c] * drd1 + d.gpe[c] * dpd1 + d.ze[c];
+    um = -d.cmudot[c] * (d.gmr[c] * drd1 + d.gmp[c] * dpd1 + d.zm[c]);
+  }
+  d.ue[t] = ue;
+  d.um[t] = um;
+}
+
+// Two launches: the (I,J) terms, then the (I,J,L) terms with the ghost
+// planes alongside (launch_ghost then scans the planes).
+void launch_member_coef(const Dev& d, double dts, cudaStream_t st) {
+  (void)dts;  // DTs enters through k_dts_ij
+  const int nij = d.nm * d.nr * d.nt;
+  k_member_ij<<<(nij + 127) / 128, 128, 0, st>>>(d);
+  const long long n = (long long)d.nm * d.nr * d.nt * d.npa;
+  const int nb_ijl = (int)((n + 127) / 128);
+  const int nb_ghost = ((d.ne * d.npa + 3) / 4) * d.nitems;
+  k_member_ijl<<<(unsigned)(nb_ijl + nb_ghost), 128, 0, st>>>(d, nb_ijl);
 }
 
 // Exclusive "last defined" scan over planes: one block per work item.
@@ -439,11 +491,8 @@ __global__ void __launch_bounds__(1024) k_ghost_scan(Dev d) {
   }
 }
 
-void launch_ghost(const Dev& d, cudaStream_t st) {
-  const int np = d.ne * d.npa;
-  k_ghost_planes<<<dim3((np + 3) / 4, d.nitems), 128, 0, st>>>(d);
-  k_ghost_scan<<<d.nitems, 1024, 0, st>>>(d);
-}
+// The planes themselves are found in launch_member_coef's second kernel.
+void launch_ghost(const Dev& d, cudaStream_t st) { k_ghost_scan<<<d.nitems, 1024, 0, st>>>(d); }
 
 // -------------------------------------------------- loss factor (bookkeeping path)
 __global__ void k_loss_apply(Dev d, const double* __restrict__ table) {
@@ -483,10 +532,13 @@ void launch_finish(const Dev& d, cudaStream_t st) {
 
 // ---------------------------------------------------------- ANISCH moments
 // Stage 1: one thread per (I>=2, J, K>=2, L-chunk): the L=1 side effect
-// (chunk 0) and partial pitch-angle sums SUME(K), SUMA(K) over L in the
-// chunk (src/ModRamRun.f90:366-378).  Partials (slot, chunk, K, J, I, 2).
+// F2(S,I,J,K,1) = F2(S,I,J,K,2) (chunk 0; src/ModRamRun.f90:366) and the
+// chunk's share of both weighted pitch-angle sums, L = 1..int(UPA(I)-1)
+// split into kMomChunks equal runs.  Partials: (slot, J, I, Q) pairs of
+// doubles, Q = (K-2)*kMomChunks + chunk, so each (I,J) owns one contiguous
+// run for stage 2.
 constexpr int kMomChunks = 4;
-__global__ void k_moments_part(Dev d) {
+__global__ void __launch_bounds__(128) k_moments_part(Dev d) {
   const int nr1 = d.nr - 1, ne1 = d.ne - 1;
   const long long n = (long long)nr1 * d.nt * ne1 * kMomChunks;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -500,79 +552,57 @@ __global__ void k_moments_part(Dev d) {
   const long long st = (long long)d.ne * d.nt * d.nr;
   const long long off = ((long long)k * d.nt + j) * d.nr + i;
   double* f = d.f2 + (long long)slot * d.ncell + off;
-  const double* we = d.epme + (long long)s * d.ncell + off;
-  const double* wa = d.epma + (long long)s * d.ncell + off;
+  const long long sa = (long long)d.ne * d.nr, sb = (long long)d.nt * d.nr;  // L strides
+  const double* __restrict__ wa = d.mw_a + (long long)s * d.npa * sa + (long long)k * d.nr + i;
+  const double* __restrict__ be = d.mw_be + (long long)j * d.nr + i;
+  const double* __restrict__ ba = d.mw_ba + (long long)j * d.nr + i;
   const double f2 = f[st];
-  if (ch == 0) f[0] = f2;  // F2(S,I,J,K,1) = F2(S,I,J,K,2)
+  if (ch == 0) f[0] = f2;
   const int u = d.upa_mom[i];
-  const int cl = (d.npa + kMomChunks - 1) / kMomChunks;
+  const int cl = (u + kMomChunks - 1) / kMomChunks;
   const int l0 = 1 + ch * cl, l1 = min(u, (ch + 1) * cl);
   double sume = 0.0, suma = 0.0;
+#pragma unroll 4
   for (int L = l0; L <= l1; ++L) {
     const double v = (L == 1) ? f2 : f[(long long)(L - 1) * st];
-    sume = fma(v, we[(long long)(L - 1) * st], sume);
-    suma = fma(v, wa[(long long)(L - 1) * st], suma);
+    const double g = v * wa[(long long)(L - 1) * sa];
+    sume = fma(g, be[(long long)(L - 1) * sb], sume);
+    suma = fma(g, ba[(long long)(L - 1) * sb], suma);
   }
-  double* part = d.mom_part + (long long)slot * kMomChunks * d.nr * d.nt * d.ne * 2;
-  const long long pi = ((((long long)ch * d.ne + k) * d.nt + j) * d.nr + i) * 2;
-  part[pi] = sume;
-  part[pi + 1] = suma;
+  const int nq = ne1 * kMomChunks;
+  double2* part = reinterpret_cast<double2*>(d.mom_part) +
+                  (((long long)slot * d.nt + j) * d.nr + i) * nq + (k - 1) * kMomChunks + ch;
+  *part = make_double2(sume, suma);
 }
 
-// Stage 2: one warp per (I>=2, J).  Lanes combine the chunk partials of 32
-// energies at a time; lane 0 then adds them in the reference's band order
-// (khi = 6,10,25,30,NE) with the RFAC factors.
-__global__ void k_moments_reduce(Dev d) {
+// Stage 2: one warp per (I>=2, J): lanes sum strided runs of the (I,J)'s
+// partials, then an xor butterfly (every lane ends with the same sums).
+__global__ void __launch_bounds__(128) k_moments_reduce(Dev d) {
   const int nr1 = d.nr - 1;
   const int lane = threadIdx.x & 31;
-  const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (t >= nr1 * d.nt) return;  // uniform per warp
+  const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (w >= nr1 * d.nt) return;  // uniform per warp
   const int2 item = d.items[blockIdx.y];
-  const int s = item.y, slot = item.x * d.ns + s;
-  const int i = 1 + t % nr1, j = t / nr1;
-  const double cv = kCS * 100;
-  const double RFAC = 4 * kPI / cv;
-  const long long cstride = (long long)d.nr * d.nt * d.ne * 2;
-  const double* part = d.mom_part + (long long)slot * kMomChunks * cstride;
-  const double* epp = d.epp + s * d.ne;
-  int khi[5] = {6, 10, 25, 30, 35};
-  khi[4] = d.ne;
-  int iwa = 0;
-  double PPER = 0., PPAR = 0., ppert = 0., ppart = 0.;
-  for (int base = 2; base <= d.ne; base += 32) {
-    const int K = base + lane;
-    double pe = 0.0, pa = 0.0;
-    if (K <= d.ne) {
-      const long long pi = (((long long)(K - 1) * d.nt + j) * d.nr + i) * 2;
-      double sume = 0.0, suma = 0.0;
-      for (int c = 0; c < kMomChunks; ++c) {
-        sume += part[c * cstride + pi];
-        suma += part[c * cstride + pi + 1];
-      }
-      pe = epp[K - 1] * sume;
-      pa = epp[K - 1] * suma;
-    }
-    const int kmax = min(32, d.ne - base + 1);
-    for (int q = 0; q < kmax; ++q) {
-      const double ve = __shfl_sync(0xffffffffu, pe, q);
-      const double va = __shfl_sync(0xffffffffu, pa, q);
-      PPER = PPER + ve;
-      PPAR = PPAR + va;
-      if (base + q == khi[iwa]) {  // close the band
-        PPAR = 2 * RFAC * PPAR;
-        PPER = RFAC * PPER;
-        ppert = ppert + PPER;
-        ppart = ppart + PPAR;
-        PPER = 0.;
-        PPAR = 0.;
-        iwa = min(iwa + 1, 4);
-      }
-    }
+  const int slot = item.x * d.ns + item.y;
+  const int i = 1 + w % nr1, j = w / nr1;
+  const int nq = (d.ne - 1) * kMomChunks;
+  const double2* __restrict__ p =
+      reinterpret_cast<const double2*>(d.mom_part) + (((long long)slot * d.nt + j) * d.nr + i) * nq;
+  double e = 0.0, a = 0.0;
+  for (int q = lane; q < nq; q += 32) {
+    const double2 v = p[q];
+    e += v.x;
+    a += v.y;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    e += __shfl_xor_sync(0xffffffffu, e, o);
+    a += __shfl_xor_sync(0xffffffffu, a, o);
   }
   if (lane == 0) {
     const long long o = (long long)slot * d.nr * d.nt + (long long)j * d.nr + i;
-    d.ppert[o] = ppert;
-    d.ppart[o] = ppart;
+    d.ppert[o] = e;
+    d.ppart[o] = a;
   }
 }
 

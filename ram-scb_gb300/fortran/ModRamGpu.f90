@@ -212,6 +212,23 @@ module ModRamGpu
        type(c_ptr), value :: ctx
        real(c_double), value :: dts
      end function
+     ! f2, ppert, ppart: arrays of NS*n_members c_ptr (c_loc of each item's
+     ! F2(S,:,:,:,:) copy and (NR,NT) moments; c_null_ptr to skip an entry;
+     ! ppert/ppart may be c_null_ptr as a whole)
+     integer(c_int) function ramgpu_ram_run_host(ctx, dts, f2, ppert, ppart) &
+          bind(C, name="ramgpu_ram_run_host")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), value :: dts
+       type(c_ptr), intent(in) :: f2(*)
+       type(c_ptr), value :: ppert, ppart
+     end function
+     integer(c_int) function ramgpu_set_pipeline_groups(ctx, groups) &
+          bind(C, name="ramgpu_set_pipeline_groups")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: groups
+     end function
      integer(c_int) function ramgpu_synchronize(ctx) bind(C, name="ramgpu_synchronize")
        import :: c_int, c_ptr
        type(c_ptr), value :: ctx

@@ -37,7 +37,7 @@ EXPORTS = (
     "ramgpu_fly_sats", "ramgpu_sum_pressure", "ramgpu_adj_replay", "ramgpu_set_pa_diffusion",
     "ramgpu_loss_wae", "ramgpu_bounce_integrals", "ramgpu_upload_f2_async", "ramgpu_download_f2_async",
     "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store", "ramgpu_compute_hI",
-    "ramgpu_get_fields",
+    "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_set_pipeline_groups",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
@@ -148,6 +148,8 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_compute_hI": ([vp, i, dp, dp, dp, dp, dp, dp, i, dp, dp, d, d], i),
         "ramgpu_get_fields": ([vp] + [dp] * 11, i),
         "ramgpu_sum_pressure": ([vp, i, dp, dp], i),
+        "ramgpu_ram_run_host": ([vp, d, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)], i),
+        "ramgpu_set_pipeline_groups": ([vp, i], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -294,6 +296,40 @@ class RamGpu:
 
     def ram_run_async(self, dts: float):
         self._ck(self.lib.ramgpu_ram_run_async(self.h, float(dts)), "ram_run_async")
+
+    def ram_run_host(self, dts: float, f2, ppert=None, ppart=None):
+        """One ram_run call with F2 on the host (ramgpu_ram_run_host): f2[slot]
+        (slot = member*NS + species; None = stays resident) is uploaded,
+        advanced and written back in place; ppert/ppart[slot], when given,
+        receive the moments.  Buffers: float64, contiguous, writable, NCELL
+        (resp. NR*NT) values in the layout of upload_f2 / moments."""
+        g = self.grid
+        nslot = self.n_members * self.ns
+
+        def table(seq, n, what):
+            if seq is None:
+                return None
+            seq = list(seq)
+            if len(seq) != nslot:
+                raise RamGpuError(f"{what}: need {nslot} entries (member*NS + species)")
+            ptrs = (_P * nslot)()
+            for k, a in enumerate(seq):
+                if a is None:
+                    continue
+                if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.size == n
+                        and a.flags.writeable and (a.flags.f_contiguous or a.flags.c_contiguous)):
+                    raise RamGpuError(f"{what}[{k}]: need a contiguous writable float64 array of {n} values")
+                ptrs[k] = a.ctypes.data_as(_P)
+            return ptrs
+
+        ncell = g.nr * g.nt * g.ne * g.npa
+        t_f2 = table(f2, ncell, "f2")
+        t_pe = table(ppert, g.nr * g.nt, "ppert")
+        t_pa = table(ppart, g.nr * g.nt, "ppart")
+        self._ck(self.lib.ramgpu_ram_run_host(self.h, float(dts), t_f2, t_pe, t_pa), "ram_run_host")
+
+    def set_pipeline_groups(self, groups: int):
+        self._ck(self.lib.ramgpu_set_pipeline_groups(self.h, int(groups)), "set_pipeline_groups")
 
     def half_step(self, dts: float, order: int):
         self._ck(self.lib.ramgpu_half_step(self.h, float(dts), int(order)), "half_step")

@@ -542,6 +542,8 @@ def make_workload(name: str, seed: int = 2024) -> Workload:
       tiny       : four species on a reduced 6x9x35x72 grid (tests)
       tiny_pert  : tiny with perturbed_fields (non-dipole, E_ind, dB/dt,
                    magnetopause cells) for coverage of the zero-in-dipole terms
+      tiny_pert8 : tiny_pert on an 8x9x35x72 grid (NR a multiple of 4: the
+                   DRIFTR lines own whole 32-byte sectors)
     """
     if name == "single_h":
         sp = [HYDROGEN]
@@ -549,10 +551,12 @@ def make_workload(name: str, seed: int = 2024) -> Workload:
         params = [(5.0, 1.0)]
         kp = lambda step: 3.0  # noqa: E731
         dts, steps = 5.0, 720
-    elif name in ("four_sp", "tiny", "tiny_pert"):
+    elif name in ("four_sp", "tiny", "tiny_pert", "tiny_pert8"):
         sp = [SPECIES[c] for c, _, _ in FOUR_SPECIES]
         if name in ("tiny", "tiny_pert"):
             g = arrays(6, 9, 35, 72, species=tuple(sp), mu_grid_nr=20)
+        elif name == "tiny_pert8":
+            g = arrays(8, 9, 35, 72, species=tuple(sp), mu_grid_nr=20)
         else:
             g = arrays(20, 25, 35, 72, species=tuple(sp))
         params = [(kt, sh) for _, kt, sh in FOUR_SPECIES]
@@ -568,7 +572,7 @@ def make_workload(name: str, seed: int = 2024) -> Workload:
         dts = 2.5
     else:
         raise ValueError(f"unknown workload {name!r}")
-    fl = perturbed_fields(g, seed=seed) if name == "tiny_pert" else dipole_fields(g, seed=seed)
+    fl = perturbed_fields(g, seed=seed) if name in ("tiny_pert", "tiny_pert8") else dipole_fields(g, seed=seed)
     f2 = [initial_f2(g, fl, s, seed=seed + 17 * (s + 1), kt=params[s][0], density_scale=params[s][1])
           for s in range(len(sp))]
     fg = [boundary_fgeos(g, s, kt=params[s][0], density_scale=params[s][1]) for s in range(len(sp))]

@@ -202,12 +202,14 @@ def test_batched_gradients_equal_solo(tiny):
         solo.close()
 
 
-def test_gradient_matches_cpu_adjoint():
+@pytest.mark.parametrize("name", ["tiny_pert", "tiny_pert8"])
+def test_gradient_matches_cpu_adjoint(name):
     """GPU adjoint vs the oracle's scalar C adjoint on a non-dipole grid with
     magnetopause-outside cells and stale DRIFTR ghosts: same J, same branch
-    records, same gradients."""
+    records, same gradients (NR = 6, and NR = 8 where the transposed DRIFTR
+    reads lambda through the read-only path)."""
     import pyoracle
-    wl = W.make_workload("tiny_pert")
+    wl = W.make_workload(name)
     g = wl.grid
     ns = len(g.species)
     rng = np.random.Generator(np.random.PCG64(41))
