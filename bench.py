@@ -37,9 +37,9 @@ UNIT = "cell-updates/s"
 # and reverse launches on the four-species standard grid (the forward E and
 # MU carry the CFL quotient's multiply; DRIFTE's forward computes and stores
 # its face coefficients, the reverse loads them).  Per face this is the
-# formulation's own count: X, beta*X, coefficient, a-term, face fma, flux
-# and the two update operations.
-FP64_OPS_PER_CELL = {"driftr": 8.18, "driftp": 7.53, "drifte": 0.5 * (9.58 + 5.78), "driftmu": 0.5 * (9.23 + 7.37)}
+# formulation's own count: X, coefficient, a-term, face fma, flux and the
+# two update operations (beta*|X| is formed on the integer pipe).
+FP64_OPS_PER_CELL = {"driftr": 0.5 * (7.12 + 7.07), "driftp": 6.43, "drifte": 0.5 * (8.58 + 4.78), "driftmu": 0.5 * (8.31 + 6.44)}
 # DRAM bytes (read + write) per launch of each sweep on the four-species
 # standard grid, the mean of its forward and reverse launches in one ncu
 # capture (profiles/sweeps_four_sp.md, current kernels): F2 is read once

@@ -135,9 +135,37 @@ __device__ __forceinline__ double bitsd(bits64 u) {
   asm("mov.b64 %0, %1;" : "=d"(x) : "l"(u));
   return x;
 }
-// beta*|x| as bits (beta > 0): the sign bit of beta*x cleared on the
-// integer pipe; IEEE rounding is symmetric, so this equals beta*fabs(x).
-__device__ __forceinline__ bits64 babs_bits(double beta, double x) { return dbits(beta * x) & kAbsMask; }
+constexpr bits64 kMantMask = 0x000FFFFFFFFFFFFFULL;
+constexpr bits64 kImplicit = 0x0010000000000000ULL;
+// The limiter's beta (1 <= beta <= 2, as the ABI clamps it): its 53-bit
+// significand shifted left by 11, and its unbiased exponent (0, or 1 for 2).
+struct BetaBits {
+  double beta;
+  bits64 m11;
+  int e;
+  __device__ __forceinline__ explicit BetaBits(double b) : beta(b) {
+    const bits64 u = dbits(b);
+    m11 = ((u & kMantMask) | kImplicit) << 11;
+    e = (int)(u >> 52) - 1023;
+  }
+};
+// beta*|x| as bits, formed on the integer pipe: the product of the two
+// significands by a 64x64-bit high multiply, truncated to 53 bits (at most
+// one unit in the last place below the rounded FP64 product; the limiter
+// compares these bits and, in its beta branches, uses them as the value).
+// Subnormal and zero |x| give the subnormal-range product the same way;
+// inf and NaN pass through.  Replaces one FP64 multiply per face.
+__device__ __forceinline__ bits64 babs_bits(const BetaBits& b, double x) {
+  const bits64 ax = dbits(x) & kAbsMask;
+  const int ex = (int)(ax >> 52);
+  const bits64 mant = ax & kMantMask;
+  const bits64 mx = ex ? (mant | kImplicit) : mant;
+  const bits64 p = __umul64hi(mx << 11, b.m11);  // floor(mx*mb / 2^42)
+  const int hi = (int)(p >> 63);                  // normal |x|: p in [2^62, 2^64)
+  const bits64 normal = ((bits64)(ex + b.e + hi) << 52) | ((p >> (10 + hi)) & kMantMask);
+  const bits64 sub = (p >> 10) << b.e;            // floor(mant*beta) < 2^53: its own encoding
+  return ex == 0x7FF ? ax : (ex ? normal : sub);
+}
 // x < 0.0 exactly as the Fortran test `C.lt.0` (false for -0.0 and NaN with
 // the sign bit clear).
 __device__ __forceinline__ bool is_neg(double x) { return dbits(x) > 0x8000000000000000ULL; }
@@ -192,11 +220,14 @@ __device__ __forceinline__ double* coef_ptr(const Dev& d, int w, int q, long lon
 }
 
 // Face value with the branch taken from a record (frozen-limiter replay):
-// LIMITER*X = beta*D | X | D | beta*X for cases 1..4, FUP for case 0.  For
-// the recorded branch this equals face_value_case bit for bit.
-__device__ __forceinline__ double face_value_frozen(double x, double d, double fup, double a, double beta,
+// LIMITER*X = beta*D | X | D | beta*X for cases 1..4, FUP for case 0, the
+// beta products formed as in face_value_case.  For the recorded branch this
+// equals face_value_case bit for bit.
+__device__ __forceinline__ double face_value_frozen(double x, double d, double fup, double a, const BetaBits& beta,
                                                     int cs) {
-  const double lx = cs == 1 ? beta * d : cs == 2 ? x : cs == 3 ? d : beta * x;
+  const double bd = bitsd(babs_bits(beta, d) | (dbits(d) & kSignMask));
+  const double bx = bitsd(babs_bits(beta, x) | (dbits(x) & kSignMask));
+  const double lx = cs == 1 ? bd : cs == 2 ? x : cs == 3 ? d : bx;
   return cs ? fma(a, lx, fup) : fup;
 }
 // F2 < 0 -> 1e-15 applied as recorded

@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
       const double* __restrict__ cr = d.cr + ((long long)m * nt + j) * nr;
       const int* __restrict__ outside = d.outside + (long long)j * nr;
       const double p4 = d.p4[s * ne + (line / nt) % ne];
-      const double beta = d.betalim;
+      const BetaBits beta(d.betalim);
       const bool closed = d.flags & 1u;
 
       const int k = (line / nt) % ne;
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
       const double* __restrict__ ca = d.ca + ((long long)m * nt) * nr + i;
       const int* __restrict__ outside = d.outside + i;
       const double p2 = d.p2[((long long)s * ne + k) * nr + i];
-      const double beta = d.betalim;
+      const BetaBits beta(d.betalim);
   #define GJ(J) fl[(long long)((J)-1) * st]
   #define CJ(J) fma(gpt[(long long)((J)-1) * nr], p2, ca[(long long)((J)-1) * nr])
       const double G1 = GJ(1), G2 = GJ(2), G3 = GJ(3), GNm = GJ(nt - 1), GN = GJ(nt);
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
       const double* __restrict__ mhde = d.mhde;
       const double* __restrict__ iwe = d.iwe;
       const bool inside = d.outside[(long long)j * nr + i] == 0;
-      const double beta = d.betalim;
+      const BetaBits beta(d.betalim);
       const bool closed = d.flags & 1u;
   #define GK(K) fl[(long long)((K)-1) * st]
   #define CK(K) (edot[(long long)((K)-1) * nr] * fma(eb[(K)-1], wet, ue))
@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
       const double* __restrict__ mhdmu = d.mhdmu;
       const double* __restrict__ iwmu = d.iwmu;
       const bool inside = d.outside[fij] == 0;
-      const double beta = d.betalim;
+      const BetaBits beta(d.betalim);
       const bool closed = d.flags & 1u;
   #define GL(L) fl[(long long)((L)-1) * st]
   #define LA(L) la[(long long)((L)-1) * st]
