@@ -367,6 +367,8 @@ def run_adjoint(args, torch, dev, stream):
     reset()
     gpu.adj_forward(2, wl.dts, kp[:2], 1, [])  # warm-up of the adjoint buffers and kernels
     gpu.adj_backward()
+    # the library's policy: checkpoints every kc calls, the record ring keeps
+    # as many trailing segments as half of the free HBM holds (here all)
     reset()
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -374,14 +376,24 @@ def run_adjoint(args, torch, dev, stream):
     t1 = time.perf_counter()
     gf, gb = gpu.adj_backward()
     t2 = time.perf_counter()
-    # the same window with every call's record kept (one segment: no recompute)
+    nseg, nkeep = gpu.adj_segments()
+    # the same window with a one-segment ring: every earlier segment is
+    # recomputed from its checkpoint (the policy for windows that do not fit)
+    gpu.set_adj_record_budget(0)
     reset()
     torch.cuda.synchronize(dev)
     t3 = time.perf_counter()
-    gpu.adj_forward(nc, wl.dts, kp, nc, obs)
+    gpu.adj_forward(nc, wl.dts, kp, kc, obs)
     t4 = time.perf_counter()
-    gf2, gb2 = gpu.adj_backward()
+    gfr, gbr = gpu.adj_backward()
     t5 = time.perf_counter()
+    gpu.set_adj_record_budget(-1)
+    same_r = max(float(np.max(np.abs(gfr - gf)) / np.max(np.abs(gf))),
+                 float(np.max(np.abs(gbr - gb)) / max(np.max(np.abs(gb)), 1e-300)))
+    # and as one segment (k = ncalls): the record of every call, no checkpoints
+    reset()
+    gpu.adj_forward(nc, wl.dts, kp, nc, obs)
+    gf2, gb2 = gpu.adj_backward()
     same = max(float(np.max(np.abs(gf2 - gf)) / np.max(np.abs(gf))),
                float(np.max(np.abs(gb2 - gb)) / max(np.max(np.abs(gb)), 1e-300)))
     rng = np.random.Generator(np.random.PCG64(707))
@@ -416,14 +428,18 @@ def run_adjoint(args, torch, dev, stream):
     out = {"window_calls": nc, "window_dts_steps": 2 * nc, "checkpoint_calls": kc, "observations": len(obs),
            "J": J, "forward_s": fwd_s, "adj_forward_s": t1 - t0, "adj_backward_s": t2 - t1,
            "adjoint_over_forward": (t2 - t0) / fwd_s,
-           "full_record": {"adj_forward_s": t4 - t3, "adj_backward_s": t5 - t4,
-                           "adjoint_over_forward": (t5 - t3) / fwd_s,
-                           "record_bytes": 8 * g.ncell * ns * nc,
-                           "gradient_vs_checkpointed_max_rel_diff": same},
+           "segments": nseg, "segments_kept": nkeep, "record_bytes": 8 * g.ncell * ns * nc,
+           "policy": "checkpoints every checkpoint_calls calls; the branch-record ring keeps the last "
+                     "segments_kept segments (half of the free HBM as budget) and recomputes the rest",
+           "recompute": {"segments_kept": 1, "segments_recomputed": nseg - 1,
+                         "adj_forward_s": t4 - t3, "adj_backward_s": t5 - t4,
+                         "adjoint_over_forward": (t5 - t3) / fwd_s,
+                         "gradient_vs_kept_max_rel_diff": same_r},
+           "single_segment_gradient_max_rel_diff": same,
            "fd_frozen_directions": len(fd), "fd_frozen_max_rel_err": max(fd) if fd else None,
            "fd_frozen_eps": "Richardson of 1e-5 and 2e-5", "fd_unfrozen_rel_err": unfrozen,
            "forward": "graph-replayed ram_run per call",
-           "adjoint": "recording forward with checkpoints + segment recompute + transposed sweeps"}
+           "adjoint": "recording forward with checkpoints + recompute of the segments not kept + transposed sweeps"}
     if args.adj_members > 0:
         out["batched"] = run_adjoint_batched(args, torch, dev, stream)
     return out

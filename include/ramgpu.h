@@ -357,35 +357,45 @@ typedef struct {
  * J[n_members] and leaves F2 at the end of the window (the moments are
  * those of the window's last call).  Every limiter branch
  * and clip is recorded; ramgpu_adj_digest returns a digest of the pattern.
- * Allocates its checkpoint and record buffers (k_ckpt*8 bytes per cell and
- * item for the record). */
+ * Allocates its checkpoint buffer and a ring of branch records (8 bytes per
+ * cell, item and call) that keeps the last nkeep checkpoint segments, as
+ * many as the record budget allows (ramgpu_set_adj_record_budget; at least
+ * one segment). */
 int ramgpu_adj_forward(ramgpu_ctx *ctx, int ncalls, double dts, const double *kp, int k_ckpt,
                        const ramgpu_obs *obs, int nobs, double *J);
 /* Backward pass: gradients of J with respect to the window's initial F2
  * (grad_f2: n_members*ns*NR*NT*NE*NPA, per (member, s) the Fortran-order
  * F2(S,:,:,:,:)) and to FGEOS (grad_fgeos: n_members*ns*NT*NE*NPA), with the
- * limiter branches frozen as recorded.  Each checkpoint segment but the
- * last (whose record the forward pass kept) is recomputed from its
- * checkpoint with recording, then transposed call by call; with k_ckpt >=
- * ncalls nothing is recomputed.  Either
+ * limiter branches frozen as recorded.  Each checkpoint segment before the
+ * kept ones is recomputed from its checkpoint with recording, then every
+ * call is transposed in reverse order; when the ring keeps every segment
+ * (or k_ckpt >= ncalls) nothing is recomputed.  Either
  * output may be NULL; both may be host or device memory.  On return F2 is
  * the window's initial state again. */
 int ramgpu_adj_backward(ramgpu_ctx *ctx, double *grad_f2, double *grad_fgeos);
+/* Device bytes the adjoint's branch-record ring may take: bytes < 0 (the
+ * default) means half of the free device memory when ramgpu_adj_forward
+ * starts; a budget below one segment keeps one segment, so every earlier
+ * segment is recomputed from its checkpoint. */
+int ramgpu_set_adj_record_budget(ramgpu_ctx *ctx, long long bytes);
+/* Checkpoint segments of the last ramgpu_adj_forward and how many of them
+ * (the last ones) the record ring keeps. */
+int ramgpu_adj_segments(ramgpu_ctx *ctx, int *nseg, int *nkeep);
 /* Digest of every branch recorded by the last ramgpu_adj_forward: equal
  * digests mean the same frozen-limiter pattern. */
 int ramgpu_adj_digest(ramgpu_ctx *ctx, unsigned long long *digest);
-/* Copy of the branch record of one call of the last checkpoint segment of
+/* Copy of the branch record of one call of a kept checkpoint segment of
  * the last ramgpu_adj_forward: 8 sweeps (R,P,E,MU,MU,E,P,R) x active items x
  * NR*NT*NE*NPA bytes, per face the limiter case (bits 0-2: 0 upwind only,
  * 1 beta*D, 2 X, 3 D, 4 beta*X) and bit 3 set when the updated cell was
  * clipped (diagnostics).  Available until a ramgpu_adj_backward that had to
- * recompute earlier segments (more than one segment) replaces it. */
+ * recompute earlier segments replaces it. */
 int ramgpu_adj_record(ramgpu_ctx *ctx, int call, unsigned char *out);
 /* The last window run again from the current F2 with every limiter branch
  * and clip taken from the record (the frozen-limiter scheme that
  * ramgpu_adj_backward differentiates, which is affine in F2 and FGEOS):
  * J[n_members] of that run; F2 ends at the window's end.  Needs every call's
- * record, i.e. ramgpu_adj_forward with k_ckpt >= ncalls.  With the recorded
+ * record: k_ckpt >= ncalls, or a ring that keeps every segment.  With the recorded
  * F2 it reproduces the recorded run bit for bit; it exists to check the
  * adjoint by finite differences on long windows, where unfrozen
  * perturbations cross limiter kinks. */

@@ -87,8 +87,12 @@ struct ramgpu_ctx {
     unsigned char* rec = nullptr;
     unsigned long long* digest = nullptr;
     size_t rec_call = 0;             // bytes of one call's record (8 sweeps)
-    bool rec_stale = false;          // the record ring no longer holds the last segment
+    bool rec_stale = false;          // the record ring no longer holds the kept segments
+    int nkeep = 1;                   // trailing segments whose records the ring keeps
   } adj;
+  // device bytes the adjoint's branch-record ring may use (-1: half of the
+  // free device memory when the window starts)
+  long long adj_record_budget = -1;
   // ramgpu_ram_run_host: item groups, their streams and events, and the
   // graph of the whole pipeline for one set of host buffers
   int pipe_groups = 4;
@@ -402,12 +406,15 @@ static int enqueue_call_rec(ramgpu_ctx* ctx, double dts, unsigned char* rec, boo
   CK(cudaMemsetAsync(rec, 0, 8 * isz, ctx->stream));
   launch_member_coef(ctx->d, dts, ctx->stream);
   launch_ghost(ctx->d, ctx->stream);
+  // DRIFTE keeps its face coefficients for the reverse half as in the plain
+  // step (same DTs and VT within a call)
+  const int co_e = (ctx->d.coef && ctx->d.coef_slot[2] >= 0) ? 1 : 0;
   launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 0 * isz);
   launch_sweep_p(ctx->d, dts, false, ctx->stream, rec + 1 * isz);
-  launch_sweep_e(ctx->d, dts, false, ctx->stream, rec + 2 * isz);
+  launch_sweep_e(ctx->d, dts, false, ctx->stream, rec + 2 * isz, false, co_e);
   launch_sweep_mu(ctx->d, dts, false, 1, ctx->d.loss2, ctx->stream, rec + 3 * isz);
   launch_sweep_mu(ctx->d, dts, false, 0, nullptr, ctx->stream, rec + 4 * isz);
-  launch_sweep_e(ctx->d, dts, false, ctx->stream, rec + 5 * isz);
+  launch_sweep_e(ctx->d, dts, false, ctx->stream, rec + 5 * isz, false, 2 * co_e);
   launch_sweep_p(ctx->d, dts, false, ctx->stream, rec + 6 * isz);
   launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 7 * isz);
   launch_finish(ctx->d, ctx->stream);
@@ -1671,6 +1678,26 @@ int ramgpu_sum_pressure(ramgpu_ctx* ctx, int member, double* pallsum, double* pp
   return RAMGPU_OK;
 }
 
+// Ring position of call c's branch record: segment c/k sits in slot
+// (c/k) mod nkeep, so the last nkeep segments survive the forward pass.
+static size_t adj_rec_slot(const ramgpu_ctx::Adj& a, int c) {
+  return (size_t)((c / a.k) % a.nkeep) * a.k + (size_t)(c % a.k);
+}
+
+int ramgpu_set_adj_record_budget(ramgpu_ctx* ctx, long long bytes) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  ctx->adj_record_budget = bytes < 0 ? -1 : bytes;
+  return RAMGPU_OK;
+}
+
+int ramgpu_adj_segments(ramgpu_ctx* ctx, int* nseg, int* nkeep) {
+  if (check_ctx(ctx) || !nseg || !nkeep) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (!ctx->adj.ready) return fail(ctx, RAMGPU_ERR_STATE, "ramgpu_adj_forward must run first");
+  *nseg = ctx->adj.nseg;
+  *nkeep = ctx->adj.nkeep;
+  return RAMGPU_OK;
+}
+
 int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp, int k_ckpt,
                        const ramgpu_obs* obs, int nobs, double* J) {
   if (check_ctx(ctx) || !kp || (nobs > 0 && !obs)) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
@@ -1715,7 +1742,22 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
   a.rec_call = (size_t)8 * d.nitems * d.ncell;
   const int kseg = k_ckpt < ncalls ? k_ckpt : ncalls;
   bool ok = cudaMalloc(&a.ckpt, sizeof(double) * a.nseg * d.nitems * d.ncell) == cudaSuccess;
-  ok = ok && cudaMalloc(&a.rec, a.rec_call * kseg) == cudaSuccess;
+  // The ring keeps the records of the last nkeep segments, as many as the
+  // budget allows (at least one); only the segments before them are
+  // recomputed from their checkpoints in the backward pass.
+  {
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const long long budget = ctx->adj_record_budget >= 0 ? ctx->adj_record_budget : (long long)(free_b / 2);
+    const long long seg_bytes = (long long)(a.rec_call * kseg);
+    long long nk = budget / seg_bytes;
+    a.nkeep = (int)(nk < 1 ? 1 : (nk > a.nseg ? a.nseg : nk));
+  }
+  if (ok && cudaMalloc(&a.rec, a.rec_call * kseg * a.nkeep) != cudaSuccess) {
+    cudaGetLastError();
+    a.nkeep = 1;
+    ok = cudaMalloc(&a.rec, a.rec_call * kseg) == cudaSuccess;
+  }
   ok = ok && cudaMalloc(&a.obs, sizeof(ObsDev) * (nobs > 0 ? nobs : 1)) == cudaSuccess;
   ok = ok && cudaMalloc(&a.fm, sizeof(double) * (nobs > 0 ? nobs : 1)) == cudaSuccess;
   ok = ok && cudaMalloc(&a.fm2, sizeof(double) * (nobs > 0 ? nobs : 1)) == cudaSuccess;
@@ -1737,7 +1779,7 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
     if (c % k_ckpt == 0)
       if ((rc = adj_copy_items(ctx, a.ckpt + (size_t)(c / k_ckpt) * d.nitems * d.ncell, true))) return rc;
     if ((rc = adj_set_kp(ctx, c))) return rc;
-    unsigned char* r = a.rec + (size_t)(c % k_ckpt) * a.rec_call;
+    unsigned char* r = a.rec + adj_rec_slot(a, c) * a.rec_call;
     if ((rc = enqueue_call_rec(ctx, dts, r, c == ncalls - 1))) return rc;
     launch_digest(r, (long long)a.rec_call, a.digest, ctx->stream);
     launch_obs_fwd(d, a.obs, nobs, c, a.fm, a.J, ctx->stream);
@@ -1767,18 +1809,19 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
   CK(cudaMemsetAsync(d.gfg, 0, sizeof(double) * nslot * nfg, ctx->stream));
   for (int seg = a.nseg - 1; seg >= 0; --seg) {
     const int c0 = seg * a.k, c1 = (c0 + a.k < a.ncalls) ? c0 + a.k : a.ncalls;
-    // The record of the last segment is still the forward pass's own (the
-    // observation values fm are kept from it for every call); earlier
-    // segments are recomputed from their checkpoint, recording branches.
-    if (seg != a.nseg - 1 || a.rec_stale) {
+    // The records of the last nkeep segments are still the forward pass's
+    // own (the observation values fm are kept from it for every call);
+    // earlier segments are recomputed from their checkpoint, recording
+    // branches into their ring slot (whose previous segment is done).
+    if (seg < a.nseg - a.nkeep || a.rec_stale) {
       if ((rc = adj_copy_items(ctx, a.ckpt + (size_t)seg * isz, false))) return rc;
       for (int c = c0; c < c1; ++c) {
         if ((rc = adj_set_kp(ctx, c))) return rc;
-        if ((rc = enqueue_call_rec(ctx, a.dts, a.rec + (size_t)(c - c0) * a.rec_call, false))) return rc;
+        if ((rc = enqueue_call_rec(ctx, a.dts, a.rec + adj_rec_slot(a, c) * a.rec_call, false))) return rc;
       }
     }
     for (int c = c1 - 1; c >= c0; --c) {  // transpose call c
-      const unsigned char* r = a.rec + (size_t)(c - c0) * a.rec_call;
+      const unsigned char* r = a.rec + adj_rec_slot(a, c) * a.rec_call;
       launch_obs_adj(d, a.obs, a.nobs, c, a.fm, ctx->stream);
       if ((rc = adj_set_kp(ctx, c))) return rc;
       launch_member_coef(d, a.dts, ctx->stream);
@@ -1798,7 +1841,7 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
     }
   }
   if ((rc = adj_copy_items(ctx, a.ckpt, false))) return rc;  // F2 back to the initial state
-  a.rec_stale = a.nseg > 1;  // the ring now holds segment 0
+  a.rec_stale = a.nseg > a.nkeep;  // recomputed segments replaced kept ones
   CK(cudaStreamSynchronize(ctx->stream));
   if (grad_f2) CK(cudaMemcpy(grad_f2, d.lam, sizeof(double) * nslot * d.ncell, cudaMemcpyDefault));
   if (grad_fgeos) CK(cudaMemcpy(grad_fgeos, d.gfg, sizeof(double) * nslot * nfg, cudaMemcpyDefault));
@@ -1809,8 +1852,10 @@ int ramgpu_adj_replay(ramgpu_ctx* ctx, double* J) {
   if (check_ctx(ctx) || !J) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
   auto& a = ctx->adj;
   if (!a.ready) return fail(ctx, RAMGPU_ERR_STATE, "ramgpu_adj_forward must run first");
-  if (a.nseg != 1 || a.rec_stale)
-    return fail(ctx, RAMGPU_ERR_STATE, "replay needs every call's record: ramgpu_adj_forward with k_ckpt >= ncalls");
+  if (a.nseg > a.nkeep || a.rec_stale)
+    return fail(ctx, RAMGPU_ERR_STATE,
+                "replay needs every call's record: ramgpu_adj_forward with k_ckpt >= ncalls or a record budget "
+                "that keeps every segment");
   if (ctx->items_dirty || a.items_version != ctx->items_version)
     return fail(ctx, RAMGPU_ERR_STATE, "active members/species changed since ramgpu_adj_forward");
   int rc = prepare(ctx, a.dts);
@@ -1820,7 +1865,7 @@ int ramgpu_adj_replay(ramgpu_ctx* ctx, double* J) {
   CK(cudaMemsetAsync(a.J2, 0, sizeof(double) * nm, ctx->stream));
   for (int c = 0; c < a.ncalls; ++c) {
     if ((rc = adj_set_kp(ctx, c))) return rc;
-    if ((rc = enqueue_call_replay(ctx, a.dts, a.rec + (size_t)c * a.rec_call))) return rc;
+    if ((rc = enqueue_call_replay(ctx, a.dts, a.rec + adj_rec_slot(a, c) * a.rec_call))) return rc;
     launch_obs_fwd(d, a.obs, a.nobs, c, a.fm2, a.J2, ctx->stream);
     ctx->launches += 1;
   }
@@ -1833,12 +1878,12 @@ int ramgpu_adj_record(ramgpu_ctx* ctx, int call, unsigned char* out) {
   if (check_ctx(ctx) || !out) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
   auto& a = ctx->adj;
   if (!a.ready) return fail(ctx, RAMGPU_ERR_STATE, "ramgpu_adj_forward must run first");
-  if (call < 0 || call >= a.ncalls || (a.ncalls > a.k && call / a.k != a.nseg - 1))
-    return fail(ctx, RAMGPU_ERR_ARG, "only calls of the last checkpoint segment are kept");
+  if (call < 0 || call >= a.ncalls || call / a.k < a.nseg - a.nkeep)
+    return fail(ctx, RAMGPU_ERR_ARG, "only calls of the kept checkpoint segments have a record");
   if (a.rec_stale)
     return fail(ctx, RAMGPU_ERR_STATE, "the record was replaced by ramgpu_adj_backward's recomputation");
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaMemcpy(out, a.rec + (size_t)(call % a.k) * a.rec_call, a.rec_call, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(out, a.rec + adj_rec_slot(a, call) * a.rec_call, a.rec_call, cudaMemcpyDeviceToHost));
   return RAMGPU_OK;
 }
 

@@ -30,32 +30,33 @@ namespace ramgpu {
 // registers: after face f, cell f-1 is final and is written out.
 
 // Scatter of one face into the window (cm1, c0, c1, c2) = cells f-1..f+2.
-// FBND(f) = FUP + a LX depends on three adjacent cells: (f-1, f, f+1) when
-// the face is upwinded from the left (C >= 0, FUP = F(f)) and (f, f+1, f+2)
-// from the right (FUP = F(f+1)); in that shifted window its derivatives are
-//   (-ak, 1+ak, 0)  for LX = D from the left or LX = X from the right,
-//   (0, 1-ak, ak)   for LX = X from the left or LX = D from the right,
-//   (0, 1, 0)       upwind only,
-// with ak = a (cases 2, 3) or beta*a (cases 1, 4).  The window and the
-// signed coefficient are picked by integer selects, so a face costs one add
-// and three fma on the FP64 pipe whatever its case.
+// FBND(f) = FUP + a LX depends on adjacent cells only: with C >= 0 (FUP =
+// F(f)) on (f-1, f) for LX = D, (f, f+1) for LX = X; with C < 0 (FUP =
+// F(f+1)) on (f, f+1) for LX = X, (f+1, f+2) for LX = D; its derivatives on
+// that pair are (-ak, 1+ak) when the pair ends at the upwind cell and
+// (1-ak, ak) when it starts there (upwind only: (1, 0)), with ak = a
+// (cases 2, 3) or beta*a (cases 1, 4).  The pair and the signed
+// coefficients are picked by integer selects, so a face costs one add and
+// two fma on the FP64 pipe whatever its case.
 __device__ __forceinline__ void face_acc(double FBb, bool neg, int cs, double ak, double& cm1,
                                          double& c0, double& c1, double& c2) {
   const bool xt = (cs == 2) | (cs == 4);  // LX = X (f, f+1)
   const bool dt = (cs == 1) | (cs == 3);  // LX = D (f-1, f) or (f+1, f+2)
-  const bool left = (dt & !neg) | (xt & neg);
-  const bool right = (xt & !neg) | (dt & neg);
-  const double sak = left ? bitsd(dbits(ak) ^ kSignMask) : (right ? ak : 0.0);
-  const double a0 = left ? sak : 0.0, a2 = right ? sak : 0.0;
-  const double a1 = 1.0 - sak;
-  double t0 = neg ? c0 : cm1, t1 = neg ? c1 : c0, t2 = neg ? c2 : c1;
-  t0 = fma(a0, FBb, t0);
-  t1 = fma(a1, FBb, t1);
-  t2 = fma(a2, FBb, t2);
-  cm1 = neg ? cm1 : t0;
-  c0 = neg ? t0 : t1;
-  c1 = neg ? t1 : t2;
-  c2 = neg ? t2 : c2;
+  const bool ends = (dt & !neg) | (xt & neg);  // pair ends at the upwind cell
+  const bool starts = (xt & !neg) | (dt & neg);
+  const double sak = ends ? bitsd(dbits(ak) ^ kSignMask) : (starts ? ak : 0.0);
+  const double m = 1.0 - sak;
+  const double b0 = ends ? sak : m, b1 = ends ? m : sak;
+  // first cell of the pair in the window: 0 = f-1, 1 = f, 2 = f+1
+  const int p = neg ? (ends ? 1 : 2) : (ends ? 0 : 1);
+  const double p0 = p == 0 ? cm1 : (p == 1 ? c0 : c1);
+  const double p1 = p == 0 ? c0 : (p == 1 ? c1 : c2);
+  const double t0 = fma(b0, FBb, p0);
+  const double t1 = fma(b1, FBb, p1);
+  cm1 = p == 0 ? t0 : cm1;
+  c0 = p == 0 ? t1 : (p == 1 ? t0 : c0);
+  c1 = p == 1 ? t1 : (p == 2 ? t0 : c1);
+  c2 = p == 2 ? t1 : c2;
 }
 
 // ak = LIMITER weight times the CORR factor a = -0.5*(C*q - s) of a face:

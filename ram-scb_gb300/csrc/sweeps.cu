@@ -168,11 +168,16 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
       double phi_prev = phiN;
       double g0 = G2, gp = G3, xm = X1, x = X2;
       bits64 bxm = bX1, bx = bX2;
+      // the cell two faces ahead is loaded one iteration early, before this
+      // face's store: the compiler cannot move a load past a store to the
+      // line at a run-time stride (DRIFTR's contiguous lines come from L1)
+      double nxt = GJ(4);
       for (int J = 2; J <= nt - 1; ++J) {
         double gpp = 0.0, xp;
         bits64 bxp;
+        const double nn = GJ(min(J + 3, nt));
         if (J <= nt - 3) {
-          gpp = GJ(J + 2);
+          gpp = nxt;
           xp = gpp - gp;
           bxp = babs_bits(beta, xp);
         } else if (J == nt - 2) {
@@ -199,6 +204,7 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
         if (kRec == 1) rl[(long long)(J - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         g0 = gp; gp = gpp;
+        nxt = nn;
         xm = x; bxm = bx; x = xp; bx = bxp;
       }
       const double rawN = (GN - phiN) + phi_prev;
@@ -277,8 +283,10 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
       }
       double g0 = G2, gp = G3, xm = X1, x = X2;
       bits64 bxm = bX1, bx = bX2;
+      double nxt = GK(4);  // loaded one iteration ahead, as in DRIFTP
       for (int K = 2; K <= ne; ++K) {
-        const double gpp = (K + 2 <= ne) ? GK(K + 2) : 0.0;
+        const double gpp = (K + 2 <= ne) ? nxt : 0.0;
+        nxt = GK(min(K + 3, ne));
         const double xp = gpp - gp; const bits64 bxp = babs_bits(beta, xp);
         const double c = (kCo == 2) ? cst[(long long)(K - 1) * st] : CK(K);
         if (kCfl && inside) q = umax64(q, dbits(bitsd(cfl_bits(c, kBits1em10)) * d.ide[K - 1]));
@@ -357,8 +365,10 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
       double g0 = G2, gp = G3, xm = X1;
       bits64 bxm = bX1;
       double x = G3 - G2; bits64 bx = babs_bits(beta, x);
+      double nxt = GL(4);  // loaded one iteration ahead, as in DRIFTP
       for (int L = 2; L <= npa - 2; ++L) {
-        double gpp = GL(L + 2);
+        double gpp = nxt;
+        nxt = GL(min(L + 3, npa));
         if (kLoss == 2) gpp *= LA(L + 2);
         const double xp = gpp - gp; const bits64 bxp = babs_bits(beta, xp);
         const double c = (kCo == 2) ? cst[(long long)(L - 1) * st] : CL(L);
@@ -450,6 +460,8 @@ void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigne
   dim3 g = grid_for(d, 2, nlines_of(d, 2));
   const int b = d.blk[2];
   if (rec && replay) k_sweep_e<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec);
+  else if (rec && co == 1) k_sweep_e<false, 1, 1><<<g, b, 0, st>>>(d, dts, rec);
+  else if (rec && co == 2) k_sweep_e<false, 1, 2><<<g, b, 0, st>>>(d, dts, rec);
   else if (rec) k_sweep_e<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec);
   else if (co == 1) k_sweep_e<true, 0, 1><<<g, b, 0, st>>>(d, dts, nullptr);
   else if (co == 2) k_sweep_e<false, 0, 2><<<g, b, 0, st>>>(d, dts, nullptr);

@@ -38,6 +38,7 @@ EXPORTS = (
     "ramgpu_loss_wae", "ramgpu_bounce_integrals", "ramgpu_upload_f2_async", "ramgpu_download_f2_async",
     "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store", "ramgpu_compute_hI",
     "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_set_pipeline_groups",
+    "ramgpu_set_adj_record_budget", "ramgpu_adj_segments",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
@@ -150,6 +151,8 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_sum_pressure": ([vp, i, dp, dp], i),
         "ramgpu_ram_run_host": ([vp, d, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)], i),
         "ramgpu_set_pipeline_groups": ([vp, i], i),
+        "ramgpu_set_adj_record_budget": ([vp, C.c_longlong], i),
+        "ramgpu_adj_segments": ([vp, ip, ip], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -513,6 +516,19 @@ class RamGpu:
         J = np.zeros(self.n_members)
         self._ck(self.lib.ramgpu_adj_replay(self.h, _dptr(J)), "adj_replay")
         return J
+
+    def set_adj_record_budget(self, nbytes: int):
+        """Device bytes the adjoint's branch-record ring may use (< 0: half of
+        the free device memory; small: one segment, every earlier segment is
+        recomputed)."""
+        self._ck(self.lib.ramgpu_set_adj_record_budget(self.h, int(nbytes)), "set_adj_record_budget")
+
+    def adj_segments(self):
+        """(checkpoint segments, segments whose records are kept) of the last
+        adj_forward."""
+        a, b = C.c_int(), C.c_int()
+        self._ck(self.lib.ramgpu_adj_segments(self.h, C.byref(a), C.byref(b)), "adj_segments")
+        return a.value, b.value
 
     def adj_digest(self) -> int:
         v = C.c_ulonglong()

@@ -174,16 +174,44 @@ def test_gradient_finite_differences_fgeos(case):
               False, 6, (1e-4, 1e-5, 1e-6))
 
 
-def test_checkpoint_spacing_invariant(case):
+@pytest.mark.parametrize("k,keep", [(1, 1), (1, 2), (1, 4), (2, 1), (4, 1)])
+def test_checkpoint_spacing_and_record_budget(case, k, keep):
+    """Checkpoints every k calls with a record ring of `keep` segments (the
+    older segments are recomputed from their checkpoints): the same J and
+    gradients as the default (every record kept); records of kept segments
+    are readable, the others are not."""
     wl, model, kp, obs, J0, _, gf, gb = case
-    _set_f2(model, wl, [1.0] * len(wl.grid.species))
-    J1 = model.adj_forward(4, wl.dts, kp, 1, obs)
-    gf1, gb1 = model.adj_backward()
-    assert abs(J1[0] - J0[0]) <= 1e-13 * J0[0]
-    assert np.max(np.abs(gf1 - gf)) <= 1e-12 * np.max(np.abs(gf))
-    assert np.max(np.abs(gb1 - gb)) <= 1e-12 * np.max(np.abs(gb))
-    # after the backward pass F2 is the window's initial state
-    assert np.array_equal(model.download_f2(0, 1), np.asfortranarray(wl.f2[1]))
+    g = wl.grid
+    ns = len(g.species)
+    per_call = 8 * ns * g.nr * g.nt * g.ne * g.npa
+    model.set_adj_record_budget(keep * k * per_call)
+    try:
+        _set_f2(model, wl, [1.0] * ns)
+        J1 = model.adj_forward(NCALLS, wl.dts, kp, k, obs)
+        nseg, nkeep = model.adj_segments()
+        assert nseg == -(-NCALLS // k) and nkeep == min(keep, nseg)
+        for c in range(NCALLS):
+            if c // k >= nseg - nkeep:
+                assert model.adj_record(c, ns).size > 0
+            else:
+                with pytest.raises(abi.RamGpuError):
+                    model.adj_record(c, ns)
+        gf1, gb1 = model.adj_backward()
+        assert abs(J1[0] - J0[0]) <= 1e-13 * J0[0]
+        assert np.max(np.abs(gf1 - gf)) <= 1e-12 * np.max(np.abs(gf))
+        assert np.max(np.abs(gb1 - gb)) <= 1e-12 * np.max(np.abs(gb))
+        # after the backward pass F2 is the window's initial state
+        assert np.array_equal(model.download_f2(0, 1), np.asfortranarray(wl.f2[1]))
+        if nseg > nkeep:  # recomputed segments replaced the kept records
+            with pytest.raises(abi.RamGpuError):
+                model.adj_record(NCALLS - 1, ns)
+            # a second backward pass recomputes everything and agrees (dJ/dFGEOS
+            # sums stale-ghost contributions with atomics: rounding order only)
+            gf2, gb2 = model.adj_backward()
+            assert np.max(np.abs(gf2 - gf1)) <= 1e-13 * np.max(np.abs(gf1))
+            assert np.max(np.abs(gb2 - gb1)) <= 1e-13 * np.max(np.abs(gb1))
+    finally:
+        model.set_adj_record_budget(-1)
 
 
 def test_batched_gradients_equal_solo(tiny):
