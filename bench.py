@@ -633,6 +633,16 @@ def run_gb300(args, rank, world, local_rank):
         gpu.set_kp(-1, kp_at(k))
         gpu.ram_run_host(wl.dts, host, pe_h, pa_h)
 
+    host_pg = [np.asfortranarray(a).copy(order="F") for a in host]  # ordinary (pageable) memory
+    pe_pg = [np.zeros(nm2) for _ in range(ns)]
+    pa_pg = [np.zeros(nm2) for _ in range(ns)]
+
+    def e2e_pageable(k):
+        # the same call from ordinary host arrays, as a Fortran caller's F2:
+        # the SMs move them over the coherent host link
+        gpu.set_kp(-1, kp_at(k))
+        gpu.ram_run_host(wl.dts, host_pg, pe_pg, pa_pg)
+
     def e2e_serial(k):
         # the same traffic as one stream: uploads, ram_run, read-back, wait
         for s in range(ns):
@@ -659,7 +669,9 @@ def run_gb300(args, rank, world, local_rank):
                    "moments of 4 species out; pipelined over 4 species groups), every step"}
     if e2e_steps:
         e2e["value"] = world * cells_per_step * e2e_steps / e2e_time(e2e_pipelined)
+        e2e["pageable_value"] = world * cells_per_step * e2e_steps / e2e_time(e2e_pageable)
         e2e["serial_value"] = world * cells_per_step * e2e_steps / e2e_time(e2e_serial)
+        e2e["pageable_path"] = "ramgpu_ram_run_host with ordinary (pageable) host arrays"
         e2e["serial_path"] = ("ramgpu_upload_f2_async x4 + ramgpu_ram_run_async + ramgpu_download_f2_async x4 "
                               "+ ramgpu_moments_async x4 + ramgpu_synchronize on one stream")
     # the same step with WPADIF on the electrons (both halves), per-kernel timed

@@ -179,7 +179,10 @@ int ramgpu_half_step(ramgpu_ctx *ctx, double dts, int order);
 int ramgpu_ram_run_async(ramgpu_ctx *ctx, double dts);
 /* One ram_run call with F2 crossing the host boundary, as the reference's
  * host array does every call: f2[slot] (slot = member*NS + species, host
- * pointers, best page-locked) holds that item's F2(S,:,:,:,:) as in
+ * pointers: page-locked buffers go through the copy engines, ordinary
+ * pageable ones through an SM copy where the device reaches pageable memory
+ * (a coherent host link such as Grace's), else blocking copies) holds that
+ * item's F2(S,:,:,:,:) as in
  * ramgpu_upload_f2; it is uploaded, advanced and written back in place.
  * The active items are split into groups (ramgpu_set_pipeline_groups,
  * default 4) that run on their own streams as their uploads land, so the

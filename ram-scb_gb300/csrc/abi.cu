@@ -995,8 +995,40 @@ int ramgpu_set_pipeline_groups(ramgpu_ctx* ctx, int groups) {
 // item's place in the full list (Dev::item0), so groups never share it.
 // Enqueue only (direct launches or inside a graph capture of the context's
 // stream, which the group streams join through the events).
+// Copy of n doubles by the SMs, for host memory the device reaches without
+// registration (pageable memory on a coherent host link, such as a Fortran
+// allocatable): asynchronous and graph-capturable where a copy-engine
+// transfer from pageable memory blocks the host.  16-byte vectors when both
+// ends allow them.
+__global__ void k_copy_f64(const double* __restrict__ src, double* __restrict__ dst, long long n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if ((((uintptr_t)src | (uintptr_t)dst) & 15u) == 0) {
+    const double2* s2 = reinterpret_cast<const double2*>(src);
+    double2* d2 = reinterpret_cast<double2*>(dst);
+    for (long long i = t0; i < n / 2; i += stride) d2[i] = s2[i];
+    if (t0 == 0 && (n & 1)) dst[n - 1] = src[n - 1];
+  } else {
+    for (long long i = t0; i < n; i += stride) dst[i] = src[i];
+  }
+}
+
+// One transfer of the pipeline: a copy-engine copy, or the SM copy when the
+// host side is pageable memory the device can reach (ctx->pageable_sm).
+static int pipe_copy(ramgpu_ctx* ctx, double* dst, const double* src, size_t n, bool host_is_pageable,
+                     cudaStream_t st) {
+  if (host_is_pageable) {
+    k_copy_f64<<<64, 256, 0, st>>>(src, dst, (long long)n);
+    ctx->launches += 1;
+    CKL("pageable copy");
+  } else {
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDefault, st));
+  }
+  return RAMGPU_OK;
+}
+
 static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, double* const* ppert,
-                            double* const* ppart, int G) {
+                            double* const* ppart, int G, const std::vector<char>& pageable) {
   const int nit = ctx->d.nitems;
   cudaEvent_t ev_prev = ctx->pipe_events[2 * G], ev_tab = ctx->pipe_events[2 * G + 1];
   const size_t n = ctx->d.ncell, nm2 = (size_t)ctx->d.nr * ctx->d.nt;
@@ -1012,7 +1044,7 @@ static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, doub
     for (int it = i0; it < i1; ++it) {
       const int slot = slot_of(it);
       if (f2[slot])
-        CK(cudaMemcpyAsync(full.f2 + (size_t)slot * n, f2[slot], n * sizeof(double), cudaMemcpyDefault, st));
+        if (int rc = pipe_copy(ctx, full.f2 + (size_t)slot * n, f2[slot], n, pageable[slot], st)) return rc;
     }
     CK(cudaEventRecord(ctx->pipe_events[2 * g], st));
   }
@@ -1032,14 +1064,16 @@ static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, doub
     ctx->d = full;
     ctx->stream = main;
     if (rc) return rc;
+    const size_t ns2 = (size_t)full.nm * full.ns;
     for (int it = i0; it < i1; ++it) {
       const int slot = slot_of(it);
-      if (f2[slot])
-        CK(cudaMemcpyAsync(f2[slot], full.f2 + (size_t)slot * n, n * sizeof(double), cudaMemcpyDefault, st));
-      if (ppert && ppert[slot])
-        CK(cudaMemcpyAsync(ppert[slot], full.ppert + (size_t)slot * nm2, nm2 * sizeof(double), cudaMemcpyDefault, st));
-      if (ppart && ppart[slot])
-        CK(cudaMemcpyAsync(ppart[slot], full.ppart + (size_t)slot * nm2, nm2 * sizeof(double), cudaMemcpyDefault, st));
+      int rc2 = RAMGPU_OK;
+      if (f2[slot]) rc2 = pipe_copy(ctx, f2[slot], full.f2 + (size_t)slot * n, n, pageable[slot], st);
+      if (!rc2 && ppert && ppert[slot])
+        rc2 = pipe_copy(ctx, ppert[slot], full.ppert + (size_t)slot * nm2, nm2, pageable[ns2 + slot], st);
+      if (!rc2 && ppart && ppart[slot])
+        rc2 = pipe_copy(ctx, ppart[slot], full.ppart + (size_t)slot * nm2, nm2, pageable[2 * ns2 + slot], st);
+      if (rc2) return rc2;
     }
     CK(cudaEventRecord(ctx->pipe_events[2 * g + 1], st));
     CK(cudaStreamWaitEvent(main, ctx->pipe_events[2 * g + 1], 0));
@@ -1077,27 +1111,37 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
   }
   const bool timing = ctx->timing;
   ctx->timing = false;
-  // a graph holds the copies' host addresses, so it is kept per buffer set
-  // and only for page-locked (or device) buffers: capturing a copy from
-  // pageable memory is not allowed
+  // Pageable host buffers are moved by the SMs where the device reaches
+  // pageable memory (a coherent host link), else by blocking copies.  A
+  // graph holds the buffers' addresses, so it is kept per buffer set, and
+  // not built when a copy would come from pageable memory through the copy
+  // engines (not capturable).
   const int nslot = ctx->d.nm * ctx->d.ns;
   std::vector<const void*> key;
+  std::vector<char> pageable;
   bool capturable = ctx->graph_on;
+  int dev = 0, pma = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev);
   for (double* const* tab : {f2, ppert, ppart}) {
     for (int k = 0; k < nslot; ++k) {
       const void* p = tab ? (const void*)tab[k] : nullptr;
       key.push_back(p);
-      if (p && capturable) {
+      bool pg = false;
+      if (p) {
         cudaPointerAttributes at{};
-        if (cudaPointerGetAttributes(&at, p) != cudaSuccess || at.type == cudaMemoryTypeUnregistered) {
+        if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
           cudaGetLastError();
-          capturable = false;
+          at.type = cudaMemoryTypeUnregistered;
         }
+        pg = at.type == cudaMemoryTypeUnregistered;
+        if (pg && !pma) capturable = false;
       }
+      pageable.push_back(pg && pma ? 1 : 0);
     }
   }
   if (!capturable) {
-    rc = enqueue_pipeline(ctx, dts, f2, ppert, ppart, G);
+    rc = enqueue_pipeline(ctx, dts, f2, ppert, ppart, G, pageable);
   } else {
     if (!ctx->pipe_exec || ctx->pipe_key != key || ctx->pipe_dts != dts || ctx->pipe_items != ctx->items_version ||
         ctx->pipe_flags != ctx->d.flags || ctx->pipe_shape != ctx->shape_version || ctx->pipe_g != G) {
@@ -1106,7 +1150,7 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
       cudaGraph_t g = nullptr;
       const long long l0 = ctx->launches;
       CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      rc = enqueue_pipeline(ctx, dts, f2, ppert, ppart, G);
+      rc = enqueue_pipeline(ctx, dts, f2, ppert, ppart, G, pageable);
       cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
       ctx->pipe_launches = ctx->launches - l0;  // kernels per replay
       ctx->launches = l0;
