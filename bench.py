@@ -38,8 +38,10 @@ UNIT = "cell-updates/s"
 # MU carry the CFL quotient's multiply; DRIFTE's forward computes and stores
 # its face coefficients, the reverse loads them).  Per face this is the
 # formulation's own count: X, coefficient, a-term, face fma, flux and the
-# two update operations (beta*|X| is formed on the integer pipe).
-FP64_OPS_PER_CELL = {"driftr": 0.5 * (7.12 + 7.07), "driftp": 6.43, "drifte": 0.5 * (8.58 + 4.78), "driftmu": 0.5 * (8.31 + 6.44)}
+# two update operations (beta*|X| and the CFL quotients are formed on the
+# integer pipe); DRIFTMU's lines are split between lane pairs, whose second
+# lane recomputes the face at the split.
+FP64_OPS_PER_CELL = {"driftr": 0.5 * (7.12 + 7.07), "driftp": 6.43, "drifte": 0.5 * (7.63 + 4.78), "driftmu": 0.5 * (7.74 + 6.76)}
 # DRAM bytes (read + write) per launch of each sweep on the four-species
 # standard grid, the mean of its forward and reverse launches in one ncu
 # capture (profiles/sweeps_four_sp.md, current kernels): F2 is read once

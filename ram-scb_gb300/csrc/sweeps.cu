@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
       double phi_prev;
       {
         const double c = (kCo == 2) ? cst[0] : CK(1);
-        if (kCfl && inside) q = umax64(q, dbits(bitsd(cfl_bits(c, kBits1em10)) * d.ide[0]));
+        if (kCfl && inside) q = umax64(q, mul_pos_bits(cfl_bits(c, kBits1em10), d.ide[0]));
         const bool neg = is_neg(c);
         const double a = (kCo == 2) ? ast[0] : fma(c, mhde[0], neg ? -0.5 : 0.5);
         if (kCo == 1) { cst[0] = c; ast[0] = a; }
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
         nxt = GK(min(K + 3, ne));
         const double xp = gpp - gp; const bits64 bxp = babs_bits(beta, xp);
         const double c = (kCo == 2) ? cst[(long long)(K - 1) * st] : CK(K);
-        if (kCfl && inside) q = umax64(q, dbits(bitsd(cfl_bits(c, kBits1em10)) * d.ide[K - 1]));
+        if (kCfl && inside) q = umax64(q, mul_pos_bits(cfl_bits(c, kBits1em10), d.ide[K - 1]));
         const bool neg = is_neg(c);
         const double a = (kCo == 2) ? ast[(long long)(K - 1) * st] : fma(c, mhde[K - 1], neg ? -0.5 : 0.5);
         if (kCo == 1) { cst[(long long)(K - 1) * st] = c; ast[(long long)(K - 1) * st] = a; }
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         }
         const double xp = gpp - gp; const bits64 bxp = babs_bits(beta, xp);
         const double c = (kCo == 2) ? cst[(long long)(L - 1) * st] : CL(L);
-        if (kCfl && inside) q = umax64(q, dbits(bitsd(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
+        if (kCfl && inside) q = umax64(q, mul_pos_bits(cfl_bits(c, kBits1em32), d.idmu[L - 1]));
         const bool neg = is_neg(c);
         const double a = (kCo == 2) ? ast[(long long)(L - 1) * st] : fma(c, mhdmu[L - 1], neg ? -0.5 : 0.5);
         if (kCo == 1) { cst[(long long)(L - 1) * st] = c; ast[(long long)(L - 1) * st] = a; }
@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         const int L = npa - 1;
         const double c = (kCo == 2) ? cst[(long long)(L - 1) * st] : CL(L);
         if (kCo == 1) cst[(long long)(L - 1) * st] = c;
-        if (kCfl && inside) q = umax64(q, dbits(bitsd(cfl_bits(c, kBits1em32)) * d.idmu[L - 1]));
+        if (kCfl && inside) q = umax64(q, mul_pos_bits(cfl_bits(c, kBits1em32), d.idmu[L - 1]));
         const double phi = c * (closed ? 0.0 : gp);
         const double raw = fma(phi_prev - phi, iwmu[L - 1], g0);
         if (kRec == 1) rl[(long long)(L - 1) * st] = (unsigned char)(is_neg(raw) ? kClipBit : 0);
@@ -529,13 +529,10 @@ static void mu_launch(const Dev& d, dim3 g, int b, double dts, const double* los
   else k_sweep_mu<false, kLoss, 0, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
 }
 // Lines are split between lane pairs when NPA >= 12 (each half keeps at
-// least four cells, so no half reads its partner's F(1) rule), for the
-// launches without the CFL reduction: measured on the four-species grid,
-// the split reverse sweep runs 12 % faster, the split forward one (CFL and
-// fused loss) 9 % slower.
+// least four cells, so no half reads its partner's F(1) rule).
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
                      cudaStream_t st, unsigned char* rec, bool replay, int co) {
-  const bool split = d.npa >= 12 && !cfl;
+  const bool split = d.npa >= 12;
   dim3 g = grid_for(d, 3, split ? 2 * nlines_of(d, 3) : nlines_of(d, 3));
   const int b = d.blk[3];
   if (split) {
