@@ -544,6 +544,7 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   d.betalim = ctx->cfg.betalim;
   const int blk0[4] = {128, 128, 64, 64};
   for (int w = 0; w < 4; ++w) { d.blk[w] = blk0[w]; d.pers[w] = 0; }
+  d.mu_lanes = d.npa >= 12 ? 2 : 1;
   const size_t nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa, ns = d.ns, nm = d.nm, nf = d.nf;
   const size_t nijl = nr * nt * npa, nfield = nf * nt * npa, nslot = nm * ns;
   bool ok = true;
@@ -1395,6 +1396,15 @@ int ramgpu_set_launch_shape(ramgpu_ctx* ctx, int sweep, int threads, int persist
   return RAMGPU_OK;
 }
 
+int ramgpu_set_mu_lanes(ramgpu_ctx* ctx, int lanes) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (lanes != 1 && lanes != 2) return fail(ctx, RAMGPU_ERR_ARG, "lanes must be 1 or 2");
+  if (lanes == 2 && ctx->d.npa < 12) return fail(ctx, RAMGPU_ERR_ARG, "two lanes per line need NPA >= 12");
+  ctx->d.mu_lanes = lanes;
+  ctx->shape_version += 1;
+  return RAMGPU_OK;
+}
+
 int ramgpu_get_launch_shape(ramgpu_ctx* ctx, int* threads4, int* persistent4) {
   if (check_ctx(ctx) || !threads4 || !persistent4) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
   for (int w = 0; w < 4; ++w) { threads4[w] = ctx->d.blk[w]; persistent4[w] = ctx->d.pers[w]; }
@@ -1428,10 +1438,13 @@ int ramgpu_autotune(ramgpu_ctx* ctx, double dts, int reps, double* best_ms4) {
   const int cand_blk[4] = {32, 64, 128, 256};
   for (int w = 0; w < 4; ++w) {
     float best = 1e30f;
-    int bb = ctx->d.blk[w], bp = ctx->d.pers[w];
+    int bb = ctx->d.blk[w], bp = ctx->d.pers[w], bl = ctx->d.mu_lanes;
+    const int nlanes = (w == 3 && ctx->d.npa >= 12) ? 2 : 1;
+    for (int lanes = nlanes; lanes >= 1; --lanes)
     for (int ib = 0; ib < 4; ++ib) {
       for (int persist = 0; persist < 2; ++persist) {
         const int blk = cand_blk[ib];
+        if (w == 3) ctx->d.mu_lanes = (nlanes == 2) ? lanes : ctx->d.mu_lanes;
         int pc = 0;
         if (persist) {
           const int per_sm = sweep_max_blocks_per_sm(w, blk);
@@ -1459,11 +1472,12 @@ int ramgpu_autotune(ramgpu_ctx* ctx, double dts, int reps, double* best_ms4) {
           cudaEventElapsedTime(&ms, e0, e1);
           if (r > 0 && ms < tbest) tbest = ms;
         }
-        if (tbest < best) { best = tbest; bb = blk; bp = pc; }
+        if (tbest < best) { best = tbest; bb = blk; bp = pc; bl = ctx->d.mu_lanes; }
       }
     }
     ctx->d.blk[w] = bb;
     ctx->d.pers[w] = bp;
+    if (w == 3) ctx->d.mu_lanes = bl;
     if (best_ms4) best_ms4[w] = best;
   }
   cudaEventDestroy(e0);

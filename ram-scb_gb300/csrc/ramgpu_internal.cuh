@@ -116,6 +116,7 @@ struct Dev {
   // a persistent grid of that many CTAs looping over (item, line-block) units
   int blk[4];
   int pers[4];
+  int mu_lanes;  // lanes per DRIFTMU line: 2 (lane pairs, NPA >= 12) or 1
 };
 
 // ---------------------------------------------------------------- bit tests

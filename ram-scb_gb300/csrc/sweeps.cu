@@ -528,11 +528,12 @@ static void mu_launch(const Dev& d, dim3 g, int b, double dts, const double* los
   else if (cfl) k_sweep_mu<true, kLoss, 0, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
   else k_sweep_mu<false, kLoss, 0, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
 }
-// Lines are split between lane pairs when NPA >= 12 (each half keeps at
-// least four cells, so no half reads its partner's F(1) rule).
+// Lines are split between lane pairs when d.mu_lanes == 2 (NPA >= 12: each
+// half keeps at least four cells, so no half reads its partner's F(1)
+// rule).
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
                      cudaStream_t st, unsigned char* rec, bool replay, int co) {
-  const bool split = d.npa >= 12;
+  const bool split = d.mu_lanes == 2 && d.npa >= 12;
   dim3 g = grid_for(d, 3, split ? 2 * nlines_of(d, 3) : nlines_of(d, 3));
   const int b = d.blk[3];
   if (split) {

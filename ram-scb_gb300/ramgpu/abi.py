@@ -38,7 +38,7 @@ EXPORTS = (
     "ramgpu_loss_wae", "ramgpu_bounce_integrals", "ramgpu_upload_f2_async", "ramgpu_download_f2_async",
     "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store", "ramgpu_compute_hI",
     "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_set_pipeline_groups",
-    "ramgpu_set_adj_record_budget", "ramgpu_adj_segments",
+    "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_mu_lanes",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
@@ -153,6 +153,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_set_pipeline_groups": ([vp, i], i),
         "ramgpu_set_adj_record_budget": ([vp, C.c_longlong], i),
         "ramgpu_adj_segments": ([vp, ip, ip], i),
+        "ramgpu_set_mu_lanes": ([vp, i], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -516,6 +517,10 @@ class RamGpu:
         J = np.zeros(self.n_members)
         self._ck(self.lib.ramgpu_adj_replay(self.h, _dptr(J)), "adj_replay")
         return J
+
+    def set_mu_lanes(self, lanes: int):
+        """Lanes per DRIFTMU line (2: lane pairs, NPA >= 12; 1)."""
+        self._ck(self.lib.ramgpu_set_mu_lanes(self.h, int(lanes)), "set_mu_lanes")
 
     def set_adj_record_budget(self, nbytes: int):
         """Device bytes the adjoint's branch-record ring may use (< 0: half of

@@ -241,3 +241,46 @@ def test_coefficient_store_is_bitwise_neutral(name):
     for o in outs[1:]:
         for a, b in zip(o, outs[0]):
             assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["tiny_pert", "four_sp"])
+def test_mu_lanes_equal(name):
+    """DRIFTMU with one lane per line and with lane pairs (the second lane
+    recomputing the flux at the split) gives the same F2, CFL and moments,
+    in the plain step (graph and direct) and in the adjoint's recorded and
+    transposed passes."""
+    wl = W.make_workload(name)
+    ns = len(wl.grid.species)
+    outs = []
+    for lanes, graph in ((1, False), (2, False), (2, True)):
+        gpu = _gpu(wl, 4.0)
+        gpu.set_mu_lanes(lanes)
+        gpu.set_graph(graph)
+        for c in range(3):
+            gpu.set_kp(-1, 3.0 + c)
+            gpu.ram_run(wl.dts)
+        gpu.apply_op(wl.dts, abi.OP_DRIFTMU, cfl=True)
+        outs.append([gpu.download_f2(0, s) for s in range(ns)] + [gpu.cfl(0, s) for s in range(ns)]
+                    + [np.concatenate(gpu.moments(0, s)) for s in range(ns)])
+        gpu.close()
+    for o in outs[1:]:
+        for a, b in zip(o, outs[0]):
+            assert np.array_equal(a, b)
+    if name != "tiny_pert":
+        return
+    grads = []
+    kp = np.array([[3.0], [4.0], [5.0]])
+    obs = [{"member": 0, "s": s, "call": c, "k": 10 + 3 * s, "l": 1 + c, "lshell": 3.0 + 0.5 * s,
+            "mlt": 6.0 * c, "log_obs": 0.0} for s in range(ns) for c in range(3)]
+    for lanes in (1, 2):
+        gpu = _gpu(wl, 4.0)
+        gpu.set_mu_lanes(lanes)
+        J = gpu.adj_forward(3, wl.dts, kp, 1, obs)
+        gf, gb = gpu.adj_backward()
+        grads.append((J, gf, gb))
+        gpu.close()
+    assert np.array_equal(grads[0][0], grads[1][0])
+    assert np.max(np.abs(grads[0][1] - grads[1][1])) <= 1e-13 * np.max(np.abs(grads[0][1]))
+    assert np.max(np.abs(grads[0][2] - grads[1][2])) <= 1e-13 * max(np.max(np.abs(grads[0][2])), 1e-300)
+    with pytest.raises(abi.RamGpuError):
+        abi.RamGpu(wl.grid, wl.fields).set_mu_lanes(3)
