@@ -48,8 +48,8 @@ FP64_OPS_PER_CELL = {"driftr": 0.5 * (7.12 + 7.07), "driftp": 6.43, "drifte": 0.
 # and the written lines stay in L2 within a launch; the forward MU also
 # reads the fused CEX/ATMOL factor, and DRIFTE stores and reloads its face
 # coefficients.
-NCU_DRAM_BYTES = {"four_sp": {"driftr": 0.5 * (44.6e6 + 44.4e6), "driftp": 0.5 * (40.7e6 + 40.6e6),
-                               "drifte": 0.5 * (109.0e6 + 129.7e6), "driftmu": 0.5 * (81.7e6 + 40.4e6)}}
+NCU_DRAM_BYTES = {"four_sp": {"driftr": 0.5 * (44.6e6 + 44.3e6), "driftp": 0.5 * (40.6e6 + 40.6e6),
+                               "drifte": 0.5 * (111.0e6 + 129.8e6), "driftmu": 0.5 * (81.8e6 + 40.3e6)}}
 
 
 def parse():
