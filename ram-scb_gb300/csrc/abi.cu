@@ -90,6 +90,7 @@ struct ramgpu_ctx {
     bool rec_stale = false;          // the record ring no longer holds the kept segments
     int nkeep = 1;                   // trailing segments whose records the ring keeps
   } adj;
+  unsigned long long* sep_dev = nullptr;  // separability measure of FFACTOR (bits of a double)
   // device bytes the adjoint's branch-record ring may use (-1: half of the
   // free device memory when the window starts)
   long long adj_record_budget = -1;
@@ -222,9 +223,20 @@ static int prepare(ramgpu_ctx* ctx, double dts) {
     ctx->pd_dirty = true;
   }
   if (ctx->static_dirty) {
-    launch_species_static(ctx->d, ctx->stream);
-    ctx->launches += 2;
+    // the moment sums take the two-fma form when FFACTOR is separable to
+    // rounding (the ARRAYS formula); deciding that reads one value back
+    const int sep_before = ctx->d.mom_sep;
+    ctx->d.mom_sep = 0;
+    launch_species_static(ctx->d, ctx->sep_dev, ctx->stream);
+    ctx->launches += 3;
     CKL("species tables");
+    unsigned long long dev_bits = ~0ULL;
+    CK(cudaMemcpyAsync(&dev_bits, ctx->sep_dev, sizeof(dev_bits), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    double dev = 1.0;
+    memcpy(&dev, &dev_bits, sizeof(dev));
+    ctx->d.mom_sep = (dev <= 1e-13) ? 1 : 0;
+    if (ctx->d.mom_sep != sep_before) ctx->shape_version += 1;  // another moment kernel: recapture
     ctx->static_dirty = false;
     ctx->tables_dts = -1.0;
   }
@@ -585,6 +597,9 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   d.rho = dalloc<double>(ctx, nr * nt, &ok);
   d.mw_a = dalloc<double>(ctx, ns * npa * ne * nr, &ok);
   d.mw_be = dalloc<double>(ctx, npa * nt * nr, &ok); d.mw_ba = dalloc<double>(ctx, npa * nt * nr, &ok);
+  d.mws_a = dalloc<double>(ctx, ns * ne * nr, &ok);
+  d.mws_be = dalloc<double>(ctx, npa * nt * nr, &ok); d.mws_ba = dalloc<double>(ctx, npa * nt * nr, &ok);
+  ctx->sep_dev = dalloc<unsigned long long>(ctx, 1, &ok);
   d.p4 = dalloc<double>(ctx, ns * ne, &ok);
   d.p2 = dalloc<double>(ctx, ns * ne * nr, &ok); d.edot = dalloc<double>(ctx, ns * ne * nr, &ok);
   d.eb = dalloc<double>(ctx, ns * ne, &ok); d.ek = dalloc<double>(ctx, ns * ne, &ok);

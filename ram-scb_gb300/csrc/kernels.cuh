@@ -62,7 +62,7 @@ void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const do
 int sweep_max_blocks_per_sm(int w, int blk);
 
 void launch_field_tables(const Dev& d, cudaStream_t st);
-void launch_species_static(const Dev& d, cudaStream_t st);
+void launch_species_static(const Dev& d, unsigned long long* sep_dev, cudaStream_t st);
 void launch_dts_tables(const Dev& d, double dts, cudaStream_t st);
 void launch_member_coef(const Dev& d, double dts, cudaStream_t st);
 void launch_ghost(const Dev& d, cudaStream_t st);

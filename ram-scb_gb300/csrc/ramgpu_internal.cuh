@@ -61,6 +61,9 @@ struct Dev {
   double *rho;            // (NR,NT): FNHS(NPA)*MU(NPA)/FNHS(NPA-1)/MU(NPA-1)
   double *mw_a;           // (ns, NPA, NE, NR): ANISCH weight RFAC*EPP(K)/FFACTOR
   double *mw_be, *mw_ba;  // (NPA, NT, NR): ANISCH weights WMU/FNHS*(1-MU^2), 2*WMU/FNHS*MU^2
+  double *mws_a;          // (ns, NE, NR): RFAC*EPP(K)*MU(2)/FFACTOR(L=2), the separable species factor
+  double *mws_be, *mws_ba;  // (NPA, NT, NR): mw_be, mw_ba over MU'(L) (MU'(1) = MU(2))
+  int mom_sep;            // FFACTOR has the separable ARRAYS form: two-fma moment sums
   // DTs-dependent per-species small tables
   double *p4;             // (ns, NE)
   double *p2;             // (ns, NR, NE)

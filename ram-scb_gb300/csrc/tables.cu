@@ -166,20 +166,28 @@ __global__ void k_species_static(Dev d) {
 //   mw_be(L,J,I)    = WMU(L)/FNHS(I,J,L)*(1-MU(L)^2)   (as B - B*MU*MU)
 //   mw_ba(L,J,I)    = 2*WMU(L)/FNHS(I,J,L)*MU(L)^2
 // so PPERT = sum over K>=2, L<=u of (F2*mw_a)*mw_be and PPART likewise.
+// ARRAYS builds FFACTOR(S,I,K,L) = LZ^2*GREL/SQRT(GREL^2-1)*MU(L) with
+// FFACTOR(S,I,K,1) = FFACTOR(S,I,K,2) (src/ModRamInit.f90:565-568): then the
+// species factor leaves the L-sum,
+//   mws_a(S,K,I)    = RFAC*EPP(S,K)*MU(2)/FFACTOR(S,I,K,2)
+//   mws_be(L,J,I)   = mw_be/MU'(L),  mws_ba = mw_ba/MU'(L),  MU'(1) = MU(2),
+// PPERT = sum over K of mws_a * sum over L of F2*mws_be: two fma per cell.
+// k_mom_sep_check measures how far the given FFACTOR is from that form.
 // The reference sums the same products band by band (khi = 6,10,25,30,NE)
-// and scales each band by RFAC; the orders differ by rounding only.  Both
-// tables stay in L2 (NS*NPA*NE*NR and NPA*NT*NR doubles).
+// and scales each band by RFAC; the orders differ by rounding only.  All
+// tables stay in L2.
 __global__ void k_moment_weights(Dev d) {
   const long long na = (long long)d.ns * d.npa * d.ne * d.nr;
   const long long nb = (long long)d.npa * d.nt * d.nr;
+  const long long nsa = (long long)d.ns * d.ne * d.nr;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const double RFAC = 4 * kPI / (kCS * 100);
   if (t < na) {
     const int I = 1 + (int)(t % d.nr);
     const int K = 1 + (int)((t / d.nr) % d.ne);
     const int L = 1 + (int)((t / ((long long)d.nr * d.ne)) % d.npa);
     const int s = (int)(t / ((long long)d.nr * d.ne * d.npa));
     const double ff = d.ffactor[(long long)s * d.nr * d.ne * d.npa + (((long long)L - 1) * d.ne + (K - 1)) * d.nr + (I - 1)];
-    const double RFAC = 4 * kPI / (kCS * 100);
     d.mw_a[t] = RFAC * d.epp[s * d.ne + K - 1] / ff;
   } else if (t < na + nb) {
     const long long c = t - na;
@@ -190,14 +198,49 @@ __global__ void k_moment_weights(Dev d) {
     const double BA = B * MU(L) * MU(L);
     d.mw_be[c] = B - BA;
     d.mw_ba[c] = 2 * BA;
+    const double mup = L == 1 ? MU(2) : MU(L);
+    d.mws_be[c] = (B - BA) / mup;
+    d.mws_ba[c] = (2 * BA) / mup;
+  } else if (t < na + nb + nsa) {
+    const long long c = t - na - nb;
+    const int I = 1 + (int)(c % d.nr);
+    const int K = 1 + (int)((c / d.nr) % d.ne);
+    const int s = (int)(c / ((long long)d.nr * d.ne));
+    const double ff2 = d.ffactor[(long long)s * d.nr * d.ne * d.npa + ((long long)1 * d.ne + (K - 1)) * d.nr + (I - 1)];
+    d.mws_a[c] = RFAC * d.epp[s * d.ne + K - 1] * MU(2) / ff2;
   }
 }
 
-void launch_species_static(const Dev& d, cudaStream_t st) {
+// Largest relative distance, over the summed cells, between the general
+// species weight and its separable form mws_a/MU'(L): the maximum of
+// |mw_a*MU'(L) - mws_a| / mws_a as bits into *out (atomic max).
+__global__ void k_mom_sep_check(Dev d, unsigned long long* out) {
+  const long long na = (long long)d.ns * d.npa * d.ne * d.nr;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double dev = 0.0;
+  if (t < na) {
+    const int I = 1 + (int)(t % d.nr);
+    const int K = 1 + (int)((t / d.nr) % d.ne);
+    const int L = 1 + (int)((t / ((long long)d.nr * d.ne)) % d.npa);
+    const int s = (int)(t / ((long long)d.nr * d.ne * d.npa));
+    if (I >= 2 && K >= 2 && L <= d.upa_mom[I - 1]) {
+      const double ws = d.mws_a[((long long)s * d.ne + (K - 1)) * d.nr + (I - 1)];
+      const double mup = L == 1 ? MU(2) : MU(L);
+      dev = fabs(d.mw_a[t] * mup - ws) / ws;
+      if (!(dev == dev)) dev = 1.0;  // NaN: not separable
+    }
+  }
+  warp_atomic_max(out, dbits(dev));
+}
+
+void launch_species_static(const Dev& d, unsigned long long* sep_dev, cudaStream_t st) {
   int n = d.ns * d.ne;
   k_species_static<<<(n + 127) / 128, 128, 0, st>>>(d);
-  const long long nw = (long long)d.ns * d.npa * d.ne * d.nr + (long long)d.npa * d.nt * d.nr;
+  const long long na = (long long)d.ns * d.npa * d.ne * d.nr;
+  const long long nw = na + (long long)d.npa * d.nt * d.nr + (long long)d.ns * d.ne * d.nr;
   k_moment_weights<<<(unsigned)((nw + 255) / 256), 256, 0, st>>>(d);
+  cudaMemsetAsync(sep_dev, 0, sizeof(unsigned long long), st);
+  k_mom_sep_check<<<(unsigned)((na + 255) / 256), 256, 0, st>>>(d, sep_dev);
 }
 
 // ------------------------------------------------------------- DTs tables
@@ -538,6 +581,7 @@ void launch_finish(const Dev& d, cudaStream_t st) {
 // doubles, Q = (K-2)*kMomChunks + chunk, so each (I,J) owns one contiguous
 // run for stage 2.
 constexpr int kMomChunks = 4;
+template <bool kSep>
 __global__ void __launch_bounds__(128) k_moments_part(Dev d) {
   const int nr1 = d.nr - 1, ne1 = d.ne - 1;
   const long long n = (long long)nr1 * d.nt * ne1 * kMomChunks;
@@ -554,8 +598,8 @@ __global__ void __launch_bounds__(128) k_moments_part(Dev d) {
   double* f = d.f2 + (long long)slot * d.ncell + off;
   const long long sa = (long long)d.ne * d.nr, sb = (long long)d.nt * d.nr;  // L strides
   const double* __restrict__ wa = d.mw_a + (long long)s * d.npa * sa + (long long)k * d.nr + i;
-  const double* __restrict__ be = d.mw_be + (long long)j * d.nr + i;
-  const double* __restrict__ ba = d.mw_ba + (long long)j * d.nr + i;
+  const double* __restrict__ be = (kSep ? d.mws_be : d.mw_be) + (long long)j * d.nr + i;
+  const double* __restrict__ ba = (kSep ? d.mws_ba : d.mw_ba) + (long long)j * d.nr + i;
   const double f2 = f[st];
   if (ch == 0) f[0] = f2;
   const int u = d.upa_mom[i];
@@ -565,9 +609,14 @@ __global__ void __launch_bounds__(128) k_moments_part(Dev d) {
 #pragma unroll 4
   for (int L = l0; L <= l1; ++L) {
     const double v = (L == 1) ? f2 : f[(long long)(L - 1) * st];
-    const double g = v * wa[(long long)(L - 1) * sa];
+    const double g = kSep ? v : v * wa[(long long)(L - 1) * sa];
     sume = fma(g, be[(long long)(L - 1) * sb], sume);
     suma = fma(g, ba[(long long)(L - 1) * sb], suma);
+  }
+  if (kSep) {  // the species factor of (S, I, K), once per partial
+    const double ws = d.mws_a[((long long)s * d.ne + k) * d.nr + i];
+    sume *= ws;
+    suma *= ws;
   }
   const int nq = ne1 * kMomChunks;
   double2* part = reinterpret_cast<double2*>(d.mom_part) +
@@ -608,7 +657,8 @@ __global__ void __launch_bounds__(128) k_moments_reduce(Dev d) {
 
 void launch_moments(const Dev& d, cudaStream_t st) {
   long long n = (long long)(d.nr - 1) * d.nt * (d.ne - 1) * kMomChunks;
-  k_moments_part<<<dim3((unsigned)((n + 127) / 128), d.nitems), 128, 0, st>>>(d);
+  if (d.mom_sep) k_moments_part<true><<<dim3((unsigned)((n + 127) / 128), d.nitems), 128, 0, st>>>(d);
+  else k_moments_part<false><<<dim3((unsigned)((n + 127) / 128), d.nitems), 128, 0, st>>>(d);
   int n2 = (d.nr - 1) * d.nt;
   k_moments_reduce<<<dim3((n2 + 3) / 4, d.nitems), 128, 0, st>>>(d);
 }

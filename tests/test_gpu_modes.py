@@ -284,3 +284,25 @@ def test_mu_lanes_equal(name):
     assert np.max(np.abs(grads[0][2] - grads[1][2])) <= 1e-13 * max(np.max(np.abs(grads[0][2])), 1e-300)
     with pytest.raises(abi.RamGpuError):
         abi.RamGpu(wl.grid, wl.fields).set_mu_lanes(3)
+
+
+def test_moments_with_non_separable_ffactor(pert):
+    """FFACTOR that is not of the separable ARRAYS form takes the general
+    moment sums; both forms match the oracle (the separable one is every
+    other test's grid)."""
+    wl = pert
+    rng = np.random.Generator(np.random.PCG64(77))
+    g = dataclasses.replace(wl.grid, ffactor=wl.grid.ffactor * rng.lognormal(0.0, 0.2, size=wl.grid.ffactor.shape))
+    o = pyoracle.Oracle(g, wl.fields)
+    gpu = _gpu(wl, 3.0, grid=g)
+    ref = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    try:
+        for step in range(2):
+            gpu.ram_run(wl.dts)
+            out = o.ram_run(ref, wl.fgeos, wl.dts, kp=3.0)
+            for s in range(len(g.species)):
+                assert rel(gpu.download_f2(0, s), ref[s]) <= TOL
+                pe, pa = gpu.moments(0, s)
+                assert rel(pe, out["ppert"][s]) <= TOL and rel(pa, out["ppart"][s]) <= TOL, (step, s)
+    finally:
+        gpu.close()
