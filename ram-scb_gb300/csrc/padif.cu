@@ -9,7 +9,10 @@
 // divisions); a call then costs per cell one fma and two multiplies in the
 // forward sweep and one fma and one multiply in the backward sweep, and
 // reads F2 once (the forward sweep parks RK in F2's own line, which stays
-// in L2 until the backward sweep reads it back).
+// in L2 until the backward sweep reads it back).  Every line pointer is
+// __restrict__: the table loads of the next cells do not depend on the
+// elimination, and only the compiler's aliasing doubt would hold them
+// behind each store to the line.
 #include "kernels.cuh"
 
 namespace ramgpu {
@@ -39,10 +42,10 @@ __global__ void k_padif_tables(Dev d, double dts) {
   const int k = 1 + (int)(t / ((long long)nr1 * d.nt));
   const long long st = (long long)d.ne * d.nt * d.nr;
   const long long off = ((long long)k * d.nt + j) * d.nr + i;
-  const double* D = d.pd_d + (long long)s * d.ncell + off;
-  double* gn = d.pd_gn + (long long)s * d.ncell + off;
-  double* inv = d.pd_inv + (long long)s * d.ncell + off;
-  double* rl = d.pd_rl + (long long)s * d.ncell + off;
+  const double* __restrict__ D = d.pd_d + (long long)s * d.ncell + off;
+  double* __restrict__ gn = d.pd_gn + (long long)s * d.ncell + off;
+  double* __restrict__ inv = d.pd_inv + (long long)s * d.ncell + off;
+  double* __restrict__ rl = d.pd_rl + (long long)s * d.ncell + off;
   const int npa = d.npa;
   double rlp = -1.0;  // RL(1)
   for (int L = 2; L <= npa - 1; ++L) {
@@ -80,22 +83,43 @@ __global__ void __launch_bounds__(128) k_padif(Dev d, const double* __restrict__
   const int npa = d.npa;
   const long long st = (long long)d.ne * d.nt * d.nr;
   const long long off = ((long long)k * d.nt + j) * d.nr + i;
-  double* fl = d.f2 + (long long)slot * d.ncell + off;
-  const double* la = loss ? loss + (long long)s * d.ncell + off : nullptr;
+  double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + off;
+  const double* __restrict__ la = loss ? loss + (long long)s * d.ncell + off : nullptr;
   if (!on) {
+#pragma unroll 8
     for (int L = 1; L <= npa; ++L) fl[(long long)(L - 1) * st] *= la[(long long)(L - 1) * st];
     return;
   }
   const long long so = (long long)s * d.ncell + off;
-  const double* gn = d.pd_gn + so;
-  const double* inv = d.pd_inv + so;
-  const double* rl = d.pd_rl + so;
+  const double* __restrict__ gn = d.pd_gn + so;
+  const double* __restrict__ inv = d.pd_inv + so;
+  const double* __restrict__ rl = d.pd_rl + so;
   const long long sij = (long long)d.nt * d.nr, fij = (long long)j * d.nr + i;
-  const double* fac = d.pd_fac + fij;
-  const double* ifac = d.pd_ifac + fij;
-  // forward elimination: RK(L) = (F(L) + GN(L) RK(L-1)) / DENOM(L), RK(1) = 0
+  const double* __restrict__ fac = d.pd_fac + fij;
+  const double* __restrict__ ifac = d.pd_ifac + fij;
+  // forward elimination: RK(L) = (F(L) + GN(L) RK(L-1)) / DENOM(L), RK(1) = 0.
+  // A species' lines are few (3-4 warps per SM), so the loads of a block of
+  // kB cells are issued together into registers before the block's
+  // dependent chain: the memory latency is paid once per block, not per cell.
+  constexpr int kB = 16;
   double rk = 0.0;
-  for (int L = 2; L <= npa - 1; ++L) {
+  int L = 2;
+  for (; L + kB - 1 <= npa - 1; L += kB) {
+    double F[kB], g[kB], iv[kB];
+#pragma unroll
+    for (int u = 0; u < kB; ++u) {
+      const long long q = (long long)(L + u - 1) * st;
+      F[u] = fl[q] * ifac[(long long)(L + u - 1) * sij];
+      g[u] = gn[q];
+      iv[u] = inv[q];
+    }
+#pragma unroll
+    for (int u = 0; u < kB; ++u) {
+      rk = fma(g[u], rk, F[u]) * iv[u];
+      fl[(long long)(L + u - 1) * st] = rk;
+    }
+  }
+  for (; L <= npa - 1; ++L) {
     const long long q = (long long)(L - 1) * st;
     const double F = fl[q] * ifac[(long long)(L - 1) * sij];
     rk = fma(gn[q], rk, F) * inv[q];
@@ -103,15 +127,34 @@ __global__ void __launch_bounds__(128) k_padif(Dev d, const double* __restrict__
   }
   // upper boundary F(NPA-1) = RK/(1+RL), F(NPA) = F(NPA-1); back substitution
   double x = rk * inv[(long long)(npa - 1) * st];
-  auto put = [&](int L, double v) {
-    const long long q = (long long)(L - 1) * st;
-    double o = v * fac[(long long)(L - 1) * sij];
+  auto put = [&](int Lq, double v) {
+    const long long q = (long long)(Lq - 1) * st;
+    double o = v * fac[(long long)(Lq - 1) * sij];
     if (loss) o *= la[q];
     fl[q] = o;
   };
   put(npa, x);
   put(npa - 1, x);
-  for (int L = npa - 2; L >= 2; --L) {
+  L = npa - 2;
+  for (; L - kB + 1 >= 2; L -= kB) {
+    double r[kB], rk2[kB], fc[kB], lf[kB];
+#pragma unroll
+    for (int u = 0; u < kB; ++u) {
+      const long long q = (long long)(L - u - 1) * st;
+      r[u] = rl[q];
+      rk2[u] = fl[q];
+      fc[u] = fac[(long long)(L - u - 1) * sij];
+      lf[u] = loss ? la[q] : 1.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kB; ++u) {
+      x = fma(-r[u], x, rk2[u]);
+      double o = x * fc[u];
+      if (loss) o *= lf[u];
+      fl[(long long)(L - u - 1) * st] = o;
+    }
+  }
+  for (; L >= 2; --L) {
     const long long q = (long long)(L - 1) * st;
     x = fma(-rl[q], x, fl[q]);
     put(L, x);
