@@ -341,6 +341,11 @@ long long ramgpu_launch_count(const ramgpu_ctx *ctx);
  * per second (a dependent-free fma loop over 8 x SMs x 256 threads); the
  * denominator of the FP64 roofline this path is bound by on GB300. */
 int ramgpu_probe_fp64(double *lane_ops_per_s);
+/* Device self-test of the integer-pipe FP64 multiply the sweeps use, bit
+ * for bit against the FP64 unit on n random operand pairs (normal, short
+ * significands and ties, zeros, subnormals, infinities, NaN, extreme
+ * exponents); *mismatches receives the count of differing results. */
+int ramgpu_selftest_arith(long long n, unsigned long long seed, long long *mismatches);
 int ramgpu_set_timing(ramgpu_ctx *ctx, int enable);
 int ramgpu_kernel_times(ramgpu_ctx *ctx, double *ms, long long *counts);
 

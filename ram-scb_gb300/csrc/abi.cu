@@ -1348,6 +1348,23 @@ int ramgpu_reset_losses(ramgpu_ctx* ctx) {
 
 long long ramgpu_launch_count(const ramgpu_ctx* ctx) { return ctx ? ctx->launches : -1; }
 
+int ramgpu_selftest_arith(long long n, unsigned long long seed, long long* mismatches) {
+  if (!mismatches || n < 0) return RAMGPU_ERR_ARG;
+  unsigned long long* bad = nullptr;
+  if (cudaMalloc(&bad, sizeof(unsigned long long)) != cudaSuccess) return RAMGPU_ERR_CUDA;
+  cudaError_t e = cudaMemset(bad, 0, sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    launch_selftest_mul(n, seed, bad, 0);
+    e = cudaGetLastError();
+  }
+  unsigned long long h = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  if (e != cudaSuccess) return RAMGPU_ERR_CUDA;
+  *mismatches = (long long)h;
+  return RAMGPU_OK;
+}
+
 int ramgpu_probe_fp64(double* lane_ops_per_s) {
   if (!lane_ops_per_s) return RAMGPU_ERR_ARG;
   int dev = 0, nsm = 0;

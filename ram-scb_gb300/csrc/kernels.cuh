@@ -131,4 +131,6 @@ void launch_fly_sats(const Dev& d, const SatDev* sats, int nsat, double* sat_flu
 void launch_sum_pressure(const Dev& d, int member, unsigned mask, double* pall, double* ppar,
                          cudaStream_t st);
 
+void launch_selftest_mul(long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t st);
+
 }  // namespace ramgpu

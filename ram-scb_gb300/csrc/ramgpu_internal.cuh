@@ -183,6 +183,42 @@ __device__ __forceinline__ bits64 mul_pos_bits(bits64 ax, double y) {
   const bits64 r = ((bits64)(ex + (int)(uy >> 52) - 1023 + hi) << 52) | ((p >> (10 + hi)) & kMantMask);
   return ex == 0x7FF ? ax : r;
 }
+// a*b rounded to nearest even, computed on the integer pipe: the 53-bit
+// significands' 106-bit product from a 64x64 multiply (high and low
+// halves), the dropped bits and a sticky bit decide the rounding (IEEE-754
+// round-half-even), the exponents add.  Zero operands give the signed zero;
+// subnormal, infinite and NaN operands and results outside the normal range
+// take the FP64 multiply, behind a warp-uniform branch so that warps without
+// such a lane do not issue it.  Bit-identical to the FP64 multiply; it
+// moves work off the FP64 unit, which is the limit of the sweeps.
+// The fallback lives out of line: a one-instruction body would be turned
+// into a predicated FP64 multiply, which the FP64 unit still issues.
+static __device__ __noinline__ double mul_rn_fallback(double a, double b) { return a * b; }
+__device__ __forceinline__ double mul_rn_int(double a, double b) {
+  const bits64 ua = dbits(a), ub = dbits(b);
+  const bits64 sign = (ua ^ ub) & kSignMask;
+  const int ea = (int)((ua >> 52) & 0x7FF), eb = (int)((ub >> 52) & 0x7FF);
+  const bits64 x = ((ua & kMantMask) | kImplicit) << 11, y = ((ub & kMantMask) | kImplicit) << 11;
+  const bits64 hi = __umul64hi(x, y);  // product / 2^64, in [2^62, 2^64)
+  const bits64 lo = x * y;
+  const int top = (int)(hi >> 63);
+  const int sh = 10 + top;
+  bits64 sig = hi >> sh;                       // 53 bits
+  const bits64 rem = hi & ((1ULL << sh) - 1);  // dropped bits of the high half
+  const bits64 half = 1ULL << (sh - 1);
+  const bool up = rem > half || (rem == half && (lo != 0 || (sig & 1)));
+  sig += up ? 1 : 0;
+  const int carry = (int)(sig >> 53);          // rounded up to 2^53
+  sig >>= carry;
+  const int E = ea + eb - 1023 + top + carry;
+  bits64 r = sign | ((bits64)E << 52) | (sig & kMantMask);
+  const bool zero = ((ua << 1) == 0) | ((ub << 1) == 0);
+  r = zero ? sign : r;
+  const bool special = (ea == 0x7FF) | (eb == 0x7FF) | (!zero & ((ea == 0) | (eb == 0) | (E <= 0) | (E >= 0x7FF)));
+  double out = bitsd(r);
+  if (special) out = mul_rn_fallback(a, b);
+  return out;
+}
 // x < 0.0 exactly as the Fortran test `C.lt.0` (false for -0.0 and NaN with
 // the sign bit clear).
 __device__ __forceinline__ bool is_neg(double x) { return dbits(x) > 0x8000000000000000ULL; }

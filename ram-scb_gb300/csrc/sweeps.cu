@@ -10,7 +10,12 @@
 //   DRIFTE  src/ModRamDrift.f90:285-376
 //   DRIFTMU src/ModRamDrift.f90:382-473
 // with the face coefficients taken from separable tables built in tables.cu
-// (C = A(I,J) + G(I,J,L)*k(K) etc.), so a face costs 8-9 FP64 add/mul/fma.
+// (C = A(I,J) + G(I,J,L)*k(K) etc.).  The FP64 unit is the limit: sign,
+// abs and limiter tests run on bit patterns, and the products that are only
+// compared (beta*|X|, the CFL quotients) and the flux C*FBND (mul_rn_int,
+// rounded exactly like the FP64 multiply) run on the integer pipe, leaving
+// 6 FP64 add/mul/fma per face.  More integer work than that made the
+// forward DRIFTE and DRIFTMU issue-bound (measured).
 #include "ramgpu_internal.cuh"
 #include "kernels.cuh"
 
@@ -85,7 +90,7 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
         const double fb = (kRec == 2)
             ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = rl[f - 1] & 7)
             : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
-        const double phi = c * fb;
+        const double phi = mul_rn_int(c, fb);
         const double raw = (g0 - phi) + phi_prev;
         fl[f - 1] = (kRec == 2) ? clip_frozen(raw, rl[f - 1]) : clip(raw);
         if (kRec == 1) rl[f - 1] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
@@ -198,7 +203,7 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
         const double fb = (kRec == 2)
             ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rj & 7)
             : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
-        const double phi = c * fb;
+        const double phi = mul_rn_int(c, fb);
         const double raw = (g0 - phi) + phi_prev;
         GJ(J) = (kRec == 2) ? clip_frozen(raw, *rj) : clip(raw);
         if (kRec == 1) rl[(long long)(J - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
@@ -298,7 +303,9 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
         double fb = (kRec == 2) ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rk & 7)
                                 : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         if (closed && K == ne) fb = 0.0;
-        const double phi = c * fb;
+        // loaded coefficients leave this sweep few FP64 operations to hide its
+        // loads behind: the FP64 multiply (uncontracted, bit-equal to mul_rn_int)
+        const double phi = (kCo == 2) ? __dmul_rn(c, fb) : mul_rn_int(c, fb);
         const double raw = fma(phi_prev - phi, iwe[K - 1], g0);
         GK(K) = (kRec == 2) ? clip_frozen(raw, *rk) : clip(raw);
         if (kRec == 1) rl[(long long)(K - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
@@ -429,7 +436,7 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         const unsigned char* rq = kRec ? rl + (long long)(L - 1) * st : nullptr;
         const double fb = (kRec == 2) ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rq & 7)
                                       : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
-        const double phi = c * fb;
+        const double phi = mul_rn_int(c, fb);
         const double raw = fma(phi_prev - phi, iwmu[L - 1], g0);
         if (kRec == 1) rl[(long long)(L - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
         double v = (kRec == 2) ? clip_frozen(raw, *rq) : clip(raw);

@@ -39,6 +39,7 @@ EXPORTS = (
     "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store", "ramgpu_compute_hI",
     "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_set_pipeline_groups",
     "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_mu_lanes",
+    "ramgpu_selftest_arith",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
 KCLASS = ("member_tables", "ghost_planes", "driftr", "driftp", "drifte", "driftmu", "finish",
@@ -154,6 +155,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_set_adj_record_budget": ([vp, C.c_longlong], i),
         "ramgpu_adj_segments": ([vp, ip, ip], i),
         "ramgpu_set_mu_lanes": ([vp, i], i),
+        "ramgpu_selftest_arith": ([C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -172,6 +174,17 @@ def probe_fp64() -> float:
     if rc != RAMGPU_OK:
         raise RamGpuError(f"ramgpu_probe_fp64: {ERRORS.get(rc, rc)}")
     return v.value
+
+
+def selftest_arith(n: int, seed: int = 1) -> int:
+    """Mismatches of the integer-pipe FP64 multiply against the FP64 unit on
+    n random operand pairs (0 expected)."""
+    lib = load_library()
+    m = C.c_longlong()
+    rc = lib.ramgpu_selftest_arith(int(n), int(seed), C.byref(m))
+    if rc != RAMGPU_OK:
+        raise RamGpuError(f"ramgpu_selftest_arith: {ERRORS.get(rc, rc)}")
+    return m.value
 
 
 def _dptr(a: np.ndarray):
