@@ -37,11 +37,11 @@ UNIT = "cell-updates/s"
 # and reverse launches on the four-species standard grid (the forward E and
 # MU carry the CFL quotient's multiply; DRIFTE's forward computes and stores
 # its face coefficients, the reverse loads them).  Per face this is the
-# formulation's own count: X, coefficient, a-term, face fma, flux and the
-# two update operations (beta*|X| and the CFL quotients are formed on the
-# integer pipe); DRIFTMU's lines are split between lane pairs, whose second
-# lane recomputes the face at the split.
-FP64_OPS_PER_CELL = {"driftr": 0.5 * (7.12 + 7.07), "driftp": 6.43, "drifte": 0.5 * (7.63 + 4.78), "driftmu": 0.5 * (7.74 + 6.76)}
+# formulation's own count: X, coefficient, a-term, face fma and the two
+# update operations (beta*|X|, the CFL quotients and the flux C*FBND are
+# formed on the integer pipe); DRIFTMU's lines are split between lane
+# pairs, whose second lane recomputes the face at the split.
+FP64_OPS_PER_CELL = {"driftr": 6.22, "driftp": 5.55, "drifte": 0.5 * (6.71 + 4.78), "driftmu": 0.5 * (6.81 + 5.84)}
 # DRAM bytes (read + write) per launch of each sweep on the four-species
 # standard grid, the mean of its forward and reverse launches in one ncu
 # capture (profiles/sweeps_four_sp.md, current kernels): F2 is read once
