@@ -237,6 +237,7 @@ def run_ensemble(args, torch, dev, stream):
     t0 = 356  # sample from DTs step 356 on: members with length < t0 + 2K retire inside it
     gpu.set_kp_all(ens.kp(t0))
     shapes, _ = gpu.autotune(base.dts)
+    gpu_groups = gpu.step_groups()
     gpu.set_graph(True)
     flush = torch.empty(max(1, args.flush_mb) << 20, dtype=torch.uint8, device=dev)
     for w in range(2):  # warm-up (captures the graph)
@@ -293,6 +294,7 @@ def run_ensemble(args, torch, dev, stream):
             "batched_over_looped": batched / looped,
             "cell_updates_per_s_batched": cell_updates / batched_s,
             "looped_sample_members": len(sub), "launch_shapes": shapes,
+            "item_groups": gpu_groups,
             "notes": "batched: one graph-replayed ram_run per step for all active members; "
                      "looped: the plain direct-launch step of one member at a time"}
 
@@ -553,6 +555,8 @@ def run_gb300(args, rank, world, local_rank):
     if args.no_coef_store:
         gpu.set_coef_store(0)
     shapes, _ = gpu.autotune(wl.dts) if not args.no_autotune else (gpu.launch_shape(), None)
+    # species groups on concurrent streams (autotuned; ramgpu_set_step_groups)
+    item_groups = gpu.step_groups()
     gpu.set_graph(not args.no_graph)
     # warm-up (builds the DTs tables, captures the graph)
     for w in range(args.warmup):
@@ -617,7 +621,7 @@ def run_gb300(args, rank, world, local_rank):
 
     # end-to-end through the C ABI with host buffers (pinned), full F2 in and
     # out every step, as the reference's host array F2 is
-    e2e_steps = 0 if args.no_e2e else max(3, min(10, args.steps))
+    e2e_steps = 0 if args.no_e2e else max(3, min(30, args.steps))
     nm2 = g.nr * g.nt
     pin = [torch.empty(g.ncell, dtype=torch.float64, pin_memory=True) for _ in range(ns)]
     host = [np.reshape(p.numpy(), (g.nr, g.nt, g.ne, g.npa), order="F") for p in pin]
@@ -657,12 +661,18 @@ def run_gb300(args, rank, world, local_rank):
                                              pa_h[s].ctypes.data_as(abi._P)), "moments")
         gpu._ck(lib.ramgpu_synchronize(h), "synchronize")
 
+    e2e_med = {}
+
     def e2e_time(fn):
         fn(0)  # warm (first use creates the group streams)
         torch.cuda.synchronize(dev)
+        ts = []
         t0 = time.perf_counter()
         for k in range(e2e_steps):
+            t1 = time.perf_counter()
             fn(k)
+            ts.append(time.perf_counter() - t1)
+        e2e_med[fn.__name__] = 1e3 * statistics.median(ts)
         return max(time.perf_counter() - t0, 1e-9)
 
     e2e = {"value": None, "unit": UNIT, "h2d_bytes_per_step": 8 * g.ncell * ns,
@@ -673,6 +683,8 @@ def run_gb300(args, rank, world, local_rank):
         e2e["value"] = world * cells_per_step * e2e_steps / e2e_time(e2e_pipelined)
         e2e["pageable_value"] = world * cells_per_step * e2e_steps / e2e_time(e2e_pageable)
         e2e["serial_value"] = world * cells_per_step * e2e_steps / e2e_time(e2e_serial)
+        e2e["ms_per_step_median"] = {"pipelined": e2e_med["e2e_pipelined"], "pageable": e2e_med["e2e_pageable"],
+                                     "serial": e2e_med["e2e_serial"]}
         e2e["pageable_path"] = "ramgpu_ram_run_host with ordinary (pageable) host arrays"
         e2e["serial_path"] = ("ramgpu_upload_f2_async x4 + ramgpu_ram_run_async + ramgpu_download_f2_async x4 "
                               "+ ramgpu_moments_async x4 + ramgpu_synchronize on one stream")
@@ -733,6 +745,7 @@ def run_gb300(args, rank, world, local_rank):
         "config": {"workload": workload_desc(wl), "step": "one ram_run call = 2 DTs steps",
                    "cells_per_step": cells_per_step, "l2": "flushed between timed steps (256 MB write)",
                    "graph": not args.no_graph, "launch_shapes": shapes,
+                   "item_groups": item_groups,
                    "coef_store": "none" if args.no_coef_store else "DRIFTE",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",

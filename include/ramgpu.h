@@ -192,8 +192,20 @@ int ramgpu_ram_run_async(ramgpu_ctx *ctx, double dts);
  * and unchanged on the host side).  Returns when every copy is back. */
 int ramgpu_ram_run_host(ramgpu_ctx *ctx, double dts, double *const *f2, double *const *ppert,
                         double *const *ppart);
-/* Number of item groups ramgpu_ram_run_host pipelines (1..8). */
+/* Number of item groups ramgpu_ram_run_host pipelines its copies over
+ * (1..8, default 4, at most one per item; 1 with RAMGPU_FLAG_LOSSES). */
 int ramgpu_set_pipeline_groups(ramgpu_ctx *ctx, int groups);
+/* The configured pipeline group count (0 for a bad context). */
+int ramgpu_pipeline_groups(const ramgpu_ctx *ctx);
+/* Number of item groups whose sweeps ramgpu_ram_run (and _async) runs on
+ * concurrent streams (1..8, default 4, at most one per item): one group's
+ * launch tails and the gaps between its dependent launches fill with the
+ * others' CTAs.  Results are the same for every count; the loss
+ * bookkeeping (RAMGPU_FLAG_LOSSES) and per-kernel timing passes run as one
+ * group.  The autotuner picks the count. */
+int ramgpu_set_step_groups(ramgpu_ctx *ctx, int groups);
+/* The configured step group count (0 for a bad context). */
+int ramgpu_step_groups(const ramgpu_ctx *ctx);
 
 /* Diagnostic: one operator of the step on every active item, as the
  * reference routine of the same name (the coefficient tables for dts are
@@ -320,9 +332,10 @@ int ramgpu_set_mu_lanes(ramgpu_ctx *ctx, int lanes);
 /* Autotuner: for each sweep in turn, tries 32/64/128/256 threads per CTA,
  * each with a one-unit-per-CTA grid and a persistent grid (resident CTAs x
  * SMs), timing whole ram_run steps on the context's active items (best of
- * reps), keeps the fastest, and restores F2 afterwards (it allocates a
- * temporary snapshot).  best_ms4 (may be NULL) receives the best step time
- * of each sweep's round. */
+ * reps), keeps the fastest, then times 1, 2, 4 and 8 item groups
+ * (ramgpu_set_step_groups) on those shapes and keeps the fastest, and
+ * restores F2 afterwards (it allocates a temporary snapshot).  best_ms4
+ * (may be NULL) receives the best step time of each sweep's round. */
 int ramgpu_autotune(ramgpu_ctx *ctx, double dts, int reps, double *best_ms4);
 
 /* Number of kernel launches this context has issued (diagnostics). */

@@ -96,7 +96,8 @@ struct ramgpu_ctx {
   long long adj_record_budget = -1;
   // ramgpu_ram_run_host: item groups, their streams and events, and the
   // graph of the whole pipeline for one set of host buffers
-  int pipe_groups = 4;
+  int pipe_groups = 4;  // ramgpu_ram_run_host's copy groups
+  int step_groups = 4;  // ram_run's concurrent item groups (autotuned)
   cudaGraphExec_t pipe_exec = nullptr;
   std::vector<const void*> pipe_key;
   double pipe_dts = -1.0;
@@ -397,7 +398,28 @@ static int enqueue_tables(ramgpu_ctx* ctx, double dts) {
   return RAMGPU_OK;
 }
 
+static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, double* const* ppert,
+                            double* const* ppart, int G, const std::vector<char>& pageable);
+static int ensure_group_streams(ramgpu_ctx* ctx, int G);
+
+// Item groups of a step: 1 with the loss bookkeeping (its partial sums are
+// indexed by list position) and in per-kernel timing passes (the events sit
+// on one stream), else the given count, at most one group per item.
+static int clamp_groups(const ramgpu_ctx* ctx, int groups) {
+  if ((ctx->cfg.flags & RAMGPU_FLAG_LOSSES) || ctx->timing) return 1;
+  return std::max(1, std::min(groups, ctx->d.nitems));
+}
+
+// One ram_run step on the device-resident F2.  With more than one item
+// group the groups' sweeps run on concurrent streams: one group's launch
+// tails and the gaps between its dependent launches are filled by the
+// others' CTAs (the same groups as ramgpu_ram_run_host, without copies).
 static int enqueue_body(ramgpu_ctx* ctx, double dts) {
+  const int G = clamp_groups(ctx, ctx->step_groups);
+  if (G > 1) {
+    if (int rc = ensure_group_streams(ctx, G)) return rc;
+    return enqueue_pipeline(ctx, dts, nullptr, nullptr, nullptr, G, {});
+  }
   if (int rc = enqueue_tables(ctx, dts)) return rc;
   return enqueue_sweeps(ctx, dts, true);
 }
@@ -533,6 +555,125 @@ __global__ void k_probe_dfma(double* out, double a, double b, int iters) {
 }
 
 // =================================================================== ABI
+// Copy of n doubles by the SMs, for host memory the device reaches without
+// registration (pageable memory on a coherent host link, such as a Fortran
+// allocatable): asynchronous and graph-capturable where a copy-engine
+// transfer from pageable memory blocks the host.  16-byte vectors when both
+// ends allow them.
+__global__ void k_copy_f64(const double* __restrict__ src, double* __restrict__ dst, long long n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if ((((uintptr_t)src | (uintptr_t)dst) & 15u) == 0) {
+    const double2* s2 = reinterpret_cast<const double2*>(src);
+    double2* d2 = reinterpret_cast<double2*>(dst);
+    for (long long i = t0; i < n / 2; i += stride) d2[i] = s2[i];
+    if (t0 == 0 && (n & 1)) dst[n - 1] = src[n - 1];
+  } else {
+    for (long long i = t0; i < n; i += stride) dst[i] = src[i];
+  }
+}
+
+// One transfer of the pipeline: a copy-engine copy, or the SM copy when the
+// host side is pageable memory the device can reach (ctx->pageable_sm).
+static int pipe_copy(ramgpu_ctx* ctx, double* dst, const double* src, size_t n, bool host_is_pageable,
+                     cudaStream_t st) {
+  if (host_is_pageable) {
+    k_copy_f64<<<64, 256, 0, st>>>(src, dst, (long long)n);
+    ctx->launches += 1;
+    CKL("pageable copy");
+  } else {
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDefault, st));
+  }
+  return RAMGPU_OK;
+}
+
+// Streams and events for G item groups.  Group g's stream gets the g-th
+// highest priority, so the block scheduler favours the groups in upload
+// order.
+static int ensure_group_streams(ramgpu_ctx* ctx, int G) {
+  if ((int)ctx->pipe_streams.size() < G) {
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    while ((int)ctx->pipe_streams.size() < G) {
+      const int prio = std::min(least, greatest + (int)ctx->pipe_streams.size());
+      cudaStream_t st = nullptr;
+      CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio));
+      ctx->pipe_streams.push_back(st);
+    }
+  }
+  while ((int)ctx->pipe_events.size() < 2 * G + 2) {
+    cudaEvent_t e = nullptr;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ctx->pipe_events.push_back(e);
+  }
+  return RAMGPU_OK;
+}
+
+// Uploads, sweeps and read-back of ram_run pipelined over item groups.
+// Stream order: the context's stream (previous work) -> event -> group
+// uploads chained in group order (so the first group starts computing
+// first) ; the per-member tables, ghost planes and CFL reset on the
+// context's stream -> event ; group g: its uploads, the tables event, its
+// sweeps and tail on a view of the work list, its read-back -> event the
+// context's stream waits for.  The coefficient store is indexed by the
+// item's place in the full list (Dev::item0), so groups never share it.
+// f2 == NULL: no copies at all (the resident step over groups).
+// Enqueue only (direct launches or inside a graph capture of the context's
+// stream, which the group streams join through the events).
+static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, double* const* ppert,
+                            double* const* ppart, int G, const std::vector<char>& pageable) {
+  const int nit = ctx->d.nitems;
+  cudaEvent_t ev_prev = ctx->pipe_events[2 * G], ev_tab = ctx->pipe_events[2 * G + 1];
+  const size_t n = ctx->d.ncell, nm2 = (size_t)ctx->d.nr * ctx->d.nt;
+  const cudaStream_t main = ctx->stream;
+  const Dev full = ctx->d;
+  auto slot_of = [&](int it) { return ctx->items_h[it].x * full.ns + ctx->items_h[it].y; };
+  CK(cudaEventRecord(ev_prev, main));
+  // uploads, in group order
+  for (int g = 0; g < G && f2; ++g) {
+    const int i0 = (int)((long long)nit * g / G), i1 = (int)((long long)nit * (g + 1) / G);
+    cudaStream_t st = ctx->pipe_streams[g];
+    CK(cudaStreamWaitEvent(st, g == 0 ? ev_prev : ctx->pipe_events[2 * (g - 1)], 0));
+    for (int it = i0; it < i1; ++it) {
+      const int slot = slot_of(it);
+      if (f2[slot])
+        if (int rc = pipe_copy(ctx, full.f2 + (size_t)slot * n, f2[slot], n, pageable[slot], st)) return rc;
+    }
+    CK(cudaEventRecord(ctx->pipe_events[2 * g], st));
+  }
+  // per-member tables and ghost planes of every item, CFL accumulators
+  if (int rc = enqueue_tables(ctx, dts)) return rc;
+  CK(cudaMemsetAsync(full.cflq, 0, sizeof(unsigned long long) * 4 * full.nm * full.ns, main));
+  CK(cudaEventRecord(ev_tab, main));
+  for (int g = 0; g < G; ++g) {
+    const int i0 = (int)((long long)nit * g / G), i1 = (int)((long long)nit * (g + 1) / G);
+    cudaStream_t st = ctx->pipe_streams[g];
+    CK(cudaStreamWaitEvent(st, ev_tab, 0));
+    ctx->stream = st;
+    ctx->d.items = full.items + i0;
+    ctx->d.nitems = i1 - i0;
+    ctx->d.item0 = i0;
+    const int rc = enqueue_sweeps(ctx, dts, false);
+    ctx->d = full;
+    ctx->stream = main;
+    if (rc) return rc;
+    const size_t ns2 = (size_t)full.nm * full.ns;
+    for (int it = i0; it < i1 && f2; ++it) {
+      const int slot = slot_of(it);
+      int rc2 = RAMGPU_OK;
+      if (f2[slot]) rc2 = pipe_copy(ctx, f2[slot], full.f2 + (size_t)slot * n, n, pageable[slot], st);
+      if (!rc2 && ppert && ppert[slot])
+        rc2 = pipe_copy(ctx, ppert[slot], full.ppert + (size_t)slot * nm2, nm2, pageable[ns2 + slot], st);
+      if (!rc2 && ppart && ppart[slot])
+        rc2 = pipe_copy(ctx, ppart[slot], full.ppart + (size_t)slot * nm2, nm2, pageable[2 * ns2 + slot], st);
+      if (rc2) return rc2;
+    }
+    CK(cudaEventRecord(ctx->pipe_events[2 * g + 1], st));
+    CK(cudaStreamWaitEvent(main, ctx->pipe_events[2 * g + 1], 0));
+  }
+  return RAMGPU_OK;
+}
+
 extern "C" {
 
 int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
@@ -1001,101 +1142,22 @@ int ramgpu_set_pipeline_groups(ramgpu_ctx* ctx, int groups) {
   return RAMGPU_OK;
 }
 
-// Uploads, sweeps and read-back of ram_run pipelined over item groups.
-// Stream order: the context's stream (previous work) -> event -> group
-// uploads chained in group order (so the first group starts computing
-// first) ; the per-member tables, ghost planes and CFL reset on the
-// context's stream -> event ; group g: its uploads, the tables event, its
-// sweeps and tail on a view of the work list, its read-back -> event the
-// context's stream waits for.  The coefficient store is indexed by the
-// item's place in the full list (Dev::item0), so groups never share it.
-// Enqueue only (direct launches or inside a graph capture of the context's
-// stream, which the group streams join through the events).
-// Copy of n doubles by the SMs, for host memory the device reaches without
-// registration (pageable memory on a coherent host link, such as a Fortran
-// allocatable): asynchronous and graph-capturable where a copy-engine
-// transfer from pageable memory blocks the host.  16-byte vectors when both
-// ends allow them.
-__global__ void k_copy_f64(const double* __restrict__ src, double* __restrict__ dst, long long n) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if ((((uintptr_t)src | (uintptr_t)dst) & 15u) == 0) {
-    const double2* s2 = reinterpret_cast<const double2*>(src);
-    double2* d2 = reinterpret_cast<double2*>(dst);
-    for (long long i = t0; i < n / 2; i += stride) d2[i] = s2[i];
-    if (t0 == 0 && (n & 1)) dst[n - 1] = src[n - 1];
-  } else {
-    for (long long i = t0; i < n; i += stride) dst[i] = src[i];
-  }
+int ramgpu_pipeline_groups(const ramgpu_ctx* ctx) {
+  return ctx ? ctx->pipe_groups : 0;
 }
 
-// One transfer of the pipeline: a copy-engine copy, or the SM copy when the
-// host side is pageable memory the device can reach (ctx->pageable_sm).
-static int pipe_copy(ramgpu_ctx* ctx, double* dst, const double* src, size_t n, bool host_is_pageable,
-                     cudaStream_t st) {
-  if (host_is_pageable) {
-    k_copy_f64<<<64, 256, 0, st>>>(src, dst, (long long)n);
-    ctx->launches += 1;
-    CKL("pageable copy");
-  } else {
-    CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDefault, st));
-  }
+int ramgpu_set_step_groups(ramgpu_ctx* ctx, int groups) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (groups < 1 || groups > 8) return fail(ctx, RAMGPU_ERR_ARG, "groups must be 1..8");
+  if (groups != ctx->step_groups) ctx->shape_version += 1;  // ram_run's graph holds the groups
+  ctx->step_groups = groups;
   return RAMGPU_OK;
 }
 
-static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, double* const* ppert,
-                            double* const* ppart, int G, const std::vector<char>& pageable) {
-  const int nit = ctx->d.nitems;
-  cudaEvent_t ev_prev = ctx->pipe_events[2 * G], ev_tab = ctx->pipe_events[2 * G + 1];
-  const size_t n = ctx->d.ncell, nm2 = (size_t)ctx->d.nr * ctx->d.nt;
-  const cudaStream_t main = ctx->stream;
-  const Dev full = ctx->d;
-  auto slot_of = [&](int it) { return ctx->items_h[it].x * full.ns + ctx->items_h[it].y; };
-  CK(cudaEventRecord(ev_prev, main));
-  // uploads, in group order
-  for (int g = 0; g < G; ++g) {
-    const int i0 = (int)((long long)nit * g / G), i1 = (int)((long long)nit * (g + 1) / G);
-    cudaStream_t st = ctx->pipe_streams[g];
-    CK(cudaStreamWaitEvent(st, g == 0 ? ev_prev : ctx->pipe_events[2 * (g - 1)], 0));
-    for (int it = i0; it < i1; ++it) {
-      const int slot = slot_of(it);
-      if (f2[slot])
-        if (int rc = pipe_copy(ctx, full.f2 + (size_t)slot * n, f2[slot], n, pageable[slot], st)) return rc;
-    }
-    CK(cudaEventRecord(ctx->pipe_events[2 * g], st));
-  }
-  // per-member tables and ghost planes of every item, CFL accumulators
-  if (int rc = enqueue_tables(ctx, dts)) return rc;
-  CK(cudaMemsetAsync(full.cflq, 0, sizeof(unsigned long long) * 4 * full.nm * full.ns, main));
-  CK(cudaEventRecord(ev_tab, main));
-  for (int g = 0; g < G; ++g) {
-    const int i0 = (int)((long long)nit * g / G), i1 = (int)((long long)nit * (g + 1) / G);
-    cudaStream_t st = ctx->pipe_streams[g];
-    CK(cudaStreamWaitEvent(st, ev_tab, 0));
-    ctx->stream = st;
-    ctx->d.items = full.items + i0;
-    ctx->d.nitems = i1 - i0;
-    ctx->d.item0 = i0;
-    const int rc = enqueue_sweeps(ctx, dts, false);
-    ctx->d = full;
-    ctx->stream = main;
-    if (rc) return rc;
-    const size_t ns2 = (size_t)full.nm * full.ns;
-    for (int it = i0; it < i1; ++it) {
-      const int slot = slot_of(it);
-      int rc2 = RAMGPU_OK;
-      if (f2[slot]) rc2 = pipe_copy(ctx, f2[slot], full.f2 + (size_t)slot * n, n, pageable[slot], st);
-      if (!rc2 && ppert && ppert[slot])
-        rc2 = pipe_copy(ctx, ppert[slot], full.ppert + (size_t)slot * nm2, nm2, pageable[ns2 + slot], st);
-      if (!rc2 && ppart && ppart[slot])
-        rc2 = pipe_copy(ctx, ppart[slot], full.ppart + (size_t)slot * nm2, nm2, pageable[2 * ns2 + slot], st);
-      if (rc2) return rc2;
-    }
-    CK(cudaEventRecord(ctx->pipe_events[2 * g + 1], st));
-    CK(cudaStreamWaitEvent(main, ctx->pipe_events[2 * g + 1], 0));
-  }
-  return RAMGPU_OK;
+int ramgpu_step_groups(const ramgpu_ctx* ctx) {
+  return ctx ? ctx->step_groups : 0;
 }
+
 
 int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* const* ppert,
                         double* const* ppart) {
@@ -1106,27 +1168,13 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
   const int nit = ctx->d.nitems;
   if (nit == 0) return RAMGPU_OK;
   // the loss bookkeeping indexes its partial sums by list position: one group
-  const bool losses = ctx->cfg.flags & RAMGPU_FLAG_LOSSES;
-  const int G = losses ? 1 : std::min(ctx->pipe_groups, nit);
-  // group g's stream gets the g-th highest priority, so the block scheduler
-  // favours the groups in upload order
-  if ((int)ctx->pipe_streams.size() < G) {
-    int least = 0, greatest = 0;
-    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-    while ((int)ctx->pipe_streams.size() < G) {
-      const int prio = std::min(least, greatest + (int)ctx->pipe_streams.size());
-      cudaStream_t st = nullptr;
-      CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio));
-      ctx->pipe_streams.push_back(st);
-    }
-  }
-  while ((int)ctx->pipe_events.size() < 2 * G + 2) {
-    cudaEvent_t e = nullptr;
-    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    ctx->pipe_events.push_back(e);
-  }
   const bool timing = ctx->timing;
   ctx->timing = false;
+  const int G = clamp_groups(ctx, ctx->pipe_groups);
+  if ((rc = ensure_group_streams(ctx, G))) {
+    ctx->timing = timing;
+    return rc;
+  }
   // Pageable host buffers are moved by the SMs where the device reaches
   // pageable memory (a coherent host link), else by blocking copies.  A
   // graph holds the buffers' addresses, so it is kept per buffer set, and
@@ -1511,6 +1559,32 @@ int ramgpu_autotune(ramgpu_ctx* ctx, double dts, int reps, double* best_ms4) {
     ctx->d.pers[w] = bp;
     if (w == 3) ctx->d.mu_lanes = bl;
     if (best_ms4) best_ms4[w] = best;
+  }
+  // then the number of concurrent item groups, 1, 2, 4 or 8 (at most one
+  // per item), on the chosen shapes
+  if (!(ctx->cfg.flags & RAMGPU_FLAG_LOSSES)) {
+    float best = 1e30f;
+    int bg = ctx->step_groups;
+    for (int G = 1; G <= 8 && G <= ctx->d.nitems; G *= 2) {
+      ctx->step_groups = G;
+      float tbest = 1e30f;
+      for (int r = 0; r <= reps; ++r) {
+        cudaEventRecord(e0, ctx->stream);
+        if (int rc2 = enqueue_body(ctx, dts)) {
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          cudaFree(snap);
+          return rc2;
+        }
+        cudaEventRecord(e1, ctx->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0 && ms < tbest) tbest = ms;
+      }
+      if (tbest < best) { best = tbest; bg = G; }
+    }
+    ctx->step_groups = bg;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -229,6 +229,12 @@ module ModRamGpu
        type(c_ptr), value :: ctx
        integer(c_int), value :: groups
      end function
+     integer(c_int) function ramgpu_set_step_groups(ctx, groups) &
+          bind(C, name="ramgpu_set_step_groups")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: groups
+     end function
      integer(c_int) function ramgpu_synchronize(ctx) bind(C, name="ramgpu_synchronize")
        import :: c_int, c_ptr
        type(c_ptr), value :: ctx

@@ -37,7 +37,8 @@ EXPORTS = (
     "ramgpu_fly_sats", "ramgpu_sum_pressure", "ramgpu_adj_replay", "ramgpu_set_pa_diffusion",
     "ramgpu_loss_wae", "ramgpu_bounce_integrals", "ramgpu_upload_f2_async", "ramgpu_download_f2_async",
     "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store", "ramgpu_compute_hI",
-    "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_set_pipeline_groups",
+    "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_set_pipeline_groups", "ramgpu_pipeline_groups",
+    "ramgpu_set_step_groups", "ramgpu_step_groups",
     "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_mu_lanes",
     "ramgpu_selftest_arith",
 )
@@ -152,6 +153,9 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_sum_pressure": ([vp, i, dp, dp], i),
         "ramgpu_ram_run_host": ([vp, d, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)], i),
         "ramgpu_set_pipeline_groups": ([vp, i], i),
+        "ramgpu_pipeline_groups": ([vp], i),
+        "ramgpu_set_step_groups": ([vp, i], i),
+        "ramgpu_step_groups": ([vp], i),
         "ramgpu_set_adj_record_budget": ([vp, C.c_longlong], i),
         "ramgpu_adj_segments": ([vp, ip, ip], i),
         "ramgpu_set_mu_lanes": ([vp, i], i),
@@ -346,7 +350,18 @@ class RamGpu:
         self._ck(self.lib.ramgpu_ram_run_host(self.h, float(dts), t_f2, t_pe, t_pa), "ram_run_host")
 
     def set_pipeline_groups(self, groups: int):
+        """Item groups ram_run_host pipelines its copies over."""
         self._ck(self.lib.ramgpu_set_pipeline_groups(self.h, int(groups)), "set_pipeline_groups")
+
+    def pipeline_groups(self) -> int:
+        return int(self.lib.ramgpu_pipeline_groups(self.h))
+
+    def set_step_groups(self, groups: int):
+        """Item groups whose sweeps ram_run runs on concurrent streams."""
+        self._ck(self.lib.ramgpu_set_step_groups(self.h, int(groups)), "set_step_groups")
+
+    def step_groups(self) -> int:
+        return int(self.lib.ramgpu_step_groups(self.h))
 
     def half_step(self, dts: float, order: int):
         self._ck(self.lib.ramgpu_half_step(self.h, float(dts), int(order)), "half_step")
@@ -480,8 +495,9 @@ class RamGpu:
         return [(int(a), int(b)) for a, b in zip(t, p)]
 
     def autotune(self, dts: float, reps: int = 3):
-        """Pick threads/CTA and persistent-vs-plain grid per sweep by timing;
-        returns the chosen shapes and their average launch times [ms]."""
+        """Pick threads/CTA and persistent-vs-plain grid per sweep, then the
+        number of item groups, by timing whole steps; returns the chosen
+        shapes and the best step time of each sweep's round [ms]."""
         ms = np.zeros(4)
         self._ck(self.lib.ramgpu_autotune(self.h, float(dts), int(reps), _dptr(ms)), "autotune")
         return self.launch_shape(), ms

@@ -2,7 +2,8 @@
 item groups, gives the same bits as upload + ram_run + download, for every
 group count, with the coefficient store, ensembles with uneven species
 sets, resident (NULL) items, the loss bookkeeping and pitch-angle
-diffusion."""
+diffusion; the resident ram_run over concurrent item groups gives the bits
+of the single-stream step."""
 import numpy as np
 import pytest
 
@@ -33,10 +34,11 @@ def _host_buffers(wl, members):
 
 
 def _reference(wl, members=1, flags=0, calls=3, setup=None):
-    """F2, moments and CFL after `calls` plain ram_run calls."""
+    """F2, moments and CFL after `calls` single-stream ram_run calls."""
     g = wl.grid
     ns = len(g.species)
     gpu = _gpu(wl, members, flags)
+    gpu.set_step_groups(1)
     if setup:
         setup(gpu)
     for c in range(calls):
@@ -73,6 +75,54 @@ def test_pipeline_equals_resident_run(tiny, groups, store):
             assert np.array_equal(gpu.download_f2(0, s), ref["f2"][s]), s
             assert np.array_equal(pe[s], ref["mom"][s][0]) and np.array_equal(pa[s], ref["mom"][s][1])
             assert np.array_equal(gpu.cfl(0, s), ref["cfl"][s])
+    finally:
+        gpu.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("groups", [2, 3, 4, 8])
+def test_resident_groups_equal_single_stream(tiny, groups, graph):
+    """ram_run with the items split over concurrent streams; an ensemble
+    with uneven species sets, so groups hold items of several members."""
+    wl = tiny
+    ns = len(wl.grid.species)
+    plans = [[0, 1, 2, 3], [1, 3], [0, 2]]
+
+    def setup(gp):
+        for m, sp in enumerate(plans):
+            gp.set_member_species(m, sp)
+        gp.set_coef_store(4)
+
+    ref = _reference(wl, members=len(plans), setup=setup)
+    gpu = _gpu(wl, members=len(plans))
+    setup(gpu)
+    gpu.set_graph(graph)
+    gpu.set_step_groups(groups)
+    assert gpu.step_groups() == groups
+    try:
+        for c in range(3):
+            gpu.set_kp(-1, 3.0 + c)
+            gpu.ram_run(wl.dts)
+        for m in range(len(plans)):
+            for s in range(ns):
+                k = m * ns + s
+                assert np.array_equal(gpu.download_f2(m, s), ref["f2"][k]), (m, s)
+                if s not in plans[m]:
+                    continue  # no moments or CFL for a species the member does not carry
+                mom = gpu.moments(m, s)
+                assert np.array_equal(mom[0], ref["mom"][k][0]) and np.array_equal(mom[1], ref["mom"][k][1])
+                assert np.array_equal(gpu.cfl(m, s), ref["cfl"][k])
+    finally:
+        gpu.close()
+
+
+def test_autotune_picks_groups(tiny):
+    wl = tiny
+    gpu = _gpu(wl)
+    try:
+        gpu.autotune(wl.dts, reps=1)
+        assert 1 <= gpu.step_groups() <= min(8, len(wl.grid.species))
+        assert gpu.pipeline_groups() == 4
     finally:
         gpu.close()
 
@@ -198,6 +248,8 @@ def test_pipeline_argument_errors(tiny):
     try:
         with pytest.raises(abi.RamGpuError):
             gpu.set_pipeline_groups(0)
+        with pytest.raises(abi.RamGpuError):
+            gpu.set_step_groups(9)
         with pytest.raises(abi.RamGpuError):
             gpu.ram_run_host(wl.dts, [None])  # wrong number of entries
         bad = [np.zeros(5)] * len(wl.grid.species)
