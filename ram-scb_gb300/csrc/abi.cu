@@ -402,6 +402,39 @@ static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, doub
                             double* const* ppart, int G, const std::vector<char>& pageable);
 static int ensure_group_streams(ramgpu_ctx* ctx, int G);
 
+// Runs fn() once per item group, each on its own stream with ctx->d
+// narrowed to the group's items (ctx->stream is the group's stream
+// meanwhile); the groups start after the work enqueued so far on the
+// context's stream, which then waits for all of them.  G == 1: fn() on the
+// context's stream, no events.  Every buffer a group's kernels write is
+// indexed by slot or by the item's place in the list (Dev::item0 and the
+// per-group offsets fn applies), so the groups never write the same bytes.
+template <class F>
+static int over_groups(ramgpu_ctx* ctx, int G, F&& fn) {
+  if (G <= 1) return fn(0);
+  const cudaStream_t main = ctx->stream;
+  const Dev full = ctx->d;
+  const int nit = full.nitems;
+  cudaEvent_t ev0 = ctx->pipe_events[2 * G + 1];
+  CK(cudaEventRecord(ev0, main));
+  for (int g = 0; g < G; ++g) {
+    const int i0 = (int)((long long)nit * g / G), i1 = (int)((long long)nit * (g + 1) / G);
+    cudaStream_t st = ctx->pipe_streams[g];
+    CK(cudaStreamWaitEvent(st, ev0, 0));
+    ctx->stream = st;
+    ctx->d.items = full.items + i0;
+    ctx->d.nitems = i1 - i0;
+    ctx->d.item0 = full.item0 + i0;
+    const int rc = fn(i0);
+    ctx->d = full;
+    ctx->stream = main;
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->pipe_events[2 * g + 1], st));
+    CK(cudaStreamWaitEvent(main, ctx->pipe_events[2 * g + 1], 0));
+  }
+  return RAMGPU_OK;
+}
+
 // Item groups of a step: 1 with the loss bookkeeping (its partial sums are
 // indexed by list position) and in per-kernel timing passes (the events sit
 // on one stream), else the given count, at most one group per item.
@@ -433,30 +466,40 @@ static void adj_free(ramgpu_ctx* ctx) {
 }
 
 // One ram_run call with every sweep recording its branches into rec
-// (8 instances of nitems*ncell bytes: R,P,E,MU forward, MU,E,P,R reverse).
+// (8 instances of nitems*ncell bytes: R,P,E,MU forward, MU,E,P,R reverse),
+// the sweeps over the step's item groups (the record of item i sits at
+// i*ncell in each instance).
 static int enqueue_call_rec(ramgpu_ctx* ctx, double dts, unsigned char* rec, bool moments) {
   const size_t isz = (size_t)ctx->d.nitems * ctx->d.ncell;
   // positions no sweep writes (e.g. cell 1 of a DRIFTR line) stay zero
   CK(cudaMemsetAsync(rec, 0, 8 * isz, ctx->stream));
   launch_member_coef(ctx->d, dts, ctx->stream);
   launch_ghost(ctx->d, ctx->stream);
+  ctx->launches += 3;
+  const int G = clamp_groups(ctx, ctx->step_groups);
+  if (int rc = ensure_group_streams(ctx, G)) return rc;
   // DRIFTE keeps its face coefficients for the reverse half as in the plain
   // step (same DTs and VT within a call)
   const int co_e = (ctx->d.coef && ctx->d.coef_slot[2] >= 0) ? 1 : 0;
-  launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 0 * isz);
-  launch_sweep_p(ctx->d, dts, false, ctx->stream, rec + 1 * isz);
-  launch_sweep_e(ctx->d, dts, false, ctx->stream, rec + 2 * isz, false, co_e);
-  launch_sweep_mu(ctx->d, dts, false, 1, ctx->d.loss2, ctx->stream, rec + 3 * isz);
-  launch_sweep_mu(ctx->d, dts, false, 0, nullptr, ctx->stream, rec + 4 * isz);
-  launch_sweep_e(ctx->d, dts, false, ctx->stream, rec + 5 * isz, false, 2 * co_e);
-  launch_sweep_p(ctx->d, dts, false, ctx->stream, rec + 6 * isz);
-  launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 7 * isz);
-  launch_finish(ctx->d, ctx->stream);
-  if (moments) launch_moments(ctx->d, ctx->stream);
-  else launch_anisch_state(ctx->d, ctx->stream);
-  ctx->launches += moments ? 13 : 12;
-  CKL("recorded ram_run");
-  return RAMGPU_OK;
+  return over_groups(ctx, G, [&](int i0) {
+    const Dev& d = ctx->d;
+    const cudaStream_t st = ctx->stream;
+    unsigned char* r = rec + (size_t)i0 * d.ncell;
+    launch_sweep_r(d, dts, false, st, r + 0 * isz);
+    launch_sweep_p(d, dts, false, st, r + 1 * isz);
+    launch_sweep_e(d, dts, false, st, r + 2 * isz, false, co_e);
+    launch_sweep_mu(d, dts, false, 1, d.loss2, st, r + 3 * isz);
+    launch_sweep_mu(d, dts, false, 0, nullptr, st, r + 4 * isz);
+    launch_sweep_e(d, dts, false, st, r + 5 * isz, false, 2 * co_e);
+    launch_sweep_p(d, dts, false, st, r + 6 * isz);
+    launch_sweep_r(d, dts, false, st, r + 7 * isz);
+    launch_finish(d, st);
+    if (moments) launch_moments(d, st);
+    else launch_anisch_state(d, st);
+    ctx->launches += moments ? 11 : 10;
+    CKL("recorded ram_run");
+    return RAMGPU_OK;
+  });
 }
 
 // One ram_run call with every sweep taking its branches and clips from rec
@@ -465,19 +508,27 @@ static int enqueue_call_replay(ramgpu_ctx* ctx, double dts, unsigned char* rec) 
   const size_t isz = (size_t)ctx->d.nitems * ctx->d.ncell;
   launch_member_coef(ctx->d, dts, ctx->stream);
   launch_ghost(ctx->d, ctx->stream);
-  launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 0 * isz, true);
-  launch_sweep_p(ctx->d, dts, false, ctx->stream, rec + 1 * isz, true);
-  launch_sweep_e(ctx->d, dts, false, ctx->stream, rec + 2 * isz, true);
-  launch_sweep_mu(ctx->d, dts, false, 1, ctx->d.loss2, ctx->stream, rec + 3 * isz, true);
-  launch_sweep_mu(ctx->d, dts, false, 0, nullptr, ctx->stream, rec + 4 * isz, true);
-  launch_sweep_e(ctx->d, dts, false, ctx->stream, rec + 5 * isz, true);
-  launch_sweep_p(ctx->d, dts, false, ctx->stream, rec + 6 * isz, true);
-  launch_sweep_r(ctx->d, dts, false, ctx->stream, rec + 7 * isz, true);
-  launch_finish(ctx->d, ctx->stream);
-  launch_anisch_state(ctx->d, ctx->stream);
-  ctx->launches += 10;
-  CKL("replayed ram_run");
-  return RAMGPU_OK;
+  ctx->launches += 3;
+  const int G = clamp_groups(ctx, ctx->step_groups);
+  if (int rc = ensure_group_streams(ctx, G)) return rc;
+  return over_groups(ctx, G, [&](int i0) {
+    const Dev& d = ctx->d;
+    const cudaStream_t st = ctx->stream;
+    unsigned char* r = rec + (size_t)i0 * d.ncell;
+    launch_sweep_r(d, dts, false, st, r + 0 * isz, true);
+    launch_sweep_p(d, dts, false, st, r + 1 * isz, true);
+    launch_sweep_e(d, dts, false, st, r + 2 * isz, true);
+    launch_sweep_mu(d, dts, false, 1, d.loss2, st, r + 3 * isz, true);
+    launch_sweep_mu(d, dts, false, 0, nullptr, st, r + 4 * isz, true);
+    launch_sweep_e(d, dts, false, st, r + 5 * isz, true);
+    launch_sweep_p(d, dts, false, st, r + 6 * isz, true);
+    launch_sweep_r(d, dts, false, st, r + 7 * isz, true);
+    launch_finish(d, st);
+    launch_anisch_state(d, st);
+    ctx->launches += 10;
+    CKL("replayed ram_run");
+    return RAMGPU_OK;
+  });
 }
 
 static int adj_copy_items(ramgpu_ctx* ctx, double* dst, bool to_ckpt) {
@@ -1969,6 +2020,8 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
   if (rc) return rc;
   const size_t nslot = (size_t)d.nm * d.ns, nfg = (size_t)d.nt * d.ne * d.npa;
   const size_t isz = (size_t)d.nitems * d.ncell;
+  const int G = clamp_groups(ctx, ctx->step_groups);
+  if ((rc = ensure_group_streams(ctx, G))) return rc;
   CK(cudaMemsetAsync(d.lam, 0, sizeof(double) * nslot * d.ncell, ctx->stream));
   CK(cudaMemsetAsync(d.gfg, 0, sizeof(double) * nslot * nfg, ctx->stream));
   for (int seg = a.nseg - 1; seg >= 0; --seg) {
@@ -1985,23 +2038,32 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
       }
     }
     for (int c = c1 - 1; c >= c0; --c) {  // transpose call c
-      const unsigned char* r = a.rec + adj_rec_slot(a, c) * a.rec_call;
+      const unsigned char* rcall = a.rec + adj_rec_slot(a, c) * a.rec_call;
       launch_obs_adj(d, a.obs, a.nobs, c, a.fm, ctx->stream);
       if ((rc = adj_set_kp(ctx, c))) return rc;
       launch_member_coef(d, a.dts, ctx->stream);
       launch_ghost(d, ctx->stream);
-      launch_adj_tail(d, ctx->stream);
-      launch_adj_sweep(d, 0, r + 7 * isz, ctx->stream);
-      launch_adj_sweep(d, 1, r + 6 * isz, ctx->stream);
-      launch_adj_sweep(d, 2, r + 5 * isz, ctx->stream);
-      launch_adj_sweep(d, 3, r + 4 * isz, ctx->stream);
-      launch_scale_lam(d, d.loss2, ctx->stream);
-      launch_adj_sweep(d, 3, r + 3 * isz, ctx->stream);
-      launch_adj_sweep(d, 2, r + 2 * isz, ctx->stream);
-      launch_adj_sweep(d, 1, r + 1 * isz, ctx->stream);
-      launch_adj_sweep(d, 0, r + 0 * isz, ctx->stream);
-      ctx->launches += 15;
-      CKL("adjoint backward");
+      ctx->launches += 4;
+      // the transposed sweeps of each item group on its own stream
+      rc = over_groups(ctx, G, [&](int i0) {
+        const Dev& dg = ctx->d;
+        const cudaStream_t st = ctx->stream;
+        const unsigned char* r = rcall + (size_t)i0 * dg.ncell;
+        launch_adj_tail(dg, st);
+        launch_adj_sweep(dg, 0, r + 7 * isz, st);
+        launch_adj_sweep(dg, 1, r + 6 * isz, st);
+        launch_adj_sweep(dg, 2, r + 5 * isz, st);
+        launch_adj_sweep(dg, 3, r + 4 * isz, st);
+        launch_scale_lam(dg, dg.loss2, st);
+        launch_adj_sweep(dg, 3, r + 3 * isz, st);
+        launch_adj_sweep(dg, 2, r + 2 * isz, st);
+        launch_adj_sweep(dg, 1, r + 1 * isz, st);
+        launch_adj_sweep(dg, 0, r + 0 * isz, st);
+        ctx->launches += 11;
+        CKL("adjoint backward");
+        return RAMGPU_OK;
+      });
+      if (rc) return rc;
     }
   }
   if ((rc = adj_copy_items(ctx, a.ckpt, false))) return rc;  // F2 back to the initial state

@@ -214,6 +214,42 @@ def test_checkpoint_spacing_and_record_budget(case, k, keep):
         model.set_adj_record_budget(-1)
 
 
+@pytest.mark.parametrize("groups", [1, 2, 3])
+def test_item_groups_same_window(case, groups):
+    """The recording forward, the replay and the transposed sweeps over 1,
+    2 or 3 concurrent item groups: the same J, records, digest and dJ/dF2
+    bits as the default groups (dJ/dFGEOS to rounding order: it sums with
+    atomics)."""
+    wl, model, kp, obs, J0, digest0, gf, gb = case
+    ns = len(wl.grid.species)
+    g0 = model.step_groups()
+    model.set_step_groups(groups)
+    try:
+        _set_f2(model, wl, [1.0] * ns)
+        J1 = model.adj_forward(NCALLS, wl.dts, kp, 2, obs)
+        assert J1[0] == J0[0]
+        assert model.adj_digest() == digest0
+        gf1, gb1 = model.adj_backward()
+        assert np.array_equal(gf1, gf)
+        assert np.max(np.abs(gb1 - gb)) <= 1e-13 * np.max(np.abs(gb))
+        _set_f2(model, wl, [1.0] * ns)
+        J2 = model.adj_forward(NCALLS, wl.dts, kp, NCALLS, obs)
+        end = [model.download_f2(0, s) for s in range(ns)]
+        rec = _records(model, ns)
+        _set_f2(model, wl, [1.0] * ns)
+        Jr = model.adj_replay()
+        assert abs(Jr[0] - J2[0]) <= 1e-14 * J2[0]
+        for s in range(ns):
+            assert np.array_equal(model.download_f2(0, s), end[s])
+        model.set_step_groups(g0)
+        _set_f2(model, wl, [1.0] * ns)
+        assert np.array_equal(model.adj_forward(NCALLS, wl.dts, kp, NCALLS, obs), J2)
+        assert np.array_equal(_records(model, ns), rec)
+        _set_f2(model, wl, [1.0] * ns)
+    finally:
+        model.set_step_groups(g0)
+
+
 def test_batched_gradients_equal_solo(tiny):
     lists = [[0, 1, 2, 3], [1, 3], [2]]
     model, kp, obs = make_case(tiny, 3, 3, 24, seed=21, species_lists=lists)
