@@ -197,6 +197,14 @@ int ramgpu_ram_run_host(ramgpu_ctx *ctx, double dts, double *const *f2, double *
 int ramgpu_set_pipeline_groups(ramgpu_ctx *ctx, int groups);
 /* The configured pipeline group count (0 for a bad context). */
 int ramgpu_pipeline_groups(const ramgpu_ctx *ctx);
+/* Diagnostics (no reference counterpart): with the trace on, each
+ * ramgpu_ram_run_host call runs without its graph and records, per group g,
+ * the times (ms after the call's first enqueued work) at which its uploads
+ * had landed, its sweeps were done and its read-back was done;
+ * ramgpu_pipeline_trace returns them for the last call as ms[3*g + 0..2]
+ * (ms holds at least 24 values) and the group count in *groups. */
+int ramgpu_set_pipeline_trace(ramgpu_ctx *ctx, int enable);
+int ramgpu_pipeline_trace(ramgpu_ctx *ctx, int *groups, float *ms);
 /* Number of item groups whose sweeps ramgpu_ram_run (and _async) runs on
  * concurrent streams (1..8, default 4, at most one per item): one group's
  * launch tails and the gaps between its dependent launches fill with the

@@ -106,6 +106,11 @@ struct ramgpu_ctx {
   int pipe_shape = -1, pipe_g = 0;
   std::vector<cudaStream_t> pipe_streams;
   std::vector<cudaEvent_t> pipe_events;  // per group: uploads done, group done; then one for the tables
+  // optional timeline of ramgpu_ram_run_host (diagnostics): start, then per
+  // group uploads landed, sweeps done, read-back done
+  bool pipe_trace = false;
+  std::vector<cudaEvent_t> trace_ev;
+  std::vector<float> trace_ms;
   // optional per-kernel-class timing
   bool timing = false;
   std::vector<cudaEvent_t> ev_free;
@@ -679,6 +684,8 @@ static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, doub
   const cudaStream_t main = ctx->stream;
   const Dev full = ctx->d;
   auto slot_of = [&](int it) { return ctx->items_h[it].x * full.ns + ctx->items_h[it].y; };
+  const bool trace = ctx->pipe_trace && f2;
+  if (trace) CK(cudaEventRecord(ctx->trace_ev[0], main));
   CK(cudaEventRecord(ev_prev, main));
   // uploads, in group order
   for (int g = 0; g < G && f2; ++g) {
@@ -691,6 +698,7 @@ static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, doub
         if (int rc = pipe_copy(ctx, full.f2 + (size_t)slot * n, f2[slot], n, pageable[slot], st)) return rc;
     }
     CK(cudaEventRecord(ctx->pipe_events[2 * g], st));
+    if (trace) CK(cudaEventRecord(ctx->trace_ev[1 + 3 * g], st));
   }
   // per-member tables and ghost planes of every item, CFL accumulators
   if (int rc = enqueue_tables(ctx, dts)) return rc;
@@ -708,6 +716,7 @@ static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, doub
     ctx->d = full;
     ctx->stream = main;
     if (rc) return rc;
+    if (trace) CK(cudaEventRecord(ctx->trace_ev[2 + 3 * g], st));
     const size_t ns2 = (size_t)full.nm * full.ns;
     for (int it = i0; it < i1 && f2; ++it) {
       const int slot = slot_of(it);
@@ -719,6 +728,7 @@ static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, doub
         rc2 = pipe_copy(ctx, ppart[slot], full.ppart + (size_t)slot * nm2, nm2, pageable[2 * ns2 + slot], st);
       if (rc2) return rc2;
     }
+    if (trace) CK(cudaEventRecord(ctx->trace_ev[3 + 3 * g], st));
     CK(cudaEventRecord(ctx->pipe_events[2 * g + 1], st));
     CK(cudaStreamWaitEvent(main, ctx->pipe_events[2 * g + 1], 0));
   }
@@ -852,6 +862,7 @@ int ramgpu_destroy(ramgpu_ctx* ctx) {
   if (ctx->pipe_exec) cudaGraphExecDestroy(ctx->pipe_exec);
   for (cudaStream_t st : ctx->pipe_streams) cudaStreamDestroy(st);
   for (cudaEvent_t e : ctx->pipe_events) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->trace_ev) cudaEventDestroy(e);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return RAMGPU_OK;
@@ -1234,7 +1245,15 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
   const int nslot = ctx->d.nm * ctx->d.ns;
   std::vector<const void*> key;
   std::vector<char> pageable;
-  bool capturable = ctx->graph_on;
+  bool capturable = ctx->graph_on && !ctx->pipe_trace;  // a traced call runs direct
+  if (ctx->pipe_trace) {
+    while ((int)ctx->trace_ev.size() < 1 + 3 * G) {
+      cudaEvent_t e = nullptr;
+      CK(cudaEventCreate(&e));
+      ctx->trace_ev.push_back(e);
+    }
+    ctx->trace_ms.clear();
+  }
   int dev = 0, pma = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev);
@@ -1294,6 +1313,28 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
   ctx->timing = timing;
   if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->pipe_trace) {
+    for (int k = 1; k < 1 + 3 * G; ++k) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, ctx->trace_ev[0], ctx->trace_ev[k]));
+      ctx->trace_ms.push_back(ms);
+    }
+  }
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_pipeline_trace(ramgpu_ctx* ctx, int enable) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  ctx->pipe_trace = enable != 0;
+  ctx->trace_ms.clear();
+  return RAMGPU_OK;
+}
+
+int ramgpu_pipeline_trace(ramgpu_ctx* ctx, int* groups, float* ms) {
+  if (check_ctx(ctx) || !groups || !ms) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (ctx->trace_ms.empty()) return fail(ctx, RAMGPU_ERR_STATE, "no traced ramgpu_ram_run_host call");
+  *groups = (int)ctx->trace_ms.size() / 3;
+  for (size_t k = 0; k < ctx->trace_ms.size(); ++k) ms[k] = ctx->trace_ms[k];
   return RAMGPU_OK;
 }
 

@@ -38,7 +38,7 @@ EXPORTS = (
     "ramgpu_loss_wae", "ramgpu_bounce_integrals", "ramgpu_upload_f2_async", "ramgpu_download_f2_async",
     "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store", "ramgpu_compute_hI",
     "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_set_pipeline_groups", "ramgpu_pipeline_groups",
-    "ramgpu_set_step_groups", "ramgpu_step_groups",
+    "ramgpu_set_step_groups", "ramgpu_step_groups", "ramgpu_set_pipeline_trace", "ramgpu_pipeline_trace",
     "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_mu_lanes",
     "ramgpu_selftest_arith",
 )
@@ -156,6 +156,8 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_pipeline_groups": ([vp], i),
         "ramgpu_set_step_groups": ([vp, i], i),
         "ramgpu_step_groups": ([vp], i),
+        "ramgpu_set_pipeline_trace": ([vp, i], i),
+        "ramgpu_pipeline_trace": ([vp, ip, C.POINTER(C.c_float)], i),
         "ramgpu_set_adj_record_budget": ([vp, C.c_longlong], i),
         "ramgpu_adj_segments": ([vp, ip, ip], i),
         "ramgpu_set_mu_lanes": ([vp, i], i),
@@ -362,6 +364,18 @@ class RamGpu:
 
     def step_groups(self) -> int:
         return int(self.lib.ramgpu_step_groups(self.h))
+
+    def set_pipeline_trace(self, enable: bool):
+        self._ck(self.lib.ramgpu_set_pipeline_trace(self.h, int(bool(enable))), "set_pipeline_trace")
+
+    def pipeline_trace(self) -> np.ndarray:
+        """(groups, 3) ms after the last traced ram_run_host call started:
+        uploads landed, sweeps done, read-back done."""
+        G = C.c_int()
+        ms = np.zeros(24, dtype=np.float32)
+        self._ck(self.lib.ramgpu_pipeline_trace(self.h, C.byref(G), ms.ctypes.data_as(C.POINTER(C.c_float))),
+                 "pipeline_trace")
+        return ms[:3 * G.value].reshape(G.value, 3).astype(np.float64)
 
     def half_step(self, dts: float, order: int):
         self._ck(self.lib.ramgpu_half_step(self.h, float(dts), int(order)), "half_step")

@@ -242,6 +242,33 @@ def test_pipeline_graph_replay(tiny, groups):
         gpu.close()
 
 
+def test_pipeline_trace(tiny):
+    """The traced call gives the same bits and a consistent timeline."""
+    wl = tiny
+    g = wl.grid
+    ns = len(g.species)
+    ref = _reference(wl, calls=2)
+    gpu = _gpu(wl)
+    gpu.set_graph(True)
+    gpu.set_pipeline_groups(2)
+    f2 = _host_buffers(wl, 1)
+    try:
+        with pytest.raises(abi.RamGpuError):
+            gpu.pipeline_trace()
+        gpu.set_pipeline_trace(True)
+        for c in range(2):
+            gpu.set_kp(-1, 3.0 + c)
+            gpu.ram_run_host(wl.dts, f2)
+        t = gpu.pipeline_trace()
+        assert t.shape == (2, 3)
+        assert np.all(t >= 0.0) and np.all(np.diff(t, axis=1) >= 0.0)
+        assert t[1, 0] >= t[0, 0]  # uploads are chained in group order
+        for s in range(ns):
+            assert np.array_equal(f2[s], ref["f2"][s]), s
+    finally:
+        gpu.close()
+
+
 def test_pipeline_argument_errors(tiny):
     wl = tiny
     gpu = _gpu(wl)
