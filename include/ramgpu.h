@@ -346,6 +346,31 @@ int ramgpu_set_mu_lanes(ramgpu_ctx *ctx, int lanes);
  * (may be NULL) receives the best step time of each sweep's round. */
 int ramgpu_autotune(ramgpu_ctx *ctx, double dts, int reps, double *best_ms4);
 
+/* ---- status word ---------------------------------------------------------
+ * The reference stops when a moment is no longer finite (ANISCH,
+ * src/ModRamRun.f90:410-413); the library reports instead.  One device pass
+ * over the active items counts non-finite F2 cells and moments and the
+ * sweeps of the last call whose largest Courant number exceeded 1 (the
+ * DtDrift* of that sweep is then below FracCFL*DTs). */
+typedef struct {
+    long long f2_nonfinite;       /* NaN or infinite F2 cells of the active items */
+    long long moments_nonfinite;  /* NaN or infinite PPERT/PPART values */
+    long long cfl_over;           /* (item, sweep) pairs of the last call with a Courant number > 1 */
+    int first_member;             /* first item (list order) holding a non-finite value: member, */
+    int first_species;            /* species; -1, -1 if none */
+} ramgpu_status;
+/* Runs the pass now (synchronises) and fills *st (may be NULL); returns
+ * RAMGPU_ERR_NUMERIC when a non-finite value was found, else RAMGPU_OK. */
+int ramgpu_check(ramgpu_ctx *ctx, ramgpu_status *st);
+/* With enable != 0 every ramgpu_ram_run / _async / ramgpu_ram_run_host
+ * appends the pass to the call (inside its graph); ramgpu_ram_run and
+ * ramgpu_ram_run_host then return RAMGPU_ERR_NUMERIC after a call that
+ * left a non-finite value, and ramgpu_last_status gives the word of the
+ * last call that ran the pass (for _async: after the stream was
+ * synchronised).  Off by default. */
+int ramgpu_set_check(ramgpu_ctx *ctx, int enable);
+int ramgpu_last_status(ramgpu_ctx *ctx, ramgpu_status *st);
+
 /* Number of kernel launches this context has issued (diagnostics). */
 long long ramgpu_launch_count(const ramgpu_ctx *ctx);
 

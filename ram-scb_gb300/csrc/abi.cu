@@ -106,6 +106,12 @@ struct ramgpu_ctx {
   int pipe_shape = -1, pipe_g = 0;
   std::vector<cudaStream_t> pipe_streams;
   std::vector<cudaEvent_t> pipe_events;  // per group: uploads done, group done; then one for the tables
+  // status word: device words and their page-locked copy; the pass is
+  // appended to every call while check_on
+  unsigned long long* status_d = nullptr;
+  unsigned long long* status_h = nullptr;
+  bool check_on = false;
+  bool status_valid = false;
   // optional timeline of ramgpu_ram_run_host (diagnostics): start, then per
   // group uploads landed, sweeps done, read-back done
   bool pipe_trace = false;
@@ -452,14 +458,29 @@ static int clamp_groups(const ramgpu_ctx* ctx, int groups) {
 // group the groups' sweeps run on concurrent streams: one group's launch
 // tails and the gaps between its dependent launches are filled by the
 // others' CTAs (the same groups as ramgpu_ram_run_host, without copies).
+// The status pass (status.cu) and the copy of its word to the host, on the
+// context's stream.
+static int enqueue_status(ramgpu_ctx* ctx) {
+  launch_status(ctx->d, ctx->status_d, ctx->stream);
+  ctx->launches += ctx->d.nitems ? 1 : 0;
+  CK(cudaMemcpyAsync(ctx->status_h, ctx->status_d, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CKL("status pass");
+  return RAMGPU_OK;
+}
+
 static int enqueue_body(ramgpu_ctx* ctx, double dts) {
   const int G = clamp_groups(ctx, ctx->step_groups);
+  int rc = RAMGPU_OK;
   if (G > 1) {
-    if (int rc = ensure_group_streams(ctx, G)) return rc;
-    return enqueue_pipeline(ctx, dts, nullptr, nullptr, nullptr, G, {});
+    if ((rc = ensure_group_streams(ctx, G))) return rc;
+    rc = enqueue_pipeline(ctx, dts, nullptr, nullptr, nullptr, G, {});
+  } else {
+    if ((rc = enqueue_tables(ctx, dts))) return rc;
+    rc = enqueue_sweeps(ctx, dts, true);
   }
-  if (int rc = enqueue_tables(ctx, dts)) return rc;
-  return enqueue_sweeps(ctx, dts, true);
+  if (!rc && ctx->check_on) rc = enqueue_status(ctx);
+  return rc;
 }
 
 static void adj_free(ramgpu_ctx* ctx) {
@@ -830,6 +851,12 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   ctx->items_d = dalloc<int2>(ctx, nslot, &ok);
   ctx->losses = dalloc<double>(ctx, nslot * 6, &ok);
   ctx->sumrc_part = dalloc<double>(ctx, (size_t)kSumrcStages * nslot * kSumrcBlocks, &ok);
+  ctx->status_d = dalloc<unsigned long long>(ctx, 4, &ok);
+  if (ok && cudaHostAlloc(&ctx->status_h, 4 * sizeof(unsigned long long), cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->status_h = nullptr;
+    ok = false;
+  }
   if (!ok) {
     ramgpu_destroy(ctx);
     return fail(nullptr, RAMGPU_ERR_NOMEM, "device allocation failed");
@@ -863,6 +890,7 @@ int ramgpu_destroy(ramgpu_ctx* ctx) {
   for (cudaStream_t st : ctx->pipe_streams) cudaStreamDestroy(st);
   for (cudaEvent_t e : ctx->pipe_events) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->trace_ev) cudaEventDestroy(e);
+  if (ctx->status_h) cudaFreeHost(ctx->status_h);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return RAMGPU_OK;
@@ -1221,6 +1249,31 @@ int ramgpu_step_groups(const ramgpu_ctx* ctx) {
 }
 
 
+// Status word in the page-locked copy -> struct; RAMGPU_ERR_NUMERIC when
+// a value was not finite.
+static int status_out(ramgpu_ctx* ctx, ramgpu_status* st) {
+  const unsigned long long* w = ctx->status_h;
+  int fm = -1, fs = -1;
+  if (w[3] != ~0ULL && w[3] < ctx->items_h.size()) {
+    fm = ctx->items_h[w[3]].x;
+    fs = ctx->items_h[w[3]].y;
+  }
+  if (st) {
+    st->f2_nonfinite = (long long)w[0];
+    st->moments_nonfinite = (long long)w[1];
+    st->cfl_over = (long long)w[2];
+    st->first_member = fm;
+    st->first_species = fs;
+  }
+  if (w[0] | w[1]) {
+    char msg[160];
+    snprintf(msg, sizeof msg, "non-finite values: %llu F2 cells, %llu moments (first in member %d, species %d)",
+             w[0], w[1], fm, fs);
+    return fail(ctx, RAMGPU_ERR_NUMERIC, msg);
+  }
+  return RAMGPU_OK;
+}
+
 int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* const* ppert,
                         double* const* ppart) {
   if (check_ctx(ctx) || !f2) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
@@ -1276,6 +1329,7 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
   }
   if (!capturable) {
     rc = enqueue_pipeline(ctx, dts, f2, ppert, ppart, G, pageable);
+    if (!rc && ctx->check_on) rc = enqueue_status(ctx);
   } else {
     if (!ctx->pipe_exec || ctx->pipe_key != key || ctx->pipe_dts != dts || ctx->pipe_items != ctx->items_version ||
         ctx->pipe_flags != ctx->d.flags || ctx->pipe_shape != ctx->shape_version || ctx->pipe_g != G) {
@@ -1285,6 +1339,7 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
       const long long l0 = ctx->launches;
       CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
       rc = enqueue_pipeline(ctx, dts, f2, ppert, ppart, G, pageable);
+      if (!rc && ctx->check_on) rc = enqueue_status(ctx);
       cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
       ctx->pipe_launches = ctx->launches - l0;  // kernels per replay
       ctx->launches = l0;
@@ -1320,6 +1375,10 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
       ctx->trace_ms.push_back(ms);
     }
   }
+  if (ctx->check_on) {
+    ctx->status_valid = true;
+    return status_out(ctx, nullptr);
+  }
   return RAMGPU_OK;
 }
 
@@ -1343,7 +1402,36 @@ int ramgpu_ram_run(ramgpu_ctx* ctx, double dts) {
   int rc = enqueue_ram_run(ctx, dts);
   if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->check_on && ctx->d.nitems) {
+    ctx->status_valid = true;
+    return status_out(ctx, nullptr);
+  }
   return RAMGPU_OK;
+}
+
+int ramgpu_check(ramgpu_ctx* ctx, ramgpu_status* st) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (ctx->items_dirty)
+    if (int rc = rebuild_items(ctx)) return rc;
+  if (int rc = enqueue_status(ctx)) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->status_valid = true;
+  return status_out(ctx, st);
+}
+
+int ramgpu_set_check(ramgpu_ctx* ctx, int enable) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if ((enable != 0) != ctx->check_on) ctx->shape_version += 1;  // the graphs hold the pass
+  ctx->check_on = enable != 0;
+  return RAMGPU_OK;
+}
+
+int ramgpu_last_status(ramgpu_ctx* ctx, ramgpu_status* st) {
+  if (check_ctx(ctx) || !st) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  if (!ctx->status_valid && !ctx->check_on) return fail(ctx, RAMGPU_ERR_STATE, "no status pass has run");
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->status_valid = true;
+  return status_out(ctx, st);
 }
 
 int ramgpu_half_step(ramgpu_ctx* ctx, double dts, int order) {

@@ -1,0 +1,68 @@
+// status.cu -- the device status word of a context.
+//
+// The reference stops the run when a moment is no longer finite (ANISCH,
+// src/ModRamRun.f90:410-413) and lets the caller shorten DTs from the
+// DtDrift* of the sweeps (src/ModRamRun.f90:204-205).  The library never
+// stops; one pass over the active items' F2 and moments instead counts
+// what the caller needs to decide:
+//   st[0]  F2 cells that are NaN or infinite,
+//   st[1]  PPERT / PPART values that are NaN or infinite,
+//   st[2]  (item, sweep) pairs of the last call whose largest Courant
+//          number (|C| for R and P, |C|/DE and |C|/DMU for E and MU, the
+//          quantity DtDrift* divides FracCFL*DTs by) exceeded 1,
+//   st[3]  the smallest list position of an item holding a non-finite
+//          value (all bits set if none).
+// Integer tests on the exponent bits: no FP64 work, one read of F2.
+#include "kernels.cuh"
+
+namespace ramgpu {
+
+namespace {
+constexpr bits64 kExpBits = 0x7ff0000000000000ULL;
+__device__ __forceinline__ unsigned nonfinite(double v) { return (dbits(v) & kExpBits) == kExpBits; }
+}  // namespace
+
+__global__ void __launch_bounds__(256) k_status(Dev d, unsigned long long* __restrict__ st) {
+  const int it = blockIdx.y;
+  const int2 item = d.items[it];
+  const long long slot = (long long)item.x * d.ns + item.y;
+  const double* __restrict__ f = d.f2 + slot * d.ncell;
+  const long long nm2 = (long long)d.nr * d.nt;
+  const double* __restrict__ pe = d.ppert + slot * nm2;
+  const double* __restrict__ pa = d.ppart + slot * nm2;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  unsigned long long nf = 0, nmom = 0;
+  for (long long c = t0; c < d.ncell; c += stride) nf += nonfinite(__ldg(f + c));
+  for (long long c = t0; c < nm2; c += stride) nmom += nonfinite(__ldg(pe + c)) + nonfinite(__ldg(pa + c));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    nf += __shfl_xor_sync(0xffffffffu, nf, o);
+    nmom += __shfl_xor_sync(0xffffffffu, nmom, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (nf) atomicAdd(&st[0], nf);
+    if (nmom) atomicAdd(&st[1], nmom);
+    if (nf | nmom) atomicMin(&st[3], (unsigned long long)it);
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 4) {
+    // the CFL accumulators hold the bits of the largest quotient of the
+    // last call (0: the sweep recorded none); DRIFTMU's floor term as in
+    // DtDriftMu (src/ModRamDrift.f90:435)
+    const unsigned long long q = d.cflq[slot * 4 + threadIdx.x];
+    double qq = bitsd(q);
+    if (threadIdx.x == 3) qq = fmax(qq, 1E-32 / d.dmu[d.npa - 1]);
+    if (q != 0ULL && qq > 1.0) atomicAdd(&st[2], 1ULL);
+  }
+}
+
+void launch_status(const Dev& d, unsigned long long* st, cudaStream_t s) {
+  cudaMemsetAsync(st, 0, 3 * sizeof(unsigned long long), s);
+  cudaMemsetAsync(st + 3, 0xff, sizeof(unsigned long long), s);
+  if (d.nitems == 0) return;
+  long long gx = (d.ncell + 256LL * 16 - 1) / (256LL * 16);  // 16 cells per thread
+  gx = gx < 1 ? 1 : (gx > 4096 ? 4096 : gx);
+  k_status<<<dim3((unsigned)gx, (unsigned)d.nitems), 256, 0, s>>>(d, st);
+}
+
+}  // namespace ramgpu

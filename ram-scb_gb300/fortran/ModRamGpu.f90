@@ -36,6 +36,14 @@ module ModRamGpu
   end type ramgpu_sat
 
   integer(c_int), parameter :: RAMGPU_OP_PADIF = 7
+  integer(c_int), parameter :: RAMGPU_ERR_NUMERIC = -4
+
+  ! device status word (ramgpu_check): replaces the stop in ANISCH
+  ! (src/ModRamRun.f90:410-413) with a return code the caller acts on
+  type, bind(C) :: ramgpu_status
+     integer(c_long_long) :: f2_nonfinite, moments_nonfinite, cfl_over
+     integer(c_int)       :: first_member, first_species
+  end type ramgpu_status
 
   interface
      integer(c_int) function ramgpu_create(cfg, ctx) bind(C, name="ramgpu_create")
@@ -234,6 +242,16 @@ module ModRamGpu
        import :: c_int, c_ptr
        type(c_ptr), value :: ctx
        integer(c_int), value :: groups
+     end function
+     integer(c_int) function ramgpu_check(ctx, st) bind(C, name="ramgpu_check")
+       import :: c_int, c_ptr, ramgpu_status
+       type(c_ptr), value :: ctx
+       type(ramgpu_status), intent(out) :: st
+     end function
+     integer(c_int) function ramgpu_set_check(ctx, enable) bind(C, name="ramgpu_set_check")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: enable
      end function
      integer(c_int) function ramgpu_synchronize(ctx) bind(C, name="ramgpu_synchronize")
        import :: c_int, c_ptr

@@ -39,6 +39,7 @@ EXPORTS = (
     "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store", "ramgpu_compute_hI",
     "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_set_pipeline_groups", "ramgpu_pipeline_groups",
     "ramgpu_set_step_groups", "ramgpu_step_groups", "ramgpu_set_pipeline_trace", "ramgpu_pipeline_trace",
+    "ramgpu_check", "ramgpu_set_check", "ramgpu_last_status",
     "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_mu_lanes",
     "ramgpu_selftest_arith",
 )
@@ -49,7 +50,18 @@ OP_DRIFTR, OP_DRIFTP, OP_DRIFTE, OP_DRIFTMU, OP_CHAREXCHANGE, OP_ATMOL, OP_ANISC
 
 
 class RamGpuError(RuntimeError):
-    pass
+    def __init__(self, msg, code=None):
+        super().__init__(msg)
+        self.code = code  # the RAMGPU_ERR_* value, when the library returned one
+
+
+class Status(C.Structure):
+    """ramgpu_status: the device status word."""
+    _fields_ = [("f2_nonfinite", C.c_longlong), ("moments_nonfinite", C.c_longlong),
+                ("cfl_over", C.c_longlong), ("first_member", C.c_int), ("first_species", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Config(C.Structure):
@@ -157,6 +169,9 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_set_step_groups": ([vp, i], i),
         "ramgpu_step_groups": ([vp], i),
         "ramgpu_set_pipeline_trace": ([vp, i], i),
+        "ramgpu_check": ([vp, C.POINTER(Status)], i),
+        "ramgpu_set_check": ([vp, i], i),
+        "ramgpu_last_status": ([vp, C.POINTER(Status)], i),
         "ramgpu_pipeline_trace": ([vp, ip, C.POINTER(C.c_float)], i),
         "ramgpu_set_adj_record_budget": ([vp, C.c_longlong], i),
         "ramgpu_adj_segments": ([vp, ip, ip], i),
@@ -213,6 +228,7 @@ class RamGpu:
         self.grid = grid
         self.ns = len(grid.species)
         self.n_members = n_members
+        self.fraccfl = fraccfl
         self.member_species = [list(range(self.ns)) for _ in range(n_members)]
         cfg = Config(grid.nr, grid.nt, grid.ne, grid.npa, self.ns, n_members, betalim, fraccfl,
                      dtsmin, flags)
@@ -233,7 +249,7 @@ class RamGpu:
         if rc != RAMGPU_OK:
             buf = C.create_string_buffer(512)
             self.lib.ramgpu_last_error(self.h, buf, 512)
-            raise RamGpuError(f"{what}: {ERRORS.get(rc, rc)}: {buf.value.decode()}")
+            raise RamGpuError(f"{what}: {ERRORS.get(rc, rc)}: {buf.value.decode()}", code=rc)
 
     def close(self):
         if getattr(self, "h", None):
@@ -364,6 +380,28 @@ class RamGpu:
 
     def step_groups(self) -> int:
         return int(self.lib.ramgpu_step_groups(self.h))
+
+    def check(self) -> dict:
+        """Status word of the active items now (ramgpu_check); a non-finite
+        value is reported in the dict, not raised."""
+        st = Status()
+        rc = self.lib.ramgpu_check(self.h, C.byref(st))
+        if rc not in (RAMGPU_OK, -4):
+            self._ck(rc, "check")
+        return st.as_dict()
+
+    def set_check(self, enable: bool):
+        """Append the status pass to every ram_run / ram_run_host; the
+        synchronous calls then raise RamGpuError (code -4) after a call that
+        left a non-finite value."""
+        self._ck(self.lib.ramgpu_set_check(self.h, int(bool(enable))), "set_check")
+
+    def last_status(self) -> dict:
+        st = Status()
+        rc = self.lib.ramgpu_last_status(self.h, C.byref(st))
+        if rc not in (RAMGPU_OK, -4):
+            self._ck(rc, "last_status")
+        return st.as_dict()
 
     def set_pipeline_trace(self, enable: bool):
         self._ck(self.lib.ramgpu_set_pipeline_trace(self.h, int(bool(enable))), "set_pipeline_trace")

@@ -18,7 +18,7 @@ CSRC = PKG_ROOT / "csrc"
 LIB_DIR = PKG_ROOT / "lib"
 LIB_PATH = LIB_DIR / "libramgpu.so"
 SOURCES = ["abi.cu", "sweeps.cu", "tables.cu", "adjoint.cu", "noalloc.cu", "outputs.cu", "padif.cu", "bounce.cu",
-           "selftest.cu"]
+           "selftest.cu", "status.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

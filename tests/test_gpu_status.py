@@ -1,0 +1,118 @@
+"""GPU: the device status word (ramgpu_check, ramgpu_set_check).  The
+reference stops when a moment is no longer finite (ANISCH,
+src/ModRamRun.f90:410-413); the library reports the count of non-finite
+F2 cells and moments, the first (member, species) holding one, and the
+sweeps of the last call whose Courant number exceeded 1, against counts
+taken with numpy on the downloaded state and against ramgpu_cfl."""
+import numpy as np
+import pytest
+
+from ramgpu import abi, workload as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def tiny():
+    return W.make_workload("tiny_pert")
+
+
+def _gpu(wl, members=1):
+    g = wl.grid
+    gpu = abi.RamGpu(g, wl.fields, n_members=members)
+    for m in range(members):
+        for s in range(len(g.species)):
+            gpu.upload_f2(m, s, wl.f2[s])
+            gpu.set_boundary(m, s, wl.fgeos[s])
+        gpu.set_kp(m, 3.0)
+    return gpu
+
+
+def _cfl_over(gpu, wl, dts, members):
+    """(item, sweep) pairs with DtDrift* below FracCFL*DTs (FracCFL*DTs is
+    far below the DtDrift caps here, so that is a Courant number above 1)."""
+    fr = gpu.fraccfl * dts
+    n = 0
+    for m in range(members):
+        for s in gpu.member_species[m]:
+            out = gpu.cfl(m, s)
+            n += int(np.sum(np.asarray(out[:4]) < fr))
+    return n
+
+
+def test_healthy_state(tiny):
+    gpu = _gpu(tiny)
+    try:
+        st = gpu.check()
+        assert st == {"f2_nonfinite": 0, "moments_nonfinite": 0, "cfl_over": 0,
+                      "first_member": -1, "first_species": -1}
+        gpu.ram_run(tiny.dts)
+        st = gpu.check()
+        assert st["f2_nonfinite"] == 0 and st["moments_nonfinite"] == 0
+        assert st["cfl_over"] == _cfl_over(gpu, tiny, tiny.dts, 1)
+    finally:
+        gpu.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_nonfinite_is_reported(tiny, graph):
+    """NaN and Inf planted in member 1, species 2: counted exactly before the
+    call, spread by the sweeps after it (the count equals numpy's on the
+    downloaded F2), and ram_run raises with the check on."""
+    wl = tiny
+    ns = len(wl.grid.species)
+    gpu = _gpu(wl, members=2)
+    gpu.set_graph(graph)
+    try:
+        bad = np.asfortranarray(np.array(wl.f2[2], copy=True))
+        bad[3, 4, 5, 6] = np.nan
+        bad[4, 2, 9, 30] = np.inf
+        bad[1, 1, 1, 1] = -np.inf
+        gpu.upload_f2(1, 2, bad)
+        st = gpu.check()
+        assert st["f2_nonfinite"] == 3 and st["moments_nonfinite"] == 0
+        assert (st["first_member"], st["first_species"]) == (1, 2)
+        with pytest.raises(abi.RamGpuError) as ei:
+            gpu.set_check(True)
+            gpu.ram_run(wl.dts)
+        assert ei.value.code == -4
+        st = gpu.last_status()
+        count = sum(int(np.sum(~np.isfinite(gpu.download_f2(m, s)))) for m in range(2) for s in range(ns))
+        assert st["f2_nonfinite"] == count > 3
+        mom = sum(int(np.sum(~np.isfinite(np.asarray(gpu.moments(m, s))))) for m in range(2) for s in range(ns))
+        assert st["moments_nonfinite"] == mom
+        assert (st["first_member"], st["first_species"]) == (1, 2)
+        assert gpu.check() == st
+        # member 0 is untouched by member 1's values
+        for s in range(ns):
+            assert np.all(np.isfinite(gpu.download_f2(0, s)))
+    finally:
+        gpu.close()
+
+
+def test_check_in_host_pipeline_and_courant(tiny):
+    """With the check on, ram_run_host maps the word too; a DTs large enough
+    to push Courant numbers above 1 is reported as ramgpu_cfl shows it."""
+    wl = tiny
+    ns = len(wl.grid.species)
+    gpu = _gpu(wl)
+    gpu.set_check(True)
+    f2 = [np.asfortranarray(wl.f2[s]).copy(order="F") for s in range(ns)]
+    try:
+        gpu.ram_run_host(wl.dts, f2)
+        st = gpu.last_status()
+        assert st["f2_nonfinite"] == 0 and st["moments_nonfinite"] == 0
+        big = 40.0 * wl.dts
+        gpu.ram_run(big)
+        st = gpu.last_status()
+        want = _cfl_over(gpu, wl, big, 1)
+        assert want > 0 and st["cfl_over"] == want
+        f2[1][2, 3, 4, 5] = np.nan
+        with pytest.raises(abi.RamGpuError) as ei:
+            gpu.ram_run_host(wl.dts, f2)
+        assert ei.value.code == -4
+        assert gpu.last_status()["f2_nonfinite"] == int(np.sum(~np.isfinite(f2[1])))
+        gpu.set_check(False)
+        gpu.ram_run(wl.dts)  # no pass appended: the call itself does not raise
+    finally:
+        gpu.close()
