@@ -349,13 +349,17 @@ int ramgpu_autotune(ramgpu_ctx *ctx, double dts, int reps, double *best_ms4);
 /* ---- status word ---------------------------------------------------------
  * The reference stops when a moment is no longer finite (ANISCH,
  * src/ModRamRun.f90:410-413); the library reports instead.  One device pass
- * over the active items counts non-finite F2 cells and moments and the
+ * over the active items counts non-finite F2 cells and moments, the
  * sweeps of the last call whose largest Courant number exceeded 1 (the
- * DtDrift* of that sweep is then below FracCFL*DTs). */
+ * DtDrift* of that sweep is then below FracCFL*DTs) and, with the check
+ * on, the clip events of the last call. */
 typedef struct {
     long long f2_nonfinite;       /* NaN or infinite F2 cells of the active items */
     long long moments_nonfinite;  /* NaN or infinite PPERT/PPART values */
     long long cfl_over;           /* (item, sweep) pairs of the last call with a Courant number > 1 */
+    long long clips;              /* cells the last call's sweeps clipped to 1e-15 (F2 < 0 after an
+                                     update, src/ModRamDrift.f90:187-190); counted only while
+                                     ramgpu_set_check is on, else 0 */
     int first_member;             /* first item (list order) holding a non-finite value: member, */
     int first_species;            /* species; -1, -1 if none */
 } ramgpu_status;

@@ -323,7 +323,7 @@ static int sumrc_stage(ramgpu_ctx* ctx, int stage, int which) {
 static int enqueue_forward(ramgpu_ctx* ctx, double dts, bool loss_fused, const double* loss_table,
                            bool clear_cfl = true) {
   if (clear_cfl)
-    CK(cudaMemsetAsync(ctx->d.cflq, 0, sizeof(unsigned long long) * 4 * ctx->d.nm * ctx->d.ns, ctx->stream));
+    CK(cudaMemsetAsync(ctx->d.cflq, 0, sizeof(unsigned long long) * 5 * ctx->d.nm * ctx->d.ns, ctx->stream));
   const Dev& d = ctx->d;
   auto co = [&](int w) { return (d.coef && d.coef_slot[w] >= 0) ? 1 : 0; };
   { Timed t(ctx, 2); launch_sweep_r(d, dts, true, ctx->stream, nullptr, false, co(0)); }
@@ -463,7 +463,7 @@ static int clamp_groups(const ramgpu_ctx* ctx, int groups) {
 static int enqueue_status(ramgpu_ctx* ctx) {
   launch_status(ctx->d, ctx->status_d, ctx->stream);
   ctx->launches += ctx->d.nitems ? 1 : 0;
-  CK(cudaMemcpyAsync(ctx->status_h, ctx->status_d, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+  CK(cudaMemcpyAsync(ctx->status_h, ctx->status_d, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                      ctx->stream));
   CKL("status pass");
   return RAMGPU_OK;
@@ -723,7 +723,7 @@ static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, doub
   }
   // per-member tables and ghost planes of every item, CFL accumulators
   if (int rc = enqueue_tables(ctx, dts)) return rc;
-  CK(cudaMemsetAsync(full.cflq, 0, sizeof(unsigned long long) * 4 * full.nm * full.ns, main));
+  CK(cudaMemsetAsync(full.cflq, 0, sizeof(unsigned long long) * 5 * full.nm * full.ns, main));
   CK(cudaEventRecord(ev_tab, main));
   for (int g = 0; g < G; ++g) {
     const int i0 = (int)((long long)nit * g / G), i1 = (int)((long long)nit * (g + 1) / G);
@@ -844,15 +844,19 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   d.lam = dalloc<double>(ctx, nslot * ncell, &ok);
   d.gfg = dalloc<double>(ctx, nslot * nt * ne * npa, &ok);
   d.plane_carry_src = dalloc<int>(ctx, nslot * ne * npa, &ok);
-  d.cflq = dalloc<unsigned long long>(ctx, nslot * 4, &ok);
+  // CFL accumulators (4 per slot) followed by the clip counters (1 per
+  // slot): one reset clears both
+  d.cflq = dalloc<unsigned long long>(ctx, nslot * 5, &ok);
+  d.clipq = d.cflq ? d.cflq + 4 * nslot : nullptr;
+  d.count_clips = 0;
   d.mom_part = dalloc<double>(ctx, nslot * 4 * nr * nt * ne * 2, &ok);
   d.ppert = dalloc<double>(ctx, nslot * nr * nt, &ok);
   d.ppart = dalloc<double>(ctx, nslot * nr * nt, &ok);
   ctx->items_d = dalloc<int2>(ctx, nslot, &ok);
   ctx->losses = dalloc<double>(ctx, nslot * 6, &ok);
   ctx->sumrc_part = dalloc<double>(ctx, (size_t)kSumrcStages * nslot * kSumrcBlocks, &ok);
-  ctx->status_d = dalloc<unsigned long long>(ctx, 4, &ok);
-  if (ok && cudaHostAlloc(&ctx->status_h, 4 * sizeof(unsigned long long), cudaHostAllocDefault) != cudaSuccess) {
+  ctx->status_d = dalloc<unsigned long long>(ctx, 5, &ok);
+  if (ok && cudaHostAlloc(&ctx->status_h, 5 * sizeof(unsigned long long), cudaHostAllocDefault) != cudaSuccess) {
     cudaGetLastError();
     ctx->status_h = nullptr;
     ok = false;
@@ -1262,6 +1266,7 @@ static int status_out(ramgpu_ctx* ctx, ramgpu_status* st) {
     st->f2_nonfinite = (long long)w[0];
     st->moments_nonfinite = (long long)w[1];
     st->cfl_over = (long long)w[2];
+    st->clips = (long long)w[4];
     st->first_member = fm;
     st->first_species = fs;
   }
@@ -1423,6 +1428,7 @@ int ramgpu_set_check(ramgpu_ctx* ctx, int enable) {
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
   if ((enable != 0) != ctx->check_on) ctx->shape_version += 1;  // the graphs hold the pass
   ctx->check_on = enable != 0;
+  ctx->d.count_clips = ctx->check_on ? 1 : 0;  // the sweeps count clip events meanwhile
   return RAMGPU_OK;
 }
 
@@ -1462,7 +1468,7 @@ int ramgpu_apply_op(ramgpu_ctx* ctx, double dts, int op, int cfl) {
   launch_member_coef(ctx->d, dts, ctx->stream);
   launch_ghost(ctx->d, ctx->stream);
   ctx->launches += 3;
-  if (cfl) CK(cudaMemsetAsync(ctx->d.cflq, 0, sizeof(unsigned long long) * 4 * ctx->d.nm * ctx->d.ns, ctx->stream));
+  if (cfl) CK(cudaMemsetAsync(ctx->d.cflq, 0, sizeof(unsigned long long) * 5 * ctx->d.nm * ctx->d.ns, ctx->stream));
   switch (op) {
     case 0: launch_sweep_r(ctx->d, dts, cfl != 0, ctx->stream); break;
     case 1: launch_sweep_p(ctx->d, dts, cfl != 0, ctx->stream); break;

@@ -132,7 +132,7 @@ void launch_sum_pressure(const Dev& d, int member, unsigned mask, double* pall, 
                          cudaStream_t st);
 
 void launch_selftest_mul(long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t st);
-// Status word of the active items (status.cu): st[4] device words.
+// Status word of the active items (status.cu): st[5] device words.
 void launch_status(const Dev& d, unsigned long long* st, cudaStream_t s);
 
 }  // namespace ramgpu

@@ -102,6 +102,8 @@ struct Dev {
   double *lam;            // (nm*ns, ncell)
   double *gfg;            // (nm*ns, NT*NE*NPA)
   unsigned long long *cflq;  // (nm*ns, 4): max over cells of the CFL quotient, as bits
+  unsigned long long *clipq;  // (nm*ns): clip events of the last call (follows cflq)
+  int count_clips;            // the sweeps count clip events (status pass on)
   double *mom_part;       // (nm*ns, NT, NR, (NE-1)*4 chunks, 2) moment partials
   double *ppert, *ppart;  // (nm*ns, NR, NT)
   double *sumrc_part;     // (nm*ns, nblk) SUMRC partial sums
@@ -266,6 +268,9 @@ __device__ __forceinline__ double face_value_case(double x, bits64 bx, double d,
   return act ? fb : fup;
 }
 constexpr int kClipBit = 8;  // recorded with the case: the updated cell was clipped
+// kRec modes of the sweeps: 0 plain, 1 record branches, 2 replay them,
+// 3 plain and count clip events into Dev::clipq
+constexpr int kRecCount = 3;
 
 // Stored face coefficient array q (0: C, 1: a) of sweep w for work item `it`.
 __device__ __forceinline__ double* coef_ptr(const Dev& d, int w, int q, long long it) {
@@ -298,6 +303,13 @@ __device__ __forceinline__ double clip(double v) { return is_neg(v) ? 1E-15 : v;
 
 // 64-bit max-reduction of a non-negative double across a warp, then one
 // atomicMax on the bit pattern (order-independent, hence deterministic).
+// Warp sum of a per-lane count added to *slot (every lane of the warp calls it).
+__device__ __forceinline__ void warp_atomic_add(unsigned long long *slot, unsigned v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v != 0u) atomicAdd(slot, (unsigned long long)v);
+}
+
 __device__ __forceinline__ void warp_atomic_max(unsigned long long *slot, unsigned long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {

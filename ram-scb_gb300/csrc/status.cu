@@ -11,7 +11,11 @@
 //          number (|C| for R and P, |C|/DE and |C|/DMU for E and MU, the
 //          quantity DtDrift* divides FracCFL*DTs by) exceeded 1,
 //   st[3]  the smallest list position of an item holding a non-finite
-//          value (all bits set if none).
+//          value (all bits set if none),
+//   st[4]  updated cells the sweeps of the last call clipped to 1e-15
+//          because they came out negative (src/ModRamDrift.f90:187-190 and
+//          the same lines of DRIFTP/E/MU), counted while the status pass is
+//          appended to each call.
 // Integer tests on the exponent bits: no FP64 work, one read of F2.
 #include "kernels.cuh"
 
@@ -53,11 +57,15 @@ __global__ void __launch_bounds__(256) k_status(Dev d, unsigned long long* __res
     double qq = bitsd(q);
     if (threadIdx.x == 3) qq = fmax(qq, 1E-32 / d.dmu[d.npa - 1]);
     if (q != 0ULL && qq > 1.0) atomicAdd(&st[2], 1ULL);
+    if (threadIdx.x == 0) {
+      const unsigned long long nc = d.clipq[slot];
+      if (nc) atomicAdd(&st[4], nc);
+    }
   }
 }
 
 void launch_status(const Dev& d, unsigned long long* st, cudaStream_t s) {
-  cudaMemsetAsync(st, 0, 3 * sizeof(unsigned long long), s);
+  cudaMemsetAsync(st, 0, 5 * sizeof(unsigned long long), s);
   cudaMemsetAsync(st + 3, 0xff, sizeof(unsigned long long), s);
   if (d.nitems == 0) return;
   long long gx = (d.ncell + 256LL * 16 - 1) / (256LL * 16);  // 16 cells per thread

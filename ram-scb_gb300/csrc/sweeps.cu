@@ -37,12 +37,13 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
     const int m = item.x, s = item.y, slot = m * d.ns + s;
     const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
     unsigned long long q = 0ULL;  // CFL quotient bits
+    unsigned nclip = 0;  // clip events (kRec == kRecCount)
     if (line < nlines) {
       const int j = line % nt;
       const int l = line / (nt * ne);
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + (long long)line * nr;
       // branch record of the frozen-limiter adjoint: one byte per face/cell
-      unsigned char* __restrict__ rl = kRec ? rec + (u / bpi) * d.ncell + (long long)line * nr : nullptr;
+      unsigned char* __restrict__ rl = (kRec == 1 || kRec == 2) ? rec + (u / bpi) * d.ncell + (long long)line * nr : nullptr;
       // face coefficients C and CORR factor a: stored by the forward sweep,
       // read back by the reverse one (same DTs, same potential)
       double* __restrict__ cst = kCo ? coef_ptr(d, 0, 0, u / bpi) + (long long)line * nr : nullptr;
@@ -93,6 +94,7 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
         const double phi = mul_rn_int(c, fb);
         const double raw = (g0 - phi) + phi_prev;
         fl[f - 1] = (kRec == 2) ? clip_frozen(raw, rl[f - 1]) : clip(raw);
+        if (kRec == kRecCount) nclip += is_neg(raw);
         if (kRec == 1) rl[f - 1] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         gm = g0; g0 = gp; gp = gpp;
@@ -113,8 +115,10 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
       const double phin = cN * fbn;
       const double rawn = (g0 - phin) + phi_prev;
       fl[nr - 1] = (kRec == 2) ? clip_frozen(rawn, rl[nr - 1]) : clip(rawn);
+      if (kRec == kRecCount) nclip += is_neg(rawn);
       if (kRec == 1) rl[nr - 1] = (unsigned char)(csn | (is_neg(rawn) ? kClipBit : 0));
     }
+    if (kRec == kRecCount) warp_atomic_add(&d.clipq[slot], nclip);
     if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 0], q);
   }
 }
@@ -135,6 +139,7 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
     const int m = item.x, s = item.y, slot = m * d.ns + s;
     const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
     unsigned long long q = 0ULL;  // CFL quotient bits
+    unsigned nclip = 0;  // clip events (kRec == kRecCount)
     if (line < nlines) {
       const int i = 1 + line % (nr - 1);
       const int kl = line / (nr - 1);
@@ -142,7 +147,7 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
       const long long st = nr;  // stride between consecutive J
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + ((long long)kl * nt) * nr + i;
       unsigned char* __restrict__ rl =
-          kRec ? rec + (u / bpi) * d.ncell + ((long long)kl * nt) * nr + i : nullptr;
+          (kRec == 1 || kRec == 2) ? rec + (u / bpi) * d.ncell + ((long long)kl * nt) * nr + i : nullptr;
       double* __restrict__ cst = kCo ? coef_ptr(d, 1, 0, u / bpi) + ((long long)kl * nt) * nr + i : nullptr;
       double* __restrict__ ast = kCo ? coef_ptr(d, 1, 1, u / bpi) + ((long long)kl * nt) * nr + i : nullptr;
       const double* __restrict__ gpt = d.gpt + ((long long)l * nt) * nr + i;
@@ -199,13 +204,14 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
         const double a = (kCo == 2) ? ast[(long long)(J - 1) * st] : fma(c, -0.5, neg ? -0.5 : 0.5);
         if (kCo == 1) { cst[(long long)(J - 1) * st] = c; ast[(long long)(J - 1) * st] = a; }
         int cs;
-        const unsigned char* rj = kRec ? rl + (long long)(J - 1) * st : nullptr;
+        const unsigned char* rj = (kRec == 1 || kRec == 2) ? rl + (long long)(J - 1) * st : nullptr;
         const double fb = (kRec == 2)
             ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rj & 7)
             : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         const double phi = mul_rn_int(c, fb);
         const double raw = (g0 - phi) + phi_prev;
         GJ(J) = (kRec == 2) ? clip_frozen(raw, *rj) : clip(raw);
+        if (kRec == kRecCount) nclip += is_neg(raw);
         if (kRec == 1) rl[(long long)(J - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         g0 = gp; gp = gpp;
@@ -214,12 +220,14 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
       }
       const double rawN = (GN - phiN) + phi_prev;
       const double vN = (kRec == 2) ? clip_frozen(rawN, rl[(long long)(nt - 1) * st]) : clip(rawN);
+      if (kRec == kRecCount) nclip += is_neg(rawN);
       GJ(nt) = vN;
       GJ(1) = vN;
       if (kRec == 1) rl[(long long)(nt - 1) * st] = (unsigned char)(csN | (is_neg(rawN) ? kClipBit : 0));
   #undef GJ
   #undef CJ
     }
+    if (kRec == kRecCount) warp_atomic_add(&d.clipq[slot], nclip);
     if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 1], q);
   }
 }
@@ -241,6 +249,7 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
     const int m = item.x, s = item.y, slot = m * d.ns + s;
     const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
     unsigned long long q = 0ULL;  // CFL quotient bits
+    unsigned nclip = 0;  // clip events (kRec == kRecCount)
     if (line < nlines) {
       const int i = 1 + line % (nr - 1);
       const int jl = line / (nr - 1);
@@ -248,7 +257,7 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
       const long long st = (long long)nt * nr;  // stride between consecutive K
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + ((long long)l * ne * nt + j) * nr + i;
       unsigned char* __restrict__ rl =
-          kRec ? rec + (u / bpi) * d.ncell + ((long long)l * ne * nt + j) * nr + i : nullptr;
+          (kRec == 1 || kRec == 2) ? rec + (u / bpi) * d.ncell + ((long long)l * ne * nt + j) * nr + i : nullptr;
       double* __restrict__ cst =
           kCo ? coef_ptr(d, 2, 0, u / bpi) + ((long long)l * ne * nt + j) * nr + i : nullptr;
       double* __restrict__ ast =
@@ -299,7 +308,7 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
         const double a = (kCo == 2) ? ast[(long long)(K - 1) * st] : fma(c, mhde[K - 1], neg ? -0.5 : 0.5);
         if (kCo == 1) { cst[(long long)(K - 1) * st] = c; ast[(long long)(K - 1) * st] = a; }
         int cs;
-        const unsigned char* rk = kRec ? rl + (long long)(K - 1) * st : nullptr;
+        const unsigned char* rk = (kRec == 1 || kRec == 2) ? rl + (long long)(K - 1) * st : nullptr;
         double fb = (kRec == 2) ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rk & 7)
                                 : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         if (closed && K == ne) fb = 0.0;
@@ -308,6 +317,7 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
         const double phi = (kCo == 2) ? __dmul_rn(c, fb) : mul_rn_int(c, fb);
         const double raw = fma(phi_prev - phi, iwe[K - 1], g0);
         GK(K) = (kRec == 2) ? clip_frozen(raw, *rk) : clip(raw);
+        if (kRec == kRecCount) nclip += is_neg(raw);
         if (kRec == 1) rl[(long long)(K - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         g0 = gp; gp = gpp;
@@ -316,6 +326,7 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
   #undef GK
   #undef CK
     }
+    if (kRec == kRecCount) warp_atomic_add(&d.clipq[slot], nclip);
     if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 2], q);
   }
 }
@@ -351,6 +362,7 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
     const int line = (int)(u % bpi) * lpb + (int)threadIdx.x / kSplit;
     const bool active = line < nlines;
     unsigned long long q = 0ULL;  // CFL quotient bits
+    unsigned nclip = 0;  // clip events (kRec == kRecCount)
     const int lc = active ? line : 0;
     const int i = 1 + lc % (nr - 1);
     const int jk = lc / (nr - 1);
@@ -358,7 +370,7 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
     const long long st = (long long)ne * nt * nr;  // stride between consecutive L
     const long long off = (long long)jk * nr + i;  // (K*NT + J)*NR + I
     double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + off;
-    unsigned char* __restrict__ rl = kRec ? rec + (u / bpi) * d.ncell + off : nullptr;
+    unsigned char* __restrict__ rl = (kRec == 1 || kRec == 2) ? rec + (u / bpi) * d.ncell + off : nullptr;
     double* __restrict__ cst = kCo ? coef_ptr(d, 3, 0, u / bpi) + off : nullptr;
     double* __restrict__ ast = kCo ? coef_ptr(d, 3, 1, u / bpi) + off : nullptr;
     const double* __restrict__ la = lossA ? lossA + (long long)s * d.ncell + off : nullptr;
@@ -433,13 +445,14 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         const double a = (kCo == 2) ? ast[(long long)(L - 1) * st] : fma(c, mhdmu[L - 1], neg ? -0.5 : 0.5);
         if (kCo == 1) { cst[(long long)(L - 1) * st] = c; ast[(long long)(L - 1) * st] = a; }
         int cs;
-        const unsigned char* rq = kRec ? rl + (long long)(L - 1) * st : nullptr;
+        const unsigned char* rq = (kRec == 1 || kRec == 2) ? rl + (long long)(L - 1) * st : nullptr;
         const double fb = (kRec == 2) ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rq & 7)
                                       : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         const double phi = mul_rn_int(c, fb);
         const double raw = fma(phi_prev - phi, iwmu[L - 1], g0);
         if (kRec == 1) rl[(long long)(L - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
         double v = (kRec == 2) ? clip_frozen(raw, *rq) : clip(raw);
+        if (kRec == kRecCount) nclip += is_neg(raw);
         if (kLoss == 1) v *= LA(L);
         GL(L) = v;
         phi_prev = phi;
@@ -456,6 +469,7 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         const double raw = fma(phi_prev - phi, iwmu[L - 1], g0);
         if (kRec == 1) rl[(long long)(L - 1) * st] = (unsigned char)(is_neg(raw) ? kClipBit : 0);
         const double v = (kRec == 2) ? clip_frozen(raw, rl[(long long)(L - 1) * st]) : clip(raw);
+        if (kRec == kRecCount) nclip += is_neg(raw);
         const double vN = v * d.rho[fij];
         if (kLoss == 1) {
           GL(L) = v * LA(L);
@@ -470,6 +484,7 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
   #undef LA
   #undef GLS
   #undef CL
+    if (kRec == kRecCount) warp_atomic_add(&d.clipq[slot], nclip);
     if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 3], q);
   }
 }
@@ -496,40 +511,55 @@ static inline int nlines_of(const Dev& d, int w) {
 void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay, int co) {
   dim3 g = grid_for(d, 0, nlines_of(d, 0));
   const int b = d.blk[0];
+  const bool n = d.count_clips;
   if (rec && replay) k_sweep_r<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec);
   else if (rec) k_sweep_r<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec);
-  else if (co == 1) k_sweep_r<true, 0, 1><<<g, b, 0, st>>>(d, dts, nullptr);
-  else if (co == 2) k_sweep_r<false, 0, 2><<<g, b, 0, st>>>(d, dts, nullptr);
-  else if (cfl) k_sweep_r<true, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr);
-  else k_sweep_r<false, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (co == 1) (n ? k_sweep_r<true, 3, 1> : k_sweep_r<true, 0, 1>)<<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (co == 2) (n ? k_sweep_r<false, 3, 2> : k_sweep_r<false, 0, 2>)<<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (cfl) (n ? k_sweep_r<true, 3, 0> : k_sweep_r<true, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr);
+  else (n ? k_sweep_r<false, 3, 0> : k_sweep_r<false, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr);
 }
 void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay, int co) {
   dim3 g = grid_for(d, 1, nlines_of(d, 1));
   const int b = d.blk[1];
+  const bool n = d.count_clips;
   if (rec && replay) k_sweep_p<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec);
   else if (rec) k_sweep_p<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec);
-  else if (co == 1) k_sweep_p<true, 0, 1><<<g, b, 0, st>>>(d, dts, nullptr);
-  else if (co == 2) k_sweep_p<false, 0, 2><<<g, b, 0, st>>>(d, dts, nullptr);
-  else if (cfl) k_sweep_p<true, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr);
-  else k_sweep_p<false, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (co == 1) (n ? k_sweep_p<true, 3, 1> : k_sweep_p<true, 0, 1>)<<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (co == 2) (n ? k_sweep_p<false, 3, 2> : k_sweep_p<false, 0, 2>)<<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (cfl) (n ? k_sweep_p<true, 3, 0> : k_sweep_p<true, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr);
+  else (n ? k_sweep_p<false, 3, 0> : k_sweep_p<false, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr);
 }
 void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay, int co) {
   dim3 g = grid_for(d, 2, nlines_of(d, 2));
   const int b = d.blk[2];
+  const bool n = d.count_clips;
   if (rec && replay) k_sweep_e<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec);
   else if (rec && co == 1) k_sweep_e<false, 1, 1><<<g, b, 0, st>>>(d, dts, rec);
   else if (rec && co == 2) k_sweep_e<false, 1, 2><<<g, b, 0, st>>>(d, dts, rec);
   else if (rec) k_sweep_e<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec);
-  else if (co == 1) k_sweep_e<true, 0, 1><<<g, b, 0, st>>>(d, dts, nullptr);
-  else if (co == 2) k_sweep_e<false, 0, 2><<<g, b, 0, st>>>(d, dts, nullptr);
-  else if (cfl) k_sweep_e<true, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr);
-  else k_sweep_e<false, 0, 0><<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (co == 1) (n ? k_sweep_e<true, 3, 1> : k_sweep_e<true, 0, 1>)<<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (co == 2) (n ? k_sweep_e<false, 3, 2> : k_sweep_e<false, 0, 2>)<<<g, b, 0, st>>>(d, dts, nullptr);
+  else if (cfl) (n ? k_sweep_e<true, 3, 0> : k_sweep_e<true, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr);
+  else (n ? k_sweep_e<false, 3, 0> : k_sweep_e<false, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr);
 }
+// The clip-counting forms of the plain (unrecorded) pitch-angle sweeps.
+template <int kLoss, int kS>
+static void mu_count(const Dev& d, dim3 g, int b, double dts, const double* loss, cudaStream_t st, bool cfl,
+                     int co) {
+  if (co == 1) k_sweep_mu<true, kLoss, 3, 1, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+  else if (co == 2) k_sweep_mu<false, kLoss, 3, 2, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+  else if (cfl) k_sweep_mu<true, kLoss, 3, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+  else k_sweep_mu<false, kLoss, 3, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+}
+
 template <int kLoss, int kS>
 static void mu_launch(const Dev& d, dim3 g, int b, double dts, const double* loss, cudaStream_t st,
                       unsigned char* rec, bool replay, bool cfl, int co) {
+  const bool n = d.count_clips;
   if (rec && replay) k_sweep_mu<false, kLoss, 2, 0, kS><<<g, b, 0, st>>>(d, dts, loss, rec);
   else if (rec) k_sweep_mu<false, kLoss, 1, 0, kS><<<g, b, 0, st>>>(d, dts, loss, rec);
+  else if (n) mu_count<kLoss, kS>(d, g, b, dts, loss, st, cfl, co);
   else if (co == 1) k_sweep_mu<true, kLoss, 0, 1, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
   else if (co == 2) k_sweep_mu<false, kLoss, 0, 2, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
   else if (cfl) k_sweep_mu<true, kLoss, 0, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);

@@ -41,7 +41,7 @@ module ModRamGpu
   ! device status word (ramgpu_check): replaces the stop in ANISCH
   ! (src/ModRamRun.f90:410-413) with a return code the caller acts on
   type, bind(C) :: ramgpu_status
-     integer(c_long_long) :: f2_nonfinite, moments_nonfinite, cfl_over
+     integer(c_long_long) :: f2_nonfinite, moments_nonfinite, cfl_over, clips
      integer(c_int)       :: first_member, first_species
   end type ramgpu_status
 

@@ -58,7 +58,8 @@ class RamGpuError(RuntimeError):
 class Status(C.Structure):
     """ramgpu_status: the device status word."""
     _fields_ = [("f2_nonfinite", C.c_longlong), ("moments_nonfinite", C.c_longlong),
-                ("cfl_over", C.c_longlong), ("first_member", C.c_int), ("first_species", C.c_int)]
+                ("cfl_over", C.c_longlong), ("clips", C.c_longlong), ("first_member", C.c_int),
+                ("first_species", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -44,7 +44,7 @@ def test_healthy_state(tiny):
     gpu = _gpu(tiny)
     try:
         st = gpu.check()
-        assert st == {"f2_nonfinite": 0, "moments_nonfinite": 0, "cfl_over": 0,
+        assert st == {"f2_nonfinite": 0, "moments_nonfinite": 0, "cfl_over": 0, "clips": 0,
                       "first_member": -1, "first_species": -1}
         gpu.ram_run(tiny.dts)
         st = gpu.check()
@@ -114,5 +114,32 @@ def test_check_in_host_pipeline_and_courant(tiny):
         assert gpu.last_status()["f2_nonfinite"] == int(np.sum(~np.isfinite(f2[1])))
         gpu.set_check(False)
         gpu.ram_run(wl.dts)  # no pass appended: the call itself does not raise
+    finally:
+        gpu.close()
+
+
+def test_clip_count_matches_recorded_clip_bits(tiny):
+    """The sweeps' clip count of a call (check on) equals the clip bits the
+    adjoint's recording forward writes for the same call from the same
+    state: one bit per updated cell that came out negative."""
+    wl = tiny
+    ns = len(wl.grid.species)
+    gpu = _gpu(wl)
+    big = 40.0 * wl.dts  # Courant numbers above 1: the update can undershoot
+    try:
+        gpu.adj_forward(1, big, [3.0], 1, [])
+        rec = gpu.adj_record(0, ns)
+        want = int(np.sum((rec & 8) != 0))
+        for s in range(ns):
+            gpu.upload_f2(0, s, wl.f2[s])
+        gpu.set_check(True)
+        gpu.set_kp(0, 3.0)
+        gpu.ram_run(big)
+        st = gpu.last_status()
+        assert want > 0 and st["clips"] == want
+        # with the check off the sweeps do not count
+        gpu.set_check(False)
+        gpu.ram_run(big)
+        assert gpu.check()["clips"] == 0
     finally:
         gpu.close()
