@@ -1,14 +1,27 @@
 // abi.cu -- the extern "C" entry points declared in include/ramgpu.h.
 //
 // The context owns every device buffer.  ramgpu_ram_run enqueues, per call,
-//   member tables (VT, E x B, U terms)   2 kernels
-//   DRIFTR ghost planes + scan           2
+//   member tables (VT, E x B, U terms) and DRIFTR ghost planes   2 kernels
+//   "last inflow line" scan of the stale DRIFTR ghosts           1
+// and then, for each item group (a slice of the active (member, species)
+// list, on its own stream; 1 to 8 groups, autotuned):
 //   R, P, E, MU (+ fused CEX/ATMOL)      4   (forward half, CFL tracked)
 //   MU, E, P, R                          4   (reverse half)
 //   periodic copy + magnetopause mask    1
 //   ANISCH moments                       2
-// for all active (member, species) items in one launch each, mirroring the
-// species loop of src/ModRamRun.f90:64-222.
+// mirroring the species loop of src/ModRamRun.f90:64-222; optionally the
+// status pass (1).  The whole call is one CUDA graph when graphs are on.
+//
+// Sections, in order:
+//   context        struct ramgpu_ctx, error and allocation helpers,
+//                  work-list rebuild and the per-DTs tables (prepare)
+//   step           the sweep sequence, item groups on concurrent streams,
+//                  the status pass, the graph of ram_run
+//   adjoint calls  recorded and replayed calls, checkpoint copies
+//   host pipeline  ramgpu_ram_run_host's uploads / sweeps / read-backs
+//   ABI            the entry points: lifecycle, inputs, state transfer,
+//                  runs, outputs, tuning, outputs for satellites and SCB,
+//                  the adjoint window, diagnostics
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
