@@ -2170,6 +2170,9 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
   const size_t isz = (size_t)d.nitems * d.ncell;
   const int G = clamp_groups(ctx, ctx->step_groups);
   if ((rc = ensure_group_streams(ctx, G))) return rc;
+  // the first DRIFTE transpose of each call keeps its face coefficients in
+  // the DRIFTE coefficient store for the second
+  const int co_e = (d.coef && d.coef_slot[2] >= 0) ? 1 : 0;
   CK(cudaMemsetAsync(d.lam, 0, sizeof(double) * nslot * d.ncell, ctx->stream));
   CK(cudaMemsetAsync(d.gfg, 0, sizeof(double) * nslot * nfg, ctx->stream));
   for (int seg = a.nseg - 1; seg >= 0; --seg) {
@@ -2200,11 +2203,11 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
         launch_adj_tail(dg, st);
         launch_adj_sweep(dg, 0, r + 7 * isz, st);
         launch_adj_sweep(dg, 1, r + 6 * isz, st);
-        launch_adj_sweep(dg, 2, r + 5 * isz, st);
+        launch_adj_sweep(dg, 2, r + 5 * isz, st, co_e);
         launch_adj_sweep(dg, 3, r + 4 * isz, st);
         launch_scale_lam(dg, dg.loss2, st);
         launch_adj_sweep(dg, 3, r + 3 * isz, st);
-        launch_adj_sweep(dg, 2, r + 2 * isz, st);
+        launch_adj_sweep(dg, 2, r + 2 * isz, st, 2 * co_e);
         launch_adj_sweep(dg, 1, r + 1 * isz, st);
         launch_adj_sweep(dg, 0, r + 0 * isz, st);
         ctx->launches += 11;

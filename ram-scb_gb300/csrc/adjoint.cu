@@ -267,6 +267,12 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
 // Cells 0..NE+2: G(1) = kap1 F(2) and G(0) = kap0 G(1) are extrapolated,
 // G(NE+1) = G(NE+2) = 0; faces 1..NE (not 1 and NE when closed); cell 1
 // is never updated (NE >= 6).
+// kCo: 0 compute the face coefficients C, 1 compute and keep them in the
+// DRIFTE coefficient store, 2 read them from it.  A call's two DRIFTE
+// transposes (of the reverse and the forward half) share C (same DTs and
+// potential), so the first keeps it for the second, as the forward sweeps
+// do; the stored value is the recomputed one, so the results do not change.
+template <int kCo>
 __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * nt * d.npa;
@@ -282,6 +288,7 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
     const long long base = ((long long)l * ne * nt + j) * nr + i;
     double* __restrict__ lam = d.lam + (long long)slot * d.ncell + base;
     const unsigned char* __restrict__ rl = rec + (u / bpi) * d.ncell + base;
+    double* __restrict__ cst = kCo ? coef_ptr(d, 2, 0, u / bpi) + base : nullptr;
     const long long fij = ((long long)l * nt + j) * nr + i;
     const double wet = d.wet[fij];
     const double ue = d.ue[(long long)m * nr * nt * d.npa + fij];
@@ -298,7 +305,8 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
     double wl0 = 0.0, wl1 = le2 * d.iwe[1], wl2 = le3 * d.iwe[2];
     double cm1 = 0.0, c0 = 0.0, c1 = le2, c2 = le3;
     auto face = [&](int K) {
-      const double C = EC(K);
+      const double C = (kCo == 2) ? cst[(long long)(K - 1) * st] : EC(K);
+      if (kCo == 1) cst[(long long)(K - 1) * st] = C;
       const bool neg = is_neg(C);
       const int cs = rl[(long long)(K - 1) * st] & 7;
       face_acc(C * (wl1 - wl0), neg, cs, face_ak<true>(C, neg, cs, d.mhde[K - 1], d.bmhde[K - 1], hb), cm1, c0,
@@ -417,7 +425,7 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
   }
 }
 
-void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_t st) {
+void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_t st, int co) {
   const int blk = 128;
   int nl;
   switch (w) {
@@ -433,7 +441,11 @@ void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_
       else k_adj_r<false><<<g, blk, 0, st>>>(d, rec);
       break;
     case 1: k_adj_p<<<g, blk, 0, st>>>(d, rec); break;
-    case 2: k_adj_e<<<g, blk, 0, st>>>(d, rec); break;
+    case 2:
+      if (co == 1) k_adj_e<1><<<g, blk, 0, st>>>(d, rec);
+      else if (co == 2) k_adj_e<2><<<g, blk, 0, st>>>(d, rec);
+      else k_adj_e<0><<<g, blk, 0, st>>>(d, rec);
+      break;
     default: k_adj_mu<<<g, blk, 0, st>>>(d, rec); break;
   }
 }

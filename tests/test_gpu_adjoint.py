@@ -250,6 +250,25 @@ def test_item_groups_same_window(case, groups):
         model.set_step_groups(g0)
 
 
+def test_drifte_transpose_store_same_bits(case):
+    """The first DRIFTE transpose of each call keeps its face coefficients
+    for the second (the DRIFTE coefficient store): the same dJ/dF2 bits as
+    recomputing them (dJ/dFGEOS to rounding order: it sums with atomics)."""
+    wl, model, kp, obs, J0, _, gf, gb = case
+    ns = len(wl.grid.species)
+    try:
+        model.set_coef_store(0)
+        _set_f2(model, wl, [1.0] * ns)
+        J1 = model.adj_forward(NCALLS, wl.dts, kp, 2, obs)
+        gf1, gb1 = model.adj_backward()
+        assert J1[0] == J0[0]
+        assert np.array_equal(gf1, gf)
+        assert np.max(np.abs(gb1 - gb)) <= 1e-13 * np.max(np.abs(gb))
+    finally:
+        model.set_coef_store(4)
+        _set_f2(model, wl, [1.0] * ns)
+
+
 def test_batched_gradients_equal_solo(tiny):
     lists = [[0, 1, 2, 3], [1, 3], [2]]
     model, kp, obs = make_case(tiny, 3, 3, 24, seed=21, species_lists=lists)
