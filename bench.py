@@ -168,11 +168,12 @@ def cpu_threads(ns):
     return outer, max(1, cores // outer)
 
 
-def cpu_time_oracle(wl, seconds, nthreads, inner=1):
+def cpu_time_oracle(wl, seconds, nthreads, inner=1, calls=None, warmup=1):
     """Time the CPU oracle (the reference's routines restated in C, species
     loop under OpenMP like the reference, `inner` threads over independent
-    lines inside each routine) on this workload; returns (cell-updates/s,
-    calls, elapsed)."""
+    lines inside each routine) on this workload: `warmup` untimed calls,
+    then `calls` timed ones (or as many as fit in `seconds`); returns
+    (cell-updates/s, calls, elapsed)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import numpy as np
     import pyoracle
@@ -181,13 +182,14 @@ def cpu_time_oracle(wl, seconds, nthreads, inner=1):
     o = pyoracle.Oracle(wl.grid, wl.fields)
     f2 = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
     cells = 2 * wl.grid.ncell * len(wl.grid.species)
-    o.ram_run(f2, wl.fgeos, wl.dts, kp=wl.kp(0), nthreads=nthreads)  # warm-up
+    for w in range(max(0, warmup)):
+        o.ram_run(f2, wl.fgeos, wl.dts, kp=wl.kp(2 * w), nthreads=nthreads)
     n, t0 = 0, time.perf_counter()
     while True:
-        o.ram_run(f2, wl.fgeos, wl.dts, kp=wl.kp(2 * n), nthreads=nthreads)
+        o.ram_run(f2, wl.fgeos, wl.dts, kp=wl.kp(2 * (warmup + n)), nthreads=nthreads)
         n += 1
         el = time.perf_counter() - t0
-        if el >= seconds or n >= 1000:
+        if (calls is not None and n >= calls) or (calls is None and (el >= seconds or n >= 1000)):
             break
     pyoracle.set_inner_threads(1)
     return cells * n / el, n, el
@@ -201,13 +203,14 @@ def run_reference(args, rank, world):
     wl = W.make_workload(args.workload)
     ns = len(wl.grid.species)
     outer, inner = cpu_threads(ns)
-    budget = max(5.0, min(60.0, 0.4 * max(args.steps, 1)))
-    v, n, el = cpu_time_oracle(wl, budget, outer, inner)
-    sample = (f"{n} ram_run calls of the workload ({workload_desc(wl)}), {el:.1f} s; "
-              f"C restatement of the reference routines (no Fortran compiler), OpenMP over "
-              f"{outer} species x {inner} line threads")
+    # W untimed warm-up steps, then exactly K timed steps; a step is one
+    # ram_run call of the workload (about 0.3 s on 16 host cores)
+    v, n, el = cpu_time_oracle(wl, 0.0, outer, inner, calls=max(1, args.steps), warmup=args.warmup)
+    sample = (f"{n} ram_run calls of the workload ({workload_desc(wl)}) after {args.warmup} warm-up "
+              f"calls, {el:.1f} s; C restatement of the reference routines (no Fortran compiler), "
+              f"OpenMP over {outer} species x {inner} line threads")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": n, "warmup": 1, "ms_per_step": 1e3 * el / n, "higher_is_better": True,
+            "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * el / n, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": workload_desc(wl), "step": "one ram_run call (2 DTs steps)"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": outer * inner, "kind": "port",
