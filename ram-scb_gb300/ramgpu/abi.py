@@ -164,7 +164,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_compute_hI": ([vp, i, dp, dp, dp, dp, dp, dp, i, dp, dp, d, d], i),
         "ramgpu_get_fields": ([vp] + [dp] * 11, i),
         "ramgpu_sum_pressure": ([vp, i, dp, dp], i),
-        "ramgpu_ram_run_host": ([vp, d, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)], i),
+        "ramgpu_ram_run_host": ([vp, d, vp, vp, vp], i),
         "ramgpu_set_pipeline_groups": ([vp, i], i),
         "ramgpu_pipeline_groups": ([vp], i),
         "ramgpu_set_step_groups": ([vp, i], i),
@@ -230,6 +230,7 @@ class RamGpu:
         self.ns = len(grid.species)
         self.n_members = n_members
         self.fraccfl = fraccfl
+        self._host_tables = None  # ram_run_host's address tables of the last buffer set
         self.member_species = [list(range(self.ns)) for _ in range(n_members)]
         cfg = Config(grid.nr, grid.nt, grid.ne, grid.npa, self.ns, n_members, betalim, fraccfl,
                      dtsmin, flags)
@@ -253,6 +254,7 @@ class RamGpu:
             raise RamGpuError(f"{what}: {ERRORS.get(rc, rc)}: {buf.value.decode()}", code=rc)
 
     def close(self):
+        self._host_tables = None
         if getattr(self, "h", None):
             self.lib.ramgpu_destroy(self.h)
             self.h = None
@@ -345,28 +347,41 @@ class RamGpu:
         (resp. NR*NT) values in the layout of upload_f2 / moments."""
         g = self.grid
         nslot = self.n_members * self.ns
+        seqs = tuple(None if q is None else list(q) for q in (f2, ppert, ppart))
+        # the address tables of the last buffer set are kept with references
+        # to its arrays (so their ids cannot be reused): a call with the same
+        # arrays, the usual case from a time loop, skips rebuilding them
+        key = tuple(None if q is None else tuple(map(id, q)) for q in seqs)
+        hit = self._host_tables is not None and self._host_tables[0] == key
+        if hit:
+            tabs = self._host_tables[1]
+            sizes = (g.nr * g.nt * g.ne * g.npa, g.nr * g.nt, g.nr * g.nt)
+            hit = all(a is None or (a.flags.writeable and a.size == n)
+                      for q, n in zip(seqs, sizes) if q is not None for a in q)
+        if not hit:
+            vtab = C.c_void_p * nslot
 
-        def table(seq, n, what):
-            if seq is None:
-                return None
-            seq = list(seq)
-            if len(seq) != nslot:
-                raise RamGpuError(f"{what}: need {nslot} entries (member*NS + species)")
-            ptrs = (_P * nslot)()
-            for k, a in enumerate(seq):
-                if a is None:
-                    continue
-                if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.size == n
-                        and a.flags.writeable and (a.flags.f_contiguous or a.flags.c_contiguous)):
-                    raise RamGpuError(f"{what}[{k}]: need a contiguous writable float64 array of {n} values")
-                ptrs[k] = a.ctypes.data_as(_P)
-            return ptrs
+            def table(seq, n, what):
+                if seq is None:
+                    return None
+                if len(seq) != nslot:
+                    raise RamGpuError(f"{what}: need {nslot} entries (member*NS + species)")
+                addrs = []
+                for k, a in enumerate(seq):
+                    if a is None:
+                        addrs.append(None)
+                        continue
+                    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.size == n
+                            and a.flags.writeable and (a.flags.f_contiguous or a.flags.c_contiguous)):
+                        raise RamGpuError(f"{what}[{k}]: need a contiguous writable float64 array of {n} values")
+                    addrs.append(a.ctypes.data)
+                return vtab(*addrs)
 
-        ncell = g.nr * g.nt * g.ne * g.npa
-        t_f2 = table(f2, ncell, "f2")
-        t_pe = table(ppert, g.nr * g.nt, "ppert")
-        t_pa = table(ppart, g.nr * g.nt, "ppart")
-        self._ck(self.lib.ramgpu_ram_run_host(self.h, float(dts), t_f2, t_pe, t_pa), "ram_run_host")
+            ncell = g.nr * g.nt * g.ne * g.npa
+            tabs = (table(seqs[0], ncell, "f2"), table(seqs[1], g.nr * g.nt, "ppert"),
+                    table(seqs[2], g.nr * g.nt, "ppart"))
+            self._host_tables = (key, tabs, seqs)
+        self._ck(self.lib.ramgpu_ram_run_host(self.h, float(dts), *tabs), "ram_run_host")
 
     def set_pipeline_groups(self, groups: int):
         """Item groups ram_run_host pipelines its copies over."""
