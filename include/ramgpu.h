@@ -189,7 +189,12 @@ int ramgpu_ram_run_async(ramgpu_ctx *ctx, double dts);
  * copies of one group overlap the sweeps of the others.  ppert/ppart,
  * when not NULL, receive each item's (NR,NT) moments (NULL entries are
  * skipped), and so does f2 (a NULL entry leaves that item's F2 resident
- * and unchanged on the host side).  Returns when every copy is back. */
+ * and unchanged on the host side).  Returns when every copy is back.
+ * Each pointer set is classified (page-locked or pageable) and, with
+ * graphs on, captured on first use and reused while the same pointers come
+ * back; after re-registering memory at the same addresses
+ * (cudaHostRegister / cudaHostUnregister), call ramgpu_set_graph to drop
+ * both. */
 int ramgpu_ram_run_host(ramgpu_ctx *ctx, double dts, double *const *f2, double *const *ppert,
                         double *const *ppart);
 /* Number of item groups ramgpu_ram_run_host pipelines its copies over

@@ -119,6 +119,12 @@ struct ramgpu_ctx {
   int pipe_shape = -1, pipe_g = 0;
   std::vector<cudaStream_t> pipe_streams;
   std::vector<cudaEvent_t> pipe_events;  // per group: uploads done, group done; then one for the tables
+  // host pointer classification of the last ramgpu_ram_run_host pointer set:
+  // per pointer, pageable memory the SMs copy; any pageable pointer the copy
+  // engines must move (no graph then)
+  std::vector<const void*> cls_key;
+  std::vector<char> cls_pageable;
+  bool cls_engine_pageable = false;
   // status word: device words and their page-locked copy; the pass is
   // appended to every call while check_on
   unsigned long long* status_d = nullptr;
@@ -1315,7 +1321,6 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
   // engines (not capturable).
   const int nslot = ctx->d.nm * ctx->d.ns;
   std::vector<const void*> key;
-  std::vector<char> pageable;
   bool capturable = ctx->graph_on && !ctx->pipe_trace;  // a traced call runs direct
   if (ctx->pipe_trace) {
     while ((int)ctx->trace_ev.size() < 1 + 3 * G) {
@@ -1325,13 +1330,17 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
     }
     ctx->trace_ms.clear();
   }
-  int dev = 0, pma = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev);
-  for (double* const* tab : {f2, ppert, ppart}) {
-    for (int k = 0; k < nslot; ++k) {
-      const void* p = tab ? (const void*)tab[k] : nullptr;
-      key.push_back(p);
+  for (double* const* tab : {f2, ppert, ppart})
+    for (int k = 0; k < nslot; ++k) key.push_back(tab ? (const void*)tab[k] : nullptr);
+  // the classification of the last pointer set is kept (a time loop passes
+  // the same buffers every call)
+  if (key != ctx->cls_key) {
+    int dev = 0, pma = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev);
+    ctx->cls_pageable.clear();
+    ctx->cls_engine_pageable = false;
+    for (const void* p : key) {
       bool pg = false;
       if (p) {
         cudaPointerAttributes at{};
@@ -1340,11 +1349,14 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
           at.type = cudaMemoryTypeUnregistered;
         }
         pg = at.type == cudaMemoryTypeUnregistered;
-        if (pg && !pma) capturable = false;
+        if (pg && !pma) ctx->cls_engine_pageable = true;
       }
-      pageable.push_back(pg && pma ? 1 : 0);
+      ctx->cls_pageable.push_back(pg && pma ? 1 : 0);
     }
+    ctx->cls_key = key;
   }
+  const std::vector<char>& pageable = ctx->cls_pageable;
+  if (ctx->cls_engine_pageable) capturable = false;
   if (!capturable) {
     rc = enqueue_pipeline(ctx, dts, f2, ppert, ppart, G, pageable);
     if (!rc && ctx->check_on) rc = enqueue_status(ctx);
@@ -1661,6 +1673,11 @@ int ramgpu_set_graph(ramgpu_ctx* ctx, int enable) {
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
   ctx->graph_on = enable != 0;
   if (!ctx->graph_on) drop_graph(ctx);
+  // the host pipeline's graph and pointer classification are rebuilt on
+  // the next ramgpu_ram_run_host
+  if (ctx->pipe_exec) cudaGraphExecDestroy(ctx->pipe_exec);
+  ctx->pipe_exec = nullptr;
+  ctx->cls_key.clear();
   return RAMGPU_OK;
 }
 
