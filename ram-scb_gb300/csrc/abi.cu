@@ -119,6 +119,11 @@ struct ramgpu_ctx {
   int pipe_shape = -1, pipe_g = 0;
   std::vector<cudaStream_t> pipe_streams;
   std::vector<cudaEvent_t> pipe_events;  // per group: uploads done, group done; then one for the tables
+  // per group: a companion stream for the F2 read-back, the event after the
+  // closing mask it starts from, and its completion
+  std::vector<cudaStream_t> pipe_copy_streams;
+  std::vector<cudaEvent_t> pipe_fin_events, pipe_copy_done;
+  cudaEvent_t finish_hook = nullptr;  // recorded after the closing mask when set
   // host pointer classification of the last ramgpu_ram_run_host pointer set:
   // per pointer, pageable memory the SMs copy; any pageable pointer the copy
   // engines must move (no graph then)
@@ -414,6 +419,7 @@ static int enqueue_sweeps(ramgpu_ctx* ctx, double dts, bool clear_cfl) {
     if ((rc = sumrc_stage(ctx, 5, 1))) return rc;
   }
   { Timed t(ctx, 6); launch_finish(ctx->d, ctx->stream); }
+  if (ctx->finish_hook) CK(cudaEventRecord(ctx->finish_hook, ctx->stream));
   { Timed t(ctx, 7); launch_moments(ctx->d, ctx->stream); }
   ctx->launches += 3;
   CKL("finish/moments");
@@ -702,6 +708,19 @@ static int ensure_group_streams(ramgpu_ctx* ctx, int G) {
     CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     ctx->pipe_events.push_back(e);
   }
+  while ((int)ctx->pipe_copy_streams.size() < G) {
+    const size_t g = ctx->pipe_copy_streams.size();
+    int prio = 0;
+    CK(cudaStreamGetPriority(ctx->pipe_streams[g], &prio));
+    cudaStream_t st = nullptr;
+    CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio));
+    ctx->pipe_copy_streams.push_back(st);
+    cudaEvent_t a = nullptr, b = nullptr;
+    CK(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
+    ctx->pipe_fin_events.push_back(a);
+    ctx->pipe_copy_done.push_back(b);
+  }
   return RAMGPU_OK;
 }
 
@@ -752,21 +771,37 @@ static int enqueue_pipeline(ramgpu_ctx* ctx, double dts, double* const* f2, doub
     ctx->d.items = full.items + i0;
     ctx->d.nitems = i1 - i0;
     ctx->d.item0 = i0;
+    ctx->finish_hook = f2 ? ctx->pipe_fin_events[g] : nullptr;
     const int rc = enqueue_sweeps(ctx, dts, false);
+    ctx->finish_hook = nullptr;
     ctx->d = full;
     ctx->stream = main;
     if (rc) return rc;
     if (trace) CK(cudaEventRecord(ctx->trace_ev[2 + 3 * g], st));
-    const size_t ns2 = (size_t)full.nm * full.ns;
-    for (int it = i0; it < i1 && f2; ++it) {
-      const int slot = slot_of(it);
-      int rc2 = RAMGPU_OK;
-      if (f2[slot]) rc2 = pipe_copy(ctx, f2[slot], full.f2 + (size_t)slot * n, n, pageable[slot], st);
-      if (!rc2 && ppert && ppert[slot])
-        rc2 = pipe_copy(ctx, ppert[slot], full.ppert + (size_t)slot * nm2, nm2, pageable[ns2 + slot], st);
-      if (!rc2 && ppart && ppart[slot])
-        rc2 = pipe_copy(ctx, ppart[slot], full.ppart + (size_t)slot * nm2, nm2, pageable[2 * ns2 + slot], st);
-      if (rc2) return rc2;
+    if (f2) {
+      // F2 is final after the closing mask except its L = 1 plane, which
+      // ANISCH then overwrites (F2(:,:,:,1) = F2(:,:,:,2)): the L >= 2 part
+      // (contiguous after the first NR*NT*NE values) goes back on the
+      // companion stream while the moments run, the L = 1 plane after them
+      const size_t n1 = (size_t)full.nr * full.nt * full.ne;
+      cudaStream_t cs = ctx->pipe_copy_streams[g];
+      CK(cudaStreamWaitEvent(cs, ctx->pipe_fin_events[g], 0));
+      const size_t ns2 = (size_t)full.nm * full.ns;
+      for (int it = i0; it < i1; ++it) {
+        const int slot = slot_of(it);
+        int rc2 = RAMGPU_OK;
+        if (f2[slot]) {
+          rc2 = pipe_copy(ctx, f2[slot] + n1, full.f2 + (size_t)slot * n + n1, n - n1, pageable[slot], cs);
+          if (!rc2) rc2 = pipe_copy(ctx, f2[slot], full.f2 + (size_t)slot * n, n1, pageable[slot], st);
+        }
+        if (!rc2 && ppert && ppert[slot])
+          rc2 = pipe_copy(ctx, ppert[slot], full.ppert + (size_t)slot * nm2, nm2, pageable[ns2 + slot], st);
+        if (!rc2 && ppart && ppart[slot])
+          rc2 = pipe_copy(ctx, ppart[slot], full.ppart + (size_t)slot * nm2, nm2, pageable[2 * ns2 + slot], st);
+        if (rc2) return rc2;
+      }
+      CK(cudaEventRecord(ctx->pipe_copy_done[g], cs));
+      CK(cudaStreamWaitEvent(st, ctx->pipe_copy_done[g], 0));
     }
     if (trace) CK(cudaEventRecord(ctx->trace_ev[3 + 3 * g], st));
     CK(cudaEventRecord(ctx->pipe_events[2 * g + 1], st));
@@ -913,6 +948,9 @@ int ramgpu_destroy(ramgpu_ctx* ctx) {
   for (cudaStream_t st : ctx->pipe_streams) cudaStreamDestroy(st);
   for (cudaEvent_t e : ctx->pipe_events) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->trace_ev) cudaEventDestroy(e);
+  for (cudaStream_t st : ctx->pipe_copy_streams) cudaStreamDestroy(st);
+  for (cudaEvent_t e : ctx->pipe_fin_events) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->pipe_copy_done) cudaEventDestroy(e);
   if (ctx->status_h) cudaFreeHost(ctx->status_h);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
