@@ -1479,6 +1479,8 @@ int ramgpu_ram_run(ramgpu_ctx* ctx, double dts) {
 
 int ramgpu_check(ramgpu_ctx* ctx, ramgpu_status* st) {
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  // the pass reads the grid's DMU (the DRIFTMU CFL floor)
+  if (!ctx->have_grid) return fail(ctx, RAMGPU_ERR_STATE, "ramgpu_set_grid must be called first");
   if (ctx->items_dirty)
     if (int rc = rebuild_items(ctx)) return rc;
   if (int rc = enqueue_status(ctx)) return rc;

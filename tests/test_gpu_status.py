@@ -143,3 +143,18 @@ def test_clip_count_matches_recorded_clip_bits(tiny):
         assert gpu.check()["clips"] == 0
     finally:
         gpu.close()
+
+
+def test_check_needs_the_grid():
+    """Before ramgpu_set_grid the pass has no grid to read: a state error."""
+    import ctypes
+
+    lib = abi.load_library()
+    cfg = abi.Config(6, 9, 35, 72, 2, 1, 1.5, 0.8, 0.1, 0)
+    h = ctypes.c_void_p()
+    assert lib.ramgpu_create(ctypes.byref(cfg), ctypes.byref(h)) == abi.RAMGPU_OK
+    try:
+        st = abi.Status()
+        assert lib.ramgpu_check(h, ctypes.byref(st)) == -3
+    finally:
+        lib.ramgpu_destroy(h)
