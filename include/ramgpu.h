@@ -338,9 +338,9 @@ int ramgpu_set_graph(ramgpu_ctx *ctx, int enable);
  * a persistent grid of that many CTAs looping over (item, line-block) units. */
 int ramgpu_set_launch_shape(ramgpu_ctx *ctx, int sweep, int threads, int persistent_ctas);
 int ramgpu_get_launch_shape(ramgpu_ctx *ctx, int *threads4, int *persistent4);
-/* Lanes per DRIFTMU line: 2 (two adjacent lanes share a line, the default
- * for NPA >= 12) or 1.  Results are the same either way; the autotuner
- * tries both. */
+/* Lanes per DRIFTMU line: 4 (NPA >= 24), 2 (adjacent lanes share a line,
+ * the default for NPA >= 12) or 1.  Results are the same bit for bit; the
+ * autotuner tries each. */
 int ramgpu_set_mu_lanes(ramgpu_ctx *ctx, int lanes);
 /* Autotuner: for each sweep in turn, tries 32/64/128/256 threads per CTA,
  * each with a one-unit-per-CTA grid and a persistent grid (resident CTAs x

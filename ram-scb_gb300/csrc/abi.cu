@@ -1734,8 +1734,9 @@ int ramgpu_set_launch_shape(ramgpu_ctx* ctx, int sweep, int threads, int persist
 
 int ramgpu_set_mu_lanes(ramgpu_ctx* ctx, int lanes) {
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
-  if (lanes != 1 && lanes != 2) return fail(ctx, RAMGPU_ERR_ARG, "lanes must be 1 or 2");
+  if (lanes != 1 && lanes != 2 && lanes != 4) return fail(ctx, RAMGPU_ERR_ARG, "lanes must be 1, 2 or 4");
   if (lanes == 2 && ctx->d.npa < 12) return fail(ctx, RAMGPU_ERR_ARG, "two lanes per line need NPA >= 12");
+  if (lanes == 4 && ctx->d.npa < 24) return fail(ctx, RAMGPU_ERR_ARG, "four lanes per line need NPA >= 24");
   ctx->d.mu_lanes = lanes;
   ctx->shape_version += 1;
   return RAMGPU_OK;
@@ -1775,12 +1776,13 @@ int ramgpu_autotune(ramgpu_ctx* ctx, double dts, int reps, double* best_ms4) {
   for (int w = 0; w < 4; ++w) {
     float best = 1e30f;
     int bb = ctx->d.blk[w], bp = ctx->d.pers[w], bl = ctx->d.mu_lanes;
-    const int nlanes = (w == 3 && ctx->d.npa >= 12) ? 2 : 1;
-    for (int lanes = nlanes; lanes >= 1; --lanes)
+    // DRIFTMU: 4, 2 and 1 lanes per line, as NPA allows
+    const int nlanes = w != 3 ? 1 : (ctx->d.npa >= 24 ? 4 : (ctx->d.npa >= 12 ? 2 : 1));
+    for (int lanes = nlanes; lanes >= 1; lanes /= 2)
     for (int ib = 0; ib < 4; ++ib) {
       for (int persist = 0; persist < 2; ++persist) {
         const int blk = cand_blk[ib];
-        if (w == 3) ctx->d.mu_lanes = (nlanes == 2) ? lanes : ctx->d.mu_lanes;
+        if (w == 3) ctx->d.mu_lanes = lanes;
         int pc = 0;
         if (persist) {
           const int per_sm = sweep_max_blocks_per_sm(w, blk);

@@ -336,13 +336,16 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
 // faces 2..NPA-2, FBND(NPA-1) = F(NPA), then the F2(NPA) extrapolation.
 // kLoss: 0 none, 1 multiply the result by table lossA (loss after the sweep),
 //        2 multiply the input by lossA (loss before the sweep).
-// kSplit 2: there are few pitch-angle lines (NR-1)*NT*NE, so two adjacent
-// lanes share one: the even lane updates cells 2..Lm, the odd lane
-// Lm+1..NPA (Lm = NPA/2).  Both run the same instructions: a "pre-face"
-// (face 1, whose flux is zero, for the even lane; face Lm, recomputed bit
-// for bit from the old values, for the odd lane), then their faces.  Every
-// old value a lane needs from its partner's cells is loaded before a
-// __syncwarp, and no lane writes before it.
+// kSplit 2 or 4: there are few pitch-angle lines (NR-1)*NT*NE, so kSplit
+// adjacent lanes share one, lane q updating cells b+1..lim of segment q
+// (b = q*S, lim = (q+1)*S with S = NPA/kSplit; lane 0 from cell 2, the last
+// lane to NPA).  All run the same instructions: a "pre-face" (face 1,
+// whose flux is zero, for lane 0; face b, recomputed bit for bit from the
+// old values, for the others), then their faces.  Every old value a lane
+// needs from its neighbours' cells (its entering window and the two cells
+// past lim) is loaded before a __syncwarp, and no lane writes before it.
+// Segments keep at least 4 cells (2 lanes: NPA >= 12; 4 lanes: NPA >= 24),
+// so no lane but lane 0 sees the F(1) = F(2) rule.
 template <bool kCfl, int kLoss, int kRec, int kCo, int kSplit>
 __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const double* __restrict__ lossA,
                                                    unsigned char* __restrict__ rec) {
@@ -353,8 +356,14 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
   const int lpb = blockDim.x / kSplit;  // lines per CTA
   const int bpi = (nlines + lpb - 1) / lpb;
   const long long nunits = (long long)bpi * d.nitems;
+  // lane pairs: the even lane ends at Lm, the odd one takes the rest
   const int half = kSplit == 2 ? (int)(threadIdx.x & 1) : 0;
   const int Lm = kSplit == 2 ? npa / 2 : npa;  // last cell of the even lane
+  // four lanes: segment q4 of seg4 cells (the last one to NPA)
+  const int q4 = kSplit == 4 ? (int)(threadIdx.x & 3) : 0;
+  const int seg4 = npa / 4;
+  const int pre = kSplit == 4 ? q4 : half;  // nonzero: the pre-face is recomputed
+  const bool last = kSplit == 4 ? q4 == 3 : (half || kSplit == 1);
   for (long long u = blockIdx.x + (long long)blockIdx.y * gridDim.x; u < nunits;
        u += (long long)gridDim.x * gridDim.y) {
     const int2 item = d.items[u / bpi];
@@ -388,31 +397,31 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
   #define LA(L) la[(long long)((L)-1) * st]
   #define GLS(L) (kLoss == 2 ? GL(L) * LA(L) : GL(L))
   #define CL(L) fma(ekv, wm[(long long)((L)-1) * sij], um[(long long)((L)-1) * sij])
-    // pre-face b (1 or Lm) and its window G(b-1..b+2); the even lane's F(1)
-    // is F(2); lim: last cell of this lane's range (its look-ahead beyond
-    // lim comes from the halo hA = G(lim+1), hB = G(lim+2))
-    const int b = half ? Lm : 1;
-    const int lim = half ? npa : Lm;
+    // pre-face b (1, Lm or q4*seg4) and its window G(b-1..b+2); the first
+    // lane's F(1) is F(2); lim: last cell of this lane's range (its
+    // look-ahead beyond lim comes from the halo hA = G(lim+1), hB = G(lim+2))
+    const int b = kSplit == 4 ? (q4 ? q4 * seg4 : 1) : (half ? Lm : 1);
+    const int lim = kSplit == 4 ? (q4 == 3 ? npa : (q4 + 1) * seg4) : (half ? npa : Lm);
     double w0 = 0.0, w1 = 0.0, w2 = 0.0, w3 = 0.0, nxt = 0.0, hA = 0.0, hB = 0.0;
     if (active) {
-      w0 = GLS(half ? b - 1 : 2);
-      w1 = GLS(half ? b : 2);
+      w0 = GLS(pre ? b - 1 : 2);
+      w1 = GLS(pre ? b : 2);
       w2 = GLS(b + 1 > 2 ? b + 1 : 2);
       w3 = GLS(b + 2);
       nxt = GL(b + 3);
-      if (kSplit == 2) {
+      if (kSplit > 1) {
         hA = GLS(min(lim + 1, npa));
         hB = GLS(min(lim + 2, npa));
       }
     }
-    if (kSplit == 2) __syncwarp();
+    if (kSplit > 1) __syncwarp();
     if (active) {
       // pre-face: the flux entering this lane's first cell
       double phi_prev;
       {
-        const double c = half ? ((kCo == 2) ? cst[(long long)(b - 1) * st] : CL(b)) : 0.0;
+        const double c = pre ? ((kCo == 2) ? cst[(long long)(b - 1) * st] : CL(b)) : 0.0;
         const bool neg = is_neg(c);
-        const double a = (kCo == 2 && half) ? ast[(long long)(b - 1) * st] : fma(c, mhdmu[b - 1], neg ? -0.5 : 0.5);
+        const double a = (kCo == 2 && pre) ? ast[(long long)(b - 1) * st] : fma(c, mhdmu[b - 1], neg ? -0.5 : 0.5);
         const double xm = w1 - w0, x = w2 - w1, xp = w3 - w2;
         int cs;
         const double fb = (kRec == 2)
@@ -426,10 +435,10 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
       bits64 bxm = babs_bits(beta, xm);
       double x = w3 - w2;
       bits64 bx = babs_bits(beta, x);
-      const int Lend = (half || kSplit == 1) ? npa - 2 : Lm;
+      const int Lend = last ? npa - 2 : (kSplit == 4 ? lim : Lm);
       for (int L = b + 1; L <= Lend; ++L) {
         double gpp;
-        if (kSplit == 2) {
+        if (kSplit > 1) {
           gpp = (L + 2 <= lim) ? nxt : (L + 2 == lim + 1 ? hA : hB);
           if (kLoss == 2 && L + 2 <= lim) gpp *= LA(L + 2);
           nxt = GL(min(L + 3, lim));
@@ -460,7 +469,7 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         xm = x; bxm = bx; x = xp; bx = bxp;
       }
       // face NPA-1: FBND = F(NPA); cell NPA-1; then the F2(NPA) ghost
-      if (half || kSplit == 1) {
+      if (last) {
         const int L = npa - 1;
         const double c = (kCo == 2) ? cst[(long long)(L - 1) * st] : CL(L);
         if (kCo == 1) cst[(long long)(L - 1) * st] = c;
@@ -565,15 +574,19 @@ static void mu_launch(const Dev& d, dim3 g, int b, double dts, const double* los
   else if (cfl) k_sweep_mu<true, kLoss, 0, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
   else k_sweep_mu<false, kLoss, 0, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
 }
-// Lines are split between lane pairs when d.mu_lanes == 2 (NPA >= 12: each
-// half keeps at least four cells, so no half reads its partner's F(1)
-// rule).
+// Lines are split between d.mu_lanes adjacent lanes (2 for NPA >= 12, 4
+// for NPA >= 24: every segment keeps at least four cells, so no lane but
+// the first reads the F(1) rule).
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
                      cudaStream_t st, unsigned char* rec, bool replay, int co) {
-  const bool split = d.mu_lanes == 2 && d.npa >= 12;
-  dim3 g = grid_for(d, 3, split ? 2 * nlines_of(d, 3) : nlines_of(d, 3));
+  const int lanes = (d.mu_lanes == 4 && d.npa >= 24) ? 4 : ((d.mu_lanes >= 2 && d.npa >= 12) ? 2 : 1);
+  dim3 g = grid_for(d, 3, lanes * nlines_of(d, 3));
   const int b = d.blk[3];
-  if (split) {
+  if (lanes == 4) {
+    if (loss_mode == 1) mu_launch<1, 4>(d, g, b, dts, loss, st, rec, replay, cfl, co);
+    else if (loss_mode == 2) mu_launch<2, 4>(d, g, b, dts, loss, st, rec, replay, cfl, co);
+    else mu_launch<0, 4>(d, g, b, dts, nullptr, st, rec, replay, cfl, co);
+  } else if (lanes == 2) {
     if (loss_mode == 1) mu_launch<1, 2>(d, g, b, dts, loss, st, rec, replay, cfl, co);
     else if (loss_mode == 2) mu_launch<2, 2>(d, g, b, dts, loss, st, rec, replay, cfl, co);
     else mu_launch<0, 2>(d, g, b, dts, nullptr, st, rec, replay, cfl, co);

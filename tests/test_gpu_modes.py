@@ -245,14 +245,15 @@ def test_coefficient_store_is_bitwise_neutral(name):
 
 @pytest.mark.parametrize("name", ["tiny_pert", "four_sp"])
 def test_mu_lanes_equal(name):
-    """DRIFTMU with one lane per line and with lane pairs (the second lane
-    recomputing the flux at the split) gives the same F2, CFL and moments,
+    """DRIFTMU with one lane per line and with 2 or 4 lanes per line (each
+    lane but the first recomputing the flux at its split) gives the same F2,
+    CFL and moments,
     in the plain step (graph and direct) and in the adjoint's recorded and
     transposed passes."""
     wl = W.make_workload(name)
     ns = len(wl.grid.species)
     outs = []
-    for lanes, graph in ((1, False), (2, False), (2, True)):
+    for lanes, graph in ((1, False), (2, False), (2, True), (4, False), (4, True)):
         gpu = _gpu(wl, 4.0)
         gpu.set_mu_lanes(lanes)
         gpu.set_graph(graph)
@@ -272,16 +273,17 @@ def test_mu_lanes_equal(name):
     kp = np.array([[3.0], [4.0], [5.0]])
     obs = [{"member": 0, "s": s, "call": c, "k": 10 + 3 * s, "l": 1 + c, "lshell": 3.0 + 0.5 * s,
             "mlt": 6.0 * c, "log_obs": 0.0} for s in range(ns) for c in range(3)]
-    for lanes in (1, 2):
+    for lanes in (1, 2, 4):
         gpu = _gpu(wl, 4.0)
         gpu.set_mu_lanes(lanes)
         J = gpu.adj_forward(3, wl.dts, kp, 1, obs)
         gf, gb = gpu.adj_backward()
         grads.append((J, gf, gb))
         gpu.close()
-    assert np.array_equal(grads[0][0], grads[1][0])
-    assert np.max(np.abs(grads[0][1] - grads[1][1])) <= 1e-13 * np.max(np.abs(grads[0][1]))
-    assert np.max(np.abs(grads[0][2] - grads[1][2])) <= 1e-13 * max(np.max(np.abs(grads[0][2])), 1e-300)
+    for k in (1, 2):
+        assert np.array_equal(grads[0][0], grads[k][0])
+        assert np.max(np.abs(grads[0][1] - grads[k][1])) <= 1e-13 * np.max(np.abs(grads[0][1]))
+        assert np.max(np.abs(grads[0][2] - grads[k][2])) <= 1e-13 * max(np.max(np.abs(grads[0][2])), 1e-300)
     with pytest.raises(abi.RamGpuError):
         abi.RamGpu(wl.grid, wl.fields).set_mu_lanes(3)
 
