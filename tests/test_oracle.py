@@ -7,8 +7,10 @@ Fortran compiler is available, so the C oracle is pinned by
     conservation, the ANISCH L=1 side effect,
   * an independent pure-Python restatement of the sweep line updates of
     src/ModRamDrift.f90 (written from the Fortran text, including DRIFTR's
-    F(NR+1:NR+2) persistence across lines), which must agree with the C
-    oracle bit for bit and exercise every limiter branch,
+    F(NR+1:NR+2) persistence across lines), fed the face coefficients of
+    the independent NumPy restatement (oracle/ram_numpy.py), never the C
+    oracle's: it must agree with the C oracle bit for bit and exercise
+    every limiter branch,
   * an independent NumPy evaluation of the CEPARA cross sections.
 """
 import dataclasses
@@ -19,6 +21,7 @@ import pytest
 
 from ramgpu import workload as W
 import pyoracle
+import ram_numpy as RN
 
 
 @pytest.fixture(scope="module")
@@ -297,7 +300,10 @@ def test_driftp_drifte_match_independent_restatement(which, name, tiny, tiny_per
     f2 = np.asfortranarray(wl.f2[s]).copy(order="F")
     cd = np.zeros_like(f2, order="F")
     f_in = f2.copy(order="F")
-    o.sweep(which, s, f2, o.vt_vols(5.0), wl.dts, cdrift=cd)
+    vt = RN.vt_vols(g, 5.0)
+    o.sweep(which, s, f2, np.asfortranarray(vt), wl.dts, cdrift=cd)
+    # the coefficients of the independent restatement, not the oracle's
+    cd = (RN.cdrift_p if which == "P" else RN.cdrift_e)(g, RN.Fld(wl.fields), s, wl.dts, vt)[0]
     counts = {k: 0 for k in ("small", "fup", "betaR", "one", "R", "beta")}
     if which == "P":
         ref = python_driftp(g, f_in, cd, counts)
@@ -314,11 +320,11 @@ def test_driftr_matches_independent_restatement(name, kp, tiny, tiny_pert):
     o = pyoracle.Oracle(g, wl.fields)
     s = 1
     # a potential strong enough that both inflow and outflow lines exist
-    vt = o.vt_vols(kp)
+    vt = RN.vt_vols(g, kp)
     f2 = np.asfortranarray(wl.f2[s]).copy(order="F")
-    cd = np.zeros_like(f2, order="F")
     f_in = f2.copy(order="F")
-    o.sweep("R", s, f2, vt, wl.dts, fgeos=wl.fgeos[s], cdrift=cd)
+    o.sweep("R", s, f2, np.asfortranarray(vt), wl.dts, fgeos=wl.fgeos[s])
+    cd = RN.cdrift_r(g, RN.Fld(wl.fields), s, wl.dts, vt)[0]
     counts = {k: 0 for k in ("small", "fup", "betaR", "one", "R", "beta")}
     ref = python_driftr(g, f_in, cd, wl.fgeos[s], wl.fields.fnhs, wl.fields.outside, counts)
     assert np.array_equal(f2, ref)
@@ -352,9 +358,10 @@ def test_driftmu_matches_independent_restatement(name, tiny, tiny_pert):
     o = pyoracle.Oracle(g, wl.fields)
     s = 2
     f2 = np.asfortranarray(wl.f2[s]).copy(order="F")
-    cd = np.zeros_like(f2, order="F")
     f_in = f2.copy(order="F")
-    o.sweep("MU", s, f2, o.vt_vols(4.0), wl.dts, cdrift=cd)
+    vt = RN.vt_vols(g, 4.0)
+    o.sweep("MU", s, f2, np.asfortranarray(vt), wl.dts)
+    cd = RN.cdrift_mu(g, RN.Fld(wl.fields), s, wl.dts, vt)[0]
     counts = {k: 0 for k in ("small", "fup", "betaR", "one", "R", "beta")}
     ref = python_driftmu(g, f_in, cd, wl.fields.fnhs, counts)
     assert np.array_equal(f2[1:], ref[1:])
