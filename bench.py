@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="four_sp", choices=["four_sp", "single_h", "refined"])
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--flush-mb", type=int, default=256)
@@ -79,6 +79,12 @@ def parse():
     ap.add_argument("--adj-member-calls", type=int, default=36)
     ap.add_argument("--only", choices=["adjoint"], default=None,
                     help="run one section alone (profiling); prints its result as JSON")
+    # internal: one CPU-oracle timing in a fresh process (see cpu_leg_fresh)
+    ap.add_argument("--cpu-leg", default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-outer", type=int, default=1, help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-inner", type=int, default=1, help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-calls", type=int, default=0, help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-warmup", type=int, default=1, help=argparse.SUPPRESS)
     return ap.parse_args()
 
 
@@ -193,6 +199,50 @@ def cpu_time_oracle(wl, seconds, nthreads, inner=1, calls=None, warmup=1):
             break
     pyoracle.set_inner_threads(1)
     return cells * n / el, n, el
+
+
+def cpu_leg_main(args):
+    """--cpu-leg: time the CPU oracle in this process (which never imports
+    torch or the CUDA library) and print one JSON object."""
+    from ramgpu import workload as W
+
+    wl = W.make_workload(args.cpu_leg)
+    v, n, el = cpu_time_oracle(wl, args.cpu_seconds, args.cpu_outer, args.cpu_inner,
+                               calls=args.cpu_calls if args.cpu_calls > 0 else None, warmup=args.cpu_warmup)
+    print(json.dumps({"value": v, "calls": n, "elapsed_s": el, "outer": args.cpu_outer, "inner": args.cpu_inner}),
+          flush=True)
+
+
+def cpu_leg_fresh(workload, outer, inner, calls=0, seconds=10.0, warmup=1):
+    """The CPU oracle timed in a fresh interpreter: the measuring process
+    holds no CUDA context, torch thread pool or GPU work of its own, so the
+    figure is the one a reference run on the same cores would see (timed in
+    the GPU process after its GPU sections, the line threads inside each
+    species did not run: the leg measured the species-threads-only rate)."""
+    cmd = [sys.executable, str(ROOT / "bench.py"), "--cpu-leg", workload, "--cpu-outer", str(outer),
+           "--cpu-inner", str(inner), "--cpu-calls", str(calls), "--cpu-seconds", str(seconds),
+           "--cpu-warmup", str(warmup)]
+    r = subprocess.run(cmd, capture_output=True, text=True, check=True)
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def cpu_baseline_fresh(workload, ns, seconds):
+    """Both CPU variants of the reference's path, each in a fresh process:
+    (1) OpenMP over species only, as the reference (at most nS threads);
+    (2) every host core: species threads x line threads inside each routine.
+    The line's value is variant 2."""
+    cores = os.cpu_count() or 1
+    o2, i2 = cpu_threads(ns)
+    v1 = cpu_leg_fresh(workload, min(ns, cores), 1, seconds=seconds)
+    v2 = cpu_leg_fresh(workload, o2, i2, seconds=seconds)
+    return {"value": v2["value"], "unit": UNIT, "cores": o2 * i2, "kind": "port",
+            "sample": (f"{v2['calls']} ram_run calls of the workload in {v2['elapsed_s']:.1f} s after 1 warm-up call, "
+                       f"fresh process; C restatement of the reference routines (-O3 -ffp-contract=off, no Fortran "
+                       f"compiler), OpenMP over {o2} species x {i2} line threads"),
+            "variants": {"species_threads": {"value": v1["value"], "threads": v1["outer"], "calls": v1["calls"],
+                                             "elapsed_s": v1["elapsed_s"]},
+                         "all_cores": {"value": v2["value"], "threads": o2 * i2, "calls": v2["calls"],
+                                       "elapsed_s": v2["elapsed_s"]}}}
 
 
 def run_reference(args, rank, world):
@@ -740,12 +790,7 @@ def run_gb300(args, rank, world, local_rank):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        outer, inner = cpu_threads(ns)
-        v, n, el = cpu_time_oracle(wl, args.cpu_seconds, outer, inner)
-        cpu = {"value": v, "unit": UNIT, "cores": outer * inner, "kind": "port",
-               "sample": f"{n} ram_run calls of the same workload in {el:.1f} s (C restatement of the "
-                         f"reference routines; OpenMP over {outer} species as the reference, "
-                         f"{inner} threads over independent lines inside each routine)"}
+        cpu = cpu_baseline_fresh(args.workload, ns, args.cpu_seconds)
     if rank != 0:
         return
     line = {
@@ -780,6 +825,9 @@ def run_gb300(args, rank, world, local_rank):
 
 def main():
     args = parse()
+    if args.cpu_leg:
+        cpu_leg_main(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

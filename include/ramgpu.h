@@ -155,7 +155,8 @@ int ramgpu_upload_f2_async(ramgpu_ctx *ctx, int member, int s, const double *f2_
 int ramgpu_download_f2_async(ramgpu_ctx *ctx, int member, int s, double *f2_s);
 int ramgpu_moments_async(ramgpu_ctx *ctx, int member, int s, double *ppert, double *ppart);
 int ramgpu_synchronize(ramgpu_ctx *ctx);
-/* The whole reference array F2(NS,NR,NT,NE,NPA) of one member. */
+/* The whole reference array F2(NS,NR,NT,NE,NPA) of one member
+ * (src/ModRamVariables.f90:31), transposed on the device (synchronous). */
 int ramgpu_upload_f2_all(ramgpu_ctx *ctx, int member, const double *f2);
 int ramgpu_download_f2_all(ramgpu_ctx *ctx, int member, double *f2);
 /* Device pointer to F2 of (member, s), (NR,NT,NE,NPA) contiguous; for
@@ -197,6 +198,28 @@ int ramgpu_ram_run_async(ramgpu_ctx *ctx, double dts);
  * both. */
 int ramgpu_ram_run_host(ramgpu_ctx *ctx, double dts, double *const *f2, double *const *ppert,
                         double *const *ppart);
+/* One ram_run call on the arrays exactly as RAM holds them: replaces the
+ * body of ram_run's species loop and tail (src/ModRamRun.f90:64-222) for a
+ * caller whose state is the module array F2(NS,NR,NT,NE,NPA)
+ * (src/ModRamVariables.f90:31, species index fastest) and whose moments are
+ * PPERT(NS,NR,NT), PPART(NS,NR,NT).  f2[m], ppert[m], ppart[m]: member m's
+ * arrays (NULL skips the transfer; ppert/ppart tables may be NULL).  The
+ * device reads F2 in place and transposes it into its per-species blocks
+ * (and back) with no host-side pass: arrays the device reaches (device,
+ * mapped page-locked, or pageable memory over a coherent host link) are read
+ * and written by the transposing kernels directly, others go through a
+ * device staging buffer and the copy engines.  Every species of a member is
+ * transferred; F2's L >= 2 planes go back while the moments are computed.
+ * Results equal ramgpu_ram_run_host's bit for bit.  With ramgpu_set_graph on
+ * (and every array reachable) the call is one CUDA graph per array set,
+ * rebuilt when an address or how the device reaches it changes. */
+int ramgpu_ram_run_ref(ramgpu_ctx *ctx, double dts, double *const *f2, double *const *ppert,
+                       double *const *ppart);
+/* force != 0: ramgpu_ram_run_ref and ramgpu_upload/download_f2_all move
+ * every array through the device staging buffer and the copy engines, even
+ * arrays the device could reach in place (no reference counterpart; for
+ * hosts whose coherent link is slower than their copy engines). */
+int ramgpu_set_ref_staging(ramgpu_ctx *ctx, int force);
 /* Number of item groups ramgpu_ram_run_host pipelines its copies over
  * (1..8, default 4, at most one per item; 1 with RAMGPU_FLAG_LOSSES). */
 int ramgpu_set_pipeline_groups(ramgpu_ctx *ctx, int groups);

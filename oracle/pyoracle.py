@@ -57,7 +57,7 @@ def build(force: bool = False) -> Path:
     src = ORACLE_DIR / "ram_oracle.c"
     if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < src.stat().st_mtime:
         cc = os.environ.get("CC", "gcc")
-        subprocess.run([cc, "-O2", "-ffp-contract=off", "-fPIC", "-fopenmp", "-std=c11", "-shared",
+        subprocess.run([cc, "-O3", "-ffp-contract=off", "-fPIC", "-fopenmp", "-std=c11", "-shared",
                         "-o", str(LIB_PATH), str(src), "-lm"], check=True)
     return LIB_PATH
 

@@ -130,6 +130,18 @@ struct ramgpu_ctx {
   std::vector<const void*> cls_key;
   std::vector<char> cls_pageable;
   bool cls_engine_pageable = false;
+  // ramgpu_ram_run_ref: graph of the whole call for one set of host arrays
+  // (their addresses and how the device reaches them), and a device staging
+  // buffer of one member's F2 for arrays only the copy engines reach
+  cudaGraphExec_t ref_exec = nullptr;
+  std::vector<const void*> ref_key;
+  double ref_dts = -1.0;
+  long long ref_items = -1, ref_launches = 0;
+  unsigned ref_flags = 0;
+  int ref_shape = -1, ref_g = 0;
+  double* ref_stage = nullptr;
+  bool ref_force_stage = false;  // move reachable arrays by the copy engines too
+  int nsm = 0;
   // status word: device words and their page-locked copy; the pass is
   // appended to every call while check_on
   unsigned long long* status_d = nullptr;
@@ -945,6 +957,8 @@ int ramgpu_destroy(ramgpu_ctx* ctx) {
   for (auto& sp : ctx->spans) { cudaEventDestroy(sp.a); cudaEventDestroy(sp.b); }
   for (cudaEvent_t e : ctx->ev_free) cudaEventDestroy(e);
   if (ctx->pipe_exec) cudaGraphExecDestroy(ctx->pipe_exec);
+  if (ctx->ref_exec) cudaGraphExecDestroy(ctx->ref_exec);
+  cudaFree(ctx->ref_stage);
   for (cudaStream_t st : ctx->pipe_streams) cudaStreamDestroy(st);
   for (cudaEvent_t e : ctx->pipe_events) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->trace_ev) cudaEventDestroy(e);
@@ -1250,27 +1264,95 @@ int ramgpu_synchronize(ramgpu_ctx* ctx) {
   return RAMGPU_OK;
 }
 
+// ---------------------------------------------- F2 in the reference layout
+// How the device reaches a caller's array: the device address kernels may
+// read or write it through, or null when only the copy engines can move it
+// (pageable memory without a coherent host link).  Looked up on every call,
+// so memory freed and reallocated at the same address is classified anew.
+static double* reach(const void* p, bool pma) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    at.type = cudaMemoryTypeUnregistered;
+  }
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return (double*)p;
+  if (at.type == cudaMemoryTypeHost) return (double*)at.devicePointer;
+  return pma ? (double*)p : nullptr;
+}
+
+static int ensure_nsm(ramgpu_ctx* ctx, int* pma) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (!ctx->nsm) CK(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, dev));
+  *pma = 0;
+  CK(cudaDeviceGetAttribute(pma, cudaDevAttrPageableMemoryAccess, dev));
+  return RAMGPU_OK;
+}
+
+static int ensure_stage(ramgpu_ctx* ctx) {
+  if (!ctx->ref_stage) CK(cudaMalloc(&ctx->ref_stage, sizeof(double) * ctx->d.ns * ctx->d.ncell));
+  return RAMGPU_OK;
+}
+
+// A member's interleaved array (NS values per cell, ncell cells; r its
+// device address or null) into its NS slot blocks (stride apart).
+static int ref_in(ramgpu_ctx* ctx, const double* host, const double* r, double* slots, long long stride,
+                  long long ncell, cudaStream_t st) {
+  const int ns = ctx->d.ns;
+  if (!r) {
+    if (int rc = ensure_stage(ctx)) return rc;
+    CK(cudaMemcpyAsync(ctx->ref_stage, host, sizeof(double) * ns * ncell, cudaMemcpyHostToDevice, st));
+    r = ctx->ref_stage;
+  }
+  launch_ref_gather(r, slots, ns, stride, 0, ncell, ctx->nsm, st);
+  ctx->launches += 1;
+  CKL("reference-layout gather");
+  return RAMGPU_OK;
+}
+
+// Cells [c0, c1) of a member's NS slot blocks into its interleaved array
+// (w its device address, or null: through the staging buffer).
+static int ref_out(ramgpu_ctx* ctx, double* host, double* w, const double* slots, long long stride, long long c0,
+                   long long c1, cudaStream_t st) {
+  const int ns = ctx->d.ns;
+  if (!w) {
+    if (int rc = ensure_stage(ctx)) return rc;
+    launch_ref_scatter(slots, ctx->ref_stage, ns, stride, c0, c1, ctx->nsm, st);
+    ctx->launches += 1;
+    CKL("reference-layout scatter");
+    CK(cudaMemcpyAsync(host + c0 * ns, ctx->ref_stage + c0 * ns, sizeof(double) * ns * (c1 - c0),
+                       cudaMemcpyDeviceToHost, st));
+    return RAMGPU_OK;
+  }
+  launch_ref_scatter(slots, w, ns, stride, c0, c1, ctx->nsm, st);
+  ctx->launches += 1;
+  CKL("reference-layout scatter");
+  return RAMGPU_OK;
+}
+
 int ramgpu_upload_f2_all(ramgpu_ctx* ctx, int member, const double* f2) {
   if (check_ctx(ctx) || !f2) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
-  const int ns = ctx->d.ns;
-  const size_t n = ctx->d.ncell;
-  std::vector<double> t(n);
-  for (int s = 0; s < ns; ++s) {
-    for (size_t c = 0; c < n; ++c) t[c] = f2[c * ns + s];
-    if (int rc = ramgpu_upload_f2(ctx, member, s, t.data())) return rc;
-  }
+  if (int rc = check_ms(ctx, member, 0)) return rc;
+  int pma = 0;
+  if (int rc = ensure_nsm(ctx, &pma)) return rc;
+  const long long n = ctx->d.ncell;
+  const double* r = ctx->ref_force_stage ? nullptr : reach(f2, pma);
+  if (int rc = ref_in(ctx, f2, r, ctx->d.f2 + (size_t)member * ctx->d.ns * n, n, n, ctx->stream))
+    return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
   return RAMGPU_OK;
 }
 
 int ramgpu_download_f2_all(ramgpu_ctx* ctx, int member, double* f2) {
   if (check_ctx(ctx) || !f2) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
-  const int ns = ctx->d.ns;
-  const size_t n = ctx->d.ncell;
-  std::vector<double> t(n);
-  for (int s = 0; s < ns; ++s) {
-    if (int rc = ramgpu_download_f2(ctx, member, s, t.data())) return rc;
-    for (size_t c = 0; c < n; ++c) f2[c * ns + s] = t[c];
-  }
+  if (int rc = check_ms(ctx, member, 0)) return rc;
+  int pma = 0;
+  if (int rc = ensure_nsm(ctx, &pma)) return rc;
+  const long long n = ctx->d.ncell;
+  double* w = ctx->ref_force_stage ? nullptr : reach(f2, pma);
+  if (int rc = ref_out(ctx, f2, w, ctx->d.f2 + (size_t)member * ctx->d.ns * n, n, 0, n, ctx->stream))
+    return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
   return RAMGPU_OK;
 }
 
@@ -1462,6 +1544,156 @@ int ramgpu_pipeline_trace(ramgpu_ctx* ctx, int* groups, float* ms) {
   if (ctx->trace_ms.empty()) return fail(ctx, RAMGPU_ERR_STATE, "no traced ramgpu_ram_run_host call");
   *groups = (int)ctx->trace_ms.size() / 3;
   for (size_t k = 0; k < ctx->trace_ms.size(); ++k) ms[k] = ctx->trace_ms[k];
+  return RAMGPU_OK;
+}
+
+// One member's arrays in the reference layout and their device addresses
+// (null: staged through the copy engines).
+struct RefMem {
+  double *f2 = nullptr, *pe = nullptr, *pa = nullptr;
+  double *f2r = nullptr, *per = nullptr, *par = nullptr;
+};
+
+// ramgpu_ram_run_ref's work: F2 of every member gathered from the
+// reference layout, the step over the item groups, then F2 scattered back:
+// its L >= 2 planes on a companion stream as soon as every group's closing
+// mask is done (they are final then), while the moments run; the L = 1
+// plane, which ANISCH's side effect rewrites, and the moments after them.
+// staged: some array is reachable only by the copy engines; everything
+// then runs in stream order on the context's stream.
+static int enqueue_ref(ramgpu_ctx* ctx, double dts, const std::vector<RefMem>& mem, bool staged, int G) {
+  const Dev full = ctx->d;
+  const int ns = full.ns, nm = full.nm, nit = full.nitems;
+  const long long n = full.ncell, nm2 = (long long)full.nr * full.nt, n1 = (long long)full.nr * full.nt * full.ne;
+  const cudaStream_t main = ctx->stream;
+  int rc = RAMGPU_OK;
+  for (int m = 0; m < nm; ++m)
+    if (mem[m].f2 && (rc = ref_in(ctx, mem[m].f2, mem[m].f2r, full.f2 + (size_t)m * ns * n, n, n, main))) return rc;
+  if ((rc = enqueue_tables(ctx, dts))) return rc;
+  CK(cudaMemsetAsync(full.cflq, 0, sizeof(unsigned long long) * 5 * full.nm * full.ns, main));
+  cudaEvent_t ev_tab = ctx->pipe_events[2 * G + 1];
+  CK(cudaEventRecord(ev_tab, main));
+  for (int g = 0; g < G; ++g) {
+    const int i0 = (int)((long long)nit * g / G), i1 = (int)((long long)nit * (g + 1) / G);
+    cudaStream_t st = G > 1 ? ctx->pipe_streams[g] : main;
+    if (G > 1) CK(cudaStreamWaitEvent(st, ev_tab, 0));
+    ctx->stream = st;
+    ctx->d.items = full.items + i0;
+    ctx->d.nitems = i1 - i0;
+    ctx->d.item0 = i0;
+    ctx->finish_hook = staged ? nullptr : ctx->pipe_fin_events[g];
+    rc = enqueue_sweeps(ctx, dts, false);
+    ctx->finish_hook = nullptr;
+    ctx->d = full;
+    ctx->stream = main;
+    if (rc) return rc;
+    if (G > 1) {
+      CK(cudaEventRecord(ctx->pipe_events[2 * g + 1], st));
+      CK(cudaStreamWaitEvent(main, ctx->pipe_events[2 * g + 1], 0));
+    }
+  }
+  const long long f2_from = staged ? 0 : n1;
+  if (!staged) {
+    cudaStream_t cs = ctx->pipe_copy_streams[0];
+    for (int g = 0; g < G; ++g) CK(cudaStreamWaitEvent(cs, ctx->pipe_fin_events[g], 0));
+    for (int m = 0; m < nm; ++m)
+      if (mem[m].f2 && (rc = ref_out(ctx, mem[m].f2, mem[m].f2r, full.f2 + (size_t)m * ns * n, n, n1, n, cs)))
+        return rc;
+    CK(cudaEventRecord(ctx->pipe_copy_done[0], cs));
+  }
+  for (int m = 0; m < nm; ++m) {
+    if (mem[m].f2 && (rc = ref_out(ctx, mem[m].f2, mem[m].f2r, full.f2 + (size_t)m * ns * n, n, 0,
+                                   staged ? n : f2_from, main)))
+      return rc;
+    if (mem[m].pe && (rc = ref_out(ctx, mem[m].pe, mem[m].per, full.ppert + (size_t)m * ns * nm2, nm2, 0, nm2, main)))
+      return rc;
+    if (mem[m].pa && (rc = ref_out(ctx, mem[m].pa, mem[m].par, full.ppart + (size_t)m * ns * nm2, nm2, 0, nm2, main)))
+      return rc;
+  }
+  if (!staged) CK(cudaStreamWaitEvent(main, ctx->pipe_copy_done[0], 0));
+  if (ctx->check_on) rc = enqueue_status(ctx);
+  return rc;
+}
+
+int ramgpu_ram_run_ref(ramgpu_ctx* ctx, double dts, double* const* f2, double* const* ppert, double* const* ppart) {
+  if (check_ctx(ctx) || !f2) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  int rc = prepare(ctx, dts);
+  if (rc) return rc;
+  ctx->last_dts = dts;
+  if (ctx->d.nitems == 0) return RAMGPU_OK;
+  int pma = 0;
+  if ((rc = ensure_nsm(ctx, &pma))) return rc;
+  const int nm = ctx->d.nm;
+  std::vector<RefMem> mem(nm);
+  std::vector<const void*> key;
+  bool staged = false;
+  for (int m = 0; m < nm; ++m) {
+    RefMem& r = mem[m];
+    r.f2 = f2[m];
+    r.pe = ppert ? ppert[m] : nullptr;
+    r.pa = ppart ? ppart[m] : nullptr;
+    const bool fs = ctx->ref_force_stage;
+    if (r.f2) staged |= !(r.f2r = fs ? nullptr : reach(r.f2, pma));
+    if (r.pe) staged |= !(r.per = fs ? nullptr : reach(r.pe, pma));
+    if (r.pa) staged |= !(r.par = fs ? nullptr : reach(r.pa, pma));
+    for (const void* p : {(const void*)r.f2, (const void*)r.pe, (const void*)r.pa, (const void*)r.f2r,
+                          (const void*)r.per, (const void*)r.par})
+      key.push_back(p);
+  }
+  const bool timing = ctx->timing;
+  ctx->timing = false;  // one call, one set of streams: no per-kernel events
+  const int G = clamp_groups(ctx, ctx->step_groups);
+  if ((rc = ensure_group_streams(ctx, G))) {
+    ctx->timing = timing;
+    return rc;
+  }
+  if (!ctx->graph_on || staged) {
+    rc = enqueue_ref(ctx, dts, mem, staged, G);
+  } else {
+    if (!ctx->ref_exec || ctx->ref_key != key || ctx->ref_dts != dts || ctx->ref_items != ctx->items_version ||
+        ctx->ref_flags != ctx->d.flags || ctx->ref_shape != ctx->shape_version || ctx->ref_g != G) {
+      if (ctx->ref_exec) cudaGraphExecDestroy(ctx->ref_exec);
+      ctx->ref_exec = nullptr;
+      cudaGraph_t g = nullptr;
+      const long long l0 = ctx->launches;
+      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      rc = enqueue_ref(ctx, dts, mem, staged, G);
+      cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+      ctx->ref_launches = ctx->launches - l0;
+      ctx->launches = l0;
+      if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&ctx->ref_exec, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (!rc && e != cudaSuccess) {
+        ctx->ref_exec = nullptr;
+        rc = cuda_fail(ctx, e, "reference-layout graph");
+      }
+      if (!rc) {
+        ctx->ref_key = key;
+        ctx->ref_dts = dts;
+        ctx->ref_items = ctx->items_version;
+        ctx->ref_flags = ctx->d.flags;
+        ctx->ref_shape = ctx->shape_version;
+        ctx->ref_g = G;
+      }
+    }
+    if (!rc) {
+      CK(cudaGraphLaunch(ctx->ref_exec, ctx->stream));
+      ctx->launches += ctx->ref_launches;
+    }
+  }
+  ctx->timing = timing;
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->check_on) {
+    ctx->status_valid = true;
+    return status_out(ctx, nullptr);
+  }
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_ref_staging(ramgpu_ctx* ctx, int force) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  ctx->ref_force_stage = force != 0;
   return RAMGPU_OK;
 }
 
@@ -1718,6 +1950,8 @@ int ramgpu_set_graph(ramgpu_ctx* ctx, int enable) {
   if (ctx->pipe_exec) cudaGraphExecDestroy(ctx->pipe_exec);
   ctx->pipe_exec = nullptr;
   ctx->cls_key.clear();
+  if (ctx->ref_exec) cudaGraphExecDestroy(ctx->ref_exec);
+  ctx->ref_exec = nullptr;
   return RAMGPU_OK;
 }
 

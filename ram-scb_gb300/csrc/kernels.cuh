@@ -133,6 +133,14 @@ void launch_fly_sats(const Dev& d, const SatDev* sats, int nsat, double* sat_flu
 void launch_sum_pressure(const Dev& d, int member, unsigned mask, double* pall, double* ppar,
                          cudaStream_t st);
 
+// F2 / moments in the reference's layout (layout.cu): slots[s*stride + c]
+// <-> ref[c*ns + s] for cells c in [c0, c1); ref may be host memory the
+// device reaches (mapped page-locked, or pageable over a coherent link).
+void launch_ref_gather(const double* ref, double* slots, int ns, long long stride, long long c0, long long c1,
+                       int nsm, cudaStream_t st);
+void launch_ref_scatter(const double* slots, double* ref, int ns, long long stride, long long c0, long long c1,
+                        int nsm, cudaStream_t st);
+
 void launch_selftest_mul(long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t st);
 // Status word of the active items (status.cu): st[5] device words.
 void launch_status(const Dev& d, unsigned long long* st, cudaStream_t s);

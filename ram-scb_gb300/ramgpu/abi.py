@@ -37,7 +37,8 @@ EXPORTS = (
     "ramgpu_fly_sats", "ramgpu_sum_pressure", "ramgpu_adj_replay", "ramgpu_set_pa_diffusion",
     "ramgpu_loss_wae", "ramgpu_bounce_integrals", "ramgpu_upload_f2_async", "ramgpu_download_f2_async",
     "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store", "ramgpu_compute_hI",
-    "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_set_pipeline_groups", "ramgpu_pipeline_groups",
+    "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_ram_run_ref", "ramgpu_set_ref_staging",
+    "ramgpu_set_pipeline_groups", "ramgpu_pipeline_groups",
     "ramgpu_set_step_groups", "ramgpu_step_groups", "ramgpu_set_pipeline_trace", "ramgpu_pipeline_trace",
     "ramgpu_check", "ramgpu_set_check", "ramgpu_last_status",
     "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_mu_lanes",
@@ -165,6 +166,8 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_get_fields": ([vp] + [dp] * 11, i),
         "ramgpu_sum_pressure": ([vp, i, dp, dp], i),
         "ramgpu_ram_run_host": ([vp, d, vp, vp, vp], i),
+        "ramgpu_ram_run_ref": ([vp, d, vp, vp, vp], i),
+        "ramgpu_set_ref_staging": ([vp, i], i),
         "ramgpu_set_pipeline_groups": ([vp, i], i),
         "ramgpu_pipeline_groups": ([vp], i),
         "ramgpu_set_step_groups": ([vp, i], i),
@@ -382,6 +385,57 @@ class RamGpu:
                     table(seqs[2], g.nr * g.nt, "ppart"))
             self._host_tables = (key, tabs, seqs)
         self._ck(self.lib.ramgpu_ram_run_host(self.h, float(dts), *tabs), "ram_run_host")
+
+    def ram_run_ref(self, dts: float, f2, ppert=None, ppart=None):
+        """One ram_run call on arrays in the reference's own layout
+        (ramgpu_ram_run_ref): f2[m] is member m's F2(NS,NR,NT,NE,NPA),
+        ppert[m]/ppart[m] its PPERT/PPART(NS,NR,NT), each a Fortran-ordered
+        (or flat) float64 array, updated in place; None skips a member."""
+        g = self.grid
+        nm = self.n_members
+        sizes = (self.ns * g.ncell, self.ns * g.nr * g.nt, self.ns * g.nr * g.nt)
+        seqs = tuple(None if q is None else list(q) for q in (f2, ppert, ppart))
+        key = tuple(None if q is None else tuple(map(id, q)) for q in seqs)
+        if getattr(self, "_ref_tables", None) is None or self._ref_tables[0] != key:
+            vtab = C.c_void_p * nm
+
+            def table(seq, n, what):
+                if seq is None:
+                    return None
+                if len(seq) != nm:
+                    raise RamGpuError(f"{what}: need {nm} entries (one per member)")
+                addrs = []
+                for k, a in enumerate(seq):
+                    if a is None:
+                        addrs.append(None)
+                        continue
+                    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.size == n
+                            and a.flags.writeable and (a.flags.f_contiguous or a.flags.c_contiguous)):
+                        raise RamGpuError(f"{what}[{k}]: need a contiguous writable float64 array of {n} values")
+                    addrs.append(a.ctypes.data)
+                return vtab(*addrs)
+
+            tabs = tuple(table(q, n, w) for q, n, w in zip(seqs, sizes, ("f2", "ppert", "ppart")))
+            self._ref_tables = (key, tabs, seqs)
+        self._ck(self.lib.ramgpu_ram_run_ref(self.h, float(dts), *self._ref_tables[1]), "ram_run_ref")
+
+    def set_ref_staging(self, force: bool):
+        """Move reference-layout arrays by the copy engines even when the
+        device reaches them in place."""
+        self._ck(self.lib.ramgpu_set_ref_staging(self.h, int(bool(force))), "set_ref_staging")
+
+    def upload_f2_all(self, member: int, f2):
+        """Member's whole F2(NS,NR,NT,NE,NPA) in the reference layout."""
+        a = np.asfortranarray(np.asarray(f2, dtype=np.float64))
+        if a.size != self.ns * self.grid.ncell:
+            raise RamGpuError("upload_f2_all: need NS*NR*NT*NE*NPA values")
+        self._ck(self.lib.ramgpu_upload_f2_all(self.h, int(member), _dptr(a)), "upload_f2_all")
+
+    def download_f2_all(self, member: int) -> np.ndarray:
+        g = self.grid
+        out = np.zeros((self.ns, g.nr, g.nt, g.ne, g.npa), order="F")
+        self._ck(self.lib.ramgpu_download_f2_all(self.h, int(member), _dptr(out)), "download_f2_all")
+        return out
 
     def set_pipeline_groups(self, groups: int):
         """Item groups ram_run_host pipelines its copies over."""

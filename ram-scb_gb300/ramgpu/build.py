@@ -18,9 +18,16 @@ CSRC = PKG_ROOT / "csrc"
 LIB_DIR = PKG_ROOT / "lib"
 LIB_PATH = LIB_DIR / "libramgpu.so"
 SOURCES = ["abi.cu", "sweeps.cu", "tables.cu", "adjoint.cu", "noalloc.cu", "outputs.cu", "padif.cu", "bounce.cu",
-           "selftest.cu", "status.cu"]
+           "selftest.cu", "status.cu", "layout.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# The coefficient tables follow the reference's rounding: no implicit
+# contraction of a*b+c into an fma (explicit fma() calls stay).  Contracting
+# GREL**2-1 (GREL - 1 ~ 1e-8 for ions at 0.1 keV) changed DRIFTE's energy
+# extrapolation factor by up to 6e-10 relative, and 1-MUBOUN**2 near MU = 1
+# the last pitch-angle rates, against the reference's separately rounded
+# product and difference.
+FILE_FLAGS = {"tables.cu": ["-fmad=false"]}
 
 
 def nvcc_path() -> str:
@@ -48,7 +55,8 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
         s = CSRC / src
         o = obj_dir / (src + ".o")
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, "-I", str(REPO_ROOT / "include"), "-c", str(s), "-o", str(o)])
+            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(src, []), "-I", str(REPO_ROOT / "include"), "-c",
+                         str(s), "-o", str(o)])
 
     def run(cmd):
         if verbose:
