@@ -84,7 +84,8 @@ typedef struct {
 
 /* ---- lifetime ------------------------------------------------------------ */
 
-/* Replaces ram_allocate's RAM arrays (src/ModRamInit.f90:68-120). */
+/* Replaces ram_allocate's RAM arrays (src/ModRamInit.f90:68-120).
+ * n_members x ns is at most 65535 (one launch-grid row per work item). */
 int ramgpu_create(const ramgpu_config *cfg, ramgpu_ctx **out);
 int ramgpu_destroy(ramgpu_ctx *ctx);
 /* Copies the last error message of ctx (or of the last failed create when
@@ -191,11 +192,11 @@ int ramgpu_ram_run_async(ramgpu_ctx *ctx, double dts);
  * when not NULL, receive each item's (NR,NT) moments (NULL entries are
  * skipped), and so does f2 (a NULL entry leaves that item's F2 resident
  * and unchanged on the host side).  Returns when every copy is back.
- * Each pointer set is classified (page-locked or pageable) and, with
- * graphs on, captured on first use and reused while the same pointers come
- * back; after re-registering memory at the same addresses
- * (cudaHostRegister / cudaHostUnregister), call ramgpu_set_graph to drop
- * both. */
+ * Every pointer is classified (page-locked or pageable) on every call; with
+ * graphs on, the call is captured on first use and replayed while the same
+ * pointers with the same classification come back (memory freed and
+ * reallocated, registered or unregistered at the same address is
+ * classified anew and the graph rebuilt). */
 int ramgpu_ram_run_host(ramgpu_ctx *ctx, double dts, double *const *f2, double *const *ppert,
                         double *const *ppart);
 /* One ram_run call on the arrays exactly as RAM holds them: replaces the
@@ -445,12 +446,15 @@ typedef struct {
  * current F2, with Kp of call c and member m in kp[c*n_members + m] (VOLS).
  * Saves a checkpoint of F2 every k_ckpt calls, evaluates J per member into
  * J[n_members] and leaves F2 at the end of the window (the moments are
- * those of the window's last call).  Every limiter branch
- * and clip is recorded; ramgpu_adj_digest returns a digest of the pattern.
- * Allocates its checkpoint buffer and a ring of branch records (8 bytes per
- * cell, item and call) that keeps the last nkeep checkpoint segments, as
- * many as the record budget allows (ramgpu_set_adj_record_budget; at least
- * one segment). */
+ * those of the window's last call).  The calls of the last nkeep checkpoint
+ * segments record every limiter branch and clip into a ring of branch
+ * records (8 bytes per cell, item and call) that holds as many segments as
+ * the record budget allows (ramgpu_set_adj_record_budget; at least one);
+ * the earlier calls, which ramgpu_adj_backward recomputes from their
+ * checkpoints, run the plain step (the same F2 bits).  ramgpu_adj_digest
+ * returns a digest of the recorded pattern.  The checkpoint buffer and the
+ * ring are allocated by the first window and reused by later windows of the
+ * same shape. */
 int ramgpu_adj_forward(ramgpu_ctx *ctx, int ncalls, double dts, const double *kp, int k_ckpt,
                        const ramgpu_obs *obs, int nobs, double *J);
 /* Backward pass: gradients of J with respect to the window's initial F2
@@ -471,8 +475,9 @@ int ramgpu_set_adj_record_budget(ramgpu_ctx *ctx, long long bytes);
 /* Checkpoint segments of the last ramgpu_adj_forward and how many of them
  * (the last ones) the record ring keeps. */
 int ramgpu_adj_segments(ramgpu_ctx *ctx, int *nseg, int *nkeep);
-/* Digest of every branch recorded by the last ramgpu_adj_forward: equal
- * digests mean the same frozen-limiter pattern. */
+/* Digest of every branch recorded by the last ramgpu_adj_forward (the
+ * calls of the kept segments): equal digests mean the same frozen-limiter
+ * pattern. */
 int ramgpu_adj_digest(ramgpu_ctx *ctx, unsigned long long *digest);
 /* Copy of the branch record of one call of a kept checkpoint segment of
  * the last ramgpu_adj_forward: 8 sweeps (R,P,E,MU,MU,E,P,R) x active items x
@@ -505,8 +510,12 @@ int ramgpu_adj_replay(ramgpu_ctx *ctx, double *J);
  *            ramgpu_f2_device_ptr);  we, wmu, ekev : host arrays (NE)/(NPA)/(NE)
  *   stream : cudaStream_t or NULL;  setrc : host, receives the sum.
  * The first call on a device looks up the scratch address on that device
- * (make it before any stream capture).  Every call reuses the same scratch,
- * which keeps the last call's contents; calls that overlap on the GPU race.
+ * (make it before any stream capture) and keeps it for the life of the
+ * process, so do not call this after a cudaDeviceReset of that device.
+ * Every call reuses the same scratch, which keeps the last call's contents;
+ * calls that overlap on the GPU race.  The call is synchronous (it waits for
+ * its stream): made on a stream under capture it returns RAMGPU_ERR_STATE
+ * and leaves the capture intact.
  * Errors are reported by ramgpu_last_error(NULL, ...).  No counterpart in the
  * reference: it exists only for callers that cannot allocate. */
 int ramgpu_sumrc_noalloc(const double *f2_dev, int nr, int nt, int ne, int npa,

@@ -534,8 +534,8 @@ static void adj_free(ramgpu_ctx* ctx) {
 // i*ncell in each instance).
 static int enqueue_call_rec(ramgpu_ctx* ctx, double dts, unsigned char* rec, bool moments) {
   const size_t isz = (size_t)ctx->d.nitems * ctx->d.ncell;
-  // positions no sweep writes (e.g. cell 1 of a DRIFTR line) stay zero
-  CK(cudaMemsetAsync(rec, 0, 8 * isz, ctx->stream));
+  // positions no sweep writes (e.g. cell 1 of a DRIFTR line) are the same
+  // in every call and stay zero from the ring's allocation
   launch_member_coef(ctx->d, dts, ctx->stream);
   launch_ghost(ctx->d, ctx->stream);
   ctx->launches += 3;
@@ -832,6 +832,9 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
                 "grid too small: need NR>=4, NT>=5, NE>=31 (ANISCH bands), NPA>=5, NS>=1, members>=1");
   const long long ncell = (long long)cfg->nr * cfg->nt * cfg->ne * cfg->npa;
   if (ncell > (1LL << 40)) return fail(nullptr, RAMGPU_ERR_ARG, "grid too large");
+  // non-persistent launches put the work item in gridDim.y (at most 65535)
+  if ((long long)cfg->n_members * cfg->ns > 65535)
+    return fail(nullptr, RAMGPU_ERR_ARG, "members x species above 65535 (the launch grid's item dimension)");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
     return fail(nullptr, RAMGPU_ERR_CUDA, "no CUDA device");
@@ -1452,14 +1455,17 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
   }
   for (double* const* tab : {f2, ppert, ppart})
     for (int k = 0; k < nslot; ++k) key.push_back(tab ? (const void*)tab[k] : nullptr);
-  // the classification of the last pointer set is kept (a time loop passes
-  // the same buffers every call)
-  if (key != ctx->cls_key) {
+  // Every pointer is classified on every call (cudaPointerGetAttributes is
+  // cheap next to the call): a buffer freed and reallocated at the same
+  // address may have changed from page-locked to pageable.  A changed
+  // classification drops the graph built on the old one.
+  {
     int dev = 0, pma = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev);
-    ctx->cls_pageable.clear();
-    ctx->cls_engine_pageable = false;
+    std::vector<char> cls;
+    bool engine = false;
+    cls.reserve(key.size());
     for (const void* p : key) {
       bool pg = false;
       if (p) {
@@ -1469,11 +1475,17 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
           at.type = cudaMemoryTypeUnregistered;
         }
         pg = at.type == cudaMemoryTypeUnregistered;
-        if (pg && !pma) ctx->cls_engine_pageable = true;
+        if (pg && !pma) engine = true;
       }
-      ctx->cls_pageable.push_back(pg && pma ? 1 : 0);
+      cls.push_back(pg && pma ? 1 : 0);
     }
-    ctx->cls_key = key;
+    if (key != ctx->cls_key || cls != ctx->cls_pageable || engine != ctx->cls_engine_pageable) {
+      if (ctx->pipe_exec) cudaGraphExecDestroy(ctx->pipe_exec);
+      ctx->pipe_exec = nullptr;
+      ctx->cls_pageable = cls;
+      ctx->cls_engine_pageable = engine;
+      ctx->cls_key = key;
+    }
   }
   const std::vector<char>& pageable = ctx->cls_pageable;
   if (ctx->cls_engine_pageable) capturable = false;
@@ -2390,30 +2402,49 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
     q.log_obs = o.log_obs;
     equatorial_stencil(d, lz, phi, o.lshell, o.mlt, &q.i0, &q.wi, &q.j0, &q.j1, &q.wj);
   }
-  adj_free(ctx);
   auto& a = ctx->adj;
-  a.ncalls = ncalls; a.k = k_ckpt; a.nseg = (ncalls + k_ckpt - 1) / k_ckpt; a.nobs = nobs; a.dts = dts;
-  a.kp.assign(kp, kp + (size_t)ncalls * nm);
-  a.items_version = ctx->items_version;
-  a.rec_call = (size_t)8 * d.nitems * d.ncell;
+  a.ready = false;
+  const int nseg = (ncalls + k_ckpt - 1) / k_ckpt;
+  const size_t rec_call = (size_t)8 * d.nitems * d.ncell;
   const int kseg = k_ckpt < ncalls ? k_ckpt : ncalls;
-  bool ok = cudaMalloc(&a.ckpt, sizeof(double) * a.nseg * d.nitems * d.ncell) == cudaSuccess;
   // The ring keeps the records of the last nkeep segments, as many as the
   // budget allows (at least one); only the segments before them are
   // recomputed from their checkpoints in the backward pass.
+  int nkeep = 1;
   {
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
+    // the ring this window would reuse counts as free
+    if (a.rec && a.rec_call == rec_call && a.k == kseg) free_b += a.rec_call * kseg * a.nkeep;
     const long long budget = ctx->adj_record_budget >= 0 ? ctx->adj_record_budget : (long long)(free_b / 2);
-    const long long seg_bytes = (long long)(a.rec_call * kseg);
+    const long long seg_bytes = (long long)(rec_call * kseg);
     long long nk = budget / seg_bytes;
-    a.nkeep = (int)(nk < 1 ? 1 : (nk > a.nseg ? a.nseg : nk));
+    nkeep = (int)(nk < 1 ? 1 : (nk > nseg ? nseg : nk));
   }
-  if (ok && cudaMalloc(&a.rec, a.rec_call * kseg * a.nkeep) != cudaSuccess) {
-    cudaGetLastError();
-    a.nkeep = 1;
-    ok = cudaMalloc(&a.rec, a.rec_call * kseg) == cudaSuccess;
+  // buffers of the previous window are reused when the new one has the
+  // same shape (a window run again, as finite differences do)
+  const bool reuse = a.rec && a.ckpt && a.rec_call == rec_call && a.k == kseg && a.nkeep == nkeep &&
+                     a.nseg == nseg && a.nobs == nobs && a.ncalls == ncalls;
+  if (!reuse) adj_free(ctx);
+  a.ncalls = ncalls; a.k = k_ckpt; a.nseg = nseg; a.nobs = nobs; a.dts = dts;
+  a.kp.assign(kp, kp + (size_t)ncalls * nm);
+  a.items_version = ctx->items_version;
+  a.rec_call = rec_call;
+  a.nkeep = nkeep;
+  bool ok = true;
+  if (!reuse) {
+    ok = cudaMalloc(&a.ckpt, sizeof(double) * a.nseg * d.nitems * d.ncell) == cudaSuccess;
+    if (ok && cudaMalloc(&a.rec, a.rec_call * kseg * a.nkeep) != cudaSuccess) {
+      cudaGetLastError();
+      a.nkeep = 1;
+      ok = cudaMalloc(&a.rec, a.rec_call * kseg) == cudaSuccess;
+    }
+    // record positions no sweep writes stay zero in every call
+    if (ok) ok = cudaMemsetAsync(a.rec, 0, a.rec_call * kseg * a.nkeep, ctx->stream) == cudaSuccess;
   }
+  if (reuse) {
+    // the same shape: obs, fm, J and the rest are reused too
+  } else {
   ok = ok && cudaMalloc(&a.obs, sizeof(ObsDev) * (nobs > 0 ? nobs : 1)) == cudaSuccess;
   ok = ok && cudaMalloc(&a.fm, sizeof(double) * (nobs > 0 ? nobs : 1)) == cudaSuccess;
   ok = ok && cudaMalloc(&a.fm2, sizeof(double) * (nobs > 0 ? nobs : 1)) == cudaSuccess;
@@ -2421,6 +2452,7 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
   ok = ok && cudaMalloc(&a.J2, sizeof(double) * nm) == cudaSuccess;
   ok = ok && cudaMalloc(&a.digest, sizeof(unsigned long long)) == cudaSuccess;
   ok = ok && cudaMalloc(&a.kp_d, sizeof(double) * (size_t)ncalls * nm) == cudaSuccess;
+  }
   if (!ok) {
     adj_free(ctx);
     return fail(ctx, RAMGPU_ERR_NOMEM, "adjoint buffers: device allocation failed");
@@ -2431,15 +2463,25 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
   CK(cudaMemcpyAsync(d.vt_mode, one.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemsetAsync(a.J, 0, sizeof(double) * nm, ctx->stream));
   CK(cudaMemsetAsync(a.digest, 0, sizeof(unsigned long long), ctx->stream));
+  // Segments whose records the ring keeps run the recording step; the
+  // earlier ones, which the backward pass recomputes from their checkpoints
+  // anyway, run the plain step (the same F2 bits, no record traffic; from
+  // its CUDA graph when graphs are on).  The digest covers the recorded calls.
+  const int first_kept = a.nseg - a.nkeep;
   for (int c = 0; c < ncalls; ++c) {
     if (c % k_ckpt == 0)
       if ((rc = adj_copy_items(ctx, a.ckpt + (size_t)(c / k_ckpt) * d.nitems * d.ncell, true))) return rc;
     if ((rc = adj_set_kp(ctx, c))) return rc;
-    unsigned char* r = a.rec + adj_rec_slot(a, c) * a.rec_call;
-    if ((rc = enqueue_call_rec(ctx, dts, r, c == ncalls - 1))) return rc;
-    launch_digest(r, (long long)a.rec_call, a.digest, ctx->stream);
+    if (c / k_ckpt < first_kept) {
+      if ((rc = enqueue_ram_run(ctx, dts))) return rc;
+    } else {
+      unsigned char* r = a.rec + adj_rec_slot(a, c) * a.rec_call;
+      if ((rc = enqueue_call_rec(ctx, dts, r, c == ncalls - 1))) return rc;
+      launch_digest(r, (long long)a.rec_call, a.digest, ctx->stream);
+      ctx->launches += 1;
+    }
     launch_obs_fwd(d, a.obs, nobs, c, a.fm, a.J, ctx->stream);
-    ctx->launches += 2;
+    ctx->launches += 1;
     CKL("adjoint forward");
   }
   CK(cudaStreamSynchronize(ctx->stream));

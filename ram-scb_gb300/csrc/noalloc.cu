@@ -15,9 +15,15 @@
 // not a device address; its device address is looked up once per device with
 // cudaGetSymbolAddress, with that device current, by the first call of
 // ramgpu_sumrc_noalloc on that device.  Make that first call before any
-// stream capture.  All calls share the one array and it keeps the contents
-// of the last call; calls that overlap on the GPU (from two host threads or
-// two streams) race on it.
+// stream capture.  The address is kept for the life of the process: after a
+// cudaDeviceReset of that device the module is loaded again and the kept
+// address is stale, so do not call this entry point after resetting the
+// device.  All calls share the one array and it keeps the contents of the
+// last call; calls that overlap on the GPU (from two host threads or two
+// streams) race on it.  Every call is synchronous (it copies the grid
+// vectors from host memory and waits for its stream), so it cannot be made
+// while its stream is being captured: such a call returns RAMGPU_ERR_STATE
+// and leaves the capture intact.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -81,13 +87,24 @@ __global__ void k_sumrc_final(double* scratch, int nblk) {
 
 int scratch_for_current_device(double** out) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return RAMGPU_ERR_CUDA;
-  if (dev < 0 || dev >= kMaxDevices) return RAMGPU_ERR_ARG;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    ramgpu::set_thread_error("ramgpu_sumrc_noalloc: no current CUDA device");
+    return RAMGPU_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= kMaxDevices) {
+    ramgpu::set_thread_error("ramgpu_sumrc_noalloc: device index " + std::to_string(dev) +
+                             " beyond the 64 devices the address table holds");
+    return RAMGPU_ERR_ARG;
+  }
   std::lock_guard<std::mutex> lock(g_mu);
   if (!g_scratch_dev[dev]) {
     double* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) return RAMGPU_ERR_CUDA;
+    if (e != cudaSuccess || !p) {
+      ramgpu::set_thread_error(std::string("ramgpu_sumrc_noalloc: cudaGetSymbolAddress of the scratch failed: ") +
+                               cudaGetErrorString(e));
+      return RAMGPU_ERR_CUDA;
+    }
     g_scratch_dev[dev] = p;
   }
   *out = g_scratch_dev[dev];
@@ -112,13 +129,17 @@ extern "C" int ramgpu_sumrc_noalloc(const double* f2_dev, int nr, int nt, int ne
                              "(fixed scratch of the no-allocation path)");
     return RAMGPU_ERR_ARG;
   }
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    ramgpu::set_thread_error("ramgpu_sumrc_noalloc: the stream is being captured; this call synchronises its "
+                             "stream and cannot be captured");
+    return RAMGPU_ERR_STATE;
+  }
   double* scratch = nullptr;
   int rc = scratch_for_current_device(&scratch);
-  if (rc != RAMGPU_OK) {
-    ramgpu::set_thread_error("ramgpu_sumrc_noalloc: cudaGetSymbolAddress of the scratch failed");
-    return rc;
-  }
-  cudaStream_t st = (cudaStream_t)stream;
+  if (rc != RAMGPU_OK) return rc;
   cudaError_t e = cudaMemcpyAsync(scratch + kOffWe, we, sizeof(double) * ne, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(scratch + kOffWmu, wmu, sizeof(double) * npa, cudaMemcpyHostToDevice, st);

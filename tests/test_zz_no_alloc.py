@@ -56,3 +56,35 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     rc, _, err = _noalloc(gpu.lib, gpu.f2_device_ptr(0, 0), wl.grid, ne=2048)
     assert rc == abi.RAMGPU_OK - 1 and "1024" in err
     gpu.close()
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    """The call waits for its stream, so on a stream under capture it must
+    return RAMGPU_ERR_STATE and leave the capture intact (it ends cleanly)."""
+    torch = pytest.importorskip("torch")
+    wl = W.make_workload("tiny")
+    gpu = abi.RamGpu(wl.grid, wl.fields)
+    gpu.upload_f2(0, 0, wl.f2[0])
+    rc0, ref, err0 = _noalloc(gpu.lib, gpu.f2_device_ptr(0, 0), wl.grid)  # the set-up call, before capture
+    assert rc0 == 0, err0
+    x = torch.zeros(4, device="cuda")
+    st = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    out = ctypes.c_double(0.0)
+    we, wmu, ekev = (np.ascontiguousarray(a, dtype=np.float64) for a in (wl.grid.we, wl.grid.wmu, wl.grid.ekev))
+    with torch.cuda.graph(g, stream=st):
+        x += 1.0
+        rc = gpu.lib.ramgpu_sumrc_noalloc(ctypes.c_void_p(gpu.f2_device_ptr(0, 0)), wl.grid.nr, wl.grid.nt,
+                                          wl.grid.ne, wl.grid.npa, we.ctypes.data_as(abi._P),
+                                          wmu.ctypes.data_as(abi._P), ekev.ctypes.data_as(abi._P),
+                                          ctypes.c_void_p(st.cuda_stream), ctypes.byref(out))
+    assert rc == -3
+    buf = ctypes.create_string_buffer(256)
+    gpu.lib.ramgpu_last_error(None, buf, 256)
+    assert b"captured" in buf.value
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(x[0]) == 1.0
+    rc1, again, err1 = _noalloc(gpu.lib, gpu.f2_device_ptr(0, 0), wl.grid)
+    assert rc1 == 0 and again == ref, err1
+    gpu.close()
