@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 RAM kinetic step.
 
-Workload (default): the four-species step on the standard RAM grid
+Headline workload: the four-species step on the standard RAM grid
 (e-, H+, He+, O+; NR=20 x NT=25 x NE=35 x NPA=72 = 1,260,000 cells per
 species; dipole field, Volland-Stern potential with Kp rising 1->6 over
 4320 DTs steps, DTs = 5 s).  One bench step is one ram_run call: the Strang
@@ -9,14 +9,22 @@ pair R,P,E,MU,CEX,ATMOL | ATMOL,CEX,MU,E,P,R for every species, the periodic
 copy, the magnetopause mask, DtsNext and the ANISCH moments -- two DTs
 steps, i.e. 2 x 4 x 1.26e6 = 10.08e6 cell-updates.
 
+Sections of the same line: the single-species step (H+, Kp 3, L2-resident),
+the refined 40x49x70x144 four-species grid (its F2 exceeds L2), WPADIF on
+the electrons, the 256-member uneven ensemble run from its first step to
+the last retirement (members split over the ranks under torchrun), and the
+2-hour adjoint window with checkpoints every 64 steps.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 Prints one JSON line (rank 0).  Under torchrun every rank advances its own
-replica of the workload on its own GPU (the path has no exchange step).
+replica of the headline workload on its own GPU (the path has no exchange
+step); the ensemble's members are partitioned over the ranks.
 """
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import math
 import os
@@ -32,24 +40,33 @@ sys.path.insert(0, str(ROOT / "ram-scb_gb300"))
 
 METRIC = "FP64 cell-updates/s"
 UNIT = "cell-updates/s"
-# FP64 instructions per cell of each sweep kernel (csrc/sweeps.cu): ncu's
-# sm__inst_executed_pipe_fp64 x 32 lanes / cells, the mean of its forward
-# and reverse launches on the four-species standard grid (the forward E and
-# MU carry the CFL quotient's multiply; DRIFTE's forward computes and stores
-# its face coefficients, the reverse loads them).  Per face this is the
-# formulation's own count: X, coefficient, a-term, face fma and the two
-# update operations (beta*|X|, the CFL quotients and the flux C*FBND are
-# formed on the integer pipe); DRIFTMU's lines are split between lane
-# pairs, whose second lane recomputes the face at the split.
-FP64_OPS_PER_CELL = {"driftr": 6.22, "driftp": 5.55, "drifte": 0.5 * (6.71 + 4.78), "driftmu": 0.5 * (6.81 + 5.84)}
-# DRAM bytes (read + write) per launch of each sweep on the four-species
-# standard grid, the mean of its forward and reverse launches in one ncu
-# capture (profiles/sweeps_four_sp.md, current kernels): F2 is read once
-# and the written lines stay in L2 within a launch; the forward MU also
-# reads the fused CEX/ATMOL factor, and DRIFTE stores and reloads its face
-# coefficients.
-NCU_DRAM_BYTES = {"four_sp": {"driftr": 0.5 * (44.6e6 + 44.3e6), "driftp": 0.5 * (40.6e6 + 40.6e6),
-                               "drifte": 0.5 * (111.0e6 + 129.8e6), "driftmu": 0.5 * (81.8e6 + 40.3e6)}}
+
+# Figures of one ncu capture of the four-species step, labelled with the
+# digest of the sweep sources they were taken from: DRAM bytes (read + write)
+# per launch and FP64 instructions per cell (DADD + DFMA + DMUL thread
+# instructions / cells), each the mean of the sweep's forward and reverse
+# launch.  The line reports whether the current sources still have that
+# digest; a changed kernel makes the figures stale until the next capture.
+NCU_CAPTURE = {
+    "sources_sha16": "unknown",
+    "command": ("ncu --set full --clock-control none -k regex:k_sweep -c 8 -o sweeps "
+                "python bench.py --steps 2 --warmup 1 --no-cpu-baseline --no-e2e --no-autotune "
+                "--members 0 --adj-calls 0 --no-padif --flush-mb 160"),
+    "dram_bytes": {"four_sp": {"driftr": 0.5 * (44.6e6 + 44.3e6), "driftp": 0.5 * (40.6e6 + 40.6e6),
+                               "drifte": 0.5 * (111.0e6 + 129.8e6), "driftmu": 0.5 * (81.8e6 + 40.3e6)}},
+    "fp64_ops_per_cell": {"driftr": 6.22, "driftp": 5.55, "drifte": 0.5 * (6.71 + 4.78),
+                          "driftmu": 0.5 * (6.81 + 5.84)},
+}
+SWEEP_SOURCES = ["ram-scb_gb300/csrc/sweeps.cu", "ram-scb_gb300/csrc/ramgpu_internal.cuh",
+                 "ram-scb_gb300/csrc/kernels.cuh"]
+SECTIONS = ("headline", "single", "refined", "padif", "ensemble", "adjoint")
+
+
+def sources_sha16():
+    h = hashlib.sha256()
+    for p in SWEEP_SOURCES:
+        h.update((ROOT / p).read_bytes())
+    return h.hexdigest()[:16]
 
 
 def parse():
@@ -59,47 +76,53 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="four_sp", choices=["four_sp", "single_h", "refined"])
+    ap.add_argument("--sections", default=",".join(SECTIONS),
+                    help="comma-separated subset of " + ",".join(SECTIONS))
     ap.add_argument("--cpu-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--flush-mb", type=int, default=256)
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--no-padif", action="store_true", help="skip the step timed with WPADIF on")
     ap.add_argument("--no-coef-store", action="store_true",
                     help="recompute the face coefficients in the reverse half instead of storing them")
-    ap.add_argument("--members", type=int, default=256, help="ensemble members (0: skip)")
-    ap.add_argument("--ensemble-steps", type=int, default=6)
+    ap.add_argument("--members", type=int, default=256, help="ensemble members")
+    ap.add_argument("--ensemble-calls", type=int, default=0,
+                    help="ram_run calls of the ensemble run (0: until the last member retires)")
     ap.add_argument("--loop-members", type=int, default=16)
     ap.add_argument("--adj-calls", type=int, default=720,
-                    help="adjoint window in ram_run calls (720 = 1440 DTs steps = 2 h); 0: skip")
+                    help="adjoint window in ram_run calls (720 = 1440 DTs steps = 2 h)")
     ap.add_argument("--adj-ckpt", type=int, default=32, help="checkpoint spacing in calls (32 = 64 steps)")
-    ap.add_argument("--adj-fd", type=int, default=4, help="finite-difference directions on the full window")
+    ap.add_argument("--adj-fd", type=int, default=16, help="finite-difference directions on the full window")
     ap.add_argument("--adj-members", type=int, default=64, help="batched-gradient members (0: skip)")
     ap.add_argument("--adj-member-calls", type=int, default=36)
-    ap.add_argument("--only", choices=["adjoint"], default=None,
-                    help="run one section alone (profiling); prints its result as JSON")
     # internal: one CPU-oracle timing in a fresh process (see cpu_leg_fresh)
     ap.add_argument("--cpu-leg", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--cpu-outer", type=int, default=1, help=argparse.SUPPRESS)
     ap.add_argument("--cpu-inner", type=int, default=1, help=argparse.SUPPRESS)
     ap.add_argument("--cpu-calls", type=int, default=0, help=argparse.SUPPRESS)
     ap.add_argument("--cpu-warmup", type=int, default=1, help=argparse.SUPPRESS)
-    return ap.parse_args()
+    args = ap.parse_args()
+    args.sections = {s.strip() for s in args.sections.split(",") if s.strip()}
+    bad = args.sections - set(SECTIONS)
+    if bad:
+        ap.error(f"unknown sections {sorted(bad)}")
+    return args
 
 
 def workload_desc(wl):
     g = wl.grid
+    kp = "Kp 3" if wl.name == "single_h" else "Kp ramp 1->6"
     return (f"{wl.name}: {len(g.species)} species ({','.join(wl.meta['species'])}) "
-            f"{g.nr}x{g.nt}x{g.ne}x{g.npa}, Kp ramp 1->6 (VOLS), DTs={wl.dts}s")
+            f"{g.nr}x{g.nt}x{g.ne}x{g.npa}, {kp} (VOLS), DTs={wl.dts}s")
 
 
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return float(d.get("hbm_gbs", 6800.0)), "measured"
-    return 6800.0, "fallback"
+        return float(d.get("hbm_gbs", 6800.0)), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    return 6800.0, "fallback (6.8 TB/s)"
 
 
 # --------------------------------------------------------------- clocks
@@ -164,6 +187,14 @@ def max_over_ranks(value: float, device=None) -> float:
     return float(t.item())
 
 
+def sum_over_ranks(values, device=None):
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t)
+    return [float(x) for x in t.tolist()]
+
+
 # ------------------------------------------------------------ CPU legs
 def cpu_threads(ns):
     """(species threads, line threads per species) using every host core:
@@ -214,11 +245,11 @@ def cpu_leg_main(args):
 
 
 def cpu_leg_fresh(workload, outer, inner, calls=0, seconds=10.0, warmup=1):
-    """The CPU oracle timed in a fresh interpreter: the measuring process
-    holds no CUDA context, torch thread pool or GPU work of its own, so the
-    figure is the one a reference run on the same cores would see (timed in
-    the GPU process after its GPU sections, the line threads inside each
-    species did not run: the leg measured the species-threads-only rate)."""
+    """The CPU oracle timed in a fresh interpreter that imports neither torch
+    nor the CUDA library, so the figure is the one a reference run on the
+    same cores sees.  (Timed inside the GPU process after its GPU sections,
+    the line threads inside each species did not run: that leg measured the
+    species-threads-only rate.)"""
     cmd = [sys.executable, str(ROOT / "bench.py"), "--cpu-leg", workload, "--cpu-outer", str(outer),
            "--cpu-inner", str(inner), "--cpu-calls", str(calls), "--cpu-seconds", str(seconds),
            "--cpu-warmup", str(warmup)]
@@ -226,19 +257,19 @@ def cpu_leg_fresh(workload, outer, inner, calls=0, seconds=10.0, warmup=1):
     return json.loads(r.stdout.strip().splitlines()[-1])
 
 
-def cpu_baseline_fresh(workload, ns, seconds):
+def cpu_baseline_fresh(workload, ns, seconds, calls=0, warmup=1):
     """Both CPU variants of the reference's path, each in a fresh process:
     (1) OpenMP over species only, as the reference (at most nS threads);
     (2) every host core: species threads x line threads inside each routine.
     The line's value is variant 2."""
     cores = os.cpu_count() or 1
     o2, i2 = cpu_threads(ns)
-    v1 = cpu_leg_fresh(workload, min(ns, cores), 1, seconds=seconds)
-    v2 = cpu_leg_fresh(workload, o2, i2, seconds=seconds)
+    v1 = cpu_leg_fresh(workload, min(ns, cores), 1, calls=calls, seconds=seconds, warmup=warmup)
+    v2 = cpu_leg_fresh(workload, o2, i2, calls=calls, seconds=seconds, warmup=warmup)
     return {"value": v2["value"], "unit": UNIT, "cores": o2 * i2, "kind": "port",
-            "sample": (f"{v2['calls']} ram_run calls of the workload in {v2['elapsed_s']:.1f} s after 1 warm-up call, "
-                       f"fresh process; C restatement of the reference routines (-O3 -ffp-contract=off, no Fortran "
-                       f"compiler), OpenMP over {o2} species x {i2} line threads"),
+            "sample": (f"{v2['calls']} ram_run calls of the workload in {v2['elapsed_s']:.1f} s after {warmup} "
+                       f"warm-up call(s), fresh process; C restatement of the reference routines (-O3 "
+                       f"-ffp-contract=off, no Fortran compiler), OpenMP over {o2} species x {i2} line threads"),
             "variants": {"species_threads": {"value": v1["value"], "threads": v1["outer"], "calls": v1["calls"],
                                              "elapsed_s": v1["elapsed_s"]},
                          "all_cores": {"value": v2["value"], "threads": o2 * i2, "calls": v2["calls"],
@@ -254,11 +285,11 @@ def run_reference(args, rank, world):
     ns = len(wl.grid.species)
     outer, inner = cpu_threads(ns)
     # W untimed warm-up steps, then exactly K timed steps; a step is one
-    # ram_run call of the workload (about 0.3 s on 16 host cores)
+    # ram_run call of the workload (about 0.1 s on 16 host cores)
     v, n, el = cpu_time_oracle(wl, 0.0, outer, inner, calls=max(1, args.steps), warmup=args.warmup)
     sample = (f"{n} ram_run calls of the workload ({workload_desc(wl)}) after {args.warmup} warm-up "
-              f"calls, {el:.1f} s; C restatement of the reference routines (no Fortran compiler), "
-              f"OpenMP over {outer} species x {inner} line threads")
+              f"calls, {el:.1f} s; C restatement of the reference routines (-O3 -ffp-contract=off, no Fortran "
+              f"compiler), OpenMP over {outer} species x {inner} line threads")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * el / n, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -269,87 +300,417 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-# ------------------------------------------------------------ GPU leg
-def run_ensemble(args, torch, dev, stream):
-    """Batched ensemble (256 uneven members on the standard grid) against
-    looping the plain single-member GPU step; returns a dict for the line."""
-    import numpy as np
+# ------------------------------------------------------------ GPU pieces
+def new_model(abi, wl, stream, members=1):
+    gpu = abi.RamGpu(wl.grid, wl.fields, n_members=members)
+    gpu.set_stream(stream.cuda_stream)
+    for m in range(members):
+        for s in range(len(wl.grid.species)):
+            gpu.upload_f2(m, s, wl.f2[s])
+            gpu.set_boundary(m, s, wl.fgeos[s])
+    return gpu
 
-    from ramgpu import abi, workload as W
+
+def timed_steps(torch, gpu, stream, wl, steps, flush, start=0):
+    """`steps` graph-replayed ram_run calls along the workload's Kp driver,
+    L2 flushed (a write larger than L2) before each, each bracketed by CUDA
+    events on the launching stream; returns the per-call ms and the number
+    of kernel launches."""
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    l0 = gpu.launch_count()
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+        gpu.set_kp(-1, wl.kp(2 * (start + k)))
+        ev[k][0].record(stream)
+        gpu.ram_run_async(wl.dts)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev], gpu.launch_count() - l0
+
+
+def kernel_pass(torch, gpu, stream, wl, flush, n):
+    """Per-kernel durations: n calls with events around every launch group
+    on the launching stream (timing mode runs direct launches on one
+    stream); returns ({class: (ms, launches)}, mean call ms)."""
+    gpu.set_timing(True)
+    gpu.kernel_times()
+    ms = []
+    for k in range(n):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+        gpu.set_kp(-1, wl.kp(2 * k))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        gpu.ram_run_async(wl.dts)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    kt = gpu.kernel_times()
+    gpu.set_timing(False)
+    return kt, statistics.mean(ms)
+
+
+def roofline(kt, wl, nitems, hbm_peak, peak_kind, fp64_peak, workload):
+    """HBM view of the dominant sweep: 16 B per cell (F2 read + write once)
+    over its event-timed launch; the FP64 view beside it."""
+    sweep = {k: v for k, v in kt.items() if k.startswith("drift")}
+    dom = max(sweep, key=lambda k: sweep[k][0])
+    dom_ms = sweep[dom][0] / sweep[dom][1]
+    cells = wl.grid.ncell * nitems
+    achieved = 16.0 * cells / (dom_ms / 1e3) / 1e9
+    current = sources_sha16() == NCU_CAPTURE["sources_sha16"]
+    ops = NCU_CAPTURE["fp64_ops_per_cell"][dom]
+    fp64 = ops * cells / (dom_ms / 1e3) / 1e9
+    traffic = NCU_CAPTURE["dram_bytes"].get(workload, {}).get(dom)
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+            "traffic": traffic if current else None, "kernel": dom, "kernel_ms": dom_ms, "peak_kind": peak_kind,
+            "traffic_source": {"capture": NCU_CAPTURE["command"], "sources_sha16": NCU_CAPTURE["sources_sha16"],
+                               "current_sources_sha16": sources_sha16(), "matches_current_sources": current,
+                               "workload": workload if traffic is not None else None},
+            "algorithmic_bytes_per_launch": 16.0 * cells,
+            "fp64": {"achieved": fp64, "peak": fp64_peak, "unit": "G lane-ops/s", "frac": fp64 / fp64_peak,
+                     "ops_per_cell": ops, "ops_per_cell_from_current_sources": current,
+                     "peak_kind": "measured live (fma loop, ramgpu_probe_fp64)"},
+            "sweeps_GBps": {k: 16.0 * cells / (v[0] / v[1] / 1e3) / 1e9 for k, v in sweep.items()}}
+
+
+def e2e_section(torch, np, abi, gpu, wl, steps):
+    """The metric end to end through the C ABI with host buffers, full F2 in
+    and out every call, as the reference's host array F2 is: the per-species
+    pipelined call from page-locked and from ordinary memory, the same
+    traffic serialised on one stream, and the call on F2 in the reference's
+    own layout F2(NS,NR,NT,NE,NPA) (page-locked and ordinary)."""
+    g = wl.grid
+    ns = len(g.species)
+    cells_per_step = 2 * g.ncell * ns
+    nm2 = g.nr * g.nt
+    pin = [torch.empty(g.ncell, dtype=torch.float64, pin_memory=True) for _ in range(ns)]
+    host = [np.reshape(p.numpy(), (g.nr, g.nt, g.ne, g.npa), order="F") for p in pin]
+    mom_t = torch.empty(2 * ns * nm2, dtype=torch.float64, pin_memory=True)
+    mom = mom_t.numpy()
+    pe_h = [mom[s * nm2:(s + 1) * nm2] for s in range(ns)]
+    pa_h = [mom[(ns + s) * nm2:(ns + s + 1) * nm2] for s in range(ns)]
+    for s in range(ns):
+        host[s][...] = gpu.download_f2(0, s)
+    host_pg = [np.asfortranarray(a).copy(order="F") for a in host]
+    pe_pg = [np.zeros(nm2) for _ in range(ns)]
+    pa_pg = [np.zeros(nm2) for _ in range(ns)]
+    ref_pin_t = torch.empty(ns * g.ncell, dtype=torch.float64, pin_memory=True)
+    ref_pin = np.reshape(ref_pin_t.numpy(), (ns, g.nr, g.nt, g.ne, g.npa), order="F")
+    ref_pin[...] = np.stack([np.asarray(a) for a in host], axis=0)
+    mref_t = torch.empty(2 * ns * nm2, dtype=torch.float64, pin_memory=True)
+    mref = mref_t.numpy()
+    pe_ref, pa_ref = mref[:ns * nm2], mref[ns * nm2:]
+    ref_pg = ref_pin.copy(order="F")
+    pe_ref_pg, pa_ref_pg = np.zeros(ns * nm2), np.zeros(ns * nm2)
+    lib, h = gpu.lib, gpu.h
+    hp = [a.ctypes.data_as(abi._P) for a in host]
+
+    def pipelined(k):
+        gpu.set_kp(-1, wl.kp(2 * k))
+        gpu.ram_run_host(wl.dts, host, pe_h, pa_h)
+
+    def pageable(k):
+        gpu.set_kp(-1, wl.kp(2 * k))
+        gpu.ram_run_host(wl.dts, host_pg, pe_pg, pa_pg)
+
+    def serial(k):
+        for s in range(ns):
+            gpu._ck(lib.ramgpu_upload_f2_async(h, 0, s, hp[s]), "upload")
+        gpu.set_kp(-1, wl.kp(2 * k))
+        gpu.ram_run_async(wl.dts)
+        for s in range(ns):
+            gpu._ck(lib.ramgpu_download_f2_async(h, 0, s, hp[s]), "download")
+            gpu._ck(lib.ramgpu_moments_async(h, 0, s, pe_h[s].ctypes.data_as(abi._P),
+                                             pa_h[s].ctypes.data_as(abi._P)), "moments")
+        gpu._ck(lib.ramgpu_synchronize(h), "synchronize")
+
+    def ref_layout(k):
+        gpu.set_kp(-1, wl.kp(2 * k))
+        gpu.ram_run_ref(wl.dts, [ref_pin], [pe_ref], [pa_ref])
+
+    def ref_layout_pageable(k):
+        gpu.set_kp(-1, wl.kp(2 * k))
+        gpu.ram_run_ref(wl.dts, [ref_pg], [pe_ref_pg], [pa_ref_pg])
+
+    med = {}
+
+    def run(fn):
+        fn(0)  # warm (first use creates the group streams, captures the graph)
+        torch.cuda.synchronize()
+        ts = []
+        t0 = time.perf_counter()
+        for k in range(steps):
+            t1 = time.perf_counter()
+            fn(k)
+            ts.append(time.perf_counter() - t1)
+        med[fn.__name__] = 1e3 * statistics.median(ts)
+        return cells_per_step * steps / max(time.perf_counter() - t0, 1e-9)
+
+    out = {"value": None, "unit": UNIT, "h2d_bytes_per_step": 8 * g.ncell * ns,
+           "d2h_bytes_per_step": 8 * g.ncell * ns + 16 * nm2 * ns,
+           "path": (f"ramgpu_set_kp + ramgpu_ram_run_host (page-locked host F2 of {ns} species in and out, "
+                    f"moments of {ns} species out; pipelined over species groups), every step")}
+    out["value"] = run(pipelined)
+    out["pageable_value"] = run(pageable)
+    out["serial_value"] = run(serial)
+    out["ref_layout_value"] = run(ref_layout)
+    out["ref_layout_pageable_value"] = run(ref_layout_pageable)
+    out["ms_per_step_median"] = dict(med)
+    out["pageable_path"] = "ramgpu_ram_run_host with ordinary (pageable) host arrays"
+    out["serial_path"] = ("ramgpu_upload_f2_async x NS + ramgpu_ram_run_async + ramgpu_download_f2_async x NS "
+                          "+ ramgpu_moments_async x NS + ramgpu_synchronize on one stream")
+    out["ref_layout_path"] = ("ramgpu_ram_run_ref on F2(NS,NR,NT,NE,NPA) and PPERT/PPART(NS,NR,NT) as RAM holds "
+                              "them (page-locked; _pageable: ordinary memory), transposed on the device")
+    del pin, mom_t, ref_pin_t, mref_t
+    return out
+
+
+def measure(args, torch, np, abi, W, stream, name, steps, warmup, world=1, clocks=False, e2e_steps=0,
+            kernel_steps=3):
+    """One workload: autotune, graph-replayed timed calls (L2 flushed), the
+    per-kernel pass, the roofline and optionally the end-to-end figures."""
+    wl = W.make_workload(name)
+    g = wl.grid
+    ns = len(g.species)
+    gpu = new_model(abi, wl, stream)
+    gpu.set_kp(-1, wl.kp(0))
+    if args.no_coef_store:
+        gpu.set_coef_store(0)
+    if args.no_autotune:
+        shapes, trials = gpu.launch_shape(), None
+    else:
+        shapes, _ = gpu.autotune(wl.dts)
+        pl, pe = gpu.autotune_trials()
+        trials = {"plain_ms": [round(x, 5) for x in pl], "persistent_ms": [round(x, 5) for x in pe]}
+    groups = gpu.step_groups()
+    gpu.set_graph(not args.no_graph)
+    flush = torch.empty(max(1, args.flush_mb) << 20, dtype=torch.uint8, device="cuda")
+    for w in range(warmup):
+        gpu.set_kp(-1, wl.kp(2 * w))
+        gpu.ram_run(wl.dts)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(torch.cuda.current_device()) if clocks else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    # an NVTX range marks the timed steps, so that a profiler can select
+    # exactly their launches (ncu --nvtx --nvtx-include "ram_run_timed_four_sp/")
+    nvtx = getattr(torch.cuda, "nvtx", None)
+    if nvtx is not None:
+        nvtx.range_push(f"ram_run_timed_{name}")
+    wall0 = time.perf_counter()
+    ms, launches = timed_steps(torch, gpu, stream, wl, steps, flush, start=warmup)
+    wall = time.perf_counter() - wall0
+    if nvtx is not None:
+        nvtx.range_pop()
+    clk = sampler.stop() if sampler else None
+    total_ms = sum(ms)
+    if world > 1:
+        total_ms = max_over_ranks(total_ms, torch.device("cuda"))
+    cells_per_step = 2 * g.ncell * ns
+    kt, kt_ms = kernel_pass(torch, gpu, stream, wl, flush, max(3, kernel_steps))
+    hbm_peak, peak_kind = measured_peaks()
+    fp64_peak = abi.probe_fp64() / 1e9
+    out = {"workload": workload_desc(wl), "cells_per_step": cells_per_step,
+           "value": world * cells_per_step * steps / (total_ms / 1e3), "ms_per_step": total_ms / steps,
+           "steps": steps, "warmup": warmup, "launches": launches, "wall_s": wall, "clocks": clk,
+           "launch_shapes": shapes, "autotune_trials": trials, "item_groups": groups,
+           "kernels_ms": {k: round(v[0] / v[1], 5) for k, v in kt.items()}, "kernel_pass_ms_per_step": kt_ms,
+           "roofline": roofline(kt, wl, ns, hbm_peak, peak_kind, fp64_peak, name)}
+    per_gpu = out["value"] / world
+    out["roofline"]["step"] = {"fused_min_GBps": per_gpu * 16 / 1e9, "fused_min_frac": per_gpu * 16 / 1e9 / hbm_peak,
+                               "unfused_GBps": per_gpu * 80 / 1e9, "unfused_frac": per_gpu * 80 / 1e9 / hbm_peak}
+    if e2e_steps:
+        e = e2e_section(torch, np, abi, gpu, wl, e2e_steps)
+        for k in ("value", "pageable_value", "serial_value", "ref_layout_value", "ref_layout_pageable_value"):
+            e[k] *= world
+        out["e2e"] = e
+    gpu.close()
+    return out
+
+
+def run_padif(torch, abi, W, stream, args):
+    """The four-species step with WPADIF on the electrons (both halves),
+    per-kernel timed."""
+    wl = W.make_workload("four_sp")
+    g = wl.grid
+    gpu = new_model(abi, wl, stream)
+    flush = torch.empty(max(1, args.flush_mb) << 20, dtype=torch.uint8, device="cuda")
+    _, base_ms = kernel_pass(torch, gpu, stream, wl, flush, 3)
+    gpu.set_pa_diffusion(0, W.pa_diffusion(g, wl.fields))
+    kt, step_ms = kernel_pass(torch, gpu, stream, wl, flush, 3)
+    gpu.close()
+    pk = kt.get("padif", (0.0, 1))
+    per = pk[0] / max(pk[1], 1)
+    # algorithmic bytes of the two launches per step: the electrons' solve
+    # reads F2 and the three elimination tables and writes F2 (40 B per
+    # cell) in both; the first also applies the loss factor to the other
+    # three species (F2 and factor in, F2 out: 24 B per cell)
+    byts = 0.5 * (40.0 + 40.0 + 3 * 24.0) * g.ncell
+    return {"species": "Electron (WPADIF after the drifts and before the reverse drifts)",
+            "step_ms": step_ms, "step_ms_without": base_ms, "kernel_ms_per_launch": per, "launches": pk[1],
+            "algorithmic_GBps": byts / (per / 1e3) / 1e9 if per > 0 else None}
+
+
+def run_ensemble(args, torch, np, abi, W, stream, rank, world):
+    """Config 4: 256 members on the standard grid (1-4 species, Kp drivers
+    piecewise linear on a 30-min cadence drawn uniform 1-7, density scale
+    lognormal sigma 0.5, lengths uniform 360-1440 DTs steps), run from step
+    0 until the last member retires, batched in one graph-replayed ram_run
+    per call; members partitioned over the ranks by work.  Against: the
+    plain single-member step looped, and sampled members' solo runs."""
+    from ramgpu import shard
 
     ens = W.make_ensemble(args.members)
     base = ens.base
     g = base.grid
-    gpu = abi.RamGpu(g, base.fields, n_members=ens.members)
+    parts = shard.partition_members(shard.member_work(ens.species, ens.length), world)
+    mine = parts[rank]
+    nm = len(mine)
+    gpu = abi.RamGpu(g, base.fields, n_members=nm)
     gpu.set_stream(stream.cuda_stream)
-    for m in range(ens.members):
-        gpu.set_member_species(m, ens.species[m])
-        for s in ens.species[m]:
-            gpu.upload_f2(m, s, base.f2[s] * ens.scale[m])
-            gpu.set_boundary(m, s, base.fgeos[s] * ens.scale[m])
-    t0 = 356  # sample from DTs step 356 on: members with length < t0 + 2K retire inside it
-    gpu.set_kp_all(ens.kp(t0))
+
+    def load(model, members):
+        for i, m in enumerate(members):
+            model.set_member_species(i, ens.species[m])
+            for s in ens.species[m]:
+                model.upload_f2(i, s, base.f2[s] * ens.scale[m])
+                model.set_boundary(i, s, base.fgeos[s] * ens.scale[m])
+
+    load(gpu, mine)
+    gpu.set_kp_all(ens.kp(0)[mine])
     shapes, _ = gpu.autotune(base.dts)
-    gpu_groups = gpu.step_groups()
+    pl, pe = gpu.autotune_trials()
+    groups = gpu.step_groups()
     gpu.set_graph(True)
-    flush = torch.empty(max(1, args.flush_mb) << 20, dtype=torch.uint8, device=dev)
-    for w in range(2):  # warm-up (captures the graph)
-        gpu.ram_run(base.dts)
-    K = max(2, min(args.ensemble_steps, 20))
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    gpu.ram_run(base.dts)  # captures the graph; the run then starts from the initial state
+    load(gpu, mine)
+    flush = torch.empty(max(1, args.flush_mb) << 20, dtype=torch.uint8, device="cuda")
+    length = np.asarray(ens.length)[mine]
+    ncalls = int(math.ceil(length.max() / 2)) if args.ensemble_calls <= 0 else args.ensemble_calls
+    active = np.ones(nm, dtype=bool)
+    nspec = np.array([len(ens.species[m]) for m in mine])
+    last_call = np.zeros(nm, dtype=int)
+    ev = []
     member_steps = 0
     cell_updates = 0
-    dead = set()
-    for k in range(K):
-        step = t0 + 2 * k
-        for m in range(ens.members):  # finished members retire
-            if step >= ens.length[m] and m not in dead:
-                gpu.set_member_active(m, False)
-                dead.add(m)
-        active = [m for m in range(ens.members) if step < ens.length[m]]
-        member_steps += 2 * len(active)
-        cell_updates += 2 * g.ncell * sum(len(ens.species[m]) for m in active)
-        gpu.set_kp_all(ens.kp(step))
-        with torch.cuda.stream(stream):
-            flush.fill_(k & 0xFF)
-        ev[k][0].record(stream)
-        gpu.ram_run_async(base.dts)
-        ev[k][1].record(stream)
-    torch.cuda.synchronize(dev)
-    batched_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
-    retired = len(dead)
-    # looped: the plain single-member step (direct launches), one member at a time
-    gpu.set_graph(False)
-    sub = list(range(0, ens.members, max(1, ens.members // args.loop_members)))[:args.loop_members]
-    for m in range(ens.members):
-        gpu.set_member_active(m, False)
-    lev = []
-    for m in sub:
-        gpu.set_member_active(m, True)
-        gpu.set_kp_all(ens.kp(t0))
-        gpu.ram_run(base.dts)  # warm (rebuilds the work list)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    wall0 = time.perf_counter()
+    for c in range(ncalls):
+        step = 2 * c
+        for i in np.nonzero(active & (step >= length))[0]:  # finished members retire
+            gpu.set_member_active(int(i), False)
+            active[i] = False
+        if not active.any():
+            break
+        member_steps += 2 * int(active.sum())
+        cell_updates += 2 * g.ncell * int(nspec[active].sum())
+        last_call[active] = c
+        gpu.set_kp_all(ens.kp(step)[mine])
+        if c % 8 == 0:  # the state (GBs) is far larger than L2; flush now and then as well
+            with torch.cuda.stream(stream):
+                flush.fill_(c & 0xFF)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            flush.fill_(m & 0xFF)
         a.record(stream)
         gpu.ram_run_async(base.dts)
         b.record(stream)
-        torch.cuda.synchronize(dev)
+        ev.append((a, b))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    batched_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    # per-member diagnostics: the sum of PPERT of each species after the
+    # member's last call, gathered on every rank
+    rows = {m: [float(np.sum(gpu.moments(i, s)[0])) for s in ens.species[m]] for i, m in enumerate(mine)}
+    allrows = shard.gather_member_rows(rows, world, rank, ens.members, torch.distributed if world > 1 else None)
+    if world > 1:
+        batched_s = max_over_ranks(batched_s, torch.device("cuda"))
+        member_steps, cell_updates = sum_over_ranks([member_steps, cell_updates], torch.device("cuda"))
+    # the persistent grids the configuration names, forced on every sweep
+    # (2 CTAs per SM looping over the work units), against the tuned shapes,
+    # a few calls with every member active again
+    for i in range(nm):
+        gpu.set_member_active(i, True)
+    gpu.set_kp_all(ens.kp(0)[mine])
+
+    def sample(n=4):
+        gpu.ram_run(base.dts)  # recapture for the shapes
+        t = []
+        for k in range(n):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            gpu.ram_run_async(base.dts)
+            b.record(stream)
+            torch.cuda.synchronize()
+            t.append(a.elapsed_time(b))
+        return statistics.median(t)
+
+    tuned_ms = sample()
+    nsm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    for w, (thr, _) in enumerate(shapes):
+        gpu.set_launch_shape(w, thr, 2 * nsm)
+    persistent_ms = sample()
+    for w, (thr, pc) in enumerate(shapes):
+        gpu.set_launch_shape(w, thr, pc)
+    # looped: the plain single-member step (direct launches), one member at a time
+    gpu.set_graph(False)
+    sub = list(range(0, nm, max(1, nm // args.loop_members)))[:args.loop_members]
+    for i in range(nm):
+        gpu.set_member_active(i, False)
+    lev = []
+    for i in sub:
+        gpu.set_member_active(i, True)
+        gpu.set_kp_all(ens.kp(0)[mine])
+        gpu.ram_run(base.dts)  # warm (rebuilds the work list)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xFF)
+        a.record(stream)
+        gpu.ram_run_async(base.dts)
+        b.record(stream)
+        torch.cuda.synchronize()
         lev.append(a.elapsed_time(b) / 1e3)
-        gpu.set_member_active(m, False)
-    looped_per_member = statistics.mean(lev)
+        gpu.set_member_active(i, False)
     gpu.close()
+    # solo runs of a few members over their whole length equal the batched run
+    solo_diff = 0.0
+    solo_members = [mine[i] for i in sub[:3]]
+    for m in solo_members:
+        solo = abi.RamGpu(g, base.fields, n_members=1)
+        solo.set_stream(stream.cuda_stream)
+        load(solo, [m])
+        solo.set_graph(True)
+        for c in range(int(last_call[mine.index(m)]) + 1):
+            solo.set_kp(0, float(ens.kp(2 * c)[m]))
+            solo.ram_run_async(base.dts)
+        torch.cuda.synchronize()
+        got = [float(np.sum(solo.moments(0, s)[0])) for s in ens.species[m]]
+        for x, y in zip(got, rows[m]):
+            solo_diff = max(solo_diff, abs(x - y) / max(abs(y), 1e-300))
+        solo.close()
+    looped = 2.0 / statistics.mean(lev)
     batched = member_steps / batched_s
-    looped = 2.0 / looped_per_member
     return {"members": ens.members, "member_species": int(sum(len(x) for x in ens.species)),
-            "steps": K, "retired_in_sample": retired,
+            "ranks": world, "members_per_rank": [len(p) for p in parts],
+            "calls": len(ev), "dts_steps": 2 * len(ev), "member_steps": int(member_steps),
+            "batched_s": batched_s, "wall_s": wall,
             "member_steps_per_s_batched": batched, "member_steps_per_s_looped": looped,
             "batched_over_looped": batched / looped,
             "cell_updates_per_s_batched": cell_updates / batched_s,
-            "looped_sample_members": len(sub), "launch_shapes": shapes,
-            "item_groups": gpu_groups,
-            "notes": "batched: one graph-replayed ram_run per step for all active members; "
-                     "looped: the plain direct-launch step of one member at a time"}
+            "looped_sample_members": len(sub), "launch_shapes": shapes, "item_groups": groups,
+            "autotune_trials": {"plain_ms": [round(x, 4) for x in pl], "persistent_ms": [round(x, 4) for x in pe]},
+            "persistent_all_sweeps_ms_per_call": persistent_ms, "tuned_ms_per_call": tuned_ms,
+            "solo_members": solo_members, "solo_vs_batched_max_rel_diff": solo_diff,
+            "diagnostics_gathered": sum(r is not None for r in allrows),
+            "notes": ("batched: the whole uneven run, from step 0 until the last member retires, one graph-replayed "
+                      "ram_run per call for all active members; looped: the plain direct-launch step of one member "
+                      "at a time; persistent: one persistent grid per sweep (2 CTAs per SM) with every member "
+                      "active, against the tuned shapes in the same state")}
 
 
 def _truth_observations(gpu, wl, kp, obs, ncalls, species, seed):
@@ -376,16 +737,26 @@ def _truth_observations(gpu, wl, kp, obs, ncalls, species, seed):
                 o["log_obs"] = math.log(sf[t, o["s"], o["k"], o["l"]])
 
 
-def run_adjoint(args, torch, dev, stream):
-    """Adjoint window on the four-species standard grid: 1440 DTs steps
-    (720 ram_run calls, Kp 1->6 ramp), 50 virtual-spacecraft samples on
-    circular equatorial orbits at L = 4-6, 10-200 keV, pitch-angle bin 2;
-    checkpoints every 64 steps.  Reports adjoint cost over the plain forward,
-    finite-difference checks on the full window, and a 64-member batched
-    gradient against looping single-member gradients."""
-    import numpy as np
+def _event_timer(torch, stream):
+    """Seconds on the device between this point of the stream and the point
+    where the returned function is called."""
+    a = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
 
-    from ramgpu import abi, sats, workload as W
+    def stop():
+        b = torch.cuda.Event(enable_timing=True)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / 1e3
+    return stop
+
+
+def run_adjoint(args, torch, np, abi, W, stream):
+    """Config 5: adjoint window on the four-species standard grid, 1440 DTs
+    steps (720 ram_run calls, Kp 1->6 ramp), 50 virtual-spacecraft samples on
+    circular equatorial orbits at L = 4-6, 10-200 keV, pitch-angle bin 2.
+    Forward and adjoint are timed with CUDA events on the same stream."""
+    from ramgpu import sats
 
     wl = W.make_workload("four_sp")
     g = wl.grid
@@ -404,6 +775,7 @@ def run_adjoint(args, torch, dev, stream):
         for s in range(ns):
             gpu.upload_f2(0, s, wl.f2[s])
             gpu.set_boundary(0, s, wl.fgeos[s])
+        torch.cuda.synchronize()
 
     reset()
     gpu.autotune(wl.dts)
@@ -412,47 +784,47 @@ def run_adjoint(args, torch, dev, stream):
         gpu.set_kp(-1, kp[c, 0])
         gpu.ram_run(wl.dts)
     reset()
-    torch.cuda.synchronize(dev)
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(stream)
+    stop = _event_timer(torch, stream)
     for c in range(nc):
         gpu.set_kp(-1, kp[c, 0])
         gpu.ram_run_async(wl.dts)
-    b.record(stream)
-    torch.cuda.synchronize(dev)
-    fwd_s = a.elapsed_time(b) / 1e3
-    reset()
-    gpu.adj_forward(2, wl.dts, kp[:2], 1, [])  # warm-up of the adjoint buffers and kernels
-    gpu.adj_backward()
-    # the library's policy: checkpoints every kc calls, the record ring keeps
-    # as many trailing segments as half of the free HBM holds (here all)
-    reset()
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    J = gpu.adj_forward(nc, wl.dts, kp, kc, obs)[0]
-    t1 = time.perf_counter()
-    gf, gb = gpu.adj_backward()
-    t2 = time.perf_counter()
-    nseg, nkeep = gpu.adj_segments()
-    # the same window with a one-segment ring: every earlier segment is
-    # recomputed from its checkpoint (the policy for windows that do not fit)
-    gpu.set_adj_record_budget(0)
-    reset()
-    torch.cuda.synchronize(dev)
-    t3 = time.perf_counter()
-    gpu.adj_forward(nc, wl.dts, kp, kc, obs)
-    t4 = time.perf_counter()
-    gfr, gbr = gpu.adj_backward()
-    t5 = time.perf_counter()
+    fwd_s = stop()
+
+    def window(k_ckpt, budget):
+        """A warm-up window (allocations) and a timed one: J, gradients,
+        forward and backward seconds, segments and kept segments."""
+        gpu.set_adj_record_budget(budget)
+        reset()
+        gpu.adj_forward(nc, wl.dts, kp, k_ckpt, obs)
+        gpu.adj_backward()
+        reset()
+        stop = _event_timer(torch, stream)
+        J = gpu.adj_forward(nc, wl.dts, kp, k_ckpt, obs)[0]
+        tf = stop()
+        stop = _event_timer(torch, stream)
+        gf, gb = gpu.adj_backward()
+        tb = stop()
+        nseg, nkeep = gpu.adj_segments()
+        return J, gf, gb, tf, tb, nseg, nkeep
+
+    # checkpoints every kc calls with a one-segment record ring: every
+    # earlier segment is recomputed from its checkpoint (the configuration's
+    # policy, and the one for windows whose records do not fit in HBM)
+    J, gfr, gbr, tfr, tbr, nseg, _ = window(kc, 0)
+    # the same checkpoints, the ring keeping as many segments as half of the
+    # free HBM holds (here all: nothing recomputed)
+    _, gf, gb, tfk, tbk, _, nkeep = window(kc, -1)
     gpu.set_adj_record_budget(-1)
-    same_r = max(float(np.max(np.abs(gfr - gf)) / np.max(np.abs(gf))),
-                 float(np.max(np.abs(gbr - gb)) / max(np.max(np.abs(gb)), 1e-300)))
-    # and as one segment (k = ncalls): the record of every call, no checkpoints
+
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+    same_r = max(rel(gfr, gf), rel(gbr, gb))
+    # one segment (k = ncalls): the record of every call, for the replays
     reset()
     gpu.adj_forward(nc, wl.dts, kp, nc, obs)
     gf2, gb2 = gpu.adj_backward()
-    same = max(float(np.max(np.abs(gf2 - gf)) / np.max(np.abs(gf))),
-               float(np.max(np.abs(gb2 - gb)) / max(np.max(np.abs(gb)), 1e-300)))
+    same = max(rel(gf2, gf), rel(gb2, gb))
     rng = np.random.Generator(np.random.PCG64(707))
 
     def fd_f2(r, eps, frozen):
@@ -464,15 +836,14 @@ def run_adjoint(args, torch, dev, stream):
         return (jj[0] - jj[1]) / (2 * eps)
 
     # finite differences of the frozen-limiter scheme (the record of the base
-    # run replayed): exact check of the adjoint on the whole window
-    # (J is the log of affine fluxes: Richardson extrapolation of two central
-    # differences removes the O(eps^2) term)
+    # run replayed, affine in F2): the exact check of the adjoint on the whole
+    # window, one central difference per direction (J is the log of affine
+    # fluxes: truncation ~ eps^2, rounding ~ 1e-16/eps)
     fd = []
     for d in range(max(0, args.adj_fd)):
         r = [rng.uniform(-1.0, 1.0, size=wl.f2[s].shape) for s in range(ns)]
         ad = sum(float(np.sum(gf2[0, s] * np.asarray(wl.f2[s]) * r[s])) for s in range(ns))
-        est = (4.0 * fd_f2(r, 1e-5, True) - fd_f2(r, 2e-5, True)) / 3.0
-        fd.append(abs(est - ad) / abs(ad))
+        fd.append(abs(fd_f2(r, 1e-6, True) - ad) / abs(ad))
     # unfrozen: perturbed runs re-decide every limiter branch (kinks crossed)
     unfrozen = {}
     if args.adj_fd > 0:
@@ -483,29 +854,27 @@ def run_adjoint(args, torch, dev, stream):
     reset()
     gpu.close()
     out = {"window_calls": nc, "window_dts_steps": 2 * nc, "checkpoint_calls": kc, "observations": len(obs),
-           "J": J, "forward_s": fwd_s, "adj_forward_s": t1 - t0, "adj_backward_s": t2 - t1,
-           "adjoint_over_forward": (t2 - t0) / fwd_s,
-           "segments": nseg, "segments_kept": nkeep, "record_bytes": 8 * g.ncell * ns * nc,
-           "policy": "checkpoints every checkpoint_calls calls; the branch-record ring keeps the last "
-                     "segments_kept segments (half of the free HBM as budget) and recomputes the rest",
-           "recompute": {"segments_kept": 1, "segments_recomputed": nseg - 1,
-                         "adj_forward_s": t4 - t3, "adj_backward_s": t5 - t4,
-                         "adjoint_over_forward": (t5 - t3) / fwd_s,
-                         "gradient_vs_kept_max_rel_diff": same_r},
+           "J": J, "forward_s": fwd_s, "timing": "CUDA events on the context's stream for forward and adjoint",
+           "adj_forward_s": tfr, "adj_backward_s": tbr, "adjoint_over_forward": (tfr + tbr) / fwd_s,
+           "segments": nseg, "segments_recomputed": nseg - 1,
+           "policy": ("checkpoints every checkpoint_calls calls; the branch-record ring keeps one segment; the "
+                      "forward pass records only that segment and runs the plain step elsewhere; the backward "
+                      "pass recomputes every earlier segment from its checkpoint, recording, then transposes"),
+           "records_kept": {"segments_kept": nkeep, "adj_forward_s": tfk, "adj_backward_s": tbk,
+                            "adjoint_over_forward": (tfk + tbk) / fwd_s,
+                            "record_bytes": 8 * g.ncell * ns * nc,
+                            "policy": "the ring keeps as many segments as half of the free HBM holds: none recomputed"},
+           "gradient_recompute_vs_kept_max_rel_diff": same_r,
            "single_segment_gradient_max_rel_diff": same,
            "fd_frozen_directions": len(fd), "fd_frozen_max_rel_err": max(fd) if fd else None,
-           "fd_frozen_eps": "Richardson of 1e-5 and 2e-5", "fd_unfrozen_rel_err": unfrozen,
-           "forward": "graph-replayed ram_run per call",
-           "adjoint": "recording forward with checkpoints + recompute of the segments not kept + transposed sweeps"}
+           "fd_frozen_eps": "central difference, eps = 1e-6", "fd_unfrozen_rel_err": unfrozen}
     if args.adj_members > 0:
-        out["batched"] = run_adjoint_batched(args, torch, dev, stream)
+        out["batched"] = run_adjoint_batched(args, torch, np, abi, W, stream)
     return out
 
 
-def run_adjoint_batched(args, torch, dev, stream):
-    import numpy as np
-
-    from ramgpu import abi, sats, workload as W
+def run_adjoint_batched(args, torch, np, abi, W, stream):
+    from ramgpu import sats
 
     ens = W.make_ensemble(args.adj_members, seed=808)
     base = ens.base
@@ -527,27 +896,26 @@ def run_adjoint_batched(args, torch, dev, stream):
             for s in ens.species[m]:
                 model.upload_f2(mi, s, np.asarray(base.f2[s]) * ens.scale[m])
                 model.set_boundary(mi, s, base.fgeos[s] * ens.scale[m])
+        torch.cuda.synchronize()
 
     reset(gpu, range(nm))
     gpu.set_graph(True)
     gpu.set_kp_all(kp[0])
     gpu.ram_run(base.dts)
     reset(gpu, range(nm))
-    torch.cuda.synchronize(dev)
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(stream)
+    stop = _event_timer(torch, stream)
     for c in range(nc):
         gpu.set_kp_all(kp[c])
         gpu.ram_run_async(base.dts)
-    b.record(stream)
-    torch.cuda.synchronize(dev)
-    fwd_s = a.elapsed_time(b) / 1e3
+    fwd_s = stop()
     reset(gpu, range(nm))
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    J = gpu.adj_forward(nc, base.dts, kp, kc, obs)
+    gpu.adj_forward(nc, base.dts, kp, kc, obs)  # warm-up (allocations)
+    gpu.adj_backward()
+    reset(gpu, range(nm))
+    stop = _event_timer(torch, stream)
+    gpu.adj_forward(nc, base.dts, kp, kc, obs)
     gf, gb = gpu.adj_backward()
-    batched_s = time.perf_counter() - t0
+    batched_s = stop()
     gpu.close()
     # looped: the same gradients one member at a time
     sub = list(range(0, nm, max(1, nm // 4)))[:4]
@@ -555,16 +923,15 @@ def run_adjoint_batched(args, torch, dev, stream):
     solo.set_stream(stream.cuda_stream)
     loop_s, agree = [], 0.0
     for m in sub:
-        reset(solo, [m])
         obs_m = [dict(o, member=0) for o in obs if o["member"] == m]
-        solo.adj_forward(1, base.dts, kp[:1, m], 1, [])  # warm-up
+        reset(solo, [m])
+        solo.adj_forward(nc, base.dts, kp[:, m], kc, obs_m)  # warm-up
         solo.adj_backward()
         reset(solo, [m])
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        Jm = solo.adj_forward(nc, base.dts, kp[:, m], kc, obs_m)
+        stop = _event_timer(torch, stream)
+        solo.adj_forward(nc, base.dts, kp[:, m], kc, obs_m)
         gfm, _ = solo.adj_backward()
-        loop_s.append(time.perf_counter() - t0)
+        loop_s.append(stop())
         for s in ens.species[m]:
             agree = max(agree, float(np.max(np.abs(gfm[0, s] - gf[m, s])) / max(np.max(np.abs(gf[m, s])), 1e-300)))
     solo.close()
@@ -585,240 +952,54 @@ def run_gb300(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    if args.only == "adjoint":
-        stream = torch.cuda.Stream(device=dev)
-        print(json.dumps({"adjoint": run_adjoint(args, torch, dev, stream)}), flush=True)
-        return
-    wl = W.make_workload(args.workload)
-    g = wl.grid
-    ns = len(g.species)
-    gpu = abi.RamGpu(g, wl.fields)
     stream = torch.cuda.Stream(device=dev)
-    gpu.set_stream(stream.cuda_stream)
-    for s in range(ns):
-        gpu.upload_f2(0, s, wl.f2[s])
-        gpu.set_boundary(0, s, wl.fgeos[s])
-    cells_per_step = 2 * g.ncell * ns
-    flush = torch.empty(max(1, args.flush_mb) << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
-
-    def kp_at(step):
-        return wl.kp(2 * step)
-
-    gpu.set_kp(-1, kp_at(0))
-    if args.no_coef_store:
-        gpu.set_coef_store(0)
-    shapes, _ = gpu.autotune(wl.dts) if not args.no_autotune else (gpu.launch_shape(), None)
-    # species groups on concurrent streams (autotuned; ramgpu_set_step_groups)
-    item_groups = gpu.step_groups()
-    gpu.set_graph(not args.no_graph)
-    # warm-up (builds the DTs tables, captures the graph)
-    for w in range(args.warmup):
-        gpu.set_kp(-1, kp_at(w))
-        gpu.ram_run(wl.dts)
-    torch.cuda.synchronize(dev)
-    if world > 1:
-        torch.distributed.barrier()
-    clocks = ClockSampler(local_rank)
-    clocks.start()
-    time.sleep(0.3)
-    launches0 = gpu.launch_count()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    torch.cuda.synchronize(dev)
-    # an NVTX range marks the timed steps, so that a profiler can select
-    # exactly their launches (ncu --nvtx --nvtx-include "ram_run_timed/")
-    nvtx = getattr(torch.cuda, "nvtx", None)
-    if nvtx is not None:
-        nvtx.range_push("ram_run_timed")
-    wall0 = time.perf_counter()
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(k & 0xFF)
-        gpu.set_kp(-1, kp_at(args.warmup + k))
-        ev[k][0].record(stream)
-        gpu.ram_run_async(wl.dts)
-        ev[k][1].record(stream)
-    torch.cuda.synchronize(dev)
-    wall = time.perf_counter() - wall0
-    if nvtx is not None:
-        nvtx.range_pop()
-    launches = gpu.launch_count() - launches0
-    clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(step_ms)
-    if world > 1:
-        total_ms = max_over_ranks(total_ms, dev)
-    value = world * cells_per_step * args.steps / (total_ms / 1e3)
-
-    # per-kernel durations: a second timed pass with events around every
-    # launch group on the launching stream (timing mode bypasses the graph)
-    gpu.set_timing(True)
-    gpu.kernel_times()
-    kt_ms = []
-    for k in range(max(3, min(args.steps, 10))):
-        with torch.cuda.stream(stream):
-            flush.fill_(k & 0xFF)
-        gpu.set_kp(-1, kp_at(k))
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        gpu.ram_run_async(wl.dts)
-        b.record(stream)
-        torch.cuda.synchronize(dev)
-        kt_ms.append(a.elapsed_time(b))
-    ktimes = gpu.kernel_times()
-    gpu.set_timing(False)
-
-    # dominant kernel and its roofline (per launch)
-    hbm_peak, peak_kind = measured_peaks()
-    sweep = {k: v for k, v in ktimes.items() if k.startswith("drift")}
-    dom = max(sweep, key=lambda k: sweep[k][0])
-    dom_ms = sweep[dom][0] / sweep[dom][1]
-    nitems = ns
-    bytes_per_launch = 16.0 * g.ncell * nitems  # F2 read + write once per sweep
-    achieved = bytes_per_launch / (dom_ms / 1e3) / 1e9
-    nfaces = g.ncell * nitems
-    fp64 = FP64_OPS_PER_CELL[dom] * nfaces / (dom_ms / 1e3) / 1e9
-    fp64_peak = abi.probe_fp64() / 1e9
-
-    # end-to-end through the C ABI with host buffers (pinned), full F2 in and
-    # out every step, as the reference's host array F2 is
-    e2e_steps = 0 if args.no_e2e else max(3, min(30, args.steps))
-    nm2 = g.nr * g.nt
-    pin = [torch.empty(g.ncell, dtype=torch.float64, pin_memory=True) for _ in range(ns)]
-    host = [np.reshape(p.numpy(), (g.nr, g.nt, g.ne, g.npa), order="F") for p in pin]
-    mom = torch.empty(2 * ns * nm2, dtype=torch.float64, pin_memory=True).numpy()
-    pe_h = [mom[s * nm2:(s + 1) * nm2] for s in range(ns)]
-    pa_h = [mom[(ns + s) * nm2:(ns + s + 1) * nm2] for s in range(ns)]
-    for s in range(ns):
-        host[s][...] = gpu.download_f2(0, s)
-    lib, h = gpu.lib, gpu.h
-    hp = [a.ctypes.data_as(abi._P) for a in host]
-
-    def e2e_pipelined(k):
-        # ramgpu_ram_run_host: uploads, sweeps and read-back of F2 and the
-        # moments of every species, pipelined over species groups
-        gpu.set_kp(-1, kp_at(k))
-        gpu.ram_run_host(wl.dts, host, pe_h, pa_h)
-
-    host_pg = [np.asfortranarray(a).copy(order="F") for a in host]  # ordinary (pageable) memory
-    pe_pg = [np.zeros(nm2) for _ in range(ns)]
-    pa_pg = [np.zeros(nm2) for _ in range(ns)]
-
-    def e2e_pageable(k):
-        # the same call from ordinary host arrays, as a Fortran caller's F2:
-        # the SMs move them over the coherent host link
-        gpu.set_kp(-1, kp_at(k))
-        gpu.ram_run_host(wl.dts, host_pg, pe_pg, pa_pg)
-
-    def e2e_serial(k):
-        # the same traffic as one stream: uploads, ram_run, read-back, wait
-        for s in range(ns):
-            gpu._ck(lib.ramgpu_upload_f2_async(h, 0, s, hp[s]), "upload")
-        gpu.set_kp(-1, kp_at(k))
-        gpu.ram_run_async(wl.dts)
-        for s in range(ns):
-            gpu._ck(lib.ramgpu_download_f2_async(h, 0, s, hp[s]), "download")
-            gpu._ck(lib.ramgpu_moments_async(h, 0, s, pe_h[s].ctypes.data_as(abi._P),
-                                             pa_h[s].ctypes.data_as(abi._P)), "moments")
-        gpu._ck(lib.ramgpu_synchronize(h), "synchronize")
-
-    e2e_med = {}
-
-    def e2e_time(fn):
-        fn(0)  # warm (first use creates the group streams)
-        torch.cuda.synchronize(dev)
-        ts = []
-        t0 = time.perf_counter()
-        for k in range(e2e_steps):
-            t1 = time.perf_counter()
-            fn(k)
-            ts.append(time.perf_counter() - t1)
-        e2e_med[fn.__name__] = 1e3 * statistics.median(ts)
-        return max(time.perf_counter() - t0, 1e-9)
-
-    e2e = {"value": None, "unit": UNIT, "h2d_bytes_per_step": 8 * g.ncell * ns,
-           "d2h_bytes_per_step": 8 * g.ncell * ns + 16 * nm2 * ns,
-           "path": "ramgpu_set_kp + ramgpu_ram_run_host (page-locked host F2 of 4 species in and out, "
-                   "moments of 4 species out; pipelined over 4 species groups), every step"}
-    if e2e_steps:
-        e2e["value"] = world * cells_per_step * e2e_steps / e2e_time(e2e_pipelined)
-        e2e["pageable_value"] = world * cells_per_step * e2e_steps / e2e_time(e2e_pageable)
-        e2e["serial_value"] = world * cells_per_step * e2e_steps / e2e_time(e2e_serial)
-        e2e["ms_per_step_median"] = {"pipelined": e2e_med["e2e_pipelined"], "pageable": e2e_med["e2e_pageable"],
-                                     "serial": e2e_med["e2e_serial"]}
-        e2e["pageable_path"] = "ramgpu_ram_run_host with ordinary (pageable) host arrays"
-        e2e["serial_path"] = ("ramgpu_upload_f2_async x4 + ramgpu_ram_run_async + ramgpu_download_f2_async x4 "
-                              "+ ramgpu_moments_async x4 + ramgpu_synchronize on one stream")
-    # the same step with WPADIF on the electrons (both halves), per-kernel timed
-    padif = None
-    if not args.no_padif:
-        gpu.set_pa_diffusion(0, W.pa_diffusion(g, wl.fields))
-        gpu.set_timing(True)
-        gpu.kernel_times()
-        pd_ms = []
-        for k in range(3):
-            with torch.cuda.stream(stream):
-                flush.fill_(k & 0xFF)
-            gpu.set_kp(-1, kp_at(k))
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            gpu.ram_run_async(wl.dts)
-            b.record(stream)
-            torch.cuda.synchronize(dev)
-            pd_ms.append(a.elapsed_time(b))
-        kt = gpu.kernel_times()
-        gpu.set_timing(False)
-        gpu.set_pa_diffusion(0, None)
-        pk = kt.get("padif", (0.0, 1))
-        per = pk[0] / max(pk[1], 1)
-        # algorithmic bytes of the two launches per step: the electrons' solve
-        # reads F2 and the three elimination tables and writes F2 (40 B per
-        # cell) in both; the first also applies the loss factor to the other
-        # three species (F2 and factor in, F2 out: 24 B per cell)
-        byts = 0.5 * (40.0 + 40.0 + 3 * 24.0) * g.ncell
-        padif = {"species": "Electron (WPADIF after the drifts and before the reverse drifts)",
-                 "step_ms": statistics.mean(pd_ms), "step_ms_without": statistics.mean(kt_ms),
-                 "kernel_ms_per_launch": per, "launches": pk[1],
-                 "algorithmic_GBps": byts / (per / 1e3) / 1e9 if per > 0 else None}
-    gpu.close()
-
-    ensemble = None
-    if rank == 0 and args.members > 0:
-        ensemble = run_ensemble(args, torch, dev, stream)
-    adjoint = None
-    if rank == 0 and args.adj_calls > 0:
-        adjoint = run_adjoint(args, torch, dev, stream)
-
+    sec = args.sections
+    head = measure(args, torch, np, abi, W, stream, args.workload, args.steps, args.warmup, world=world,
+                   clocks=True, e2e_steps=0 if args.no_e2e else max(3, min(30, args.steps)),
+                   kernel_steps=max(3, min(args.steps, 10)))
+    single = refined = padif = ensemble = adjoint = None
+    if rank == 0 and "single" in sec and args.workload != "single_h":
+        # config 1: one species, 10 MB of F2, L2-resident between its sweeps
+        single = measure(args, torch, np, abi, W, stream, "single_h", 20, 3)
+        single["l2"] = ("working set (F2 10.1 MB + tables) inside the 129 MB L2: within a step the sweeps' "
+                        "algorithmic traffic (roofline.sweeps_GBps, 16 B per cell) is served by L2; L2 is flushed "
+                        "between steps")
+    if rank == 0 and "refined" in sec and args.workload != "refined":
+        # config 3: F2 of 632 MB, larger than L2: the HBM roofline case
+        refined = measure(args, torch, np, abi, W, stream, "refined", 10, 2,
+                          e2e_steps=0 if args.no_e2e else 5, kernel_steps=3)
+    if rank == 0 and "padif" in sec:
+        padif = run_padif(torch, abi, W, stream, args)
+    if "ensemble" in sec and args.members > 0:
+        ensemble = run_ensemble(args, torch, np, abi, W, stream, rank, world)
+    if rank == 0 and "adjoint" in sec and args.adj_calls > 0:
+        adjoint = run_adjoint(args, torch, np, abi, W, stream)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        ns = len(W.make_workload(args.workload).grid.species)
         cpu = cpu_baseline_fresh(args.workload, ns, args.cpu_seconds)
+        if single is not None:
+            single["cpu_baseline"] = cpu_baseline_fresh("single_h", 1, args.cpu_seconds)
+        if refined is not None:
+            # a bounded sample: one timed call per variant (a few seconds each)
+            refined["cpu_baseline"] = cpu_baseline_fresh("refined", 4, 0.0, calls=1, warmup=1)
     if rank != 0:
         return
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_desc(wl), "step": "one ram_run call = 2 DTs steps",
-                   "cells_per_step": cells_per_step, "l2": "flushed between timed steps (256 MB write)",
-                   "graph": not args.no_graph, "launch_shapes": shapes,
-                   "item_groups": item_groups,
+        "config": {"workload": head["workload"], "step": "one ram_run call = 2 DTs steps",
+                   "cells_per_step": head["cells_per_step"], "l2": "flushed between timed steps (256 MB write)",
+                   "graph": not args.no_graph, "launch_shapes": head["launch_shapes"],
+                   "autotune_trials": head["autotune_trials"], "item_groups": head["item_groups"],
                    "coef_store": "none" if args.no_coef_store else "DRIFTE",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak,
-                     "traffic": NCU_DRAM_BYTES.get(args.workload, {}).get(dom), "kernel": dom,
-                     "kernel_ms": dom_ms, "peak_kind": peak_kind,
-                     "fp64": {"achieved": fp64, "peak": fp64_peak, "unit": "G lane-ops/s",
-                              "frac": fp64 / fp64_peak, "ops_per_cell": FP64_OPS_PER_CELL[dom],
-                              "peak_kind": "measured live (fma loop, ramgpu_probe_fp64)"},
-                     # whole-step views: the fused minimum (F2 read and written once per
-                     # DTs step, 16 B per cell-update) and the unfused sweep sequence
-                     # (4 sweeps x 16 B + CEX 16 B = 80 B per cell-update)
-                     "step": {"fused_min_GBps": value * 16 / 1e9, "fused_min_frac": value * 16 / 1e9 / hbm_peak,
-                              "unfused_GBps": value * 80 / 1e9, "unfused_frac": value * 80 / 1e9 / hbm_peak}},
-        "kernels_ms": {k: round(v[0] / v[1], 5) for k, v in ktimes.items()},
-        "kernel_pass_ms_per_step": statistics.mean(kt_ms),
-        "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
-        "padif": padif, "ensemble": ensemble, "adjoint": adjoint, "wall_s": wall,
+        "roofline": head["roofline"], "kernels_ms": head["kernels_ms"],
+        "kernel_pass_ms_per_step": head["kernel_pass_ms_per_step"],
+        "e2e": head.get("e2e"), "cpu_baseline": cpu, "clocks": head["clocks"], "gpu_launches": head["launches"],
+        "single_species": single, "refined": refined, "padif": padif, "ensemble": ensemble, "adjoint": adjoint,
+        "wall_s": head["wall_s"],
     }
     print(json.dumps(line), flush=True)
 

@@ -374,6 +374,10 @@ int ramgpu_set_mu_lanes(ramgpu_ctx *ctx, int lanes);
  * restores F2 afterwards (it allocates a temporary snapshot).  best_ms4
  * (may be NULL) receives the best step time of each sweep's round. */
 int ramgpu_autotune(ramgpu_ctx *ctx, double dts, int reps, double *best_ms4);
+/* The best whole-step trial time of the last ramgpu_autotune for each sweep
+ * (R, P, E, MU) with a plain grid and with a persistent grid [ms]; 0 where
+ * that kind was not tried (diagnostics: why the tuner chose what it chose). */
+int ramgpu_autotune_trials(ramgpu_ctx *ctx, double *plain_ms4, double *persistent_ms4);
 
 /* ---- status word ---------------------------------------------------------
  * The reference stops when a moment is no longer finite (ANISCH,

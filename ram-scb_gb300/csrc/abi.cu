@@ -140,6 +140,9 @@ struct ramgpu_ctx {
   unsigned ref_flags = 0;
   int ref_shape = -1, ref_g = 0;
   double* ref_stage = nullptr;
+  // best whole-step trial times of the last autotune per sweep, plain grid
+  // and persistent grid [ms] (0: not tried)
+  double tune_plain_ms[4] = {0, 0, 0, 0}, tune_pers_ms[4] = {0, 0, 0, 0};
   bool ref_force_stage = false;  // move reachable arrays by the copy engines too
   int nsm = 0;
   // status word: device words and their page-locked copy; the pass is
@@ -2020,6 +2023,7 @@ int ramgpu_autotune(ramgpu_ctx* ctx, double dts, int reps, double* best_ms4) {
   cudaEventCreate(&e1);
   const int cand_blk[4] = {32, 64, 128, 256};
   for (int w = 0; w < 4; ++w) {
+    ctx->tune_plain_ms[w] = ctx->tune_pers_ms[w] = 0.0;
     float best = 1e30f;
     int bb = ctx->d.blk[w], bp = ctx->d.pers[w], bl = ctx->d.mu_lanes;
     // DRIFTMU: 4, 2 and 1 lanes per line, as NPA allows
@@ -2057,6 +2061,8 @@ int ramgpu_autotune(ramgpu_ctx* ctx, double dts, int reps, double* best_ms4) {
           if (r > 0 && ms < tbest) tbest = ms;
         }
         if (tbest < best) { best = tbest; bb = blk; bp = pc; bl = ctx->d.mu_lanes; }
+        double& rec = persist ? ctx->tune_pers_ms[w] : ctx->tune_plain_ms[w];
+        if (rec == 0.0 || tbest < rec) rec = tbest;
       }
     }
     ctx->d.blk[w] = bb;
@@ -2102,6 +2108,15 @@ int ramgpu_autotune(ramgpu_ctx* ctx, double dts, int reps, double* best_ms4) {
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "autotune");
   ctx->shape_version += 1;
+  return RAMGPU_OK;
+}
+
+int ramgpu_autotune_trials(ramgpu_ctx* ctx, double* plain_ms4, double* persistent_ms4) {
+  if (check_ctx(ctx) || !plain_ms4 || !persistent_ms4) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  for (int w = 0; w < 4; ++w) {
+    plain_ms4[w] = ctx->tune_plain_ms[w];
+    persistent_ms4[w] = ctx->tune_pers_ms[w];
+  }
   return RAMGPU_OK;
 }
 

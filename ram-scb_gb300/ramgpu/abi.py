@@ -37,7 +37,7 @@ EXPORTS = (
     "ramgpu_fly_sats", "ramgpu_sum_pressure", "ramgpu_adj_replay", "ramgpu_set_pa_diffusion",
     "ramgpu_loss_wae", "ramgpu_bounce_integrals", "ramgpu_upload_f2_async", "ramgpu_download_f2_async",
     "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store", "ramgpu_compute_hI",
-    "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_ram_run_ref", "ramgpu_set_ref_staging",
+    "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_ram_run_ref", "ramgpu_set_ref_staging", "ramgpu_autotune_trials",
     "ramgpu_set_pipeline_groups", "ramgpu_pipeline_groups",
     "ramgpu_set_step_groups", "ramgpu_step_groups", "ramgpu_set_pipeline_trace", "ramgpu_pipeline_trace",
     "ramgpu_check", "ramgpu_set_check", "ramgpu_last_status",
@@ -168,6 +168,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_ram_run_host": ([vp, d, vp, vp, vp], i),
         "ramgpu_ram_run_ref": ([vp, d, vp, vp, vp], i),
         "ramgpu_set_ref_staging": ([vp, i], i),
+        "ramgpu_autotune_trials": ([vp, dp, dp], i),
         "ramgpu_set_pipeline_groups": ([vp, i], i),
         "ramgpu_pipeline_groups": ([vp], i),
         "ramgpu_set_step_groups": ([vp, i], i),
@@ -623,6 +624,13 @@ class RamGpu:
         ms = np.zeros(4)
         self._ck(self.lib.ramgpu_autotune(self.h, float(dts), int(reps), _dptr(ms)), "autotune")
         return self.launch_shape(), ms
+
+    def autotune_trials(self):
+        """Best whole-step trial of the last autotune per sweep (R, P, E, MU):
+        (plain-grid ms, persistent-grid ms); 0 where not tried."""
+        a, b = np.zeros(4), np.zeros(4)
+        self._ck(self.lib.ramgpu_autotune_trials(self.h, _dptr(a), _dptr(b)), "autotune_trials")
+        return a, b
 
     # --------------------------------------------------------------- adjoint
     def adj_forward(self, ncalls: int, dts: float, kp, k_ckpt: int, obs):

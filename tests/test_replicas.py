@@ -62,3 +62,70 @@ def test_reference_arm_under_torchrun():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_member_partition_covers_and_balances():
+    """Ensemble members over ranks by work (species x length): every member
+    exactly once, and the heaviest rank within Graham's 4/3 bound of the
+    ideal share."""
+    from ramgpu import shard, workload as W
+
+    ens = W.make_ensemble(256)
+    work = shard.member_work(ens.species, ens.length)
+    for world in (1, 2, 3, 8):
+        parts = shard.partition_members(work, world)
+        flat = sorted(m for p in parts for m in p)
+        assert flat == list(range(256))
+        loads = [sum(work[m] for m in p) for p in parts]
+        assert max(loads) <= 4.0 / 3.0 * max(sum(work) / world, max(work)) + 1e-9
+    with pytest.raises(ValueError):
+        shard.partition_members(work, 0)
+
+
+def _shard_worker(rank, world, port, out):
+    import numpy as np
+    import torch
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    torch.distributed.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        sys.path.insert(0, str(ROOT / "ram-scb_gb300"))
+        from ramgpu import shard, workload as W
+
+        ens = W.make_ensemble(48, seed=77)
+        sums = [float(np.sum(a)) for a in ens.base.f2]
+        parts = shard.partition_members(shard.member_work(ens.species, ens.length), world)
+        # each rank's diagnostic rows for its own members only
+        rows = {m: [sums[s] * float(ens.scale[m]) for s in ens.species[m]] for m in parts[rank]}
+        allrows = shard.gather_member_rows(rows, world, rank, ens.members, torch.distributed)
+        out.put((rank, parts, allrows))
+    finally:
+        torch.distributed.destroy_process_group()
+
+
+def test_member_shards_gather_gloo():
+    """Two ranks each advance their own members (here: the members' initial
+    diagnostics) and every rank gathers all rows, in member order, each
+    exactly once -- the host side of the ensemble split over GPUs."""
+    torch = pytest.importorskip("torch")
+    import numpy as np
+    sys.path.insert(0, str(ROOT / "ram-scb_gb300"))
+    from ramgpu import workload as W
+
+    mp = torch.multiprocessing.get_context("spawn")
+    q = mp.Queue()
+    port = _free_port()
+    ps = [mp.Process(target=_shard_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    got = dict((r, (parts, rows)) for r, parts, rows in (q.get(timeout=180) for _ in ps))
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    ens = W.make_ensemble(48, seed=77)
+    sums = [float(np.sum(a)) for a in ens.base.f2]
+    expect = [[sums[s] * float(ens.scale[m]) for s in ens.species[m]] for m in range(48)]
+    parts0, rows0 = got[0]
+    parts1, rows1 = got[1]
+    assert parts0 == parts1 and sorted(parts0[0] + parts0[1]) == list(range(48))
+    assert parts0[0] and parts0[1]
+    assert rows0 == rows1 == expect
