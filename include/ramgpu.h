@@ -37,6 +37,7 @@ extern "C" {
 #define RAMGPU_ERR_STATE (-3)    /* call made before its inputs were set */
 #define RAMGPU_ERR_NUMERIC (-4)  /* non-finite value detected */
 #define RAMGPU_ERR_NOMEM (-5)    /* device allocation failed */
+#define RAMGPU_ERR_IO (-6)       /* file cannot be opened, read or written, or fails its checksum */
 
 /* Charge-exchange cross-section branch of CEPARA (src/ModRamLoss.f90:38-87). */
 #define RAMGPU_CEX_NONE 0      /* "Electron" (CEX_file 'na'): no loss */
@@ -499,6 +500,33 @@ int ramgpu_adj_record(ramgpu_ctx *ctx, int call, unsigned char *out);
  * adjoint by finite differences on long windows, where unfrozen
  * perturbations cross limiter kinks. */
 int ramgpu_adj_replay(ramgpu_ctx *ctx, double *J);
+
+/* ---- snapshots ----------------------------------------------------------- */
+
+/* The evolving state of a context in one file, the counterpart of RAM's
+ * write_restart / read_restart (src/ModRamRestart.f90:12,386) for the state
+ * this library owns: per member its species set, active flag, Kp or
+ * explicit potential and VT, per (member, species) F2, FGEOS and the last
+ * moments.  Grid and field tables are inputs and are set again by the
+ * caller.  Layout (little-endian): a 128-byte header "RAMGPUS1", version 1,
+ * header size, NR, NT, NE, NPA, NS, members (int32), flags, 0 (uint32), the
+ * caller's time (double), payload bytes, checksum (uint64: FNV-1a over the
+ * payload's 64-bit words), zero padding; then per member {species mask,
+ * active, VT mode, 0 (int32), Kp, VT(NR+1,NT)} and per slot {F2, FGEOS,
+ * PPERT, PPART} in the ABI's layouts.  ramgpu_load_state checks the whole
+ * file (RAMGPU_ERR_IO: unreadable or checksum mismatch; RAMGPU_ERR_ARG:
+ * other dimensions) before it changes anything, and returns the saved time
+ * in *time (may be NULL).  Both synchronise the context's stream. */
+typedef struct {
+    int nr, nt, ne, npa, ns, n_members;
+    unsigned flags;
+    double time;
+} ramgpu_snapshot_info_t;
+int ramgpu_save_state(ramgpu_ctx *ctx, const char *path, double time);
+int ramgpu_load_state(ramgpu_ctx *ctx, const char *path, double *time);
+/* Header of a snapshot file after checking its checksum; needs no context
+ * (and no GPU).  Errors go to ramgpu_last_error(NULL, ...). */
+int ramgpu_snapshot_info(const char *path, ramgpu_snapshot_info_t *info);
 
 /* ---- no-allocation variant --------------------------------------------- */
 

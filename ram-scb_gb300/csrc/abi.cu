@@ -24,12 +24,15 @@
 //                  the adjoint window, diagnostics
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <string.h>
 
 #include <algorithm>
 #include <string>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/ramgpu.h"
 #include "kernels.cuh"
@@ -178,12 +181,23 @@ static cudaEvent_t take_event(ramgpu_ctx* c) {
   }
   return e;
 }
-// Brackets a launch group with events when timing is enabled.
+// NVTX range names of the kernel classes (the classes of ramgpu_kernel_times).
+static const char* const kClassName[] = {"member tables", "DRIFTR ghost planes", "DRIFTR", "DRIFTP", "DRIFTE",
+                                         "DRIFTMU", "periodic copy and mask", "ANISCH", "DTs tables",
+                                         "SUMRC", "WPADIF"};
+// An NVTX range over a scope (a no-op unless a profiler injects NVTX).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+// Brackets a launch group with an NVTX range of its kernel class and, when
+// timing is enabled, with events.
 struct Timed {
   ramgpu_ctx* c;
   int kind;
   cudaEvent_t a = nullptr;
   Timed(ramgpu_ctx* c_, int k) : c(c_), kind(k) {
+    nvtxRangePushA(kClassName[k]);
     if (c->timing) {
       a = take_event(c);
       cudaEventRecord(a, c->stream);
@@ -195,6 +209,7 @@ struct Timed {
       cudaEventRecord(b, c->stream);
       c->spans.push_back({kind, a, b});
     }
+    nvtxRangePop();
   }
 };
 static int fail(ramgpu_ctx* c, int code, const std::string& msg) {
@@ -1370,6 +1385,7 @@ int ramgpu_f2_device_ptr(ramgpu_ctx* ctx, int member, int s, double** dptr) {
 }
 
 int ramgpu_ram_run_async(ramgpu_ctx* ctx, double dts) {
+  NvtxRange range_("ramgpu_ram_run_async");
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
   return enqueue_ram_run(ctx, dts);
 }
@@ -1426,6 +1442,7 @@ static int status_out(ramgpu_ctx* ctx, ramgpu_status* st) {
 
 int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* const* ppert,
                         double* const* ppart) {
+  NvtxRange range_("ramgpu_ram_run_host");
   if (check_ctx(ctx) || !f2) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
   int rc = prepare(ctx, dts);
   if (rc) return rc;
@@ -1631,6 +1648,7 @@ static int enqueue_ref(ramgpu_ctx* ctx, double dts, const std::vector<RefMem>& m
 }
 
 int ramgpu_ram_run_ref(ramgpu_ctx* ctx, double dts, double* const* f2, double* const* ppert, double* const* ppart) {
+  NvtxRange range_("ramgpu_ram_run_ref");
   if (check_ctx(ctx) || !f2) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
   int rc = prepare(ctx, dts);
   if (rc) return rc;
@@ -1713,6 +1731,7 @@ int ramgpu_set_ref_staging(ramgpu_ctx* ctx, int force) {
 }
 
 int ramgpu_ram_run(ramgpu_ctx* ctx, double dts) {
+  NvtxRange range_("ramgpu_ram_run");
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
   int rc = enqueue_ram_run(ctx, dts);
   if (rc) return rc;
@@ -2120,6 +2139,201 @@ int ramgpu_autotune_trials(ramgpu_ctx* ctx, double* plain_ms4, double* persisten
   return RAMGPU_OK;
 }
 
+
+// ------------------------------------------------------------- snapshots
+// The evolving state of a context in one file (the counterpart of RAM's
+// write_restart/read_restart, src/ModRamRestart.f90:12,386, for the state
+// this library owns; grid and field tables are inputs and are not saved).
+// Layout, little-endian:
+//   header (128 bytes): "RAMGPUS1", version 1, header bytes 128, NR, NT,
+//     NE, NPA, NS, members, flags, 0, the caller's time [s], payload bytes,
+//     checksum, zero padding;
+//   payload: per member {species mask, active, VT mode (int32), 0 (int32),
+//     Kp, VT(NR+1,NT)} then per (member, species) slot {F2(NR,NT,NE,NPA),
+//     FGEOS(NT,NE,NPA), PPERT(NR,NT), PPART(NR,NT)} (doubles).
+// The checksum is FNV-1a over the payload's 64-bit words.
+namespace {
+constexpr char kSnapMagic[8] = {'R', 'A', 'M', 'G', 'P', 'U', 'S', '1'};
+constexpr uint64_t kFnvOffset = 1469598103934665603ULL, kFnvPrime = 1099511628211ULL;
+struct SnapHeader {
+  char magic[8];
+  uint32_t version, header_bytes;
+  int32_t nr, nt, ne, npa, ns, nm;
+  uint32_t flags, pad0;
+  double time;
+  uint64_t payload_bytes, checksum;
+  unsigned char pad[128 - 8 - 8 - 24 - 8 - 8 - 16];
+};
+static_assert(sizeof(SnapHeader) == 128, "snapshot header is 128 bytes");
+uint64_t fnv_words(uint64_t h, const void* p, size_t nbytes) {
+  const unsigned char* b = (const unsigned char*)p;
+  for (size_t i = 0; i + 8 <= nbytes; i += 8) {
+    uint64_t w;
+    memcpy(&w, b + i, 8);
+    h = (h ^ w) * kFnvPrime;
+  }
+  return h;
+}
+uint64_t snap_payload_bytes(long long nr, long long nt, long long ne, long long npa, long long ns, long long nm) {
+  const long long member = 16 + 8 + 8 * (nr + 1) * nt;
+  const long long slot = 8 * (nr * nt * ne * npa + nt * ne * npa + 2 * nr * nt);
+  return (uint64_t)(nm * member + nm * ns * slot);
+}
+// Reads the header and checks the payload against its checksum.
+int snap_verify(FILE* f, SnapHeader* h, std::string* why) {
+  if (fread(h, sizeof(*h), 1, f) != 1) { *why = "short header"; return RAMGPU_ERR_IO; }
+  if (memcmp(h->magic, kSnapMagic, 8) != 0 || h->version != 1 || h->header_bytes != 128) {
+    *why = "not a ramgpu snapshot (magic, version or header size)";
+    return RAMGPU_ERR_IO;
+  }
+  if (h->nr < 1 || h->nt < 1 || h->ne < 1 || h->npa < 1 || h->ns < 1 || h->nm < 1 ||
+      h->payload_bytes != snap_payload_bytes(h->nr, h->nt, h->ne, h->npa, h->ns, h->nm)) {
+    *why = "snapshot sizes inconsistent";
+    return RAMGPU_ERR_IO;
+  }
+  std::vector<unsigned char> buf(1 << 24);
+  uint64_t left = h->payload_bytes, hs = kFnvOffset;
+  while (left > 0) {
+    const size_t n = (size_t)std::min<uint64_t>(left, buf.size());
+    if (fread(buf.data(), 1, n, f) != n) { *why = "snapshot payload truncated"; return RAMGPU_ERR_IO; }
+    hs = fnv_words(hs, buf.data(), n);
+    left -= n;
+  }
+  if (hs != h->checksum) { *why = "snapshot checksum mismatch"; return RAMGPU_ERR_IO; }
+  return RAMGPU_OK;
+}
+}  // namespace
+
+int ramgpu_snapshot_info(const char* path, ramgpu_snapshot_info_t* info) {
+  if (!path) return fail(nullptr, RAMGPU_ERR_ARG, "null path");
+  FILE* f = fopen(path, "rb");
+  if (!f) return fail(nullptr, RAMGPU_ERR_IO, std::string("cannot open ") + path);
+  SnapHeader h{};
+  std::string why;
+  const int rc = snap_verify(f, &h, &why);
+  fclose(f);
+  if (rc) return fail(nullptr, rc, why);
+  if (info) {
+    info->nr = h.nr; info->nt = h.nt; info->ne = h.ne; info->npa = h.npa; info->ns = h.ns; info->n_members = h.nm;
+    info->flags = h.flags;
+    info->time = h.time;
+  }
+  return RAMGPU_OK;
+}
+
+int ramgpu_save_state(ramgpu_ctx* ctx, const char* path, double time) {
+  if (check_ctx(ctx) || !path) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  NvtxRange range_("ramgpu_save_state");
+  const Dev& d = ctx->d;
+  const int nm = d.nm, ns = d.ns;
+  const size_t ncell = d.ncell, nfg = (size_t)d.nt * d.ne * d.npa, nm2 = (size_t)d.nr * d.nt;
+  const size_t nvt = (size_t)d.nf * d.nt;
+  CK(cudaStreamSynchronize(ctx->stream));
+  SnapHeader h{};
+  memcpy(h.magic, kSnapMagic, 8);
+  h.version = 1; h.header_bytes = 128;
+  h.nr = d.nr; h.nt = d.nt; h.ne = d.ne; h.npa = d.npa; h.ns = ns; h.nm = nm;
+  h.flags = ctx->cfg.flags;
+  h.time = time;
+  h.payload_bytes = snap_payload_bytes(d.nr, d.nt, d.ne, d.npa, ns, nm);
+  FILE* f = fopen(path, "wb");
+  if (!f) return fail(ctx, RAMGPU_ERR_IO, std::string("cannot create ") + path);
+  bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
+  uint64_t hs = kFnvOffset;
+  auto put = [&](const void* p, size_t n) {
+    if (ok) ok = fwrite(p, 1, n, f) == n;
+    hs = fnv_words(hs, p, n);
+  };
+  std::vector<double> kp(nm), vt(nvt), buf(ncell);
+  std::vector<int> mode(nm);
+  cudaError_t e = cudaMemcpy(kp.data(), d.kp, sizeof(double) * nm, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(mode.data(), d.vt_mode, sizeof(int) * nm, cudaMemcpyDeviceToHost);
+  for (int m = 0; m < nm && e == cudaSuccess; ++m) {
+    int32_t rec[4] = {0, ctx->member_active[m], mode[m], 0};
+    for (int sp : ctx->member_species[m]) rec[0] |= 1 << sp;
+    put(rec, sizeof(rec));
+    put(&kp[m], sizeof(double));
+    e = cudaMemcpy(vt.data(), d.vt + (size_t)m * nvt, sizeof(double) * nvt, cudaMemcpyDeviceToHost);
+    put(vt.data(), sizeof(double) * nvt);
+  }
+  for (int slot = 0; slot < nm * ns && e == cudaSuccess; ++slot) {
+    const struct { const double* src; size_t n; } parts[4] = {
+        {d.f2 + (size_t)slot * ncell, ncell}, {d.fgeos + (size_t)slot * nfg, nfg},
+        {d.ppert + (size_t)slot * nm2, nm2}, {d.ppart + (size_t)slot * nm2, nm2}};
+    for (const auto& q : parts) {
+      if (e == cudaSuccess) e = cudaMemcpy(buf.data(), q.src, sizeof(double) * q.n, cudaMemcpyDeviceToHost);
+      put(buf.data(), sizeof(double) * q.n);
+    }
+  }
+  h.checksum = hs;
+  if (ok) ok = fseek(f, 0, SEEK_SET) == 0 && fwrite(&h, sizeof(h), 1, f) == 1;
+  ok = (fclose(f) == 0) && ok;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "ramgpu_save_state");
+  if (!ok) return fail(ctx, RAMGPU_ERR_IO, std::string("write failed: ") + path);
+  return RAMGPU_OK;
+}
+
+int ramgpu_load_state(ramgpu_ctx* ctx, const char* path, double* time) {
+  if (check_ctx(ctx) || !path) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
+  NvtxRange range_("ramgpu_load_state");
+  Dev& d = ctx->d;
+  const int nm = d.nm, ns = d.ns;
+  const size_t ncell = d.ncell, nfg = (size_t)d.nt * d.ne * d.npa, nm2 = (size_t)d.nr * d.nt;
+  const size_t nvt = (size_t)d.nf * d.nt;
+  FILE* f = fopen(path, "rb");
+  if (!f) return fail(ctx, RAMGPU_ERR_IO, std::string("cannot open ") + path);
+  // the whole file is checked before anything on the device changes
+  SnapHeader h{};
+  std::string why;
+  if (int rc = snap_verify(f, &h, &why)) {
+    fclose(f);
+    return fail(ctx, rc, why);
+  }
+  if (h.nr != d.nr || h.nt != d.nt || h.ne != d.ne || h.npa != d.npa || h.ns != ns || h.nm != nm) {
+    fclose(f);
+    return fail(ctx, RAMGPU_ERR_ARG, "snapshot dimensions differ from the context's");
+  }
+  fseek(f, sizeof(SnapHeader), SEEK_SET);
+  bool ok = true;
+  auto get = [&](void* p, size_t n) { if (ok) ok = fread(p, 1, n, f) == n; };
+  std::vector<double> vt(nvt), buf(ncell);
+  int rc = RAMGPU_OK;
+  for (int m = 0; m < nm && ok && !rc; ++m) {
+    int32_t rec[4];
+    double kp = 0.0;
+    get(rec, sizeof(rec));
+    get(&kp, sizeof(kp));
+    get(vt.data(), sizeof(double) * nvt);
+    if (!ok) break;
+    std::vector<int> list;
+    for (int sp = 0; sp < ns; ++sp)
+      if (rec[0] & (1 << sp)) list.push_back(sp);
+    rc = ramgpu_set_member_species(ctx, m, (int)list.size(), list.data());
+    if (!rc) rc = ramgpu_set_member_active(ctx, m, rec[1]);
+    if (!rc) rc = rec[2] ? ramgpu_set_kp(ctx, m, kp) : ramgpu_set_potential(ctx, m, vt.data());
+    if (!rc && rec[2]) {
+      // the potential of the last call, as saved (VOLS recomputes it from Kp anyway)
+      CK(cudaMemcpyAsync(d.vt + (size_t)m * nvt, vt.data(), sizeof(double) * nvt, cudaMemcpyHostToDevice,
+                         ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+    }
+  }
+  for (int slot = 0; slot < nm * ns && ok && !rc; ++slot) {
+    double* const dst[4] = {d.f2 + (size_t)slot * ncell, d.fgeos + (size_t)slot * nfg, d.ppert + (size_t)slot * nm2,
+                            d.ppart + (size_t)slot * nm2};
+    const size_t cnt[4] = {ncell, nfg, nm2, nm2};
+    for (int q = 0; q < 4 && ok; ++q) {
+      get(buf.data(), sizeof(double) * cnt[q]);
+      if (ok) CK(cudaMemcpy(dst[q], buf.data(), sizeof(double) * cnt[q], cudaMemcpyHostToDevice));
+    }
+  }
+  fclose(f);
+  if (rc) return rc;
+  if (!ok) return fail(ctx, RAMGPU_ERR_IO, std::string("read failed: ") + path);
+  if (time) *time = h.time;
+  return RAMGPU_OK;
+}
+
 // Bit s set when species s belongs to the member (retired members keep
 // their last state and are still sampled).
 static unsigned species_mask(const ramgpu_ctx* ctx, int member) {
@@ -2383,6 +2597,7 @@ int ramgpu_adj_segments(ramgpu_ctx* ctx, int* nseg, int* nkeep) {
 
 int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp, int k_ckpt,
                        const ramgpu_obs* obs, int nobs, double* J) {
+  NvtxRange range_("ramgpu_adj_forward");
   if (check_ctx(ctx) || !kp || (nobs > 0 && !obs)) return fail(ctx, RAMGPU_ERR_ARG, "null argument");
   if (ncalls < 1 || k_ckpt < 1 || nobs < 0) return fail(ctx, RAMGPU_ERR_ARG, "ncalls, k_ckpt >= 1, nobs >= 0");
   if (ctx->cfg.flags & RAMGPU_FLAG_LOSSES)
@@ -2508,6 +2723,7 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
 }
 
 int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
+  NvtxRange range_("ramgpu_adj_backward");
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
   auto& a = ctx->adj;
   if (!a.ready) return fail(ctx, RAMGPU_ERR_STATE, "ramgpu_adj_forward must run first");

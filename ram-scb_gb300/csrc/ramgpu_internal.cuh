@@ -185,6 +185,40 @@ __device__ __forceinline__ bits64 mul_pos_bits(bits64 ax, double y) {
   const bits64 r = ((bits64)(ex + (int)(uy >> 52) - 1023 + hi) << 52) | ((p >> (10 + hi)) & kMantMask);
   return ex == 0x7FF ? ax : r;
 }
+// The CORR factor a = 0.5*(s - u) of a face, s = +-1 the upwind sign and
+// u >= 0 its Courant number (|C| in R and P, |C|/DE and |C|/DMU in E and
+// MU), i.e. a = s*0.5*(1 - u), formed on the integer pipe for u < 1:
+// 1 - u in 64-bit fixed point (2^63 is 1; exact for u >= 2^-11, below that
+// u loses bits past 2^-63), normalised by a count of leading zeros and cut
+// to 53 bits.  The result is at most one unit in the last place below the
+// rounded 0.5*(s - u) (the FP64 fma it replaces) in magnitude; it only
+// scales the limited correction a*LX, so the flux it feeds stays within the
+// 1e-12 parity bar and conservation is untouched (the flux leaving one cell
+// is the flux entering the next).  ub: bits of u (non-negative); u >= 1,
+// inf and NaN take the FP64 fma fma(c, mh, s*0.5) behind a warp-uniform
+// branch.  Replaces one FP64 operation per face.
+static __device__ __noinline__ double corr_a_fallback(double c, double mh, bool neg) {
+  return fma(c, mh, neg ? -0.5 : 0.5);
+}
+__device__ __forceinline__ double corr_a_int(bits64 ub, bool neg, double c, double mh) {
+  const int eu = (int)(ub >> 52);
+  const bits64 mu = (ub & kMantMask) | (eu ? kImplicit : 0ULL);
+  const int sl = eu - 1012;  // E + 11: U = u * 2^63
+  const bits64 U = sl >= 0 ? (mu << (sl < 63 ? sl : 63)) : (mu >> (-sl < 63 ? -sl : 63));
+  const bits64 D = 0x8000000000000000ULL - U;  // (1 - u) * 2^63 > 0 for u < 1
+  const int lz = __clzll((long long)D);
+  const bits64 N = D << lz;
+  double out = bitsd((neg ? kSignMask : 0ULL) | ((bits64)(1022 - lz) << 52) | ((N >> 11) & kMantMask));
+  if (eu >= 1023) out = corr_a_fallback(c, mh, neg);
+  return out;
+}
+// u = |c|*y as bits (truncated significand product, as mul_pos_bits) for a
+// positive normal y; zero and subnormal |c| give u = 0.
+__device__ __forceinline__ bits64 courant_bits(double c, double y) {
+  const bits64 ax = dbits(c) & kAbsMask;
+  return ax < kImplicit ? 0ULL : mul_pos_bits(ax, y);
+}
+
 // a*b rounded to nearest even, computed on the integer pipe: the 53-bit
 // significands' 106-bit product from a 64x64 multiply (high and low
 // halves), the dropped bits and a sticky bit decide the rounding (IEEE-754

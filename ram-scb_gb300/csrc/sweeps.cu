@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
         c = (kCo == 2) ? cst[f - 1] : ((f == nr - 1) ? cNm : fma(grt[f - 1], p4, cr[f - 1]));
         if (kCfl && outside[f - 1] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
         const bool neg = is_neg(c);
-        const double a = (kCo == 2) ? ast[f - 1] : fma(c, -0.5, neg ? -0.5 : 0.5);
+        const double a = (kCo == 2) ? ast[f - 1] : corr_a_int(dbits(c) & kAbsMask, neg, c, -0.5);
         if (kCo == 1) { cst[f - 1] = c; ast[f - 1] = a; }
         int cs;
         const double fb = (kRec == 2)
@@ -108,8 +108,9 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
         fbn = g0;
       } else {
         const double xp = g2 - g1; const bits64 bxp = babs_bits(beta, xp);
-        fbn = (kRec == 2) ? face_value_frozen(x, xp, g1, fma(cN, -0.5, -0.5), beta, csn = rl[nr - 1] & 7)
-                          : face_value_case(x, bx, xp, bxp, g1, fma(cN, -0.5, -0.5), csn);
+        const double an = corr_a_int(dbits(cN) & kAbsMask, true, cN, -0.5);
+        fbn = (kRec == 2) ? face_value_frozen(x, xp, g1, an, beta, csn = rl[nr - 1] & 7)
+                          : face_value_case(x, bx, xp, bxp, g1, an, csn);
       }
       if (closed) fbn = 0.0;
       const double phin = cN * fbn;
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
       int csN;
       {
         const bool neg = is_neg(cN);
-        const double a = (kCo == 2) ? ast[(long long)(nt - 1) * st] : fma(cN, -0.5, neg ? -0.5 : 0.5);
+        const double a = (kCo == 2) ? ast[(long long)(nt - 1) * st] : corr_a_int(dbits(cN) & kAbsMask, neg, cN, -0.5);
         if (kCo == 1) { cst[(long long)(nt - 1) * st] = cN; ast[(long long)(nt - 1) * st] = a; }
         phiN = cN * ((kRec == 2)
             ? face_value_frozen(XN, neg ? X2 : XNm, neg ? G2 : GN, a, beta, csN = rl[(long long)(nt - 1) * st] & 7)
@@ -201,7 +202,7 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
         const double c = (kCo == 2) ? cst[(long long)(J - 1) * st] : CJ(J);
         if (kCfl && outside[(long long)(J - 1) * nr] == 0) q = umax64(q, cfl_bits(c, kBits1em10));
         const bool neg = is_neg(c);
-        const double a = (kCo == 2) ? ast[(long long)(J - 1) * st] : fma(c, -0.5, neg ? -0.5 : 0.5);
+        const double a = (kCo == 2) ? ast[(long long)(J - 1) * st] : corr_a_int(dbits(c) & kAbsMask, neg, c, -0.5);
         if (kCo == 1) { cst[(long long)(J - 1) * st] = c; ast[(long long)(J - 1) * st] = a; }
         int cs;
         const unsigned char* rj = (kRec == 1 || kRec == 2) ? rl + (long long)(J - 1) * st : nullptr;

@@ -231,6 +231,35 @@ module ModRamGpu
        type(c_ptr), intent(in) :: f2(*)
        type(c_ptr), value :: ppert, ppart
      end function
+     ! ram_run on RAM's own arrays: f2(m) = c_loc(F2) of member m, the whole
+     ! F2(NS,NR,NT,NE,NPA) as the module holds it; ppert(m), ppart(m) =
+     ! c_loc(PPERT), c_loc(PPART) (NS,NR,NT); c_null_ptr skips an entry
+     integer(c_int) function ramgpu_ram_run_ref(ctx, dts, f2, ppert, ppart) &
+          bind(C, name="ramgpu_ram_run_ref")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), value :: dts
+       type(c_ptr), intent(in) :: f2(*), ppert(*), ppart(*)
+     end function
+     integer(c_int) function ramgpu_set_ref_staging(ctx, force) bind(C, name="ramgpu_set_ref_staging")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: force
+     end function
+     ! restart files of the device state (write_restart / read_restart);
+     ! path: a NUL-terminated file name (trim(name)//c_null_char)
+     integer(c_int) function ramgpu_save_state(ctx, path, time) bind(C, name="ramgpu_save_state")
+       import :: c_int, c_ptr, c_char, c_double
+       type(c_ptr), value :: ctx
+       character(kind=c_char), intent(in) :: path(*)
+       real(c_double), value :: time
+     end function
+     integer(c_int) function ramgpu_load_state(ctx, path, time) bind(C, name="ramgpu_load_state")
+       import :: c_int, c_ptr, c_char, c_double
+       type(c_ptr), value :: ctx
+       character(kind=c_char), intent(in) :: path(*)
+       real(c_double), intent(out) :: time
+     end function
      integer(c_int) function ramgpu_set_pipeline_groups(ctx, groups) &
           bind(C, name="ramgpu_set_pipeline_groups")
        import :: c_int, c_ptr

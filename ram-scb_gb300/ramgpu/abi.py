@@ -38,6 +38,7 @@ EXPORTS = (
     "ramgpu_loss_wae", "ramgpu_bounce_integrals", "ramgpu_upload_f2_async", "ramgpu_download_f2_async",
     "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store", "ramgpu_compute_hI",
     "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_ram_run_ref", "ramgpu_set_ref_staging", "ramgpu_autotune_trials",
+    "ramgpu_save_state", "ramgpu_load_state", "ramgpu_snapshot_info",
     "ramgpu_set_pipeline_groups", "ramgpu_pipeline_groups",
     "ramgpu_set_step_groups", "ramgpu_step_groups", "ramgpu_set_pipeline_trace", "ramgpu_pipeline_trace",
     "ramgpu_check", "ramgpu_set_check", "ramgpu_last_status",
@@ -64,6 +65,24 @@ class Status(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class SnapshotInfo(C.Structure):
+    """ramgpu_snapshot_info_t: header of a snapshot file."""
+    _fields_ = [("nr", C.c_int), ("nt", C.c_int), ("ne", C.c_int), ("npa", C.c_int), ("ns", C.c_int),
+                ("n_members", C.c_int), ("flags", C.c_uint), ("time", C.c_double)]
+
+
+def snapshot_info(path) -> dict:
+    """Header of a snapshot file after its checksum is checked (no GPU)."""
+    lib = load_library()
+    info = SnapshotInfo()
+    rc = lib.ramgpu_snapshot_info(str(path).encode(), C.byref(info))
+    if rc != RAMGPU_OK:
+        buf = C.create_string_buffer(256)
+        lib.ramgpu_last_error(None, buf, 256)
+        raise RamGpuError(f"snapshot_info: {buf.value.decode()}", rc)
+    return {k: getattr(info, k) for k, _ in SnapshotInfo._fields_}
 
 
 class Config(C.Structure):
@@ -169,6 +188,9 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_ram_run_ref": ([vp, d, vp, vp, vp], i),
         "ramgpu_set_ref_staging": ([vp, i], i),
         "ramgpu_autotune_trials": ([vp, dp, dp], i),
+        "ramgpu_save_state": ([vp, C.c_char_p, d], i),
+        "ramgpu_load_state": ([vp, C.c_char_p, dp], i),
+        "ramgpu_snapshot_info": ([C.c_char_p, C.POINTER(SnapshotInfo)], i),
         "ramgpu_set_pipeline_groups": ([vp, i], i),
         "ramgpu_pipeline_groups": ([vp], i),
         "ramgpu_set_step_groups": ([vp, i], i),
@@ -419,6 +441,16 @@ class RamGpu:
             tabs = tuple(table(q, n, w) for q, n, w in zip(seqs, sizes, ("f2", "ppert", "ppart")))
             self._ref_tables = (key, tabs, seqs)
         self._ck(self.lib.ramgpu_ram_run_ref(self.h, float(dts), *self._ref_tables[1]), "ram_run_ref")
+
+    def save_state(self, path, time: float = 0.0):
+        """The context's evolving state to a snapshot file (ramgpu_save_state)."""
+        self._ck(self.lib.ramgpu_save_state(self.h, str(path).encode(), float(time)), "save_state")
+
+    def load_state(self, path) -> float:
+        """State from a snapshot file; returns the time saved with it."""
+        t = C.c_double(0.0)
+        self._ck(self.lib.ramgpu_load_state(self.h, str(path).encode(), C.byref(t)), "load_state")
+        return t.value
 
     def set_ref_staging(self, force: bool):
         """Move reference-layout arrays by the copy engines even when the
