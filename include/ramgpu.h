@@ -222,6 +222,19 @@ int ramgpu_ram_run_ref(ramgpu_ctx *ctx, double dts, double *const *f2, double *c
  * arrays the device could reach in place (no reference counterpart; for
  * hosts whose coherent link is slower than their copy engines). */
 int ramgpu_set_ref_staging(ramgpu_ctx *ctx, int force);
+/* Chunks of L planes the host calls (ramgpu_ram_run_host, ramgpu_ram_run_ref)
+ * pipeline F2 over: 1..8, or 0 for the item-group pipeline of
+ * ramgpu_set_pipeline_groups (also taken with RAMGPU_FLAG_LOSSES, the
+ * pitch-angle diffusion or the pipeline trace; the reference-layout call
+ * then runs unpipelined), or -1 (default): item groups for
+ * ramgpu_ram_run_host, 4 chunks for ramgpu_ram_run_ref, the faster choice
+ * of each on the four-species step.  L is F2's slowest index,
+ * so a chunk is one contiguous range of every array, and the R, P, E sweeps
+ * and the closing copy/mask work plane by plane: chunk c's forward R, P, E
+ * run while chunk c+1 lands, the pitch-angle sweeps once all are in, and
+ * chunk c goes back right after its reverse R while the next computes.
+ * Results are the same for every count. */
+int ramgpu_set_pipeline_chunks(ramgpu_ctx *ctx, int chunks);
 /* Number of item groups ramgpu_ram_run_host pipelines its copies over
  * (1..8, default 4, at most one per item; 1 with RAMGPU_FLAG_LOSSES). */
 int ramgpu_set_pipeline_groups(ramgpu_ctx *ctx, int groups);

@@ -113,6 +113,11 @@ struct ramgpu_ctx {
   // ramgpu_ram_run_host: item groups, their streams and events, and the
   // graph of the whole pipeline for one set of host buffers
   int pipe_groups = 4;  // ramgpu_ram_run_host's copy groups
+  // the host calls' plane-chunk pipeline: chunks of L planes (0: off) and
+  // its events (per chunk: input landed, forward R/P/E done, chunk done;
+  // then start, tables, pitch-angle sweeps done)
+  int pipe_chunks = -1;  // -1: per call (item groups for per-species arrays, 4 chunks for the reference layout)
+  std::vector<cudaEvent_t> chunk_events;
   int step_groups = 4;  // ram_run's concurrent item groups (autotuned)
   cudaGraphExec_t pipe_exec = nullptr;
   std::vector<const void*> pipe_key;
@@ -754,6 +759,111 @@ static int ensure_group_streams(ramgpu_ctx* ctx, int G) {
   return RAMGPU_OK;
 }
 
+// ram_run with F2 crossing the host boundary, pipelined over chunks of L
+// planes.  L is the slowest index of F2, in the library's per-species
+// blocks and in the reference's F2(NS,NR,NT,NE,NPA) alike, so a chunk of
+// planes is one contiguous range of every array; and every line of the R,
+// P and E sweeps and of the closing copy/mask lies in one plane.  So the
+// forward R, P, E of chunk c run as soon as its planes have landed (while
+// the next chunk's arrive over the host link), the pitch-angle sweeps
+// (whose lines span every plane) run once all chunks are in, and the
+// reverse E, P, R and the copy/mask of chunk c are followed at once by its
+// read-back (while the next chunk computes).  ANISCH, which rewrites the
+// L = 1 plane, runs last; that plane and the moments go back after it.
+// Streams: chunk c on its own stream; inputs chained in chunk order (they
+// share the link); the per-member tables, ghost planes and pitch-angle
+// sweeps on the context's stream, joined by events.  in(c, stream, l0, l1)
+// and out(c, stream, l0, l1) enqueue the copies of planes [l0, l1);
+// tail(stream) the L = 1 plane and the moments.  The sweeps over disjoint
+// planes write disjoint cells, and CFL maxima and clip counts combine by
+// atomic max/add, so results equal the resident step's bit for bit.
+static int ensure_chunk_events(ramgpu_ctx* ctx, int C) {
+  while ((int)ctx->chunk_events.size() < 3 * C + 3) {
+    cudaEvent_t e = nullptr;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ctx->chunk_events.push_back(e);
+  }
+  return RAMGPU_OK;
+}
+
+template <class In, class Out, class Tail>
+static int enqueue_chunked(ramgpu_ctx* ctx, double dts, int C, In&& in, Out&& out, Tail&& tail) {
+  if (int rc = ensure_group_streams(ctx, C)) return rc;
+  if (int rc = ensure_chunk_events(ctx, C)) return rc;
+  const Dev full = ctx->d;
+  const cudaStream_t main = ctx->stream;
+  const int npa = full.npa;
+  auto lo = [&](int c) { return (int)((long long)npa * c / C); };
+  cudaEvent_t* ev = ctx->chunk_events.data();
+  cudaEvent_t ev_start = ev[3 * C], ev_tab = ev[3 * C + 1], ev_mu = ev[3 * C + 2];
+  auto co = [&](int w, int k) { return (full.coef && full.coef_slot[w] >= 0) ? k : 0; };
+  int rc = RAMGPU_OK;
+  CK(cudaEventRecord(ev_start, main));
+  if ((rc = enqueue_tables(ctx, dts))) return rc;
+  CK(cudaMemsetAsync(full.cflq, 0, sizeof(unsigned long long) * 5 * full.nm * full.ns, main));
+  CK(cudaEventRecord(ev_tab, main));
+  for (int c = 0; c < C; ++c) {
+    cudaStream_t st = ctx->pipe_streams[c];
+    CK(cudaStreamWaitEvent(st, c == 0 ? ev_start : ev[3 * (c - 1)], 0));
+    if ((rc = in(c, st, lo(c), lo(c + 1)))) return rc;
+    CK(cudaEventRecord(ev[3 * c], st));
+    CK(cudaStreamWaitEvent(st, ev_tab, 0));
+    Dev dc = full;
+    dc.lw0 = lo(c);
+    dc.lw1 = lo(c + 1);
+    { NvtxRange r("DRIFTR"); launch_sweep_r(dc, dts, true, st, nullptr, false, co(0, 1)); }
+    { NvtxRange r("DRIFTP"); launch_sweep_p(dc, dts, true, st, nullptr, false, co(1, 1)); }
+    { NvtxRange r("DRIFTE"); launch_sweep_e(dc, dts, true, st, nullptr, false, co(2, 1)); }
+    ctx->launches += 3;
+    CKL("chunk forward sweeps");
+    CK(cudaEventRecord(ev[3 * c + 1], st));
+    CK(cudaStreamWaitEvent(main, ev[3 * c + 1], 0));
+  }
+  {
+    NvtxRange r("DRIFTMU");
+    launch_sweep_mu(full, dts, true, 1, full.loss2, main, nullptr, false, co(3, 1));
+    launch_sweep_mu(full, dts, false, 0, nullptr, main, nullptr, false, co(3, 2));
+    ctx->launches += 2;
+    CKL("pitch-angle sweeps");
+  }
+  CK(cudaEventRecord(ev_mu, main));
+  for (int c = 0; c < C; ++c) {
+    cudaStream_t st = ctx->pipe_streams[c];
+    CK(cudaStreamWaitEvent(st, ev_mu, 0));
+    Dev dc = full;
+    dc.lw0 = lo(c);
+    dc.lw1 = lo(c + 1);
+    { NvtxRange r("DRIFTE"); launch_sweep_e(dc, dts, false, st, nullptr, false, co(2, 2)); }
+    { NvtxRange r("DRIFTP"); launch_sweep_p(dc, dts, false, st, nullptr, false, co(1, 2)); }
+    { NvtxRange r("DRIFTR"); launch_sweep_r(dc, dts, false, st, nullptr, false, co(0, 2)); }
+    launch_finish(dc, st);
+    ctx->launches += 4;
+    CKL("chunk reverse sweeps");
+    if ((rc = out(c, st, lo(c), lo(c + 1)))) return rc;
+    CK(cudaEventRecord(ev[3 * c + 2], st));
+    CK(cudaStreamWaitEvent(main, ev[3 * c + 2], 0));
+  }
+  { NvtxRange r("ANISCH"); launch_moments(full, main); }
+  ctx->launches += 2;
+  CKL("moments");
+  if ((rc = tail(main))) return rc;
+  if (ctx->check_on) rc = enqueue_status(ctx);
+  return rc;
+}
+
+// Whether the host calls take the plane-chunk pipeline: not with the loss
+// bookkeeping, the pitch-angle diffusion or the per-group trace (those keep
+// the item-group pipeline), and only with at least two planes per chunk.
+// auto_chunks: the count used while the setting is automatic (-1).  Measured
+// on the four-species step: per-species page-locked arrays go faster over
+// the item-group pipeline (0.69 ms per call against 0.93-1.07 ms chunked),
+// the reference layout over 4 chunks (0.88 ms against 0.91 ms unchunked).
+static int chunk_count(const ramgpu_ctx* ctx, int auto_chunks) {
+  const int want = ctx->pipe_chunks < 0 ? auto_chunks : ctx->pipe_chunks;
+  if (want <= 0 || (ctx->cfg.flags & RAMGPU_FLAG_LOSSES) || ctx->pd_any() || ctx->pipe_trace) return 0;
+  return std::max(1, std::min(want, ctx->d.npa / 2));
+}
+
 // Uploads, sweeps and read-back of ram_run pipelined over item groups.
 // Stream order: the context's stream (previous work) -> event -> group
 // uploads chained in group order (so the first group starts computing
@@ -867,6 +977,8 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   const int blk0[4] = {128, 128, 64, 64};
   for (int w = 0; w < 4; ++w) { d.blk[w] = blk0[w]; d.pers[w] = 0; }
   d.mu_lanes = d.npa >= 12 ? 2 : 1;
+  d.lw0 = 0;
+  d.lw1 = d.npa;
   const size_t nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa, ns = d.ns, nm = d.nm, nf = d.nf;
   const size_t nijl = nr * nt * npa, nfield = nf * nt * npa, nslot = nm * ns;
   bool ok = true;
@@ -986,6 +1098,7 @@ int ramgpu_destroy(ramgpu_ctx* ctx) {
   for (cudaStream_t st : ctx->pipe_copy_streams) cudaStreamDestroy(st);
   for (cudaEvent_t e : ctx->pipe_fin_events) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->pipe_copy_done) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->chunk_events) cudaEventDestroy(e);
   if (ctx->status_h) cudaFreeHost(ctx->status_h);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -1509,19 +1622,62 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
   }
   const std::vector<char>& pageable = ctx->cls_pageable;
   if (ctx->cls_engine_pageable) capturable = false;
+  const int C = ctx->cls_engine_pageable ? 0 : chunk_count(ctx, 0);
+  // the copies of planes [l0, l1) of every item with a host array
+  const long long plane = (long long)ctx->d.nr * ctx->d.nt * ctx->d.ne;
+  const size_t nm2 = (size_t)ctx->d.nr * ctx->d.nt, ns2 = (size_t)nslot;
+  auto h_in = [&](int, cudaStream_t st, int l0, int l1) {
+    for (size_t i = 0; i < ctx->items_h.size(); ++i) {
+      const int slot = ctx->items_h[i].x * ctx->d.ns + ctx->items_h[i].y;
+      if (f2[slot])
+        if (int r = pipe_copy(ctx, ctx->d.f2 + (size_t)slot * ctx->d.ncell + l0 * plane, f2[slot] + l0 * plane,
+                              (size_t)(l1 - l0) * plane, pageable[slot], st))
+          return r;
+    }
+    return RAMGPU_OK;
+  };
+  auto h_out = [&](int, cudaStream_t st, int l0, int l1) {
+    const int a = std::max(l0, 1);  // the L = 1 plane goes back after ANISCH
+    for (size_t i = 0; i < ctx->items_h.size() && a < l1; ++i) {
+      const int slot = ctx->items_h[i].x * ctx->d.ns + ctx->items_h[i].y;
+      if (f2[slot])
+        if (int r = pipe_copy(ctx, f2[slot] + a * plane, ctx->d.f2 + (size_t)slot * ctx->d.ncell + a * plane,
+                              (size_t)(l1 - a) * plane, pageable[slot], st))
+          return r;
+    }
+    return RAMGPU_OK;
+  };
+  auto h_tail = [&](cudaStream_t st) {
+    for (size_t i = 0; i < ctx->items_h.size(); ++i) {
+      const int slot = ctx->items_h[i].x * ctx->d.ns + ctx->items_h[i].y;
+      int r = RAMGPU_OK;
+      if (f2[slot])
+        r = pipe_copy(ctx, f2[slot], ctx->d.f2 + (size_t)slot * ctx->d.ncell, (size_t)plane, pageable[slot], st);
+      if (!r && ppert && ppert[slot])
+        r = pipe_copy(ctx, ppert[slot], ctx->d.ppert + (size_t)slot * nm2, nm2, pageable[ns2 + slot], st);
+      if (!r && ppart && ppart[slot])
+        r = pipe_copy(ctx, ppart[slot], ctx->d.ppart + (size_t)slot * nm2, nm2, pageable[2 * ns2 + slot], st);
+      if (r) return r;
+    }
+    return RAMGPU_OK;
+  };
+  auto enqueue = [&]() {
+    if (C > 0) return enqueue_chunked(ctx, dts, C, h_in, h_out, h_tail);
+    int r = enqueue_pipeline(ctx, dts, f2, ppert, ppart, G, pageable);
+    if (!r && ctx->check_on) r = enqueue_status(ctx);
+    return r;
+  };
   if (!capturable) {
-    rc = enqueue_pipeline(ctx, dts, f2, ppert, ppart, G, pageable);
-    if (!rc && ctx->check_on) rc = enqueue_status(ctx);
+    rc = enqueue();
   } else {
     if (!ctx->pipe_exec || ctx->pipe_key != key || ctx->pipe_dts != dts || ctx->pipe_items != ctx->items_version ||
-        ctx->pipe_flags != ctx->d.flags || ctx->pipe_shape != ctx->shape_version || ctx->pipe_g != G) {
+        ctx->pipe_flags != ctx->d.flags || ctx->pipe_shape != ctx->shape_version || ctx->pipe_g != G + 16 * C) {
       if (ctx->pipe_exec) cudaGraphExecDestroy(ctx->pipe_exec);
       ctx->pipe_exec = nullptr;
       cudaGraph_t g = nullptr;
       const long long l0 = ctx->launches;
       CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      rc = enqueue_pipeline(ctx, dts, f2, ppert, ppart, G, pageable);
-      if (!rc && ctx->check_on) rc = enqueue_status(ctx);
+      rc = enqueue();
       cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
       ctx->pipe_launches = ctx->launches - l0;  // kernels per replay
       ctx->launches = l0;
@@ -1542,7 +1698,7 @@ int ramgpu_ram_run_host(ramgpu_ctx* ctx, double dts, double* const* f2, double* 
       ctx->pipe_items = ctx->items_version;
       ctx->pipe_flags = ctx->d.flags;
       ctx->pipe_shape = ctx->shape_version;
-      ctx->pipe_g = G;
+      ctx->pipe_g = G + 16 * C;
     }
     CK(cudaGraphLaunch(ctx->pipe_exec, ctx->stream));
     ctx->launches += ctx->pipe_launches;
@@ -1680,17 +1836,53 @@ int ramgpu_ram_run_ref(ramgpu_ctx* ctx, double dts, double* const* f2, double* c
     ctx->timing = timing;
     return rc;
   }
+  const int C = staged ? 0 : chunk_count(ctx, 4);
+  const long long plane = (long long)ctx->d.nr * ctx->d.nt * ctx->d.ne;
+  const int ns = ctx->d.ns;
+  const long long n = ctx->d.ncell, nm2 = (long long)ctx->d.nr * ctx->d.nt;
+  auto r_in = [&](int, cudaStream_t st, int l0, int l1) {
+    for (int m = 0; m < nm; ++m)
+      if (mem[m].f2) {
+        launch_ref_gather(mem[m].f2r, ctx->d.f2 + (size_t)m * ns * n, ns, n, l0 * plane, l1 * plane, ctx->nsm, st);
+        ctx->launches += 1;
+      }
+    CKL("reference-layout gather");
+    return RAMGPU_OK;
+  };
+  auto r_out = [&](int, cudaStream_t st, int l0, int l1) {
+    const int a = std::max(l0, 1);  // the L = 1 plane goes back after ANISCH
+    for (int m = 0; m < nm && a < l1; ++m)
+      if (mem[m].f2) {
+        launch_ref_scatter(ctx->d.f2 + (size_t)m * ns * n, mem[m].f2r, ns, n, a * plane, l1 * plane, ctx->nsm, st);
+        ctx->launches += 1;
+      }
+    CKL("reference-layout scatter");
+    return RAMGPU_OK;
+  };
+  auto r_tail = [&](cudaStream_t st) {
+    for (int m = 0; m < nm; ++m) {
+      int r = RAMGPU_OK;
+      if (mem[m].f2) r = ref_out(ctx, mem[m].f2, mem[m].f2r, ctx->d.f2 + (size_t)m * ns * n, n, 0, plane, st);
+      if (!r && mem[m].pe) r = ref_out(ctx, mem[m].pe, mem[m].per, ctx->d.ppert + (size_t)m * ns * nm2, nm2, 0, nm2, st);
+      if (!r && mem[m].pa) r = ref_out(ctx, mem[m].pa, mem[m].par, ctx->d.ppart + (size_t)m * ns * nm2, nm2, 0, nm2, st);
+      if (r) return r;
+    }
+    return RAMGPU_OK;
+  };
+  auto enqueue = [&]() {
+    return C > 0 ? enqueue_chunked(ctx, dts, C, r_in, r_out, r_tail) : enqueue_ref(ctx, dts, mem, staged, G);
+  };
   if (!ctx->graph_on || staged) {
-    rc = enqueue_ref(ctx, dts, mem, staged, G);
+    rc = enqueue();
   } else {
     if (!ctx->ref_exec || ctx->ref_key != key || ctx->ref_dts != dts || ctx->ref_items != ctx->items_version ||
-        ctx->ref_flags != ctx->d.flags || ctx->ref_shape != ctx->shape_version || ctx->ref_g != G) {
+        ctx->ref_flags != ctx->d.flags || ctx->ref_shape != ctx->shape_version || ctx->ref_g != G + 16 * C) {
       if (ctx->ref_exec) cudaGraphExecDestroy(ctx->ref_exec);
       ctx->ref_exec = nullptr;
       cudaGraph_t g = nullptr;
       const long long l0 = ctx->launches;
       CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      rc = enqueue_ref(ctx, dts, mem, staged, G);
+      rc = enqueue();
       cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
       ctx->ref_launches = ctx->launches - l0;
       ctx->launches = l0;
@@ -1706,7 +1898,7 @@ int ramgpu_ram_run_ref(ramgpu_ctx* ctx, double dts, double* const* f2, double* c
         ctx->ref_items = ctx->items_version;
         ctx->ref_flags = ctx->d.flags;
         ctx->ref_shape = ctx->shape_version;
-        ctx->ref_g = G;
+        ctx->ref_g = G + 16 * C;
       }
     }
     if (!rc) {
@@ -1721,6 +1913,13 @@ int ramgpu_ram_run_ref(ramgpu_ctx* ctx, double dts, double* const* f2, double* c
     ctx->status_valid = true;
     return status_out(ctx, nullptr);
   }
+  return RAMGPU_OK;
+}
+
+int ramgpu_set_pipeline_chunks(ramgpu_ctx* ctx, int chunks) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (chunks < -1 || chunks > 8) return fail(ctx, RAMGPU_ERR_ARG, "chunks must be -1..8");
+  ctx->pipe_chunks = chunks;
   return RAMGPU_OK;
 }
 

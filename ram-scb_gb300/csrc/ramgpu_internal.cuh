@@ -122,6 +122,9 @@ struct Dev {
   int blk[4];
   int pers[4];
   int mu_lanes;  // lanes per DRIFTMU line: 2 (lane pairs, NPA >= 12) or 1
+  // L window of the R, P and E sweeps and the closing copy/mask: planes
+  // [lw0, lw1) (0 and NPA: all); a host pipeline runs them chunk by chunk
+  int lw0, lw1;
 };
 
 // ---------------------------------------------------------------- bit tests

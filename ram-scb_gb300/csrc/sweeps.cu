@@ -26,7 +26,10 @@ namespace ramgpu {
 template <bool kCfl, int kRec, int kCo>
 __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
-  const int nlines = nt * ne * d.npa;
+  // the lines of the L window [lw0, lw1) (all of them unless a pipeline
+  // runs the step plane chunk by plane chunk): L is the slowest index
+  const int line0 = d.lw0 * nt * ne;
+  const int nlines = nt * ne * (d.lw1 - d.lw0);
   // Work units are (item, block of lines).  A grid of (blocks per item,
   // items) gives one unit per CTA; a persistent grid loops over them.
   const int bpi = (nlines + blockDim.x - 1) / blockDim.x;
@@ -35,10 +38,10 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
        u += (long long)gridDim.x * gridDim.y) {
     const int2 item = d.items[u / bpi];
     const int m = item.x, s = item.y, slot = m * d.ns + s;
-    const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
+    const int line = line0 + (int)(u % bpi) * blockDim.x + threadIdx.x;
     unsigned long long q = 0ULL;  // CFL quotient bits
     unsigned nclip = 0;  // clip events (kRec == kRecCount)
-    if (line < nlines) {
+    if (line < line0 + nlines) {
       const int j = line % nt;
       const int l = line / (nt * ne);
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + (long long)line * nr;
@@ -129,7 +132,8 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
 template <bool kCfl, int kRec, int kCo>
 __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
-  const int nlines = (nr - 1) * ne * d.npa;
+  const int line0 = d.lw0 * (nr - 1) * ne;  // the L window, as in DRIFTR
+  const int nlines = (nr - 1) * ne * (d.lw1 - d.lw0);
   // Work units are (item, block of lines).  A grid of (blocks per item,
   // items) gives one unit per CTA; a persistent grid loops over them.
   const int bpi = (nlines + blockDim.x - 1) / blockDim.x;
@@ -138,10 +142,10 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
        u += (long long)gridDim.x * gridDim.y) {
     const int2 item = d.items[u / bpi];
     const int m = item.x, s = item.y, slot = m * d.ns + s;
-    const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
+    const int line = line0 + (int)(u % bpi) * blockDim.x + threadIdx.x;
     unsigned long long q = 0ULL;  // CFL quotient bits
     unsigned nclip = 0;  // clip events (kRec == kRecCount)
-    if (line < nlines) {
+    if (line < line0 + nlines) {
       const int i = 1 + line % (nr - 1);
       const int kl = line / (nr - 1);
       const int k = kl % ne, l = kl / ne;
@@ -239,7 +243,8 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
 template <bool kCfl, int kRec, int kCo>
 __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
-  const int nlines = (nr - 1) * nt * d.npa;
+  const int line0 = d.lw0 * (nr - 1) * nt;  // the L window, as in DRIFTR
+  const int nlines = (nr - 1) * nt * (d.lw1 - d.lw0);
   // Work units are (item, block of lines).  A grid of (blocks per item,
   // items) gives one unit per CTA; a persistent grid loops over them.
   const int bpi = (nlines + blockDim.x - 1) / blockDim.x;
@@ -248,10 +253,10 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
        u += (long long)gridDim.x * gridDim.y) {
     const int2 item = d.items[u / bpi];
     const int m = item.x, s = item.y, slot = m * d.ns + s;
-    const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
+    const int line = line0 + (int)(u % bpi) * blockDim.x + threadIdx.x;
     unsigned long long q = 0ULL;  // CFL quotient bits
     unsigned nclip = 0;  // clip events (kRec == kRecCount)
-    if (line < nlines) {
+    if (line < line0 + nlines) {
       const int i = 1 + line % (nr - 1);
       const int jl = line / (nr - 1);
       const int j = jl % nt, l = jl / nt;
@@ -506,11 +511,13 @@ static inline dim3 grid_for(const Dev& d, int w, int nlines) {
   if (d.pers[w] > 0) return dim3(d.pers[w], 1, 1);
   return dim3((nlines + blk - 1) / blk, d.nitems, 1);
 }
+// Lines of sweep w: R, P and E within the L window [lw0, lw1); every
+// pitch-angle line spans all L, so DRIFTMU always takes them all.
 static inline int nlines_of(const Dev& d, int w) {
   switch (w) {
-    case 0: return d.nt * d.ne * d.npa;
-    case 1: return (d.nr - 1) * d.ne * d.npa;
-    case 2: return (d.nr - 1) * d.nt * d.npa;
+    case 0: return d.nt * d.ne * (d.lw1 - d.lw0);
+    case 1: return (d.nr - 1) * d.ne * (d.lw1 - d.lw0);
+    case 2: return (d.nr - 1) * d.nt * (d.lw1 - d.lw0);
     default: return (d.nr - 1) * d.nt * d.ne;
   }
 }

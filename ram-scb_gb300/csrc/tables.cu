@@ -553,9 +553,10 @@ void launch_loss_apply(const Dev& d, const double* table, cudaStream_t st) {
 
 // ------------------------------------ periodic copy + magnetopause mask
 __global__ void k_finish(Dev d, int any_outside) {
-  const long long n = (long long)d.nr * d.ne * d.npa;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= n) return;
+  // the (I, K, L) of the L window [lw0, lw1)
+  const long long n = (long long)d.nr * d.ne * (d.lw1 - d.lw0);
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x + (long long)d.lw0 * d.nr * d.ne;
+  if (t >= n + (long long)d.lw0 * d.nr * d.ne) return;
   const int2 item = d.items[blockIdx.y];
   const int slot = item.x * d.ns + item.y;
   const int i = (int)(t % d.nr);
@@ -569,7 +570,7 @@ __global__ void k_finish(Dev d, int any_outside) {
 
 void launch_finish(const Dev& d, cudaStream_t st) {
   // any_outside is folded into the flags word bit 31 by the host
-  long long n = (long long)d.nr * d.ne * d.npa;
+  long long n = (long long)d.nr * d.ne * (d.lw1 - d.lw0);
   k_finish<<<dim3((unsigned)((n + 255) / 256), d.nitems), 256, 0, st>>>(d, (d.flags >> 31) & 1u);
 }
 

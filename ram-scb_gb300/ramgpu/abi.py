@@ -38,7 +38,7 @@ EXPORTS = (
     "ramgpu_loss_wae", "ramgpu_bounce_integrals", "ramgpu_upload_f2_async", "ramgpu_download_f2_async",
     "ramgpu_moments_async", "ramgpu_synchronize", "ramgpu_set_coef_store", "ramgpu_compute_hI",
     "ramgpu_get_fields", "ramgpu_ram_run_host", "ramgpu_ram_run_ref", "ramgpu_set_ref_staging", "ramgpu_autotune_trials",
-    "ramgpu_save_state", "ramgpu_load_state", "ramgpu_snapshot_info",
+    "ramgpu_save_state", "ramgpu_load_state", "ramgpu_snapshot_info", "ramgpu_set_pipeline_chunks",
     "ramgpu_set_pipeline_groups", "ramgpu_pipeline_groups",
     "ramgpu_set_step_groups", "ramgpu_step_groups", "ramgpu_set_pipeline_trace", "ramgpu_pipeline_trace",
     "ramgpu_check", "ramgpu_set_check", "ramgpu_last_status",
@@ -189,6 +189,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_set_ref_staging": ([vp, i], i),
         "ramgpu_autotune_trials": ([vp, dp, dp], i),
         "ramgpu_save_state": ([vp, C.c_char_p, d], i),
+        "ramgpu_set_pipeline_chunks": ([vp, i], i),
         "ramgpu_load_state": ([vp, C.c_char_p, dp], i),
         "ramgpu_snapshot_info": ([C.c_char_p, C.POINTER(SnapshotInfo)], i),
         "ramgpu_set_pipeline_groups": ([vp, i], i),
@@ -469,6 +470,10 @@ class RamGpu:
         out = np.zeros((self.ns, g.nr, g.nt, g.ne, g.npa), order="F")
         self._ck(self.lib.ramgpu_download_f2_all(self.h, int(member), _dptr(out)), "download_f2_all")
         return out
+
+    def set_pipeline_chunks(self, chunks: int):
+        """Chunks of L planes the host calls pipeline F2 over (0: item groups)."""
+        self._ck(self.lib.ramgpu_set_pipeline_chunks(self.h, int(chunks)), "set_pipeline_chunks")
 
     def set_pipeline_groups(self, groups: int):
         """Item groups ram_run_host pipelines its copies over."""

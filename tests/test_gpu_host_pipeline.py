@@ -286,3 +286,34 @@ def test_pipeline_argument_errors(tiny):
             gpu.ram_run_host(-1.0, _host_buffers(wl, 1))
     finally:
         gpu.close()
+
+
+@pytest.mark.parametrize("chunks", [0, 1, 2, 3, 4, 8])
+@pytest.mark.parametrize("graph", [False, True])
+def test_plane_chunk_pipeline_equals_resident_run(tiny, chunks, graph):
+    """ram_run_host over 0 (item groups), 1..8 chunks of L planes: the same
+    F2, moments and CFL bits as the resident single-stream step, with the
+    status pass (clip counts) on."""
+    wl = tiny
+    g = wl.grid
+    ns = len(g.species)
+    ref = _reference(wl)
+    gpu = _gpu(wl)
+    gpu.set_pipeline_chunks(chunks)
+    gpu.set_graph(graph)
+    gpu.set_check(True)
+    f2 = _host_buffers(wl, 1)
+    pe = [np.empty((g.nr, g.nt), order="F") for _ in range(ns)]
+    pa = [np.empty((g.nr, g.nt), order="F") for _ in range(ns)]
+    try:
+        for c in range(3):
+            gpu.set_kp(-1, 3.0 + c)
+            gpu.ram_run_host(wl.dts, f2, pe, pa)
+        for s in range(ns):
+            assert np.array_equal(f2[s], ref["f2"][s]), s
+            assert np.array_equal(gpu.download_f2(0, s), ref["f2"][s]), s
+            assert np.array_equal(pe[s], ref["mom"][s][0]) and np.array_equal(pa[s], ref["mom"][s][1])
+            assert np.array_equal(gpu.cfl(0, s), ref["cfl"][s])
+        assert gpu.last_status()["f2_nonfinite"] == 0
+    finally:
+        gpu.close()

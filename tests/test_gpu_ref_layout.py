@@ -80,9 +80,10 @@ def _reference(wl, members, species, calls):
 
 
 @pytest.mark.parametrize("memory", ["pageable", "pinned"])
-@pytest.mark.parametrize("graph,stage,groups", [(False, False, 1), (True, False, 4), (True, True, 2),
-                                                (False, True, 3)])
-def test_ram_run_ref_equals_per_species_path(wl, memory, graph, stage, groups):
+@pytest.mark.parametrize("graph,stage,groups,chunks", [(False, False, 1, 0), (True, False, 4, 0), (True, True, 2, 4),
+                                                       (False, True, 3, 0), (False, False, 2, 3),
+                                                       (True, False, 4, 4), (True, False, 1, 8)])
+def test_ram_run_ref_equals_per_species_path(wl, memory, graph, stage, groups, chunks):
     g = wl.grid
     ns = len(g.species)
     members = 2
@@ -94,6 +95,7 @@ def test_ram_run_ref_equals_per_species_path(wl, memory, graph, stage, groups):
     gpu.set_graph(graph)
     gpu.set_ref_staging(stage)
     gpu.set_step_groups(groups)
+    gpu.set_pipeline_chunks(chunks)
     keep = []
     f2, pe, pa = [], [], []
     for m in range(members):
