@@ -48,14 +48,19 @@ UNIT = "cell-updates/s"
 # launch.  The line reports whether the current sources still have that
 # digest; a changed kernel makes the figures stale until the next capture.
 NCU_CAPTURE = {
-    "sources_sha16": "unknown",
-    "command": ("ncu --set full --clock-control none -k regex:k_sweep -c 8 -o sweeps "
-                "python bench.py --steps 2 --warmup 1 --no-cpu-baseline --no-e2e --no-autotune "
-                "--members 0 --adj-calls 0 --no-padif --flush-mb 160"),
-    "dram_bytes": {"four_sp": {"driftr": 0.5 * (44.6e6 + 44.3e6), "driftp": 0.5 * (40.6e6 + 40.6e6),
-                               "drifte": 0.5 * (111.0e6 + 129.8e6), "driftmu": 0.5 * (81.8e6 + 40.3e6)}},
-    "fp64_ops_per_cell": {"driftr": 6.22, "driftp": 5.55, "drifte": 0.5 * (6.71 + 4.78),
-                          "driftmu": 0.5 * (6.81 + 5.84)},
+    # ncu on the sources named by sources_sha16 (profiles/sweeps_four_sp.md,
+    # profiles/driftr_refined.md): one kernel per command, each captured
+    # launch advances one species, so a four-species launch is scaled by 4.
+    "sources_sha16": "65ef85f50ccc6757",
+    "command": ("ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum,"
+                "smsp__sass_thread_inst_executed_op_{dadd,dfma,dmul}_pred_on.sum --clock-control none "
+                "-k regex:k_sweep_<r|p|e|mu> -c 2 python bench.py --steps 2 --warmup 1 --sections headline "
+                "--no-cpu-baseline --no-e2e --no-autotune [--workload refined]"),
+    "dram_bytes": {"four_sp": {"driftr": 4 * 11.02e6, "driftp": 4 * 10.39e6,
+                               "drifte": 4 * 0.5 * (11.34e6 + 29.98e6), "driftmu": 4 * 0.5 * (20.47e6 + 10.53e6)},
+                   "refined": {"driftr": 4 * 0.5 * (268.16e6 + 267.80e6)}},
+    "fp64_ops_per_cell": {"driftr": 5.02, "driftp": 4.64, "drifte": 0.5 * (6.70 + 4.78),
+                          "driftmu": 0.5 * (6.62 + 5.69)},
 }
 SWEEP_SOURCES = ["ram-scb_gb300/csrc/sweeps.cu", "ram-scb_gb300/csrc/ramgpu_internal.cuh",
                  "ram-scb_gb300/csrc/kernels.cuh"]
@@ -807,10 +812,16 @@ def run_adjoint(args, torch, np, abi, W, stream):
         nseg, nkeep = gpu.adj_segments()
         return J, gf, gb, tf, tb, nseg, nkeep
 
-    # checkpoints every kc calls with a one-segment record ring: every
-    # earlier segment is recomputed from its checkpoint (the configuration's
-    # policy, and the one for windows whose records do not fit in HBM)
-    J, gfr, gbr, tfr, tbr, nseg, _ = window(kc, 0)
+    # checkpoints every kc calls with the smallest record ring, two segments:
+    # every earlier segment is recomputed from its checkpoint on a second
+    # stream while the next one is transposed (the configuration's policy,
+    # and the one for windows whose records do not fit in HBM)
+    J, gfr, gbr, tfr, tbr, nseg, nkeep_r = window(kc, 0)
+    # the same without the overlap: a one-segment ring, each segment
+    # recomputed and then transposed on the same streams
+    gpu.set_adj_overlap(False)
+    _, gfs, gbs, tfs, tbs, _, nkeep_s = window(kc, 0)
+    gpu.set_adj_overlap(True)
     # the same checkpoints, the ring keeping as many segments as half of the
     # free HBM holds (here all: nothing recomputed)
     _, gf, gb, tfk, tbk, _, nkeep = window(kc, -1)
@@ -820,6 +831,7 @@ def run_adjoint(args, torch, np, abi, W, stream):
         return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
     same_r = max(rel(gfr, gf), rel(gbr, gb))
+    same_s = max(rel(gfs, gf), rel(gbs, gb))
     # one segment (k = ncalls): the record of every call, for the replays
     reset()
     gpu.adj_forward(nc, wl.dts, kp, nc, obs)
@@ -856,10 +868,16 @@ def run_adjoint(args, torch, np, abi, W, stream):
     out = {"window_calls": nc, "window_dts_steps": 2 * nc, "checkpoint_calls": kc, "observations": len(obs),
            "J": J, "forward_s": fwd_s, "timing": "CUDA events on the context's stream for forward and adjoint",
            "adj_forward_s": tfr, "adj_backward_s": tbr, "adjoint_over_forward": (tfr + tbr) / fwd_s,
-           "segments": nseg, "segments_recomputed": nseg - 1,
-           "policy": ("checkpoints every checkpoint_calls calls; the branch-record ring keeps one segment; the "
-                      "forward pass records only that segment and runs the plain step elsewhere; the backward "
-                      "pass recomputes every earlier segment from its checkpoint, recording, then transposes"),
+           "segments": nseg, "segments_kept": nkeep_r, "segments_recomputed": nseg - nkeep_r,
+           "policy": ("checkpoints every checkpoint_calls calls; the branch-record ring keeps two segments; the "
+                      "forward pass records only those and runs the plain step elsewhere; the backward pass "
+                      "recomputes every earlier segment from its checkpoint, recording, on a second stream "
+                      "while the following segment is transposed"),
+           "sequential_recompute": {"segments_kept": nkeep_s, "adj_forward_s": tfs, "adj_backward_s": tbs,
+                                    "adjoint_over_forward": (tfs + tbs) / fwd_s,
+                                    "gradient_vs_kept_max_rel_diff": same_s,
+                                    "policy": ("one-segment ring; each earlier segment recomputed, then "
+                                               "transposed, on the same streams")},
            "records_kept": {"segments_kept": nkeep, "adj_forward_s": tfk, "adj_backward_s": tbk,
                             "adjoint_over_forward": (tfk + tbk) / fwd_s,
                             "record_bytes": 8 * g.ncell * ns * nc,

@@ -467,7 +467,9 @@ typedef struct {
  * those of the window's last call).  The calls of the last nkeep checkpoint
  * segments record every limiter branch and clip into a ring of branch
  * records (8 bytes per cell, item and call) that holds as many segments as
- * the record budget allows (ramgpu_set_adj_record_budget; at least one);
+ * the record budget allows (ramgpu_set_adj_record_budget; at least one,
+ * two when the window has several segments and the overlapped
+ * recomputation is on);
  * the earlier calls, which ramgpu_adj_backward recomputes from their
  * checkpoints, run the plain step (the same F2 bits).  ramgpu_adj_digest
  * returns a digest of the recorded pattern.  The checkpoint buffer and the
@@ -481,15 +483,24 @@ int ramgpu_adj_forward(ramgpu_ctx *ctx, int ncalls, double dts, const double *kp
  * limiter branches frozen as recorded.  Each checkpoint segment before the
  * kept ones is recomputed from its checkpoint with recording, then every
  * call is transposed in reverse order; when the ring keeps every segment
- * (or k_ckpt >= ncalls) nothing is recomputed.  Either
+ * (or k_ckpt >= ncalls) nothing is recomputed.  With the overlapped
+ * recomputation on (ramgpu_set_adj_overlap) segment s-1 is recomputed on a
+ * second stream, with its own per-member tables, while segment s is
+ * transposed; the results are the same bits.  Either
  * output may be NULL; both may be host or device memory.  On return F2 is
  * the window's initial state again. */
 int ramgpu_adj_backward(ramgpu_ctx *ctx, double *grad_f2, double *grad_fgeos);
 /* Device bytes the adjoint's branch-record ring may take: bytes < 0 (the
  * default) means half of the free device memory when ramgpu_adj_forward
- * starts; a budget below one segment keeps one segment, so every earlier
- * segment is recomputed from its checkpoint. */
+ * starts; a budget below one segment keeps one segment (two with the
+ * overlapped recomputation), so every earlier segment is recomputed from
+ * its checkpoint. */
 int ramgpu_set_adj_record_budget(ramgpu_ctx *ctx, long long bytes);
+/* Overlapped recomputation in ramgpu_adj_backward (on = 1, the default):
+ * needs a ring of two segments (ramgpu_adj_forward then keeps at least
+ * two) and device memory for a copy of the per-member tables and ghost
+ * planes, allocated by the first backward pass that recomputes. */
+int ramgpu_set_adj_overlap(ramgpu_ctx *ctx, int on);
 /* Checkpoint segments of the last ramgpu_adj_forward and how many of them
  * (the last ones) the record ring keeps. */
 int ramgpu_adj_segments(ramgpu_ctx *ctx, int *nseg, int *nkeep);

@@ -110,6 +110,15 @@ struct ramgpu_ctx {
   // device bytes the adjoint's branch-record ring may use (-1: half of the
   // free device memory when the window starts)
   long long adj_record_budget = -1;
+  // ramgpu_adj_backward's overlapped recomputation: the segment before the
+  // one being transposed is recomputed on a second stream meanwhile, with
+  // its own copies of the per-member tables and ghost planes (adj_q points
+  // into adj_shadow); per ring slot the events "recomputed" and
+  // "transposed", then one for the start and the end
+  bool adj_overlap = true;
+  cudaStream_t adj_stream = nullptr;
+  void* adj_shadow = nullptr;
+  std::vector<cudaEvent_t> adj_events;
   // ramgpu_ram_run_host: item groups, their streams and events, and the
   // graph of the whole pipeline for one set of host buffers
   int pipe_groups = 4;  // ramgpu_ram_run_host's copy groups
@@ -1099,6 +1108,9 @@ int ramgpu_destroy(ramgpu_ctx* ctx) {
   for (cudaEvent_t e : ctx->pipe_fin_events) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->pipe_copy_done) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->chunk_events) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->adj_events) cudaEventDestroy(e);
+  if (ctx->adj_stream) cudaStreamDestroy(ctx->adj_stream);
+  cudaFree(ctx->adj_shadow);
   if (ctx->status_h) cudaFreeHost(ctx->status_h);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -2837,8 +2849,11 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
   const size_t rec_call = (size_t)8 * d.nitems * d.ncell;
   const int kseg = k_ckpt < ncalls ? k_ckpt : ncalls;
   // The ring keeps the records of the last nkeep segments, as many as the
-  // budget allows (at least one); only the segments before them are
-  // recomputed from their checkpoints in the backward pass.
+  // budget allows (at least one, two with the overlapped recomputation:
+  // the segment being recomputed and the one being transposed); only the
+  // segments before them are recomputed from their checkpoints in the
+  // backward pass.
+  const long long least = (ctx->adj_overlap && nseg > 1) ? 2 : 1;
   int nkeep = 1;
   {
     size_t free_b = 0, total_b = 0;
@@ -2848,7 +2863,7 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
     const long long budget = ctx->adj_record_budget >= 0 ? ctx->adj_record_budget : (long long)(free_b / 2);
     const long long seg_bytes = (long long)(rec_call * kseg);
     long long nk = budget / seg_bytes;
-    nkeep = (int)(nk < 1 ? 1 : (nk > nseg ? nseg : nk));
+    nkeep = (int)(nk < least ? least : (nk > nseg ? nseg : nk));
   }
   // buffers of the previous window are reused when the new one has the
   // same shape (a window run again, as finite differences do)
@@ -2921,6 +2936,83 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
   return RAMGPU_OK;
 }
 
+int ramgpu_set_adj_overlap(ramgpu_ctx* ctx, int on) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  ctx->adj_overlap = on != 0;
+  return RAMGPU_OK;
+}
+
+// The second stream, its events (2 per ring slot + 2) and the shadow copies
+// of everything a recorded call writes besides F2 and its record: Kp, the
+// per-member tables CR, CA, DRD1, DPD1, UE, UM and the DRIFTR ghost planes.
+// Returns in q the context's Dev with those pointers replaced and without
+// the coefficient store (the DRIFTE reverse recomputes its coefficients:
+// the same bits) or clip counting.
+static int adj_shadow_prepare(ramgpu_ctx* ctx, Dev& q) {
+  const Dev& d = ctx->d;
+  const size_t nm = (size_t)d.nm, nij = nm * d.nr * d.nt, nijl = nij * d.npa;
+  const size_t npl = nm * d.ns * d.ne * d.npa;
+  auto up = [](size_t n) { return (n + 31) / 32 * 32; };  // 256-byte pieces
+  const size_t ndbl = up(nm) + 4 * up(nij) + 2 * up(nijl) + 2 * up(npl);
+  const size_t bytes = 8 * ndbl + 4 * 3 * up(npl);
+  if (!ctx->adj_shadow && cudaMalloc(&ctx->adj_shadow, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->adj_shadow = nullptr;
+    return fail(ctx, RAMGPU_ERR_NOMEM, "adjoint recomputation tables: device allocation failed");
+  }
+  if (!ctx->adj_stream) {
+    int prio = 0;
+    if (!ctx->pipe_streams.empty()) CK(cudaStreamGetPriority(ctx->pipe_streams[0], &prio));
+    CK(cudaStreamCreateWithPriority(&ctx->adj_stream, cudaStreamNonBlocking, prio));
+  }
+  const size_t nev = 2 * (size_t)ctx->adj.nkeep + 2;
+  while (ctx->adj_events.size() < nev) {
+    cudaEvent_t e = nullptr;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ctx->adj_events.push_back(e);
+  }
+  double* p = (double*)ctx->adj_shadow;
+  auto take = [&](size_t n) { double* r = p; p += up(n); return r; };
+  q = d;
+  q.kp = take(nm);
+  q.cr = take(nij); q.ca = take(nij); q.drd1 = take(nij); q.dpd1 = take(nij);
+  q.ue = take(nijl); q.um = take(nijl);
+  q.plane_last = take(npl); q.plane_carry = take(npl);
+  int* ip = (int*)p;
+  q.plane_has = ip; ip += up(npl);
+  q.plane_last_src = ip; ip += up(npl);
+  q.plane_carry_src = ip;
+  q.coef = nullptr;
+  q.count_clips = 0;
+  return RAMGPU_OK;
+}
+
+// Call `call` of the window recomputed on stream st with the shadow tables
+// q, every sweep recording into rec: the sequence of enqueue_call_rec over
+// the whole work list as one group (the same records: a group's record
+// sits at its items' place in the list).
+static int adj_recompute_call(ramgpu_ctx* ctx, const Dev& q, cudaStream_t st, int call, double dts,
+                              unsigned char* rec) {
+  const int nm = ctx->cfg.n_members;
+  CK(cudaMemcpyAsync(q.kp, ctx->adj.kp_d + (size_t)call * nm, sizeof(double) * nm, cudaMemcpyDeviceToDevice, st));
+  const size_t isz = (size_t)q.nitems * q.ncell;
+  launch_member_coef(q, dts, st);
+  launch_ghost(q, st);
+  launch_sweep_r(q, dts, false, st, rec + 0 * isz);
+  launch_sweep_p(q, dts, false, st, rec + 1 * isz);
+  launch_sweep_e(q, dts, false, st, rec + 2 * isz);
+  launch_sweep_mu(q, dts, false, 1, q.loss2, st, rec + 3 * isz);
+  launch_sweep_mu(q, dts, false, 0, nullptr, st, rec + 4 * isz);
+  launch_sweep_e(q, dts, false, st, rec + 5 * isz);
+  launch_sweep_p(q, dts, false, st, rec + 6 * isz);
+  launch_sweep_r(q, dts, false, st, rec + 7 * isz);
+  launch_finish(q, st);
+  launch_anisch_state(q, st);
+  ctx->launches += 13;
+  CKL("adjoint recomputation");
+  return RAMGPU_OK;
+}
+
 int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
   NvtxRange range_("ramgpu_adj_backward");
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
@@ -2940,28 +3032,28 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
   const int co_e = (d.coef && d.coef_slot[2] >= 0) ? 1 : 0;
   CK(cudaMemsetAsync(d.lam, 0, sizeof(double) * nslot * d.ncell, ctx->stream));
   CK(cudaMemsetAsync(d.gfg, 0, sizeof(double) * nslot * nfg, ctx->stream));
-  for (int seg = a.nseg - 1; seg >= 0; --seg) {
-    const int c0 = seg * a.k, c1 = (c0 + a.k < a.ncalls) ? c0 + a.k : a.ncalls;
-    // The records of the last nkeep segments are still the forward pass's
-    // own (the observation values fm are kept from it for every call);
-    // earlier segments are recomputed from their checkpoint, recording
-    // branches into their ring slot (whose previous segment is done).
-    if (seg < a.nseg - a.nkeep || a.rec_stale) {
-      if ((rc = adj_copy_items(ctx, a.ckpt + (size_t)seg * isz, false))) return rc;
-      for (int c = c0; c < c1; ++c) {
-        if ((rc = adj_set_kp(ctx, c))) return rc;
-        if ((rc = enqueue_call_rec(ctx, a.dts, a.rec + adj_rec_slot(a, c) * a.rec_call, false))) return rc;
-      }
-    }
+  // The records of the last nkeep segments are still the forward pass's
+  // own (the observation values fm are kept from it for every call);
+  // earlier segments are recomputed from their checkpoint, recording
+  // branches into their ring slot (whose previous segment is done).
+  auto needs = [&](int seg) { return seg < a.nseg - a.nkeep || a.rec_stale; };
+  auto calls_of = [&](int seg, int& c0, int& c1) {
+    c0 = seg * a.k;
+    c1 = (c0 + a.k < a.ncalls) ? c0 + a.k : a.ncalls;
+  };
+  auto transpose = [&](int seg) -> int {
+    int c0, c1;
+    calls_of(seg, c0, c1);
     for (int c = c1 - 1; c >= c0; --c) {  // transpose call c
       const unsigned char* rcall = a.rec + adj_rec_slot(a, c) * a.rec_call;
       launch_obs_adj(d, a.obs, a.nobs, c, a.fm, ctx->stream);
-      if ((rc = adj_set_kp(ctx, c))) return rc;
+      int r2 = adj_set_kp(ctx, c);
+      if (r2) return r2;
       launch_member_coef(d, a.dts, ctx->stream);
       launch_ghost(d, ctx->stream);
       ctx->launches += 4;
       // the transposed sweeps of each item group on its own stream
-      rc = over_groups(ctx, G, [&](int i0) {
+      r2 = over_groups(ctx, G, [&](int i0) {
         const Dev& dg = ctx->d;
         const cudaStream_t st = ctx->stream;
         const unsigned char* r = rcall + (size_t)i0 * dg.ncell;
@@ -2979,7 +3071,66 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
         CKL("adjoint backward");
         return RAMGPU_OK;
       });
-      if (rc) return rc;
+      if (r2) return r2;
+    }
+    return RAMGPU_OK;
+  };
+  const bool any_recompute = a.rec_stale || a.nseg > a.nkeep;
+  if (ctx->adj_overlap && any_recompute && a.nkeep >= 2) {
+    // Segment seg - 1 is recomputed on the second stream while segment seg
+    // is transposed: their ring slots differ (nkeep >= 2), the second
+    // stream has its own per-member tables and ghost planes, and the
+    // transposes read neither F2 nor those tables.  Recomputing segment s
+    // waits until the segment that last held its slot (s + nkeep) has been
+    // transposed; transposing s waits until s is recomputed.  An event per
+    // slot suffices: when either wait is enqueued, the slot's latest record
+    // is the one waited for.
+    Dev q;
+    if ((rc = adj_shadow_prepare(ctx, q))) return rc;
+    const cudaStream_t qs = ctx->adj_stream;
+    const int nk = a.nkeep;
+    cudaEvent_t* evR = ctx->adj_events.data();
+    cudaEvent_t* evT = evR + nk;
+    cudaEvent_t evStart = evT[nk], evEnd = evT[nk + 1];
+    CK(cudaEventRecord(evStart, ctx->stream));
+    CK(cudaStreamWaitEvent(qs, evStart, 0));
+    auto recompute = [&](int seg) -> int {
+      if (seg + nk < a.nseg) CK(cudaStreamWaitEvent(qs, evT[seg % nk], 0));
+      const size_t n = d.ncell;
+      for (size_t i = 0; i < ctx->items_h.size(); ++i) {
+        const int slot = ctx->items_h[i].x * d.ns + ctx->items_h[i].y;
+        CK(cudaMemcpyAsync(d.f2 + (size_t)slot * n, a.ckpt + (size_t)seg * isz + i * n, sizeof(double) * n,
+                           cudaMemcpyDeviceToDevice, qs));
+      }
+      int c0, c1;
+      calls_of(seg, c0, c1);
+      for (int c = c0; c < c1; ++c)
+        if (int r2 = adj_recompute_call(ctx, q, qs, c, a.dts, a.rec + adj_rec_slot(a, c) * a.rec_call)) return r2;
+      CK(cudaEventRecord(evR[seg % nk], qs));
+      return RAMGPU_OK;
+    };
+    const int top = a.nseg - 1;
+    if (needs(top) && (rc = recompute(top))) return rc;
+    for (int seg = top; seg >= 0; --seg) {
+      if (seg >= 1 && needs(seg - 1) && (rc = recompute(seg - 1))) return rc;
+      if (needs(seg)) CK(cudaStreamWaitEvent(ctx->stream, evR[seg % nk], 0));
+      if ((rc = transpose(seg))) return rc;
+      CK(cudaEventRecord(evT[seg % nk], ctx->stream));
+    }
+    CK(cudaEventRecord(evEnd, qs));
+    CK(cudaStreamWaitEvent(ctx->stream, evEnd, 0));
+  } else {
+    for (int seg = a.nseg - 1; seg >= 0; --seg) {
+      if (needs(seg)) {
+        if ((rc = adj_copy_items(ctx, a.ckpt + (size_t)seg * isz, false))) return rc;
+        int c0, c1;
+        calls_of(seg, c0, c1);
+        for (int c = c0; c < c1; ++c) {
+          if ((rc = adj_set_kp(ctx, c))) return rc;
+          if ((rc = enqueue_call_rec(ctx, a.dts, a.rec + adj_rec_slot(a, c) * a.rec_call, false))) return rc;
+        }
+      }
+      if ((rc = transpose(seg))) return rc;
     }
   }
   if ((rc = adj_copy_items(ctx, a.ckpt, false))) return rc;  // F2 back to the initial state

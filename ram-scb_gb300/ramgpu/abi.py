@@ -42,7 +42,7 @@ EXPORTS = (
     "ramgpu_set_pipeline_groups", "ramgpu_pipeline_groups",
     "ramgpu_set_step_groups", "ramgpu_step_groups", "ramgpu_set_pipeline_trace", "ramgpu_pipeline_trace",
     "ramgpu_check", "ramgpu_set_check", "ramgpu_last_status",
-    "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_mu_lanes",
+    "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_adj_overlap", "ramgpu_set_mu_lanes",
     "ramgpu_selftest_arith",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
@@ -203,6 +203,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_pipeline_trace": ([vp, ip, C.POINTER(C.c_float)], i),
         "ramgpu_set_adj_record_budget": ([vp, C.c_longlong], i),
         "ramgpu_adj_segments": ([vp, ip, ip], i),
+        "ramgpu_set_adj_overlap": ([vp, i], i),
         "ramgpu_set_mu_lanes": ([vp, i], i),
         "ramgpu_selftest_arith": ([C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)], i),
     }
@@ -723,6 +724,12 @@ class RamGpu:
         the free device memory; small: one segment, every earlier segment is
         recomputed)."""
         self._ck(self.lib.ramgpu_set_adj_record_budget(self.h, int(nbytes)), "set_adj_record_budget")
+
+    def set_adj_overlap(self, on: bool):
+        """Recompute segment s-1 on a second stream while segment s is
+        transposed in adj_backward (default on; the ring then keeps at least
+        two segments)."""
+        self._ck(self.lib.ramgpu_set_adj_overlap(self.h, 1 if on else 0), "set_adj_overlap")
 
     def adj_segments(self):
         """(checkpoint segments, segments whose records are kept) of the last

@@ -174,22 +174,27 @@ def test_gradient_finite_differences_fgeos(case):
               False, 6, (1e-4, 1e-5, 1e-6))
 
 
+@pytest.mark.parametrize("overlap", [False, True])
 @pytest.mark.parametrize("k,keep", [(1, 1), (1, 2), (1, 4), (2, 1), (4, 1)])
-def test_checkpoint_spacing_and_record_budget(case, k, keep):
+def test_checkpoint_spacing_and_record_budget(case, k, keep, overlap):
     """Checkpoints every k calls with a record ring of `keep` segments (the
-    older segments are recomputed from their checkpoints): the same J and
-    gradients as the default (every record kept); records of kept segments
-    are readable, the others are not."""
+    older segments are recomputed from their checkpoints, on a second stream
+    while the next segment is transposed when overlap is on; the ring then
+    keeps at least two): the same J and gradients as the default (every
+    record kept); records of kept segments are readable, the others are
+    not."""
     wl, model, kp, obs, J0, _, gf, gb = case
     g = wl.grid
     ns = len(g.species)
     per_call = 8 * ns * g.nr * g.nt * g.ne * g.npa
     model.set_adj_record_budget(keep * k * per_call)
+    model.set_adj_overlap(overlap)
     try:
         _set_f2(model, wl, [1.0] * ns)
         J1 = model.adj_forward(NCALLS, wl.dts, kp, k, obs)
         nseg, nkeep = model.adj_segments()
-        assert nseg == -(-NCALLS // k) and nkeep == min(keep, nseg)
+        least = 2 if overlap and nseg > 1 else 1
+        assert nseg == -(-NCALLS // k) and nkeep == min(max(keep, least), nseg)
         for c in range(NCALLS):
             if c // k >= nseg - nkeep:
                 assert model.adj_record(c, ns).size > 0
@@ -212,6 +217,7 @@ def test_checkpoint_spacing_and_record_budget(case, k, keep):
             assert np.max(np.abs(gb2 - gb1)) <= 1e-13 * np.max(np.abs(gb1))
     finally:
         model.set_adj_record_budget(-1)
+        model.set_adj_overlap(True)
 
 
 @pytest.mark.parametrize("groups", [1, 2, 3])
