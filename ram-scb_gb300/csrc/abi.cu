@@ -97,6 +97,7 @@ struct ramgpu_ctx {
     double dts = 0.0;
     long long items_version = -1;
     std::vector<double> kp;          // ncalls * nm
+    std::vector<int> obs_calls;      // observations per call
     double* kp_d = nullptr;          // the same on the device (copied per call device-to-device)
     ObsDev* obs = nullptr;
     double *fm = nullptr, *fm2 = nullptr, *J = nullptr, *J2 = nullptr, *ckpt = nullptr;
@@ -118,6 +119,8 @@ struct ramgpu_ctx {
   bool adj_overlap = true;
   cudaStream_t adj_stream = nullptr;
   void* adj_shadow = nullptr;
+  double* adj_shadow_coef = nullptr;  // the second stream's DRIFTE coefficient store
+  size_t adj_shadow_coef_bytes = 0;
   std::vector<cudaEvent_t> adj_events;
   // ramgpu_ram_run_host: item groups, their streams and events, and the
   // graph of the whole pipeline for one set of host buffers
@@ -1111,6 +1114,7 @@ int ramgpu_destroy(ramgpu_ctx* ctx) {
   for (cudaEvent_t e : ctx->adj_events) cudaEventDestroy(e);
   if (ctx->adj_stream) cudaStreamDestroy(ctx->adj_stream);
   cudaFree(ctx->adj_shadow);
+  cudaFree(ctx->adj_shadow_coef);
   if (ctx->status_h) cudaFreeHost(ctx->status_h);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -2872,6 +2876,8 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
   if (!reuse) adj_free(ctx);
   a.ncalls = ncalls; a.k = k_ckpt; a.nseg = nseg; a.nobs = nobs; a.dts = dts;
   a.kp.assign(kp, kp + (size_t)ncalls * nm);
+  a.obs_calls.assign(ncalls, 0);
+  for (int t = 0; t < nobs; ++t) a.obs_calls[obs[t].call] += 1;
   a.items_version = ctx->items_version;
   a.rec_call = rec_call;
   a.nkeep = nkeep;
@@ -2943,17 +2949,18 @@ int ramgpu_set_adj_overlap(ramgpu_ctx* ctx, int on) {
 }
 
 // The second stream, its events (2 per ring slot + 2) and the shadow copies
-// of everything a recorded call writes besides F2 and its record: Kp, the
-// per-member tables CR, CA, DRD1, DPD1, UE, UM and the DRIFTR ghost planes.
-// Returns in q the context's Dev with those pointers replaced and without
-// the coefficient store (the DRIFTE reverse recomputes its coefficients:
-// the same bits) or clip counting.
+// of everything a recorded call writes besides F2 and its record: the
+// per-member tables CR, CA, DRD1, DPD1, UE, UM and the DRIFTR ghost planes,
+// and a coefficient store of its own when the context has one (without it
+// the DRIFTE reverse recomputes its coefficients: the same bits, two FP64
+// operations per cell more).  Returns in q the context's Dev with those
+// pointers replaced and without clip counting.
 static int adj_shadow_prepare(ramgpu_ctx* ctx, Dev& q) {
   const Dev& d = ctx->d;
   const size_t nm = (size_t)d.nm, nij = nm * d.nr * d.nt, nijl = nij * d.npa;
   const size_t npl = nm * d.ns * d.ne * d.npa;
   auto up = [](size_t n) { return (n + 31) / 32 * 32; };  // 256-byte pieces
-  const size_t ndbl = up(nm) + 4 * up(nij) + 2 * up(nijl) + 2 * up(npl);
+  const size_t ndbl = 4 * up(nij) + 2 * up(nijl) + 2 * up(npl);
   const size_t bytes = 8 * ndbl + 4 * 3 * up(npl);
   if (!ctx->adj_shadow && cudaMalloc(&ctx->adj_shadow, bytes) != cudaSuccess) {
     cudaGetLastError();
@@ -2974,7 +2981,6 @@ static int adj_shadow_prepare(ramgpu_ctx* ctx, Dev& q) {
   double* p = (double*)ctx->adj_shadow;
   auto take = [&](size_t n) { double* r = p; p += up(n); return r; };
   q = d;
-  q.kp = take(nm);
   q.cr = take(nij); q.ca = take(nij); q.drd1 = take(nij); q.dpd1 = take(nij);
   q.ue = take(nijl); q.um = take(nijl);
   q.plane_last = take(npl); q.plane_carry = take(npl);
@@ -2983,6 +2989,19 @@ static int adj_shadow_prepare(ramgpu_ctx* ctx, Dev& q) {
   q.plane_last_src = ip; ip += up(npl);
   q.plane_carry_src = ip;
   q.coef = nullptr;
+  if (d.coef) {
+    int nw = 0;
+    for (int w = 0; w < 4; ++w) nw += d.coef_slot[w] >= 0 ? 1 : 0;
+    const size_t need = (size_t)2 * nw * d.coef_items * d.ncell * sizeof(double);
+    if (ctx->adj_shadow_coef_bytes != need) {
+      cudaFree(ctx->adj_shadow_coef);
+      ctx->adj_shadow_coef = nullptr;
+      ctx->adj_shadow_coef_bytes = 0;
+      if (cudaMalloc(&ctx->adj_shadow_coef, need) == cudaSuccess) ctx->adj_shadow_coef_bytes = need;
+      else { ctx->adj_shadow_coef = nullptr; cudaGetLastError(); }
+    }
+    q.coef = ctx->adj_shadow_coef;
+  }
   q.count_clips = 0;
   return RAMGPU_OK;
 }
@@ -2993,17 +3012,18 @@ static int adj_shadow_prepare(ramgpu_ctx* ctx, Dev& q) {
 // sits at its items' place in the list).
 static int adj_recompute_call(ramgpu_ctx* ctx, const Dev& q, cudaStream_t st, int call, double dts,
                               unsigned char* rec) {
-  const int nm = ctx->cfg.n_members;
-  CK(cudaMemcpyAsync(q.kp, ctx->adj.kp_d + (size_t)call * nm, sizeof(double) * nm, cudaMemcpyDeviceToDevice, st));
+  Dev qc = q;  // Kp of the call read from the window's array
+  qc.kp = ctx->adj.kp_d + (size_t)call * ctx->cfg.n_members;
   const size_t isz = (size_t)q.nitems * q.ncell;
-  launch_member_coef(q, dts, st);
+  const int co_e = (q.coef && q.coef_slot[2] >= 0) ? 1 : 0;
+  launch_member_coef(qc, dts, st);
   launch_ghost(q, st);
   launch_sweep_r(q, dts, false, st, rec + 0 * isz);
   launch_sweep_p(q, dts, false, st, rec + 1 * isz);
-  launch_sweep_e(q, dts, false, st, rec + 2 * isz);
+  launch_sweep_e(q, dts, false, st, rec + 2 * isz, false, co_e);
   launch_sweep_mu(q, dts, false, 1, q.loss2, st, rec + 3 * isz);
   launch_sweep_mu(q, dts, false, 0, nullptr, st, rec + 4 * isz);
-  launch_sweep_e(q, dts, false, st, rec + 5 * isz);
+  launch_sweep_e(q, dts, false, st, rec + 5 * isz, false, 2 * co_e);
   launch_sweep_p(q, dts, false, st, rec + 6 * isz);
   launch_sweep_r(q, dts, false, st, rec + 7 * isz);
   launch_finish(q, st);
@@ -3046,14 +3066,18 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
     calls_of(seg, c0, c1);
     for (int c = c1 - 1; c >= c0; --c) {  // transpose call c
       const unsigned char* rcall = a.rec + adj_rec_slot(a, c) * a.rec_call;
-      launch_obs_adj(d, a.obs, a.nobs, c, a.fm, ctx->stream);
-      int r2 = adj_set_kp(ctx, c);
-      if (r2) return r2;
-      launch_member_coef(d, a.dts, ctx->stream);
-      launch_ghost(d, ctx->stream);
-      ctx->launches += 4;
+      if (a.obs_calls[c]) {
+        launch_obs_adj(d, a.obs, a.nobs, c, a.fm, ctx->stream);
+        ctx->launches += 1;
+      }
+      // the per-member tables of call c, Kp read from the window's array
+      Dev dk = d;
+      dk.kp = a.kp_d + (size_t)c * ctx->cfg.n_members;
+      launch_member_coef(dk, a.dts, ctx->stream);
+      launch_ghost(dk, ctx->stream);
+      ctx->launches += 3;
       // the transposed sweeps of each item group on its own stream
-      r2 = over_groups(ctx, G, [&](int i0) {
+      int r2 = over_groups(ctx, G, [&](int i0) {
         const Dev& dg = ctx->d;
         const cudaStream_t st = ctx->stream;
         const unsigned char* r = rcall + (size_t)i0 * dg.ncell;
@@ -3062,12 +3086,11 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
         launch_adj_sweep(dg, 1, r + 6 * isz, st);
         launch_adj_sweep(dg, 2, r + 5 * isz, st, co_e);
         launch_adj_sweep(dg, 3, r + 4 * isz, st);
-        launch_scale_lam(dg, dg.loss2, st);
-        launch_adj_sweep(dg, 3, r + 3 * isz, st);
+        launch_adj_sweep(dg, 3, r + 3 * isz, st, 0, dg.loss2);  // CEX/ATMOL^T fused
         launch_adj_sweep(dg, 2, r + 2 * isz, st, 2 * co_e);
         launch_adj_sweep(dg, 1, r + 1 * isz, st);
         launch_adj_sweep(dg, 0, r + 0 * isz, st);
-        ctx->launches += 11;
+        ctx->launches += 10;
         CKL("adjoint backward");
         return RAMGPU_OK;
       });
@@ -3134,6 +3157,7 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
     }
   }
   if ((rc = adj_copy_items(ctx, a.ckpt, false))) return rc;  // F2 back to the initial state
+  if ((rc = adj_set_kp(ctx, 0))) return rc;                  // and Kp that of its first call
   a.rec_stale = a.nseg > a.nkeep;  // recomputed segments replaced kept ones
   CK(cudaStreamSynchronize(ctx->stream));
   if (grad_f2) CK(cudaMemcpy(grad_f2, d.lam, sizeof(double) * nslot * d.ncell, cudaMemcpyDefault));

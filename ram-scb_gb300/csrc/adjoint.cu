@@ -59,6 +59,87 @@ __device__ __forceinline__ void face_acc(double FBb, bool neg, int cs, double ak
   c2 = p == 2 ? t1 : c2;
 }
 
+// ---- the face weights on the integer pipe
+// The transposed sweeps are bound by the FP64 unit with three quarters of
+// their issue slots free (one FP64 warp instruction holds its pipe about as
+// long as 65 issue slots), so the two FP64 operations per face that form
+// the weights of face_acc, ak = k*a and m = 1 - sak, can move to integer
+// instructions where the sweep has the latency to spare (kAdjIntMask).
+// The fixed point is a signed 64-bit integer with 2^52 as 1: it keeps every
+// bit of its input down to 2^-52, so a and m differ from the FP64 fma and
+// add they replace by at most 2^-53 and 2^-52 absolute; they scale FBb in
+// the two accumulations, whose own rounding is of that size.  Courant
+// numbers of 1024 and more, inf and NaN give NaN weights.
+
+// Sweeps (bit w: R, P, E, MU) whose transposes form ak and m on the
+// integer pipe.
+constexpr unsigned kAdjIntMask = 0xAu;
+constexpr bits64 kNaNBits = 0x7FF8000000000000ULL;
+
+// |v| 2^-52 (v < 2^63) as the bits of a double with the given sign.
+__device__ __forceinline__ bits64 fix52_to_bits(bits64 v, bool neg) {
+  const int lz = __clzll((long long)(v | 1ULL));
+  const bits64 r = ((bits64)(1034 - lz) << 52) | (((v << lz) >> 11) & kMantMask);
+  return (neg ? kSignMask : 0ULL) | (v ? r : 0ULL);
+}
+// |x| 2^52 for the bits of a double with |x| < 1024 (lower bits cut).
+__device__ __forceinline__ bits64 bits_to_fix52(bits64 x) {
+  const int e = (int)((x >> 52) & 0x7FF);
+  const bits64 mant = (x & kMantMask) | (e ? kImplicit : 0ULL);
+  const int sh = e - 1023;
+  return sh >= 0 ? (mant << (sh < 10 ? sh : 10)) : (mant >> (-sh < 63 ? -sh : 63));
+}
+// The CORR factor a = s*0.5*(1 - u) (s = -1 for neg) as bits, from the bits
+// ub of the Courant number u >= 0.
+__device__ __forceinline__ bits64 corr_a_fix(bits64 ub, bool neg) {
+  const long long D = (long long)(1ULL << 52) - (long long)bits_to_fix52(ub);  // (1 - u) 2^52
+  const bits64 r = fix52_to_bits((bits64)(D < 0 ? -D : D), neg != (D < 0));
+  const bits64 half = (r << 1) ? r - (1ULL << 52) : r;  // r / 2
+  return (ub >> 52) >= 1033 ? kNaNBits : half;
+}
+// 1 - x for the bits of x (|x| < 1024) as bits.
+__device__ __forceinline__ bits64 one_minus_bits(bits64 x) {
+  const bits64 X = bits_to_fix52(x);
+  const long long M = (x >> 63) ? (long long)((1ULL << 52) + X) : (long long)(1ULL << 52) - (long long)X;
+  const bits64 r = fix52_to_bits((bits64)(M < 0 ? -M : M), M < 0);
+  return ((x >> 52) & 0x7FF) >= 1033 ? kNaNBits : r;
+}
+// face_acc with ak = k*a from the CORR factor a (bits; k = beta for cases
+// 1, 4 by babs_bits) and m = 1 - sak, both on the integer pipe.
+__device__ __forceinline__ void face_acc_a(double FBb, bool neg, int cs, bits64 a, const BetaBits& beta,
+                                           double& cm1, double& c0, double& c1, double& c2) {
+  const bool xt = (cs == 2) | (cs == 4);
+  const bool dt = (cs == 1) | (cs == 3);
+  const bool ends = (dt & !neg) | (xt & neg);
+  const bool starts = (xt & !neg) | (dt & neg);
+  const bool kb = (cs == 1) | (cs == 4);
+  const bits64 ak = kb ? ((a & kSignMask) | babs_bits(beta, bitsd(a))) : a;
+  const bits64 sak = ends ? (ak ^ kSignMask) : (starts ? ak : 0ULL);
+  const bits64 m = one_minus_bits(sak);
+  const double b0 = bitsd(ends ? sak : m), b1 = bitsd(ends ? m : sak);
+  const int p = neg ? (ends ? 1 : 2) : (ends ? 0 : 1);
+  const double p0 = p == 0 ? cm1 : (p == 1 ? c0 : c1);
+  const double p1 = p == 0 ? c0 : (p == 1 ? c1 : c2);
+  const double t0 = fma(b0, FBb, p0);
+  const double t1 = fma(b1, FBb, p1);
+  cm1 = p == 0 ? t0 : cm1;
+  c0 = p == 0 ? t1 : (p == 1 ? t0 : c0);
+  c1 = p == 1 ? t1 : (p == 2 ? t0 : c1);
+  c2 = p == 2 ? t1 : c2;
+}
+// Bits of the Courant number |c|*y (y = 1/DE or 1/DMU, positive normal):
+// the significands' product cut to 53 bits (as mul_pos_bits), 0 for zero,
+// subnormal or underflowing |c|*y, inf when it overflows or c is not finite.
+__device__ __forceinline__ bits64 courant_u(double c, double y) {
+  const bits64 ax = dbits(c) & kAbsMask, uy = dbits(y);
+  const int ex = (int)(ax >> 52);
+  const bits64 p = __umul64hi(((ax & kMantMask) | kImplicit) << 11, ((uy & kMantMask) | kImplicit) << 11);
+  const int hi = (int)(p >> 63);
+  const int e = ex + (int)(uy >> 52) - 1023 + hi;
+  const bits64 r = ((bits64)e << 52) | ((p >> (10 + hi)) & kMantMask);
+  return (ex == 0x7FF || e >= 0x7FF) ? 0x7FF0000000000000ULL : ((ax < kImplicit || e <= 0) ? 0ULL : r);
+}
+
 // ak = LIMITER weight times the CORR factor a = -0.5*(C*q - s) of a face:
 // fma(C, -0.5*k*q, 0.5*k*s) with k = beta for cases 1, 4 and 1 otherwise
 // (q = 1 for R and P; -0.5*q comes from the -0.5/DE, -0.5/DMU tables).
@@ -127,6 +208,7 @@ __global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __
     const double* __restrict__ cr = d.cr + ((long long)m * nt + j) * nr;
     const double p4 = d.p4[s * ne + k];
     const double hb = 0.5 * d.betalim, bmh = -hb;
+    const BetaBits beta(d.betalim);
     const bool closed = d.flags & 1u;
     const int n = nr;  // >= 4
     const double cN = fma(grt[n - 1], p4, cr[n - 1]);
@@ -138,7 +220,10 @@ __global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __
     auto face = [&](int f, double C) {
       const bool neg = is_neg(C);
       const int cs = rl[f - 1] & 7;
-      face_acc(C * (le1 - le0), neg, cs, face_ak<false>(C, neg, cs, -0.5, bmh, hb), cm1, c0, c1, c2);
+      if (kAdjIntMask & 1u)
+        face_acc_a(C * (le1 - le0), neg, cs, corr_a_fix(dbits(C) & kAbsMask, neg), beta, cm1, c0, c1, c2);
+      else
+        face_acc(C * (le1 - le0), neg, cs, face_ak<false>(C, neg, cs, -0.5, bmh, hb), cm1, c0, c1, c2);
     };
     auto advance = [&](int f, double le3) {  // cell f-1 is final; cell f+3 enters
       lam[f - 2] = cm1;
@@ -205,6 +290,7 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
     const double* __restrict__ ca = d.ca + ((long long)m * nt) * nr + i;
     const double p2 = d.p2[((long long)s * ne + k) * nr + i];
     const double hb = 0.5 * d.betalim, bmh = -hb;
+    const BetaBits beta(d.betalim);
     const int n = nt;
 #define PC(J) fma(gpt[(long long)((J)-1) * nr], p2, ca[(long long)((J)-1) * nr])
 #define PLE(J) masked(lam, rl, (long long)((J)-1) * st)
@@ -242,7 +328,10 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
       const double C = PC(J);
       const bool neg = is_neg(C);
       const int cs = rl[(long long)(J - 1) * st] & 7;
-      face_acc(C * (le1 - le0), neg, cs, face_ak<false>(C, neg, cs, -0.5, bmh, hb), cm1, c0, c1, c2);
+      if (kAdjIntMask & 2u)
+        face_acc_a(C * (le1 - le0), neg, cs, corr_a_fix(dbits(C) & kAbsMask, neg), beta, cm1, c0, c1, c2);
+      else
+        face_acc(C * (le1 - le0), neg, cs, face_ak<false>(C, neg, cs, -0.5, bmh, hb), cm1, c0, c1, c2);
       lam[(long long)(J - 2) * st] = cm1;
       cm1 = c0; c0 = c1; c1 = c2; c2 = add;
       le0 = le1; le1 = lnext; lnext = lec;
@@ -289,12 +378,14 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
     double* __restrict__ lam = d.lam + (long long)slot * d.ncell + base;
     const unsigned char* __restrict__ rl = rec + (u / bpi) * d.ncell + base;
     double* __restrict__ cst = kCo ? coef_ptr(d, 2, 0, u / bpi) + base : nullptr;
+    double* __restrict__ csa = kCo ? coef_ptr(d, 2, 1, u / bpi) + base : nullptr;
     const long long fij = ((long long)l * nt + j) * nr + i;
     const double wet = d.wet[fij];
     const double ue = d.ue[(long long)m * nr * nt * d.npa + fij];
     const double* __restrict__ edot = d.edot + (long long)s * ne * nr + i;
     const double* __restrict__ eb = d.eb + s * ne;
     const double hb = 0.5 * d.betalim;
+    const BetaBits beta(d.betalim);
     const bool closed = d.flags & 1u;
     const int n = ne;
 #define EC(K) (edot[(long long)((K)-1) * nr] * fma(eb[(K)-1], wet, ue))
@@ -309,8 +400,16 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
       if (kCo == 1) cst[(long long)(K - 1) * st] = C;
       const bool neg = is_neg(C);
       const int cs = rl[(long long)(K - 1) * st] & 7;
-      face_acc(C * (wl1 - wl0), neg, cs, face_ak<true>(C, neg, cs, d.mhde[K - 1], d.bmhde[K - 1], hb), cm1, c0,
-               c1, c2);
+      if (kAdjIntMask & 4u) {
+        // the CORR factor a too goes to the store (case-free: each transpose
+        // applies its own record's k)
+        const bits64 a = (kCo == 2) ? dbits(csa[(long long)(K - 1) * st]) : corr_a_fix(courant_u(C, d.ide[K - 1]), neg);
+        if (kCo == 1) csa[(long long)(K - 1) * st] = bitsd(a);
+        face_acc_a(C * (wl1 - wl0), neg, cs, a, beta, cm1, c0, c1, c2);
+      } else {
+        face_acc(C * (wl1 - wl0), neg, cs, face_ak<true>(C, neg, cs, d.mhde[K - 1], d.bmhde[K - 1], hb), cm1, c0,
+                 c1, c2);
+      }
     };
     auto shift = [&](double lec, double wl) {
       cm1 = c0; c0 = c1; c1 = c2; c2 = lec;
@@ -350,7 +449,12 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
 // Cells 1..NPA: G(1) = F(2); faces 2..NPA-2; FBND(NPA-1) = F(NPA) (0 when
 // closed); cells 2..NPA-1 updated; then F2(NPA) = F2new(NPA-1)*rho
 // (NPA >= 9).
-__global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __restrict__ rec) {
+// loss (may be null): the CEX/ATMOL factor table the forward sweep applied
+// to its result (cells L >= 2 of its lines; the table is 1 elsewhere), so
+// lambda is scaled by it as it is read, the transposed loss fused in.
+template <bool kLoss>
+__global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __restrict__ rec,
+                                                const double* __restrict__ loss) {
   const int nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa;
   const int nlines = (nr - 1) * nt * ne;
   WORK_LOOP(nlines) {
@@ -371,14 +475,23 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
     const double* __restrict__ um = d.um + (long long)m * nt * nr * npa + fij;
     const double ekv = d.ek[s * ne + jk / nt];
     const double hb = 0.5 * d.betalim;
+    const BetaBits beta(d.betalim);
     const bool closed = d.flags & 1u;
     const int n = npa;
 #define MC(L) fma(ekv, wm[(long long)((L)-1) * sij], um[(long long)((L)-1) * sij])
-#define MLE(L) masked(lam, rl, (long long)((L)-1) * st)
+    const double* __restrict__ ls = kLoss ? loss + (long long)s * d.ncell + off : nullptr;
+    auto lv = [&](int L) {  // lambda of cell L (>= 2), scaled by the loss factor
+      const double v = lam[(long long)(L - 1) * st];
+      return kLoss ? v * ls[(long long)(L - 1) * st] : v;
+    };
+    auto mle = [&](int L) {  // masked as in masked(): both loads issued unconditionally
+      const double v = lv(L);
+      return (__ldg(rl + (long long)(L - 1) * st) & kClipBit) ? 0.0 : v;
+    };
+#define MLE(L) mle(L)
     const double out1 = lam[0];
     // le(NPA-1) takes rho * lambda(NPA) (F2(NPA) = F2new(NPA-1)*rho)
-    const double leNm = (rl[(long long)(n - 2) * st] & kClipBit)
-                            ? 0.0 : fma(d.rho[fij], lam[(long long)(n - 1) * st], lam[(long long)(n - 2) * st]);
+    const double leNm = (rl[(long long)(n - 2) * st] & kClipBit) ? 0.0 : fma(d.rho[fij], lv(n), lv(n - 1));
     const double le2 = MLE(2), le3 = MLE(3), le4 = MLE(4);
     double wl0 = le2 * d.iwmu[1], wl1 = le3 * d.iwmu[2], wl2 = le4 * d.iwmu[3];
     double cm1 = 0.0, c0 = le2, c1 = le3, c2 = le4;
@@ -386,8 +499,11 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
       const double C = MC(L);
       const bool neg = is_neg(C);
       const int cs = rl[(long long)(L - 1) * st] & 7;
-      face_acc(C * (wl1 - wl0), neg, cs, face_ak<true>(C, neg, cs, d.mhdmu[L - 1], d.bmhdmu[L - 1], hb), cm1,
-               c0, c1, c2);
+      if (kAdjIntMask & 8u)
+        face_acc_a(C * (wl1 - wl0), neg, cs, corr_a_fix(courant_u(C, d.idmu[L - 1]), neg), beta, cm1, c0, c1, c2);
+      else
+        face_acc(C * (wl1 - wl0), neg, cs, face_ak<true>(C, neg, cs, d.mhdmu[L - 1], d.bmhdmu[L - 1], hb), cm1,
+                 c0, c1, c2);
     };
     auto shift = [&](double lec, double wl) {
       cm1 = c0; c0 = c1; c1 = c2; c2 = lec;
@@ -425,7 +541,7 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
   }
 }
 
-void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_t st, int co) {
+void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_t st, int co, const double* loss) {
   const int blk = 128;
   int nl;
   switch (w) {
@@ -446,7 +562,10 @@ void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_
       else if (co == 2) k_adj_e<2><<<g, blk, 0, st>>>(d, rec);
       else k_adj_e<0><<<g, blk, 0, st>>>(d, rec);
       break;
-    default: k_adj_mu<<<g, blk, 0, st>>>(d, rec); break;
+    default:
+      if (loss) k_adj_mu<true><<<g, blk, 0, st>>>(d, rec, loss);
+      else k_adj_mu<false><<<g, blk, 0, st>>>(d, rec, nullptr);
+      break;
   }
 }
 

@@ -82,7 +82,8 @@ struct ObsDev {
 };
 // co (DRIFTE only): 0 compute C, 1 compute and store it, 2 load it (needs
 // the DRIFTE coefficient store).
-void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_t st, int co = 0);
+void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_t st, int co = 0,
+                      const double* loss = nullptr);
 void launch_adj_tail(const Dev& d, cudaStream_t st);
 void launch_scale_lam(const Dev& d, const double* table, cudaStream_t st);
 void launch_obs_fwd(const Dev& d, const ObsDev* obs, int nobs, int call, double* fm, double* J,
