@@ -880,7 +880,7 @@ def run_adjoint(args, torch, np, abi, W, stream):
                                                "transposed, on the same streams")},
            "records_kept": {"segments_kept": nkeep, "adj_forward_s": tfk, "adj_backward_s": tbk,
                             "adjoint_over_forward": (tfk + tbk) / fwd_s,
-                            "record_bytes": 8 * g.ncell * ns * nc,
+                            "record_bytes": 4 * g.ncell * ns * nc,
                             "policy": "the ring keeps as many segments as half of the free HBM holds: none recomputed"},
            "gradient_recompute_vs_kept_max_rel_diff": same_r,
            "single_segment_gradient_max_rel_diff": same,

@@ -466,11 +466,10 @@ typedef struct {
  * J[n_members] and leaves F2 at the end of the window (the moments are
  * those of the window's last call).  The calls of the last nkeep checkpoint
  * segments record every limiter branch and clip into a ring of branch
- * records (8 bytes per cell, item and call) that holds as many segments as
- * the record budget allows (ramgpu_set_adj_record_budget; at least one,
- * two when the window has several segments and the overlapped
- * recomputation is on);
- * the earlier calls, which ramgpu_adj_backward recomputes from their
+ * records (4 bits per face and sweep: 4 bytes per cell, item and call) that
+ * holds as many segments as the record budget allows
+ * (ramgpu_set_adj_record_budget; at least one, two when the window has
+ * several segments and the overlapped recomputation is on); the earlier calls, which ramgpu_adj_backward recomputes from their
  * checkpoints, run the plain step (the same F2 bits).  ramgpu_adj_digest
  * returns a digest of the recorded pattern.  The checkpoint buffer and the
  * ring are allocated by the first window and reused by later windows of the
@@ -512,8 +511,9 @@ int ramgpu_adj_digest(ramgpu_ctx *ctx, unsigned long long *digest);
  * the last ramgpu_adj_forward: 8 sweeps (R,P,E,MU,MU,E,P,R) x active items x
  * NR*NT*NE*NPA bytes, per face the limiter case (bits 0-2: 0 upwind only,
  * 1 beta*D, 2 X, 3 D, 4 beta*X) and bit 3 set when the updated cell was
- * clipped (diagnostics).  Available until a ramgpu_adj_backward that had to
- * recompute earlier segments replaces it. */
+ * clipped (diagnostics; the device keeps four bits per face, the forward
+ * and reverse sweeps of one direction sharing a byte).  Available until a
+ * ramgpu_adj_backward that had to recompute earlier segments replaces it. */
 int ramgpu_adj_record(ramgpu_ctx *ctx, int call, unsigned char *out);
 /* The last window run again from the current F2 with every limiter branch
  * and clip taken from the record (the frozen-limiter scheme that

@@ -103,7 +103,7 @@ struct ramgpu_ctx {
     double *fm = nullptr, *fm2 = nullptr, *J = nullptr, *J2 = nullptr, *ckpt = nullptr;
     unsigned char* rec = nullptr;
     unsigned long long* digest = nullptr;
-    size_t rec_call = 0;             // bytes of one call's record (8 sweeps)
+    size_t rec_call = 0;             // bytes of one call's record (8 sweeps, 4 bits per face)
     bool rec_stale = false;          // the record ring no longer holds the kept segments
     int nkeep = 1;                   // trailing segments whose records the ring keeps
   } adj;
@@ -120,6 +120,8 @@ struct ramgpu_ctx {
   cudaStream_t adj_stream = nullptr;
   void* adj_shadow = nullptr;
   double* adj_shadow_coef = nullptr;  // the second stream's DRIFTE coefficient store
+  void* adj_ring = nullptr;           // the transposes' per-call table sets
+  std::vector<cudaEvent_t> adj_ring_events;
   size_t adj_shadow_coef_bytes = 0;
   std::vector<cudaEvent_t> adj_events;
   // ramgpu_ram_run_host: item groups, their streams and events, and the
@@ -583,14 +585,14 @@ static int enqueue_call_rec(ramgpu_ctx* ctx, double dts, unsigned char* rec, boo
     const Dev& d = ctx->d;
     const cudaStream_t st = ctx->stream;
     unsigned char* r = rec + (size_t)i0 * d.ncell;
-    launch_sweep_r(d, dts, false, st, r + 0 * isz);
-    launch_sweep_p(d, dts, false, st, r + 1 * isz);
-    launch_sweep_e(d, dts, false, st, r + 2 * isz, false, co_e);
-    launch_sweep_mu(d, dts, false, 1, d.loss2, st, r + 3 * isz);
-    launch_sweep_mu(d, dts, false, 0, nullptr, st, r + 4 * isz);
-    launch_sweep_e(d, dts, false, st, r + 5 * isz, false, 2 * co_e);
-    launch_sweep_p(d, dts, false, st, r + 6 * isz);
-    launch_sweep_r(d, dts, false, st, r + 7 * isz);
+    launch_sweep_r(d, dts, false, st, r + 0 * isz, false, 0, 0);
+    launch_sweep_p(d, dts, false, st, r + 1 * isz, false, 0, 0);
+    launch_sweep_e(d, dts, false, st, r + 2 * isz, false, co_e, 0);
+    launch_sweep_mu(d, dts, false, 1, d.loss2, st, r + 3 * isz, false, 0, 0);
+    launch_sweep_mu(d, dts, false, 0, nullptr, st, r + 3 * isz, false, 0, 4);
+    launch_sweep_e(d, dts, false, st, r + 2 * isz, false, 2 * co_e, 4);
+    launch_sweep_p(d, dts, false, st, r + 1 * isz, false, 0, 4);
+    launch_sweep_r(d, dts, false, st, r + 0 * isz, false, 0, 4);
     launch_finish(d, st);
     if (moments) launch_moments(d, st);
     else launch_anisch_state(d, st);
@@ -613,14 +615,14 @@ static int enqueue_call_replay(ramgpu_ctx* ctx, double dts, unsigned char* rec) 
     const Dev& d = ctx->d;
     const cudaStream_t st = ctx->stream;
     unsigned char* r = rec + (size_t)i0 * d.ncell;
-    launch_sweep_r(d, dts, false, st, r + 0 * isz, true);
-    launch_sweep_p(d, dts, false, st, r + 1 * isz, true);
-    launch_sweep_e(d, dts, false, st, r + 2 * isz, true);
-    launch_sweep_mu(d, dts, false, 1, d.loss2, st, r + 3 * isz, true);
-    launch_sweep_mu(d, dts, false, 0, nullptr, st, r + 4 * isz, true);
-    launch_sweep_e(d, dts, false, st, r + 5 * isz, true);
-    launch_sweep_p(d, dts, false, st, r + 6 * isz, true);
-    launch_sweep_r(d, dts, false, st, r + 7 * isz, true);
+    launch_sweep_r(d, dts, false, st, r + 0 * isz, true, 0, 0);
+    launch_sweep_p(d, dts, false, st, r + 1 * isz, true, 0, 0);
+    launch_sweep_e(d, dts, false, st, r + 2 * isz, true, 0, 0);
+    launch_sweep_mu(d, dts, false, 1, d.loss2, st, r + 3 * isz, true, 0, 0);
+    launch_sweep_mu(d, dts, false, 0, nullptr, st, r + 3 * isz, true, 0, 4);
+    launch_sweep_e(d, dts, false, st, r + 2 * isz, true, 0, 4);
+    launch_sweep_p(d, dts, false, st, r + 1 * isz, true, 0, 4);
+    launch_sweep_r(d, dts, false, st, r + 0 * isz, true, 0, 4);
     launch_finish(d, st);
     launch_anisch_state(d, st);
     ctx->launches += 10;
@@ -1115,6 +1117,8 @@ int ramgpu_destroy(ramgpu_ctx* ctx) {
   if (ctx->adj_stream) cudaStreamDestroy(ctx->adj_stream);
   cudaFree(ctx->adj_shadow);
   cudaFree(ctx->adj_shadow_coef);
+  cudaFree(ctx->adj_ring);
+  for (cudaEvent_t e : ctx->adj_ring_events) cudaEventDestroy(e);
   if (ctx->status_h) cudaFreeHost(ctx->status_h);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -2844,13 +2848,16 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
     if (!found) return fail(ctx, RAMGPU_ERR_ARG, "observation of an inactive (member, species)");
     ObsDev& q = oh[t];
     q.member = o.member; q.slot = o.member * d.ns + o.s; q.call = o.call; q.k = o.k; q.l = o.l;
+    q.item = 0;
+    for (size_t it = 0; it < ctx->items_h.size(); ++it)
+      if (ctx->items_h[it].x == o.member && ctx->items_h[it].y == o.s) q.item = (int)it;
     q.log_obs = o.log_obs;
     equatorial_stencil(d, lz, phi, o.lshell, o.mlt, &q.i0, &q.wi, &q.j0, &q.j1, &q.wj);
   }
   auto& a = ctx->adj;
   a.ready = false;
   const int nseg = (ncalls + k_ckpt - 1) / k_ckpt;
-  const size_t rec_call = (size_t)8 * d.nitems * d.ncell;
+  const size_t rec_call = (size_t)4 * d.nitems * d.ncell;
   const int kseg = k_ckpt < ncalls ? k_ckpt : ncalls;
   // The ring keeps the records of the last nkeep segments, as many as the
   // budget allows (at least one, two with the overlapped recomputation:
@@ -2930,8 +2937,10 @@ int ramgpu_adj_forward(ramgpu_ctx* ctx, int ncalls, double dts, const double* kp
       launch_digest(r, (long long)a.rec_call, a.digest, ctx->stream);
       ctx->launches += 1;
     }
-    launch_obs_fwd(d, a.obs, nobs, c, a.fm, a.J, ctx->stream);
-    ctx->launches += 1;
+    if (a.obs_calls[c]) {  // calls with observations only
+      launch_obs_fwd(d, a.obs, nobs, c, a.fm, a.J, ctx->stream);
+      ctx->launches += 1;
+    }
     CKL("adjoint forward");
   }
   CK(cudaStreamSynchronize(ctx->stream));
@@ -2955,14 +2964,33 @@ int ramgpu_set_adj_overlap(ramgpu_ctx* ctx, int on) {
 // the DRIFTE reverse recomputes its coefficients: the same bits, two FP64
 // operations per cell more).  Returns in q the context's Dev with those
 // pointers replaced and without clip counting.
-static int adj_shadow_prepare(ramgpu_ctx* ctx, Dev& q) {
-  const Dev& d = ctx->d;
+// One set of the tables a call writes besides F2: per member CR, CA, DRD1,
+// DPD1, UE, UM, per slot the DRIFTR ghost planes (256-byte pieces).
+static size_t table_set_bytes(const Dev& d) {
   const size_t nm = (size_t)d.nm, nij = nm * d.nr * d.nt, nijl = nij * d.npa;
   const size_t npl = nm * d.ns * d.ne * d.npa;
-  auto up = [](size_t n) { return (n + 31) / 32 * 32; };  // 256-byte pieces
-  const size_t ndbl = 4 * up(nij) + 2 * up(nijl) + 2 * up(npl);
-  const size_t bytes = 8 * ndbl + 4 * 3 * up(npl);
-  if (!ctx->adj_shadow && cudaMalloc(&ctx->adj_shadow, bytes) != cudaSuccess) {
+  auto up = [](size_t n) { return (n + 31) / 32 * 32; };
+  return 8 * (4 * up(nij) + 2 * up(nijl) + 2 * up(npl)) + 4 * 3 * up(npl);
+}
+// q's table pointers into the set at base.
+static void table_set_assign(void* base, Dev& q) {
+  const size_t nm = (size_t)q.nm, nij = nm * q.nr * q.nt, nijl = nij * q.npa;
+  const size_t npl = nm * q.ns * q.ne * q.npa;
+  auto up = [](size_t n) { return (n + 31) / 32 * 32; };
+  double* p = (double*)base;
+  auto take = [&](size_t n) { double* r = p; p += up(n); return r; };
+  q.cr = take(nij); q.ca = take(nij); q.drd1 = take(nij); q.dpd1 = take(nij);
+  q.ue = take(nijl); q.um = take(nijl);
+  q.plane_last = take(npl); q.plane_carry = take(npl);
+  int* ip = (int*)p;
+  q.plane_has = ip; ip += up(npl);
+  q.plane_last_src = ip; ip += up(npl);
+  q.plane_carry_src = ip;
+}
+
+static int adj_shadow_prepare(ramgpu_ctx* ctx, Dev& q) {
+  const Dev& d = ctx->d;
+  if (!ctx->adj_shadow && cudaMalloc(&ctx->adj_shadow, table_set_bytes(d)) != cudaSuccess) {
     cudaGetLastError();
     ctx->adj_shadow = nullptr;
     return fail(ctx, RAMGPU_ERR_NOMEM, "adjoint recomputation tables: device allocation failed");
@@ -2978,16 +3006,8 @@ static int adj_shadow_prepare(ramgpu_ctx* ctx, Dev& q) {
     CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     ctx->adj_events.push_back(e);
   }
-  double* p = (double*)ctx->adj_shadow;
-  auto take = [&](size_t n) { double* r = p; p += up(n); return r; };
   q = d;
-  q.cr = take(nij); q.ca = take(nij); q.drd1 = take(nij); q.dpd1 = take(nij);
-  q.ue = take(nijl); q.um = take(nijl);
-  q.plane_last = take(npl); q.plane_carry = take(npl);
-  int* ip = (int*)p;
-  q.plane_has = ip; ip += up(npl);
-  q.plane_last_src = ip; ip += up(npl);
-  q.plane_carry_src = ip;
+  table_set_assign(ctx->adj_shadow, q);
   q.coef = nullptr;
   if (d.coef) {
     int nw = 0;
@@ -3006,6 +3026,28 @@ static int adj_shadow_prepare(ramgpu_ctx* ctx, Dev& q) {
   return RAMGPU_OK;
 }
 
+// The transposes' ring of kAdjTableRing table sets (per call: the tables of
+// call c sit in set c mod kAdjTableRing) and its events: per set "tables
+// written" and, per item group, "group done with them", then the fork.
+constexpr int kAdjTableRing = 3;
+static int adj_ring_prepare(ramgpu_ctx* ctx, int G) {
+  const size_t per = table_set_bytes(ctx->d);
+  if (!ctx->adj_ring) {
+    if (cudaMalloc(&ctx->adj_ring, per * kAdjTableRing) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->adj_ring = nullptr;
+      return fail(ctx, RAMGPU_ERR_NOMEM, "adjoint table ring: device allocation failed");
+    }
+  }
+  const size_t nev = (size_t)kAdjTableRing * (1 + G) + 1;
+  while (ctx->adj_ring_events.size() < nev) {
+    cudaEvent_t e = nullptr;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ctx->adj_ring_events.push_back(e);
+  }
+  return RAMGPU_OK;
+}
+
 // Call `call` of the window recomputed on stream st with the shadow tables
 // q, every sweep recording into rec: the sequence of enqueue_call_rec over
 // the whole work list as one group (the same records: a group's record
@@ -3018,14 +3060,14 @@ static int adj_recompute_call(ramgpu_ctx* ctx, const Dev& q, cudaStream_t st, in
   const int co_e = (q.coef && q.coef_slot[2] >= 0) ? 1 : 0;
   launch_member_coef(qc, dts, st);
   launch_ghost(q, st);
-  launch_sweep_r(q, dts, false, st, rec + 0 * isz);
-  launch_sweep_p(q, dts, false, st, rec + 1 * isz);
-  launch_sweep_e(q, dts, false, st, rec + 2 * isz, false, co_e);
-  launch_sweep_mu(q, dts, false, 1, q.loss2, st, rec + 3 * isz);
-  launch_sweep_mu(q, dts, false, 0, nullptr, st, rec + 4 * isz);
-  launch_sweep_e(q, dts, false, st, rec + 5 * isz, false, 2 * co_e);
-  launch_sweep_p(q, dts, false, st, rec + 6 * isz);
-  launch_sweep_r(q, dts, false, st, rec + 7 * isz);
+  launch_sweep_r(q, dts, false, st, rec + 0 * isz, false, 0, 0);
+  launch_sweep_p(q, dts, false, st, rec + 1 * isz, false, 0, 0);
+  launch_sweep_e(q, dts, false, st, rec + 2 * isz, false, co_e, 0);
+  launch_sweep_mu(q, dts, false, 1, q.loss2, st, rec + 3 * isz, false, 0, 0);
+  launch_sweep_mu(q, dts, false, 0, nullptr, st, rec + 3 * isz, false, 0, 4);
+  launch_sweep_e(q, dts, false, st, rec + 2 * isz, false, 2 * co_e, 4);
+  launch_sweep_p(q, dts, false, st, rec + 1 * isz, false, 0, 4);
+  launch_sweep_r(q, dts, false, st, rec + 0 * isz, false, 0, 4);
   launch_finish(q, st);
   launch_anisch_state(q, st);
   ctx->launches += 13;
@@ -3061,41 +3103,70 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
     c0 = seg * a.k;
     c1 = (c0 + a.k < a.ncalls) ? c0 + a.k : a.ncalls;
   };
+  // The transposes of a segment: call c's per-member tables go into table
+  // set c mod kAdjTableRing on the context's stream, and each item group
+  // streams through the segment's calls on its own stream, waiting only for
+  // its call's tables; the table set is rewritten once every group is done
+  // with it.  No join between calls: one group's launch tails and the gaps
+  // between its dependent launches are filled by the others.
+  if ((rc = adj_ring_prepare(ctx, G))) return rc;
+  const size_t tset = table_set_bytes(d);
   auto transpose = [&](int seg) -> int {
     int c0, c1;
     calls_of(seg, c0, c1);
+    const cudaStream_t main = ctx->stream;
+    const Dev full = ctx->d;
+    const int T = kAdjTableRing;
+    cudaEvent_t* evTab = ctx->adj_ring_events.data();
+    cudaEvent_t* evUse = evTab + T;  // [g * T + set]
+    cudaEvent_t evFork = evTab[T * (1 + G)];
+    auto gstream = [&](int g) { return G > 1 ? ctx->pipe_streams[g] : main; };
+    if (G > 1) {
+      CK(cudaEventRecord(evFork, main));
+      for (int g = 0; g < G; ++g) CK(cudaStreamWaitEvent(gstream(g), evFork, 0));
+    }
     for (int c = c1 - 1; c >= c0; --c) {  // transpose call c
-      const unsigned char* rcall = a.rec + adj_rec_slot(a, c) * a.rec_call;
-      if (a.obs_calls[c]) {
-        launch_obs_adj(d, a.obs, a.nobs, c, a.fm, ctx->stream);
-        ctx->launches += 1;
-      }
-      // the per-member tables of call c, Kp read from the window's array
-      Dev dk = d;
-      dk.kp = a.kp_d + (size_t)c * ctx->cfg.n_members;
-      launch_member_coef(dk, a.dts, ctx->stream);
-      launch_ghost(dk, ctx->stream);
+      const int sl = c % T;
+      if (G > 1)
+        for (int g = 0; g < G; ++g) CK(cudaStreamWaitEvent(main, evUse[g * T + sl], 0));
+      Dev dk = full;
+      table_set_assign((char*)ctx->adj_ring + tset * sl, dk);
+      dk.kp = a.kp_d + (size_t)c * ctx->cfg.n_members;  // Kp read from the window's array
+      launch_member_coef(dk, a.dts, main);
+      launch_ghost(dk, main);
       ctx->launches += 3;
-      // the transposed sweeps of each item group on its own stream
-      int r2 = over_groups(ctx, G, [&](int i0) {
-        const Dev& dg = ctx->d;
-        const cudaStream_t st = ctx->stream;
+      if (G > 1) CK(cudaEventRecord(evTab[sl], main));
+      const unsigned char* rcall = a.rec + adj_rec_slot(a, c) * a.rec_call;
+      for (int g = 0; g < G; ++g) {
+        const int i0 = (int)((long long)full.nitems * g / G), i1 = (int)((long long)full.nitems * (g + 1) / G);
+        if (i1 <= i0) continue;
+        const cudaStream_t st = gstream(g);
+        if (G > 1) CK(cudaStreamWaitEvent(st, evTab[sl], 0));
+        Dev dg = dk;
+        dg.items = full.items + i0;
+        dg.nitems = i1 - i0;
+        dg.item0 = full.item0 + i0;
+        if (a.obs_calls[c]) {  // the group's observations of call c
+          launch_obs_adj(dg, a.obs, a.nobs, c, a.fm, st);
+          ctx->launches += 1;
+        }
         const unsigned char* r = rcall + (size_t)i0 * dg.ncell;
         launch_adj_tail(dg, st);
-        launch_adj_sweep(dg, 0, r + 7 * isz, st);
-        launch_adj_sweep(dg, 1, r + 6 * isz, st);
-        launch_adj_sweep(dg, 2, r + 5 * isz, st, co_e);
-        launch_adj_sweep(dg, 3, r + 4 * isz, st);
-        launch_adj_sweep(dg, 3, r + 3 * isz, st, 0, dg.loss2);  // CEX/ATMOL^T fused
-        launch_adj_sweep(dg, 2, r + 2 * isz, st, 2 * co_e);
-        launch_adj_sweep(dg, 1, r + 1 * isz, st);
-        launch_adj_sweep(dg, 0, r + 0 * isz, st);
+        launch_adj_sweep(dg, 0, r + 0 * isz, 4, st);
+        launch_adj_sweep(dg, 1, r + 1 * isz, 4, st);
+        launch_adj_sweep(dg, 2, r + 2 * isz, 4, st, co_e);
+        launch_adj_sweep(dg, 3, r + 3 * isz, 4, st);
+        launch_adj_sweep(dg, 3, r + 3 * isz, 0, st, 0, dg.loss2);  // CEX/ATMOL^T fused
+        launch_adj_sweep(dg, 2, r + 2 * isz, 0, st, 2 * co_e);
+        launch_adj_sweep(dg, 1, r + 1 * isz, 0, st);
+        launch_adj_sweep(dg, 0, r + 0 * isz, 0, st);
         ctx->launches += 10;
         CKL("adjoint backward");
-        return RAMGPU_OK;
-      });
-      if (r2) return r2;
+        if (G > 1) CK(cudaEventRecord(evUse[g * T + sl], st));
+      }
     }
+    if (G > 1)  // join: the segment's last call in every group
+      for (int g = 0; g < G; ++g) CK(cudaStreamWaitEvent(main, evUse[g * T + c0 % T], 0));
     return RAMGPU_OK;
   };
   const bool any_recompute = a.rec_stale || a.nseg > a.nkeep;
@@ -3183,8 +3254,10 @@ int ramgpu_adj_replay(ramgpu_ctx* ctx, double* J) {
   for (int c = 0; c < a.ncalls; ++c) {
     if ((rc = adj_set_kp(ctx, c))) return rc;
     if ((rc = enqueue_call_replay(ctx, a.dts, a.rec + adj_rec_slot(a, c) * a.rec_call))) return rc;
-    launch_obs_fwd(d, a.obs, a.nobs, c, a.fm2, a.J2, ctx->stream);
-    ctx->launches += 1;
+    if (a.obs_calls[c]) {
+      launch_obs_fwd(d, a.obs, a.nobs, c, a.fm2, a.J2, ctx->stream);
+      ctx->launches += 1;
+    }
   }
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemcpy(J, a.J2, sizeof(double) * nm, cudaMemcpyDeviceToHost));
@@ -3200,7 +3273,17 @@ int ramgpu_adj_record(ramgpu_ctx* ctx, int call, unsigned char* out) {
   if (a.rec_stale)
     return fail(ctx, RAMGPU_ERR_STATE, "the record was replaced by ramgpu_adj_backward's recomputation");
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaMemcpy(out, a.rec + adj_rec_slot(a, call) * a.rec_call, a.rec_call, cudaMemcpyDeviceToHost));
+  // the device keeps sweeps w and 7-w in the low and high nibbles of one
+  // byte (instance w < 4); unpack into one byte per face and sweep
+  std::vector<unsigned char> packed(a.rec_call);
+  CK(cudaMemcpy(packed.data(), a.rec + adj_rec_slot(a, call) * a.rec_call, a.rec_call, cudaMemcpyDeviceToHost));
+  const size_t isz = a.rec_call / 4;
+  for (int w = 0; w < 8; ++w) {
+    const unsigned char* src = packed.data() + (size_t)(w < 4 ? w : 7 - w) * isz;
+    const int sh = w < 4 ? 0 : 4;
+    unsigned char* dst = out + (size_t)w * isz;
+    for (size_t i = 0; i < isz; ++i) dst[i] = (unsigned char)((src[i] >> sh) & 0x0F);
+  }
   return RAMGPU_OK;
 }
 

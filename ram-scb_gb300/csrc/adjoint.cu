@@ -1,8 +1,10 @@
 // adjoint.cu -- frozen-limiter adjoint of the RAM kinetic step.
 //
 // With the limiter branch of every face and the clip state of every cell
-// frozen (recorded by the forward sweeps, one byte per face: 0 upwind only,
-// 1 beta*D, 2 X, 3 D, 4 beta*X, plus kClipBit), each sweep of
+// frozen (recorded by the forward sweeps, four bits per face: 0 upwind
+// only, 1 beta*D, 2 X, 3 D, 4 beta*X, plus kClipBit; a call's forward and
+// reverse sweeps of one direction share a byte, the reverse one in the high
+// nibble, read here with the shift rsh), each sweep of
 // src/ModRamDrift.f90 is a linear map of its line
 //   Fnew(i) = G(i) + w(i) (Phi(i-1) - Phi(i)),  Phi(f) = C(f) FBND(f),
 //   FBND(f) = FUP(f) + a(f) LX(f),  LX in {beta D, X, D, beta X},
@@ -168,9 +170,9 @@ __device__ __forceinline__ double face_ak(double C, bool neg, int cs, double mh,
 // sector is read again after a write in the same launch.
 template <bool kNc = false>
 __device__ __forceinline__ double masked(const double* __restrict__ lam, const unsigned char* __restrict__ rl,
-                                         long long off) {
+                                         long long off, int rsh) {
   const double v = kNc ? __ldg(lam + off) : lam[off];
-  return (__ldg(rl + off) & kClipBit) ? 0.0 : v;
+  return ((__ldg(rl + off) >> rsh) & kClipBit) ? 0.0 : v;
 }
 
 #define WORK_LOOP(NLINES)                                                          \
@@ -193,7 +195,7 @@ __device__ __forceinline__ double masked(const double* __restrict__ lam, const u
 // Six resident CTAs per SM as the register target: without it the compiler
 // aims at a higher occupancy and spills the window (measured slower).
 template <bool kNc>
-__global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __restrict__ rec) {
+__global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __restrict__ rec, int rsh) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = nt * ne * d.npa;
   WORK_LOOP(nlines) {
@@ -214,12 +216,12 @@ __global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __
     const double cN = fma(grt[n - 1], p4, cr[n - 1]);
     const bool inflow = is_neg(cN);
     // le(i) = lambda of updated, unclipped cell i (i = 2..NR); window = cells f-1..f+2
-    double le0 = masked<kNc>(lam, rl, 1), le1 = masked<kNc>(lam, rl, 2), le2 = masked<kNc>(lam, rl, 3);
+    double le0 = masked<kNc>(lam, rl, 1, rsh), le1 = masked<kNc>(lam, rl, 2, rsh), le2 = masked<kNc>(lam, rl, 3, rsh);
     double cm1 = lam[0], c0 = le0, c1 = le1, c2 = le2;
     if (inflow && !closed) c0 += fma(grt[0], p4, cr[0]) * le0;  // FBND(1) = F(2)
     auto face = [&](int f, double C) {
       const bool neg = is_neg(C);
-      const int cs = rl[f - 1] & 7;
+      const int cs = (rl[f - 1] >> rsh) & 7;
       if (kAdjIntMask & 1u)
         face_acc_a(C * (le1 - le0), neg, cs, corr_a_fix(dbits(C) & kAbsMask, neg), beta, cm1, c0, c1, c2);
       else
@@ -233,7 +235,7 @@ __global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __
     int f = 2;
     for (; f <= n - 3; ++f) {
       face(f, fma(grt[f - 1], p4, cr[f - 1]));
-      advance(f, masked<kNc>(lam, rl, f + 2));
+      advance(f, masked<kNc>(lam, rl, f + 2, rsh));
     }
     for (; f <= n - 1; ++f) {
       face(f, fma(grt[f - 1], p4, cr[f - 1]));
@@ -271,7 +273,7 @@ __global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __
 // J = 2..NT with FBND(1) = FBND(NT).  Faces NT-1 and NT wrap onto cells
 // 1..3; they are transposed first, their contributions held in registers
 // and added when the window reaches those cells (NT >= 7).
-__global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __restrict__ rec) {
+__global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __restrict__ rec, int rsh) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * ne * d.npa;
   WORK_LOOP(nlines) {
@@ -293,16 +295,16 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
     const BetaBits beta(d.betalim);
     const int n = nt;
 #define PC(J) fma(gpt[(long long)((J)-1) * nr], p2, ca[(long long)((J)-1) * nr])
-#define PLE(J) masked(lam, rl, (long long)((J)-1) * st)
+#define PLE(J) masked(lam, rl, (long long)((J)-1) * st, rsh)
     // le(NT) takes lambda of cell 1 too (F2(1) = F2new(NT))
-    const double leN = (rl[(long long)(n - 1) * st] & kClipBit) ? 0.0 : lam[(long long)(n - 1) * st] + lam[0];
+    const double leN = ((rl[(long long)(n - 1) * st] >> rsh) & kClipBit) ? 0.0 : lam[(long long)(n - 1) * st] + lam[0];
     const double leNm = PLE(n - 1), le2 = PLE(2);
     // w1..w3: contributions to cells 1..3, tNm2..tN: to cells NT-2..NT
     double w1 = 0.0, w2 = 0.0, w3 = 0.0, tNm2 = 0.0, tNm1 = 0.0, tN = 0.0;
     {  // face NT-1: X = F(NT)-F(NT-1); D = F(NT-1)-F(NT-2) (s=+1) or F(2)-F(1) (s=-1)
       const double C = PC(n - 1);
       const bool neg = is_neg(C);
-      const int cs = rl[(long long)(n - 2) * st] & 7;
+      const int cs = (rl[(long long)(n - 2) * st] >> rsh) & 7;
       const double FBb = C * (leN - leNm);
       const double V = face_ak<false>(C, neg, cs, -0.5, bmh, hb) * FBb;
       if (neg) tN += FBb; else tNm1 += FBb;
@@ -313,7 +315,7 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
     {  // face NT: X = F(2)-F(NT); D = F(NT)-F(NT-1) (s=+1) or F(3)-F(2) (s=-1)
       const double C = PC(n);
       const bool neg = is_neg(C);
-      const int cs = rl[(long long)(n - 1) * st] & 7;
+      const int cs = (rl[(long long)(n - 1) * st] >> rsh) & 7;
       const double FBb = C * (le2 - leN);  // Pb(NT) = -le(NT) + Pb(1), Pb(1) = le(2)
       const double V = face_ak<false>(C, neg, cs, -0.5, bmh, hb) * FBb;
       if (neg) w2 += FBb; else tN += FBb;
@@ -327,7 +329,7 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
     auto step = [&](int J, double add, double lec) {  // face J, then cell J+3 enters
       const double C = PC(J);
       const bool neg = is_neg(C);
-      const int cs = rl[(long long)(J - 1) * st] & 7;
+      const int cs = (rl[(long long)(J - 1) * st] >> rsh) & 7;
       if (kAdjIntMask & 2u)
         face_acc_a(C * (le1 - le0), neg, cs, corr_a_fix(dbits(C) & kAbsMask, neg), beta, cm1, c0, c1, c2);
       else
@@ -362,7 +364,7 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
 // potential), so the first keeps it for the second, as the forward sweeps
 // do; the stored value is the recomputed one, so the results do not change.
 template <int kCo>
-__global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __restrict__ rec) {
+__global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __restrict__ rec, int rsh) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * nt * d.npa;
   WORK_LOOP(nlines) {
@@ -389,7 +391,7 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
     const bool closed = d.flags & 1u;
     const int n = ne;
 #define EC(K) (edot[(long long)((K)-1) * nr] * fma(eb[(K)-1], wet, ue))
-#define ELE(K) masked(lam, rl, (long long)((K)-1) * st)
+#define ELE(K) masked(lam, rl, (long long)((K)-1) * st, rsh)
     const double out1 = lam[0];
     // wl(K) = le(K)/WE(K) for K = 2..NE, 0 elsewhere; window = cells K-1..K+2
     const double le2 = ELE(2), le3 = ELE(3);
@@ -399,7 +401,7 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
       const double C = (kCo == 2) ? cst[(long long)(K - 1) * st] : EC(K);
       if (kCo == 1) cst[(long long)(K - 1) * st] = C;
       const bool neg = is_neg(C);
-      const int cs = rl[(long long)(K - 1) * st] & 7;
+      const int cs = (rl[(long long)(K - 1) * st] >> rsh) & 7;
       if (kAdjIntMask & 4u) {
         // the CORR factor a too goes to the store (case-free: each transpose
         // applies its own record's k)
@@ -453,7 +455,7 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
 // to its result (cells L >= 2 of its lines; the table is 1 elsewhere), so
 // lambda is scaled by it as it is read, the transposed loss fused in.
 template <bool kLoss>
-__global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __restrict__ rec,
+__global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __restrict__ rec, int rsh,
                                                 const double* __restrict__ loss) {
   const int nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa;
   const int nlines = (nr - 1) * nt * ne;
@@ -486,19 +488,19 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
     };
     auto mle = [&](int L) {  // masked as in masked(): both loads issued unconditionally
       const double v = lv(L);
-      return (__ldg(rl + (long long)(L - 1) * st) & kClipBit) ? 0.0 : v;
+      return ((__ldg(rl + (long long)(L - 1) * st) >> rsh) & kClipBit) ? 0.0 : v;
     };
 #define MLE(L) mle(L)
     const double out1 = lam[0];
     // le(NPA-1) takes rho * lambda(NPA) (F2(NPA) = F2new(NPA-1)*rho)
-    const double leNm = (rl[(long long)(n - 2) * st] & kClipBit) ? 0.0 : fma(d.rho[fij], lv(n), lv(n - 1));
+    const double leNm = ((rl[(long long)(n - 2) * st] >> rsh) & kClipBit) ? 0.0 : fma(d.rho[fij], lv(n), lv(n - 1));
     const double le2 = MLE(2), le3 = MLE(3), le4 = MLE(4);
     double wl0 = le2 * d.iwmu[1], wl1 = le3 * d.iwmu[2], wl2 = le4 * d.iwmu[3];
     double cm1 = 0.0, c0 = le2, c1 = le3, c2 = le4;
     auto face = [&](int L) {
       const double C = MC(L);
       const bool neg = is_neg(C);
-      const int cs = rl[(long long)(L - 1) * st] & 7;
+      const int cs = (rl[(long long)(L - 1) * st] >> rsh) & 7;
       if (kAdjIntMask & 8u)
         face_acc_a(C * (wl1 - wl0), neg, cs, corr_a_fix(courant_u(C, d.idmu[L - 1]), neg), beta, cm1, c0, c1, c2);
       else
@@ -541,7 +543,8 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
   }
 }
 
-void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_t st, int co, const double* loss) {
+void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, int rsh, cudaStream_t st, int co,
+                      const double* loss) {
   const int blk = 128;
   int nl;
   switch (w) {
@@ -553,18 +556,18 @@ void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_
   dim3 g((nl + blk - 1) / blk, d.nitems, 1);
   switch (w) {
     case 0:
-      if (d.nr % 4 == 0) k_adj_r<true><<<g, blk, 0, st>>>(d, rec);
-      else k_adj_r<false><<<g, blk, 0, st>>>(d, rec);
+      if (d.nr % 4 == 0) k_adj_r<true><<<g, blk, 0, st>>>(d, rec, rsh);
+      else k_adj_r<false><<<g, blk, 0, st>>>(d, rec, rsh);
       break;
-    case 1: k_adj_p<<<g, blk, 0, st>>>(d, rec); break;
+    case 1: k_adj_p<<<g, blk, 0, st>>>(d, rec, rsh); break;
     case 2:
-      if (co == 1) k_adj_e<1><<<g, blk, 0, st>>>(d, rec);
-      else if (co == 2) k_adj_e<2><<<g, blk, 0, st>>>(d, rec);
-      else k_adj_e<0><<<g, blk, 0, st>>>(d, rec);
+      if (co == 1) k_adj_e<1><<<g, blk, 0, st>>>(d, rec, rsh);
+      else if (co == 2) k_adj_e<2><<<g, blk, 0, st>>>(d, rec, rsh);
+      else k_adj_e<0><<<g, blk, 0, st>>>(d, rec, rsh);
       break;
     default:
-      if (loss) k_adj_mu<true><<<g, blk, 0, st>>>(d, rec, loss);
-      else k_adj_mu<false><<<g, blk, 0, st>>>(d, rec, nullptr);
+      if (loss) k_adj_mu<true><<<g, blk, 0, st>>>(d, rec, rsh, loss);
+      else k_adj_mu<false><<<g, blk, 0, st>>>(d, rec, rsh, nullptr);
       break;
   }
 }
@@ -659,7 +662,7 @@ __global__ void k_obs_adj(Dev d, const ObsDev* __restrict__ obs, int nobs, int c
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nobs) return;
   const ObsDev o = obs[t];
-  if (o.call != call) return;
+  if (o.call != call || o.item < d.item0 || o.item >= d.item0 + d.nitems) return;  // call c, this group
   const int s = o.slot % d.ns;
   const double v = fm[t];
   const double g = 2.0 * (log(v) - o.log_obs) / v;

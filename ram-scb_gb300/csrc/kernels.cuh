@@ -49,15 +49,17 @@ __device__ __forceinline__ int stale_ghost_src(const Dev& d, int m, int slot, in
 }
 
 // rec: branch record of the sweep, written (replay false) or, with replay
-// true, read back to run the sweep with those branches and clips frozen.
+// true, read back to run the sweep with those branches and clips frozen;
+// rsh: its nibble of the record bytes (0: low, forward half; 4: high,
+// reverse half).
 void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr,
-                    bool replay = false, int co = 0);
+                    bool replay = false, int co = 0, int rsh = 0);
 void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr,
-                    bool replay = false, int co = 0);
+                    bool replay = false, int co = 0, int rsh = 0);
 void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr,
-                    bool replay = false, int co = 0);
+                    bool replay = false, int co = 0, int rsh = 0);
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
-                     cudaStream_t st, unsigned char* rec = nullptr, bool replay = false, int co = 0);
+                     cudaStream_t st, unsigned char* rec = nullptr, bool replay = false, int co = 0, int rsh = 0);
 
 int sweep_max_blocks_per_sm(int w, int blk);
 
@@ -76,13 +78,14 @@ void launch_flux(const Dev& d, int slot, int s, double* out, cudaStream_t st);
 // ---- frozen-limiter adjoint (adjoint.cu)
 struct ObsDev {
   int member, slot, call, k, l;
+  int item;            // place of (member, s) in the work list
   int i0, j0, j1;      // 0-based corner indices: I = i0, i0+1; J = j0, j1
   double wi, wj;       // bilinear weights of the upper corners
   double log_obs;
 };
 // co (DRIFTE only): 0 compute C, 1 compute and store it, 2 load it (needs
 // the DRIFTE coefficient store).
-void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, cudaStream_t st, int co = 0,
+void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, int rsh, cudaStream_t st, int co = 0,
                       const double* loss = nullptr);
 void launch_adj_tail(const Dev& d, cudaStream_t st);
 void launch_scale_lam(const Dev& d, const double* table, cudaStream_t st);

@@ -21,10 +21,19 @@
 
 namespace ramgpu {
 
+// Branch records hold two sweeps per byte, four bits each (three case bits
+// and the clip bit): a call's forward-half sweep in the low nibble and the
+// reverse-half sweep of the same direction in the high one (rsh = 4), which
+// ORs its code into the byte the forward sweep wrote earlier in the call.
+__device__ __forceinline__ unsigned rget(const unsigned char* p, int rsh) { return (unsigned)*p >> rsh; }
+__device__ __forceinline__ void rput(unsigned char* p, int rsh, unsigned v) {
+  *p = (unsigned char)(rsh ? (*p | (v << 4)) : v);
+}
+
 // ----------------------------------------------------------------- DRIFTR
 // Line (J,K,L) along I = 1..NR.  Faces 2..NR-1 (and NR on inflow lines).
 template <bool kCfl, int kRec, int kCo>
-__global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned char* __restrict__ rec) {
+__global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned char* __restrict__ rec, int rsh) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   // the lines of the L window [lw0, lw1) (all of them unless a pipeline
   // runs the step plane chunk by plane chunk): L is the slowest index
@@ -92,13 +101,13 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
         if (kCo == 1) { cst[f - 1] = c; ast[f - 1] = a; }
         int cs;
         const double fb = (kRec == 2)
-            ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = rl[f - 1] & 7)
+            ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = rget(rl + (f - 1), rsh) & 7)
             : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         const double phi = mul_rn_int(c, fb);
         const double raw = (g0 - phi) + phi_prev;
-        fl[f - 1] = (kRec == 2) ? clip_frozen(raw, rl[f - 1]) : clip(raw);
+        fl[f - 1] = (kRec == 2) ? clip_frozen(raw, rget(rl + (f - 1), rsh)) : clip(raw);
         if (kRec == kRecCount) nclip += is_neg(raw);
-        if (kRec == 1) rl[f - 1] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
+        if (kRec == 1) rput(rl + (f - 1), rsh, cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         gm = g0; g0 = gp; gp = gpp;
         xm = x; bxm = bx; x = xp; bx = bxp;
@@ -112,15 +121,15 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
       } else {
         const double xp = g2 - g1; const bits64 bxp = babs_bits(beta, xp);
         const double an = corr_a_int(dbits(cN) & kAbsMask, true, cN, -0.5);
-        fbn = (kRec == 2) ? face_value_frozen(x, xp, g1, an, beta, csn = rl[nr - 1] & 7)
+        fbn = (kRec == 2) ? face_value_frozen(x, xp, g1, an, beta, csn = rget(rl + (nr - 1), rsh) & 7)
                           : face_value_case(x, bx, xp, bxp, g1, an, csn);
       }
       if (closed) fbn = 0.0;
       const double phin = cN * fbn;
       const double rawn = (g0 - phin) + phi_prev;
-      fl[nr - 1] = (kRec == 2) ? clip_frozen(rawn, rl[nr - 1]) : clip(rawn);
+      fl[nr - 1] = (kRec == 2) ? clip_frozen(rawn, rget(rl + (nr - 1), rsh)) : clip(rawn);
       if (kRec == kRecCount) nclip += is_neg(rawn);
-      if (kRec == 1) rl[nr - 1] = (unsigned char)(csn | (is_neg(rawn) ? kClipBit : 0));
+      if (kRec == 1) rput(rl + (nr - 1), rsh, csn | (is_neg(rawn) ? kClipBit : 0));
     }
     if (kRec == kRecCount) warp_atomic_add(&d.clipq[slot], nclip);
     if (kCfl) warp_atomic_max(&d.cflq[slot * 4 + 0], q);
@@ -130,7 +139,7 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
 // ----------------------------------------------------------------- DRIFTP
 // Line (I,K,L), I = 2..NR, along J = 1..NT, periodic with J=1 == J=NT.
 template <bool kCfl, int kRec, int kCo>
-__global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned char* __restrict__ rec) {
+__global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned char* __restrict__ rec, int rsh) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int line0 = d.lw0 * (nr - 1) * ne;  // the L window, as in DRIFTR
   const int nlines = (nr - 1) * ne * (d.lw1 - d.lw0);
@@ -177,7 +186,7 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
         const double a = (kCo == 2) ? ast[(long long)(nt - 1) * st] : corr_a_int(dbits(cN) & kAbsMask, neg, cN, -0.5);
         if (kCo == 1) { cst[(long long)(nt - 1) * st] = cN; ast[(long long)(nt - 1) * st] = a; }
         phiN = cN * ((kRec == 2)
-            ? face_value_frozen(XN, neg ? X2 : XNm, neg ? G2 : GN, a, beta, csN = rl[(long long)(nt - 1) * st] & 7)
+            ? face_value_frozen(XN, neg ? X2 : XNm, neg ? G2 : GN, a, beta, csN = rget(rl + (long long)(nt - 1) * st, rsh) & 7)
             : face_value_case(XN, bXN, neg ? X2 : XNm, neg ? bX2 : bXNm, neg ? G2 : GN, a, csN));
       }
       double phi_prev = phiN;
@@ -211,24 +220,24 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
         int cs;
         const unsigned char* rj = (kRec == 1 || kRec == 2) ? rl + (long long)(J - 1) * st : nullptr;
         const double fb = (kRec == 2)
-            ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rj & 7)
+            ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = rget(rj, rsh) & 7)
             : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         const double phi = mul_rn_int(c, fb);
         const double raw = (g0 - phi) + phi_prev;
-        GJ(J) = (kRec == 2) ? clip_frozen(raw, *rj) : clip(raw);
+        GJ(J) = (kRec == 2) ? clip_frozen(raw, rget(rj, rsh)) : clip(raw);
         if (kRec == kRecCount) nclip += is_neg(raw);
-        if (kRec == 1) rl[(long long)(J - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
+        if (kRec == 1) rput(rl + ((long long)(J - 1) * st), rsh, cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         g0 = gp; gp = gpp;
         nxt = nn;
         xm = x; bxm = bx; x = xp; bx = bxp;
       }
       const double rawN = (GN - phiN) + phi_prev;
-      const double vN = (kRec == 2) ? clip_frozen(rawN, rl[(long long)(nt - 1) * st]) : clip(rawN);
+      const double vN = (kRec == 2) ? clip_frozen(rawN, rget(rl + (long long)(nt - 1) * st, rsh)) : clip(rawN);
       if (kRec == kRecCount) nclip += is_neg(rawN);
       GJ(nt) = vN;
       GJ(1) = vN;
-      if (kRec == 1) rl[(long long)(nt - 1) * st] = (unsigned char)(csN | (is_neg(rawN) ? kClipBit : 0));
+      if (kRec == 1) rput(rl + ((long long)(nt - 1) * st), rsh, csN | (is_neg(rawN) ? kClipBit : 0));
   #undef GJ
   #undef CJ
     }
@@ -241,7 +250,7 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
 // Line (I,J,L), I = 2..NR, along K = 1..NE with extrapolated F(0), F(1)
 // and F(NE+1) = F(NE+2) = 0.  Cell K = 1 is never written.
 template <bool kCfl, int kRec, int kCo>
-__global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned char* __restrict__ rec) {
+__global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned char* __restrict__ rec, int rsh) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int line0 = d.lw0 * (nr - 1) * nt;  // the L window, as in DRIFTR
   const int nlines = (nr - 1) * nt * (d.lw1 - d.lw0);
@@ -295,10 +304,10 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
         const double a = (kCo == 2) ? ast[0] : fma(c, mhde[0], neg ? -0.5 : 0.5);
         if (kCo == 1) { cst[0] = c; ast[0] = a; }
         int cs;
-        double fb = (kRec == 2) ? face_value_frozen(X1, neg ? X2 : X0, neg ? G2 : G1, a, beta, cs = rl[0] & 7)
+        double fb = (kRec == 2) ? face_value_frozen(X1, neg ? X2 : X0, neg ? G2 : G1, a, beta, cs = rget(rl, rsh) & 7)
                                 : face_value_case(X1, bX1, neg ? X2 : X0, neg ? bX2 : bX0, neg ? G2 : G1, a, cs);
         if (closed) fb = 0.0;
-        if (kRec == 1) rl[0] = (unsigned char)cs;
+        if (kRec == 1) rput(rl, rsh, cs);
         phi_prev = c * fb;
       }
       double g0 = G2, gp = G3, xm = X1, x = X2;
@@ -315,16 +324,16 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
         if (kCo == 1) { cst[(long long)(K - 1) * st] = c; ast[(long long)(K - 1) * st] = a; }
         int cs;
         const unsigned char* rk = (kRec == 1 || kRec == 2) ? rl + (long long)(K - 1) * st : nullptr;
-        double fb = (kRec == 2) ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rk & 7)
+        double fb = (kRec == 2) ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = rget(rk, rsh) & 7)
                                 : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         if (closed && K == ne) fb = 0.0;
         // loaded coefficients leave this sweep few FP64 operations to hide its
         // loads behind: the FP64 multiply (uncontracted, bit-equal to mul_rn_int)
         const double phi = (kCo == 2) ? __dmul_rn(c, fb) : mul_rn_int(c, fb);
         const double raw = fma(phi_prev - phi, iwe[K - 1], g0);
-        GK(K) = (kRec == 2) ? clip_frozen(raw, *rk) : clip(raw);
+        GK(K) = (kRec == 2) ? clip_frozen(raw, rget(rk, rsh)) : clip(raw);
         if (kRec == kRecCount) nclip += is_neg(raw);
-        if (kRec == 1) rl[(long long)(K - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
+        if (kRec == 1) rput(rl + ((long long)(K - 1) * st), rsh, cs | (is_neg(raw) ? kClipBit : 0));
         phi_prev = phi;
         g0 = gp; gp = gpp;
         xm = x; bxm = bx; x = xp; bx = bxp;
@@ -354,7 +363,7 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
 // so no lane but lane 0 sees the F(1) = F(2) rule.
 template <bool kCfl, int kLoss, int kRec, int kCo, int kSplit>
 __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const double* __restrict__ lossA,
-                                                   unsigned char* __restrict__ rec) {
+                                                   unsigned char* __restrict__ rec, int rsh) {
   const int nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa;
   const int nlines = (nr - 1) * nt * ne;
   // Work units are (item, block of lines).  A grid of (blocks per item,
@@ -431,7 +440,7 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         const double xm = w1 - w0, x = w2 - w1, xp = w3 - w2;
         int cs;
         const double fb = (kRec == 2)
-            ? face_value_frozen(x, neg ? xp : xm, neg ? w2 : w1, a, beta, cs = rl[(long long)(b - 1) * st] & 7)
+            ? face_value_frozen(x, neg ? xp : xm, neg ? w2 : w1, a, beta, cs = rget(rl + (long long)(b - 1) * st, rsh) & 7)
             : face_value_case(x, babs_bits(beta, x), neg ? xp : xm, babs_bits(beta, neg ? xp : xm),
                               neg ? w2 : w1, a, cs);
         phi_prev = c * fb;
@@ -461,12 +470,12 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         if (kCo == 1) { cst[(long long)(L - 1) * st] = c; ast[(long long)(L - 1) * st] = a; }
         int cs;
         const unsigned char* rq = (kRec == 1 || kRec == 2) ? rl + (long long)(L - 1) * st : nullptr;
-        const double fb = (kRec == 2) ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = *rq & 7)
+        const double fb = (kRec == 2) ? face_value_frozen(x, neg ? xp : xm, neg ? gp : g0, a, beta, cs = rget(rq, rsh) & 7)
                                       : face_value_case(x, bx, neg ? xp : xm, neg ? bxp : bxm, neg ? gp : g0, a, cs);
         const double phi = mul_rn_int(c, fb);
         const double raw = fma(phi_prev - phi, iwmu[L - 1], g0);
-        if (kRec == 1) rl[(long long)(L - 1) * st] = (unsigned char)(cs | (is_neg(raw) ? kClipBit : 0));
-        double v = (kRec == 2) ? clip_frozen(raw, *rq) : clip(raw);
+        if (kRec == 1) rput(rl + ((long long)(L - 1) * st), rsh, cs | (is_neg(raw) ? kClipBit : 0));
+        double v = (kRec == 2) ? clip_frozen(raw, rget(rq, rsh)) : clip(raw);
         if (kRec == kRecCount) nclip += is_neg(raw);
         if (kLoss == 1) v *= LA(L);
         GL(L) = v;
@@ -482,8 +491,8 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
         if (kCfl && inside) q = umax64(q, mul_pos_bits(cfl_bits(c, kBits1em32), d.idmu[L - 1]));
         const double phi = c * (closed ? 0.0 : gp);
         const double raw = fma(phi_prev - phi, iwmu[L - 1], g0);
-        if (kRec == 1) rl[(long long)(L - 1) * st] = (unsigned char)(is_neg(raw) ? kClipBit : 0);
-        const double v = (kRec == 2) ? clip_frozen(raw, rl[(long long)(L - 1) * st]) : clip(raw);
+        if (kRec == 1) rput(rl + ((long long)(L - 1) * st), rsh, is_neg(raw) ? kClipBit : 0);
+        const double v = (kRec == 2) ? clip_frozen(raw, rget(rl + (long long)(L - 1) * st, rsh)) : clip(raw);
         if (kRec == kRecCount) nclip += is_neg(raw);
         const double vN = v * d.rho[fij];
         if (kLoss == 1) {
@@ -525,83 +534,86 @@ static inline int nlines_of(const Dev& d, int w) {
 // co: 0 compute the face coefficients, 1 compute and store them, 2 load
 // the stored ones (needs d.coef; the plain, store and load forms give
 // identical results).
-void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay, int co) {
+void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay, int co,
+                    int rsh) {
   dim3 g = grid_for(d, 0, nlines_of(d, 0));
   const int b = d.blk[0];
   const bool n = d.count_clips;
-  if (rec && replay) k_sweep_r<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec);
-  else if (rec) k_sweep_r<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec);
-  else if (co == 1) (n ? k_sweep_r<true, 3, 1> : k_sweep_r<true, 0, 1>)<<<g, b, 0, st>>>(d, dts, nullptr);
-  else if (co == 2) (n ? k_sweep_r<false, 3, 2> : k_sweep_r<false, 0, 2>)<<<g, b, 0, st>>>(d, dts, nullptr);
-  else if (cfl) (n ? k_sweep_r<true, 3, 0> : k_sweep_r<true, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr);
-  else (n ? k_sweep_r<false, 3, 0> : k_sweep_r<false, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr);
+  if (rec && replay) k_sweep_r<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec, rsh);
+  else if (rec) k_sweep_r<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec, rsh);
+  else if (co == 1) (n ? k_sweep_r<true, 3, 1> : k_sweep_r<true, 0, 1>)<<<g, b, 0, st>>>(d, dts, nullptr, 0);
+  else if (co == 2) (n ? k_sweep_r<false, 3, 2> : k_sweep_r<false, 0, 2>)<<<g, b, 0, st>>>(d, dts, nullptr, 0);
+  else if (cfl) (n ? k_sweep_r<true, 3, 0> : k_sweep_r<true, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr, 0);
+  else (n ? k_sweep_r<false, 3, 0> : k_sweep_r<false, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr, 0);
 }
-void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay, int co) {
+void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay, int co,
+                    int rsh) {
   dim3 g = grid_for(d, 1, nlines_of(d, 1));
   const int b = d.blk[1];
   const bool n = d.count_clips;
-  if (rec && replay) k_sweep_p<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec);
-  else if (rec) k_sweep_p<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec);
-  else if (co == 1) (n ? k_sweep_p<true, 3, 1> : k_sweep_p<true, 0, 1>)<<<g, b, 0, st>>>(d, dts, nullptr);
-  else if (co == 2) (n ? k_sweep_p<false, 3, 2> : k_sweep_p<false, 0, 2>)<<<g, b, 0, st>>>(d, dts, nullptr);
-  else if (cfl) (n ? k_sweep_p<true, 3, 0> : k_sweep_p<true, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr);
-  else (n ? k_sweep_p<false, 3, 0> : k_sweep_p<false, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr);
+  if (rec && replay) k_sweep_p<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec, rsh);
+  else if (rec) k_sweep_p<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec, rsh);
+  else if (co == 1) (n ? k_sweep_p<true, 3, 1> : k_sweep_p<true, 0, 1>)<<<g, b, 0, st>>>(d, dts, nullptr, 0);
+  else if (co == 2) (n ? k_sweep_p<false, 3, 2> : k_sweep_p<false, 0, 2>)<<<g, b, 0, st>>>(d, dts, nullptr, 0);
+  else if (cfl) (n ? k_sweep_p<true, 3, 0> : k_sweep_p<true, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr, 0);
+  else (n ? k_sweep_p<false, 3, 0> : k_sweep_p<false, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr, 0);
 }
-void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay, int co) {
+void launch_sweep_e(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec, bool replay, int co,
+                    int rsh) {
   dim3 g = grid_for(d, 2, nlines_of(d, 2));
   const int b = d.blk[2];
   const bool n = d.count_clips;
-  if (rec && replay) k_sweep_e<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec);
-  else if (rec && co == 1) k_sweep_e<false, 1, 1><<<g, b, 0, st>>>(d, dts, rec);
-  else if (rec && co == 2) k_sweep_e<false, 1, 2><<<g, b, 0, st>>>(d, dts, rec);
-  else if (rec) k_sweep_e<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec);
-  else if (co == 1) (n ? k_sweep_e<true, 3, 1> : k_sweep_e<true, 0, 1>)<<<g, b, 0, st>>>(d, dts, nullptr);
-  else if (co == 2) (n ? k_sweep_e<false, 3, 2> : k_sweep_e<false, 0, 2>)<<<g, b, 0, st>>>(d, dts, nullptr);
-  else if (cfl) (n ? k_sweep_e<true, 3, 0> : k_sweep_e<true, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr);
-  else (n ? k_sweep_e<false, 3, 0> : k_sweep_e<false, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr);
+  if (rec && replay) k_sweep_e<false, 2, 0><<<g, b, 0, st>>>(d, dts, rec, rsh);
+  else if (rec && co == 1) k_sweep_e<false, 1, 1><<<g, b, 0, st>>>(d, dts, rec, rsh);
+  else if (rec && co == 2) k_sweep_e<false, 1, 2><<<g, b, 0, st>>>(d, dts, rec, rsh);
+  else if (rec) k_sweep_e<false, 1, 0><<<g, b, 0, st>>>(d, dts, rec, rsh);
+  else if (co == 1) (n ? k_sweep_e<true, 3, 1> : k_sweep_e<true, 0, 1>)<<<g, b, 0, st>>>(d, dts, nullptr, 0);
+  else if (co == 2) (n ? k_sweep_e<false, 3, 2> : k_sweep_e<false, 0, 2>)<<<g, b, 0, st>>>(d, dts, nullptr, 0);
+  else if (cfl) (n ? k_sweep_e<true, 3, 0> : k_sweep_e<true, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr, 0);
+  else (n ? k_sweep_e<false, 3, 0> : k_sweep_e<false, 0, 0>)<<<g, b, 0, st>>>(d, dts, nullptr, 0);
 }
 // The clip-counting forms of the plain (unrecorded) pitch-angle sweeps.
 template <int kLoss, int kS>
 static void mu_count(const Dev& d, dim3 g, int b, double dts, const double* loss, cudaStream_t st, bool cfl,
                      int co) {
-  if (co == 1) k_sweep_mu<true, kLoss, 3, 1, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-  else if (co == 2) k_sweep_mu<false, kLoss, 3, 2, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-  else if (cfl) k_sweep_mu<true, kLoss, 3, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-  else k_sweep_mu<false, kLoss, 3, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+  if (co == 1) k_sweep_mu<true, kLoss, 3, 1, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr, 0);
+  else if (co == 2) k_sweep_mu<false, kLoss, 3, 2, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr, 0);
+  else if (cfl) k_sweep_mu<true, kLoss, 3, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr, 0);
+  else k_sweep_mu<false, kLoss, 3, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr, 0);
 }
 
 template <int kLoss, int kS>
 static void mu_launch(const Dev& d, dim3 g, int b, double dts, const double* loss, cudaStream_t st,
-                      unsigned char* rec, bool replay, bool cfl, int co) {
+                      unsigned char* rec, bool replay, bool cfl, int co, int rsh) {
   const bool n = d.count_clips;
-  if (rec && replay) k_sweep_mu<false, kLoss, 2, 0, kS><<<g, b, 0, st>>>(d, dts, loss, rec);
-  else if (rec) k_sweep_mu<false, kLoss, 1, 0, kS><<<g, b, 0, st>>>(d, dts, loss, rec);
+  if (rec && replay) k_sweep_mu<false, kLoss, 2, 0, kS><<<g, b, 0, st>>>(d, dts, loss, rec, rsh);
+  else if (rec) k_sweep_mu<false, kLoss, 1, 0, kS><<<g, b, 0, st>>>(d, dts, loss, rec, rsh);
   else if (n) mu_count<kLoss, kS>(d, g, b, dts, loss, st, cfl, co);
-  else if (co == 1) k_sweep_mu<true, kLoss, 0, 1, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-  else if (co == 2) k_sweep_mu<false, kLoss, 0, 2, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-  else if (cfl) k_sweep_mu<true, kLoss, 0, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
-  else k_sweep_mu<false, kLoss, 0, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr);
+  else if (co == 1) k_sweep_mu<true, kLoss, 0, 1, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr, 0);
+  else if (co == 2) k_sweep_mu<false, kLoss, 0, 2, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr, 0);
+  else if (cfl) k_sweep_mu<true, kLoss, 0, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr, 0);
+  else k_sweep_mu<false, kLoss, 0, 0, kS><<<g, b, 0, st>>>(d, dts, loss, nullptr, 0);
 }
 // Lines are split between d.mu_lanes adjacent lanes (2 for NPA >= 12, 4
 // for NPA >= 24: every segment keeps at least four cells, so no lane but
 // the first reads the F(1) rule).
 void launch_sweep_mu(const Dev& d, double dts, bool cfl, int loss_mode, const double* loss,
-                     cudaStream_t st, unsigned char* rec, bool replay, int co) {
+                     cudaStream_t st, unsigned char* rec, bool replay, int co, int rsh) {
   const int lanes = (d.mu_lanes == 4 && d.npa >= 24) ? 4 : ((d.mu_lanes >= 2 && d.npa >= 12) ? 2 : 1);
   dim3 g = grid_for(d, 3, lanes * nlines_of(d, 3));
   const int b = d.blk[3];
   if (lanes == 4) {
-    if (loss_mode == 1) mu_launch<1, 4>(d, g, b, dts, loss, st, rec, replay, cfl, co);
-    else if (loss_mode == 2) mu_launch<2, 4>(d, g, b, dts, loss, st, rec, replay, cfl, co);
-    else mu_launch<0, 4>(d, g, b, dts, nullptr, st, rec, replay, cfl, co);
+    if (loss_mode == 1) mu_launch<1, 4>(d, g, b, dts, loss, st, rec, replay, cfl, co, rsh);
+    else if (loss_mode == 2) mu_launch<2, 4>(d, g, b, dts, loss, st, rec, replay, cfl, co, rsh);
+    else mu_launch<0, 4>(d, g, b, dts, nullptr, st, rec, replay, cfl, co, rsh);
   } else if (lanes == 2) {
-    if (loss_mode == 1) mu_launch<1, 2>(d, g, b, dts, loss, st, rec, replay, cfl, co);
-    else if (loss_mode == 2) mu_launch<2, 2>(d, g, b, dts, loss, st, rec, replay, cfl, co);
-    else mu_launch<0, 2>(d, g, b, dts, nullptr, st, rec, replay, cfl, co);
+    if (loss_mode == 1) mu_launch<1, 2>(d, g, b, dts, loss, st, rec, replay, cfl, co, rsh);
+    else if (loss_mode == 2) mu_launch<2, 2>(d, g, b, dts, loss, st, rec, replay, cfl, co, rsh);
+    else mu_launch<0, 2>(d, g, b, dts, nullptr, st, rec, replay, cfl, co, rsh);
   } else {
-    if (loss_mode == 1) mu_launch<1, 1>(d, g, b, dts, loss, st, rec, replay, cfl, co);
-    else if (loss_mode == 2) mu_launch<2, 1>(d, g, b, dts, loss, st, rec, replay, cfl, co);
-    else mu_launch<0, 1>(d, g, b, dts, nullptr, st, rec, replay, cfl, co);
+    if (loss_mode == 1) mu_launch<1, 1>(d, g, b, dts, loss, st, rec, replay, cfl, co, rsh);
+    else if (loss_mode == 2) mu_launch<2, 1>(d, g, b, dts, loss, st, rec, replay, cfl, co, rsh);
+    else mu_launch<0, 1>(d, g, b, dts, nullptr, st, rec, replay, cfl, co, rsh);
   }
 }
 

@@ -186,7 +186,7 @@ def test_checkpoint_spacing_and_record_budget(case, k, keep, overlap):
     wl, model, kp, obs, J0, _, gf, gb = case
     g = wl.grid
     ns = len(g.species)
-    per_call = 8 * ns * g.nr * g.nt * g.ne * g.npa
+    per_call = 4 * ns * g.nr * g.nt * g.ne * g.npa  # 4 bits per face and sweep, 8 sweeps
     model.set_adj_record_budget(keep * k * per_call)
     model.set_adj_overlap(overlap)
     try:
