@@ -545,8 +545,12 @@ def run_padif(torch, abi, W, stream, args):
     g = wl.grid
     gpu = new_model(abi, wl, stream)
     flush = torch.empty(max(1, args.flush_mb) << 20, dtype=torch.uint8, device="cuda")
+    # each measured pass follows an untimed one, so that the once-per-DTs
+    # tables (and, with WPADIF on, its elimination tables) are built outside it
+    kernel_pass(torch, gpu, stream, wl, flush, 1)
     _, base_ms = kernel_pass(torch, gpu, stream, wl, flush, 3)
     gpu.set_pa_diffusion(0, W.pa_diffusion(g, wl.fields))
+    kernel_pass(torch, gpu, stream, wl, flush, 1)
     kt, step_ms = kernel_pass(torch, gpu, stream, wl, flush, 3)
     gpu.close()
     pk = kt.get("padif", (0.0, 1))

@@ -585,14 +585,14 @@ static int enqueue_call_rec(ramgpu_ctx* ctx, double dts, unsigned char* rec, boo
     const Dev& d = ctx->d;
     const cudaStream_t st = ctx->stream;
     unsigned char* r = rec + (size_t)i0 * d.ncell;
-    launch_sweep_r(d, dts, false, st, r + 0 * isz, false, 0, 0);
-    launch_sweep_p(d, dts, false, st, r + 1 * isz, false, 0, 0);
-    launch_sweep_e(d, dts, false, st, r + 2 * isz, false, co_e, 0);
-    launch_sweep_mu(d, dts, false, 1, d.loss2, st, r + 3 * isz, false, 0, 0);
-    launch_sweep_mu(d, dts, false, 0, nullptr, st, r + 3 * isz, false, 0, 4);
-    launch_sweep_e(d, dts, false, st, r + 2 * isz, false, 2 * co_e, 4);
-    launch_sweep_p(d, dts, false, st, r + 1 * isz, false, 0, 4);
     launch_sweep_r(d, dts, false, st, r + 0 * isz, false, 0, 4);
+    launch_sweep_p(d, dts, false, st, r + 1 * isz, false, 0, 4);
+    launch_sweep_e(d, dts, false, st, r + 2 * isz, false, co_e, 4);
+    launch_sweep_mu(d, dts, false, 1, d.loss2, st, r + 3 * isz, false, 0, 4);
+    launch_sweep_mu(d, dts, false, 0, nullptr, st, r + 3 * isz, false, 0, 0);
+    launch_sweep_e(d, dts, false, st, r + 2 * isz, false, 2 * co_e, 0);
+    launch_sweep_p(d, dts, false, st, r + 1 * isz, false, 0, 0);
+    launch_sweep_r(d, dts, false, st, r + 0 * isz, false, 0, 0);
     launch_finish(d, st);
     if (moments) launch_moments(d, st);
     else launch_anisch_state(d, st);
@@ -615,14 +615,14 @@ static int enqueue_call_replay(ramgpu_ctx* ctx, double dts, unsigned char* rec) 
     const Dev& d = ctx->d;
     const cudaStream_t st = ctx->stream;
     unsigned char* r = rec + (size_t)i0 * d.ncell;
-    launch_sweep_r(d, dts, false, st, r + 0 * isz, true, 0, 0);
-    launch_sweep_p(d, dts, false, st, r + 1 * isz, true, 0, 0);
-    launch_sweep_e(d, dts, false, st, r + 2 * isz, true, 0, 0);
-    launch_sweep_mu(d, dts, false, 1, d.loss2, st, r + 3 * isz, true, 0, 0);
-    launch_sweep_mu(d, dts, false, 0, nullptr, st, r + 3 * isz, true, 0, 4);
-    launch_sweep_e(d, dts, false, st, r + 2 * isz, true, 0, 4);
-    launch_sweep_p(d, dts, false, st, r + 1 * isz, true, 0, 4);
     launch_sweep_r(d, dts, false, st, r + 0 * isz, true, 0, 4);
+    launch_sweep_p(d, dts, false, st, r + 1 * isz, true, 0, 4);
+    launch_sweep_e(d, dts, false, st, r + 2 * isz, true, 0, 4);
+    launch_sweep_mu(d, dts, false, 1, d.loss2, st, r + 3 * isz, true, 0, 4);
+    launch_sweep_mu(d, dts, false, 0, nullptr, st, r + 3 * isz, true, 0, 0);
+    launch_sweep_e(d, dts, false, st, r + 2 * isz, true, 0, 0);
+    launch_sweep_p(d, dts, false, st, r + 1 * isz, true, 0, 0);
+    launch_sweep_r(d, dts, false, st, r + 0 * isz, true, 0, 0);
     launch_finish(d, st);
     launch_anisch_state(d, st);
     ctx->launches += 10;
@@ -3060,14 +3060,14 @@ static int adj_recompute_call(ramgpu_ctx* ctx, const Dev& q, cudaStream_t st, in
   const int co_e = (q.coef && q.coef_slot[2] >= 0) ? 1 : 0;
   launch_member_coef(qc, dts, st);
   launch_ghost(q, st);
-  launch_sweep_r(q, dts, false, st, rec + 0 * isz, false, 0, 0);
-  launch_sweep_p(q, dts, false, st, rec + 1 * isz, false, 0, 0);
-  launch_sweep_e(q, dts, false, st, rec + 2 * isz, false, co_e, 0);
-  launch_sweep_mu(q, dts, false, 1, q.loss2, st, rec + 3 * isz, false, 0, 0);
-  launch_sweep_mu(q, dts, false, 0, nullptr, st, rec + 3 * isz, false, 0, 4);
-  launch_sweep_e(q, dts, false, st, rec + 2 * isz, false, 2 * co_e, 4);
-  launch_sweep_p(q, dts, false, st, rec + 1 * isz, false, 0, 4);
   launch_sweep_r(q, dts, false, st, rec + 0 * isz, false, 0, 4);
+  launch_sweep_p(q, dts, false, st, rec + 1 * isz, false, 0, 4);
+  launch_sweep_e(q, dts, false, st, rec + 2 * isz, false, co_e, 4);
+  launch_sweep_mu(q, dts, false, 1, q.loss2, st, rec + 3 * isz, false, 0, 4);
+  launch_sweep_mu(q, dts, false, 0, nullptr, st, rec + 3 * isz, false, 0, 0);
+  launch_sweep_e(q, dts, false, st, rec + 2 * isz, false, 2 * co_e, 0);
+  launch_sweep_p(q, dts, false, st, rec + 1 * isz, false, 0, 0);
+  launch_sweep_r(q, dts, false, st, rec + 0 * isz, false, 0, 0);
   launch_finish(q, st);
   launch_anisch_state(q, st);
   ctx->launches += 13;
@@ -3152,14 +3152,14 @@ int ramgpu_adj_backward(ramgpu_ctx* ctx, double* grad_f2, double* grad_fgeos) {
         }
         const unsigned char* r = rcall + (size_t)i0 * dg.ncell;
         launch_adj_tail(dg, st);
-        launch_adj_sweep(dg, 0, r + 0 * isz, 4, st);
-        launch_adj_sweep(dg, 1, r + 1 * isz, 4, st);
-        launch_adj_sweep(dg, 2, r + 2 * isz, 4, st, co_e);
-        launch_adj_sweep(dg, 3, r + 3 * isz, 4, st);
-        launch_adj_sweep(dg, 3, r + 3 * isz, 0, st, 0, dg.loss2);  // CEX/ATMOL^T fused
-        launch_adj_sweep(dg, 2, r + 2 * isz, 0, st, 2 * co_e);
-        launch_adj_sweep(dg, 1, r + 1 * isz, 0, st);
         launch_adj_sweep(dg, 0, r + 0 * isz, 0, st);
+        launch_adj_sweep(dg, 1, r + 1 * isz, 0, st);
+        launch_adj_sweep(dg, 2, r + 2 * isz, 0, st, co_e);
+        launch_adj_sweep(dg, 3, r + 3 * isz, 0, st);
+        launch_adj_sweep(dg, 3, r + 3 * isz, 4, st, 0, dg.loss2);  // CEX/ATMOL^T fused
+        launch_adj_sweep(dg, 2, r + 2 * isz, 4, st, 2 * co_e);
+        launch_adj_sweep(dg, 1, r + 1 * isz, 4, st);
+        launch_adj_sweep(dg, 0, r + 0 * isz, 4, st);
         ctx->launches += 10;
         CKL("adjoint backward");
         if (G > 1) CK(cudaEventRecord(evUse[g * T + sl], st));
@@ -3273,14 +3273,14 @@ int ramgpu_adj_record(ramgpu_ctx* ctx, int call, unsigned char* out) {
   if (a.rec_stale)
     return fail(ctx, RAMGPU_ERR_STATE, "the record was replaced by ramgpu_adj_backward's recomputation");
   CK(cudaStreamSynchronize(ctx->stream));
-  // the device keeps sweeps w and 7-w in the low and high nibbles of one
+  // the device keeps sweeps w and 7-w in the high and low nibbles of one
   // byte (instance w < 4); unpack into one byte per face and sweep
   std::vector<unsigned char> packed(a.rec_call);
   CK(cudaMemcpy(packed.data(), a.rec + adj_rec_slot(a, call) * a.rec_call, a.rec_call, cudaMemcpyDeviceToHost));
   const size_t isz = a.rec_call / 4;
   for (int w = 0; w < 8; ++w) {
     const unsigned char* src = packed.data() + (size_t)(w < 4 ? w : 7 - w) * isz;
-    const int sh = w < 4 ? 0 : 4;
+    const int sh = w < 4 ? 4 : 0;
     unsigned char* dst = out + (size_t)w * isz;
     for (size_t i = 0; i < isz; ++i) dst[i] = (unsigned char)((src[i] >> sh) & 0x0F);
   }

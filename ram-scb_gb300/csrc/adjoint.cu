@@ -3,7 +3,7 @@
 // With the limiter branch of every face and the clip state of every cell
 // frozen (recorded by the forward sweeps, four bits per face: 0 upwind
 // only, 1 beta*D, 2 X, 3 D, 4 beta*X, plus kClipBit; a call's forward and
-// reverse sweeps of one direction share a byte, the reverse one in the high
+// reverse sweeps of one direction share a byte, the forward one in the high
 // nibble, read here with the shift rsh), each sweep of
 // src/ModRamDrift.f90 is a linear map of its line
 //   Fnew(i) = G(i) + w(i) (Phi(i-1) - Phi(i)),  Phi(f) = C(f) FBND(f),
@@ -16,6 +16,8 @@
 // including the stale ghosts an outflow line inherits from an earlier
 // inflow line.
 #include <math.h>
+
+#include <type_traits>
 
 #include "kernels.cuh"
 
@@ -194,8 +196,8 @@ __device__ __forceinline__ double masked(const double* __restrict__ lam, const u
 // owns whole sectors and lambda can be read ahead through the read-only path.
 // Six resident CTAs per SM as the register target: without it the compiler
 // aims at a higher occupancy and spills the window (measured slower).
-template <bool kNc>
-__global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __restrict__ rec, int rsh) {
+template <bool kNc, int rsh>
+__global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = nt * ne * d.npa;
   WORK_LOOP(nlines) {
@@ -273,7 +275,8 @@ __global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __
 // J = 2..NT with FBND(1) = FBND(NT).  Faces NT-1 and NT wrap onto cells
 // 1..3; they are transposed first, their contributions held in registers
 // and added when the window reaches those cells (NT >= 7).
-__global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __restrict__ rec, int rsh) {
+template <int rsh>
+__global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * ne * d.npa;
   WORK_LOOP(nlines) {
@@ -363,8 +366,8 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
 // transposes (of the reverse and the forward half) share C (same DTs and
 // potential), so the first keeps it for the second, as the forward sweeps
 // do; the stored value is the recomputed one, so the results do not change.
-template <int kCo>
-__global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __restrict__ rec, int rsh) {
+template <int kCo, int rsh>
+__global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __restrict__ rec) {
   const int nr = d.nr, nt = d.nt, ne = d.ne;
   const int nlines = (nr - 1) * nt * d.npa;
   WORK_LOOP(nlines) {
@@ -454,8 +457,8 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
 // loss (may be null): the CEX/ATMOL factor table the forward sweep applied
 // to its result (cells L >= 2 of its lines; the table is 1 elsewhere), so
 // lambda is scaled by it as it is read, the transposed loss fused in.
-template <bool kLoss>
-__global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __restrict__ rec, int rsh,
+template <bool kLoss, int rsh>
+__global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __restrict__ rec,
                                                 const double* __restrict__ loss) {
   const int nr = d.nr, nt = d.nt, ne = d.ne, npa = d.npa;
   const int nlines = (nr - 1) * nt * ne;
@@ -554,22 +557,28 @@ void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, int rsh, cu
     default: nl = (d.nr - 1) * d.nt * d.ne; break;
   }
   dim3 g((nl + blk - 1) / blk, d.nitems, 1);
-  switch (w) {
-    case 0:
-      if (d.nr % 4 == 0) k_adj_r<true><<<g, blk, 0, st>>>(d, rec, rsh);
-      else k_adj_r<false><<<g, blk, 0, st>>>(d, rec, rsh);
-      break;
-    case 1: k_adj_p<<<g, blk, 0, st>>>(d, rec, rsh); break;
-    case 2:
-      if (co == 1) k_adj_e<1><<<g, blk, 0, st>>>(d, rec, rsh);
-      else if (co == 2) k_adj_e<2><<<g, blk, 0, st>>>(d, rec, rsh);
-      else k_adj_e<0><<<g, blk, 0, st>>>(d, rec, rsh);
-      break;
-    default:
-      if (loss) k_adj_mu<true><<<g, blk, 0, st>>>(d, rec, rsh, loss);
-      else k_adj_mu<false><<<g, blk, 0, st>>>(d, rec, rsh, nullptr);
-      break;
-  }
+  // the record nibble is a template parameter: 0 low (reverse half), 4 high
+  auto go = [&](auto sh) {
+    constexpr int R = decltype(sh)::value;
+    switch (w) {
+      case 0:
+        if (d.nr % 4 == 0) k_adj_r<true, R><<<g, blk, 0, st>>>(d, rec);
+        else k_adj_r<false, R><<<g, blk, 0, st>>>(d, rec);
+        break;
+      case 1: k_adj_p<R><<<g, blk, 0, st>>>(d, rec); break;
+      case 2:
+        if (co == 1) k_adj_e<1, R><<<g, blk, 0, st>>>(d, rec);
+        else if (co == 2) k_adj_e<2, R><<<g, blk, 0, st>>>(d, rec);
+        else k_adj_e<0, R><<<g, blk, 0, st>>>(d, rec);
+        break;
+      default:
+        if (loss) k_adj_mu<true, R><<<g, blk, 0, st>>>(d, rec, loss);
+        else k_adj_mu<false, R><<<g, blk, 0, st>>>(d, rec, nullptr);
+        break;
+    }
+  };
+  if (rsh) go(std::integral_constant<int, 4>());
+  else go(std::integral_constant<int, 0>());
 }
 
 // ---------------------------------------------------------- ram_run tail^T

@@ -50,8 +50,8 @@ __device__ __forceinline__ int stale_ghost_src(const Dev& d, int m, int slot, in
 
 // rec: branch record of the sweep, written (replay false) or, with replay
 // true, read back to run the sweep with those branches and clips frozen;
-// rsh: its nibble of the record bytes (0: low, forward half; 4: high,
-// reverse half).
+// rsh: its nibble of the record bytes (4: high, forward half, written
+// first; 0: low, reverse half, ORed in).
 void launch_sweep_r(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr,
                     bool replay = false, int co = 0, int rsh = 0);
 void launch_sweep_p(const Dev& d, double dts, bool cfl, cudaStream_t st, unsigned char* rec = nullptr,

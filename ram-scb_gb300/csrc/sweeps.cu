@@ -22,12 +22,13 @@
 namespace ramgpu {
 
 // Branch records hold two sweeps per byte, four bits each (three case bits
-// and the clip bit): a call's forward-half sweep in the low nibble and the
-// reverse-half sweep of the same direction in the high one (rsh = 4), which
-// ORs its code into the byte the forward sweep wrote earlier in the call.
+// and the clip bit): a call's forward-half sweep in the high nibble
+// (rsh = 4), written first, and the reverse-half sweep of the same
+// direction in the low one, which ORs its code into that byte.  (The
+// reverse half is transposed first; its nibble is the cheaper one to read.)
 __device__ __forceinline__ unsigned rget(const unsigned char* p, int rsh) { return (unsigned)*p >> rsh; }
 __device__ __forceinline__ void rput(unsigned char* p, int rsh, unsigned v) {
-  *p = (unsigned char)(rsh ? (*p | (v << 4)) : v);
+  *p = (unsigned char)(rsh ? (v << 4) : (*p | v));
 }
 
 // ----------------------------------------------------------------- DRIFTR
