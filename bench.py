@@ -51,14 +51,14 @@ NCU_CAPTURE = {
     # ncu on the sources named by sources_sha16 (profiles/sweeps_four_sp.md,
     # profiles/driftr_refined.md): one kernel per command, each captured
     # launch advances one species, so a four-species launch is scaled by 4.
-    "sources_sha16": "65ef85f50ccc6757",
+    "sources_sha16": "2540ea28841301a8",
     "command": ("ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum,"
                 "smsp__sass_thread_inst_executed_op_{dadd,dfma,dmul}_pred_on.sum --clock-control none "
                 "-k regex:k_sweep_<r|p|e|mu> -c 2 python bench.py --steps 2 --warmup 1 --sections headline "
                 "--no-cpu-baseline --no-e2e --no-autotune [--workload refined]"),
-    "dram_bytes": {"four_sp": {"driftr": 4 * 11.02e6, "driftp": 4 * 10.39e6,
-                               "drifte": 4 * 0.5 * (11.34e6 + 29.98e6), "driftmu": 4 * 0.5 * (20.47e6 + 10.53e6)},
-                   "refined": {"driftr": 4 * 0.5 * (268.16e6 + 267.80e6)}},
+    "dram_bytes": {"four_sp": {"driftr": 4 * 11.02e6, "driftp": 4 * 0.5 * (10.39e6 + 10.40e6),
+                               "drifte": 4 * 0.5 * (11.34e6 + 29.98e6), "driftmu": 4 * 0.5 * (20.47e6 + 10.52e6)},
+                   "refined": {"driftr": 4 * 0.5 * (268.3e6 + 267.9e6)}},
     "fp64_ops_per_cell": {"driftr": 5.02, "driftp": 4.64, "drifte": 0.5 * (6.70 + 4.78),
                           "driftmu": 0.5 * (6.62 + 5.69)},
 }
