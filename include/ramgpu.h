@@ -424,6 +424,17 @@ int ramgpu_last_status(ramgpu_ctx *ctx, ramgpu_status *st);
 
 /* Number of kernel launches this context has issued (diagnostics). */
 long long ramgpu_launch_count(const ramgpu_ctx *ctx);
+/* Bounds-checked builds (no reference counterpart): libramgpu_bounds.so is
+ * the same library compiled with RAMGPU_BOUNDS_CHECK, whose sweep and
+ * transposed-sweep kernels test every line's index ranges (work item,
+ * slot, first and last cell, table rows, coefficient-store item) before
+ * touching it, count a failed test in the context's log and skip that line.
+ * *checked: 1 in such a build, 0 otherwise (the log is then empty);
+ * *failures: failed tests since ramgpu_create; *check, *value: the id of the
+ * first failed test (1-4 the R, P, E, MU sweeps, 11-14 their transposes; 0
+ * when none failed) and the line it was testing.  Any pointer may be NULL.
+ * Synchronises the context's stream. */
+int ramgpu_bounds_report(ramgpu_ctx *ctx, int *checked, long long *failures, int *check, long long *value);
 
 /* Per-kernel timing with CUDA events recorded on the context's stream
  * around every launch group (diagnostics; no reference counterpart).

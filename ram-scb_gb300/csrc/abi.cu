@@ -1043,6 +1043,11 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   d.loss1 = dalloc<double>(ctx, ns * ncell, &ok); d.loss2 = dalloc<double>(ctx, ns * ncell, &ok);
   d.charge = dalloc<double>(ctx, ns * ncell, &ok); d.atm = dalloc<double>(ctx, ns * ncell, &ok);
   d.kp = dalloc<double>(ctx, nm, &ok); d.vt_mode = dalloc<int>(ctx, nm, &ok);
+#ifdef RAMGPU_BOUNDS_CHECK
+  d.bounds = dalloc<unsigned long long>(ctx, 3, &ok);  // the bounds log (zeroed)
+#else
+  d.bounds = nullptr;
+#endif
   d.vt = dalloc<double>(ctx, nm * nf * nt, &ok);
   d.cr = dalloc<double>(ctx, nm * nr * nt, &ok); d.ca = dalloc<double>(ctx, nm * nr * nt, &ok);
   d.ue = dalloc<double>(ctx, nm * nijl, &ok); d.um = dalloc<double>(ctx, nm * nijl, &ok);
@@ -2127,6 +2132,20 @@ int ramgpu_reset_losses(ramgpu_ctx* ctx) {
     }
   }
   CK(cudaStreamSynchronize(ctx->stream));
+  return RAMGPU_OK;
+}
+
+int ramgpu_bounds_report(ramgpu_ctx* ctx, int* checked, long long* failures, int* check, long long* value) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  unsigned long long log[3] = {0ULL, 0ULL, 0ULL};
+  if (ctx->d.bounds) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(log, ctx->d.bounds, sizeof(log), cudaMemcpyDeviceToHost));
+  }
+  if (checked) *checked = ctx->d.bounds ? 1 : 0;
+  if (failures) *failures = (long long)log[0];
+  if (check) *check = log[0] ? (int)log[1] - 1 : 0;
+  if (value) *value = (long long)log[2];
   return RAMGPU_OK;
 }
 

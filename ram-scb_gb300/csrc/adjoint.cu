@@ -206,6 +206,12 @@ __global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __
     const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
     if (line >= nlines) continue;
     const int j = line % nt, k = (line / nt) % ne, l = line / (nt * ne);
+    // bounds-checked builds: the line's cells, its GRT and CR rows
+    if (!rg_ok(d, rg_item(d, item) && rg_span((long long)line * nr, nr, 1, d.ncell) &&
+                      rg_span(((long long)l * nt + j) * nr, nr, 1, (long long)nr * nt * d.npa) &&
+                      rg_span(((long long)m * nt + j) * nr, nr, 1, (long long)d.nm * nr * nt),
+               kRgAdjR, line))
+      continue;
     double* __restrict__ lam = d.lam + (long long)slot * d.ncell + (long long)line * nr;
     const unsigned char* __restrict__ rl = rec + (u / bpi) * d.ncell + (long long)line * nr;
     const double* __restrict__ grt = d.grt + ((long long)l * nt + j) * nr;
@@ -289,6 +295,12 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
     const int k = kl % ne, l = kl / ne;
     const long long st = nr;
     const long long base = ((long long)kl * nt) * nr + i;
+    // bounds-checked builds: the line's cells, its GPT and CA columns
+    if (!rg_ok(d, rg_item(d, item) && rg_span(base, nt, nr, d.ncell) &&
+                      rg_span((long long)l * nt * nr + i, nt, nr, (long long)nr * nt * d.npa) &&
+                      rg_span((long long)m * nt * nr + i, nt, nr, (long long)d.nm * nr * nt),
+               kRgAdjP, line))
+      continue;
     double* __restrict__ lam = d.lam + (long long)slot * d.ncell + base;
     const unsigned char* __restrict__ rl = rec + (u / bpi) * d.ncell + base;
     const double* __restrict__ gpt = d.gpt + ((long long)l * nt) * nr + i;
@@ -380,6 +392,15 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
     const int j = jl % nt, l = jl / nt;
     const long long st = (long long)nt * nr;
     const long long base = ((long long)l * ne * nt + j) * nr + i;
+    // bounds-checked builds: the line's cells, its (I,J,L) entry and UE, its
+    // EDOT column, the coefficient store's item
+    if (!rg_ok(d, rg_item(d, item) && rg_span(base, ne, st, d.ncell) &&
+                      rg_span((long long)m * nr * nt * d.npa + ((long long)l * nt + j) * nr + i, 1, 1,
+                              (long long)d.nm * nr * nt * d.npa) &&
+                      rg_span((long long)s * ne * nr + i, ne, nr, (long long)d.ns * ne * nr) &&
+                      (!kCo || d.item0 + u / bpi < d.coef_items),
+               kRgAdjE, line))
+      continue;
     double* __restrict__ lam = d.lam + (long long)slot * d.ncell + base;
     const unsigned char* __restrict__ rl = rec + (u / bpi) * d.ncell + base;
     double* __restrict__ cst = kCo ? coef_ptr(d, 2, 0, u / bpi) + base : nullptr;
@@ -472,6 +493,13 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
     const int j = jk % nt;
     const long long st = (long long)ne * nt * nr;
     const long long off = (long long)jk * nr + i;
+    // bounds-checked builds: the line's cells, its WM and UM columns
+    if (!rg_ok(d, rg_item(d, item) && rg_span(off, npa, st, d.ncell) &&
+                      rg_span((long long)j * nr + i, npa, (long long)nt * nr, (long long)nr * nt * npa) &&
+                      rg_span((long long)m * nt * nr * npa + (long long)j * nr + i, npa, (long long)nt * nr,
+                              (long long)d.nm * nr * nt * npa),
+               kRgAdjMu, line))
+      continue;
     double* __restrict__ lam = d.lam + (long long)slot * d.ncell + off;
     const unsigned char* __restrict__ rl = rec + (u / bpi) * d.ncell + off;
     const long long sij = (long long)nt * nr;

@@ -125,7 +125,43 @@ struct Dev {
   // L window of the R, P and E sweeps and the closing copy/mask: planes
   // [lw0, lw1) (0 and NPA: all); a host pipeline runs them chunk by chunk
   int lw0, lw1;
+  // bounds-checked builds: {failed tests, first check id + 1, its value};
+  // null otherwise
+  unsigned long long* bounds;
 };
+
+// ---------------------------------------------------- bounds-checked builds
+// Compiled with RAMGPU_BOUNDS_CHECK (libramgpu_bounds.so), the streaming
+// kernels test, per line, the index ranges they are about to use (work
+// item, slot, the line's first and last cell, the table rows it reads).  A
+// failed test is counted in the context's log with the id of the first one
+// and its value, and the line is skipped, so nothing is read or written out
+// of range; the line's lanes still take part in every warp-wide operation.
+// Without the macro the tests compile away (rg_ok is true).
+#ifdef RAMGPU_BOUNDS_CHECK
+__device__ __forceinline__ bool rg_ok(const Dev& d, bool ok, int check, long long value) {
+  if (!ok && d.bounds) {
+    if (atomicAdd(d.bounds, 1ULL) == 0ULL) {
+      d.bounds[1] = (unsigned long long)(check + 1);
+      d.bounds[2] = (unsigned long long)value;
+    }
+  }
+  return ok;
+}
+#else
+__device__ __forceinline__ bool rg_ok(const Dev&, bool, int, long long) { return true; }
+#endif
+// [first, first + (n - 1) * stride] inside [0, size)
+__device__ __forceinline__ bool rg_span(long long first, long long n, long long stride, long long size) {
+  return first >= 0 && n >= 1 && first + (n - 1) * stride < size;
+}
+// The work item's (member, species) and slot inside the context's arrays.
+__device__ __forceinline__ bool rg_item(const Dev& d, int2 item) {
+  return item.x >= 0 && item.x < d.nm && item.y >= 0 && item.y < d.ns;
+}
+// check ids
+enum RgCheck { kRgSweepR = 1, kRgSweepP, kRgSweepE, kRgSweepMu, kRgAdjR = 11, kRgAdjP, kRgAdjE, kRgAdjMu,
+               kRgGather = 21, kRgScatter };
 
 // ---------------------------------------------------------------- bit tests
 // The bit pattern moves through an opaque PTX mov: with a plain bit cast

@@ -51,7 +51,15 @@ __global__ void __launch_bounds__(256) k_sweep_r(Dev d, double dts, unsigned cha
     const int line = line0 + (int)(u % bpi) * blockDim.x + threadIdx.x;
     unsigned long long q = 0ULL;  // CFL quotient bits
     unsigned nclip = 0;  // clip events (kRec == kRecCount)
-    if (line < line0 + nlines) {
+    // bounds-checked builds: the line's cells, its GRT and CR rows, the
+    // coefficient store's item
+    const bool lok = line >= line0 + nlines ||
+        rg_ok(d, rg_item(d, item) && rg_span((long long)line * nr, nr, 1, d.ncell) &&
+                     rg_span(((long long)(line / (nt * ne)) * nt + line % nt) * nr, nr, 1, (long long)nr * nt * d.npa) &&
+                     rg_span(((long long)item.x * nt + line % nt) * nr, nr, 1, (long long)d.nm * nr * nt) &&
+                     (!kCo || d.item0 + u / bpi < d.coef_items),
+              kRgSweepR, line);
+    if (line < line0 + nlines && lok) {
       const int j = line % nt;
       const int l = line / (nt * ne);
       double* __restrict__ fl = d.f2 + (long long)slot * d.ncell + (long long)line * nr;
@@ -155,7 +163,17 @@ __global__ void __launch_bounds__(256) k_sweep_p(Dev d, double dts, unsigned cha
     const int line = line0 + (int)(u % bpi) * blockDim.x + threadIdx.x;
     unsigned long long q = 0ULL;  // CFL quotient bits
     unsigned nclip = 0;  // clip events (kRec == kRecCount)
-    if (line < line0 + nlines) {
+    // bounds-checked builds: the line's cells, its GPT and CA columns, the
+    // coefficient store's item
+    const bool lok = line >= line0 + nlines ||
+        rg_ok(d, rg_item(d, item) &&
+                     rg_span((long long)(line / (nr - 1)) * nt * nr + 1 + line % (nr - 1), nt, nr, d.ncell) &&
+                     rg_span((long long)(line / (nr - 1) / ne) * nt * nr + 1 + line % (nr - 1), nt, nr,
+                             (long long)nr * nt * d.npa) &&
+                     rg_span((long long)item.x * nt * nr + 1 + line % (nr - 1), nt, nr, (long long)d.nm * nr * nt) &&
+                     (!kCo || d.item0 + u / bpi < d.coef_items),
+              kRgSweepP, line);
+    if (line < line0 + nlines && lok) {
       const int i = 1 + line % (nr - 1);
       const int kl = line / (nr - 1);
       const int k = kl % ne, l = kl / ne;
@@ -266,7 +284,18 @@ __global__ void __launch_bounds__(256) k_sweep_e(Dev d, double dts, unsigned cha
     const int line = line0 + (int)(u % bpi) * blockDim.x + threadIdx.x;
     unsigned long long q = 0ULL;  // CFL quotient bits
     unsigned nclip = 0;  // clip events (kRec == kRecCount)
-    if (line < line0 + nlines) {
+    // bounds-checked builds: the line's cells, its (I,J,L) table entry and
+    // UE, its EDOT column, the coefficient store's item
+    const bool lok = line >= line0 + nlines ||
+        rg_ok(d, rg_item(d, item) &&
+                     rg_span(((long long)(line / (nr - 1) / nt) * ne * nt + (line / (nr - 1)) % nt) * nr + 1 +
+                                 line % (nr - 1), ne, (long long)nt * nr, d.ncell) &&
+                     rg_span((long long)item.x * nr * nt * d.npa + (long long)(line / (nr - 1)) * nr + 1 +
+                                 line % (nr - 1), 1, 1, (long long)d.nm * nr * nt * d.npa) &&
+                     rg_span((long long)item.y * ne * nr + 1 + line % (nr - 1), ne, nr, (long long)d.ns * ne * nr) &&
+                     (!kCo || d.item0 + u / bpi < d.coef_items),
+              kRgSweepE, line);
+    if (line < line0 + nlines && lok) {
       const int i = 1 + line % (nr - 1);
       const int jl = line / (nr - 1);
       const int j = jl % nt, l = jl / nt;
@@ -385,7 +414,18 @@ __global__ void __launch_bounds__(256) k_sweep_mu(Dev d, double dts, const doubl
     const int2 item = d.items[u / bpi];
     const int m = item.x, s = item.y, slot = m * d.ns + s;
     const int line = (int)(u % bpi) * lpb + (int)threadIdx.x / kSplit;
-    const bool active = line < nlines;
+    // bounds-checked builds: the line's cells, its WM and UM columns, the
+    // coefficient store's item (the lanes sharing a line test the same)
+    const bool active = line < nlines &&
+        rg_ok(d, rg_item(d, item) &&
+                     rg_span((long long)(line / (nr - 1)) * nr + 1 + line % (nr - 1), npa, (long long)ne * nt * nr,
+                             d.ncell) &&
+                     rg_span((long long)((line / (nr - 1)) % nt) * nr + 1 + line % (nr - 1), npa, (long long)nt * nr,
+                             (long long)nr * nt * npa) &&
+                     rg_span((long long)item.x * nt * nr * npa + ((line / (nr - 1)) % nt) * nr + 1 + line % (nr - 1),
+                             npa, (long long)nt * nr, (long long)d.nm * nr * nt * npa) &&
+                     (!kCo || d.item0 + u / bpi < d.coef_items),
+              kRgSweepMu, line);
     unsigned long long q = 0ULL;  // CFL quotient bits
     unsigned nclip = 0;  // clip events (kRec == kRecCount)
     const int lc = active ? line : 0;

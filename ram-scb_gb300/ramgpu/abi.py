@@ -42,7 +42,7 @@ EXPORTS = (
     "ramgpu_set_pipeline_groups", "ramgpu_pipeline_groups",
     "ramgpu_set_step_groups", "ramgpu_step_groups", "ramgpu_set_pipeline_trace", "ramgpu_pipeline_trace",
     "ramgpu_check", "ramgpu_set_check", "ramgpu_last_status",
-    "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_adj_overlap", "ramgpu_set_mu_lanes",
+    "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_adj_overlap", "ramgpu_bounds_report", "ramgpu_set_mu_lanes",
     "ramgpu_selftest_arith",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
@@ -204,6 +204,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_set_adj_record_budget": ([vp, C.c_longlong], i),
         "ramgpu_adj_segments": ([vp, ip, ip], i),
         "ramgpu_set_adj_overlap": ([vp, i], i),
+        "ramgpu_bounds_report": ([vp, ip, C.POINTER(C.c_longlong), ip, C.POINTER(C.c_longlong)], i),
         "ramgpu_set_mu_lanes": ([vp, i], i),
         "ramgpu_selftest_arith": ([C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)], i),
     }
@@ -724,6 +725,16 @@ class RamGpu:
         the free device memory; small: one segment, every earlier segment is
         recomputed)."""
         self._ck(self.lib.ramgpu_set_adj_record_budget(self.h, int(nbytes)), "set_adj_record_budget")
+
+    def bounds_report(self) -> dict:
+        """The bounds-checked build's log (ramgpu_bounds_report): checked
+        (1 in libramgpu_bounds.so), failures, the first failed check and its
+        line."""
+        ck, ch = C.c_int(), C.c_int()
+        fl, va = C.c_longlong(), C.c_longlong()
+        self._ck(self.lib.ramgpu_bounds_report(self.h, C.byref(ck), C.byref(fl), C.byref(ch), C.byref(va)),
+                 "bounds_report")
+        return {"checked": ck.value, "failures": fl.value, "check": ch.value, "value": va.value}
 
     def set_adj_overlap(self, on: bool):
         """Recompute segment s-1 on a second stream while segment s is

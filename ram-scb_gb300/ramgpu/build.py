@@ -17,6 +17,9 @@ REPO_ROOT = PKG_ROOT.parent
 CSRC = PKG_ROOT / "csrc"
 LIB_DIR = PKG_ROOT / "lib"
 LIB_PATH = LIB_DIR / "libramgpu.so"
+# the same library with every streamed line's index ranges tested in the
+# sweep and transposed-sweep kernels (RAMGPU_BOUNDS_CHECK); for tests
+LIB_BOUNDS_PATH = LIB_DIR / "libramgpu_bounds.so"
 SOURCES = ["abi.cu", "sweeps.cu", "tables.cu", "adjoint.cu", "noalloc.cu", "outputs.cu", "padif.cu", "bounce.cu",
            "selftest.cu", "status.cu", "layout.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -44,10 +47,13 @@ def _stale(target: Path, deps) -> bool:
     return any(Path(p).stat().st_mtime > t for p in deps)
 
 
-def build_library(force: bool = False, verbose: bool = False) -> Path:
-    """Compile csrc/*.cu for sm_103a and link libramgpu.so (in-tree)."""
+def build_library(force: bool = False, verbose: bool = False, bounds: bool = False) -> Path:
+    """Compile csrc/*.cu for sm_103a and link libramgpu.so (in-tree); with
+    bounds, the bounds-checked libramgpu_bounds.so."""
     nvcc = nvcc_path()
-    obj_dir = LIB_DIR / "obj"
+    obj_dir = LIB_DIR / ("obj_bounds" if bounds else "obj")
+    lib_path = LIB_BOUNDS_PATH if bounds else LIB_PATH
+    extra = ["-DRAMGPU_BOUNDS_CHECK"] if bounds else []
     obj_dir.mkdir(parents=True, exist_ok=True)
     headers = list(CSRC.glob("*.cuh")) + [REPO_ROOT / "include" / "ramgpu.h"]
     jobs = []
@@ -55,8 +61,8 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
         s = CSRC / src
         o = obj_dir / (src + ".o")
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(src, []), "-I", str(REPO_ROOT / "include"), "-c",
-                         str(s), "-o", str(o)])
+            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, *extra, *FILE_FLAGS.get(src, []), "-I", str(REPO_ROOT / "include"),
+                         "-c", str(s), "-o", str(o)])
 
     def run(cmd):
         if verbose:
@@ -69,10 +75,17 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         list(ex.map(run, jobs))
     objs = [str(obj_dir / (s + ".o")) for s in SOURCES]
-    if force or jobs or _stale(LIB_PATH, objs):
-        run([nvcc, *ARCH, "-shared", "-o", str(LIB_PATH), *objs, "-lcudart"])
-    return LIB_PATH
+    if force or jobs or _stale(lib_path, objs):
+        run([nvcc, *ARCH, "-shared", "-o", str(lib_path), *objs, "-lcudart"])
+    return lib_path
+
+
+def build_all(force: bool = False, verbose: bool = False) -> list[Path]:
+    """Both libraries, compiled concurrently."""
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        futs = [ex.submit(build_library, force, verbose, b) for b in (False, True)]
+        return [f.result() for f in futs]
 
 
 if __name__ == "__main__":
-    print(build_library(force=True, verbose=True))
+    print(build_all(force=True, verbose=True))

@@ -19,10 +19,13 @@ def test_header_and_binding_agree():
     assert declared_symbols() == sorted(abi.EXPORTS)
 
 
-def test_library_exports_every_symbol():
-    if not build.LIB_PATH.exists():
-        build.build_library()
-    lib = ctypes.CDLL(str(build.LIB_PATH))
+@pytest.mark.parametrize("bounds", [False, True])
+def test_library_exports_every_symbol(bounds):
+    """Both the release library and the bounds-checked one."""
+    path = build.LIB_BOUNDS_PATH if bounds else build.LIB_PATH
+    if not path.exists():
+        build.build_library(bounds=bounds)
+    lib = ctypes.CDLL(str(path))
     missing = [s for s in declared_symbols() if not hasattr(lib, s)]
     assert not missing, missing
 
