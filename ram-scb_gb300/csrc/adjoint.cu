@@ -78,6 +78,15 @@ __device__ __forceinline__ void face_acc(double FBb, bool neg, int cs, double ak
 // Sweeps (bit w: R, P, E, MU) whose transposes form ak and m on the
 // integer pipe.
 constexpr unsigned kAdjIntMask = 0xAu;
+// Sweeps whose transposes form the face product FBb = C*DL (and, in E, the
+// coefficient's EDOT product) with mul_rn_int, the FP64 product bit for bit
+// on the integer pipe.  Measured on GB300: E gains slightly; in R the
+// lighter kernel fits seven CTAs per SM instead of six and its lane-strided
+// lines then miss in L1 (four times slower), so R keeps the FP64 product.
+constexpr unsigned kAdjMulIntMask = 0x4u;
+__device__ __forceinline__ double adj_mul(unsigned bit, double a, double b) {
+  return (kAdjMulIntMask & bit) ? mul_rn_int(a, b) : a * b;
+}
 constexpr bits64 kNaNBits = 0x7FF8000000000000ULL;
 
 // |v| 2^-52 (v < 2^63) as the bits of a double with the given sign.
@@ -233,7 +242,7 @@ __global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __
       if (kAdjIntMask & 1u)
         face_acc_a(C * (le1 - le0), neg, cs, corr_a_fix(dbits(C) & kAbsMask, neg), beta, cm1, c0, c1, c2);
       else
-        face_acc(C * (le1 - le0), neg, cs, face_ak<false>(C, neg, cs, -0.5, bmh, hb), cm1, c0, c1, c2);
+        face_acc(adj_mul(1u, C, le1 - le0), neg, cs, face_ak<false>(C, neg, cs, -0.5, bmh, hb), cm1, c0, c1, c2);
     };
     auto advance = [&](int f, double le3) {  // cell f-1 is final; cell f+3 enters
       lam[f - 2] = cm1;
@@ -414,7 +423,7 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
     const BetaBits beta(d.betalim);
     const bool closed = d.flags & 1u;
     const int n = ne;
-#define EC(K) (edot[(long long)((K)-1) * nr] * fma(eb[(K)-1], wet, ue))
+#define EC(K) adj_mul(4u, edot[(long long)((K)-1) * nr], fma(eb[(K)-1], wet, ue))
 #define ELE(K) masked(lam, rl, (long long)((K)-1) * st, rsh)
     const double out1 = lam[0];
     // wl(K) = le(K)/WE(K) for K = 2..NE, 0 elsewhere; window = cells K-1..K+2
@@ -433,7 +442,7 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
         if (kCo == 1) csa[(long long)(K - 1) * st] = bitsd(a);
         face_acc_a(C * (wl1 - wl0), neg, cs, a, beta, cm1, c0, c1, c2);
       } else {
-        face_acc(C * (wl1 - wl0), neg, cs, face_ak<true>(C, neg, cs, d.mhde[K - 1], d.bmhde[K - 1], hb), cm1, c0,
+        face_acc(adj_mul(4u, C, wl1 - wl0), neg, cs, face_ak<true>(C, neg, cs, d.mhde[K - 1], d.bmhde[K - 1], hb), cm1, c0,
                  c1, c2);
       }
     };
