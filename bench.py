@@ -51,14 +51,14 @@ NCU_CAPTURE = {
     # ncu on the sources named by sources_sha16 (profiles/sweeps_four_sp.md,
     # profiles/driftr_refined.md): one kernel per command, each captured
     # launch advances one species, so a four-species launch is scaled by 4.
-    "sources_sha16": "2540ea28841301a8",
+    "sources_sha16": "0e986e1de47377a3",
     "command": ("ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum,"
                 "smsp__sass_thread_inst_executed_op_{dadd,dfma,dmul}_pred_on.sum --clock-control none "
                 "-k regex:k_sweep_<r|p|e|mu> -c 2 python bench.py --steps 2 --warmup 1 --sections headline "
                 "--no-cpu-baseline --no-e2e --no-autotune [--workload refined]"),
-    "dram_bytes": {"four_sp": {"driftr": 4 * 11.02e6, "driftp": 4 * 0.5 * (10.39e6 + 10.40e6),
+    "dram_bytes": {"four_sp": {"driftr": 4 * 11.02e6, "driftp": 4 * 10.39e6,
                                "drifte": 4 * 0.5 * (11.34e6 + 29.98e6), "driftmu": 4 * 0.5 * (20.47e6 + 10.52e6)},
-                   "refined": {"driftr": 4 * 0.5 * (268.3e6 + 267.9e6)}},
+                   "refined": {"driftr": 4 * 0.5 * (267.84e6 + 268.13e6)}},
     "fp64_ops_per_cell": {"driftr": 5.02, "driftp": 4.64, "drifte": 0.5 * (6.70 + 4.78),
                           "driftmu": 0.5 * (6.62 + 5.69)},
 }
@@ -938,6 +938,7 @@ def run_adjoint_batched(args, torch, np, abi, W, stream):
     gpu.adj_forward(nc, base.dts, kp, kc, obs)
     gf, gb = gpu.adj_backward()
     batched_s = stop()
+    nseg, nkeep = gpu.adj_segments()
     gpu.close()
     # looped: the same gradients one member at a time
     sub = list(range(0, nm, max(1, nm // 4)))[:4]
@@ -959,7 +960,8 @@ def run_adjoint_batched(args, torch, np, abi, W, stream):
     solo.close()
     looped = 1.0 / statistics.mean(loop_s)
     return {"members": nm, "member_species": int(sum(len(x) for x in ens.species)), "window_calls": nc,
-            "checkpoint_calls": kc, "observations": len(obs), "forward_s": fwd_s, "adjoint_s": batched_s,
+            "checkpoint_calls": kc, "observations": len(obs), "segments": nseg, "segments_kept": nkeep,
+            "forward_s": fwd_s, "adjoint_s": batched_s,
             "adjoint_over_forward": batched_s / fwd_s,
             "member_gradients_per_s_batched": nm / batched_s, "member_gradients_per_s_looped": looped,
             "batched_over_looped": (nm / batched_s) / looped,
