@@ -413,6 +413,14 @@ typedef struct {
 /* Runs the pass now (synchronises) and fills *st (may be NULL); returns
  * RAMGPU_ERR_NUMERIC when a non-finite value was found, else RAMGPU_OK. */
 int ramgpu_check(ramgpu_ctx *ctx, ramgpu_status *st);
+/* F2 diagnostics of (member, s) in one device pass (no reference
+ * counterpart: the reductions the reference's logs would need, done where
+ * F2 lives): the smallest and largest F2 over all cells (exact), and the
+ * number content, the sum of F2*WE(K)*WMU(L) over the cells the sweeps
+ * update (I >= 2, J <= NT-1, K >= 2, 2 <= L <= NPA-1), which closed
+ * boundaries conserve.  The sum runs in a fixed order: the same bits on
+ * every call.  Any output may be NULL; synchronises the context's stream. */
+int ramgpu_f2_stats(ramgpu_ctx *ctx, int member, int s, double *f2_min, double *f2_max, double *content);
 /* With enable != 0 every ramgpu_ram_run / _async / ramgpu_ram_run_host
  * appends the pass to the call (inside its graph); ramgpu_ram_run and
  * ramgpu_ram_run_host then return RAMGPU_ERR_NUMERIC after a call that

@@ -36,6 +36,7 @@
 
 #include "../../include/ramgpu.h"
 #include "kernels.cuh"
+#include "diag.cuh"
 
 using namespace ramgpu;
 
@@ -170,6 +171,9 @@ struct ramgpu_ctx {
   // status word: device words and their page-locked copy; the pass is
   // appended to every call while check_on
   unsigned long long* status_d = nullptr;
+  // ramgpu_f2_stats: the partial content sums and the min/max keys
+  double* stat_part = nullptr;
+  unsigned long long* stat_mm = nullptr;
   unsigned long long* status_h = nullptr;
   bool check_on = false;
   bool status_valid = false;
@@ -1074,6 +1078,8 @@ int ramgpu_create(const ramgpu_config* cfg, ramgpu_ctx** out) {
   ctx->losses = dalloc<double>(ctx, nslot * 6, &ok);
   ctx->sumrc_part = dalloc<double>(ctx, (size_t)kSumrcStages * nslot * kSumrcBlocks, &ok);
   ctx->status_d = dalloc<unsigned long long>(ctx, 5, &ok);
+  ctx->stat_part = dalloc<double>(ctx, kF2StatBlocks, &ok);
+  ctx->stat_mm = dalloc<unsigned long long>(ctx, 2, &ok);
   if (ok && cudaHostAlloc(&ctx->status_h, 5 * sizeof(unsigned long long), cudaHostAllocDefault) != cudaSuccess) {
     cudaGetLastError();
     ctx->status_h = nullptr;
@@ -2048,6 +2054,26 @@ int ramgpu_moments(ramgpu_ctx* ctx, int member, int s, double* ppert, double* pp
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemcpy(ppert, ctx->d.ppert + o, n * sizeof(double), cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(ppart, ctx->d.ppart + o, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return RAMGPU_OK;
+}
+
+int ramgpu_f2_stats(ramgpu_ctx* ctx, int member, int s, double* f2_min, double* f2_max, double* content) {
+  if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
+  if (int rc = check_ms(ctx, member, s)) return rc;
+  if (!ctx->have_grid) return fail(ctx, RAMGPU_ERR_STATE, "grid not set");
+  launch_f2_stats(ctx->d, (long long)member * ctx->d.ns + s, ctx->stat_part, ctx->stat_mm, ctx->stream);
+  ctx->launches += 1;
+  CKL("f2 statistics");
+  double part[kF2StatBlocks];
+  unsigned long long mm[2];
+  CK(cudaMemcpyAsync(part, ctx->stat_part, sizeof part, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(mm, ctx->stat_mm, sizeof mm, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  double sum = 0.0;
+  for (int b = 0; b < kF2StatBlocks; ++b) sum += part[b];  // fixed order
+  if (f2_min) *f2_min = f2_stats_key_value(mm[0]);
+  if (f2_max) *f2_max = f2_stats_key_value(mm[1]);
+  if (content) *content = sum;
   return RAMGPU_OK;
 }
 

@@ -17,7 +17,10 @@
 //          the same lines of DRIFTP/E/MU), counted while the status pass is
 //          appended to each call.
 // Integer tests on the exponent bits: no FP64 work, one read of F2.
+#include <string.h>
+
 #include "kernels.cuh"
+#include "diag.cuh"
 
 namespace ramgpu {
 
@@ -71,6 +74,79 @@ void launch_status(const Dev& d, unsigned long long* st, cudaStream_t s) {
   long long gx = (d.ncell + 256LL * 16 - 1) / (256LL * 16);  // 16 cells per thread
   gx = gx < 1 ? 1 : (gx > 4096 ? 4096 : gx);
   k_status<<<dim3((unsigned)gx, (unsigned)d.nitems), 256, 0, s>>>(d, st);
+}
+
+// ------------------------------------------------------------ F2 statistics
+// One (member, species) slot: the smallest and largest F2 over all cells
+// and the number content, the sum of F2*WE(K)*WMU(L) over the cells the
+// sweeps update (I >= 2, J <= NT-1 with J = NT the periodic copy of J = 1,
+// K >= 2, 2 <= L <= NPA-1), the quantity closed boundaries conserve.  Each
+// block sums a fixed set of cells in a fixed order and reduces through
+// shared memory in a fixed tree, so the partials, and the host's ordered sum
+// of them, are the same bits on every call.  Min and max go through an
+// order-preserving integer key (sign-magnitude to two's-complement order).
+namespace {
+__device__ __forceinline__ bits64 order_key(double v) {
+  const bits64 b = dbits(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+}  // namespace
+
+__global__ void __launch_bounds__(256) k_f2_stats(Dev d, long long slot, double* __restrict__ part,
+                                                  unsigned long long* __restrict__ mm) {
+  __shared__ double sh[256];
+  __shared__ unsigned long long smin[8], smax[8];
+  const double* __restrict__ f = d.f2 + slot * d.ncell;
+  const long long nrt = (long long)d.nr * d.nt, nrte = nrt * d.ne;
+  double acc = 0.0;
+  bits64 kmin = ~0ULL, kmax = 0ULL;
+  for (long long c = blockIdx.x * 256LL + threadIdx.x; c < d.ncell; c += 256LL * gridDim.x) {
+    const double v = __ldg(f + c);
+    const bits64 k = order_key(v);
+    kmin = k < kmin ? k : kmin;
+    kmax = k > kmax ? k : kmax;
+    const int i = (int)(c % d.nr), j = (int)((c / d.nr) % d.nt);
+    const int k3 = (int)((c / nrt) % d.ne), l = (int)(c / nrte);
+    if (i >= 1 && j <= d.nt - 2 && k3 >= 1 && l >= 1 && l <= d.npa - 2) acc = fma(v, d.we[k3] * d.wmu[l], acc);
+  }
+  sh[threadIdx.x] = acc;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const bits64 a = __shfl_xor_sync(0xffffffffu, kmin, o), b = __shfl_xor_sync(0xffffffffu, kmax, o);
+    kmin = a < kmin ? a : kmin;
+    kmax = b > kmax ? b : kmax;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    smin[threadIdx.x >> 5] = kmin;
+    smax[threadIdx.x >> 5] = kmax;
+  }
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = sh[0];
+    for (int w = 1; w < 8; ++w) {
+      kmin = smin[w] < kmin ? smin[w] : kmin;
+      kmax = smax[w] > kmax ? smax[w] : kmax;
+    }
+    atomicMin(&mm[0], smin[0] < kmin ? smin[0] : kmin);
+    atomicMax(&mm[1], smax[0] > kmax ? smax[0] : kmax);
+  }
+}
+
+double f2_stats_key_value(unsigned long long k) {
+  const unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFULL) : ~k;
+  double v;
+  memcpy(&v, &b, sizeof v);
+  return v;
+}
+
+void launch_f2_stats(const Dev& d, long long slot, double* part, unsigned long long* mm, cudaStream_t s) {
+  cudaMemsetAsync(mm, 0xff, sizeof(unsigned long long), s);                          // min key
+  cudaMemsetAsync(mm + 1, 0, sizeof(unsigned long long), s);                         // max key
+  k_f2_stats<<<kF2StatBlocks, 256, 0, s>>>(d, slot, part, mm);
 }
 
 }  // namespace ramgpu

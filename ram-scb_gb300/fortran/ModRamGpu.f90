@@ -277,6 +277,14 @@ module ModRamGpu
        type(c_ptr), value :: ctx
        type(ramgpu_status), intent(out) :: st
      end function
+     ! F2 diagnostics of (member, s): min, max, number content sum F2*WE*WMU
+     integer(c_int) function ramgpu_f2_stats(ctx, member, s, f2_min, f2_max, content) &
+          bind(C, name="ramgpu_f2_stats")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: member, s
+       real(c_double), intent(out) :: f2_min, f2_max, content
+     end function
      integer(c_int) function ramgpu_set_check(ctx, enable) bind(C, name="ramgpu_set_check")
        import :: c_int, c_ptr
        type(c_ptr), value :: ctx

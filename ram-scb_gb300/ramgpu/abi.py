@@ -42,7 +42,8 @@ EXPORTS = (
     "ramgpu_set_pipeline_groups", "ramgpu_pipeline_groups",
     "ramgpu_set_step_groups", "ramgpu_step_groups", "ramgpu_set_pipeline_trace", "ramgpu_pipeline_trace",
     "ramgpu_check", "ramgpu_set_check", "ramgpu_last_status",
-    "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_adj_overlap", "ramgpu_bounds_report", "ramgpu_set_mu_lanes",
+    "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_adj_overlap", "ramgpu_bounds_report",
+    "ramgpu_f2_stats", "ramgpu_set_mu_lanes",
     "ramgpu_selftest_arith",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
@@ -205,6 +206,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_adj_segments": ([vp, ip, ip], i),
         "ramgpu_set_adj_overlap": ([vp, i], i),
         "ramgpu_bounds_report": ([vp, ip, C.POINTER(C.c_longlong), ip, C.POINTER(C.c_longlong)], i),
+        "ramgpu_f2_stats": ([vp, i, i, dp, dp, dp], i),
         "ramgpu_set_mu_lanes": ([vp, i], i),
         "ramgpu_selftest_arith": ([C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)], i),
     }
@@ -725,6 +727,14 @@ class RamGpu:
         the free device memory; small: one segment, every earlier segment is
         recomputed)."""
         self._ck(self.lib.ramgpu_set_adj_record_budget(self.h, int(nbytes)), "set_adj_record_budget")
+
+    def f2_stats(self, member: int, s: int):
+        """(smallest F2, largest F2, number content sum F2*WE*WMU over the
+        updated cells) of (member, s), one device pass (ramgpu_f2_stats)."""
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        self._ck(self.lib.ramgpu_f2_stats(self.h, int(member), int(s), C.byref(a), C.byref(b), C.byref(c)),
+                 "f2_stats")
+        return a.value, b.value, c.value
 
     def bounds_report(self) -> dict:
         """The bounds-checked build's log (ramgpu_bounds_report): checked
