@@ -77,12 +77,11 @@ __device__ __forceinline__ void face_acc(double FBb, bool neg, int cs, double ak
 
 // Sweeps (bit w: R, P, E, MU) whose transposes form ak and m on the
 // integer pipe.
-constexpr unsigned kAdjIntMask = 0xAu;
+constexpr unsigned kAdjIntMask = 0xBu;
 // Sweeps whose transposes form the face product FBb = C*DL (and, in E, the
 // coefficient's EDOT product) with mul_rn_int, the FP64 product bit for bit
-// on the integer pipe.  Measured on GB300: E gains slightly; in R the
-// lighter kernel fits seven CTAs per SM instead of six and its lane-strided
-// lines then miss in L1 (four times slower), so R keeps the FP64 product.
+// on the integer pipe.  Measured on GB300 over the whole adjoint window: E
+// gains slightly, R (shared-memory tiles, integer weights) loses.
 constexpr unsigned kAdjMulIntMask = 0x4u;
 __device__ __forceinline__ double adj_mul(unsigned bit, double a, double b) {
   return (kAdjMulIntMask & bit) ? mul_rn_int(a, b) : a * b;
@@ -201,87 +200,130 @@ __device__ __forceinline__ double masked(const double* __restrict__ lam, const u
 // inflow lines); FBND(1) = F(2) on inflow lines, FBND(NR) = F(NR) on outflow
 // lines (both 0 when closed).  The ghosts' adjoints go to dJ/dFGEOS, for an
 // outflow line to the FGEOS cell its stale ghost came from.
-// kNc (NR a multiple of 4): a line is NR doubles at a multiple of NR, so it
-// owns whole sectors and lambda can be read ahead through the read-only path.
-// Six resident CTAs per SM as the register target: without it the compiler
-// aims at a higher occupancy and spills the window (measured slower).
-template <bool kNc, int rsh>
-__global__ void __launch_bounds__(128, 6) k_adj_r(Dev d, const unsigned char* __restrict__ rec) {
+// A CTA takes blockDim.x consecutive lines of one item.  They are contiguous
+// in memory (blockDim.x*NR doubles of lambda and as many record bytes), so
+// the CTA loads them into shared memory with coalesced loads, each thread
+// transposes its line there, and the CTA stores the tile back coalesced.
+// Read in place, the lanes' lines lie 8*NR bytes apart: every warp load
+// touches 32 sectors and leans on L1, and at seven CTAs per SM L1 no longer
+// held them (four times slower).  Rows of the lambda tile are NR|1 doubles
+// apart, so the 8-byte accesses of a half-warp fall in distinct banks.
+#ifdef RAMGPU_BOUNDS_CHECK
+constexpr bool kBoundsChecked = true;
+#else
+constexpr bool kBoundsChecked = false;
+#endif
+size_t adj_r_smem(const Dev& d, int threads) {
+  return (size_t)threads * (size_t)(d.nr | 1) * sizeof(double) + (size_t)threads * (size_t)d.nr;
+}
+template <int rsh>
+__global__ void __launch_bounds__(128) k_adj_r(Dev d, const unsigned char* __restrict__ rec) {
+  extern __shared__ double tile[];
   const int nr = d.nr, nt = d.nt, ne = d.ne;
+  const int ts = nr | 1;
+  unsigned char* rtile = (unsigned char*)(tile + (size_t)blockDim.x * ts);
   const int nlines = nt * ne * d.npa;
-  WORK_LOOP(nlines) {
+  const int bpi = (nlines + blockDim.x - 1) / blockDim.x;
+  const long long nunits = (long long)bpi * d.nitems;
+  for (long long u = blockIdx.x + (long long)blockIdx.y * gridDim.x; u < nunits;
+       u += (long long)gridDim.x * gridDim.y) {  // uniform across the CTA
     const int2 item = d.items[u / bpi];
     const int m = item.x, s = item.y, slot = m * d.ns + s;
-    const int line = (int)(u % bpi) * blockDim.x + threadIdx.x;
-    if (line >= nlines) continue;
+    const int lfirst = (int)(u % bpi) * blockDim.x;
+    const int nl = min((int)blockDim.x, nlines - lfirst);
+    // bounds-checked builds: the tile's cells (the whole CTA skips it)
+    if (kBoundsChecked) {
+      const bool ok = rg_item(d, item) && rg_span((long long)lfirst * nr, (long long)nl * nr, 1, d.ncell);
+      if (threadIdx.x == 0) rg_ok(d, ok, kRgAdjR, lfirst);
+      if (!ok) continue;
+    }
+    double* __restrict__ gl = d.lam + (long long)slot * d.ncell + (long long)lfirst * nr;
+    const unsigned char* __restrict__ gr = rec + (u / bpi) * d.ncell + (long long)lfirst * nr;
+    for (int e = threadIdx.x; e < nl * nr; e += blockDim.x) {
+      const int ln = e / nr;
+      tile[ln * ts + (e - ln * nr)] = gl[e];
+      rtile[e] = __ldg(gr + e);
+    }
+    __syncthreads();
+    const int line = lfirst + threadIdx.x;
     const int j = line % nt, k = (line / nt) % ne, l = line / (nt * ne);
-    // bounds-checked builds: the line's cells, its GRT and CR rows
-    if (!rg_ok(d, rg_item(d, item) && rg_span((long long)line * nr, nr, 1, d.ncell) &&
-                      rg_span(((long long)l * nt + j) * nr, nr, 1, (long long)nr * nt * d.npa) &&
+    // bounds-checked builds: the line's GRT and CR rows
+    const bool lok = threadIdx.x < nl &&
+        (!kBoundsChecked ||
+         rg_ok(d, rg_span(((long long)l * nt + j) * nr, nr, 1, (long long)nr * nt * d.npa) &&
                       rg_span(((long long)m * nt + j) * nr, nr, 1, (long long)d.nm * nr * nt),
-               kRgAdjR, line))
-      continue;
-    double* __restrict__ lam = d.lam + (long long)slot * d.ncell + (long long)line * nr;
-    const unsigned char* __restrict__ rl = rec + (u / bpi) * d.ncell + (long long)line * nr;
-    const double* __restrict__ grt = d.grt + ((long long)l * nt + j) * nr;
-    const double* __restrict__ cr = d.cr + ((long long)m * nt + j) * nr;
-    const double p4 = d.p4[s * ne + k];
-    const double hb = 0.5 * d.betalim, bmh = -hb;
-    const BetaBits beta(d.betalim);
-    const bool closed = d.flags & 1u;
-    const int n = nr;  // >= 4
-    const double cN = fma(grt[n - 1], p4, cr[n - 1]);
-    const bool inflow = is_neg(cN);
-    // le(i) = lambda of updated, unclipped cell i (i = 2..NR); window = cells f-1..f+2
-    double le0 = masked<kNc>(lam, rl, 1, rsh), le1 = masked<kNc>(lam, rl, 2, rsh), le2 = masked<kNc>(lam, rl, 3, rsh);
-    double cm1 = lam[0], c0 = le0, c1 = le1, c2 = le2;
-    if (inflow && !closed) c0 += fma(grt[0], p4, cr[0]) * le0;  // FBND(1) = F(2)
-    auto face = [&](int f, double C) {
-      const bool neg = is_neg(C);
-      const int cs = (rl[f - 1] >> rsh) & 7;
-      if (kAdjIntMask & 1u)
-        face_acc_a(C * (le1 - le0), neg, cs, corr_a_fix(dbits(C) & kAbsMask, neg), beta, cm1, c0, c1, c2);
-      else
-        face_acc(adj_mul(1u, C, le1 - le0), neg, cs, face_ak<false>(C, neg, cs, -0.5, bmh, hb), cm1, c0, c1, c2);
-    };
-    auto advance = [&](int f, double le3) {  // cell f-1 is final; cell f+3 enters
-      lam[f - 2] = cm1;
-      cm1 = c0; c0 = c1; c1 = c2; c2 = le3;
-      le0 = le1; le1 = le2; le2 = le3;
-    };
-    int f = 2;
-    for (; f <= n - 3; ++f) {
-      face(f, fma(grt[f - 1], p4, cr[f - 1]));
-      advance(f, masked<kNc>(lam, rl, f + 2, rsh));
-    }
-    for (; f <= n - 1; ++f) {
-      face(f, fma(grt[f - 1], p4, cr[f - 1]));
-      advance(f, 0.0);
-    }
-    // face NR: transposed on inflow lines, FBND(NR) = F(NR) on outflow lines
-    if (!closed) {
-      if (inflow) face(n, cN);
-      else c0 -= cN * le0;
-    }
-    lam[n - 2] = cm1;
-    lam[n - 1] = c0;
-    const double gN1 = c1, gN2 = c2;  // ghosts F(NR+1), F(NR+2)
-    const long long nfg = (long long)nt * ne * d.npa;
-    if (inflow) {
-      if (d.outside[(long long)j * nr + n - 1] != 1) {
-        const double fh = d.fnhs[((long long)l * nt + j) * d.nf + n - 1];
-        atomicAdd(&d.gfg[slot * nfg + line], d.conf1 * fh * gN1 + d.conf2 * fh * gN2);
+               kRgAdjR, line));
+    if (lok) {
+      double* lam = tile + threadIdx.x * ts;
+      const unsigned char* rl = rtile + threadIdx.x * nr;
+      const double* __restrict__ grt = d.grt + ((long long)l * nt + j) * nr;
+      const double* __restrict__ cr = d.cr + ((long long)m * nt + j) * nr;
+      const double p4 = d.p4[s * ne + k];
+      const double hb = 0.5 * d.betalim, bmh = -hb;
+      const BetaBits beta(d.betalim);
+      const bool closed = d.flags & 1u;
+      const int n = nr;  // >= 4
+      auto mk = [&](int c) { return ((rl[c] >> rsh) & kClipBit) ? 0.0 : lam[c]; };  // masked lambda
+      const double cN = fma(grt[n - 1], p4, cr[n - 1]);
+      const bool inflow = is_neg(cN);
+      // le(i) = lambda of updated, unclipped cell i (i = 2..NR); window = cells f-1..f+2
+      double le0 = mk(1), le1 = mk(2), le2 = mk(3);
+      double cm1 = lam[0], c0 = le0, c1 = le1, c2 = le2;
+      if (inflow && !closed) c0 += fma(grt[0], p4, cr[0]) * le0;  // FBND(1) = F(2)
+      auto face = [&](int f, double C) {
+        const bool neg = is_neg(C);
+        const int cs = (rl[f - 1] >> rsh) & 7;
+        if (kAdjIntMask & 1u)
+          face_acc_a(adj_mul(1u, C, le1 - le0), neg, cs, corr_a_fix(dbits(C) & kAbsMask, neg), beta, cm1, c0, c1,
+                     c2);
+        else
+          face_acc(adj_mul(1u, C, le1 - le0), neg, cs, face_ak<false>(C, neg, cs, -0.5, bmh, hb), cm1, c0, c1, c2);
+      };
+      auto advance = [&](int f, double le3) {  // cell f-1 is final; cell f+3 enters
+        lam[f - 2] = cm1;
+        cm1 = c0; c0 = c1; c1 = c2; c2 = le3;
+        le0 = le1; le1 = le2; le2 = le3;
+      };
+      int f = 2;
+      for (; f <= n - 3; ++f) {
+        face(f, fma(grt[f - 1], p4, cr[f - 1]));
+        advance(f, mk(f + 2));
       }
-    } else if (gN1 != 0.0) {
-      const int src = stale_ghost_src(d, m, slot, j, k, l, p4);
-      if (src >= 0) {
-        const int jj = src % nt, ll = src / (nt * ne);
-        if (d.outside[(long long)jj * nr + n - 1] != 1) {
-          const double fh = d.fnhs[((long long)ll * nt + jj) * d.nf + n - 1];
-          atomicAdd(&d.gfg[slot * nfg + src], d.conf1 * fh * gN1);
+      for (; f <= n - 1; ++f) {
+        face(f, fma(grt[f - 1], p4, cr[f - 1]));
+        advance(f, 0.0);
+      }
+      // face NR: transposed on inflow lines, FBND(NR) = F(NR) on outflow lines
+      if (!closed) {
+        if (inflow) face(n, cN);
+        else c0 -= cN * le0;
+      }
+      lam[n - 2] = cm1;
+      lam[n - 1] = c0;
+      const double gN1 = c1, gN2 = c2;  // ghosts F(NR+1), F(NR+2)
+      const long long nfg = (long long)nt * ne * d.npa;
+      if (inflow) {
+        if (d.outside[(long long)j * nr + n - 1] != 1) {
+          const double fh = d.fnhs[((long long)l * nt + j) * d.nf + n - 1];
+          atomicAdd(&d.gfg[slot * nfg + line], d.conf1 * fh * gN1 + d.conf2 * fh * gN2);
+        }
+      } else if (gN1 != 0.0) {
+        const int src = stale_ghost_src(d, m, slot, j, k, l, p4);
+        if (src >= 0) {
+          const int jj = src % nt, ll = src / (nt * ne);
+          if (d.outside[(long long)jj * nr + n - 1] != 1) {
+            const double fh = d.fnhs[((long long)ll * nt + jj) * d.nf + n - 1];
+            atomicAdd(&d.gfg[slot * nfg + src], d.conf1 * fh * gN1);
+          }
         }
       }
     }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nl * nr; e += blockDim.x) {
+      const int ln = e / nr;
+      gl[e] = tile[ln * ts + (e - ln * nr)];
+    }
+    __syncthreads();  // the next unit reuses the tile
   }
 }
 
@@ -598,10 +640,7 @@ void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, int rsh, cu
   auto go = [&](auto sh) {
     constexpr int R = decltype(sh)::value;
     switch (w) {
-      case 0:
-        if (d.nr % 4 == 0) k_adj_r<true, R><<<g, blk, 0, st>>>(d, rec);
-        else k_adj_r<false, R><<<g, blk, 0, st>>>(d, rec);
-        break;
+      case 0: k_adj_r<R><<<g, blk, adj_r_smem(d, blk), st>>>(d, rec); break;
       case 1: k_adj_p<R><<<g, blk, 0, st>>>(d, rec); break;
       case 2:
         if (co == 1) k_adj_e<1, R><<<g, blk, 0, st>>>(d, rec);
