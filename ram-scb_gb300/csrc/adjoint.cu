@@ -80,8 +80,10 @@ __device__ __forceinline__ void face_acc(double FBb, bool neg, int cs, double ak
 constexpr unsigned kAdjIntMask = 0xBu;
 // Sweeps whose transposes form the face product FBb = C*DL (and, in E, the
 // coefficient's EDOT product) with mul_rn_int, the FP64 product bit for bit
-// on the integer pipe.  Measured on GB300 over the whole adjoint window: E
-// gains slightly, R (shared-memory tiles, integer weights) loses.
+// on the integer pipe.  Measured on GB300: the DRIFTE transposes that form
+// C gain, the one that loads C (fewer FP64 operations left) loses and keeps
+// the FP64 product (the bits are the same either way); R (shared-memory
+// tiles, integer weights) loses over the whole adjoint window.
 constexpr unsigned kAdjMulIntMask = 0x4u;
 __device__ __forceinline__ double adj_mul(unsigned bit, double a, double b) {
   return (kAdjMulIntMask & bit) ? mul_rn_int(a, b) : a * b;
@@ -484,8 +486,8 @@ __global__ void __launch_bounds__(128) k_adj_e(Dev d, const unsigned char* __res
         if (kCo == 1) csa[(long long)(K - 1) * st] = bitsd(a);
         face_acc_a(C * (wl1 - wl0), neg, cs, a, beta, cm1, c0, c1, c2);
       } else {
-        face_acc(adj_mul(4u, C, wl1 - wl0), neg, cs, face_ak<true>(C, neg, cs, d.mhde[K - 1], d.bmhde[K - 1], hb), cm1, c0,
-                 c1, c2);
+        face_acc(adj_mul(kCo == 2 ? 0u : 4u, C, wl1 - wl0), neg, cs,
+                 face_ak<true>(C, neg, cs, d.mhde[K - 1], d.bmhde[K - 1], hb), cm1, c0, c1, c2);
       }
     };
     auto shift = [&](double lec, double wl) {
