@@ -49,8 +49,9 @@ UNIT = "cell-updates/s"
 # digest; a changed kernel makes the figures stale until the next capture.
 NCU_CAPTURE = {
     # ncu on the sources named by sources_sha16 (profiles/sweeps_four_sp.md,
-    # profiles/driftr_refined.md): one kernel per command, each captured
-    # launch advances one species, so a four-species launch is scaled by 4.
+    # profiles/driftr_refined.md, profiles/sweeps_l2.md): one kernel per
+    # command, each captured launch advances one species, so a four-species
+    # launch of the timing pass is scaled by 4.
     "sources_sha16": "0e986e1de47377a3",
     "command": ("ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum,"
                 "smsp__sass_thread_inst_executed_op_{dadd,dfma,dmul}_pred_on.sum --clock-control none "
@@ -58,7 +59,14 @@ NCU_CAPTURE = {
                 "--no-cpu-baseline --no-e2e --no-autotune [--workload refined]"),
     "dram_bytes": {"four_sp": {"driftr": 4 * 11.02e6, "driftp": 4 * 10.39e6,
                                "drifte": 4 * 0.5 * (11.34e6 + 29.98e6), "driftmu": 4 * 0.5 * (20.47e6 + 10.52e6)},
+                   "single_h": {"driftr": 11.03e6, "driftp": 10.39e6,
+                                "drifte": 0.5 * (11.28e6 + 29.98e6), "driftmu": 0.5 * (20.47e6 + 10.52e6)},
                    "refined": {"driftr": 4 * 0.5 * (267.84e6 + 268.13e6)}},
+    # lts__t_bytes.sum per launch of the timing pass (profiles/sweeps_l2.md)
+    "l2_bytes": {"four_sp": {"driftr": 4 * 0.5 * (112.05e6 + 111.84e6), "driftp": 4 * 0.5 * (38.79e6 + 39.11e6),
+                             "drifte": 4 * 0.5 * (68.85e6 + 69.59e6), "driftmu": 4 * 0.5 * (77.47e6 + 58.90e6)},
+                 "single_h": {"driftr": 0.5 * (111.71e6 + 111.96e6), "driftp": 0.5 * (38.67e6 + 39.26e6),
+                              "drifte": 0.5 * (68.84e6 + 69.67e6), "driftmu": 0.5 * (77.55e6 + 59.12e6)}},
     "fp64_ops_per_cell": {"driftr": 5.02, "driftp": 4.64, "drifte": 0.5 * (6.70 + 4.78),
                           "driftmu": 0.5 * (6.62 + 5.69)},
 }
@@ -356,9 +364,10 @@ def kernel_pass(torch, gpu, stream, wl, flush, n):
     return kt, statistics.mean(ms)
 
 
-def roofline(kt, wl, nitems, hbm_peak, peak_kind, fp64_peak, workload):
+def roofline(kt, wl, nitems, hbm_peak, peak_kind, fp64_peak, workload, l2_peak=None):
     """HBM view of the dominant sweep: 16 B per cell (F2 read + write once)
-    over its event-timed launch; the FP64 view beside it."""
+    over its event-timed launch; the FP64 view and the L2 view (the ncu L2
+    bytes of the same launch against the live L2 probe) beside it."""
     sweep = {k: v for k, v in kt.items() if k.startswith("drift")}
     dom = max(sweep, key=lambda k: sweep[k][0])
     dom_ms = sweep[dom][0] / sweep[dom][1]
@@ -377,7 +386,23 @@ def roofline(kt, wl, nitems, hbm_peak, peak_kind, fp64_peak, workload):
             "fp64": {"achieved": fp64, "peak": fp64_peak, "unit": "G lane-ops/s", "frac": fp64 / fp64_peak,
                      "ops_per_cell": ops, "ops_per_cell_from_current_sources": current,
                      "peak_kind": "measured live (fma loop, ramgpu_probe_fp64)"},
-            "sweeps_GBps": {k: 16.0 * cells / (v[0] / v[1] / 1e3) / 1e9 for k, v in sweep.items()}}
+            "sweeps_GBps": {k: 16.0 * cells / (v[0] / v[1] / 1e3) / 1e9 for k, v in sweep.items()},
+            "l2": l2_view(sweep, dom, workload, current, l2_peak)}
+
+
+def l2_view(sweep, dom, workload, current, l2_peak):
+    """L2 traffic of the sweeps (ncu lts__t_bytes of the capture, per launch
+    of the timing pass) over their event-timed launches, against the live
+    L2 read-bandwidth probe; null when the capture is not of the current
+    sources or of this workload."""
+    l2b = NCU_CAPTURE.get("l2_bytes", {}).get(workload)
+    if not current or not l2b or l2_peak is None:
+        return None
+    gbps = {k: l2b[k] / (v[0] / v[1] / 1e3) / 1e9 for k, v in sweep.items() if k in l2b}
+    return {"achieved": gbps.get(dom), "peak": l2_peak, "unit": "GB/s",
+            "frac": gbps[dom] / l2_peak if dom in gbps else None, "kernel": dom,
+            "bytes_per_launch": l2b.get(dom), "sweeps_GBps": gbps,
+            "peak_kind": "measured live (L1-bypassing 16-byte loads over 32 MB held in L2, ramgpu_probe_l2)"}
 
 
 def e2e_section(torch, np, abi, gpu, wl, steps):
@@ -520,12 +545,13 @@ def measure(args, torch, np, abi, W, stream, name, steps, warmup, world=1, clock
     kt, kt_ms = kernel_pass(torch, gpu, stream, wl, flush, max(3, kernel_steps))
     hbm_peak, peak_kind = measured_peaks()
     fp64_peak = abi.probe_fp64() / 1e9
+    l2_peak = abi.probe_l2() / 1e9
     out = {"workload": workload_desc(wl), "cells_per_step": cells_per_step,
            "value": world * cells_per_step * steps / (total_ms / 1e3), "ms_per_step": total_ms / steps,
            "steps": steps, "warmup": warmup, "launches": launches, "wall_s": wall, "clocks": clk,
            "launch_shapes": shapes, "autotune_trials": trials, "item_groups": groups,
            "kernels_ms": {k: round(v[0] / v[1], 5) for k, v in kt.items()}, "kernel_pass_ms_per_step": kt_ms,
-           "roofline": roofline(kt, wl, ns, hbm_peak, peak_kind, fp64_peak, name)}
+           "roofline": roofline(kt, wl, ns, hbm_peak, peak_kind, fp64_peak, name, l2_peak)}
     per_gpu = out["value"] / world
     out["roofline"]["step"] = {"fused_min_GBps": per_gpu * 16 / 1e9, "fused_min_frac": per_gpu * 16 / 1e9 / hbm_peak,
                                "unfused_GBps": per_gpu * 80 / 1e9, "unfused_frac": per_gpu * 80 / 1e9 / hbm_peak}

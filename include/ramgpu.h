@@ -457,6 +457,10 @@ int ramgpu_bounds_report(ramgpu_ctx *ctx, int *checked, long long *failures, int
  * per second (a dependent-free fma loop over 8 x SMs x 256 threads); the
  * denominator of the FP64 roofline this path is bound by on GB300. */
 int ramgpu_probe_fp64(double *lane_ops_per_s);
+/* Measured L2 read bandwidth of the current device in bytes per second
+ * (16-byte loads that bypass L1, 200 passes over a 32 MB buffer held in
+ * L2); the denominator of the sweeps' L2 view (no reference counterpart). */
+int ramgpu_probe_l2(double *bytes_per_s);
 /* Device self-test of the integer-pipe FP64 multiply the sweeps use, bit
  * for bit against the FP64 unit on n random operand pairs (normal, short
  * significands and ties, zeros, subnormals, infinities, NaN, extreme

@@ -709,6 +709,21 @@ __global__ void k_probe_dfma(double* out, double a, double b, int iters) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// L2 read-bandwidth probe: every thread streams 16-byte loads that bypass
+// L1 over a buffer resident in L2, many passes; the XOR of what it read is
+// stored so the loads stay.
+__global__ void k_probe_l2(const uint4* __restrict__ buf, long long n16, int passes, unsigned* out) {
+  unsigned acc = 0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  for (int p = 0; p < passes; ++p)
+    for (long long i = t0; i < n16; i += stride) {
+      const uint4 v = __ldcg(buf + i);
+      acc ^= v.x ^ v.y ^ v.z ^ v.w;
+    }
+  out[t0] = acc;
+}
+
 // =================================================================== ABI
 // Copy of n doubles by the SMs, for host memory the device reaches without
 // registration (pageable memory on a coherent host link, such as a Fortran
@@ -2223,6 +2238,45 @@ int ramgpu_probe_fp64(double* lane_ops_per_s) {
   cudaFree(out);
   if (e != cudaSuccess) return fail(nullptr, RAMGPU_ERR_CUDA, cudaGetErrorString(e));
   *lane_ops_per_s = 8.0 * iters * (double)block * grid / (best * 1e-3);
+  return RAMGPU_OK;
+}
+
+int ramgpu_probe_l2(double* bytes_per_s) {
+  if (!bytes_per_s) return RAMGPU_ERR_ARG;
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return fail(nullptr, RAMGPU_ERR_CUDA, "no CUDA device");
+  const size_t bytes = 32u << 20;  // within either die's half of L2
+  const int block = 256, grid = nsm * 4, passes = 200;
+  void* buf = nullptr;
+  unsigned* out = nullptr;
+  if (cudaMalloc(&buf, bytes) != cudaSuccess || cudaMalloc(&out, sizeof(unsigned) * block * grid) != cudaSuccess) {
+    cudaFree(buf);
+    cudaGetLastError();
+    return fail(nullptr, RAMGPU_ERR_NOMEM, "probe allocation failed");
+  }
+  cudaMemset(buf, 1, bytes);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int r = 0; r < 4; ++r) {  // the first run brings the buffer into L2
+    cudaEventRecord(e0, 0);
+    k_probe_l2<<<grid, block>>>((const uint4*)buf, (long long)(bytes / 16), passes, out);
+    cudaEventRecord(e1, 0);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (r > 0 && ms < best) best = ms;
+  }
+  cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  cudaFree(out);
+  if (e != cudaSuccess) return fail(nullptr, RAMGPU_ERR_CUDA, cudaGetErrorString(e));
+  *bytes_per_s = (double)passes * (double)bytes / (best * 1e-3);
   return RAMGPU_OK;
 }
 

@@ -43,7 +43,7 @@ EXPORTS = (
     "ramgpu_set_step_groups", "ramgpu_step_groups", "ramgpu_set_pipeline_trace", "ramgpu_pipeline_trace",
     "ramgpu_check", "ramgpu_set_check", "ramgpu_last_status",
     "ramgpu_set_adj_record_budget", "ramgpu_adj_segments", "ramgpu_set_adj_overlap", "ramgpu_bounds_report",
-    "ramgpu_f2_stats", "ramgpu_set_mu_lanes",
+    "ramgpu_f2_stats", "ramgpu_probe_l2", "ramgpu_set_mu_lanes",
     "ramgpu_selftest_arith",
 )
 BAD_DATA = -1.0E10  # BadDataFlag of the satellite products
@@ -207,6 +207,7 @@ def load_library(path: str | Path | None = None, build_if_missing: bool = False)
         "ramgpu_set_adj_overlap": ([vp, i], i),
         "ramgpu_bounds_report": ([vp, ip, C.POINTER(C.c_longlong), ip, C.POINTER(C.c_longlong)], i),
         "ramgpu_f2_stats": ([vp, i, i, dp, dp, dp], i),
+        "ramgpu_probe_l2": ([dp], i),
         "ramgpu_set_mu_lanes": ([vp, i], i),
         "ramgpu_selftest_arith": ([C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)], i),
     }
@@ -226,6 +227,16 @@ def probe_fp64() -> float:
     rc = lib.ramgpu_probe_fp64(C.byref(v))
     if rc != RAMGPU_OK:
         raise RamGpuError(f"ramgpu_probe_fp64: {ERRORS.get(rc, rc)}")
+    return v.value
+
+
+def probe_l2() -> float:
+    """L2 read bandwidth of the current GPU in bytes per second."""
+    lib = load_library()
+    v = C.c_double()
+    rc = lib.ramgpu_probe_l2(C.byref(v))
+    if rc != RAMGPU_OK:
+        raise RamGpuError(f"ramgpu_probe_l2: {ERRORS.get(rc, rc)}")
     return v.value
 
 
