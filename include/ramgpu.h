@@ -217,10 +217,16 @@ int ramgpu_ram_run_host(ramgpu_ctx *ctx, double dts, double *const *f2, double *
  * rebuilt when an address or how the device reaches it changes. */
 int ramgpu_ram_run_ref(ramgpu_ctx *ctx, double dts, double *const *f2, double *const *ppert,
                        double *const *ppart);
-/* force != 0: ramgpu_ram_run_ref and ramgpu_upload/download_f2_all move
- * every array through the device staging buffer and the copy engines, even
- * arrays the device could reach in place (no reference counterpart; for
- * hosts whose coherent link is slower than their copy engines). */
+/* How ramgpu_ram_run_ref and ramgpu_upload/download_f2_all move arrays the
+ * device could reach in place (no reference counterpart): force = 0 (the
+ * default) in place, read and written by the transposing kernels; 1 every
+ * array through the device staging buffer and the copy engines,
+ * unpipelined; 2 page-locked F2 arrays of ramgpu_ram_run_ref through the
+ * copy engines plane chunk by plane chunk into a device staging area
+ * inside the pipeline, the others in place.  On GB300's coherent Grace
+ * link in place is fastest (0.88 ms per four-species call, against
+ * 0.95-1.08 ms for 2 and 1.00 ms for 1); 1 and 2 are for hosts whose link
+ * favours the copy engines. */
 int ramgpu_set_ref_staging(ramgpu_ctx *ctx, int force);
 /* Chunks of L planes the host calls (ramgpu_ram_run_host, ramgpu_ram_run_ref)
  * pipeline F2 over: 1..8, or 0 for the item-group pipeline of

@@ -167,6 +167,12 @@ struct ramgpu_ctx {
   // and persistent grid [ms] (0: not tried)
   double tune_plain_ms[4] = {0, 0, 0, 0}, tune_pers_ms[4] = {0, 0, 0, 0};
   bool ref_force_stage = false;  // move reachable arrays by the copy engines too
+  // ramgpu_ram_run_ref: page-locked F2 arrays through the copy engines chunk
+  // by chunk (a device staging area per member) instead of SM reads over the
+  // host link
+  bool ref_ce = false;
+  double* ref_ce_stage = nullptr;
+  size_t ref_ce_bytes = 0;
   int nsm = 0;
   // status word: device words and their page-locked copy; the pass is
   // appended to every call while check_on
@@ -1132,6 +1138,7 @@ int ramgpu_destroy(ramgpu_ctx* ctx) {
   if (ctx->pipe_exec) cudaGraphExecDestroy(ctx->pipe_exec);
   if (ctx->ref_exec) cudaGraphExecDestroy(ctx->ref_exec);
   cudaFree(ctx->ref_stage);
+  cudaFree(ctx->ref_ce_stage);
   for (cudaStream_t st : ctx->pipe_streams) cudaStreamDestroy(st);
   for (cudaEvent_t e : ctx->pipe_events) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->trace_ev) cudaEventDestroy(e);
@@ -1786,6 +1793,7 @@ int ramgpu_pipeline_trace(ramgpu_ctx* ctx, int* groups, float* ms) {
 struct RefMem {
   double *f2 = nullptr, *pe = nullptr, *pa = nullptr;
   double *f2r = nullptr, *per = nullptr, *par = nullptr;
+  double* f2ce = nullptr;  // device staging of a page-locked F2 moved by the copy engines
 };
 
 // ramgpu_ram_run_ref's work: F2 of every member gathered from the
@@ -1869,10 +1877,25 @@ int ramgpu_ram_run_ref(ramgpu_ctx* ctx, double dts, double* const* f2, double* c
     r.pa = ppart ? ppart[m] : nullptr;
     const bool fs = ctx->ref_force_stage;
     if (r.f2) staged |= !(r.f2r = fs ? nullptr : reach(r.f2, pma));
+    if (r.f2 && r.f2r && ctx->ref_ce) {
+      cudaPointerAttributes at{};
+      if (cudaPointerGetAttributes(&at, r.f2) != cudaSuccess) cudaGetLastError();
+      if (at.type == cudaMemoryTypeHost) {
+        const size_t need = sizeof(double) * (size_t)nm * ctx->d.ns * ctx->d.ncell;
+        if (ctx->ref_ce_bytes < need) {
+          cudaFree(ctx->ref_ce_stage);
+          ctx->ref_ce_stage = nullptr;
+          ctx->ref_ce_bytes = 0;
+          CK(cudaMalloc(&ctx->ref_ce_stage, need));
+          ctx->ref_ce_bytes = need;
+        }
+        r.f2ce = ctx->ref_ce_stage + (size_t)m * ctx->d.ns * ctx->d.ncell;
+      }
+    }
     if (r.pe) staged |= !(r.per = fs ? nullptr : reach(r.pe, pma));
     if (r.pa) staged |= !(r.par = fs ? nullptr : reach(r.pa, pma));
     for (const void* p : {(const void*)r.f2, (const void*)r.pe, (const void*)r.pa, (const void*)r.f2r,
-                          (const void*)r.per, (const void*)r.par})
+                          (const void*)r.per, (const void*)r.par, (const void*)r.f2ce})
       key.push_back(p);
   }
   const bool timing = ctx->timing;
@@ -1889,7 +1912,13 @@ int ramgpu_ram_run_ref(ramgpu_ctx* ctx, double dts, double* const* f2, double* c
   auto r_in = [&](int, cudaStream_t st, int l0, int l1) {
     for (int m = 0; m < nm; ++m)
       if (mem[m].f2) {
-        launch_ref_gather(mem[m].f2r, ctx->d.f2 + (size_t)m * ns * n, ns, n, l0 * plane, l1 * plane, ctx->nsm, st);
+        const double* src = mem[m].f2r;
+        if (mem[m].f2ce) {  // the chunk by the copy engines, then gathered on the device
+          const size_t o = (size_t)l0 * plane * ns, b = sizeof(double) * (size_t)(l1 - l0) * plane * ns;
+          CK(cudaMemcpyAsync(mem[m].f2ce + o, mem[m].f2 + o, b, cudaMemcpyHostToDevice, st));
+          src = mem[m].f2ce;
+        }
+        launch_ref_gather(src, ctx->d.f2 + (size_t)m * ns * n, ns, n, l0 * plane, l1 * plane, ctx->nsm, st);
         ctx->launches += 1;
       }
     CKL("reference-layout gather");
@@ -1899,8 +1928,13 @@ int ramgpu_ram_run_ref(ramgpu_ctx* ctx, double dts, double* const* f2, double* c
     const int a = std::max(l0, 1);  // the L = 1 plane goes back after ANISCH
     for (int m = 0; m < nm && a < l1; ++m)
       if (mem[m].f2) {
-        launch_ref_scatter(ctx->d.f2 + (size_t)m * ns * n, mem[m].f2r, ns, n, a * plane, l1 * plane, ctx->nsm, st);
+        double* dst = mem[m].f2ce ? mem[m].f2ce : mem[m].f2r;
+        launch_ref_scatter(ctx->d.f2 + (size_t)m * ns * n, dst, ns, n, a * plane, l1 * plane, ctx->nsm, st);
         ctx->launches += 1;
+        if (mem[m].f2ce) {
+          const size_t o = (size_t)a * plane * ns, b = sizeof(double) * (size_t)(l1 - a) * plane * ns;
+          CK(cudaMemcpyAsync(mem[m].f2 + o, mem[m].f2ce + o, b, cudaMemcpyDeviceToHost, st));
+        }
       }
     CKL("reference-layout scatter");
     return RAMGPU_OK;
@@ -1971,7 +2005,9 @@ int ramgpu_set_pipeline_chunks(ramgpu_ctx* ctx, int chunks) {
 
 int ramgpu_set_ref_staging(ramgpu_ctx* ctx, int force) {
   if (check_ctx(ctx)) return RAMGPU_ERR_ARG;
-  ctx->ref_force_stage = force != 0;
+  if (force < 0 || force > 2) return fail(ctx, RAMGPU_ERR_ARG, "force: 0, 1 or 2");
+  ctx->ref_force_stage = force == 1;
+  ctx->ref_ce = force == 2;
   return RAMGPU_OK;
 }
 

@@ -468,10 +468,12 @@ class RamGpu:
         self._ck(self.lib.ramgpu_load_state(self.h, str(path).encode(), C.byref(t)), "load_state")
         return t.value
 
-    def set_ref_staging(self, force: bool):
-        """Move reference-layout arrays by the copy engines even when the
-        device reaches them in place."""
-        self._ck(self.lib.ramgpu_set_ref_staging(self.h, int(bool(force))), "set_ref_staging")
+    def set_ref_staging(self, mode):
+        """How reference-layout arrays move (ramgpu_set_ref_staging): 0 (or
+        False) in place where the device reaches them; 1 (or True) through
+        the staging buffer and the copy engines, unpipelined; 2 page-locked
+        arrays through the copy engines chunk by chunk, inside the pipeline."""
+        self._ck(self.lib.ramgpu_set_ref_staging(self.h, int(mode)), "set_ref_staging")
 
     def upload_f2_all(self, member: int, f2):
         """Member's whole F2(NS,NR,NT,NE,NPA) in the reference layout."""

@@ -82,7 +82,8 @@ def _reference(wl, members, species, calls):
 @pytest.mark.parametrize("memory", ["pageable", "pinned"])
 @pytest.mark.parametrize("graph,stage,groups,chunks", [(False, False, 1, 0), (True, False, 4, 0), (True, True, 2, 4),
                                                        (False, True, 3, 0), (False, False, 2, 3),
-                                                       (True, False, 4, 4), (True, False, 1, 8)])
+                                                       (True, False, 4, 4), (True, False, 1, 8),
+                                                       (True, 2, 4, 4), (False, 2, 2, 3), (True, 2, 1, 8)])
 def test_ram_run_ref_equals_per_species_path(wl, memory, graph, stage, groups, chunks):
     g = wl.grid
     ns = len(g.species)
