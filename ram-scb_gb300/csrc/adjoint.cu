@@ -177,13 +177,9 @@ __device__ __forceinline__ double face_ak(double C, bool neg, int cs, double mh,
 // lambda of cell c of a line (stride st) masked by the clip bit.  Both
 // loads are issued unconditionally (the record through the read-only path)
 // so that the next cells' loads can run ahead of the window's arithmetic.
-// kNc: lambda too through the read-only path, for lines that own whole
-// 32-byte sectors and are read ahead of where they are written, so no
-// sector is read again after a write in the same launch.
-template <bool kNc = false>
 __device__ __forceinline__ double masked(const double* __restrict__ lam, const unsigned char* __restrict__ rl,
                                          long long off, int rsh) {
-  const double v = kNc ? __ldg(lam + off) : lam[off];
+  const double v = lam[off];
   return ((__ldg(rl + off) >> rsh) & kClipBit) ? 0.0 : v;
 }
 
@@ -698,18 +694,6 @@ void launch_adj_tail(const Dev& d, cudaStream_t st) {
   k_adj_anisch<<<dim3((unsigned)((n1 + 255) / 256), d.nitems), 256, 0, st>>>(d);
   long long n2 = (long long)d.nr * d.ne * d.npa;
   k_adj_copy_mask<<<dim3((unsigned)((n2 + 255) / 256), d.nitems), 256, 0, st>>>(d, (d.flags >> 31) & 1u);
-}
-
-__global__ void k_scale_lam(Dev d, const double* __restrict__ table) {
-  const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (c >= d.ncell) return;
-  const int2 item = d.items[blockIdx.y];
-  const int slot = item.x * d.ns + item.y;
-  d.lam[(long long)slot * d.ncell + c] *= table[(long long)item.y * d.ncell + c];
-}
-
-void launch_scale_lam(const Dev& d, const double* table, cudaStream_t st) {
-  k_scale_lam<<<dim3((unsigned)((d.ncell + 255) / 256), d.nitems), 256, 0, st>>>(d, table);
 }
 
 // ------------------------------------------------------------- observations

@@ -88,7 +88,6 @@ struct ObsDev {
 void launch_adj_sweep(const Dev& d, int w, const unsigned char* rec, int rsh, cudaStream_t st, int co = 0,
                       const double* loss = nullptr);
 void launch_adj_tail(const Dev& d, cudaStream_t st);
-void launch_scale_lam(const Dev& d, const double* table, cudaStream_t st);
 void launch_obs_fwd(const Dev& d, const ObsDev* obs, int nobs, int call, double* fm, double* J,
                     cudaStream_t st);
 void launch_obs_adj(const Dev& d, const ObsDev* obs, int nobs, int call, const double* fm,

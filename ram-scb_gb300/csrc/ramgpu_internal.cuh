@@ -251,12 +251,6 @@ __device__ __forceinline__ double corr_a_int(bits64 ub, bool neg, double c, doub
   if (eu >= 1023) out = corr_a_fallback(c, mh, neg);
   return out;
 }
-// u = |c|*y as bits (truncated significand product, as mul_pos_bits) for a
-// positive normal y; zero and subnormal |c| give u = 0.
-__device__ __forceinline__ bits64 courant_bits(double c, double y) {
-  const bits64 ax = dbits(c) & kAbsMask;
-  return ax < kImplicit ? 0ULL : mul_pos_bits(ax, y);
-}
 
 // a*b rounded to nearest even, computed on the integer pipe: the 53-bit
 // significands' 106-bit product from a 64x64 multiply (high and low
@@ -297,7 +291,6 @@ __device__ __forceinline__ double mul_rn_int(double a, double b) {
 // x < 0.0 exactly as the Fortran test `C.lt.0` (false for -0.0 and NaN with
 // the sign bit clear).
 __device__ __forceinline__ bool is_neg(double x) { return dbits(x) > 0x8000000000000000ULL; }
-__device__ __forceinline__ bool is_neg_or_nan(double x) { return (long long)dbits(x) < 0 && (dbits(x) << 1) != 0; }
 // |x| > 1e-27
 __device__ __forceinline__ bool abs_gt_1em27(double x) {
   const unsigned long long t = 0x3A53CE9A36F23C10ULL;  // bits of 1.0E-27
