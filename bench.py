@@ -52,21 +52,22 @@ NCU_CAPTURE = {
     # profiles/driftr_refined.md, profiles/sweeps_l2.md): one kernel per
     # command, each captured launch advances one species, so a four-species
     # launch of the timing pass is scaled by 4.
-    "sources_sha16": "0e986e1de47377a3",
-    "command": ("ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum,"
+    "sources_sha16": "8faa21e4265be355",
+    "command": ("ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum,lts__t_bytes.sum,"
                 "smsp__sass_thread_inst_executed_op_{dadd,dfma,dmul}_pred_on.sum --clock-control none "
                 "-k regex:k_sweep_<r|p|e|mu> -c 2 python bench.py --steps 2 --warmup 1 --sections headline "
-                "--no-cpu-baseline --no-e2e --no-autotune [--workload refined]"),
+                "--no-cpu-baseline --no-e2e --no-autotune [--workload refined|single_h]"),
     "dram_bytes": {"four_sp": {"driftr": 4 * 11.02e6, "driftp": 4 * 10.39e6,
                                "drifte": 4 * 0.5 * (11.34e6 + 29.98e6), "driftmu": 4 * 0.5 * (20.47e6 + 10.52e6)},
-                   "single_h": {"driftr": 11.03e6, "driftp": 10.39e6,
-                                "drifte": 0.5 * (11.28e6 + 29.98e6), "driftmu": 0.5 * (20.47e6 + 10.52e6)},
-                   "refined": {"driftr": 4 * 0.5 * (267.84e6 + 268.13e6)}},
+                   "single_h": {"driftr": 11.03e6, "driftp": 10.40e6,
+                                "drifte": 0.5 * (11.33e6 + 29.98e6), "driftmu": 0.5 * (20.47e6 + 10.52e6)},
+                   "refined": {"driftr": 4 * 0.5 * (268.51e6 + 267.80e6)}},
     # lts__t_bytes.sum per launch of the timing pass (profiles/sweeps_l2.md)
-    "l2_bytes": {"four_sp": {"driftr": 4 * 0.5 * (112.05e6 + 111.84e6), "driftp": 4 * 0.5 * (38.79e6 + 39.11e6),
-                             "drifte": 4 * 0.5 * (68.85e6 + 69.59e6), "driftmu": 4 * 0.5 * (77.47e6 + 58.90e6)},
-                 "single_h": {"driftr": 0.5 * (111.71e6 + 111.96e6), "driftp": 0.5 * (38.67e6 + 39.26e6),
-                              "drifte": 0.5 * (68.84e6 + 69.67e6), "driftmu": 0.5 * (77.55e6 + 59.12e6)}},
+    "l2_bytes": {"four_sp": {"driftr": 4 * 0.5 * (112.45e6 + 112.11e6), "driftp": 4 * 0.5 * (39.40e6 + 39.16e6),
+                             "drifte": 4 * 0.5 * (70.01e6 + 70.05e6), "driftmu": 4 * 0.5 * (78.02e6 + 58.62e6)},
+                 "single_h": {"driftr": 0.5 * (112.54e6 + 111.96e6), "driftp": 0.5 * (39.44e6 + 39.26e6),
+                              "drifte": 0.5 * (70.63e6 + 70.04e6), "driftmu": 0.5 * (78.13e6 + 58.64e6)},
+                 "refined": {"driftr": 4 * 0.5 * (2156.6e6 + 2314.6e6)}},
     "fp64_ops_per_cell": {"driftr": 5.02, "driftp": 4.64, "drifte": 0.5 * (6.70 + 4.78),
                           "driftmu": 0.5 * (6.62 + 5.69)},
 }
