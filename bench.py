@@ -116,6 +116,7 @@ def parse():
     ap.add_argument("--cpu-inner", type=int, default=1, help=argparse.SUPPRESS)
     ap.add_argument("--cpu-calls", type=int, default=0, help=argparse.SUPPRESS)
     ap.add_argument("--cpu-warmup", type=int, default=1, help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-impl", default="port", choices=["port", "ref"], help=argparse.SUPPRESS)
     args = ap.parse_args()
     args.sections = {s.strip() for s in args.sections.split(",") if s.strip()}
     bad = args.sections - set(SECTIONS)
@@ -246,70 +247,141 @@ def cpu_time_oracle(wl, seconds, nthreads, inner=1, calls=None, warmup=1):
     return cells * n / el, n, el
 
 
+REF_DESC = ("the reference's own Fortran routines (src/ModRamDrift.f90, src/ModRamLoss.f90, src/ModRamRun.f90) "
+            "translated to C by oracle/f90c.py and built by gcc -O3 -ffp-contract=off (no Fortran compiler here), "
+            "run through its own ram_run with its own OpenMP loop over species")
+
+
+def cpu_time_ref(wl, seconds, nthreads, calls=None, warmup=1):
+    """Time the reference's own ram_run (translated, oracle/_ref) on this
+    workload with nthreads OpenMP threads on its species loop (the only
+    parallelism the reference has): `warmup` untimed calls, then `calls`
+    timed ones (or as many as fit in `seconds`); returns (cell-updates/s,
+    calls, elapsed).  The state stays in the reference's module arrays."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import refrun
+
+    ref = refrun.RefRam(wl.grid, wl.fields, threads=nthreads)
+    ref.load_state(wl.f2, wl.fgeos)
+    cells = 2 * wl.grid.ncell * len(wl.grid.species)
+    for w in range(max(0, warmup)):
+        ref.step(wl.dts, wl.kp(2 * w))
+    n, t0 = 0, time.perf_counter()
+    while True:
+        ref.step(wl.dts, wl.kp(2 * (warmup + n)))
+        n += 1
+        el = time.perf_counter() - t0
+        if (calls is not None and n >= calls) or (calls is None and (el >= seconds or n >= 1000)):
+            break
+    return cells * n / el, n, el
+
+
+def ref_available():
+    sys.path.insert(0, str(ROOT / "oracle"))
+    try:
+        import refrun
+
+        return refrun.build() is not None
+    except Exception:  # noqa: BLE001 -- no compiler or no sources: the port stands in
+        return False
+
+
 def cpu_leg_main(args):
-    """--cpu-leg: time the CPU oracle in this process (which never imports
-    torch or the CUDA library) and print one JSON object."""
+    """--cpu-leg: time a CPU leg in this process (which never imports torch
+    or the CUDA library) and print one JSON object: the translated reference
+    (--cpu-impl ref) or the C oracle (--cpu-impl port)."""
     from ramgpu import workload as W
 
     wl = W.make_workload(args.cpu_leg)
-    v, n, el = cpu_time_oracle(wl, args.cpu_seconds, args.cpu_outer, args.cpu_inner,
-                               calls=args.cpu_calls if args.cpu_calls > 0 else None, warmup=args.cpu_warmup)
+    calls = args.cpu_calls if args.cpu_calls > 0 else None
+    if args.cpu_impl == "ref":
+        v, n, el = cpu_time_ref(wl, args.cpu_seconds, args.cpu_outer, calls=calls, warmup=args.cpu_warmup)
+    else:
+        v, n, el = cpu_time_oracle(wl, args.cpu_seconds, args.cpu_outer, args.cpu_inner, calls=calls,
+                                   warmup=args.cpu_warmup)
     print(json.dumps({"value": v, "calls": n, "elapsed_s": el, "outer": args.cpu_outer, "inner": args.cpu_inner}),
           flush=True)
 
 
-def cpu_leg_fresh(workload, outer, inner, calls=0, seconds=10.0, warmup=1):
-    """The CPU oracle timed in a fresh interpreter that imports neither torch
+def cpu_leg_fresh(workload, outer, inner, calls=0, seconds=10.0, warmup=1, impl="port"):
+    """A CPU leg timed in a fresh interpreter that imports neither torch
     nor the CUDA library, so the figure is the one a reference run on the
     same cores sees.  (Timed inside the GPU process after its GPU sections,
     the line threads inside each species did not run: that leg measured the
     species-threads-only rate.)"""
     cmd = [sys.executable, str(ROOT / "bench.py"), "--cpu-leg", workload, "--cpu-outer", str(outer),
            "--cpu-inner", str(inner), "--cpu-calls", str(calls), "--cpu-seconds", str(seconds),
-           "--cpu-warmup", str(warmup)]
+           "--cpu-warmup", str(warmup), "--cpu-impl", impl]
     r = subprocess.run(cmd, capture_output=True, text=True, check=True)
     return json.loads(r.stdout.strip().splitlines()[-1])
 
 
-def cpu_baseline_fresh(workload, ns, seconds, calls=0, warmup=1):
-    """Both CPU variants of the reference's path, each in a fresh process:
-    (1) OpenMP over species only, as the reference (at most nS threads);
-    (2) every host core: species threads x line threads inside each routine.
-    The line's value is variant 2."""
+def cpu_baseline_fresh(workload, ns, seconds, calls=0, warmup=1, ref_calls=None, ref_warmup=None):
+    """The CPU legs, each in a fresh process:
+    reference: the reference's own routines (translated), OpenMP over
+      species as the reference (at most nS threads) -- the line's value;
+    port_species_threads / port_all_cores: the C oracle with the same
+      species threads, and with every host core (line threads inside each
+      routine), as reported before the reference could be run here.
+    Without the translated reference the port's all-cores leg is the value
+    (kind "port")."""
     cores = os.cpu_count() or 1
     o2, i2 = cpu_threads(ns)
-    v1 = cpu_leg_fresh(workload, min(ns, cores), 1, calls=calls, seconds=seconds, warmup=warmup)
+    ot = min(ns, cores)
+    v1 = cpu_leg_fresh(workload, ot, 1, calls=calls, seconds=seconds, warmup=warmup)
     v2 = cpu_leg_fresh(workload, o2, i2, calls=calls, seconds=seconds, warmup=warmup)
+    variants = {"port_species_threads": {"value": v1["value"], "threads": v1["outer"], "calls": v1["calls"],
+                                         "elapsed_s": v1["elapsed_s"]},
+                "port_all_cores": {"value": v2["value"], "threads": o2 * i2, "calls": v2["calls"],
+                                   "elapsed_s": v2["elapsed_s"]}}
+    if ref_available():
+        rc = calls if ref_calls is None else ref_calls
+        rw = warmup if ref_warmup is None else ref_warmup
+        vr = cpu_leg_fresh(workload, ot, 1, calls=rc, seconds=seconds, warmup=rw, impl="ref")
+        variants["reference"] = {"value": vr["value"], "threads": ot, "calls": vr["calls"],
+                                 "elapsed_s": vr["elapsed_s"]}
+        return {"value": vr["value"], "unit": UNIT, "cores": ot, "kind": "reference",
+                "sample": (f"{vr['calls']} ram_run calls of the workload in {vr['elapsed_s']:.1f} s after {rw} "
+                           f"warm-up call(s), fresh process; {REF_DESC}, {ot} threads"),
+                "variants": variants}
     return {"value": v2["value"], "unit": UNIT, "cores": o2 * i2, "kind": "port",
             "sample": (f"{v2['calls']} ram_run calls of the workload in {v2['elapsed_s']:.1f} s after {warmup} "
                        f"warm-up call(s), fresh process; C restatement of the reference routines (-O3 "
                        f"-ffp-contract=off, no Fortran compiler), OpenMP over {o2} species x {i2} line threads"),
-            "variants": {"species_threads": {"value": v1["value"], "threads": v1["outer"], "calls": v1["calls"],
-                                             "elapsed_s": v1["elapsed_s"]},
-                         "all_cores": {"value": v2["value"], "threads": o2 * i2, "calls": v2["calls"],
-                                       "elapsed_s": v2["elapsed_s"]}}}
+            "variants": variants}
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference's own ram_run (translated to C, with
+    its own OpenMP loop over species, so at most nS threads) on this arm's
+    workload; the C oracle on every host core where the translated reference
+    is not available."""
     from ramgpu import workload as W
 
     if rank != 0:
         return
     wl = W.make_workload(args.workload)
     ns = len(wl.grid.species)
-    outer, inner = cpu_threads(ns)
     # W untimed warm-up steps, then exactly K timed steps; a step is one
-    # ram_run call of the workload (about 0.1 s on 16 host cores)
-    v, n, el = cpu_time_oracle(wl, 0.0, outer, inner, calls=max(1, args.steps), warmup=args.warmup)
-    sample = (f"{n} ram_run calls of the workload ({workload_desc(wl)}) after {args.warmup} warm-up "
-              f"calls, {el:.1f} s; C restatement of the reference routines (-O3 -ffp-contract=off, no Fortran "
-              f"compiler), OpenMP over {outer} species x {inner} line threads")
+    # ram_run call of the workload
+    if ref_available():
+        threads = min(ns, os.cpu_count() or 1)
+        v, n, el = cpu_time_ref(wl, 0.0, threads, calls=max(1, args.steps), warmup=args.warmup)
+        kind, cores = "reference", threads
+        sample = (f"{n} ram_run calls of the workload ({workload_desc(wl)}) after {args.warmup} warm-up "
+                  f"calls, {el:.1f} s; {REF_DESC}, {threads} threads")
+    else:
+        outer, inner = cpu_threads(ns)
+        v, n, el = cpu_time_oracle(wl, 0.0, outer, inner, calls=max(1, args.steps), warmup=args.warmup)
+        kind, cores = "port", outer * inner
+        sample = (f"{n} ram_run calls of the workload ({workload_desc(wl)}) after {args.warmup} warm-up "
+                  f"calls, {el:.1f} s; C restatement of the reference routines (-O3 -ffp-contract=off, no Fortran "
+                  f"compiler), OpenMP over {outer} species x {inner} line threads")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * el / n, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": workload_desc(wl), "step": "one ram_run call (2 DTs steps)"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": outer * inner, "kind": "port",
-                             "sample": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -1033,7 +1105,7 @@ def run_gb300(args, rank, world, local_rank):
             single["cpu_baseline"] = cpu_baseline_fresh("single_h", 1, args.cpu_seconds)
         if refined is not None:
             # a bounded sample: one timed call per variant (a few seconds each)
-            refined["cpu_baseline"] = cpu_baseline_fresh("refined", 4, 0.0, calls=1, warmup=1)
+            refined["cpu_baseline"] = cpu_baseline_fresh("refined", 4, 0.0, calls=1, warmup=1, ref_warmup=0)
     if rank != 0:
         return
     line = {

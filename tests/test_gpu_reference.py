@@ -1,0 +1,107 @@
+"""GPU: the CUDA ram_run against the reference's own routines.
+
+Two sources, neither a restatement of this project:
+
+* the committed fixtures of tests/golden (made by tests/golden/make_golden.py
+  from the reference's ram_run, src/ModRamRun.f90:16-225, translated by
+  oracle/f90c.py): the GPU advances alone along a three-call Kp ramp on the
+  perturbed 8x9x35x72 grid and meets every call's sums, sampled cells,
+  moments, FLUX and DtsNext;
+* the translated reference itself, built on this machine from
+  oracle/_ref/ramref.c: whole-array comparisons per call (each call started
+  from the reference's state) on the test grids and on the standard
+  20x25x35x72 four-species grid.
+
+Bar: 1e-12 relative max-norm per call (FP64), as the rest of the parity suite.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from ramgpu import abi, workload as W
+import refrun
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def rel(a, b):
+    den = np.max(np.abs(b))
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / (den if den > 0 else 1.0))
+
+
+def _gpu(wl, kp):
+    g = wl.grid
+    gpu = abi.RamGpu(g, wl.fields)
+    for s in range(len(g.species)):
+        gpu.upload_f2(0, s, wl.f2[s])
+        gpu.set_boundary(0, s, wl.fgeos[s])
+    gpu.set_kp(0, kp)
+    return gpu
+
+
+def _check_summary(gpu, sd_all, dts_next):
+    assert abs(gpu.cfl(0, 0)[4] - dts_next) <= TOL * dts_next
+    for s, sd in enumerate(sd_all):
+        f = gpu.download_f2(0, s)
+        assert abs(np.sum(f) - sd["sum"]) <= 1e-12 * abs(sd["sum"]), s
+        scale = max(abs(v) for _, v in sd["cells"])
+        for c, v in sd["cells"]:
+            assert abs(f[tuple(c)] - v) <= TOL * scale, (s, c)
+        pe, pa = gpu.moments(0, s)
+        for arr, key in ((pe, "ppert"), (pa, "ppart")):
+            sc = max(abs(v) for _, v in sd[key])
+            for c, v in sd[key]:
+                assert abs(arr[tuple(c)] - v) <= TOL * sc, (s, key, c)
+        fl = gpu.flux(0, s)
+        sc = max(abs(v) for _, v in sd["flux"])
+        for c, v in sd["flux"]:
+            assert abs(fl[tuple(c)] - v) <= TOL * sc, (s, c)
+
+
+def test_follows_reference_ramp_fixture():
+    from conftest import ROOT
+    gd = json.loads((ROOT / "tests" / "golden" / "ram_run_ramp.json").read_text())
+    wl = W.make_workload(gd["workload"])
+    gpu = _gpu(wl, gd["calls"][0]["kp"])
+    try:
+        for call in gd["calls"]:
+            gpu.set_kp(0, call["kp"])
+            gpu.ram_run(gd["dts"])
+            _check_summary(gpu, call["species"], call["dts_next"])
+    finally:
+        gpu.close()
+
+
+@pytest.fixture(scope="module")
+def have_ref():
+    if refrun.build() is None:
+        pytest.skip("translated reference not present (oracle/_ref/ramref.c)")
+    return True
+
+
+@pytest.mark.parametrize("name,kps", [("tiny_pert8", (1.0, 3.5, 6.0)), ("four_sp", (3.0,))])
+def test_whole_arrays_against_translated_reference(have_ref, name, kps):
+    """Each call from the reference's state: F2, PPERT/PPART, FLUX of every
+    species and DtsNext within 1e-12."""
+    wl = W.make_workload(name)
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields)
+    f_ref = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    gpu = _gpu(wl, kps[0])
+    try:
+        for kp in kps:
+            for s in range(len(g.species)):
+                gpu.upload_f2(0, s, f_ref[s])
+            gpu.set_kp(0, kp)
+            gpu.ram_run(wl.dts)
+            r = ref.ram_run(f_ref, wl.fgeos, wl.dts, kp)
+            assert abs(gpu.cfl(0, 0)[4] - r["dts_next"]) <= TOL * r["dts_next"]
+            for s in range(len(g.species)):
+                assert rel(gpu.download_f2(0, s), f_ref[s]) <= TOL, (kp, s)
+                pe, pa = gpu.moments(0, s)
+                assert rel(pe, r["ppert"][s]) <= TOL and rel(pa, r["ppart"][s]) <= TOL, (kp, s)
+                assert rel(gpu.flux(0, s), r["flux"][s]) <= TOL, (kp, s)
+    finally:
+        gpu.close()

@@ -522,7 +522,8 @@ def _golden():
 
 
 def test_oracle_matches_golden_fixture():
-    """The committed fixture (tests/golden/make_golden.py) pins the oracle's
+    """The committed fixture (tests/golden/make_golden.py, made by the
+    reference's own ram_run translated by oracle/f90c.py) pins the oracle's
     ram_run on the non-dipole test grid; libm differences between machines
     stay far inside 1e-12."""
     gd = _golden()
@@ -540,3 +541,31 @@ def test_oracle_matches_golden_fixture():
             sc = max(abs(v) for _, v in sd[key])
             for c, v in sd[key]:
                 assert abs(out[key][s][tuple(c)] - v) <= 1e-12 * sc
+
+
+def test_oracle_follows_reference_ramp_fixture():
+    """Three successive calls along a Kp ramp on the perturbed 8x9x35x72
+    grid against the reference's own results (tests/golden/ram_run_ramp.json):
+    sums, sampled cells, moments, FLUX, DtsNext and the SUMRC losses."""
+    import json
+    from conftest import ROOT
+    gd = json.loads((ROOT / "tests" / "golden" / "ram_run_ramp.json").read_text())
+    wl = W.make_workload(gd["workload"])
+    o = pyoracle.Oracle(wl.grid, wl.fields)
+    f2 = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    losses = {s: (0.0, 0.0, 0.0, 0.0) for s in range(len(wl.grid.species))}
+    for call in gd["calls"]:
+        out = o.ram_run(f2, wl.fgeos, gd["dts"], kp=call["kp"], want_flux=True, losses=losses)
+        losses = out["losses"]
+        assert abs(out["dts_next"] - call["dts_next"]) <= 1e-12 * call["dts_next"]
+        for s, sd in enumerate(call["species"]):
+            assert abs(np.sum(f2[s]) - sd["sum"]) <= 1e-12 * abs(sd["sum"])
+            scale = max(abs(v) for _, v in sd["cells"])
+            for c, v in sd["cells"]:
+                assert abs(f2[s][tuple(c)] - v) <= 1e-12 * scale
+            for key in ("ppert", "ppart", "flux"):
+                sc = max(abs(v) for _, v in sd[key])
+                for c, v in sd[key]:
+                    assert abs(out[key][s][tuple(c)] - v) <= 1e-12 * sc
+            for a, b in zip(losses[s], call["losses"][s]):
+                assert abs(a - b) <= 1e-12 * max(abs(b), 1e-300)

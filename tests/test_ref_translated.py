@@ -1,0 +1,124 @@
+"""The C oracle against the reference's own routines, bit for bit.
+
+oracle/f90c.py translates the reference's Fortran (src/ModRamDrift.f90,
+src/ModRamLoss.f90, src/ModRamRun.f90 and their modules) to C and gcc
+builds it (with array bounds checks in libramref_check.so);
+oracle/refrun.py runs the reference's ram_run (src/ModRamRun.f90:16-225)
+and its single routines on the same inputs as the oracle.  Every output is
+compared for exact equality: F2, the moments, FLUX, VT, DtsNext, the
+DtDrift minima, the SUMRC loss bookkeeping, CHARGE/ATLOS and the CDrift
+coefficient arrays of each sweep.
+
+Needs the reference's tree (to translate) or a translated oracle/_ref/ramref.c.
+"""
+import numpy as np
+import pytest
+
+import pyoracle
+import refrun
+from ramgpu import workload as W
+
+pytestmark = pytest.mark.skipif(refrun.build() is None,
+                                reason="translated reference unavailable (no reference tree, no oracle/_ref/ramref.c)")
+
+
+def _runs(name, kps, check):
+    wl = W.make_workload(name)
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields, check=check)
+    o = pyoracle.Oracle(g, wl.fields)
+    f_ref = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    f_or = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    losses = {s: (0.0, 0.0, 0.0, 0.0) for s in range(len(g.species))}
+    for kp in kps:
+        r = ref.ram_run(f_ref, wl.fgeos, wl.dts, kp)
+        out = o.ram_run(f_or, wl.fgeos, wl.dts, kp=kp, want_flux=True, losses=losses)
+        losses = out["losses"]
+        yield g, ref, r, out, f_ref, f_or
+
+
+@pytest.mark.parametrize("name", ["tiny", "tiny_pert", "tiny_pert8"])
+def test_ram_run_bit_for_bit(name):
+    """Three calls along a Kp ramp (bounds-checked build of the reference)."""
+    for g, ref, r, out, f_ref, f_or in _runs(name, (1.0, 3.5, 6.0), check=True):
+        for s in range(len(g.species)):
+            assert np.array_equal(f_ref[s], f_or[s]), s
+            assert np.array_equal(r["ppert"][s], out["ppert"][s]), s
+            assert np.array_equal(r["ppart"][s], out["ppart"][s]), s
+            assert np.array_equal(r["flux"][s], out["flux"][s]), s
+            assert r["losses"][s] == tuple(out["losses"][s]), s
+        assert np.array_equal(r["vt"], out["vt"])
+        assert r["dts_next"] == out["dts_next"]
+        assert ref.stubs() == {"coulpara": len(g.species)}
+
+
+def test_standard_grid_bit_for_bit():
+    """The 20x25x35x72 four-species step (e-, H+, He+, O+), one call."""
+    for g, ref, r, out, f_ref, f_or in _runs("four_sp", (3.0,), check=False):
+        for s in range(len(g.species)):
+            assert np.array_equal(f_ref[s], f_or[s]), s
+            assert np.array_equal(r["ppert"][s], out["ppert"][s]), s
+            assert np.array_equal(r["flux"][s], out["flux"][s]), s
+        assert r["dts_next"] == out["dts_next"]
+
+
+@pytest.mark.parametrize("which,routine", [("R", "driftr"), ("P", "driftp"), ("E", "drifte"), ("MU", "driftmu")])
+def test_single_sweeps_and_coefficients(which, routine):
+    """DRIFTPARA then one sweep of the reference on every species of the
+    perturbed grid (stale DRIFTR ghosts included): F2, the CDrift array
+    and the DtDrift minimum."""
+    wl = W.make_workload("tiny_pert8")
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields, check=True)
+    o = pyoracle.Oracle(g, wl.fields)
+    kp = 4.0
+    vt = o.vt_vols(kp)
+    ref.a["vt"][...] = vt
+    ref.set("modramtiming::dts", wl.dts)
+    for s in range(len(g.species)):
+        ref.a["f2"][s] = wl.f2[s]
+        ref.a["fgeos"][s] = wl.fgeos[s]
+        ref.subroutine("driftpara", s)
+        ref.subroutine(routine, s)
+        f = np.asfortranarray(wl.f2[s]).copy(order="F")
+        cd = np.zeros_like(f, order="F")
+        dt = o.sweep(which, s, f, vt, wl.dts, fgeos=wl.fgeos[s], cdrift=cd)
+        assert np.array_equal(ref.a["f2"][s], f), s
+        assert np.array_equal(ref.view("modramdrift::cdrift" + which.lower()), cd), s
+        assert ref.view("modramvariables::dtdrift" + which.lower())[s] == dt, s
+        ref.call("driftend")
+
+
+def test_cepara_tables():
+    """CHARGE (analytic H+, He+, O+ cross sections; none for e-) and ATLOS."""
+    wl = W.make_workload("tiny_pert")
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields)
+    o = pyoracle.Oracle(g, wl.fields)
+    ref.set("modramtiming::dts", wl.dts)
+    for s in range(len(g.species)):
+        ref.subroutine("cepara", s)
+        charge, atlos = o.cepara(s, wl.dts)
+        assert np.array_equal(ref.a["charge"][s], charge), s
+        assert np.array_equal(ref.a["atlos"][s], atlos), s
+    assert np.all(ref.a["charge"][0] == 1.0)
+    assert np.any(ref.a["charge"][1] < 1.0)
+
+
+def test_stale_ghost_lines_occur():
+    """The perturbed grid has DRIFTR lines that are outflow at NR and
+    upwinded from the right at NR-1 (they read the previous inflow line's
+    ghost), so the bit-for-bit sweeps above cover that quirk."""
+    wl = W.make_workload("tiny_pert8")
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields)
+    o = pyoracle.Oracle(g, wl.fields)
+    ref.a["vt"][...] = o.vt_vols(4.0)
+    ref.set("modramtiming::dts", wl.dts)
+    ref.a["f2"][1] = wl.f2[1]
+    ref.a["fgeos"][1] = wl.fgeos[1]
+    ref.subroutine("driftpara", 1)
+    ref.subroutine("driftr", 1)
+    cd = ref.view("modramdrift::cdriftr")
+    assert ((cd[-1] >= 0) & (cd[-2] < 0)).any() and (cd[-1] < 0).any()
+    ref.call("driftend")
