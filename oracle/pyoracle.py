@@ -1,9 +1,9 @@
 """ctypes binding of the CPU oracle (oracle/ram_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline / reference leg, never by the product.  Parity of
-the oracle against the Fortran reference is unpinned (no Fortran compiler,
-no per-routine golden vectors in the reference); see ram_oracle.h.
+bench.py's CPU legs, never by the product.  The oracle equals the
+reference's own routines bit for bit (they run here translated from the
+Fortran by oracle/f90c.py, oracle/refrun.py); see ram_oracle.h.
 """
 from __future__ import annotations
 

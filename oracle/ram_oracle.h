@@ -6,14 +6,14 @@
  * the CUDA path and as the timed CPU baseline.  Nothing in the product
  * (the ramgpu library and its host package) links or calls it.
  *
- * Parity status: the reference is Fortran 90 and no Fortran compiler
- * exists on either build machine, and the reference ships no per-routine
- * golden vectors for these routines.  Parity of this restatement is
- * therefore UNPINNED by the reference itself; it is pinned by
- * known-answer tests (hand-computed limiter branches, exact conservation,
- * identity at zero drift, periodicity, the DRIFTR stale-ghost case, the
- * ANISCH L=1 side effect) and by an independent NumPy restatement of the
- * charge-exchange and moment formulas.
+ * Parity status: pinned by the reference itself.  No Fortran compiler
+ * exists on either build machine, so oracle/f90c.py translates the
+ * reference's own routines (src/ModRamDrift.f90, src/ModRamLoss.f90,
+ * src/ModRamRun.f90) to C and oracle/refrun.py runs its ram_run; this
+ * restatement equals it bit for bit (F2, moments, FLUX, VT, DtsNext, the
+ * SUMRC bookkeeping, every CDrift array and DtDrift minimum, CHARGE and
+ * ATLOS: tests/test_ref_translated.py).  Known-answer tests and an
+ * independent NumPy restatement (oracle/ram_numpy.py) pin it as well.
  *
  * Layout: every array is Fortran column-major with the reference's
  * dimensions, for ONE species (the reference's leading S index removed):
