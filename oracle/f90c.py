@@ -1331,7 +1331,10 @@ class Translator:
         return cur, base, cur_sym
 
     def gen_call(self, name, args, ctx):
-        """Intrinsic function call (user functions are not in the subset)."""
+        """Function call: a translated user function, else an intrinsic."""
+        up = self.find_proc(name, ctx.proc)
+        if up is not None and up.is_func:
+            return self.gen_user_call(up, args, ctx)
         if name not in _INTRINSIC:
             raise Unsupported(f"function {name}")
         kw = {a.name: a.e for a in args if isinstance(a, Kw)}
@@ -1416,6 +1419,27 @@ class Translator:
                 raise Unsupported(f"{name} with mask/dim")
             return self.gen_reduce(name, pos[0], ctx)
         raise Unsupported(f"intrinsic {name}")
+
+    def gen_user_call(self, p, args, ctx):
+        """A translated function: arguments by reference (temporaries for
+        expressions) inside a statement expression."""
+        self.prepare_proc(p)
+        self.ensure_proc(p)
+        if len(args) != len(p.args):
+            raise Unsupported(f"argument count of {p.name}")
+        pre, cargs = [], []
+        for dn, a in zip(p.args, args):
+            ds = p.syms.get(dn)
+            if ds is None or isinstance(a, Kw) or ds.rank or ds.base not in ("i", "r", "l"):
+                raise Unsupported(f"argument {dn} of {p.name}")
+            c, t = self.gen(a, ctx.scalar())
+            v = ctx.newtmp("_fa")
+            pre.append(f"{self.ctype(ds)} {v} = {self.conv(c, t, ds.base)};")
+            cargs.append(f"&{v}")
+        r = p.syms.get(p.result)
+        if r is None:
+            raise Unsupported(f"result of {p.name}")
+        return f"({{ {' '.join(pre)} {self.proc_cname(p)}({', '.join(cargs)}); }})", r.base
 
     def _whole_array(self, e, ctx):
         if not isinstance(e, Ref):
@@ -2172,9 +2196,11 @@ class Translator:
 REF_FILES = ["src/nrtype.f90", "share/Library/src/ModNumConst.f90", "share/Library/src/ModTimeConvert.f90",
              "src/ModRamGrids.f90", "src/ModRamMain.f90", "src/ModRamParams.f90", "src/ModRamTiming.f90",
              "src/ModRamConst.f90", "src/ModRamSpecies.f90", "src/ModRamVariables.f90", "src/ModRamDrift.f90",
-             "src/ModRamLoss.f90", "src/ModRamRun.f90"]
+             "src/ModRamLoss.f90", "src/ModRamRun.f90", "src/ModRamInit.f90", "src/ModRamFunctions.f90",
+             "src/ModRamWPI.f90"]
 REF_PROCS = ["definespecies", "driftend", "driftpara", "driftr", "driftp", "drifte", "driftmu", "cepara",
-             "charexchange", "atmol", "ram_run", "sumrc", "anisch"]
+             "charexchange", "atmol", "ram_run", "sumrc", "anisch", "arrays", "acosd", "asind", "cosd", "sind",
+             "ram_sum_pressure", "wpadif", "flcscatter"]
 
 
 def translate_files(paths, procs, out_dir, extra=(), stem="ramref"):

@@ -201,6 +201,7 @@ class RefRam(RefLib):
             if q != sp.charge:
                 raise ValueError(f"species {sp.name}: charge {q} in the reference table, {sp.charge} in the grid")
         nr, nt, ne, npa = g.nr, g.nt, g.ne, g.npa
+        slen = self.get("modramgrids::slen")
         # shapes of ram_allocate (src/ModRamInit.f90:68-146)
         shapes = {
             "f2": (ns, nr, nt, ne, npa), "flux": (ns, nr, nt, ne, npa), "charge": (ns, nr, nt, ne, npa),
@@ -216,6 +217,11 @@ class RefRam(RefLib):
             "fgeos": (ns, nt, ne, npa), "dtdriftr": (ns,), "dtdriftp": (ns,), "dtdrifte": (ns,),
             "dtdriftmu": (ns,), "setrc": (ns,), "elorc": (ns,), "lsdr": (ns,), "lscha": (ns,), "lsatm": (ns,),
             "lscoe": (ns,), "lscsc": (ns,), "lswae": (ns,), "xne": (nr, nt),
+            # ARRAYS' outputs (src/ModRamInit.f90:97-101) and the coefficient
+            # arrays of WPADIF / FLCscatter and ram_sum_pressure
+            "amla": (slen,), "be": (nr + 1, slen), "zrpabn": (nr, npa, slen), "pa": (npa,), "pabn": (npa,),
+            "mlt": (nt,), "vbnd": (ns, ne), "facgr": (ns, ne), "pallsum": (nr, nt), "pparsum": (nr, nt),
+            "ataw": (nr, nt, ne, npa), "atac": (nr, nt, ne, npa), "flc_coef": (4, nr, nt, ne, npa),
         }
         self.a = {}
         for name, shp in shapes.items():
@@ -285,6 +291,51 @@ class RefRam(RefLib):
         self.set("modramvariables::kp", kp)
         self.set("modramtiming::uts", uts)
         self.call("ram_run")
+
+    # ------------------------------------------------------------ other routines
+    def arrays(self):
+        """The reference's ARRAYS (src/ModRamInit.f90:364-587) for every
+        species: the grid it builds, read back from the module arrays."""
+        for s in range(self.ns):
+            self.call("arrays", s + 1)
+        a = self.a
+        out = {k: a[k].copy() for k in ("lz", "rlz", "phi", "mlt", "ekev", "ebnd", "we", "de", "mu", "dmu", "wmu",
+                                         "pa", "pabn", "upa", "rmas", "grel", "grbnd", "v", "vbnd", "ffactor",
+                                         "epp", "ernh")}
+        for k in ("dl1", "mdr", "conf1", "conf2"):
+            out[k] = self.get("modramvariables::" + k)
+        out["dphi"] = self.get("modramgrids::dphi")
+        return out
+
+    def wpadif(self, s, f2, daa, dts):
+        """The reference's WPADIF (src/ModRamWPI.f90:643-714) on species s
+        (an electron species: ATAW = daa, ATAC = 0); f2 updated in place."""
+        self.a["ataw"][...] = daa
+        self.a["atac"][...] = 0.0
+        self.a["f2"][s] = f2
+        self.set("modramtiming::dts", dts)
+        self.call("wpadif", s + 1)
+        f2[...] = self.a["f2"][s]
+
+    def flcscatter(self, s, f2, coef, dts):
+        """The reference's FLCscatter (src/ModRamLoss.f90:513-575) on species
+        s with FLC_coef(s,...) = coef, after the first boundary cycle
+        (TimeRamElapsed >= Dt_bc); f2 updated in place."""
+        self.a["flc_coef"][s] = coef
+        self.a["f2"][s] = f2
+        self.set("modramtiming::dts", dts)
+        self.set("modramtiming::timeramelapsed", self.get("modramtiming::dt_bc"))
+        self.call("flcscatter", s + 1)
+        f2[...] = self.a["f2"][s]
+
+    def sum_pressure(self, ppert, ppart):
+        """The reference's ram_sum_pressure (src/ModRamFunctions.f90:272-297)
+        over every species: (PAllSum, PParSum)."""
+        for s in range(self.ns):
+            self.a["ppert"][s] = ppert[s]
+            self.a["ppart"][s] = ppart[s]
+        self.call("ram_sum_pressure")
+        return self.a["pallsum"].copy(), self.a["pparsum"].copy()
 
     def subroutine(self, name, s):
         """Call one species-indexed reference routine (DRIFTPARA, DRIFTR, ...,

@@ -105,3 +105,42 @@ def test_whole_arrays_against_translated_reference(have_ref, name, kps):
                 assert rel(gpu.flux(0, s), r["flux"][s]) <= TOL, (kp, s)
     finally:
         gpu.close()
+
+
+def test_implicit_diffusion_against_translated_reference(have_ref):
+    """The CUDA WPADIF / FLCscatter (one application) against the reference's
+    own WPADIF (electrons) and FLCscatter (ions)."""
+    wl = W.make_workload("tiny_pert")
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields)
+    d = {0: W.pa_diffusion(g, wl.fields, seed=30), 2: W.pa_diffusion(g, wl.fields, seed=32)}
+    gpu = _gpu(wl, 3.0)
+    try:
+        for s, a in d.items():
+            gpu.set_pa_diffusion(s, a)
+        gpu.apply_op(wl.dts, abi.OP_PADIF)
+        for s, a in d.items():
+            f = np.asfortranarray(wl.f2[s]).copy(order="F")
+            (ref.wpadif if s == 0 else ref.flcscatter)(s, f, a, wl.dts)
+            assert rel(gpu.download_f2(0, s), f) <= TOL, s
+    finally:
+        gpu.close()
+
+
+def test_sum_pressure_against_translated_reference(have_ref):
+    """The CUDA ram_sum_pressure hand-off after one ram_run, against the
+    reference's ram_sum_pressure on the reference's own moments."""
+    wl = W.make_workload("tiny_pert")
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields)
+    f_ref = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    gpu = _gpu(wl, 3.0)
+    try:
+        gpu.ram_run(wl.dts)
+        r = ref.ram_run(f_ref, wl.fgeos, wl.dts, 3.0)
+        pall, ppar = ref.sum_pressure([r["ppert"][s] for s in range(len(g.species))],
+                                      [r["ppart"][s] for s in range(len(g.species))])
+        gpall, gppar = gpu.sum_pressure(0)
+        assert rel(gpall, pall) <= TOL and rel(gppar, ppar) <= TOL
+    finally:
+        gpu.close()

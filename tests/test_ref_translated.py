@@ -7,7 +7,10 @@ oracle/refrun.py runs the reference's ram_run (src/ModRamRun.f90:16-225)
 and its single routines on the same inputs as the oracle.  Every output is
 compared for exact equality: F2, the moments, FLUX, VT, DtsNext, the
 DtDrift minima, the SUMRC loss bookkeeping, CHARGE/ATLOS and the CDrift
-coefficient arrays of each sweep.
+coefficient arrays of each sweep; beside the step, the grid construction
+(ARRAYS, src/ModRamInit.f90), the implicit pitch-angle diffusion (WPADIF,
+src/ModRamWPI.f90; FLCscatter, src/ModRamLoss.f90) and ram_sum_pressure
+(src/ModRamFunctions.f90).
 
 Needs the reference's tree (to translate) or a translated oracle/_ref/ramref.c.
 """
@@ -122,3 +125,52 @@ def test_stale_ghost_lines_occur():
     cd = ref.view("modramdrift::cdriftr")
     assert ((cd[-1] >= 0) & (cd[-2] < 0)).any() and (cd[-1] < 0).any()
     ref.call("driftend")
+
+
+@pytest.mark.parametrize("name", ["four_sp", "single_h"])
+def test_arrays_grid_bit_for_bit(name):
+    """The standard-grid construction of ramgpu/workload.py against the
+    reference's ARRAYS (src/ModRamInit.f90:364-587) for every species:
+    radial, MLT, energy and pitch-angle grids, the loss-cone index UPA,
+    GREL/GRBND/V/VBND, FFACTOR, EPP, ERNH, CONF1/2, DL1, MDR, DPHI."""
+    wl = W.make_workload(name)
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields, check=True)
+    out = ref.arrays()
+    for k, v in out.items():
+        mine = np.asarray(getattr(g, k), dtype=np.float64)
+        assert mine.shape == np.shape(v), k
+        assert np.array_equal(mine, np.asarray(v, dtype=np.float64)), k
+
+
+def test_implicit_diffusion_bit_for_bit():
+    """The oracle's implicit pitch-angle diffusion against the reference's
+    WPADIF (electrons, src/ModRamWPI.f90:643-714) and FLCscatter (ions,
+    src/ModRamLoss.f90:513-575)."""
+    wl = W.make_workload("tiny_pert")
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields, check=True)
+    o = pyoracle.Oracle(g, wl.fields)
+    for s, fn in ((0, "wpadif"), (1, "flcscatter"), (3, "flcscatter")):
+        daa = W.pa_diffusion(g, wl.fields, seed=30 + s)
+        f_ref = np.asfortranarray(wl.f2[s]).copy(order="F")
+        f_or = f_ref.copy(order="F")
+        getattr(ref, fn)(s, f_ref, daa, wl.dts)
+        o.padif(f_or, daa, wl.dts)
+        assert not np.array_equal(f_ref, wl.f2[s])
+        assert np.array_equal(f_ref, f_or), (s, fn)
+
+
+def test_sum_pressure_bit_for_bit():
+    """pyoracle.sum_pressure against the reference's ram_sum_pressure
+    (src/ModRamFunctions.f90:272-297)."""
+    wl = W.make_workload("tiny")
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields)
+    rng = np.random.Generator(np.random.PCG64(5))
+    pe = [np.asfortranarray(rng.random((g.nr, g.nt))) for _ in g.species]
+    pa = [np.asfortranarray(rng.random((g.nr, g.nt))) for _ in g.species]
+    pall, ppar = ref.sum_pressure(pe, pa)
+    idx = list(range(len(g.species)))
+    epall, eppar = pyoracle.sum_pressure(dict(enumerate(pe)), dict(enumerate(pa)), idx)
+    assert np.array_equal(pall, epall) and np.array_equal(ppar, eppar)
