@@ -2,7 +2,8 @@
 
 The short parity tests start every step from the initial state.  Here the
 GPU advances alone along a whole workload; at sampled steps its state is
-downloaded, the oracle takes one ram_run call from that state, and the
+downloaded, the oracle (or the reference's own ram_run, translated) takes
+one ram_run call from that state, and the
 GPU's own next call must agree to the per-step bar (1e-12 relative
 max-norm) for F2, the moments, FLUX and DtsNext.  Late in a run F2 has
 steepened, the limiter takes every branch and clip events occur, so this
@@ -49,7 +50,8 @@ def _gpu(wl, grid=None, flags=0):
 
 
 def _check_call(gpu, o, wl, kp, nthreads):
-    """One call from the GPU's current state on both sides; returns the
+    """One call from the GPU's current state on both sides (o: the C oracle,
+    or the reference's own ram_run when o is a refrun.RefRam); returns the
     worst relative error of F2 and the clip events of the GPU's call."""
     g = wl.grid
     ns = len(g.species)
@@ -57,7 +59,10 @@ def _check_call(gpu, o, wl, kp, nthreads):
     gpu.set_kp(0, kp)
     gpu.ram_run(wl.dts)
     clips = gpu.last_status()["clips"]
-    out = o.ram_run(ref, wl.fgeos, wl.dts, kp=kp, want_flux=True, nthreads=nthreads)
+    if isinstance(o, pyoracle.Oracle):
+        out = o.ram_run(ref, wl.fgeos, wl.dts, kp=kp, want_flux=True, nthreads=nthreads)
+    else:
+        out = o.ram_run(ref, wl.fgeos, wl.dts, kp)
     worst = 0.0
     for s in range(ns):
         e = rel(gpu.download_f2(0, s), ref[s])
@@ -72,11 +77,17 @@ def _check_call(gpu, o, wl, kp, nthreads):
     return worst, clips
 
 
-def _long_run(name, calls, samples):
+def _long_run(name, calls, samples, checker="oracle"):
     wl = W.make_workload(name)
     g = wl.grid
     outer, inner = _threads(len(g.species))
-    o = pyoracle.Oracle(g, wl.fields)
+    if checker == "reference":
+        import refrun
+        if refrun.build() is None:
+            pytest.skip("translated reference not present (oracle/_ref/ramref.c)")
+        o = refrun.RefRam(g, wl.fields, threads=outer)
+    else:
+        o = pyoracle.Oracle(g, wl.fields)
     gpu = _gpu(wl)
     gpu.set_graph(True)
     gpu.set_check(True)  # status word each call: counts the clip events
@@ -112,6 +123,14 @@ def test_four_species_kp_ramp_4320_steps():
     rep = _long_run("four_sp", 2160, [0, 45, 180, 360, 900, 1440, 1980, 2159])
     assert max(w for w, _ in rep.values()) <= TOL
     print("four_sp per-step rel err / clips by call:", rep)
+
+
+def test_four_species_ramp_against_reference():
+    """The same ramp checked against the reference's own ram_run (its
+    Fortran translated by oracle/f90c.py) at calls 0, 360, 1440 and 2159."""
+    rep = _long_run("four_sp", 2160, [0, 360, 1440, 2159], checker="reference")
+    assert max(w for w, _ in rep.values()) <= TOL
+    print("four_sp against the reference, per-step rel err / clips by call:", rep)
 
 
 def content_q(g, f2):
