@@ -120,6 +120,14 @@ class RefLib:
         else:
             raise TypeError(f"{name}: unsupported type")
 
+    def set_str(self, name, value):
+        """A character variable, blank-padded to its length."""
+        p, b, r, e = self._addr(name)
+        if b != 3 or r:
+            raise TypeError(f"{name} is not a character scalar")
+        raw = value.encode()[:e].ljust(e, b" ")
+        C.memmove(p, raw, e)
+
     def get(self, name):
         p, b, r, e = self._addr(name)
         if r:
@@ -248,14 +256,27 @@ class RefRam(RefLib):
         return self.call("refdrv_species_charge", i, 0)[1]
 
     # ------------------------------------------------------------ the step
-    def ram_run(self, f2s, fgeos, dts, kp, uts=0.0):
+    def ram_run(self, f2s, fgeos, dts, kp, uts=0.0, potential=None):
         """One reference ram_run over every species.  f2s: list of
         (NR,NT,NE,NPA) arrays, updated in place; fgeos: list of (NT,NE,NPA).
+        potential: None for the Volland-Stern VT from Kp, else (VTOL, VTN,
+        T, TOLV, DtEfi) for the interpolated branch
+        VT = VTOL + (VTN-VTOL)*(T-TOLV)/DtEfi (src/ModRamRun.f90:46-52).
         Returns the outputs in the layout of the C oracle's ram_run."""
         a = self.a
         for s in range(self.ns):
             a["f2"][s] = f2s[s]
             a["fgeos"][s] = fgeos[s]
+        if potential is None:
+            self.set_str("modramparams::electric", "VOLS")
+        else:
+            vtol, vtn, t, tolv, dtefi = potential
+            self.set_str("modramparams::electric", "WESC")
+            a["vtol"][...] = vtol
+            a["vtn"][...] = vtn
+            self.set("modramtiming::t", t)
+            self.set("modramvariables::tolv", tolv)
+            self.set("modramtiming::dtefi", dtefi)
         self.set("modramtiming::dts", dts)
         self.set("modramvariables::kp", kp)
         self.set("modramtiming::uts", uts)

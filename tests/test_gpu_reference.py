@@ -144,3 +144,33 @@ def test_sum_pressure_against_translated_reference(have_ref):
         assert rel(gpall, pall) <= TOL and rel(gppar, ppar) <= TOL
     finally:
         gpu.close()
+
+
+def test_interpolated_potential_against_translated_reference(have_ref):
+    """ramgpu_set_potential (the non-VOLS branch) against the reference's
+    ram_run with electric /= 'VOLS': VT interpolated between two potential
+    tables (src/ModRamRun.f90:46-52), two calls."""
+    wl = W.make_workload("tiny_pert8")
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields)
+    rng = np.random.Generator(np.random.PCG64(3))
+    base = W.vols_vt(g, 3.0)
+    vtol = np.asfortranarray(base * (1 + 0.1 * rng.standard_normal(base.shape)))
+    vtn = np.asfortranarray(base * (1.5 + 0.1 * rng.standard_normal(base.shape)))
+    f_ref = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    gpu = _gpu(wl, 3.0)
+    try:
+        for t in (350.0, 520.0):
+            # each call from the reference's state; VT as the reference forms it
+            for s in range(len(g.species)):
+                gpu.upload_f2(0, s, f_ref[s])
+            gpu.set_potential(0, np.asfortranarray(vtol + (vtn - vtol) * (t - 300.0) / 300.0))
+            gpu.ram_run(wl.dts)
+            r = ref.ram_run(f_ref, wl.fgeos, wl.dts, 3.0, potential=(vtol, vtn, t, 300.0, 300.0))
+            assert abs(gpu.cfl(0, 0)[4] - r["dts_next"]) <= TOL * r["dts_next"]
+            for s in range(len(g.species)):
+                assert rel(gpu.download_f2(0, s), f_ref[s]) <= TOL, (t, s)
+                pe, pa = gpu.moments(0, s)
+                assert rel(pe, r["ppert"][s]) <= TOL and rel(pa, r["ppart"][s]) <= TOL, (t, s)
+    finally:
+        gpu.close()

@@ -174,3 +174,26 @@ def test_sum_pressure_bit_for_bit():
     idx = list(range(len(g.species)))
     epall, eppar = pyoracle.sum_pressure(dict(enumerate(pe)), dict(enumerate(pa)), idx)
     assert np.array_equal(pall, epall) and np.array_equal(ppar, eppar)
+
+
+def test_interpolated_potential_branch():
+    """ram_run's non-VOLS branch, VT = VTOL + (VTN-VTOL)*(T-TOLV)/DtEfi
+    (src/ModRamRun.f90:46-52): the reference's VT equals the same
+    expression in NumPy, and the oracle given that VT equals the reference
+    bit for bit."""
+    wl = W.make_workload("tiny_pert8")
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields, check=True)
+    o = pyoracle.Oracle(g, wl.fields)
+    rng = np.random.Generator(np.random.PCG64(3))
+    vtol = np.asfortranarray(o.vt_vols(2.0) * (1 + 0.1 * rng.standard_normal((g.nr + 1, g.nt))))
+    vtn = np.asfortranarray(o.vt_vols(5.0) * (1 + 0.1 * rng.standard_normal((g.nr + 1, g.nt))))
+    f_ref = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    f_or = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+    r = ref.ram_run(f_ref, wl.fgeos, wl.dts, 3.0, potential=(vtol, vtn, 450.0, 300.0, 300.0))
+    assert np.array_equal(r["vt"], vtol + (vtn - vtol) * (450.0 - 300.0) / 300.0)
+    out = o.ram_run(f_or, wl.fgeos, wl.dts, vt=r["vt"], want_flux=True)
+    for s in range(len(g.species)):
+        assert np.array_equal(f_ref[s], f_or[s]), s
+        assert np.array_equal(r["ppert"][s], out["ppert"][s]), s
+    assert r["dts_next"] == out["dts_next"]
