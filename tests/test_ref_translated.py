@@ -197,3 +197,23 @@ def test_interpolated_potential_branch():
         assert np.array_equal(f_ref[s], f_or[s]), s
         assert np.array_equal(r["ppert"][s], out["ppert"][s]), s
     assert r["dts_next"] == out["dts_next"]
+
+
+def test_species_threads_bit_for_bit():
+    """The reference's !$OMP PARALLEL DO over species (thread-local
+    THREADPRIVATE arrays in the translation): four threads give the
+    single-thread results bit for bit."""
+    wl = W.make_workload("tiny_pert8")
+    g = wl.grid
+    outs = []
+    for threads in (1, 4):
+        ref = refrun.RefRam(g, wl.fields, threads=threads)
+        f = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
+        r = [ref.ram_run(f, wl.fgeos, wl.dts, kp) for kp in (2.0, 5.0)]
+        outs.append((f, r))
+    (f1, r1), (f4, r4) = outs
+    for s in range(len(g.species)):
+        assert np.array_equal(f1[s], f4[s]), s
+        assert np.array_equal(r1[1]["ppert"][s], r4[1]["ppert"][s]), s
+        assert r1[1]["losses"][s] == r4[1]["losses"][s], s
+    assert r1[1]["dts_next"] == r4[1]["dts_next"]
