@@ -540,7 +540,10 @@ def e2e_section(torch, np, abi, gpu, wl, steps):
     med = {}
 
     def run(fn):
-        fn(0)  # warm (first use creates the group streams, captures the graph)
+        # three warm-up calls (the first creates the group streams and
+        # captures the graph; the first few also touch the host buffers)
+        for w in range(3):
+            fn(w)
         torch.cuda.synchronize()
         ts = []
         t0 = time.perf_counter()
