@@ -423,6 +423,34 @@ def initial_f2(g: Grid, f: Fields, s: int, seed: int, kt=5.0, kappa=3.0, amp=1.0
     return np.ascontiguousarray(f2)
 
 
+def edge_state(f2s, seed: int = 5):
+    """Copies of the species' F2 arrays edited to reach every corner of the
+    sweeps: blocks of exact zeros (faces with X = 0, the |X| <= 1e-27
+    upwind branch, R = 0), cells of 1e-30 (differences below 1e-27 next to
+    zeros), isolated spikes 1e3 above their neighbours (limiter ratios
+    R < 0 and R > beta, and at high Kp updates that come out negative and
+    are clipped to 1e-15), and a whole line of one value (X = 0 along it)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for f in f2s:
+        a = np.array(f, dtype=np.float64, copy=True)
+        nr, nt, ne, npa = a.shape
+        for _ in range(6):  # zero blocks
+            i0, j0 = int(rng.integers(nr - 2)), int(rng.integers(nt - 3))
+            k0, l0 = int(rng.integers(1, ne - 4)), int(rng.integers(1, npa - 6))
+            a[i0:i0 + 2, j0:j0 + 3, k0:k0 + 4, l0:l0 + 6] = 0.0
+        for _ in range(64):  # tiny cells
+            a[tuple(int(rng.integers(d)) for d in a.shape)] = 1e-30
+        for _ in range(64):  # spikes
+            c = tuple(int(rng.integers(d)) for d in a.shape)
+            a[c] = a[c] * 1e3 + 1e-10
+        i, j, k = int(rng.integers(1, nr)), int(rng.integers(nt)), int(rng.integers(1, ne))
+        a[i, j, k, :] = a[i, j, k, 1]  # one flat pitch-angle line
+        a[:, nt - 1] = a[:, 0]
+        out.append(np.asfortranarray(a))
+    return out
+
+
 def boundary_fgeos(g: Grid, s: int, kt=5.0, kappa=3.0, amp=1.0e5, density_scale=1.0) -> np.ndarray:
     """FGEOS(J,K,L) = flux(K)*FFACTOR(S,NR,K,L) for L=2..int(UPA(NR)-1), as GEOSB.
     C order (J,K,L)."""

@@ -174,3 +174,34 @@ def test_interpolated_potential_against_translated_reference(have_ref):
                 assert rel(pe, r["ppert"][s]) <= TOL and rel(pa, r["ppart"][s]) <= TOL, (t, s)
     finally:
         gpu.close()
+
+
+def test_edge_states_against_translated_reference(have_ref):
+    """States built to reach every corner (workload.edge_state: zero blocks,
+    1e-30 cells, spikes, a flat line), Kp 1, then Kp 9 with DTs = 200 s
+    (Courant numbers above 1, clipped updates), then Kp 5; each call from
+    the reference's state, within 1e-12."""
+    wl = W.make_workload("tiny_pert8")
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields)
+    f_ref = W.edge_state(wl.f2)
+    gpu = _gpu(wl, 1.0)
+    try:
+        gpu.set_check(True)
+        clips = 0
+        for kp, dts in ((1.0, 5.0), (9.0, 200.0), (5.0, 5.0)):
+            for s in range(len(g.species)):
+                gpu.upload_f2(0, s, f_ref[s])
+            gpu.set_kp(0, kp)
+            gpu.ram_run(dts)
+            clips += gpu.last_status()["clips"]
+            r = ref.ram_run(f_ref, wl.fgeos, dts, kp)
+            assert abs(gpu.cfl(0, 0)[4] - r["dts_next"]) <= TOL * r["dts_next"]
+            for s in range(len(g.species)):
+                assert rel(gpu.download_f2(0, s), f_ref[s]) <= TOL, (kp, s)
+                pe, pa = gpu.moments(0, s)
+                assert rel(pe, r["ppert"][s]) <= TOL and rel(pa, r["ppart"][s]) <= TOL, (kp, s)
+                assert rel(gpu.flux(0, s), r["flux"][s]) <= TOL, (kp, s)
+        assert clips > 0
+    finally:
+        gpu.close()

@@ -217,3 +217,42 @@ def test_species_threads_bit_for_bit():
         assert np.array_equal(r1[1]["ppert"][s], r4[1]["ppert"][s]), s
         assert r1[1]["losses"][s] == r4[1]["losses"][s], s
     assert r1[1]["dts_next"] == r4[1]["dts_next"]
+
+
+EDGE_CALLS = ((1.0, 5.0), (9.0, 200.0), (5.0, 5.0))  # (Kp, DTs)
+
+
+def test_edge_states_bit_for_bit():
+    """States built to reach every corner (workload.edge_state: zero blocks,
+    1e-30 cells, spikes, a flat line) along Kp 1, then Kp 9 with DTs = 200 s
+    (Courant numbers above 1: the CFL limit is below DTs and updates come
+    out negative and are clipped), then Kp 5: the oracle equals the
+    reference bit for bit, and clip events did occur."""
+    wl = W.make_workload("tiny_pert8")
+    g = wl.grid
+    ref = refrun.RefRam(g, wl.fields, check=True)
+    o = pyoracle.Oracle(g, wl.fields)
+    f_ref = W.edge_state(wl.f2)
+    f_or = [a.copy(order="F") for a in f_ref]
+    # the corners are reached: every limiter case (0 upwind, 1 beta*R, 2 one,
+    # 3 R, 4 beta) and clipped updates (bit 3) in the forward sweeps of the
+    # Kp 9 / 200 s call, recorded by the oracle on a copy of the state
+    rec_cases, clips = set(), 0
+    vt = o.vt_vols(9.0)
+    for s in range(len(g.species)):
+        f = f_ref[s].copy(order="F")
+        for which in ("R", "P", "E", "MU"):
+            _, _, _, rec, _ = o.sweep_rec(which, s, f, vt, 200.0, fgeos=wl.fgeos[s])
+            rec_cases |= set(np.unique(rec & 7).tolist())
+            clips += int(np.count_nonzero(rec & 8))
+    assert rec_cases >= {0, 1, 2, 3, 4} and clips > 0, (rec_cases, clips)
+    for kp, dts in EDGE_CALLS:
+        r = ref.ram_run(f_ref, wl.fgeos, dts, kp)
+        out = o.ram_run(f_or, wl.fgeos, dts, kp=kp, want_flux=True)
+        for s in range(len(g.species)):
+            assert np.array_equal(f_ref[s], f_or[s]), (kp, s)
+            assert np.array_equal(r["ppert"][s], out["ppert"][s]), (kp, s)
+            assert np.array_equal(r["flux"][s], out["flux"][s]), (kp, s)
+        assert r["dts_next"] == out["dts_next"]
+        if dts > 100.0:
+            assert min(min(v) for v in r["dtdrift"].values()) < dts
