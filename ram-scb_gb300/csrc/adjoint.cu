@@ -83,7 +83,9 @@ constexpr unsigned kAdjIntMask = 0xBu;
 // on the integer pipe.  Measured on GB300: the DRIFTE transposes that form
 // C gain, the one that loads C (fewer FP64 operations left) loses and keeps
 // the FP64 product (the bits are the same either way); R (shared-memory
-// tiles, integer weights) loses over the whole adjoint window.
+// tiles, integer weights) loses over the whole adjoint window; P (bit 2) is
+// neutral and MU (bit 8) loses (backward 0.720-0.731 s with E alone, 0.725
+// with E and P, 0.736 with E and MU, 0.755 with all three, on one box).
 constexpr unsigned kAdjMulIntMask = 0x4u;
 __device__ __forceinline__ double adj_mul(unsigned bit, double a, double b) {
   return (kAdjMulIntMask & bit) ? mul_rn_int(a, b) : a * b;
@@ -369,7 +371,7 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
       const double C = PC(n - 1);
       const bool neg = is_neg(C);
       const int cs = (rl[(long long)(n - 2) * st] >> rsh) & 7;
-      const double FBb = C * (leN - leNm);
+      const double FBb = adj_mul(2u, C, leN - leNm);
       const double V = face_ak<false>(C, neg, cs, -0.5, bmh, hb) * FBb;
       if (neg) tN += FBb; else tNm1 += FBb;
       if (cs == 2 || cs == 4) { tN += V; tNm1 -= V; }
@@ -380,7 +382,7 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
       const double C = PC(n);
       const bool neg = is_neg(C);
       const int cs = (rl[(long long)(n - 1) * st] >> rsh) & 7;
-      const double FBb = C * (le2 - leN);  // Pb(NT) = -le(NT) + Pb(1), Pb(1) = le(2)
+      const double FBb = adj_mul(2u, C, le2 - leN);  // Pb(NT) = -le(NT) + Pb(1), Pb(1) = le(2)
       const double V = face_ak<false>(C, neg, cs, -0.5, bmh, hb) * FBb;
       if (neg) w2 += FBb; else tN += FBb;
       if (cs == 2 || cs == 4) { w2 += V; tN -= V; }
@@ -395,9 +397,9 @@ __global__ void __launch_bounds__(128) k_adj_p(Dev d, const unsigned char* __res
       const bool neg = is_neg(C);
       const int cs = (rl[(long long)(J - 1) * st] >> rsh) & 7;
       if (kAdjIntMask & 2u)
-        face_acc_a(C * (le1 - le0), neg, cs, corr_a_fix(dbits(C) & kAbsMask, neg), beta, cm1, c0, c1, c2);
+        face_acc_a(adj_mul(2u, C, le1 - le0), neg, cs, corr_a_fix(dbits(C) & kAbsMask, neg), beta, cm1, c0, c1, c2);
       else
-        face_acc(C * (le1 - le0), neg, cs, face_ak<false>(C, neg, cs, -0.5, bmh, hb), cm1, c0, c1, c2);
+        face_acc(adj_mul(2u, C, le1 - le0), neg, cs, face_ak<false>(C, neg, cs, -0.5, bmh, hb), cm1, c0, c1, c2);
       lam[(long long)(J - 2) * st] = cm1;
       cm1 = c0; c0 = c1; c1 = c2; c2 = add;
       le0 = le1; le1 = lnext; lnext = lec;
@@ -582,10 +584,11 @@ __global__ void __launch_bounds__(128) k_adj_mu(Dev d, const unsigned char* __re
       const bool neg = is_neg(C);
       const int cs = (rl[(long long)(L - 1) * st] >> rsh) & 7;
       if (kAdjIntMask & 8u)
-        face_acc_a(C * (wl1 - wl0), neg, cs, corr_a_fix(courant_u(C, d.idmu[L - 1]), neg), beta, cm1, c0, c1, c2);
+        face_acc_a(adj_mul(8u, C, wl1 - wl0), neg, cs, corr_a_fix(courant_u(C, d.idmu[L - 1]), neg), beta, cm1, c0, c1,
+                   c2);
       else
-        face_acc(C * (wl1 - wl0), neg, cs, face_ak<true>(C, neg, cs, d.mhdmu[L - 1], d.bmhdmu[L - 1], hb), cm1,
-                 c0, c1, c2);
+        face_acc(adj_mul(8u, C, wl1 - wl0), neg, cs, face_ak<true>(C, neg, cs, d.mhdmu[L - 1], d.bmhdmu[L - 1], hb),
+                 cm1, c0, c1, c2);
     };
     auto shift = [&](double lec, double wl) {
       cm1 = c0; c0 = c1; c1 = c2; c2 = lec;
