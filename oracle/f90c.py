@@ -130,7 +130,6 @@ def read_statements(path: str):
 
 
 # ---------------------------------------------------------------- lexing
-_DOTOPS = ("and", "or", "not", "eq", "ne", "lt", "le", "gt", "ge", "eqv", "neqv", "true", "false")
 _TOK = re.compile(r"""
   (?P<ws>\s+)
  |(?P<str>'(?:[^']|'')*'|"(?:[^"]|"")*")
@@ -862,13 +861,8 @@ class Translator:
         self.mods = modules
         self.want = [p.lower() for p in procs]
         self.types = {}
-        self.out_globals = []
         self.used_globals = {}    # cname -> Sym
-        self.proc_code = []
-        self.protos = []
         self.translated = {}      # proc name -> cname
-        self.entry = []           # (fortran name, cname, nargs)
-        self.const_cache = {}
 
     # ------------------------------------------------------------ scoping
     def setup(self):
@@ -1134,7 +1128,7 @@ class Translator:
             return f"(*a_{s.name})"
         return f"l_{s.name}"
 
-    def gen(self, e, ctx, want=None):
+    def gen(self, e, ctx):
         """-> (code, base) for a scalar (or elemental) expression."""
         if isinstance(e, Num):
             t = e.text.split("_")[0]
@@ -1238,9 +1232,6 @@ class Translator:
         return f"pow({self.conv(a, ta, 'r')}, {b})", "r"
 
     # array element / section handling ------------------------------------
-    def _arr_base(self, s, ctx):
-        return self.sym_code(s, ctx)
-
     def elem_index(self, arr, s, args, ctx, where):
         """Offset expression of an element (args scalar or sections mapped
         onto the elemental loops)."""
