@@ -9,8 +9,8 @@ Two sources, neither a restatement of this project:
   moments, FLUX and DtsNext;
 * the translated reference itself, built on this machine from
   oracle/_ref/ramref.c: whole-array comparisons per call (each call started
-  from the reference's state) on the test grids and on the standard
-  20x25x35x72 four-species grid.
+  from the reference's state) on the test grids, on the standard
+  20x25x35x72 four-species grid and on the refined 40x49x70x144 grid.
 
 Bar: 1e-12 relative max-norm per call (FP64), as the rest of the parity suite.
 """
@@ -81,7 +81,7 @@ def have_ref():
     return True
 
 
-@pytest.mark.parametrize("name,kps", [("tiny_pert8", (1.0, 3.5, 6.0)), ("four_sp", (3.0,))])
+@pytest.mark.parametrize("name,kps", [("tiny_pert8", (1.0, 3.5, 6.0)), ("four_sp", (3.0,)), ("refined", (4.0,))])
 def test_whole_arrays_against_translated_reference(have_ref, name, kps):
     """Each call from the reference's state: F2, PPERT/PPART, FLUX of every
     species and DtsNext within 1e-12."""
