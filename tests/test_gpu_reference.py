@@ -87,7 +87,7 @@ def test_whole_arrays_against_translated_reference(have_ref, name, kps):
     species and DtsNext within 1e-12."""
     wl = W.make_workload(name)
     g = wl.grid
-    ref = refrun.RefRam(g, wl.fields)
+    ref = refrun.RefRam(g, wl.fields, threads=len(g.species))  # its species loop, bitwise as one thread
     f_ref = [np.asfortranarray(a).copy(order="F") for a in wl.f2]
     gpu = _gpu(wl, kps[0])
     try:
